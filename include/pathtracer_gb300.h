@@ -1,0 +1,341 @@
+/*
+ * pathtracer_gb300.h -- C-ABI of the GB300 wavefront NEE(+MIS) path integrator.
+ *
+ * This is the drop-in boundary for the render loop of 747745124/PathTracer.
+ * The reference exposes C++ virtual interfaces and one free function per
+ * integrator; every entry point below names the reference interface it
+ * replaces (file:line within the reference project).  All functions are
+ * `extern "C"`, take plain pointers and sizes, never throw, and return an
+ * int status: PT_OK (0) or a negative PT_ERR_* code.  The message of the last
+ * failure on a context is read with pt_last_error().
+ *
+ * Threading: one pt_context per host thread, or external locking.  Device
+ * work of a context runs on that context's own CUDA stream.
+ */
+#ifndef PATHTRACER_GB300_H
+#define PATHTRACER_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- status */
+enum {
+  PT_OK = 0,
+  PT_ERR_INVALID = -1,     /* bad argument / malformed scene or job        */
+  PT_ERR_CUDA = -2,        /* a CUDA call failed                           */
+  PT_ERR_NOMEM = -3,       /* device or host allocation failed             */
+  PT_ERR_NOT_FOUND = -4,   /* unknown scene / request id                   */
+  PT_ERR_DEVICE = -5,      /* device-side error flag (iteration cap hit)   */
+  PT_ERR_BUSY = -6,        /* admission refused: not enough free HBM       */
+  PT_ERR_CANCELLED = -7,   /* request was cancelled                        */
+  PT_ERR_TOO_LARGE = -8    /* size beyond a fixed, documented maximum      */
+};
+
+/* ------------------------------------------------------------- materials
+ * Mirrors the reference's Material family (include/material/material.hpp:15-77)
+ * and its subclasses.  p[] holds the constructor arguments in order:
+ *   LAMBERTIAN        Lambertian(albedo)                      material.hpp:79
+ *                       p[0..2] albedo
+ *   CONDUCTOR         Conductor(eta, k, alpha_x, alpha_y)     conductor.hpp:4
+ *                       p[0..2] eta, p[3..5] k, p[6] alpha_x, p[7] alpha_y
+ *   MF_DIELECTRIC     MFDielectric(eta, alpha_x, alpha_y)     dielectric.hpp:15
+ *                       p[0] eta, p[1] alpha_x, p[2] alpha_y
+ *   THIN_DIELECTRIC   ThinDielectric(eta, use_split_ray)      thinDielectric.hpp:10
+ *                       p[0] eta, flags bit0 = use_split_ray
+ *   PHONG             Phong(diffuse, specular, ambient, n)    material.hpp:303
+ *                       p[0..2] diffuse, p[3..5] specular, p[6..8] ambient,
+ *                       p[9] shininess
+ *   DISNEY            DisneyPrincipledBSDF(13 params)         disneyPrincipledBSDF.hpp:34
+ *                       p[0..2] baseColor, p[3] specular_transmission,
+ *                       p[4] metallic, p[5] subsurface, p[6] specular,
+ *                       p[7] roughness, p[8] specular_tint, p[9] anisotropic,
+ *                       p[10] sheen, p[11] sheen_tint, p[12] clearcoat,
+ *                       p[13] clearcoat_gloss, p[14] eta
+ *   HAIR              HairMarschner(sigma_a, h, eta, beta_m, beta_n, alpha)
+ *                                                             hairMarsch.hpp:7
+ *                       p[0..2] sigma_a, p[3] h, p[4] eta, p[5] beta_m,
+ *                       p[6] beta_n, p[7] alpha (radians).
+ *                       flags bit1: sigma_a is derived from p[8] eumelanin and
+ *                       p[9] pheomelanin concentrations (extension).
+ *   DIFFUSE_EMITTER   DiffuseEmitter(color, intensity)        material.hpp:467
+ *                       p[0..2] color, p[3] intensity
+ */
+enum {
+  PT_MAT_LAMBERTIAN = 0,
+  PT_MAT_CONDUCTOR = 1,
+  PT_MAT_MF_DIELECTRIC = 2,
+  PT_MAT_THIN_DIELECTRIC = 3,
+  PT_MAT_PHONG = 4,
+  PT_MAT_DISNEY = 5,
+  PT_MAT_HAIR = 6,
+  PT_MAT_DIFFUSE_EMITTER = 7,
+  PT_MAT_COUNT = 8
+};
+#define PT_MAT_FLAG_SPLIT_RAY 1
+#define PT_MAT_FLAG_MELANIN 2
+
+typedef struct pt_material_desc {
+  int32_t type;
+  int32_t flags;
+  float p[30];
+} pt_material_desc; /* 128 bytes */
+
+/* ------------------------------------------------------------- geometry
+ * A triangle mesh in world space: TriangleMesh(MeshData, material)
+ * (include/primitives/triangleMesh.hpp:8, include/mesh_io/meshData.hpp:6).
+ * normals / uvs and their index arrays are optional (NULL).  Decorators of
+ * the reference (Translate/Rotate/Scale/FlipFace, utils/objectTransform.hpp)
+ * are applied by the host C++ layer before upload. */
+typedef struct pt_mesh_desc {
+  const float *positions;       /* 3 * n_positions */
+  int32_t n_positions;
+  const float *normals;         /* 3 * n_normals, optional */
+  int32_t n_normals;
+  const float *uvs;             /* 2 * n_uvs, optional */
+  int32_t n_uvs;
+  const int32_t *indices;       /* 3 * n_triangles */
+  const int32_t *normal_indices;/* 3 * n_triangles, optional */
+  const int32_t *uv_indices;    /* 3 * n_triangles, optional */
+  int32_t n_triangles;
+  int32_t material;
+} pt_mesh_desc;
+
+/* AARectangle<axis>(k, d0_min, d0_max, d1_min, d1_max, material)
+ * (include/base/primitive.hpp:205-269).  axis 0 = X (YZRectangle),
+ * 1 = Y (XZRectangle), 2 = Z (XYRectangle). flip_face mirrors FlipFace. */
+typedef struct pt_quad_desc {
+  int32_t axis;
+  float k, d0_min, d0_max, d1_min, d1_max;
+  int32_t material;
+  int32_t flip_face;
+} pt_quad_desc;
+
+/* Sphere(center, radius, material) (include/base/primitive.hpp:81-203). */
+typedef struct pt_sphere_desc {
+  float center[3];
+  float radius;
+  int32_t material;
+  int32_t flip_face;
+} pt_sphere_desc;
+
+/* Entry of the scene's ObjectList in insertion order (objectList.hpp:176).
+ * The order fixes the top-level BVH build (bvh.hpp:46-102) and light
+ * discovery order (lightDiscovery.hpp:5-81). */
+enum { PT_OBJ_MESH = 0, PT_OBJ_QUAD = 1, PT_OBJ_SPHERE = 2 };
+typedef struct pt_object_desc {
+  int32_t kind;
+  int32_t index;
+} pt_object_desc;
+
+/* EnvironmentLight + HDRITexture (include/light/envLight.hpp:4,
+ * include/texture/texture.hpp:97).  texels are RGB float, width*height*3,
+ * stored as the reference's texels[x][y] with y = 0 the BOTTOM row:
+ * texels[(y * width + x) * 3 + c]. */
+typedef struct pt_env_desc {
+  const float *texels;
+  int32_t width;
+  int32_t height;
+  float intensity;
+} pt_env_desc;
+
+/* HomogeneousMedium(sigma_a, sigma_s, scale, Le, Le_scale, g)
+ * (include/medium/homogeneous.hpp:31-68), filling the whole scene. */
+typedef struct pt_medium_desc {
+  float sigma_a[3];
+  float sigma_s[3];
+  float g;
+} pt_medium_desc;
+
+typedef struct pt_scene_desc {
+  const pt_material_desc *materials;
+  int32_t n_materials;
+  const pt_mesh_desc *meshes;
+  int32_t n_meshes;
+  const pt_quad_desc *quads;
+  int32_t n_quads;
+  const pt_sphere_desc *spheres;
+  int32_t n_spheres;
+  const pt_object_desc *objects;
+  int32_t n_objects;
+  const pt_env_desc *env;       /* NULL: no environment light */
+  const pt_medium_desc *medium; /* NULL: vacuum */
+  float bg_color[3];            /* SceneInfo::bg_color, renderManager.hpp:41 */
+  int32_t bvh_mode;             /* PT_BVH_REFERENCE (default) */
+} pt_scene_desc;
+
+enum { PT_BVH_REFERENCE = 0 };
+
+/* ------------------------------------------------------------------ jobs
+ * PerspectiveCamera(fov, aspect, focalDist, aperture, up, front, position)
+ * (src/base/camera.cpp:7-35).  Lens radius = focalDist / aperture * 0.5. */
+typedef struct pt_camera_desc {
+  float fov;        /* radians */
+  float aspect;
+  float focal_dist;
+  float aperture;
+  float up[3];
+  float front[3];
+  float position[3];
+  float shutter;    /* motion-blur shutter length (extension); 0 = off */
+} pt_camera_desc;
+
+/* Estimator.  REF_NEE restates include/integrator/maxdepth_nee.hpp:9-256
+ * (light-sampled direct light only, BSDF-sampled emitter hits dropped, the
+ * environment counted by both strategies).  NEE_MIS combines light and
+ * BSDF sampling with the power heuristic of maxdepth_mis.hpp:10-15. */
+enum { PT_EST_REF_NEE = 0, PT_EST_NEE_MIS = 1 };
+
+/* Sampler for the per-bounce dimensions (sampler.hpp:5 RandomStrategy),
+ * plus a jittered stratified sampler. */
+enum {
+  PT_SAMPLER_HALTON_NONE = 0,
+  PT_SAMPLER_HALTON_PERMUTE = 1,
+  PT_SAMPLER_HALTON_OWEN = 2,
+  PT_SAMPLER_STRATIFIED = 3
+};
+
+/* Environment light sampling: the reference's uniform sphere
+ * (texture.hpp:120-131) or a luminance alias table (extension). */
+enum { PT_ENV_UNIFORM = 0, PT_ENV_ALIAS = 1 };
+
+typedef struct pt_job_desc {
+  int32_t scene;
+  int32_t width, height;
+  int32_t spp_x, spp_y;      /* stratified pixel grid, framebuffer.cpp:131 */
+  int32_t spp_begin;         /* render samples [spp_begin, spp_end) of the grid */
+  int32_t spp_end;           /* 0 = spp_x * spp_y */
+  int32_t max_depth;         /* MAX_RAY_DEPTH, config.hpp:7 */
+  int32_t rr_start;          /* Russian roulette from this depth; -1 = off */
+  int32_t estimator;         /* PT_EST_* */
+  int32_t sampler;           /* PT_SAMPLER_* */
+  int32_t env_sampling;      /* PT_ENV_* */
+  int32_t light_samples_x;   /* LIGHT_SAMPLE_X, config.hpp:5 (default 2) */
+  int32_t light_samples_y;   /* LIGHT_SAMPLE_Y, config.hpp:6 (default 2) */
+  uint32_t seed;             /* seeds every non-Halton draw */
+  uint32_t sampler_seed;     /* HaltonSampler seed (PermuteDigits only) */
+  pt_camera_desc camera;
+  float gamma;               /* GAMMA, config.hpp:10 */
+  int32_t reserved[4];
+} pt_job_desc;
+
+typedef struct pt_stats {
+  uint64_t paths;
+  uint64_t segments;     /* path vertices shaded */
+  uint64_t rays;         /* closest-hit rays traced */
+  uint64_t shadow_rays;  /* any-hit rays traced */
+  double ms;             /* device time of the render */
+  uint64_t algorithmic_bytes; /* 192*segments + 88*shadow_rays + 24*paths */
+} pt_stats;
+
+/* -------------------------------------------------------------- context */
+int pt_create(void **ctx, int device);
+int pt_destroy(void *ctx);
+/* Copies the last error message of ctx (or of the library if ctx is NULL)
+ * into buf (NUL-terminated, at most n bytes). */
+int pt_last_error(void *ctx, char *buf, size_t n);
+int pt_version(void);
+
+/* Flattens and uploads a scene (replaces the scene set-up part of
+ * SceneInfo::render, include/render/renderManager.hpp:80-95: BVH build,
+ * light discovery).  Host arrays are copied; the caller keeps ownership. */
+int pt_scene_upload(void *ctx, const pt_scene_desc *desc, int32_t *scene_id);
+int pt_scene_release(void *ctx, int32_t scene_id);
+/* Counts of the flattened scene: [0] triangles, [1] quads, [2] spheres,
+ * [3] BVH4 nodes, [4] lights, [5] device bytes. */
+int pt_scene_info(void *ctx, int32_t scene_id, int64_t *out6);
+
+/* Renders one job synchronously (replaces the pixel loop of
+ * SceneInfo::render, renderManager.hpp:97-155, calling getRayColor,
+ * maxdepth_nee.hpp:9).  film_rgb is a HOST buffer of width*height*3 floats
+ * indexed [j][i][c] with j = 0 the bottom row (FrameBuffer::_pixel_color,
+ * framebuffer.cpp:23); it receives the mean over samples
+ * [spp_begin, spp_end).  stats may be NULL. */
+int pt_render(void *ctx, const pt_job_desc *job, float *film_rgb,
+              pt_stats *stats);
+/* Same, into a DEVICE buffer of width*height*3 floats that receives the
+ * SUM (not the mean) of the samples rendered, accumulated onto its contents.
+ * Runs on the context's stream, returns after the work is enqueued unless
+ * sync != 0. */
+int pt_render_device(void *ctx, const pt_job_desc *job, float *d_film_sum,
+                     int sync, pt_stats *stats);
+
+/* FrameBuffer::writeToFile pixel path (framebuffer.cpp:27-58): NaN -> 0,
+ * pow(c, 1/gamma), clamp [0,1], *255 truncated to u8, rows flipped so that
+ * row 0 of rgb8 is the top of the image.  Host buffers. */
+int pt_tonemap(void *ctx, const float *film_rgb, int32_t width, int32_t height,
+               float gamma, uint8_t *rgb8);
+
+/* ------------------------------------------------- batch test entry points
+ * Sampler sequences (HaltonSampler::SampleDimension, sampler.hpp:54-73):
+ * out[i * dims + d] = sample of dimension d at sample index first_index + i. */
+int pt_sampler_eval(void *ctx, int32_t strategy, uint32_t seed,
+                    uint32_t first_index, int32_t n, int32_t dims, float *out);
+
+/* Closest hit (BVHNode::intersect, bvh.hpp:27-41 and the primitives below
+ * it).  rays: n * 6 floats (origin, direction), tmin/tmax per call.
+ * Outputs: t (FLT_MAX on miss), prim (-1 on miss; triangles are numbered
+ * mesh by mesh in upload order, then quads, then spheres), uv barycentrics. */
+int pt_trace_closest(void *ctx, int32_t scene_id, const float *rays, int32_t n,
+                     float tmin, float tmax, float *t, int32_t *prim,
+                     float *uv);
+/* Occlusion test with the shadow-ray intervals of maxdepth_nee.hpp:117-166:
+ * occluded[i] = 1 if anything is hit in [tmin, tmax_i]. */
+int pt_trace_any(void *ctx, int32_t scene_id, const float *rays,
+                 const float *tmax, int32_t n, float tmin, uint8_t *occluded);
+
+/* BSDF evaluation (Material::f and Material::scatter_pdf(wo, wi, rec),
+ * material.hpp:32-61).  Arrays of n items, 3 floats per vector. `front` is
+ * HitRecord::is_inside (materialBase.hpp:47-52: true when the ray hit the
+ * front face).  Outputs f (3n) and pdf (n). */
+int pt_bsdf_eval(void *ctx, const pt_material_desc *mat, int32_t n,
+                 const float *wo, const float *wi, const float *normal,
+                 const uint8_t *front, float *f, float *pdf);
+/* BSDF sampling (Material::scatter, material.hpp:18-27) with the sampler
+ * values uc, u (2n).  Outputs: ok (scatter's return), wi (3n),
+ * attenuation (3n), pdf_val (n), sampled_type (BxDFFlags bits). */
+int pt_bsdf_sample(void *ctx, const pt_material_desc *mat, int32_t n,
+                   const float *wo, const float *normal, const uint8_t *front,
+                   const float *uc, const float *u, uint8_t *ok, float *wi,
+                   float *attenuation, float *pdf_val, uint32_t *sampled_type);
+
+/* ----------------------------------------------------- batched rendering
+ * Many jobs (different scenes, sizes, spp) in one persistent launch per
+ * bounce, replayed from a captured CUDA graph.  films[k] are host buffers
+ * receiving each job's mean image.  Extension: no counterpart in the
+ * reference, which renders one scene per process. */
+int pt_render_batch(void *ctx, const pt_job_desc *jobs, int32_t n_jobs,
+                    float **films, pt_stats *stats);
+
+/* ------------------------------------------------------------- serving
+ * A request loop over resident scenes with continuous batching.  Requests
+ * are admitted while free HBM allows; each owns a device film that is
+ * refined until its target RMSE estimate or spp cap.  Extension. */
+typedef struct pt_request_desc {
+  pt_job_desc job;
+  float target_rmse;   /* stop when the estimated RMSE falls below this */
+  int32_t spp_cap;     /* ... or when this many samples were taken */
+  int32_t spp_per_pass;/* samples added per scheduling pass */
+} pt_request_desc;
+
+int pt_server_create(void *ctx, int64_t hbm_budget_bytes, int32_t max_slots,
+                     void **server);
+int pt_server_destroy(void *server);
+int pt_submit(void *server, const pt_request_desc *req, int64_t *request_id);
+/* Runs one scheduling pass (admission + one batched step over all active
+ * requests).  Returns the number of requests still active in *active. */
+int pt_server_step(void *server, int32_t *active);
+/* state: 0 queued, 1 running, 2 done, 3 cancelled, 4 failed.  When done,
+ * film (host, may be NULL) receives the mean image; spp_done and the
+ * latency (submit to completion, ms) are reported. */
+int pt_poll(void *server, int64_t request_id, int32_t *state, float *film,
+            int32_t *spp_done, double *latency_ms);
+int pt_cancel(void *server, int64_t request_id);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PATHTRACER_GB300_H */

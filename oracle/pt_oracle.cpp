@@ -1,0 +1,1465 @@
+// pt_oracle.cpp -- CPU restatement of the reference's path integrator.
+//
+// ORACLE: test infrastructure only.  Only tests/, __graft_entry__.smoke()
+// and bench.py's CPU-baseline leg load this library, as the checker of the
+// CUDA path; nothing in the product links it.
+//
+// What it restates (reference file:line at each piece):
+//   * samplers: HaltonSampler None / PermuteDigits / Owen (pt_oracle_math.hpp)
+//   * scene: BVHNode (bvh.hpp:27-102), MeshBVHNode (meshBVH.cpp:6-143),
+//     TriangleMesh (triangleMesh.cpp:28-54), AARectangle (primitive.cpp),
+//     Sphere (primitive.hpp:124-170), FlipFace (objectTransform.hpp:5-38)
+//   * materials: pt_oracle_bsdf.hpp / below
+//   * lights: QuadLight, SphereLight, EnvironmentLight + HDRITexture
+//     (light.hpp, envLight.hpp, texture.hpp, texture.cpp:95-149),
+//     discover_emissive_objects_as_lights (lightDiscovery.hpp:5-81)
+//   * integrator: getRayColor of maxdepth_nee.hpp:9-256 (recursive, REF_NEE)
+//     and the build's NEE+MIS / medium / roulette extensions (iterative)
+//   * the pixel loop of SceneInfo::render (renderManager.hpp:97-155)
+// Every draw the reference takes from gl::rand_num uses the build's
+// counter-based generator with the same (path, bounce, slot) keys as the CUDA
+// path, so the two can be compared path by path; Halton dimensions are the
+// reference's.
+//
+// Parity is pinned by tests/golden/ (fixtures written by running the
+// reference itself, tests/golden/make_golden.py).
+#include <algorithm>
+#include <array>
+#include <atomic>
+#include <chrono>
+#include <cmath>
+#include <cstdint>
+#include <cstdlib>
+#include <cstring>
+#include <memory>
+#include <numeric>
+#include <thread>
+#include <vector>
+
+#include "../include/pathtracer_gb300.h"
+#include "pt_oracle_bsdf.hpp"
+
+namespace orc {
+
+// ================================================================ materials
+Material make_material(int type, int flags, const float *p) {
+  Material m;
+  m.type = type;
+  m.flags = flags;
+  std::memcpy(m.p, p, sizeof m.p);
+  if (type == PT_MAT_CONDUCTOR) m.tr = TR{p[6], p[7]};
+  if (type == PT_MAT_MF_DIELECTRIC) m.tr = TR{p[1], p[2]};
+  if (type == PT_MAT_DISNEY) {  // disneyPrincipledBSDF.hpp:34-66
+    const float st = p[3], metallic = p[4], sheen = p[10], cc = p[12];
+    m.w[0] = (1 - metallic) * (1 - st);
+    m.w[1] = (1 - st * (1 - metallic));
+    m.w[2] = (1 - metallic) * st;
+    m.w[3] = (float)(0.25 * cc);
+    m.w[4] = (1 - metallic) * sheen;
+    m.tr = TR::from_rough(p[7], p[9]);
+    m.cc = CC{(1.f - p[13]) * 0.1f + p[13] * 0.001f};
+  }
+  if (type == PT_MAT_HAIR) {  // hairMarsch.hpp:9-34
+    const float bm = p[5], bn = p[6], alpha = p[7];
+    m.v[0] = sqr(0.726f * bm + 0.812f * sqr(bm) + 3.7f * std::pow(bm, 20.f));
+    m.v[1] = (float)(.25 * m.v[0]);
+    m.v[2] = 4 * m.v[0];
+    m.v[3] = m.v[2];
+    m.s = 0.626657069f * (0.265f * bn + 1.194f * sqr(bn) + 5.372f * std::pow(bn, 22.f));
+    m.s2k[0] = std::sin(alpha);
+    m.c2k[0] = safe_sqrt(1 - sqr(m.s2k[0]));
+    for (int i = 1; i < 3; ++i) {
+      m.s2k[i] = 2 * m.c2k[i - 1] * m.s2k[i - 1];
+      m.c2k[i] = sqr(m.c2k[i - 1]) - sqr(m.s2k[i - 1]);
+    }
+    if (flags & PT_MAT_FLAG_MELANIN)  // pbrt-v3 SigmaAFromConcentration (extension)
+      m.sigma_a = V(0.419f, 0.697f, 1.37f) * p[8] + V(0.187f, 0.4f, 1.05f) * p[9];
+    else
+      m.sigma_a = V(p[0], p[1], p[2]);
+  }
+  return m;
+}
+
+static V base_color(const Material &m) { return V(m.p[0], m.p[1], m.p[2]); }
+
+// ---- Disney lobes (disneyDiffuse/Metal/Glass/Sheen/Clearcoat.hpp)
+static V dis_diffuse_f(const Material &m, V wow, V wiw, V n) {
+  Onb b(n);
+  V wo = b.local(wow), wi = b.local(wiw);
+  float ci = std::fabs(wi.z), co = std::fabs(wo.z);
+  const float rough = m.p[7], ss = m.p[5];
+  V wh = (wo + wi).normalize();
+  float whwi = dot(wh, wi);
+  float fd90 = 0.5f + 2.f * rough * std::pow(std::fabs(whwi), 2.f);
+  V base = base_color(m);
+  V bd = base * (float)(1.f / PI);
+  bd = bd * (hacked_schlick(ci, fd90) * hacked_schlick(co, fd90));
+  float fss90 = rough * std::pow(std::fabs(whwi), 2.f);
+  V bs = (1.25f * base) * (float)(1.f / PI);
+  bs = bs * (hacked_schlick(ci, fss90) * hacked_schlick(co, fss90) * (1.f / (ci + co) - 0.5f) + 0.5f);
+  return (1.f - ss) * bd + bs * ss;
+}
+static V dis_metal_f(const Material &m, V wow, V wiw, V n, bool variant) {
+  Onb b(n);
+  V wo = b.local(wow), wi = b.local(wiw);
+  V wh = (wo + wi).normalize();
+  if (wi.z <= 0 || wo.z <= 0 || m.tr.smooth()) return V(0.f);
+  float dhi = std::fabs(dot(wh, wi));
+  V base = base_color(m);
+  V F0 = base;
+  if (variant) {  // f_variant with its default arguments (disneyMetal.hpp:98-124)
+    const float st = 0.5f, eta = 1.0f, specular = 0.5f, metallic = 0.5f;
+    V Ks = V(1 - st) + st * base;
+    float R0 = sqr((eta - 1) / (eta + 1));
+    F0 = specular * R0 * (1 - metallic) * Ks + metallic * base;
+  }
+  V F = fresnel_schlick(dhi, F0);
+  float D = m.tr.D(wh), G = m.tr.G(wo, wi);
+  return F * D * G / std::fabs(4.f * wi.z * wo.z);
+}
+static V dis_sheen_f(const Material &m, V wow, V wiw, V n) {
+  Onb b(n);
+  V wo = b.local(wow), wi = b.local(wiw);
+  V wh = (wo + wi).normalize();
+  float a = std::fabs(dot(wh, wi));
+  V base = base_color(m);
+  float lum = dot(base, V(0.2126f, 0.7152f, 0.0722f));
+  V tint = lum > 0.0f ? base / lum : V(1.0f);
+  const float st = m.p[11];
+  V cs = V(1.f + st * (tint.x - 1.f), 1.f + st * (tint.y - 1.f), 1.f + st * (tint.z - 1.f));
+  return cs * std::pow((1 - a), 5.f);
+}
+static V dis_clearcoat_f(const Material &m, V wow, V wiw, V n) {
+  Onb b(n);
+  V wo = b.local(wow), wi = b.local(wiw);
+  V wh = (wo + wi).normalize();
+  if (wi.z <= 0 || wo.z <= 0) return V(0.f);
+  float a = std::fabs(dot(wh, wi));
+  V F = fresnel_schlick(a, V(sqr((1.5f - 1) / (1.5f + 1))));
+  return F * m.cc.D(wh) * m.cc.G(wo, wi) / std::fabs(4.f * wi.z * wo.z);
+}
+static float eta_of(const Material &m) { return m.type == PT_MAT_DISNEY ? m.p[14] : m.p[0]; }
+static V glass_f(const Material &m, V wo, V wi, V n, bool tinted) {
+  Onb b(n);
+  return mfd_f(m.tr, eta_of(m), b.local(wo.normalize()), b.local(wi.normalize()), base_color(m), tinted);
+}
+static float glass_pdf(const Material &m, V wo, V wi, V n) {
+  if (eta_of(m) == 1 || m.tr.smooth()) return 0.f;
+  Onb b(n);
+  return mfd_at(m.tr, eta_of(m), b.local(wo.normalize()), b.local(wi.normalize()));
+}
+// MFDielectric::scatter / DisneyGlass::scatter (dielectric.hpp:19-98)
+static bool glass_scatter(const Material &m, V wo, V n, Scatter &s, float uc, float u0, float u1, bool tinted) {
+  const float eta = eta_of(m);
+  if (eta == 1 || m.tr.smooth()) {
+    float R = fresnel_dielectric(dot(n, wo), eta), T = 1 - R;
+    if (R == 0 && T == 0) return false;
+    if (uc < R / (R + T)) {
+      s.dir = reflect_p(wo, n).normalize();
+      s.type = SPEC | REFL;
+      s.att = V(1.0f);
+      s.pdf_val = R;
+      return true;
+    }
+    V wt;
+    float etap;
+    if (!refract_p(wo, n, eta, etap, wt)) return false;
+    s.dir = wt;
+    s.type = SPEC | TRANS;
+    s.pdf_val = T;
+    s.att = V(1.0f);  // TransportMode::Importance (config.hpp:23)
+    return true;
+  }
+  Onb b(n);
+  V wol = b.local(wo);
+  V wi = mfd_get(m.tr, eta, b, wol, uc, u0, u1);
+  if (wi.near_zero()) return false;
+  s.dir = wi;
+  bool is_refl = dot(b.local(wi), b.local(wo)) > 0;
+  s.type = is_refl ? (GLOSSY | REFL) : (GLOSSY | TRANS);
+  s.att = glass_f(m, wo, wi, n, tinted);
+  s.pdf_val = mfd_at(m.tr, eta, wol, b.local(wi.normalize()));
+  return true;
+}
+
+// ---- hair (hairMarsch.hpp, hairMarsch.cpp, hairPDF.cpp)
+static float hair_Mp(float ci, float co, float si, float so, float v) {
+  float a = ci * co / v, b = si * so / v;
+  return (v <= .1) ? (fast_exp(log_i0f(a) - b - 1 / v + 0.6931f + std::log(1 / (2 * v))))
+                   : (fast_exp(-b) * i0f(a)) / (std::sinh(1 / v) * 2 * v);
+}
+static float hair_Phi(int p, float go, float gt) { return (float)(2 * p * gt - 2 * go + p * PI); }
+static float logistic(float x, float s) {
+  x = std::abs(x);
+  return std::exp(-x / s) / (s * sqr(1 + std::exp(-x / s)));
+}
+static float logistic_cdf(float x, float s) { return 1 / (1 + std::exp(-x / s)); }
+static float hair_Np(float phi, int p, float s, float go, float gt) {
+  float dphi = phi - hair_Phi(p, go, gt);
+  while (dphi > PI) dphi -= (float)(2 * PI);
+  while (dphi < -PI) dphi += (float)(2 * PI);
+  return logistic(dphi, s) / (logistic_cdf((float)PI, s) - logistic_cdf((float)-PI, s));
+}
+static void hair_Ap(float co, float eta, float h, V T, V ap[4]) {
+  float cgo = safe_sqrt(1 - sqr(h));
+  float f = fresnel_dielectric(co * cgo, eta);
+  ap[0] = V(f);
+  ap[1] = sqr(1 - f) * T;
+  ap[2] = ap[1] * T * f;
+  V d = V(1.f) - T * f;
+  ap[3] = d.near_zero() ? V(0.f) : ap[2] * f * T / d;
+}
+static void hair_ApPDF(const Material &m, float co, float out[4]) {
+  const float eta = m.p[4], h = m.p[3];
+  float so = safe_sqrt(1 - sqr(co));
+  float ct = safe_sqrt(1 - sqr(so / eta));
+  float etap = safe_sqrt(sqr(eta) - sqr(so)) / co;
+  float cgt = safe_sqrt(1 - sqr(h / etap));
+  float k = 2 * cgt / ct;
+  V T(std::exp(-m.sigma_a.x * k), std::exp(-m.sigma_a.y * k), std::exp(-m.sigma_a.z * k));
+  V ap[4];
+  hair_Ap(co, eta, h, T, ap);
+  float sumY = 0.f;
+  for (auto &a : ap) sumY += (a.x + a.y + a.z) / 3.f;
+  for (int i = 0; i < 4; ++i) out[i] = ((ap[i].x + ap[i].y + ap[i].z) / 3.f) / sumY;
+}
+static void hair_rot(const Material &m, int p, float so, float co, float &sp, float &cp) {
+  if (p == 0) {
+    sp = so * m.c2k[1] - co * m.s2k[1];
+    cp = co * m.c2k[1] + so * m.s2k[1];
+  } else if (p == 1) {
+    sp = so * m.c2k[0] + co * m.s2k[0];
+    cp = co * m.c2k[0] - so * m.s2k[0];
+  } else if (p == 2) {
+    sp = so * m.c2k[2] + co * m.s2k[2];
+    cp = co * m.c2k[2] - so * m.s2k[2];
+  } else {
+    sp = so;
+    cp = co;
+  }
+  cp = std::abs(cp);
+}
+static V hair_eval(const Material &m, V wi, V wo) {  // hairMarsch.cpp:28-97
+  const float eta = m.p[4], h = m.p[3];
+  float so = wo.x, co = safe_sqrt(1 - so * so), phio = std::atan2(wo.z, wo.y);
+  float go = std::asin(std::clamp(so, -1.f, 1.f));
+  float si = wi.x, ci = safe_sqrt(1 - si * si), phii = std::atan2(wi.z, wi.y);
+  float ct = safe_sqrt(1 - sqr(so / eta));
+  float etap = safe_sqrt(sqr(eta) - sqr(so));
+  float sgt = h / etap, cgt = safe_sqrt(1 - sgt * sgt);
+  float gt = std::asin(std::clamp(sgt, -1.f, 1.f));
+  float k = 2 * cgt / ct;
+  V T(fast_exp(-m.sigma_a.x * k), fast_exp(-m.sigma_a.y * k), fast_exp(-m.sigma_a.z * k));
+  float phi = phii - phio;
+  V ap[4];
+  hair_Ap(co, eta, h, T, ap);
+  V bsdf(0.f);
+  for (int p = 0; p < 3; ++p) bsdf += ap[p] * (hair_Mp(ci, co, si, so, m.v[p]) * hair_Np(phi, p, m.s, go, gt));
+  bsdf += hair_Mp(ci, co, si, so, m.v[3]) * ap[3] / (float)(2 * PI);
+  if (std::abs(wi.z) > 0.f) bsdf = bsdf / std::abs(wi.z);
+  return bsdf;
+}
+static float hair_at(const Material &m, V wol, V wil) {  // hairPDF.cpp:101-152
+  const float eta = m.p[4], h = m.p[3];
+  float si = wil.x, ci = safe_sqrt(1 - si * si), phii = std::atan2(wil.z, wil.y);
+  float so = wol.x, co = safe_sqrt(1 - so * so), phio = std::atan2(wol.z, wol.y);
+  float go = std::asin(std::clamp(so, -1.f, 1.f));
+  float etap = safe_sqrt(sqr(eta) - sqr(so)) / co;
+  float gt = std::asin(std::clamp(h / etap, -1.f, 1.f));
+  float dphi = phii - phio;
+  if (dphi < -PI)
+    dphi += (float)(2 * PI);
+  else if (dphi > PI)
+    dphi -= (float)(2 * PI);
+  float ap[4];
+  hair_ApPDF(m, co, ap);
+  float pdf = 0.f;
+  for (int p = 0; p < 3; ++p) {
+    float sp, cp;
+    hair_rot(m, p, so, co, sp, cp);
+    pdf += ap[p] * hair_Mp(ci, cp, si, sp, m.v[p]) * hair_Np(dphi, p, m.s, go, gt);
+  }
+  return pdf;
+}
+
+bool mat_scatter(const Material &m, V ray_dir, const Hit &rec, Scatter &s, float uc, float u0, float u1) {
+  const V n = rec.normal;
+  const V wo = -ray_dir.normalize();
+  switch (m.type) {
+  case PT_MAT_LAMBERTIAN: {  // material.hpp:88-105
+    s.type = DIFF | REFL;
+    s.att = base_color(m) * (float)(1.0f / PI);
+    Onb b(n);
+    s.dir = b.at(cosine_sample(u0, u1)).normalize();
+    s.pdf_val = cosine_pdf_at(n, s.dir);
+    return true;
+  }
+  case PT_MAT_CONDUCTOR: {  // conductor.hpp:11-63, mfPDF.hpp:19-45 (BIASED_SAMPLING)
+    if (m.tr.smooth()) {
+      V wi = reflect_p(wo, n).normalize();
+      if (dot(n, wi) <= 0) return false;
+      s.dir = wi;
+      s.att = fresnel_complex(std::fabs(dot(n, wi)), V(m.p[0], m.p[1], m.p[2]), V(m.p[3], m.p[4], m.p[5]));
+      s.type = SPEC | REFL;
+      s.pdf_val = 0.f;
+      return true;
+    }
+    Onb b(n);
+    V wol = b.local(wo.normalize());
+    V mm = m.tr.sample_wm(wol, u0, u1);
+    V wil = reflect_p(wol, mm);
+    if (!same_hemi(wol, wil)) wil.z = -wol.z;
+    V wi = b.at(wil).normalize();
+    if (wi.near_zero()) return false;
+    if (dot(n, wi) <= 0) return false;
+    s.dir = wi;
+    s.type = GLOSSY | REFL;
+    s.att = mat_f(m, wo, wi, rec);
+    s.pdf_val = mf_at(m.tr, b, wol, wi);
+    return true;
+  }
+  case PT_MAT_MF_DIELECTRIC:
+    return glass_scatter(m, wo, n, s, uc, u0, u1, false);
+  case PT_MAT_THIN_DIELECTRIC: {  // thinDielectric.hpp:14-68
+    float R = fresnel_dielectric(std::fabs(dot(n, wo)), m.p[0]), T = 1 - R;
+    if (R < 1) {
+      R += sqr(T) * R / (1 - sqr(R));
+      T = 1 - R;
+    }
+    if (R == 0 && T == 0) return false;
+    if (m.flags & PT_MAT_FLAG_SPLIT_RAY) {
+      s.type = (SPEC | REFL) | (SPEC | TRANS);
+      s.pdf_val = R;
+      return true;
+    }
+    if (uc < R / (R + T)) {
+      s.dir = reflect_p(wo, n).normalize();
+      s.type = SPEC | REFL;
+      s.pdf_val = R;
+    } else {
+      s.dir = -wo.normalize();
+      s.type = SPEC | TRANS;
+      s.pdf_val = T;
+    }
+    s.att = V(1.0f);
+    return true;
+  }
+  case PT_MAT_PHONG: {
+    // The build's consistent form of Phong::scatter (material.hpp:320-366):
+    // lobe picked with uc, attenuation = f, pdf_val = scatter_pdf.
+    float si = (m.p[3] + m.p[4] + m.p[5]) / 3.0f, di = (m.p[0] + m.p[1] + m.p[2]) / 3.0f;
+    float sp = si / (si + di);
+    if (uc < sp) {
+      V R = reflect_gl(-wo, n);
+      Onb b(R);
+      float theta = std::acos(std::pow(u0, 1.0f / (m.p[9] + 1.0f)));
+      float phi = (float)(2.0f * PI * u1);
+      float st = std::sin(theta);
+      s.dir = b.at(V(st * std::cos(phi), st * std::sin(phi), std::cos(theta))).normalize();
+      s.type = GLOSSY | REFL;
+    } else {
+      Onb b(n);
+      s.dir = b.at(cosine_sample(u0, u1));
+      s.type = DIFF | REFL;
+    }
+    s.att = mat_f(m, wo, s.dir, rec);
+    s.pdf_val = mat_pdf(m, wo, s.dir, rec);
+    return s.pdf_val > 0.f;
+  }
+  case PT_MAT_DISNEY: {  // disneyPrincipledBSDF.cpp:3-80
+    if (rec.is_inside) return glass_scatter(m, wo, n, s, uc, u0, u1, true);
+    float pmf, ur;
+    int lobe = sample_discrete(m.w, 4, uc, &pmf, &ur);
+    if (lobe == -1 || pmf <= 1e-6f) return false;
+    const float v0 = ur, v1 = u1;
+    if (lobe == 0) {
+      Onb b(n);
+      V wi = b.at(cosine_sample(v0, v1));
+      s.dir = wi.normalize();
+      s.pdf_val = cosine_pdf_at(n, wi);
+      s.type = DIFF | REFL;
+    } else if (lobe == 1) {
+      if (m.tr.smooth()) {
+        V wi = reflect_p(wo, n).normalize();
+        if (dot(n, wi) <= 0) return false;
+        s.dir = wi;
+        s.att = fresnel_schlick(std::fabs(dot(n, wi)), base_color(m));
+        s.type = SPEC | REFL;
+        s.pdf_val = 0.f;
+        return true;
+      }
+      Onb b(n);
+      V wol = b.local(wo.normalize());
+      V mm = m.tr.sample_wm(wol, v0, v1);
+      V wil = reflect_p(wol, mm);
+      if (!same_hemi(wol, wil)) wil.z = -wol.z;
+      V wi = b.at(wil).normalize();
+      if (wi.near_zero() || dot(n, wi) <= 0) return false;
+      s.dir = wi;
+      s.pdf_val = mf_at(m.tr, b, wol, wi);
+      s.type = GLOSSY | REFL;
+    } else if (lobe == 2) {
+      if (!glass_scatter(m, wo, n, s, ur, v0, v1, true)) return false;
+      if (s.type & SPEC) return true;
+    } else {
+      Onb b(n);
+      V wol = b.local(wo.normalize());
+      V h = m.cc.sample_h(v0, v1);
+      V wil = reflect_p(wol, h);
+      if (!same_hemi(wol, wil)) wil.z = -wol.z;
+      V wi = b.at(wil).normalize();
+      if (dot(n, wi) <= 0) return false;
+      s.dir = wi;
+      s.pdf_val = m.cc.at(b, wol, wi);
+      s.type = GLOSSY | REFL;
+    }
+    if (s.pdf_val <= 1e-6f) return false;
+    V wi = s.dir.normalize();
+    Hit r2 = rec;
+    r2.is_inside = false;
+    s.att = mat_f(m, wo, wi, r2);
+    s.pdf_val = mat_pdf(m, wo, wi, r2);
+    if (s.pdf_val <= 1e-7f) return false;
+    return true;
+  }
+  case PT_MAT_HAIR: {  // hairMarsch.cpp:4-26 + hairPDF.cpp:14-99
+    const float eta = m.p[4], h = m.p[3];
+    Onb b(n);
+    V wol = b.local(wo);
+    float so = wol.x, co = safe_sqrt(1 - so * so), phio = std::atan2(wol.z, wol.y);
+    float go = std::asin(std::clamp(so, -1.f, 1.f));
+    float apd[4];
+    hair_ApPDF(m, co, apd);
+    int p = sample_discrete(apd, 4, uc, nullptr, nullptr);
+    float sp, cp;
+    hair_rot(m, p, so, co, sp, cp);
+    float ct = 1 + m.v[p] * std::log(std::max(u0, (float)1e-5) + (1.f - u0) * fast_exp(-2.f / m.v[p]));
+    float st = safe_sqrt(1 - sqr(ct));
+    float cphi_ = (float)std::cos(2 * PI * u1);
+    float si = -ct * sp + st * cphi_ * cp;
+    float ci = safe_sqrt(1 - sqr(si));
+    float etap = safe_sqrt(sqr(eta) - sqr(so)) / co;
+    float gt = std::asin(std::clamp(h / etap, -1.f, 1.f));
+    float dphi;
+    if (p < 3) {
+      float lo = logistic_cdf((float)-PI, m.s), hi = logistic_cdf((float)PI, m.s);
+      float uu = lo + uc * (hi - lo);
+      float x = -m.s * std::log(1 / uu - 1);
+      dphi = hair_Phi(p, go, gt) + std::clamp(x, (float)-PI, (float)PI);
+    } else {
+      dphi = (float)(2 * PI * uc);
+    }
+    float phii = dphi + phio;
+    V wil(si, ci * std::cos(phii), ci * std::sin(phii));
+    V wi = b.at(wil).normalize();
+    s.att = mat_f(m, wo, wi, rec);
+    s.pdf_val = hair_at(m, wol, b.local(wi));
+    s.dir = wi;
+    s.type = GLOSSY | REFL;
+    return true;
+  }
+  default:
+    return false;  // DiffuseEmitter::scatter (material.hpp:475-481)
+  }
+}
+
+V mat_f(const Material &m, V wo, V wi, const Hit &rec) {
+  const V n = rec.normal;
+  switch (m.type) {
+  case PT_MAT_LAMBERTIAN:
+    return base_color(m) * (float)(1.0f / PI);
+  case PT_MAT_CONDUCTOR: {  // conductor.hpp:109-139
+    Onb b(n);
+    V wol = b.local(wo.normalize()), wil = b.local(wi.normalize());
+    if (wil.z <= 0 || wol.z <= 0) return V(0.f);
+    if (m.tr.smooth()) return V(0.f);
+    V ml = (wol + wil).normalize();
+    float D = m.tr.D(ml), G = m.tr.G(wol, wil);
+    V F = fresnel_complex(std::fabs(dot(wol, ml)), V(m.p[0], m.p[1], m.p[2]), V(m.p[3], m.p[4], m.p[5]));
+    return D * F * G / (4.f * std::abs(wol.z) * std::abs(wil.z));
+  }
+  case PT_MAT_MF_DIELECTRIC:
+    return glass_f(m, wo, wi, n, false);
+  case PT_MAT_PHONG: {  // material.hpp:369-411
+    V o = wo.normalize(), i = wi.normalize();
+    float ci = dot(n, i);
+    if (ci <= 0) return V(0.f);
+    float si = (m.p[3] + m.p[4] + m.p[5]) / 3.0f, di = (m.p[0] + m.p[1] + m.p[2]) / 3.0f;
+    float sp = si / (si + di);
+    V diff = base_color(m) * (float)(1.0f / PI);
+    V R = reflect_p(o, n);
+    float ca = std::max(dot(i, R), 0.0f);
+    float pt = std::pow(ca, m.p[9]);
+    float norm = (float)((m.p[9] + 2.0f) / (2.0f * PI));
+    V spec = V(m.p[3], m.p[4], m.p[5]) * (norm * pt);
+    return sp * spec + (1.0f - sp) * diff;
+  }
+  case PT_MAT_DISNEY: {  // disneyPrincipledBSDF.hpp:72-91
+    if (rec.is_inside) return glass_f(m, wo, wi, n, true);
+    V r(0.f);
+    r += dis_diffuse_f(m, wo, wi, n) * m.w[0];
+    r += dis_metal_f(m, wo, wi, n, true) * m.w[1];
+    r += glass_f(m, wo, wi, n, true) * m.w[2];
+    r += dis_clearcoat_f(m, wo, wi, n) * m.w[3];
+    r += dis_sheen_f(m, wo, wi, n) * m.w[4];
+    return r;
+  }
+  case PT_MAT_HAIR: {
+    Onb b(n);
+    return hair_eval(m, b.local(wi.normalize()), b.local(wo.normalize()));
+  }
+  default:
+    return V(0.f);
+  }
+}
+
+float mat_pdf(const Material &m, V wo, V wi, const Hit &rec) {
+  const V n = rec.normal;
+  switch (m.type) {
+  case PT_MAT_LAMBERTIAN:
+    return cosine_pdf_at(n, wi);
+  case PT_MAT_CONDUCTOR: {  // conductor.hpp:81-99
+    if (m.tr.smooth()) return 0.f;
+    Onb b(n);
+    if (dot(n, wi) <= 0) return 0.0f;
+    return mf_at(m.tr, b, b.local(wo.normalize()), wi);
+  }
+  case PT_MAT_MF_DIELECTRIC:
+    return glass_pdf(m, wo, wi, n);
+  case PT_MAT_PHONG: {  // material.hpp:414-463
+    V o = wo.normalize(), i = wi.normalize();
+    float si = (m.p[3] + m.p[4] + m.p[5]) / 3.0f, di = (m.p[0] + m.p[1] + m.p[2]) / 3.0f;
+    float tot = si + di;
+    if (tot == 0.f) return 0.f;
+    float ps = si / tot, pd = di / tot;
+    float pls = 0.f, pld = 0.f;
+    if (ps > 0) {
+      V R = reflect_gl(-o, n.normalize()).normalize();
+      float c = std::max(dot(i.normalize(), R), 0.0f);
+      pls = (float)((m.p[9] + 1.0f) / (2.0f * PI) * std::pow(c, m.p[9]));
+    }
+    if (pd > 0) {
+      float c = dot(i, n.normalize());
+      if (c > 0) pld = (float)(c / PI);
+    }
+    return ps * pls + pd * pld;
+  }
+  case PT_MAT_DISNEY: {  // disneyPrincipledBSDF.cpp:82-113
+    if (rec.is_inside) return glass_pdf(m, wo, wi, n);
+    float sw = m.w[0] + m.w[1] + m.w[2] + m.w[3];
+    float p = 0.f;
+    p += (m.w[0] / sw) * cosine_pdf_at(n, wi);
+    float pm = 0.f;
+    if (!m.tr.smooth()) {
+      Onb b(n);
+      pm = mf_at(m.tr, b, b.local(wo.normalize()), wi);
+    }
+    p += (m.w[1] / sw) * pm;
+    p += (m.w[2] / sw) * glass_pdf(m, wo, wi, n);
+    Onb b(n);
+    p += (m.w[3] / sw) * m.cc.at(b, b.local(wo.normalize()), wi);
+    return p;
+  }
+  case PT_MAT_HAIR: {
+    Onb b(n);
+    return hair_at(m, b.local(wo), b.local(wi.normalize()));
+  }
+  default:
+    return 0.f;
+  }
+}
+
+V mat_emit(const Material &m, V ray_dir, const Hit &rec) {  // material.hpp:483-488
+  if (m.type != PT_MAT_DIFFUSE_EMITTER) return V(0.f);
+  if (dot(rec.normal, -ray_dir) > 0) return V(m.p[0], m.p[1], m.p[2]) * m.p[3];
+  return V(0.0f);
+}
+
+// ==================================================================== scene
+struct Box {
+  V lo, hi;
+  // AABB::intersect (aabb.hpp:21-42)
+  bool hit(V o, V d, float tmin, float tmax) const {
+    for (int i = 0; i < 3; i++) {
+      float inv = 1.0f / d[i];
+      float t0 = (lo[i] - o[i]) * inv;
+      float t1 = (hi[i] - o[i]) * inv;
+      if (inv < 0.0f) std::swap(t0, t1);
+      tmin = t0 > tmin ? t0 : tmin;
+      tmax = t1 < tmax ? t1 : tmax;
+      if (tmax <= tmin) return false;
+    }
+    return true;
+  }
+};
+static Box merge(const Box &a, const Box &b) {
+  return Box{V(std::min(a.lo.x, b.lo.x), std::min(a.lo.y, b.lo.y), std::min(a.lo.z, b.lo.z)),
+             V(std::max(a.hi.x, b.hi.x), std::max(a.hi.y, b.hi.y), std::max(a.hi.z, b.hi.z))};
+}
+
+struct MeshO {
+  std::vector<V> pos, nrm;
+  std::vector<std::array<int, 3>> tri, ntri;
+  int mat = 0, prim_base = 0;
+  Box aabb;
+  struct Node {
+    Box box;
+    int left = -1, right = -1;
+    std::vector<int> ids;
+  };
+  std::vector<Node> nodes;
+  int build(std::vector<int> ids) {  // MeshBVHNode ctor (meshBVH.cpp:6-55)
+    V mn(INFINITY), mx(-INFINITY);
+    for (int id : ids)
+      for (int k : tri[id]) {
+        mn = V(std::min(mn.x, pos[k].x), std::min(mn.y, pos[k].y), std::min(mn.z, pos[k].z));
+        mx = V(std::max(mx.x, pos[k].x), std::max(mx.y, pos[k].y), std::max(mx.z, pos[k].z));
+      }
+    int me = (int)nodes.size();
+    nodes.emplace_back();
+    nodes[me].box = Box{mn - V(1e-3f), mx + V(1e-3f)};
+    int count = (int)ids.size();
+    if (count <= 4) {
+      nodes[me].ids = ids;
+      return me;
+    }
+    V ext = mx - mn;
+    int axis = ext.x > ext.y && ext.x > ext.z ? 0 : ext.y > ext.z ? 1 : 2;
+    std::sort(ids.begin(), ids.end(), [&](int a, int b) {
+      V ca = (pos[tri[a][0]] + pos[tri[a][1]] + pos[tri[a][2]]) / 3.0f;
+      V cb = (pos[tri[b][0]] + pos[tri[b][1]] + pos[tri[b][2]]) / 3.0f;
+      return ca[axis] < cb[axis];
+    });
+    int mid = count / 2;
+    int l = build(std::vector<int>(ids.begin(), ids.begin() + mid));
+    int r = build(std::vector<int>(ids.begin() + mid, ids.end()));
+    nodes[me].left = l;
+    nodes[me].right = r;
+    return me;
+  }
+  // hitTriangle (meshBVH.cpp:85-143)
+  bool hit_tri(int id, V o, V d, float tmin, float tmax, Hit &rec) const {
+    const V &p0 = pos[tri[id][0]], &p1 = pos[tri[id][1]], &p2 = pos[tri[id][2]];
+    V e1 = p1 - p0, e2 = p2 - p0;
+    V P = cross(d, e2);
+    float det = dot(e1, P);
+    if (std::fabs(det) < 1e-8f) return false;
+    float inv = 1.0f / det;
+    V T = o - p0;
+    float u = dot(T, P) * inv;
+    if (u < 0 || u > 1) return false;
+    V Q = cross(T, e1);
+    float v = dot(d, Q) * inv;
+    if (v < 0 || u + v > 1) return false;
+    float t = dot(e2, Q) * inv;
+    if (t < tmin || t > tmax) return false;
+    V n;
+    if (!nrm.empty()) {
+      const auto &ni = ntri[id];
+      n = normalize((1 - u - v) * nrm[ni[0]] + u * nrm[ni[1]] + v * nrm[ni[2]]);
+    } else {
+      n = normalize(cross(e1, e2));
+    }
+    V Ng = normalize(cross(e1, e2));
+    if (dot(n, Ng) < 0.f) n = -n;
+    rec.normal = n;
+    rec.t = t;
+    rec.position = o + t * d;
+    rec.prim = prim_base + id;
+    return true;
+  }
+  bool hit_node(int ni, V o, V d, float tmin, float tmax, Hit &rec) const {  // meshBVH.cpp:57-83
+    const Node &N = nodes[ni];
+    if (!N.box.hit(o, d, tmin, tmax)) return false;
+    bool hit = false;
+    float closest = tmax;
+    if (N.left < 0) {
+      for (int id : N.ids)
+        if (hit_tri(id, o, d, tmin, closest, rec)) {
+          hit = true;
+          closest = rec.t;
+        }
+    } else {
+      if (hit_node(N.left, o, d, tmin, closest, rec)) {
+        hit = true;
+        closest = rec.t;
+      }
+      if (hit_node(N.right, o, d, tmin, closest, rec)) hit = true;
+    }
+    return hit;
+  }
+};
+
+struct Obj {
+  int kind, index;
+  Box box;
+  int mat, flip, prim;
+  int light = -1;
+  // quad
+  int axis;
+  float k, d0min, d0max, d1min, d1max;
+  // sphere
+  V c;
+  float r;
+};
+
+struct Light {
+  int type;  // 0 quad, 1 sphere, 2 env
+  V v0, e1, e2, normal, c, color;
+  float radius = 0, area = 0, intensity = 0;
+};
+
+struct Scene {
+  std::vector<Material> mats;
+  std::vector<MeshO> meshes;
+  std::vector<Obj> objs;
+  struct TNode {
+    Box box;
+    int left = -1, right = -1;  // node ids (>= 0) or ~object
+  };
+  std::vector<TNode> top;
+  int root = 0;
+  std::vector<Light> lights;
+  bool has_env = false;
+  int env_w = 0, env_h = 0;
+  float env_intensity = 1.f;
+  std::vector<V> texels;  // [y][x]
+  std::vector<float> env_pdf, alias_prob;
+  std::vector<int> alias_idx;
+  V bg;
+  bool medium = false;
+  V sig_a, sig_s;
+  float sig_t_max = 0.f;
+
+  // Sphere / AARectangle / TriangleMesh intersect (+ FlipFace, set_normal)
+  bool hit_obj(int oi, V o, V d, float tmin, float tmax, Hit &rec) const {
+    const Obj &ob = objs[oi];
+    if (ob.kind == PT_OBJ_MESH) {
+      const MeshO &M = meshes[ob.index];
+      if (!M.hit_node(0, o, d, tmin, tmax, rec)) return false;
+      rec.set_normal(d, rec.normal);
+      rec.mat = M.mat;
+      rec.light = -1;
+      return true;
+    }
+    V dn = d.normalize();
+    if (ob.kind == PT_OBJ_QUAD) {  // primitive.cpp:31-122
+      int a = ob.axis, a0 = a == 0 ? 1 : 0, a1 = a == 2 ? 1 : 2;
+      float t = (ob.k - o[a]) / dn[a];
+      if (t < tmin || t > tmax) return false;
+      float q0 = o[a0] + t * dn[a0], q1 = o[a1] + t * dn[a1];
+      if (q0 < ob.d0min || q0 > ob.d0max || q1 < ob.d1min || q1 > ob.d1max) return false;
+      rec.t = t;
+      rec.position = o + t * dn;
+      V nn(a == 0 ? 1.f : 0.f, a == 1 ? 1.f : 0.f, a == 2 ? 1.f : 0.f);
+      rec.set_normal(d, nn);
+    } else {  // primitive.hpp:124-170
+      V oc = o - ob.c;
+      float A = dot(dn, dn), B = 2 * dot(dn, oc), Cc = dot(oc, oc) - ob.r * ob.r;
+      float disc = B * B - 4 * A * Cc;
+      if (disc < 0) return false;
+      float delta = std::sqrt(disc);
+      float t = (-B - delta) / (2 * A);
+      if (t < tmin || t > tmax) {
+        t = (-B + delta) / (2 * A);
+        if (t < tmin || t > tmax) return false;
+      }
+      rec.t = t;
+      rec.position = o + t * dn;
+      rec.set_normal(d, (rec.position - ob.c).normalize());
+    }
+    if (ob.flip) rec.is_inside = !rec.is_inside;
+    rec.mat = ob.mat;
+    rec.prim = ob.prim;
+    rec.light = ob.light;
+    return true;
+  }
+  bool hit_ref(int ref, V o, V d, float tmin, float tmax, Hit &rec) const {
+    if (ref < 0) return hit_obj(~ref, o, d, tmin, tmax, rec);
+    // BVHNode::intersect (bvh.hpp:27-41): left, then right with tmax = left.t
+    const TNode &N = top[ref];
+    if (!N.box.hit(o, d, tmin, tmax)) return false;
+    bool lh = hit_ref(N.left, o, d, tmin, tmax, rec);
+    bool rh = hit_ref(N.right, o, d, tmin, lh ? rec.t : tmax, rec);
+    return lh || rh;
+  }
+  bool intersect(V o, V d, Hit &rec, float tmin = 0.0001f, float tmax = 1e5f) const {
+    return hit_ref(root, o, d, tmin, tmax, rec);
+  }
+  Box ref_box(int ref) const { return ref < 0 ? objs[~ref].box : top[ref].box; }
+  // BVHNode ctor (bvh.hpp:46-102): halves of the insertion order, rand()
+  // axis per node, the axis ordering only the 2-object case.
+  int build_top(int i, int j) {
+    int axis = std::rand() % 3;
+    TNode N;
+    if (j - i == 1) {
+      N.left = N.right = ~i;
+    } else if (j - i == 2) {
+      const Box &a = objs[i].box, &b = objs[i + 1].box;
+      bool lt = (a.lo[axis] + a.hi[axis]) * 0.5f < (b.lo[axis] + b.hi[axis]) * 0.5f;
+      N.left = lt ? ~i : ~(i + 1);
+      N.right = lt ? ~(i + 1) : ~i;
+    } else {
+      int mid = i + (j - i) / 2;
+      N.left = build_top(i, mid);
+      N.right = build_top(mid, j);
+    }
+    N.box = merge(ref_box(N.left), ref_box(N.right));
+    top.push_back(N);
+    return (int)top.size() - 1;
+  }
+
+  // HDRITexture::getTexelColor(dir) (texture.hpp:105-115, texture.cpp:112-143)
+  V env_le(V dir) const {
+    V dn = dir.normalize();
+    float theta = std::acos(-dn.y);
+    float phi = (float)(std::atan2(-dn.z, dn.x) + PI);
+    float u = (float)(phi / (2.0f * PI)), v = (float)(theta / PI);
+    unsigned x = (unsigned)(u * env_w), y = (unsigned)(v * env_h);
+    float x1 = (u * env_w) - x, y1 = (v * env_h) - y;
+    x = std::clamp(x, 0u, (unsigned)env_w - 2);
+    y = std::clamp(y, 0u, (unsigned)env_h - 2);
+    float x2 = (float)(1.0 - x1), y2 = (float)(1.0 - y1);
+    V c1 = texels[y * env_w + x], c2 = texels[y * env_w + x + 1];
+    V c3 = texels[(y + 1) * env_w + x], c4 = texels[(y + 1) * env_w + x + 1];
+    V c12 = c1 * x2 + c2 * x1, c34 = c3 * x2 + c4 * x1;
+    return (c12 * y2 + c34 * y1) * env_intensity;
+  }
+  float env_alias_pdf(V dir) const {
+    V dn = dir.normalize();
+    float theta = std::acos(std::clamp(-dn.y, -1.f, 1.f));
+    float phi = (float)(std::atan2(-dn.z, dn.x) + PI);
+    float u = (float)(phi / (2 * PI)), v = (float)(theta / PI);
+    int cx = std::min((int)(u * env_w), env_w - 1), cy = std::min((int)(v * env_h), env_h - 1);
+    float st = std::sin(theta);
+    if (st <= 0) return 0.f;
+    return (float)(env_pdf[cy * env_w + cx] * (double)(env_w * env_h) / (2 * PI * PI * st));
+  }
+  V env_alias_sample(float u0, float u1, float u2, float &pdf) const {
+    const int N = env_w * env_h;
+    float f = u0 * N;
+    int i = std::min((int)f, N - 1);
+    int cell = (f - i < alias_prob[i]) ? i : alias_idx[i];
+    int cx = cell % env_w, cy = cell / env_w;
+    float u = (cx + u1) / env_w, v = (cy + u2) / env_h;
+    float st = (float)std::sin(PI * v), ct = (float)std::cos(PI * v);
+    float sp = (float)std::sin(2 * PI * u), cp = (float)std::cos(2 * PI * u);
+    pdf = st > 0 ? (float)(env_pdf[cell] * (double)N / (2 * PI * PI * st)) : 0.f;
+    return V(-st * cp, -ct, st * sp);
+  }
+};
+
+Scene *build_scene(const pt_scene_desc *d) {
+  auto *S = new Scene();
+  for (int i = 0; i < d->n_materials; ++i)
+    S->mats.push_back(make_material(d->materials[i].type, d->materials[i].flags, d->materials[i].p));
+  int n_tris = 0;
+  std::vector<int> tri_base;
+  for (int m = 0; m < d->n_meshes; ++m) {
+    tri_base.push_back(n_tris);
+    n_tris += d->meshes[m].n_triangles;
+  }
+  S->meshes.resize(d->n_meshes);
+  for (int m = 0; m < d->n_meshes; ++m) {
+    const pt_mesh_desc &md = d->meshes[m];
+    MeshO &M = S->meshes[m];
+    for (int i = 0; i < md.n_positions; ++i)
+      M.pos.emplace_back(md.positions[3 * i], md.positions[3 * i + 1], md.positions[3 * i + 2]);
+    if (md.normals)
+      for (int i = 0; i < md.n_normals; ++i)
+        M.nrm.emplace_back(md.normals[3 * i], md.normals[3 * i + 1], md.normals[3 * i + 2]);
+    const int32_t *ni = md.normal_indices ? md.normal_indices : md.indices;
+    for (int t = 0; t < md.n_triangles; ++t) {
+      M.tri.push_back({md.indices[3 * t], md.indices[3 * t + 1], md.indices[3 * t + 2]});
+      M.ntri.push_back({ni[3 * t], ni[3 * t + 1], ni[3 * t + 2]});
+    }
+    M.mat = md.material;
+    M.prim_base = tri_base[m];
+    V mn(INFINITY), mx(-INFINITY);
+    for (auto &p : M.pos) {
+      mn = V(std::min(mn.x, p.x), std::min(mn.y, p.y), std::min(mn.z, p.z));
+      mx = V(std::max(mx.x, p.x), std::max(mx.y, p.y), std::max(mx.z, p.z));
+    }
+    M.aabb = Box{mn - V(1e-3f), mx + V(1e-3f)};
+    std::vector<int> ids(md.n_triangles);
+    std::iota(ids.begin(), ids.end(), 0);
+    M.build(ids);
+  }
+  for (int o = 0; o < d->n_objects; ++o) {
+    const pt_object_desc &od = d->objects[o];
+    Obj ob{};
+    ob.kind = od.kind;
+    ob.index = od.index;
+    if (od.kind == PT_OBJ_MESH) {
+      ob.box = S->meshes[od.index].aabb;
+      ob.mat = d->meshes[od.index].material;
+    } else if (od.kind == PT_OBJ_QUAD) {
+      const pt_quad_desc &q = d->quads[od.index];
+      ob.axis = q.axis;
+      ob.k = q.k;
+      ob.d0min = q.d0_min;
+      ob.d0max = q.d0_max;
+      ob.d1min = q.d1_min;
+      ob.d1max = q.d1_max;
+      ob.mat = q.material;
+      ob.flip = q.flip_face;
+      ob.prim = n_tris + od.index;
+      int a0 = q.axis == 0 ? 1 : 0, a1 = q.axis == 2 ? 1 : 2;
+      V lo, hi;
+      lo[q.axis] = q.k - 1e-3f;
+      hi[q.axis] = q.k + 1e-3f;
+      lo[a0] = q.d0_min;
+      hi[a0] = q.d0_max;
+      lo[a1] = q.d1_min;
+      hi[a1] = q.d1_max;
+      ob.box = Box{lo, hi};
+    } else {
+      const pt_sphere_desc &s = d->spheres[od.index];
+      ob.c = V(s.center[0], s.center[1], s.center[2]);
+      ob.r = s.radius;
+      ob.mat = s.material;
+      ob.flip = s.flip_face;
+      ob.prim = n_tris + d->n_quads + od.index;
+      ob.box = Box{ob.c - V(s.radius), ob.c + V(s.radius)};
+    }
+    S->objs.push_back(ob);
+  }
+  std::srand(1);
+  S->root = S->build_top(0, (int)S->objs.size());
+  // lights (lightDiscovery.hpp:5-81, light.hpp:55-306)
+  for (auto &ob : S->objs) {
+    if (ob.kind == PT_OBJ_MESH) continue;
+    const Material &m = S->mats[ob.mat];
+    if (m.type != PT_MAT_DIFFUSE_EMITTER || m.p[3] <= 0.f) continue;
+    Light L{};
+    L.intensity = m.p[3];
+    L.color = V(m.p[0], m.p[1], m.p[2]);
+    if (ob.kind == PT_OBJ_QUAD) {
+      auto put = [&](float a, float b) {
+        V v;
+        v[ob.axis] = ob.k;
+        v[ob.axis == 0 ? 1 : 0] = a;
+        v[ob.axis == 2 ? 1 : 2] = b;
+        return v;
+      };
+      V v0 = put(ob.d0min, ob.d1min), v1 = put(ob.d0max, ob.d1min), v3 = put(ob.d0min, ob.d1max);
+      L.type = 0;
+      L.v0 = v0;
+      L.e1 = v1 - v0;
+      L.e2 = v3 - v0;
+      L.normal = cross(L.e1, L.e2).normalize();
+      L.area = cross(L.e1, L.e2).length();
+    } else {
+      L.type = 1;
+      L.c = ob.c;
+      L.radius = ob.r;
+      L.area = (float)(4 * PI * ob.r * ob.r);
+    }
+    ob.light = (int)S->lights.size();
+    S->lights.push_back(L);
+  }
+  if (d->env) {
+    S->has_env = true;
+    S->env_w = d->env->width;
+    S->env_h = d->env->height;
+    S->env_intensity = d->env->intensity;
+    const int W = S->env_w, H = S->env_h, N = W * H;
+    for (int i = 0; i < N; ++i)
+      S->texels.emplace_back(d->env->texels[3 * i], d->env->texels[3 * i + 1], d->env->texels[3 * i + 2]);
+    // luminance alias table over texel cells (extension)
+    std::vector<double> w(N);
+    double sum = 0;
+    for (int y = 0; y < H; ++y)
+      for (int x = 0; x < W; ++x) {
+        double l = 0;
+        for (int dy = 0; dy < 2; ++dy)
+          for (int dx = 0; dx < 2; ++dx) {
+            const V &t = S->texels[std::min(y + dy, H - 1) * W + std::min(x + dx, W - 1)];
+            l += 0.2126 * t.x + 0.7152 * t.y + 0.0722 * t.z;
+          }
+        w[y * W + x] = std::max(0.0, l * 0.25) * std::sin(PI * (y + 0.5) / H);
+        sum += w[y * W + x];
+      }
+    double fl = (sum > 0 ? sum / N : 1.0) * 1e-3;
+    sum = 0;
+    for (int y = 0; y < H; ++y)
+      for (int x = 0; x < W; ++x) {
+        w[y * W + x] += fl * std::sin(PI * (y + 0.5) / H);
+        sum += w[y * W + x];
+      }
+    S->env_pdf.resize(N);
+    for (int i = 0; i < N; ++i) S->env_pdf[i] = (float)(w[i] / sum);
+    S->alias_prob.assign(N, 1.f);
+    S->alias_idx.resize(N);
+    std::vector<double> sc(N);
+    std::vector<int> sm, lg;
+    for (int i = 0; i < N; ++i) {
+      sc[i] = w[i] / sum * N;
+      S->alias_idx[i] = i;
+      (sc[i] < 1.0 ? sm : lg).push_back(i);
+    }
+    while (!sm.empty() && !lg.empty()) {
+      int s = sm.back(), l = lg.back();
+      sm.pop_back();
+      lg.pop_back();
+      S->alias_prob[s] = (float)sc[s];
+      S->alias_idx[s] = l;
+      sc[l] = (sc[l] + sc[s]) - 1.0;
+      (sc[l] < 1.0 ? sm : lg).push_back(l);
+    }
+    Light L{};
+    L.type = 2;
+    L.intensity = d->env->intensity;
+    S->lights.push_back(L);
+  }
+  S->bg = V(d->bg_color[0], d->bg_color[1], d->bg_color[2]);
+  if (d->medium) {
+    S->medium = true;
+    S->sig_a = V(d->medium->sigma_a[0], d->medium->sigma_a[1], d->medium->sigma_a[2]);
+    S->sig_s = V(d->medium->sigma_s[0], d->medium->sigma_s[1], d->medium->sigma_s[2]);
+    S->sig_t_max = max_component(S->sig_a + S->sig_s);
+  }
+  return S;
+}
+
+// ================================================================ integrator
+struct PathCtx {
+  const Scene *S;
+  const pt_job_desc *job;
+  uint64_t key;
+  uint32_t halton_index;
+  int pixel, k;
+};
+
+static float dim_value(const PathCtx &P, int dim) {
+  const pt_job_desc &j = *P.job;
+  if (j.sampler == PT_SAMPLER_STRATIFIED) {
+    const uint32_t Sn = (uint32_t)(j.spp_x * j.spp_y);
+    uint32_t h = (uint32_t)mix_bits(((uint64_t)P.pixel << 20) ^ ((uint64_t)dim << 8) ^ j.seed);
+    uint32_t stratum = (uint32_t)permutation_element((uint32_t)P.k, Sn, h);
+    float jit = rand01(P.key, 4096u + (uint32_t)dim);
+    return std::min(((float)stratum + jit) / (float)Sn, (float)0x1.fffffep-1);
+  }
+  return halton_sample(j.sampler, j.sampler_seed, dim, P.halton_index);
+}
+
+static float power_heuristic(float nf, float fpdf, float ng, float gpdf) {  // maxdepth_mis.hpp:10-15
+  float f = nf * fpdf, g = ng * gpdf;
+  if (std::isinf(f)) return 1.f;
+  float f2 = f * f, g2 = g * g;
+  return (f2 + g2) > 0.f ? f2 / (f2 + g2) : 0.f;
+}
+
+struct LightSample {
+  bool valid = false;
+  V wl, Le;
+  float tmax = 0, pdf = 0, G = 0, NoI = 0, NoL = 0, d2 = 0;
+  bool env = false;
+};
+
+// One NEE light sample (maxdepth_nee.hpp:94-210) at shading point x with
+// normal n.  surface: NoI weights G; in a medium (surface=false) G = NoL/d2.
+static LightSample sample_light(const PathCtx &P, V x, V n, int bounce, int ls, bool surface) {
+  const Scene &S = *P.S;
+  const pt_job_desc &j = *P.job;
+  const uint32_t rbase = 64u + 32u * (uint32_t)bounce;
+  const int si = ls / j.light_samples_y, sj = ls % j.light_samples_y;
+  float ox = ((float)si + rand01(P.key, rbase + 2u * ls)) / (float)j.light_samples_x;
+  float oy = ((float)sj + rand01(P.key, rbase + 2u * ls + 1u)) / (float)j.light_samples_y;
+  const int nl = (int)S.lights.size();
+  int li = (int)(rand01(P.key, rbase + 20u + ls) * nl) % nl;
+  const Light &L = S.lights[li];
+  LightSample r;
+  if (L.type == 2) {
+    float pdir;
+    if (j.env_sampling == PT_ENV_ALIAS) {
+      r.wl = S.env_alias_sample(ox, oy, rand01(P.key, rbase + 28u + ls), pdir);
+    } else {  // uniformSampleSphere * 1e5 (random.hpp:7-15, envLight.hpp:26-43)
+      float z = 1.0f - 2.0f * ox;
+      float rr = std::sqrt(std::max(0.f, 1.f - z * z));
+      float phi = (float)(2.0f * PI * oy);
+      V pinf = V(rr * std::cos(phi), rr * std::sin(phi), z) * 1e5f;
+      r.wl = (pinf - x).normalize();
+      pdir = (float)(1.f / (4.f * PI));
+    }
+    r.env = true;
+    r.tmax = std::numeric_limits<float>::max();
+    r.pdf = pdir / (float)nl;
+    r.NoI = surface ? std::max(0.f, dot(n, r.wl)) : 1.f;
+    r.G = r.NoI;
+    r.Le = S.env_le(r.wl);
+    r.valid = r.pdf > 1e-7f;
+    return r;
+  }
+  V lp, ln;
+  if (L.type == 0) {  // QuadLight::get_sample / get_normal_at
+    lp = L.v0 + ox * L.e1 + oy * L.e2;
+    ln = L.normal;
+  } else {  // SphereLight::get_sample
+    float theta = (float)(2 * PI * ox);
+    float phi = std::acos(2 * oy - 1);
+    lp = L.c + L.radius * V(std::sin(phi) * std::cos(theta), std::sin(phi) * std::sin(theta), std::cos(phi));
+    ln = (lp - L.c).normalize();
+  }
+  V ld = lp - x;
+  float len = ld.length();
+  r.wl = ld.normalize();
+  r.valid = len >= 0.001f;
+  r.tmax = len - 0.001f;
+  r.pdf = (L.area <= 1e-7f) ? 0.f : 1.f / (L.area * (float)nl);
+  r.NoI = surface ? std::max(0.f, dot(n, r.wl)) : 1.f;
+  r.NoL = std::max(0.f, dot(ln, -r.wl));
+  r.d2 = len * len;
+  r.G = (r.d2 < 1e-7f) ? 0.f : r.NoL * r.NoI / r.d2;
+  r.Le = (dot(ln, -r.wl) > 0.0f) ? L.color * L.intensity : V(0.f);
+  if (!(r.pdf > 1e-7f)) r.valid = false;
+  return r;
+}
+
+// REF_NEE: getRayColor of maxdepth_nee.hpp:9-256, recursive, for scenes
+// without a medium.
+static V ray_color_ref(const PathCtx &P, V o, V d, int depth, int bounce) {
+  const Scene &S = *P.S;
+  const pt_job_desc &j = *P.job;
+  if (depth == 0) return V(0.f);
+  Hit rec;
+  if (!S.intersect(o, d, rec)) {
+    if (S.has_env) return S.env_le(d.normalize());
+    return S.bg;
+  }
+  const Material &M = S.mats[rec.mat];
+  const int dim0 = 3 * bounce;
+  float uc = dim_value(P, dim0), u0 = dim_value(P, dim0 + 1), u1 = dim_value(P, dim0 + 2);
+  Scatter s;
+  if (!mat_scatter(M, d, rec, s, uc, u0, u1)) return mat_emit(M, d, rec);
+  bool hr = s.spec_r(), ht = s.spec_t();
+  if (hr && ht) {  // split ray: both children weighted R and T
+    float R = s.pdf_val, T = 1.0f - R;
+    V wo = -d.normalize();
+    V sum(0.0f);
+    for (int b = 0; b < 2; ++b) {
+      V wi = b == 0 ? reflect_p(wo, rec.normal) : -wo;
+      sum += (b == 0 ? R : T) * ray_color_ref(P, rec.position, wi, depth - 1, bounce + 1);
+    }
+    return mat_emit(M, d, rec) + sum;
+  }
+  if (hr || ht) return mat_emit(M, d, rec) + s.att * ray_color_ref(P, rec.position, s.dir, depth - 1, bounce + 1);
+  V wo = -d.normalize();
+  V wi = s.dir.normalize();
+  float cos_t = std::abs(dot(rec.normal, wi));
+  V light_term(0.f);
+  const int LN = j.light_samples_x * j.light_samples_y;
+  if (!S.lights.empty() && LN > 0) {
+    for (int ls = 0; ls < LN; ++ls) {
+      LightSample L = sample_light(P, rec.position, rec.normal, bounce, ls, true);
+      float V_ = 0.f;
+      if (L.valid) {
+        Hit sh;
+        V_ = S.intersect(rec.position, L.wl, sh, 0.001f, L.tmax) ? 0.f : 1.f;
+      }
+      if (V_ > 0.f && L.pdf > 1e-7f) light_term += mat_f(M, wo, L.wl, rec) * L.Le * L.G / L.pdf;
+    }
+    light_term = light_term / (float)LN;
+  }
+  if (depth - 1 == 0) return mat_emit(M, d, rec) + light_term;
+  Hit next;
+  bool nh = S.intersect(rec.position, wi, next);
+  if (nh && S.mats[next.mat].type == PT_MAT_DIFFUSE_EMITTER) return mat_emit(M, d, rec) + light_term;
+  V att = s.att;
+  if (j.rr_start >= 0 && bounce >= j.rr_start) {  // roulette_naive.hpp:35-38 on the continuation
+    float q = std::clamp(max_component(s.att), 0.5f, 1.0f);
+    if (rand01(P.key, 64u + 32u * (uint32_t)bounce + 31u) > q) return mat_emit(M, d, rec) + light_term;
+    att = att / q;
+  }
+  return mat_emit(M, d, rec) + light_term +
+         att * ray_color_ref(P, rec.position, wi, depth - 1, bounce + 1) * cos_t / s.pdf_val;
+}
+
+// The build's iterative estimator: REF_NEE semantics or NEE+MIS, with the
+// homogeneous medium and Russian roulette extensions.
+static V ray_color_iter(const PathCtx &P, V o, V d) {
+  const Scene &S = *P.S;
+  const pt_job_desc &j = *P.job;
+  const bool mis = j.estimator == PT_EST_NEE_MIS;
+  const int LN = j.light_samples_x * j.light_samples_y;
+  const int limit = mis ? j.max_depth + 1 : j.max_depth;
+  V L(0.f), beta(1.f);
+  float prev_pdf = -1.f;
+  const int dpb = S.medium ? 4 : 3;
+  for (int bounce = 0; bounce < limit; ++bounce) {
+    Hit rec;
+    bool hit = S.intersect(o, d, rec);
+    const uint32_t rbase = 64u + 32u * (uint32_t)bounce;
+    bool in_medium = false;
+    float t_s = 0.f;
+    if (S.medium && bounce < j.max_depth) {
+      float uf = dim_value(P, dpb * bounce);
+      t_s = -std::log(1 - uf) / S.sig_t_max;
+      in_medium = t_s < (hit ? rec.t : std::numeric_limits<float>::infinity());
+    } else if (S.medium && bounce >= j.max_depth) {
+      // the extra MIS bounce only looks for emission along the segment: the
+      // medium transmittance weights it
+      float tt = hit ? rec.t : std::numeric_limits<float>::infinity();
+      beta = beta * V(std::exp(-S.sig_t_max * tt));
+    }
+    if (in_medium) {
+      // medium scattering vertex (extension): weight sigma_s / sigma_t
+      V x = o + t_s * d.normalize();
+      beta = beta * (S.sig_s / (S.sig_a + S.sig_s));
+      const float phase = (float)(1.0 / (4.0 * PI));
+      for (int ls = 0; ls < LN && !S.lights.empty(); ++ls) {
+        LightSample Ls = sample_light(P, x, V(0, 0, 1), bounce, ls, false);
+        if (!Ls.valid || Ls.env) continue;
+        float pl = Ls.pdf;
+        float G = Ls.G;
+        if (mis && Ls.NoL > 0.f) {
+          pl = Ls.pdf * Ls.d2 / Ls.NoL;
+          G = 1.f;
+        }
+        if (G <= 0.f) continue;
+        Hit sh;
+        if (S.intersect(x, Ls.wl, sh, 0.001f, Ls.tmax)) continue;
+        float w = mis ? power_heuristic((float)LN, pl, 1.f, phase) : 1.f;
+        float tr = std::exp(-S.sig_t_max * std::sqrt(Ls.d2));
+        L += beta * Ls.Le * (phase * G / pl * w * tr / (float)LN);
+      }
+      float u0 = dim_value(P, dpb * bounce + 2), u1 = dim_value(P, dpb * bounce + 3);
+      float z = 1.f - 2.f * u0, rr = std::sqrt(std::max(0.f, 1.f - z * z));
+      float ph = (float)(2 * PI * u1);
+      o = x;
+      d = V(rr * std::cos(ph), rr * std::sin(ph), z);
+      prev_pdf = phase;
+      if (bounce + 1 >= limit) break;
+      continue;
+    }
+    if (!hit) {
+      if (S.has_env) {
+        float w = 1.f;
+        if (mis && prev_pdf >= 0.f) {
+          float pl = j.env_sampling == PT_ENV_ALIAS ? S.env_alias_pdf(d) : (float)(1.0 / (4.0 * PI));
+          w = power_heuristic(1.f, prev_pdf, (float)LN, pl / (float)S.lights.size());
+        }
+        L += beta * S.env_le(d.normalize()) * w;
+      } else {
+        L += beta * S.bg;
+      }
+      break;
+    }
+    const Material &M = S.mats[rec.mat];
+    if (M.type == PT_MAT_DIFFUSE_EMITTER) {
+      if (prev_pdf < 0.f) {
+        L += beta * mat_emit(M, d, rec);
+      } else if (mis) {
+        if (rec.light >= 0) {
+          const Light &Lt = S.lights[rec.light];
+          V ln = Lt.type == 0 ? Lt.normal : (rec.position - Lt.c).normalize();
+          float cl = dot(ln, -d.normalize());
+          if (cl > 0.f) {
+            float pl = rec.t * rec.t / (cl * Lt.area * (float)S.lights.size());
+            L += beta * Lt.color * Lt.intensity * power_heuristic(1.f, prev_pdf, (float)LN, pl);
+          }
+        } else {
+          L += beta * mat_emit(M, d, rec);
+        }
+      }
+      break;
+    }
+    if (bounce >= j.max_depth) break;
+    const int dim0 = dpb * bounce + (S.medium ? 1 : 0);
+    float uc = dim_value(P, dim0), u0 = dim_value(P, dim0 + 1), u1 = dim_value(P, dim0 + 2);
+    Scatter s;
+    V wo = -d.normalize();
+    bool ok = mat_scatter(M, d, rec, s, uc, u0, u1);
+    const bool hr = s.spec_r(), ht = s.spec_t();
+    if (ok && (hr || ht)) {
+      if (bounce + 1 >= limit) break;
+      V wi = s.dir;
+      if (hr && ht) wi = (uc < s.pdf_val) ? reflect_p(wo, rec.normal).normalize() : -wo;
+      beta = beta * ((hr && ht) ? V(1.f) : s.att);
+      prev_pdf = -1.f;
+      o = rec.position;
+      d = wi;
+      continue;
+    }
+    if (!ok && !mis) break;
+    if (!S.lights.empty()) {
+      V lt(0.f);
+      for (int ls = 0; ls < LN; ++ls) {
+        LightSample Ls = sample_light(P, rec.position, rec.normal, bounce, ls, true);
+        if (!Ls.valid) continue;
+        float pl = Ls.pdf, G = Ls.G;
+        if (mis && !Ls.env && Ls.NoL > 0.f) {
+          pl = Ls.pdf * Ls.d2 / Ls.NoL;
+          G = Ls.NoI;
+        }
+        if (G <= 0.f) continue;
+        V f = mat_f(M, wo, Ls.wl, rec);
+        float w = mis ? power_heuristic((float)LN, pl, 1.f, mat_pdf(M, wo, Ls.wl, rec)) : 1.f;
+        V c = f * Ls.Le * (G / pl * w / (float)LN);
+        if (c.x == 0.f && c.y == 0.f && c.z == 0.f) continue;
+        Hit sh;
+        if (S.intersect(rec.position, Ls.wl, sh, 0.001f, Ls.tmax)) continue;
+        float tr = S.medium ? (Ls.env ? 0.f : std::exp(-S.sig_t_max * std::sqrt(Ls.d2))) : 1.f;
+        lt += beta * c * tr;
+      }
+      L += lt;
+    }
+    if (!ok || bounce + 1 >= limit) break;
+    V wi = s.dir.normalize();
+    float c = std::abs(dot(rec.normal, wi));
+    V nb = beta * s.att * (c / s.pdf_val);
+    if (j.rr_start >= 0 && bounce >= j.rr_start) {
+      float q = std::clamp(max_component(s.att), 0.5f, 1.0f);
+      if (rand01(P.key, rbase + 31u) > q) break;
+      nb = nb / q;
+    }
+    beta = nb;
+    prev_pdf = s.pdf_val;
+    o = rec.position;
+    d = wi;
+  }
+  return L;
+}
+
+// Camera + pixel offsets: PerspectiveCamera (camera.cpp:7-56) and
+// FrameBuffer::setOffsets (framebuffer.cpp:131-145) with the build's RNG.
+struct Camera {
+  V pos, bl, hor, ver, hv, vv;
+  float r;
+  explicit Camera(const pt_camera_desc &c) {
+    float h = std::tan(c.fov / 2.f);
+    float ph = 1.0f * h * 2.0f, pw = ph * c.aspect;
+    V up(c.up[0], c.up[1], c.up[2]), front(c.front[0], c.front[1], c.front[2]);
+    pos = V(c.position[0], c.position[1], c.position[2]);
+    V lookat = -front.normalize();
+    hv = cross(up, lookat).normalize();
+    vv = cross(lookat, hv).normalize();
+    hor = hv * pw * c.focal_dist;
+    ver = vv * ph * c.focal_dist;
+    bl = pos - hor / 2.0f - ver / 2.0f;
+    bl = bl - lookat * c.focal_dist;
+    r = c.focal_dist / c.aperture * 0.5f;
+  }
+};
+
+static std::vector<std::pair<float, float>> offsets(const pt_job_desc &j) {
+  std::vector<std::pair<float, float>> off;
+  const uint64_t key = path_key(j.seed ^ 0x5bd1e995u, 0xffffffffffull);
+  for (int i = 0; i < j.spp_x; ++i)
+    for (int k = 0; k < j.spp_y; ++k) {
+      const uint32_t s = (uint32_t)(i * j.spp_y + k);
+      float a = (float)i / (float)j.spp_x, b = (float)(i + 1) / (float)j.spp_x;
+      float c = (float)k / (float)j.spp_y, d = (float)(k + 1) / (float)j.spp_y;
+      off.push_back({a + (b - a) * rand01(key, 2 * s), c + (d - c) * rand01(key, 2 * s + 1)});
+    }
+  return off;
+}
+
+}  // namespace orc
+
+using namespace orc;
+
+extern "C" {
+
+void *or_scene_create(const pt_scene_desc *d) { return build_scene(d); }
+void or_scene_destroy(void *s) { delete static_cast<Scene *>(s); }
+int or_scene_num_lights(void *s) { return (int)static_cast<Scene *>(s)->lights.size(); }
+
+void or_sampler_eval(int strategy, uint32_t seed, uint32_t first, int n, int dims, float *out) {
+  for (int i = 0; i < n; ++i)
+    for (int d = 0; d < dims; ++d) out[(size_t)i * dims + d] = halton_sample(strategy, seed, d, first + (uint32_t)i);
+}
+
+void or_trace_closest(void *s, const float *rays, int n, float tmin, float tmax, float *t, int *prim) {
+  const Scene &S = *static_cast<Scene *>(s);
+  for (int i = 0; i < n; ++i) {
+    Hit rec;
+    V o(rays[6 * i], rays[6 * i + 1], rays[6 * i + 2]), d(rays[6 * i + 3], rays[6 * i + 4], rays[6 * i + 5]);
+    bool h = S.intersect(o, d, rec, tmin, tmax);
+    t[i] = h ? rec.t : std::numeric_limits<float>::max();
+    prim[i] = h ? rec.prim : -1;
+  }
+}
+
+void or_bsdf_eval(const pt_material_desc *md, int n, const float *wo, const float *wi, const float *nrm,
+                  const uint8_t *front, float *f, float *pdf) {
+  Material m = make_material(md->type, md->flags, md->p);
+  for (int i = 0; i < n; ++i) {
+    Hit rec;
+    rec.normal = V(nrm[3 * i], nrm[3 * i + 1], nrm[3 * i + 2]);
+    rec.is_inside = front[i] != 0;
+    V o(wo[3 * i], wo[3 * i + 1], wo[3 * i + 2]), w(wi[3 * i], wi[3 * i + 1], wi[3 * i + 2]);
+    V fv = mat_f(m, o, w, rec);
+    f[3 * i] = fv.x;
+    f[3 * i + 1] = fv.y;
+    f[3 * i + 2] = fv.z;
+    pdf[i] = mat_pdf(m, o, w, rec);
+  }
+}
+
+void or_bsdf_sample(const pt_material_desc *md, int n, const float *wo, const float *nrm, const uint8_t *front,
+                    const float *uc, const float *u, uint8_t *ok, float *wi, float *att, float *pdf, uint32_t *ty) {
+  Material m = make_material(md->type, md->flags, md->p);
+  for (int i = 0; i < n; ++i) {
+    Hit rec;
+    rec.normal = V(nrm[3 * i], nrm[3 * i + 1], nrm[3 * i + 2]);
+    rec.is_inside = front[i] != 0;
+    Scatter s;
+    V o(wo[3 * i], wo[3 * i + 1], wo[3 * i + 2]);
+    bool r = mat_scatter(m, -o, rec, s, uc[i], u[2 * i], u[2 * i + 1]);
+    ok[i] = r;
+    for (int c = 0; c < 3; ++c) {
+      wi[3 * i + c] = r ? s.dir[c] : 0.f;
+      att[3 * i + c] = r ? s.att[c] : 0.f;
+    }
+    pdf[i] = r ? s.pdf_val : 0.f;
+    ty[i] = r ? s.type : 0u;
+  }
+}
+
+// Renders the job; mean/var are width*height*3, [j][i][c].  recursive != 0
+// selects the recursive REF_NEE restatement (scenes without a medium).
+int or_render(void *s, const pt_job_desc *job, float *mean, float *var, int threads, int recursive) {
+  const Scene &S = *static_cast<Scene *>(s);
+  const pt_job_desc &j = *job;
+  Camera cam(j.camera);
+  auto off = offsets(j);
+  const int W = j.width, H = j.height, Sn = j.spp_x * j.spp_y;
+  const int b = j.spp_begin, e = j.spp_end ? j.spp_end : Sn;
+  if (threads <= 0) threads = (int)std::max(1u, std::thread::hardware_concurrency());
+  const bool use_rec = recursive && !S.medium && j.estimator == PT_EST_REF_NEE;
+  std::atomic<int> next_col{0};
+  auto worker = [&]() {
+    for (int i = next_col++; i < W; i = next_col++) {
+      for (int jj = 0; jj < H; ++jj) {
+        double sum[3] = {0, 0, 0}, sq[3] = {0, 0, 0};
+        for (int k = b; k < e; ++k) {
+          uint64_t lin = ((uint64_t)i * H + jj) * (uint64_t)Sn + k;
+          PathCtx P{&S, &j, path_key(j.seed, lin), (uint32_t)(lin + 1u), jj * W + i, k};
+          float u = ((float)i + off[k].first) / (float)W, v = ((float)jj + off[k].second) / (float)H;
+          float lx = -cam.r + (cam.r - -cam.r) * rand01(P.key, 1u);
+          float ly = -cam.r + (cam.r - -cam.r) * rand01(P.key, 2u);
+          V ps = cam.pos + (cam.hv * lx + cam.vv * ly);
+          V dir = (cam.bl + u * cam.hor + v * cam.ver - ps).normalize();
+          V c = use_rec ? ray_color_ref(P, ps, dir, j.max_depth, 0) : ray_color_iter(P, ps, dir);
+          for (int ch = 0; ch < 3; ++ch) {
+            sum[ch] += c[ch];
+            sq[ch] += (double)c[ch] * c[ch];
+          }
+        }
+        const int n = e - b;
+        for (int ch = 0; ch < 3; ++ch) {
+          double m = sum[ch] / n;
+          mean[(jj * W + i) * 3 + ch] = (float)m;
+          if (var) var[(jj * W + i) * 3 + ch] = (float)(n > 1 ? (sq[ch] - n * m * m) / (n - 1) : 0.0);
+        }
+      }
+    }
+  };
+  std::vector<std::thread> pool;
+  for (int t = 0; t < threads; ++t) pool.emplace_back(worker);
+  for (auto &t : pool) t.join();
+  return 0;
+}
+
+}  // extern "C"

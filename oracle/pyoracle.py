@@ -1,0 +1,109 @@
+"""Python binding of the CPU oracle (oracle/pt_oracle.cpp).
+
+ORACLE: test infrastructure.  Only tests/, __graft_entry__.smoke() and the
+CPU-baseline leg of bench.py use it, as the checker of the CUDA path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from pathtracer_gb300 import native as N
+
+from .build_oracle import OUT, build
+
+f32p = C.POINTER(C.c_float)
+i32p = C.POINTER(C.c_int32)
+u8p = C.POINTER(C.c_uint8)
+u32p = C.POINTER(C.c_uint32)
+
+_lib = None
+
+
+def load():
+    global _lib
+    if _lib is None:
+        if not OUT.exists():
+            build()
+        lib = C.CDLL(str(OUT))
+        lib.or_scene_create.argtypes = [C.POINTER(N.SceneDesc)]
+        lib.or_scene_create.restype = C.c_void_p
+        lib.or_scene_destroy.argtypes = [C.c_void_p]
+        lib.or_scene_num_lights.argtypes = [C.c_void_p]
+        lib.or_sampler_eval.argtypes = [C.c_int, C.c_uint32, C.c_uint32, C.c_int, C.c_int, f32p]
+        lib.or_trace_closest.argtypes = [C.c_void_p, f32p, C.c_int, C.c_float, C.c_float, f32p, i32p]
+        lib.or_bsdf_eval.argtypes = [C.POINTER(N.MaterialDesc), C.c_int, f32p, f32p, f32p, u8p, f32p, f32p]
+        lib.or_bsdf_sample.argtypes = [C.POINTER(N.MaterialDesc), C.c_int, f32p, f32p, u8p, f32p, f32p, u8p, f32p,
+                                       f32p, f32p, u32p]
+        lib.or_render.argtypes = [C.c_void_p, C.POINTER(N.JobDesc), f32p, f32p, C.c_int, C.c_int]
+        _lib = lib
+    return _lib
+
+
+def _p(a, t):
+    return a.ctypes.data_as(C.POINTER(t))
+
+
+class OracleScene:
+    def __init__(self, scene):
+        self.lib = load()
+        self.sb = N.make_scene_desc(scene)
+        self.h = self.lib.or_scene_create(C.byref(self.sb.desc))
+
+    def __del__(self):
+        try:
+            self.lib.or_scene_destroy(self.h)
+        except Exception:
+            pass
+
+    def trace_closest(self, rays, tmin=1e-4, tmax=1e5):
+        rays = np.ascontiguousarray(rays, np.float32)
+        n = rays.shape[0]
+        t = np.zeros(n, np.float32)
+        prim = np.zeros(n, np.int32)
+        self.lib.or_trace_closest(self.h, _p(rays, C.c_float), n, tmin, tmax, _p(t, C.c_float), _p(prim, C.c_int32))
+        return t, prim
+
+    def render(self, job, threads=0, recursive=True):
+        mean = np.zeros((job.height, job.width, 3), np.float32)
+        var = np.zeros_like(mean)
+        self.lib.or_render(self.h, C.byref(job), _p(mean, C.c_float), _p(var, C.c_float), threads,
+                           1 if recursive else 0)
+        return mean, var
+
+
+def render(scene, job, threads=0, recursive=True):
+    return OracleScene(scene).render(job, threads, recursive)
+
+
+def sampler_eval(strategy, first_index, n, dims, seed=0):
+    out = np.zeros((n, dims), np.float32)
+    load().or_sampler_eval(strategy, seed, first_index, n, dims, _p(out, C.c_float))
+    return out
+
+
+def bsdf_eval(mat, wo, wi, nrm, front):
+    wo, wi, nrm = (np.ascontiguousarray(a, np.float32) for a in (wo, wi, nrm))
+    front = np.ascontiguousarray(front, np.uint8)
+    n = wo.shape[0]
+    f = np.zeros((n, 3), np.float32)
+    pdf = np.zeros(n, np.float32)
+    load().or_bsdf_eval(C.byref(mat), n, _p(wo, C.c_float), _p(wi, C.c_float), _p(nrm, C.c_float),
+                        _p(front, C.c_uint8), _p(f, C.c_float), _p(pdf, C.c_float))
+    return f, pdf
+
+
+def bsdf_sample(mat, wo, nrm, front, uc, u):
+    wo, nrm, uc, u = (np.ascontiguousarray(a, np.float32) for a in (wo, nrm, uc, u))
+    front = np.ascontiguousarray(front, np.uint8)
+    n = wo.shape[0]
+    ok = np.zeros(n, np.uint8)
+    wi = np.zeros((n, 3), np.float32)
+    att = np.zeros((n, 3), np.float32)
+    pdf = np.zeros(n, np.float32)
+    ty = np.zeros(n, np.uint32)
+    load().or_bsdf_sample(C.byref(mat), n, _p(wo, C.c_float), _p(nrm, C.c_float), _p(front, C.c_uint8),
+                          _p(uc, C.c_float), _p(u, C.c_float), _p(ok, C.c_uint8), _p(wi, C.c_float),
+                          _p(att, C.c_float), _p(pdf, C.c_float), _p(ty, C.c_uint32))
+    return ok, wi, att, pdf, ty

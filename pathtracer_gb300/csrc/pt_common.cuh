@@ -1,0 +1,291 @@
+// pt_common.cuh -- vector math, counter-based RNG and the Halton-family
+// samplers shared by every kernel of the wavefront path integrator.
+//
+// Host+device functions.  Where the reference's result must be reproduced
+// bit for bit (sampler sequences, ray/primitive tests) the arithmetic is
+// written with explicitly rounded operations so that no multiply-add is
+// contracted; everywhere else ordinary float arithmetic (FMA allowed) is used
+// and parity is held to the 1e-4 relative bar of the BSDF tests.
+#pragma once
+#include <cstdint>
+#include <cfloat>
+#include <cmath>
+#include <cstring>
+
+#if defined(__CUDACC__)
+#define PT_HD __host__ __device__ __forceinline__
+#else
+#define PT_HD inline
+#endif
+
+#ifndef PT_PI
+#define PT_PI 3.14159265358979323846
+#endif
+#define PT_INV_PI_F 0.318309886183790671538f
+
+namespace pt {
+
+#if !defined(__CUDACC__)
+using std::isinf;
+#endif
+
+// ------------------------------------------------------ exact arithmetic
+// Rounded single-precision operations that are never fused.
+#if defined(__CUDA_ARCH__)
+PT_HD float xmul(float a, float b) { return __fmul_rn(a, b); }
+PT_HD float xadd(float a, float b) { return __fadd_rn(a, b); }
+PT_HD float xsub(float a, float b) { return __fsub_rn(a, b); }
+PT_HD float xdiv(float a, float b) { return __fdiv_rn(a, b); }
+PT_HD float xsqrt(float a) { return __fsqrt_rn(a); }
+PT_HD double xdmul(double a, double b) { return __dmul_rn(a, b); }
+#else
+PT_HD float xmul(float a, float b) { return a * b; }
+PT_HD float xadd(float a, float b) { return a + b; }
+PT_HD float xsub(float a, float b) { return a - b; }
+PT_HD float xdiv(float a, float b) { return a / b; }
+PT_HD float xsqrt(float a) { return std::sqrt(a); }
+PT_HD double xdmul(double a, double b) { return a * b; }
+#endif
+
+// sin/cos of pi*x and of x (device intrinsics; libm on the host).
+PT_HD void sincospi_(float x, float *s, float *c) {
+#if defined(__CUDA_ARCH__)
+  sincospif(x, s, c);
+#else
+  *s = sinf(x * (float)PT_PI);
+  *c = cosf(x * (float)PT_PI);
+#endif
+}
+PT_HD void sincos_(float x, float *s, float *c) {
+#if defined(__CUDA_ARCH__)
+  sincosf(x, s, c);
+#else
+  *s = sinf(x);
+  *c = cosf(x);
+#endif
+}
+
+PT_HD uint32_t f2u(float f) {
+#if defined(__CUDA_ARCH__)
+  return __float_as_uint(f);
+#else
+  uint32_t u;
+  std::memcpy(&u, &f, 4);
+  return u;
+#endif
+}
+PT_HD float u2f(uint32_t u) {
+#if defined(__CUDA_ARCH__)
+  return __uint_as_float(u);
+#else
+  float f;
+  std::memcpy(&f, &u, 4);
+  return f;
+#endif
+}
+
+// ------------------------------------------------------------ float3
+struct V3 {
+  float x, y, z;
+};
+PT_HD V3 v3(float x, float y, float z) { return V3{x, y, z}; }
+PT_HD V3 v3(float s) { return V3{s, s, s}; }
+PT_HD V3 operator+(V3 a, V3 b) { return V3{a.x + b.x, a.y + b.y, a.z + b.z}; }
+PT_HD V3 operator-(V3 a, V3 b) { return V3{a.x - b.x, a.y - b.y, a.z - b.z}; }
+PT_HD V3 operator-(V3 a) { return V3{-a.x, -a.y, -a.z}; }
+PT_HD V3 operator*(V3 a, float s) { return V3{a.x * s, a.y * s, a.z * s}; }
+PT_HD V3 operator*(float s, V3 a) { return V3{a.x * s, a.y * s, a.z * s}; }
+PT_HD V3 operator*(V3 a, V3 b) { return V3{a.x * b.x, a.y * b.y, a.z * b.z}; }
+PT_HD V3 operator/(V3 a, float s) { return V3{a.x / s, a.y / s, a.z / s}; }
+PT_HD V3 operator/(V3 a, V3 b) { return V3{a.x / b.x, a.y / b.y, a.z / b.z}; }
+PT_HD V3 &operator+=(V3 &a, V3 b) { a = a + b; return a; }
+PT_HD V3 &operator*=(V3 &a, V3 b) { a = a * b; return a; }
+PT_HD V3 &operator*=(V3 &a, float s) { a = a * s; return a; }
+PT_HD float dot(V3 a, V3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+PT_HD V3 cross(V3 a, V3 b) {
+  return V3{a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+PT_HD float length(V3 a) { return sqrtf(dot(a, a)); }
+// gl::vec::normalize (matrix.hpp:337-343): each component divided by the length.
+PT_HD V3 normalize(V3 a) {
+  float l = length(a);
+  return V3{a.x / l, a.y / l, a.z / l};
+}
+PT_HD float max_comp(V3 a) { return fmaxf(a.x, fmaxf(a.y, a.z)); }
+PT_HD bool near_zero(V3 a) { return fabsf(a.x) < 1e-6f && fabsf(a.y) < 1e-6f && fabsf(a.z) < 1e-6f; }
+
+// Exact (never fused) forms in the reference's operation order:
+// dot = ((0 + a0*b0) + a1*b1) + a2*b2 (matrix.hpp:553-559),
+// cross = a1*b2 - a2*b1 ... (matrix.hpp:571-579).
+PT_HD float xdot(V3 a, V3 b) {
+  return xadd(xadd(xmul(a.x, b.x), xmul(a.y, b.y)), xmul(a.z, b.z));
+}
+PT_HD V3 xcross(V3 a, V3 b) {
+  return V3{xsub(xmul(a.y, b.z), xmul(a.z, b.y)), xsub(xmul(a.z, b.x), xmul(a.x, b.z)),
+            xsub(xmul(a.x, b.y), xmul(a.y, b.x))};
+}
+PT_HD V3 xsubv(V3 a, V3 b) { return V3{xsub(a.x, b.x), xsub(a.y, b.y), xsub(a.z, b.z)}; }
+PT_HD V3 xnormalize(V3 a) {
+  float l = xsqrt(xdot(a, a));
+  return V3{xdiv(a.x, l), xdiv(a.y, l), xdiv(a.z, l)};
+}
+// o + t*d with each product rounded before the add (Ray::at, ray.hpp:21).
+PT_HD V3 xat(V3 o, V3 d, float t) {
+  return V3{xadd(o.x, xmul(t, d.x)), xadd(o.y, xmul(t, d.y)), xadd(o.z, xmul(t, d.z))};
+}
+
+// Orthonormal basis around n (OrthoBasis, utils/orthoBasis.hpp:15-36).
+struct Onb {
+  V3 u, v, w;
+};
+PT_HD Onb make_onb(V3 n) {
+  Onb b;
+  b.w = normalize(n);
+  V3 a = (fabsf(n.x) > 0.9f) ? v3(0.f, 1.f, 0.f) : v3(1.f, 0.f, 0.f);
+  b.v = normalize(cross(b.w, a));
+  b.u = cross(b.w, b.v);
+  return b;
+}
+PT_HD V3 to_world(const Onb &b, V3 l) { return l.x * b.u + l.y * b.v + l.z * b.w; }
+PT_HD V3 to_local(const Onb &b, V3 v) { return V3{dot(v, b.u), dot(v, b.v), dot(v, b.w)}; }
+
+// ------------------------------------------------------------ hashing
+// pbrt::mixBits (utils/hash.hpp:62-69): 64-bit finalizer of
+// zimbry.blogspot.ch/2011/09 (variant 13 of Stafford's mixers).
+PT_HD uint64_t mix_bits(uint64_t v) {
+  v ^= (v >> 31);
+  v *= 0x7fb5d329728ea185ull;
+  v ^= (v >> 27);
+  v *= 0x81dadef4bc2dd44dull;
+  v ^= (v >> 33);
+  return v;
+}
+
+// gl::permutationElement (utils/utility.hpp:434-464): Kensler's hashed
+// permutation of [0, l) ("Correlated Multi-Jittered Sampling", 2013).
+PT_HD uint32_t permutation_element(uint32_t i, uint32_t l, uint32_t p) {
+  uint32_t w = l - 1;
+  w |= w >> 1;
+  w |= w >> 2;
+  w |= w >> 4;
+  w |= w >> 8;
+  w |= w >> 16;
+  do {
+    i ^= p;
+    i *= 0xe170893du;
+    i ^= p >> 16;
+    i ^= (i & w) >> 4;
+    i ^= p >> 8;
+    i *= 0x0929eb3fu;
+    i ^= p >> 23;
+    i ^= (i & w) >> 1;
+    i *= 1u | p >> 27;
+    i *= 0x6935fa69u;
+    i ^= (i & w) >> 11;
+    i *= 0x74dcb303u;
+    i ^= (i & w) >> 2;
+    i *= 0x9e501cc3u;
+    i ^= (i & w) >> 2;
+    i *= 0xc860a3dfu;
+    i &= w;
+    i ^= i >> 5;
+  } while (i >= l);
+  return (i + p) % l;
+}
+
+// Counter-based uniform draws for everything the reference takes from
+// gl::rand_num() (pixel-offset grid, lens, light pick, light-point jitter,
+// Russian roulette).  SplitMix64's output function (Steele, Lea, Flood,
+// OOPSLA 2014) over key ^ slot*golden; 24 high bits -> [0, 1).
+PT_HD uint64_t splitmix64(uint64_t z) {
+  z += 0x9e3779b97f4a7c15ull;
+  z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+  z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+  return z ^ (z >> 31);
+}
+PT_HD float rand01(uint64_t key, uint32_t slot) {
+  uint64_t h = splitmix64(key ^ ((uint64_t)slot * 0xd1b54a32d192ed03ull));
+  return (float)(h >> 40) * (1.0f / 16777216.0f);
+}
+PT_HD uint64_t path_key(uint32_t seed, uint64_t sample_id) {
+  return splitmix64(((uint64_t)seed << 40) ^ sample_id);
+}
+
+// ------------------------------------------------------------ samplers
+// Halton bases (gl::Primes, utility.hpp:400-402).  The reference indexes
+// Primes[dim] without a bound (digitPerm.hpp:101), which is undefined for
+// dim >= 25; this build defines it as Primes[dim % 25], the rule the
+// unscrambled radicalInverse already uses (utility.hpp:408).
+#define PT_PRIME_COUNT 25
+struct HaltonTables {
+  int32_t prime[PT_PRIME_COUNT];
+  int32_t ndigits[PT_PRIME_COUNT];    // digits visited by the double loop test
+  double inv_base_m[PT_PRIME_COUNT];  // invBase^ndigits, accumulated as the loop does
+  int32_t perm_offset[PT_PRIME_COUNT];// into perm[] (PermuteDigits tables)
+};
+
+// gl::radicalInverse (utility.hpp:406-420), float arithmetic.
+PT_HD float radical_inverse(const HaltonTables &T, int dim, uint64_t a) {
+  const int bi = dim % PT_PRIME_COUNT;
+  const uint32_t base = (uint32_t)T.prime[bi];
+  const float inv_base = xdiv(1.0f, (float)base);
+  float inv_base_m = 1.0f;
+  uint64_t rev = 0;
+  while (a) {
+    uint64_t next = a / base;
+    uint64_t digit = a - next * base;
+    rev = rev * base + digit;
+    inv_base_m = xmul(inv_base_m, inv_base);
+    a = next;
+  }
+  float r = xmul((float)rev, inv_base_m);
+  const float one_minus_eps = 0x1.fffffep-1f;
+  return r < one_minus_eps ? r : one_minus_eps;
+}
+
+PT_HD float clamp_to_float(double r) {
+  const double one_minus_eps = 0x1.fffffffffffffp-1;
+  return (float)(r < one_minus_eps ? r : one_minus_eps);
+}
+
+// gl::owenScrambledRadicalInverse (sampler/digitPerm.hpp:99-133) with the
+// hash HaltonSampler passes (sampler.hpp:69-71).  The sample index is a
+// uint32 in the reference, so the digit extraction runs on 32 bits.
+PT_HD float owen_radical_inverse(const HaltonTables &T, int dim, uint32_t index) {
+  const int bi = dim % PT_PRIME_COUNT;
+  const uint32_t base = (uint32_t)T.prime[bi];
+  const uint32_t hash = (uint32_t)mix_bits(1u + ((uint32_t)dim << 4));
+  uint32_t a = index;
+  uint64_t rev = 0;
+  const int nd = T.ndigits[bi];
+  for (int di = 0; di < nd; ++di) {
+    uint32_t next = a / base;
+    uint32_t digit = a - next * base;
+    uint32_t dh = (uint32_t)mix_bits(hash ^ (uint32_t)rev ^ ((uint32_t)di << 16));
+    digit = permutation_element(digit, base, dh);
+    rev = rev * base + digit;
+    a = next;
+  }
+  return clamp_to_float(xdmul(T.inv_base_m[bi], (double)rev));
+}
+
+// gl::scrambledRadicalInverse with DigitPermutation tables
+// (sampler/digitPerm.hpp:12-97); perm holds uint16 entries per base.
+PT_HD float permuted_radical_inverse(const HaltonTables &T, const uint16_t *perm, int dim,
+                                     uint32_t index) {
+  if (dim >= PT_PRIME_COUNT) return radical_inverse(T, dim, index);  // sampler.hpp:60-63
+  const uint32_t base = (uint32_t)T.prime[dim];
+  const uint16_t *p = perm + T.perm_offset[dim];
+  uint32_t a = index;
+  uint64_t rev = 0;
+  const int nd = T.ndigits[dim];
+  for (int di = 0; di < nd; ++di) {
+    uint32_t next = a / base;
+    uint32_t digit = a - next * base;
+    rev = rev * base + p[di * base + digit];
+    a = next;
+  }
+  return clamp_to_float(xdmul(T.inv_base_m[dim], (double)rev));
+}
+
+}  // namespace pt

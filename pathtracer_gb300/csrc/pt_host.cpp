@@ -1,0 +1,1235 @@
+// pt_host.cpp -- C-ABI of the GB300 path integrator (include/pathtracer_gb300.h):
+// scene flattening and BVH construction with the reference's split rules,
+// light discovery, device residency, the wave loop of pt_render, and the
+// batch test entry points.  No exception crosses the ABI.
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <numeric>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "pt_host.h"
+
+namespace pt {
+
+// ------------------------------------------------------------- errors
+static std::mutex g_err_mu;
+static std::string g_last_error;
+
+struct PtError : std::runtime_error {
+  int code;
+  PtError(int c, const std::string &m) : std::runtime_error(m), code(c) {}
+};
+
+void fail(int code, const std::string &msg) { throw PtError(code, msg); }
+void cuda_check(cudaError_t e, const char *what) {
+  if (e != cudaSuccess) fail(PT_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+// ------------------------------------------------------- Halton tables
+// gl::Primes (utility.hpp:400-402), digit counts and inverse radix powers
+// exactly as the double loop of owenScrambledRadicalInverse computes them
+// (digitPerm.hpp:105-128).
+HaltonTables make_halton_tables() {
+  static const int primes[PT_PRIME_COUNT] = {2,  3,  5,  7,  11, 13, 17, 19, 23, 29, 31, 37, 41,
+                                             43, 47, 53, 59, 61, 67, 71, 73, 79, 83, 89, 97};
+  HaltonTables T;
+  int off = 0;
+  for (int b = 0; b < PT_PRIME_COUNT; ++b) {
+    const int base = primes[b];
+    T.prime[b] = base;
+    const double inv_base = 1.0 / (double)base;
+    double inv_base_m = 1.0;
+    int nd = 0;
+    while (1.0 - (base - 1) * inv_base_m < 1.0) {
+      ++nd;
+      inv_base_m *= inv_base;
+    }
+    T.ndigits[b] = nd;
+    T.inv_base_m[b] = inv_base_m;
+    T.perm_offset[b] = off;
+    off += nd * base;
+  }
+  return T;
+}
+
+// MurmurHash64A (Austin Appleby, public domain), the byte hash that
+// pbrt::hash applies to its packed arguments (hash.hpp:10-58, 84-91).
+static uint64_t murmur64a(const unsigned char *key, size_t len, uint64_t seed) {
+  const uint64_t m = 0xc6a4a7935bd1e995ull;
+  const int r = 47;
+  uint64_t h = seed ^ (len * m);
+  const unsigned char *end = key + 8 * (len / 8);
+  for (; key != end; key += 8) {
+    uint64_t k;
+    std::memcpy(&k, key, 8);
+    k *= m;
+    k ^= k >> r;
+    k *= m;
+    h ^= k;
+    h *= m;
+  }
+  const size_t rem = len & 7;
+  for (size_t b = rem; b > 0; --b) h ^= uint64_t(key[b - 1]) << (8 * (b - 1));
+  if (rem) h *= m;
+  h ^= h >> r;
+  h *= m;
+  h ^= h >> r;
+  return h;
+}
+
+// DigitPermutation tables (digitPerm.hpp:14-39) for every base.
+std::vector<uint16_t> make_digit_permutations(const HaltonTables &T, uint32_t seed) {
+  size_t total = 0;
+  for (int b = 0; b < PT_PRIME_COUNT; ++b) total += (size_t)T.ndigits[b] * T.prime[b];
+  std::vector<uint16_t> perm(total);
+  for (int b = 0; b < PT_PRIME_COUNT; ++b) {
+    const int base = T.prime[b];
+    for (int di = 0; di < T.ndigits[b]; ++di) {
+      unsigned char buf[12];
+      int32_t bb = base, dd = di;
+      std::memcpy(buf, &bb, 4);
+      std::memcpy(buf + 4, &dd, 4);
+      std::memcpy(buf + 8, &seed, 4);
+      uint64_t dseed = murmur64a(buf, 12, 0);
+      for (int v = 0; v < base; ++v)
+        perm[T.perm_offset[b] + (size_t)di * base + v] =
+            (uint16_t)permutation_element((uint32_t)v, (uint32_t)base, (uint32_t)dseed);
+    }
+  }
+  return perm;
+}
+
+// ------------------------------------------------------------ materials
+MatRec derive_material(const pt_material_desc &m) {
+  MatRec r;
+  std::memset(&r, 0, sizeof r);
+  r.type = m.type;
+  r.flags = m.flags;
+  std::memcpy(r.p, m.p, sizeof r.p);
+  if (m.type < 0 || m.type >= PT_MAT_COUNT) fail(PT_ERR_INVALID, "unknown material type");
+  if (m.type == PT_MAT_DISNEY) {
+    // DisneyPrincipledBSDF ctor (disneyPrincipledBSDF.hpp:34-66)
+    const float st = m.p[3], metallic = m.p[4], sheen = m.p[10], cc = m.p[12];
+    r.d[0] = (1 - metallic) * (1 - st);
+    r.d[1] = (1 - st * (1 - metallic));
+    r.d[2] = (1 - metallic) * st;
+    r.d[3] = (float)(0.25 * cc);
+    r.d[4] = (1 - metallic) * sheen;
+    TR t = tr_from_roughness(m.p[7], m.p[9]);
+    r.d[5] = t.ax;
+    r.d[6] = t.ay;
+    const float g = m.p[13];
+    r.d[7] = (1.f - g) * 0.1f + g * 0.001f;  // ClearcoatTRD::fromClearcoatGloss
+  } else if (m.type == PT_MAT_HAIR) {
+    // HairMarschner ctor (hairMarsch.hpp:9-34)
+    const float bm = m.p[5], bn = m.p[6], alpha = m.p[7];
+    float v0 = sqr(0.726f * bm + 0.812f * sqr(bm) + 3.7f * std::pow(bm, 20.f));
+    r.d[0] = v0;
+    r.d[1] = (float)(.25 * v0);
+    r.d[2] = 4 * v0;
+    r.d[3] = r.d[2];
+    const float sqrt_pi_over8 = 0.626657069f;
+    r.d[4] = sqrt_pi_over8 * (0.265f * bn + 1.194f * sqr(bn) + 5.372f * std::pow(bn, 22.f));
+    float s2k[3], c2k[3];
+    s2k[0] = std::sin(alpha);
+    c2k[0] = safe_sqrt(1 - sqr(s2k[0]));
+    for (int i = 1; i < 3; ++i) {
+      s2k[i] = 2 * c2k[i - 1] * s2k[i - 1];
+      c2k[i] = sqr(c2k[i - 1]) - sqr(s2k[i - 1]);
+    }
+    for (int i = 0; i < 3; ++i) {
+      r.d[5 + i] = s2k[i];
+      r.d[8 + i] = c2k[i];
+    }
+    if (m.flags & PT_MAT_FLAG_MELANIN) {
+      // Absorption from melanin concentrations (d'Eon et al. 2011, as
+      // tabulated in pbrt-v3 HairBSDF::SigmaAFromConcentration): extension.
+      const float eu[3] = {0.419f, 0.697f, 1.37f}, ph[3] = {0.187f, 0.4f, 1.05f};
+      for (int c = 0; c < 3; ++c) r.d[11 + c] = m.p[8] * eu[c] + m.p[9] * ph[c];
+    } else {
+      for (int c = 0; c < 3; ++c) r.d[11 + c] = m.p[c];
+    }
+  }
+  return r;
+}
+
+// ---------------------------------------------------------------- scene
+struct Box {
+  float lo[3], hi[3];
+};
+static Box box_empty() {
+  Box b;
+  for (int a = 0; a < 3; ++a) {
+    b.lo[a] = INFINITY;
+    b.hi[a] = -INFINITY;
+  }
+  return b;
+}
+static Box box_merge(const Box &x, const Box &y) {
+  Box b;
+  for (int a = 0; a < 3; ++a) {
+    b.lo[a] = std::min(x.lo[a], y.lo[a]);
+    b.hi[a] = std::max(x.hi[a], y.hi[a]);
+  }
+  return b;
+}
+static float box_area(const Box &b) {
+  float dx = b.hi[0] - b.lo[0], dy = b.hi[1] - b.lo[1], dz = b.hi[2] - b.lo[2];
+  if (!(dx >= 0.f)) return 0.f;
+  return 2.f * (dx * dy + dy * dz + dz * dx);
+}
+
+// Binary tree in the shape the reference builds.
+struct BNode {
+  Box box;
+  int left = -1, right = -1;  // internal
+  int first = -1, count = 0;  // leaf: range of leaf_prims
+};
+
+struct Builder {
+  const pt_scene_desc *d;
+  std::vector<BNode> nodes;
+  std::vector<int> leaf_prims;    // global prim ids in leaf order
+  std::vector<int> tri_base;      // first global prim id of each mesh
+  int n_tris = 0;
+
+  const float *pos(int mesh, int v) const { return d->meshes[mesh].positions + 3 * v; }
+
+  // MeshBVHNode (meshBVH.cpp:6-55): box of the triangles +- 1e-3; leaf at
+  // <= 4 triangles; otherwise split at the median of the centroids along
+  // the longest axis, sorted with std::sort and the reference's comparator.
+  int build_mesh(int mesh, std::vector<int> ids) {
+    const pt_mesh_desc &m = d->meshes[mesh];
+    Box b = box_empty();
+    for (int id : ids)
+      for (int k = 0; k < 3; ++k) {
+        const float *p = pos(mesh, m.indices[3 * id + k]);
+        for (int a = 0; a < 3; ++a) {
+          b.lo[a] = std::min(b.lo[a], p[a]);
+          b.hi[a] = std::max(b.hi[a], p[a]);
+        }
+      }
+    const float eps = 1e-3f;
+    Box pb;
+    for (int a = 0; a < 3; ++a) {
+      pb.lo[a] = b.lo[a] - eps;
+      pb.hi[a] = b.hi[a] + eps;
+    }
+    int me = (int)nodes.size();
+    nodes.push_back(BNode());
+    nodes[me].box = pb;
+    int count = (int)ids.size();
+    if (count <= 4) {
+      nodes[me].first = (int)leaf_prims.size();
+      nodes[me].count = count;
+      for (int id : ids) leaf_prims.push_back(tri_base[mesh] + id);
+      return me;
+    }
+    float ext[3] = {b.hi[0] - b.lo[0], b.hi[1] - b.lo[1], b.hi[2] - b.lo[2]};
+    int axis = ext[0] > ext[1] && ext[0] > ext[2] ? 0 : ext[1] > ext[2] ? 1 : 2;
+    auto centroid = [&](int t) {
+      // (v0 + v1 + v2) / 3.0f, component-wise as the reference's vec ops
+      const float *a = pos(mesh, m.indices[3 * t]), *bb = pos(mesh, m.indices[3 * t + 1]),
+                  *c = pos(mesh, m.indices[3 * t + 2]);
+      return ((a[axis] + bb[axis]) + c[axis]) / 3.0f;
+    };
+    std::sort(ids.begin(), ids.end(), [&](int x, int y) { return centroid(x) < centroid(y); });
+    int mid = count / 2;
+    int l = build_mesh(mesh, std::vector<int>(ids.begin(), ids.begin() + mid));
+    int r = build_mesh(mesh, std::vector<int>(ids.begin() + mid, ids.end()));
+    nodes[me].left = l;
+    nodes[me].right = r;
+    return me;
+  }
+
+  Box object_box(int o) const {
+    const pt_object_desc &od = d->objects[o];
+    Box b;
+    if (od.kind == PT_OBJ_MESH) {  // TriangleMesh::meshAABB (triangleMesh.cpp:10-18)
+      const pt_mesh_desc &m = d->meshes[od.index];
+      b = box_empty();
+      for (int v = 0; v < m.n_positions; ++v)
+        for (int a = 0; a < 3; ++a) {
+          b.lo[a] = std::min(b.lo[a], m.positions[3 * v + a]);
+          b.hi[a] = std::max(b.hi[a], m.positions[3 * v + a]);
+        }
+      for (int a = 0; a < 3; ++a) {
+        b.lo[a] -= 1e-3f;
+        b.hi[a] += 1e-3f;
+      }
+    } else if (od.kind == PT_OBJ_QUAD) {  // AARectangle::getAABB (primitive.cpp:6-28)
+      const pt_quad_desc &q = d->quads[od.index];
+      int a0 = q.axis == 0 ? 1 : 0, a1 = q.axis == 2 ? 1 : 2;
+      b.lo[q.axis] = q.k - 1e-3f;
+      b.hi[q.axis] = q.k + 1e-3f;
+      b.lo[a0] = q.d0_min;
+      b.hi[a0] = q.d0_max;
+      b.lo[a1] = q.d1_min;
+      b.hi[a1] = q.d1_max;
+    } else {  // Sphere::getAABB (primitive.hpp:117-122)
+      const pt_sphere_desc &s = d->spheres[od.index];
+      for (int a = 0; a < 3; ++a) {
+        b.lo[a] = s.center[a] - s.radius;
+        b.hi[a] = s.center[a] + s.radius;
+      }
+    }
+    return b;
+  }
+
+  int object_subtree(int o) {
+    const pt_object_desc &od = d->objects[o];
+    if (od.kind == PT_OBJ_MESH) {
+      const pt_mesh_desc &m = d->meshes[od.index];
+      std::vector<int> ids(m.n_triangles);
+      std::iota(ids.begin(), ids.end(), 0);
+      return build_mesh(od.index, ids);
+    }
+    int me = (int)nodes.size();
+    nodes.push_back(BNode());
+    nodes[me].box = object_box(o);
+    nodes[me].first = (int)leaf_prims.size();
+    nodes[me].count = 1;
+    int prim = od.kind == PT_OBJ_QUAD ? n_tris + od.index : n_tris + d->n_quads + od.index;
+    leaf_prims.push_back(prim);
+    return me;
+  }
+
+  // BVHNode (bvh.hpp:46-102).  The reference sorts a local copy of the
+  // object list and then recurses on the UNSORTED list, so the subtrees
+  // split the insertion order in halves; the split axis drawn from rand()
+  // only orders the two children of a two-object node.  rand() is called
+  // once per node, in construction order, as the reference does.
+  int build_top(int i, int j) {
+    int axis = std::rand() % 3;
+    if (j - i == 1) return object_subtree(i);
+    if (j - i == 2) {
+      Box a = object_box(i), b = object_box(i + 1);
+      bool first_left = (a.lo[axis] + a.hi[axis]) * 0.5f < (b.lo[axis] + b.hi[axis]) * 0.5f;
+      int l = object_subtree(first_left ? i : i + 1);
+      int r = object_subtree(first_left ? i + 1 : i);
+      int me = (int)nodes.size();
+      nodes.push_back(BNode());
+      nodes[me].left = l;
+      nodes[me].right = r;
+      nodes[me].box = box_merge(nodes[l].box, nodes[r].box);
+      return me;
+    }
+    int mid = i + (j - i) / 2;
+    int l = build_top(i, mid);
+    int r = build_top(mid, j);
+    int me = (int)nodes.size();
+    nodes.push_back(BNode());
+    nodes[me].left = l;
+    nodes[me].right = r;
+    nodes[me].box = box_merge(nodes[l].box, nodes[r].box);
+    return me;
+  }
+};
+
+struct Bvh4Out {
+  std::vector<Bvh4Node> nodes;
+  std::vector<int> leaf_order;  // leaf prims in item order
+  int max_depth = 0;
+};
+
+static void collapse(const Builder &B, int bn, Bvh4Out &out, int depth, int me) {
+  // gather up to 4 children by expanding the largest internal child
+  std::vector<int> ch = {B.nodes[bn].left, B.nodes[bn].right};
+  if (B.nodes[bn].left < 0) ch = {bn};  // a leaf as the root
+  while (ch.size() < 4) {
+    int best = -1;
+    float ba = -1.f;
+    for (size_t k = 0; k < ch.size(); ++k) {
+      const BNode &c = B.nodes[ch[k]];
+      if (c.left >= 0 && box_area(c.box) > ba) {
+        ba = box_area(c.box);
+        best = (int)k;
+      }
+    }
+    if (best < 0) break;
+    int x = ch[best];
+    ch[best] = B.nodes[x].left;
+    ch.insert(ch.begin() + best + 1, B.nodes[x].right);
+  }
+  out.max_depth = std::max(out.max_depth, depth + 1);
+  Bvh4Node &N0 = out.nodes[me];
+  for (int k = 0; k < 4; ++k) {
+    N0.lo_x[k] = N0.lo_y[k] = N0.lo_z[k] = INFINITY;
+    N0.hi_x[k] = N0.hi_y[k] = N0.hi_z[k] = -INFINITY;
+    N0.child[k] = 0;
+    N0.count[k] = -1;
+  }
+  for (size_t k = 0; k < ch.size(); ++k) {
+    const BNode &c = B.nodes[ch[k]];
+    Bvh4Node &N = out.nodes[me];
+    N.lo_x[k] = c.box.lo[0];
+    N.lo_y[k] = c.box.lo[1];
+    N.lo_z[k] = c.box.lo[2];
+    N.hi_x[k] = c.box.hi[0];
+    N.hi_y[k] = c.box.hi[1];
+    N.hi_z[k] = c.box.hi[2];
+    if (c.left < 0) {
+      N.child[k] = (int)out.leaf_order.size();
+      N.count[k] = c.count;
+      for (int t = 0; t < c.count; ++t) out.leaf_order.push_back(B.leaf_prims[c.first + t]);
+    } else {
+      int idx = (int)out.nodes.size();
+      out.nodes.push_back(Bvh4Node());
+      out.nodes[me].child[k] = idx;
+      out.nodes[me].count[k] = 0;
+      collapse(B, ch[k], out, depth + 1, idx);
+    }
+  }
+}
+
+template <class T>
+static T *dupload(const std::vector<T> &v, std::vector<void *> &owned, cudaStream_t st) {
+  if (v.empty()) return nullptr;
+  void *p = nullptr;
+  cuda_check(cudaMalloc(&p, sizeof(T) * v.size()), "cudaMalloc(scene)");
+  owned.push_back(p);
+  cuda_check(cudaMemcpyAsync(p, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice, st),
+             "upload scene");
+  return static_cast<T *>(p);
+}
+
+std::unique_ptr<Scene> build_scene(const pt_scene_desc *d, cudaStream_t st) {
+  if (!d) fail(PT_ERR_INVALID, "null scene description");
+  if (d->n_objects <= 0) fail(PT_ERR_INVALID, "scene has no objects");  // renderManager.hpp:64
+  auto S = std::make_unique<Scene>();
+  Builder B;
+  B.d = d;
+  for (int m = 0; m < d->n_meshes; ++m) {
+    const pt_mesh_desc &md = d->meshes[m];
+    if (md.n_triangles < 0 || (md.n_triangles > 0 && (!md.positions || !md.indices)))
+      fail(PT_ERR_INVALID, "mesh without positions or indices");
+    if (md.material < 0 || md.material >= d->n_materials) fail(PT_ERR_INVALID, "mesh material out of range");
+    for (int t = 0; t < 3 * md.n_triangles; ++t)
+      if (md.indices[t] < 0 || md.indices[t] >= md.n_positions)
+        fail(PT_ERR_INVALID, "mesh index out of range");
+    B.tri_base.push_back(B.n_tris);
+    B.n_tris += md.n_triangles;
+  }
+  for (int q = 0; q < d->n_quads; ++q)
+    if (d->quads[q].material < 0 || d->quads[q].material >= d->n_materials || d->quads[q].axis < 0 ||
+        d->quads[q].axis > 2)
+      fail(PT_ERR_INVALID, "bad quad");
+  for (int s = 0; s < d->n_spheres; ++s)
+    if (d->spheres[s].material < 0 || d->spheres[s].material >= d->n_materials)
+      fail(PT_ERR_INVALID, "bad sphere");
+  for (int o = 0; o < d->n_objects; ++o) {
+    const pt_object_desc &od = d->objects[o];
+    int lim = od.kind == PT_OBJ_MESH ? d->n_meshes : od.kind == PT_OBJ_QUAD ? d->n_quads : d->n_spheres;
+    if (od.kind < 0 || od.kind > 2 || od.index < 0 || od.index >= lim)
+      fail(PT_ERR_INVALID, "bad object entry");
+  }
+  const int n_prims = B.n_tris + d->n_quads + d->n_spheres;
+  std::srand(1);  // the reference's BVH build draws from rand() with its default seed
+  int root = B.build_top(0, d->n_objects);
+
+  Bvh4Out out;
+  out.nodes.push_back(Bvh4Node());
+  collapse(B, root, out, 0, 0);
+  if (3 * out.max_depth + 1 > PT_STACK)
+    fail(PT_ERR_TOO_LARGE, "BVH deeper than the traversal stack (" + std::to_string(out.max_depth) + ")");
+
+  // leaf items and shading records
+  std::vector<Item> items(out.leaf_order.size());
+  std::vector<PrimShade> shade(n_prims);
+  std::vector<int> prim_item(n_prims, -1);
+  std::vector<int> prim_mesh(B.n_tris), prim_tri(B.n_tris);
+  for (int m = 0; m < d->n_meshes; ++m)
+    for (int t = 0; t < d->meshes[m].n_triangles; ++t) {
+      prim_mesh[B.tri_base[m] + t] = m;
+      prim_tri[B.tri_base[m] + t] = t;
+    }
+  for (size_t k = 0; k < out.leaf_order.size(); ++k) {
+    const int prim = out.leaf_order[k];
+    Item &it = items[k];
+    std::memset(&it, 0, sizeof it);
+    it.a[3] = u2f((uint32_t)prim);
+    prim_item[prim] = (int)k;
+    if (prim < B.n_tris) {
+      const pt_mesh_desc &m = d->meshes[prim_mesh[prim]];
+      const int t = prim_tri[prim];
+      const float *p0 = m.positions + 3 * m.indices[3 * t];
+      const float *p1 = m.positions + 3 * m.indices[3 * t + 1];
+      const float *p2 = m.positions + 3 * m.indices[3 * t + 2];
+      for (int a = 0; a < 3; ++a) {
+        it.a[a] = p0[a];
+        it.b[a] = p1[a] - p0[a];  // e1 = p1 - p0 (meshBVH.cpp:91)
+        it.c[a] = p2[a] - p0[a];  // e2 = p2 - p0 (meshBVH.cpp:92)
+      }
+      it.b[3] = u2f(ITEM_TRI);
+    } else if (prim < B.n_tris + d->n_quads) {
+      const pt_quad_desc &q = d->quads[prim - B.n_tris];
+      it.a[0] = q.k;
+      it.a[1] = q.d0_min;
+      it.a[2] = q.d0_max;
+      it.b[0] = q.d1_min;
+      it.b[1] = q.d1_max;
+      it.b[2] = (float)q.axis;
+      it.b[3] = u2f(ITEM_QUAD);
+    } else {
+      const pt_sphere_desc &s = d->spheres[prim - B.n_tris - d->n_quads];
+      it.a[0] = s.center[0];
+      it.a[1] = s.center[1];
+      it.a[2] = s.center[2];
+      it.b[0] = s.radius;
+      it.b[3] = u2f(ITEM_SPHERE);
+    }
+  }
+  for (int prim = 0; prim < n_prims; ++prim) {
+    PrimShade &ps = shade[prim];
+    std::memset(&ps, 0, sizeof ps);
+    ps.item = prim_item[prim];
+    ps.light = -1;
+    if (prim < B.n_tris) {
+      const pt_mesh_desc &m = d->meshes[prim_mesh[prim]];
+      const int t = prim_tri[prim];
+      ps.material = m.material;
+      if (m.normals && m.n_normals > 0) {
+        const int32_t *ni = m.normal_indices ? m.normal_indices : m.indices;
+        bool okn = true;
+        for (int k = 0; k < 3; ++k) okn = okn && ni[3 * t + k] >= 0 && ni[3 * t + k] < m.n_normals;
+        if (okn) {
+          ps.flags |= PT_PRIM_SMOOTH;
+          for (int a = 0; a < 3; ++a) {
+            ps.n0[a] = m.normals[3 * ni[3 * t] + a];
+            ps.n1[a] = m.normals[3 * ni[3 * t + 1] + a];
+            ps.n2[a] = m.normals[3 * ni[3 * t + 2] + a];
+          }
+        }
+      }
+    } else if (prim < B.n_tris + d->n_quads) {
+      const pt_quad_desc &q = d->quads[prim - B.n_tris];
+      ps.material = q.material;
+      if (q.flip_face) ps.flags |= PT_PRIM_FLIP;
+    } else {
+      const pt_sphere_desc &s = d->spheres[prim - B.n_tris - d->n_quads];
+      ps.material = s.material;
+      if (s.flip_face) ps.flags |= PT_PRIM_FLIP;
+    }
+  }
+
+  // materials
+  std::vector<MatRec> mats;
+  for (int i = 0; i < d->n_materials; ++i) mats.push_back(derive_material(d->materials[i]));
+
+  // light discovery (lightDiscovery.hpp:5-81): emissive quads and spheres in
+  // object order, then the environment light (renderManager.hpp:115-118).
+  std::vector<LightRec> lights;
+  for (int o = 0; o < d->n_objects; ++o) {
+    const pt_object_desc &od = d->objects[o];
+    if (od.kind == PT_OBJ_MESH) continue;  // meshes are not discovered as lights
+    int mi = od.kind == PT_OBJ_QUAD ? d->quads[od.index].material : d->spheres[od.index].material;
+    const pt_material_desc &md = d->materials[mi];
+    if (md.type != PT_MAT_DIFFUSE_EMITTER || md.p[3] <= 0.f) continue;
+    LightRec L;
+    std::memset(&L, 0, sizeof L);
+    L.intensity = md.p[3];
+    for (int c = 0; c < 3; ++c) L.color[c] = md.p[c];
+    if (od.kind == PT_OBJ_QUAD) {
+      // QuadLight(AARectangle<axis>) vertices (light.hpp:71-108)
+      const pt_quad_desc &q = d->quads[od.index];
+      float v0[3], v1[3], v3_[3];
+      auto put = [&](float *v, float a, float b) {
+        if (q.axis == 0) { v[0] = q.k; v[1] = a; v[2] = b; }
+        else if (q.axis == 1) { v[0] = a; v[1] = q.k; v[2] = b; }
+        else { v[0] = a; v[1] = b; v[2] = q.k; }
+      };
+      put(v0, q.d0_min, q.d1_min);
+      put(v1, q.d0_max, q.d1_min);
+      put(v3_, q.d0_min, q.d1_max);
+      L.type = LIGHT_QUAD;
+      L.prim = B.n_tris + od.index;
+      V3 e1 = v3(v1[0] - v0[0], v1[1] - v0[1], v1[2] - v0[2]);
+      V3 e2 = v3(v3_[0] - v0[0], v3_[1] - v0[1], v3_[2] - v0[2]);
+      V3 c = cross(e1, e2);
+      V3 nn = normalize(c);
+      for (int a = 0; a < 3; ++a) L.v0[a] = v0[a];
+      L.e1[0] = e1.x; L.e1[1] = e1.y; L.e1[2] = e1.z;
+      L.e2[0] = e2.x; L.e2[1] = e2.y; L.e2[2] = e2.z;
+      L.normal[0] = nn.x; L.normal[1] = nn.y; L.normal[2] = nn.z;
+      L.area = length(c);
+    } else {
+      const pt_sphere_desc &s = d->spheres[od.index];
+      L.type = LIGHT_SPHERE;
+      L.prim = B.n_tris + d->n_quads + od.index;
+      for (int a = 0; a < 3; ++a) L.v0[a] = s.center[a];
+      L.radius = s.radius;
+      L.area = (float)(4 * PT_PI * s.radius * s.radius);
+    }
+    shade[L.prim].light = (int)lights.size();
+    lights.push_back(L);
+  }
+
+  // environment map + luminance alias table
+  std::vector<float4> tex;
+  std::vector<float> aprob, apdf;
+  std::vector<int32_t> aidx;
+  if (d->env) {
+    const pt_env_desc &e = *d->env;
+    if (!e.texels || e.width < 2 || e.height < 2) fail(PT_ERR_INVALID, "environment map smaller than 2x2");
+    const int W = e.width, H = e.height, N = W * H;
+    tex.resize(N);
+    for (int i = 0; i < N; ++i) tex[i] = make_float4(e.texels[3 * i], e.texels[3 * i + 1], e.texels[3 * i + 2], 0.f);
+    // cell (x, y) covers u in [x/W, (x+1)/W): weight = mean luminance of the
+    // texels the bilinear lookup blends there, times sin(theta), plus a floor
+    std::vector<double> w(N);
+    double sum = 0.0;
+    for (int y = 0; y < H; ++y)
+      for (int x = 0; x < W; ++x) {
+        double l = 0.0;
+        for (int dy = 0; dy < 2; ++dy)
+          for (int dx = 0; dx < 2; ++dx) {
+            int xx = std::min(x + dx, W - 1), yy = std::min(y + dy, H - 1);
+            const float4 &t = tex[yy * W + xx];
+            l += 0.2126 * t.x + 0.7152 * t.y + 0.0722 * t.z;
+          }
+        double st = std::sin(PT_PI * (y + 0.5) / H);
+        w[y * W + x] = std::max(0.0, l * 0.25) * st;
+        sum += w[y * W + x];
+      }
+    double floor_w = (sum > 0 ? sum / N : 1.0) * 1e-3;
+    sum = 0.0;
+    for (int y = 0; y < H; ++y) {
+      double st = std::sin(PT_PI * (y + 0.5) / H);
+      for (int x = 0; x < W; ++x) {
+        w[y * W + x] += floor_w * st;
+        sum += w[y * W + x];
+      }
+    }
+    apdf.resize(N);
+    for (int i = 0; i < N; ++i) apdf[i] = (float)(w[i] / sum);
+    // Vose's alias method
+    aprob.assign(N, 1.f);
+    aidx.resize(N);
+    std::vector<double> sc(N);
+    std::vector<int> small, large;
+    for (int i = 0; i < N; ++i) {
+      sc[i] = w[i] / sum * N;
+      aidx[i] = i;
+      (sc[i] < 1.0 ? small : large).push_back(i);
+    }
+    while (!small.empty() && !large.empty()) {
+      int s = small.back(); small.pop_back();
+      int l = large.back(); large.pop_back();
+      aprob[s] = (float)sc[s];
+      aidx[s] = l;
+      sc[l] = (sc[l] + sc[s]) - 1.0;
+      (sc[l] < 1.0 ? small : large).push_back(l);
+    }
+    LightRec L;
+    std::memset(&L, 0, sizeof L);
+    L.type = LIGHT_ENV;
+    L.prim = -1;
+    L.intensity = e.intensity;
+    L.area = INFINITY;
+    lights.push_back(L);
+    S->env_w = W;
+    S->env_h = H;
+  }
+
+  // upload
+  S->nodes = dupload(out.nodes, S->owned, st);
+  S->items = dupload(items, S->owned, st);
+  S->shade = dupload(shade, S->owned, st);
+  S->materials = dupload(mats, S->owned, st);
+  S->lights = dupload(lights, S->owned, st);
+  SceneView &V = S->view;
+  std::memset(&V, 0, sizeof V);
+  V.nodes = S->nodes;
+  V.items = S->items;
+  V.shade = S->shade;
+  V.materials = S->materials;
+  V.lights = S->lights;
+  V.n_lights = (int)lights.size();
+  V.n_nodes = (int)out.nodes.size();
+  V.n_prims = n_prims;
+  for (int c = 0; c < 3; ++c) V.bg[c] = d->bg_color[c];
+  if (d->env) {
+    V.env.texels = dupload(tex, S->owned, st);
+    V.env.alias_prob = dupload(aprob, S->owned, st);
+    V.env.alias_idx = dupload(aidx, S->owned, st);
+    V.env.pdf = dupload(apdf, S->owned, st);
+    V.env.width = d->env->width;
+    V.env.height = d->env->height;
+    V.env.intensity = d->env->intensity;
+    V.env.present = 1;
+  }
+  if (d->medium) {
+    V.has_medium = 1;
+    float tmax = 0.f;
+    for (int c = 0; c < 3; ++c) {
+      V.sigma_a[c] = d->medium->sigma_a[c];
+      V.sigma_s[c] = d->medium->sigma_s[c];
+      tmax = std::max(tmax, V.sigma_a[c] + V.sigma_s[c]);
+    }
+    V.sigma_t_max = tmax;
+    V.medium_g = d->medium->g;
+  }
+  S->n_tris = B.n_tris;
+  S->n_quads = d->n_quads;
+  S->n_spheres = d->n_spheres;
+  S->bvh_depth = out.max_depth;
+  size_t bytes = 0;
+  bytes += out.nodes.size() * sizeof(Bvh4Node) + items.size() * sizeof(Item) + shade.size() * sizeof(PrimShade);
+  bytes += mats.size() * sizeof(MatRec) + lights.size() * sizeof(LightRec);
+  bytes += tex.size() * sizeof(float4) + aprob.size() * 12;
+  S->device_bytes = bytes;
+  cuda_check(cudaStreamSynchronize(st), "scene upload");
+  return S;
+}
+
+Scene::~Scene() {
+  for (void *p : owned) cudaFree(p);
+}
+
+// -------------------------------------------------------------- context
+Context::Context(int dev) : device(dev) {
+  cuda_check(cudaSetDevice(dev), "cudaSetDevice");
+  cuda_check(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "cudaStreamCreate");
+  cudaDeviceProp prop;
+  cuda_check(cudaGetDeviceProperties(&prop, dev), "cudaGetDeviceProperties");
+  num_sms = prop.multiProcessorCount;
+  halton = make_halton_tables();
+  upload_halton_tables(halton, stream);
+  kernel_attributes(&kinfo);
+  cfg.trace_blocks = num_sms * std::max(1, kinfo.trace_blocks_per_sm);
+  cfg.shade_blocks = num_sms * std::max(1, kinfo.shade_blocks_per_sm);
+  cfg.max_blocks_simple = num_sms * 8;
+  cfg.sort_by_material = 0;
+  const char *cap = std::getenv("PT_WAVE_PATHS");
+  wave_cap = cap ? std::max(1024, std::atoi(cap)) : (1 << 22);
+  const char *srt = std::getenv("PT_SORT_BY_MATERIAL");
+  if (srt) cfg.sort_by_material = std::atoi(srt);
+  cuda_check(cudaMalloc(&d_err, sizeof(int)), "cudaMalloc(err)");
+  cuda_check(cudaMemsetAsync(d_err, 0, sizeof(int), stream), "memset err");
+  cuda_check(cudaStreamSynchronize(stream), "context init");
+}
+
+Context::~Context() {
+  cudaSetDevice(device);
+  free_queues();
+  for (auto &kv : perms) cudaFree(kv.second);
+  if (d_film) cudaFree(d_film);
+  if (d_offsets) cudaFree(d_offsets);
+  if (d_scratch) cudaFree(d_scratch);
+  if (d_err) cudaFree(d_err);
+  if (stream) cudaStreamDestroy(stream);
+}
+
+void Context::free_queues() {
+  for (void *p : qmem) cudaFree(p);
+  qmem.clear();
+  q_cap = 0;
+  q_ln = 0;
+}
+
+void Context::ensure_queues(int cap, int ln) {
+  if (cap <= q_cap && ln <= q_ln) return;
+  free_queues();
+  auto alloc = [&](size_t bytes) {
+    void *p = nullptr;
+    cuda_check(cudaMalloc(&p, bytes), "cudaMalloc(queues)");
+    qmem.push_back(p);
+    return p;
+  };
+  const size_t c = (size_t)cap;
+  Q.cap = cap;
+  Q.beta = (float4 *)alloc(c * 16);
+  Q.L = (float4 *)alloc(c * 16);
+  Q.ray_o[0] = (float4 *)alloc(c * 16);
+  Q.ray_o[1] = (float4 *)alloc(c * 16);
+  Q.ray_d[0] = (float4 *)alloc(c * 16);
+  Q.ray_d[1] = (float4 *)alloc(c * 16);
+  Q.hit = (float4 *)alloc(c * 16);
+  Q.sh_o = (float4 *)alloc(c * 16);
+  Q.sh_d = (float4 *)alloc(c * 16 * ln);
+  Q.sh_c = (float4 *)alloc(c * 16 * ln);
+  Q.counts = (int *)alloc(64);
+  Q.stats = (unsigned long long *)alloc(64);
+  Q.sort_key = (int *)alloc(c * 4);
+  Q.order = (int *)alloc(c * 4);
+  Q.bins = (int *)alloc(sizeof(int) * 2 * PT_SORT_BINS);
+  Q.err = d_err;
+  q_cap = cap;
+  q_ln = ln;
+}
+
+const uint16_t *Context::perm_for(uint32_t seed) {
+  auto it = perms.find(seed);
+  if (it != perms.end()) return it->second;
+  std::vector<uint16_t> p = make_digit_permutations(halton, seed);
+  uint16_t *dp = nullptr;
+  cuda_check(cudaMalloc(&dp, p.size() * 2), "cudaMalloc(perm)");
+  cuda_check(cudaMemcpyAsync(dp, p.data(), p.size() * 2, cudaMemcpyHostToDevice, stream), "upload perm");
+  cuda_check(cudaStreamSynchronize(stream), "upload perm");
+  perms[seed] = dp;
+  return dp;
+}
+
+Scene *Context::scene(int id) {
+  auto it = scenes.find(id);
+  if (it == scenes.end()) fail(PT_ERR_NOT_FOUND, "unknown scene id " + std::to_string(id));
+  return it->second.get();
+}
+
+// PerspectiveCamera constructor (camera.cpp:7-35).
+CameraView make_camera(const pt_camera_desc &c) {
+  CameraView C;
+  const float m = 1.0f;
+  float theta = c.fov / 2.f;
+  float h = std::tan(theta);
+  float ph = m * h * 2.0f;
+  float pw = ph * c.aspect;
+  V3 up = v3(c.up[0], c.up[1], c.up[2]), front = v3(c.front[0], c.front[1], c.front[2]);
+  V3 pos = v3(c.position[0], c.position[1], c.position[2]);
+  V3 lookat = -normalize(front);
+  V3 hv = normalize(cross(up, lookat));
+  V3 vv = normalize(cross(lookat, hv));
+  V3 hor = hv * pw * c.focal_dist;
+  V3 ver = vv * ph * c.focal_dist;
+  V3 bl = pos - hor / 2.0f - ver / 2.0f;
+  bl = bl - lookat * c.focal_dist;
+  auto put = [](float *d, V3 v) { d[0] = v.x; d[1] = v.y; d[2] = v.z; };
+  put(C.position, pos);
+  put(C.bottom_left, bl);
+  put(C.horizontal, hor);
+  put(C.vertical, ver);
+  put(C.h_vec, hv);
+  put(C.v_vec, vv);
+  C.lens_radius = c.focal_dist / c.aperture * 0.5f;
+  return C;
+}
+
+// FrameBuffer::setOffsets (framebuffer.cpp:131-145): one jittered spp_x by
+// spp_y grid per frame, shared by every pixel, i outer.
+std::vector<float2> make_offsets(const pt_job_desc &j) {
+  std::vector<float2> off;
+  const uint64_t key = path_key(j.seed ^ 0x5bd1e995u, 0xffffffffffull);
+  for (int i = 0; i < j.spp_x; ++i)
+    for (int k = 0; k < j.spp_y; ++k) {
+      const uint32_t s = (uint32_t)(i * j.spp_y + k);
+      float a = (float)i / (float)j.spp_x, b = (float)(i + 1) / (float)j.spp_x;
+      float c = (float)k / (float)j.spp_y, d = (float)(k + 1) / (float)j.spp_y;
+      off.push_back(make_float2(a + (b - a) * rand01(key, 2 * s), c + (d - c) * rand01(key, 2 * s + 1)));
+    }
+  return off;
+}
+
+void validate_job(const pt_job_desc &j) {
+  if (j.width <= 0 || j.height <= 0 || j.spp_x <= 0 || j.spp_y <= 0)
+    fail(PT_ERR_INVALID, "job size must be positive");
+  if (j.max_depth < 0) fail(PT_ERR_INVALID, "max_depth must be >= 0");
+  if (j.light_samples_x <= 0 || j.light_samples_y <= 0 ||
+      j.light_samples_x * j.light_samples_y > PT_MAX_LIGHT_SAMPLES)
+    fail(PT_ERR_INVALID, "light samples must be in [1, 16]");
+  const int spp = j.spp_x * j.spp_y;
+  const int e = j.spp_end ? j.spp_end : spp;
+  if (j.spp_begin < 0 || e > spp || j.spp_begin >= e) fail(PT_ERR_INVALID, "bad sample range");
+  if (j.estimator < 0 || j.estimator > 1 || j.sampler < 0 || j.sampler > 3 || j.env_sampling < 0 ||
+      j.env_sampling > 1)
+    fail(PT_ERR_INVALID, "bad enum in job");
+  if (j.camera.aperture == 0.f) fail(PT_ERR_INVALID, "camera aperture must be non-zero");
+}
+
+DeviceJob Context::device_job(const pt_job_desc &j, Scene *S) {
+  DeviceJob J;
+  std::memset(&J, 0, sizeof J);
+  J.job.width = j.width;
+  J.job.height = j.height;
+  J.job.spp_x = j.spp_x;
+  J.job.spp_y = j.spp_y;
+  J.job.spp = j.spp_x * j.spp_y;
+  J.job.spp_begin = j.spp_begin;
+  J.job.max_depth = j.max_depth;
+  J.job.rr_start = j.rr_start;
+  J.job.estimator = j.estimator;
+  J.job.sampler = j.sampler;
+  J.job.env_sampling = (S->view.env.present ? j.env_sampling : PT_ENV_UNIFORM);
+  J.job.light_nx = j.light_samples_x;
+  J.job.light_ny = j.light_samples_y;
+  J.job.seed = j.seed;
+  J.job.cam = make_camera(j.camera);
+  J.perm = j.sampler == PT_SAMPLER_HALTON_PERMUTE ? perm_for(j.sampler_seed) : nullptr;
+  return J;
+}
+
+void Context::render_device(const pt_job_desc &j, float *d_film, pt_stats *stats, bool sync) {
+  validate_job(j);
+  Scene *S = scene(j.scene);
+  DeviceJob J = device_job(j, S);
+  // offsets table
+  std::vector<float2> off = make_offsets(j);
+  if ((int)off.size() > offsets_cap) {
+    if (d_offsets) cudaFree(d_offsets);
+    cuda_check(cudaMalloc(&d_offsets, off.size() * sizeof(float2)), "cudaMalloc(offsets)");
+    offsets_cap = (int)off.size();
+  }
+  cuda_check(cudaMemcpyAsync(d_offsets, off.data(), off.size() * sizeof(float2), cudaMemcpyHostToDevice, stream),
+             "upload offsets");
+  J.job.offsets = d_offsets;
+  const long long npix = (long long)j.width * j.height;
+  const int e = j.spp_end ? j.spp_end : j.spp_x * j.spp_y;
+  const long long total = npix * (e - j.spp_begin);
+  int n = wave_cap;
+  if (npix <= wave_cap) n = (int)((wave_cap / npix) * npix);
+  if ((long long)n > total) n = (int)total;
+  const int LN = j.light_samples_x * j.light_samples_y;
+  ensure_queues(n, LN);
+  cuda_check(cudaMemsetAsync(Q.stats, 0, 64, stream), "memset stats");
+  auto t0 = std::chrono::steady_clock::now();
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  cudaEventRecord(e0, stream);
+  for (long long g0 = 0; g0 < total; g0 += n) {
+    int cnt = (int)std::min<long long>(n, total - g0);
+    launch_wave(S->view, J, Q, g0, cnt, d_film, cfg, stream);
+  }
+  cudaEventRecord(e1, stream);
+  cuda_check(cudaGetLastError(), "launch");
+  if (sync || stats) {
+    cuda_check(cudaStreamSynchronize(stream), "render");
+    int herr = 0;
+    cuda_check(cudaMemcpy(&herr, d_err, sizeof(int), cudaMemcpyDeviceToHost), "read err");
+    if (herr) {
+      cudaMemset(d_err, 0, sizeof(int));
+      fail(PT_ERR_DEVICE, "device traversal error flag " + std::to_string(herr));
+    }
+  }
+  if (stats) {
+    unsigned long long h[4];
+    cuda_check(cudaMemcpy(h, Q.stats, sizeof h, cudaMemcpyDeviceToHost), "read stats");
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    stats->paths = h[0];
+    stats->segments = h[1];
+    stats->rays = h[2];
+    stats->shadow_rays = h[3];
+    stats->ms = ms;
+    stats->algorithmic_bytes = 192ull * h[1] + 88ull * h[3] + 24ull * h[0];
+  }
+  (void)t0;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+}
+
+float *Context::film_buffer(size_t floats) {
+  if (floats > film_cap) {
+    if (d_film) cudaFree(d_film);
+    d_film = nullptr;
+    cuda_check(cudaMalloc(&d_film, floats * sizeof(float)), "cudaMalloc(film)");
+    film_cap = floats;
+  }
+  return d_film;
+}
+
+void *Context::scratch(size_t bytes) {
+  if (bytes > scratch_cap) {
+    if (d_scratch) cudaFree(d_scratch);
+    d_scratch = nullptr;
+    cuda_check(cudaMalloc(&d_scratch, bytes), "cudaMalloc(scratch)");
+    scratch_cap = bytes;
+  }
+  return d_scratch;
+}
+
+}  // namespace pt
+
+// ================================================================ C-ABI
+using namespace pt;
+
+static int set_error(Context *c, int code, const std::string &msg) {
+  if (c) c->last_error = msg;
+  std::lock_guard<std::mutex> lk(g_err_mu);
+  g_last_error = msg;
+  return code;
+}
+
+#define PT_GUARD(ctxptr, body)                                   \
+  try {                                                          \
+    body;                                                        \
+    return PT_OK;                                                \
+  } catch (const PtError &e) {                                   \
+    return set_error(ctxptr, e.code, e.what());                  \
+  } catch (const std::bad_alloc &) {                             \
+    return set_error(ctxptr, PT_ERR_NOMEM, "host out of memory"); \
+  } catch (const std::exception &e) {                            \
+    return set_error(ctxptr, PT_ERR_INVALID, e.what());          \
+  } catch (...) {                                                \
+    return set_error(ctxptr, PT_ERR_INVALID, "unknown error");   \
+  }
+
+static Context *as_ctx(void *p) {
+  if (!p) fail(PT_ERR_INVALID, "null context");
+  return static_cast<Context *>(p);
+}
+
+extern "C" {
+
+int pt_version(void) { return 1; }
+
+int pt_create(void **ctx, int device) {
+  PT_GUARD(nullptr, {
+    if (!ctx) fail(PT_ERR_INVALID, "null output pointer");
+    *ctx = new Context(device);
+  });
+}
+
+int pt_destroy(void *ctx) {
+  PT_GUARD(nullptr, { delete static_cast<Context *>(ctx); });
+}
+
+int pt_last_error(void *ctx, char *buf, size_t n) {
+  if (!buf || n == 0) return PT_ERR_INVALID;
+  std::string m;
+  if (ctx) {
+    m = static_cast<Context *>(ctx)->last_error;
+  } else {
+    std::lock_guard<std::mutex> lk(g_err_mu);
+    m = g_last_error;
+  }
+  std::snprintf(buf, n, "%s", m.c_str());
+  return PT_OK;
+}
+
+int pt_scene_upload(void *ctx, const pt_scene_desc *desc, int32_t *scene_id) {
+  Context *c = static_cast<Context *>(ctx);
+  PT_GUARD(c, {
+    c = as_ctx(ctx);
+    if (!scene_id) fail(PT_ERR_INVALID, "null scene_id");
+    cuda_check(cudaSetDevice(c->device), "cudaSetDevice");
+    auto S = build_scene(desc, c->stream);
+    int id = c->next_scene++;
+    c->scenes[id] = std::move(S);
+    *scene_id = id;
+  });
+}
+
+int pt_scene_release(void *ctx, int32_t scene_id) {
+  Context *c = static_cast<Context *>(ctx);
+  PT_GUARD(c, {
+    c = as_ctx(ctx);
+    cuda_check(cudaStreamSynchronize(c->stream), "sync");
+    if (!c->scenes.erase(scene_id)) fail(PT_ERR_NOT_FOUND, "unknown scene id");
+  });
+}
+
+int pt_scene_info(void *ctx, int32_t scene_id, int64_t *out6) {
+  Context *c = static_cast<Context *>(ctx);
+  PT_GUARD(c, {
+    c = as_ctx(ctx);
+    Scene *S = c->scene(scene_id);
+    out6[0] = S->n_tris;
+    out6[1] = S->n_quads;
+    out6[2] = S->n_spheres;
+    out6[3] = S->view.n_nodes;
+    out6[4] = S->view.n_lights;
+    out6[5] = (int64_t)S->device_bytes;
+  });
+}
+
+int pt_render_device(void *ctx, const pt_job_desc *job, float *d_film_sum, int sync, pt_stats *stats) {
+  Context *c = static_cast<Context *>(ctx);
+  PT_GUARD(c, {
+    c = as_ctx(ctx);
+    if (!job || !d_film_sum) fail(PT_ERR_INVALID, "null job or film");
+    cuda_check(cudaSetDevice(c->device), "cudaSetDevice");
+    c->render_device(*job, d_film_sum, stats, sync != 0);
+  });
+}
+
+int pt_render(void *ctx, const pt_job_desc *job, float *film_rgb, pt_stats *stats) {
+  Context *c = static_cast<Context *>(ctx);
+  PT_GUARD(c, {
+    c = as_ctx(ctx);
+    if (!job || !film_rgb) fail(PT_ERR_INVALID, "null job or film");
+    validate_job(*job);
+    cuda_check(cudaSetDevice(c->device), "cudaSetDevice");
+    const size_t nf = (size_t)job->width * job->height * 3;
+    float *df = c->film_buffer(nf);
+    cuda_check(cudaMemsetAsync(df, 0, nf * sizeof(float), c->stream), "memset film");
+    c->render_device(*job, df, stats, false);
+    cuda_check(cudaMemcpyAsync(film_rgb, df, nf * sizeof(float), cudaMemcpyDeviceToHost, c->stream), "film d2h");
+    cuda_check(cudaStreamSynchronize(c->stream), "render");
+    int herr = 0;
+    cuda_check(cudaMemcpy(&herr, c->d_err, sizeof(int), cudaMemcpyDeviceToHost), "read err");
+    if (herr) {
+      cudaMemset(c->d_err, 0, sizeof(int));
+      fail(PT_ERR_DEVICE, "device traversal error flag " + std::to_string(herr));
+    }
+    const int e = job->spp_end ? job->spp_end : job->spp_x * job->spp_y;
+    const float inv = 1.f / (float)(e - job->spp_begin);
+    for (size_t i = 0; i < nf; ++i) film_rgb[i] *= inv;
+  });
+}
+
+int pt_tonemap(void *ctx, const float *film_rgb, int32_t width, int32_t height, float gamma, uint8_t *rgb8) {
+  Context *c = static_cast<Context *>(ctx);
+  PT_GUARD(c, {
+    c = as_ctx(ctx);
+    if (!film_rgb || !rgb8 || width <= 0 || height <= 0 || gamma <= 0.f) fail(PT_ERR_INVALID, "bad tonemap args");
+    const size_t nf = (size_t)width * height * 3;
+    char *buf = (char *)c->scratch(nf * 5);
+    float *df = (float *)buf;
+    uint8_t *d8 = (uint8_t *)(buf + nf * 4);
+    cuda_check(cudaMemcpyAsync(df, film_rgb, nf * 4, cudaMemcpyHostToDevice, c->stream), "h2d");
+    launch_tonemap(df, width, height, gamma, d8, c->stream);
+    cuda_check(cudaMemcpyAsync(rgb8, d8, nf, cudaMemcpyDeviceToHost, c->stream), "d2h");
+    cuda_check(cudaStreamSynchronize(c->stream), "tonemap");
+  });
+}
+
+int pt_sampler_eval(void *ctx, int32_t strategy, uint32_t seed, uint32_t first_index, int32_t n, int32_t dims,
+                    float *out) {
+  Context *c = static_cast<Context *>(ctx);
+  PT_GUARD(c, {
+    c = as_ctx(ctx);
+    if (n < 0 || dims <= 0 || !out || strategy < 0 || strategy > 2) fail(PT_ERR_INVALID, "bad sampler args");
+    if (n == 0) return PT_OK;
+    const size_t bytes = (size_t)n * dims * sizeof(float);
+    float *d = (float *)c->scratch(bytes);
+    const uint16_t *perm = strategy == PT_SAMPLER_HALTON_PERMUTE ? c->perm_for(seed) : nullptr;
+    launch_sampler_eval(strategy, perm, first_index, n, dims, d, c->stream);
+    cuda_check(cudaGetLastError(), "sampler launch");
+    cuda_check(cudaMemcpyAsync(out, d, bytes, cudaMemcpyDeviceToHost, c->stream), "d2h");
+    cuda_check(cudaStreamSynchronize(c->stream), "sampler");
+  });
+}
+
+static int trace_common(void *ctx, int32_t scene_id, bool any, const float *rays, const float *tmaxs, int32_t n,
+                        float tmin, float tmax, float *t, int32_t *prim, float *uv, uint8_t *occ) {
+  Context *c = static_cast<Context *>(ctx);
+  PT_GUARD(c, {
+    c = as_ctx(ctx);
+    if (n < 0 || !rays) fail(PT_ERR_INVALID, "bad trace args");
+    if (n == 0) return PT_OK;
+    Scene *S = c->scene(scene_id);
+    const size_t nn = (size_t)n;
+    char *buf = (char *)c->scratch(nn * (24 + 4 + 4 + 4 + 8 + 1) + 256);
+    float *dr = (float *)buf;
+    float *dtm = (float *)(buf + nn * 24);
+    float *dt = (float *)(buf + nn * 28);
+    int *dp = (int *)(buf + nn * 32);
+    float *duv = (float *)(buf + nn * 36);
+    uint8_t *docc = (uint8_t *)(buf + nn * 44);
+    cuda_check(cudaMemcpyAsync(dr, rays, nn * 24, cudaMemcpyHostToDevice, c->stream), "h2d rays");
+    if (any) cuda_check(cudaMemcpyAsync(dtm, tmaxs, nn * 4, cudaMemcpyHostToDevice, c->stream), "h2d tmax");
+    launch_trace_test(S->view, any, dr, dtm, n, tmin, tmax, dt, dp, duv, docc, c->d_err, c->stream);
+    cuda_check(cudaGetLastError(), "trace launch");
+    if (any) {
+      cuda_check(cudaMemcpyAsync(occ, docc, nn, cudaMemcpyDeviceToHost, c->stream), "d2h");
+    } else {
+      cuda_check(cudaMemcpyAsync(t, dt, nn * 4, cudaMemcpyDeviceToHost, c->stream), "d2h");
+      cuda_check(cudaMemcpyAsync(prim, dp, nn * 4, cudaMemcpyDeviceToHost, c->stream), "d2h");
+      if (uv) cuda_check(cudaMemcpyAsync(uv, duv, nn * 8, cudaMemcpyDeviceToHost, c->stream), "d2h");
+    }
+    cuda_check(cudaStreamSynchronize(c->stream), "trace");
+    int herr = 0;
+    cuda_check(cudaMemcpy(&herr, c->d_err, sizeof(int), cudaMemcpyDeviceToHost), "read err");
+    if (herr) {
+      cudaMemset(c->d_err, 0, sizeof(int));
+      fail(PT_ERR_DEVICE, "device traversal error flag " + std::to_string(herr));
+    }
+  });
+}
+
+int pt_trace_closest(void *ctx, int32_t scene_id, const float *rays, int32_t n, float tmin, float tmax, float *t,
+                     int32_t *prim, float *uv) {
+  if (!t || !prim) return PT_ERR_INVALID;
+  return trace_common(ctx, scene_id, false, rays, nullptr, n, tmin, tmax, t, prim, uv, nullptr);
+}
+
+int pt_trace_any(void *ctx, int32_t scene_id, const float *rays, const float *tmax, int32_t n, float tmin,
+                 uint8_t *occluded) {
+  if (!tmax || !occluded) return PT_ERR_INVALID;
+  return trace_common(ctx, scene_id, true, rays, tmax, n, tmin, 0.f, nullptr, nullptr, nullptr, occluded);
+}
+
+int pt_bsdf_eval(void *ctx, const pt_material_desc *mat, int32_t n, const float *wo, const float *wi,
+                 const float *normal, const uint8_t *front, float *f, float *pdf) {
+  Context *c = static_cast<Context *>(ctx);
+  PT_GUARD(c, {
+    c = as_ctx(ctx);
+    if (!mat || n < 0 || !wo || !wi || !normal || !front || !f || !pdf) fail(PT_ERR_INVALID, "bad bsdf args");
+    if (n == 0) return PT_OK;
+    MatRec m = derive_material(*mat);
+    const size_t nn = (size_t)n;
+    char *buf = (char *)c->scratch(sizeof(MatRec) + nn * (12 * 3 + 1 + 12 + 4) + 1024);
+    MatRec *dm = (MatRec *)buf;
+    float *dwo = (float *)(buf + 256);
+    float *dwi = dwo + 3 * nn;
+    float *dn = dwi + 3 * nn;
+    float *df = dn + 3 * nn;
+    float *dpdf = df + 3 * nn;
+    uint8_t *dfr = (uint8_t *)(dpdf + nn);
+    cuda_check(cudaMemcpyAsync(dm, &m, sizeof m, cudaMemcpyHostToDevice, c->stream), "h2d");
+    cuda_check(cudaMemcpyAsync(dwo, wo, nn * 12, cudaMemcpyHostToDevice, c->stream), "h2d");
+    cuda_check(cudaMemcpyAsync(dwi, wi, nn * 12, cudaMemcpyHostToDevice, c->stream), "h2d");
+    cuda_check(cudaMemcpyAsync(dn, normal, nn * 12, cudaMemcpyHostToDevice, c->stream), "h2d");
+    cuda_check(cudaMemcpyAsync(dfr, front, nn, cudaMemcpyHostToDevice, c->stream), "h2d");
+    launch_bsdf_eval(dm, n, dwo, dwi, dn, dfr, df, dpdf, c->stream);
+    cuda_check(cudaGetLastError(), "bsdf launch");
+    cuda_check(cudaMemcpyAsync(f, df, nn * 12, cudaMemcpyDeviceToHost, c->stream), "d2h");
+    cuda_check(cudaMemcpyAsync(pdf, dpdf, nn * 4, cudaMemcpyDeviceToHost, c->stream), "d2h");
+    cuda_check(cudaStreamSynchronize(c->stream), "bsdf");
+  });
+}
+
+int pt_bsdf_sample(void *ctx, const pt_material_desc *mat, int32_t n, const float *wo, const float *normal,
+                   const uint8_t *front, const float *uc, const float *u, uint8_t *ok, float *wi,
+                   float *attenuation, float *pdf_val, uint32_t *sampled_type) {
+  Context *c = static_cast<Context *>(ctx);
+  PT_GUARD(c, {
+    c = as_ctx(ctx);
+    if (!mat || n < 0 || !wo || !normal || !front || !uc || !u || !ok || !wi || !attenuation || !pdf_val ||
+        !sampled_type)
+      fail(PT_ERR_INVALID, "bad bsdf args");
+    if (n == 0) return PT_OK;
+    MatRec m = derive_material(*mat);
+    const size_t nn = (size_t)n;
+    char *buf = (char *)c->scratch(sizeof(MatRec) + nn * 80 + 1024);
+    MatRec *dm = (MatRec *)buf;
+    float *dwo = (float *)(buf + 256);
+    float *dn = dwo + 3 * nn;
+    float *duc = dn + 3 * nn;
+    float *du = duc + nn;
+    float *dwi = du + 2 * nn;
+    float *datt = dwi + 3 * nn;
+    float *dpdf = datt + 3 * nn;
+    uint32_t *dty = (uint32_t *)(dpdf + nn);
+    uint8_t *dfr = (uint8_t *)(dty + nn);
+    uint8_t *dok = dfr + nn;
+    cuda_check(cudaMemcpyAsync(dm, &m, sizeof m, cudaMemcpyHostToDevice, c->stream), "h2d");
+    cuda_check(cudaMemcpyAsync(dwo, wo, nn * 12, cudaMemcpyHostToDevice, c->stream), "h2d");
+    cuda_check(cudaMemcpyAsync(dn, normal, nn * 12, cudaMemcpyHostToDevice, c->stream), "h2d");
+    cuda_check(cudaMemcpyAsync(duc, uc, nn * 4, cudaMemcpyHostToDevice, c->stream), "h2d");
+    cuda_check(cudaMemcpyAsync(du, u, nn * 8, cudaMemcpyHostToDevice, c->stream), "h2d");
+    cuda_check(cudaMemcpyAsync(dfr, front, nn, cudaMemcpyHostToDevice, c->stream), "h2d");
+    launch_bsdf_sample(dm, n, dwo, dn, dfr, duc, du, dok, dwi, datt, dpdf, dty, c->stream);
+    cuda_check(cudaGetLastError(), "bsdf launch");
+    cuda_check(cudaMemcpyAsync(ok, dok, nn, cudaMemcpyDeviceToHost, c->stream), "d2h");
+    cuda_check(cudaMemcpyAsync(wi, dwi, nn * 12, cudaMemcpyDeviceToHost, c->stream), "d2h");
+    cuda_check(cudaMemcpyAsync(attenuation, datt, nn * 12, cudaMemcpyDeviceToHost, c->stream), "d2h");
+    cuda_check(cudaMemcpyAsync(pdf_val, dpdf, nn * 4, cudaMemcpyDeviceToHost, c->stream), "d2h");
+    cuda_check(cudaMemcpyAsync(sampled_type, dty, nn * 4, cudaMemcpyDeviceToHost, c->stream), "d2h");
+    cuda_check(cudaStreamSynchronize(c->stream), "bsdf");
+  });
+}
+
+}  // extern "C"

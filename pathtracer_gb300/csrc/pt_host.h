@@ -1,0 +1,78 @@
+// pt_host.h -- host-side objects behind the C-ABI: resident scenes and the
+// per-thread rendering context (stream, work queues, device buffers).
+#pragma once
+#include <cstddef>
+#include <map>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "pt_bsdf.cuh"
+#include "pt_kernels.h"
+
+namespace pt {
+
+void fail(int code, const std::string &msg);
+void cuda_check(cudaError_t e, const char *what);
+
+HaltonTables make_halton_tables();
+std::vector<uint16_t> make_digit_permutations(const HaltonTables &T, uint32_t seed);
+MatRec derive_material(const pt_material_desc &m);
+CameraView make_camera(const pt_camera_desc &c);
+std::vector<float2> make_offsets(const pt_job_desc &j);
+void validate_job(const pt_job_desc &j);
+
+// A flattened scene resident in HBM.
+struct Scene {
+  SceneView view;
+  Bvh4Node *nodes = nullptr;
+  Item *items = nullptr;
+  PrimShade *shade = nullptr;
+  MatRec *materials = nullptr;
+  LightRec *lights = nullptr;
+  std::vector<void *> owned;
+  int n_tris = 0, n_quads = 0, n_spheres = 0, bvh_depth = 0;
+  int env_w = 0, env_h = 0;
+  size_t device_bytes = 0;
+  ~Scene();
+};
+
+std::unique_ptr<Scene> build_scene(const pt_scene_desc *d, cudaStream_t st);
+
+struct Context {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  int num_sms = 0;
+  HaltonTables halton;
+  KernelInfo kinfo;
+  LaunchCfg cfg;
+  int wave_cap = 1 << 22;
+  std::string last_error;
+  std::map<int, std::unique_ptr<Scene>> scenes;
+  int next_scene = 1;
+  std::map<uint32_t, uint16_t *> perms;
+
+  Queues Q{};
+  std::vector<void *> qmem;
+  int q_cap = 0, q_ln = 0;
+  float *d_film = nullptr;
+  size_t film_cap = 0;
+  float2 *d_offsets = nullptr;
+  int offsets_cap = 0;
+  void *d_scratch = nullptr;
+  size_t scratch_cap = 0;
+  int *d_err = nullptr;
+
+  explicit Context(int dev);
+  ~Context();
+  void free_queues();
+  void ensure_queues(int cap, int ln);
+  const uint16_t *perm_for(uint32_t seed);
+  Scene *scene(int id);
+  DeviceJob device_job(const pt_job_desc &j, Scene *S);
+  void render_device(const pt_job_desc &j, float *d_film, pt_stats *stats, bool sync);
+  float *film_buffer(size_t floats);
+  void *scratch(size_t bytes);
+};
+
+}  // namespace pt

@@ -1,0 +1,64 @@
+// pt_kernels.h -- host-visible interface of the wavefront kernels
+// (pt_kernels.cu) used by the C-ABI layer (pt_host.cpp).
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+#include "../../include/pathtracer_gb300.h"
+#include "pt_scene.cuh"
+
+#define PT_MAX_LIGHT_SAMPLES 16
+#define PT_SORT_BINS 16
+
+namespace pt {
+
+struct DeviceJob {
+  JobView job;
+  const uint16_t *perm;  // PermuteDigits tables for job.sampler_seed
+};
+
+// Work queues of one context, sized for `cap` paths per wave (SoA in HBM).
+struct Queues {
+  int cap;
+  float4 *beta;       // throughput.xyz, pdf of the sampled continuation (<0: delta)
+  float4 *L;          // radiance accumulated by the path
+  float4 *ray_o[2];   // RayQueue ping-pong: origin.xyz, path slot (int bits)
+  float4 *ray_d[2];   //                     direction.xyz
+  float4 *hit;        // HitQueue: t, prim (int bits), u, v
+  float4 *sh_o;       // ShadowQueue: origin.xyz, path slot
+  float4 *sh_d;       // [light sample][cap]: direction.xyz, tmax (<0: none)
+  float4 *sh_c;       // [light sample][cap]: unoccluded contribution
+  int *counts;        // [0],[1] ray queues, [2] shadow queue
+  unsigned long long *stats;  // [0] paths [1] segments [2] rays [3] shadow rays
+  int *err;           // device error flag (stack overflow / iteration cap)
+  int *sort_key, *order, *bins;
+};
+
+struct LaunchCfg {
+  int trace_blocks;
+  int shade_blocks;
+  int max_blocks_simple;
+  int sort_by_material;
+};
+
+struct KernelInfo {
+  int trace_regs, shade_regs;
+  int trace_blocks_per_sm, shade_blocks_per_sm, shadow_blocks_per_sm;
+};
+
+void upload_halton_tables(const HaltonTables &T, cudaStream_t st);
+void launch_sampler_eval(int strategy, const uint16_t *perm, uint32_t first, int n, int dims,
+                         float *out, cudaStream_t st);
+void launch_trace_test(const SceneView &S, bool any, const float *rays, const float *tmaxs, int n,
+                       float tmin, float tmax, float *t, int *prim, float *uv, uint8_t *occ,
+                       int *err, cudaStream_t st);
+void launch_bsdf_eval(const MatRec *m, int n, const float *wo, const float *wi, const float *nrm,
+                      const uint8_t *front, float *f, float *pdf, cudaStream_t st);
+void launch_bsdf_sample(const MatRec *m, int n, const float *wo, const float *nrm,
+                        const uint8_t *front, const float *uc, const float *u, uint8_t *ok,
+                        float *wi, float *att, float *pdf, uint32_t *type, cudaStream_t st);
+void launch_wave(const SceneView &S, const DeviceJob &J, const Queues &Q, long long g0, int n,
+                 float *film, const LaunchCfg &cfg, cudaStream_t st);
+void launch_tonemap(const float *film, int W, int H, float gamma, uint8_t *out, cudaStream_t st);
+void kernel_attributes(KernelInfo *info);
+
+}  // namespace pt

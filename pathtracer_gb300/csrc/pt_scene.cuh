@@ -1,0 +1,134 @@
+// pt_scene.cuh -- device layout of a flattened scene and of a render job.
+//
+// A scene is uploaded once (pt_scene_upload) and stays resident in HBM:
+//   * BVH4 nodes, 128 B each (one L2 line): child boxes as SoA float4 rows,
+//     child references and leaf item counts;
+//   * leaf items, 48 B each (3 x float4), in leaf order: a triangle keeps
+//     v0, e1 = v1 - v0, e2 = v2 - v0 exactly as the reference's hitTriangle
+//     computes them (meshBVH.cpp:91-93), an AARectangle its plane and
+//     extent, a sphere its centre and radius;
+//   * per-primitive shading records (material, vertex normals);
+//   * the material table, the light table (discovered like
+//     lightDiscovery.hpp:5-81) and the environment map with its alias table.
+#pragma once
+#include "pt_common.cuh"
+
+// Entries of the per-thread traversal stack (shared memory).  A BVH4 of
+// depth D needs at most 3 * D + 1 entries; scene upload rejects deeper trees.
+#ifndef PT_STACK
+#define PT_STACK 48
+#endif
+
+namespace pt {
+
+enum ItemType : int32_t { ITEM_TRI = 0, ITEM_QUAD = 1, ITEM_SPHERE = 2 };
+
+struct alignas(128) Bvh4Node {
+  float lo_x[4], hi_x[4];
+  float lo_y[4], hi_y[4];
+  float lo_z[4], hi_z[4];
+  int32_t child[4];  // internal: node index; leaf: first item index
+  int32_t count[4];  // internal: 0; leaf: number of items; empty slot: -1
+};
+static_assert(sizeof(Bvh4Node) == 128, "BVH4 node must be one 128-byte line");
+
+// Leaf item (48 B).  a.w / b.w carry the primitive id and the item type as
+// integer bits.
+struct alignas(16) Item {
+  float a[4];
+  float b[4];
+  float c[4];
+};
+
+// Shading record of a primitive (64 B).
+struct alignas(16) PrimShade {
+  int32_t material;
+  int32_t flags;     // bit0 smooth normals present, bit1 FlipFace
+  int32_t item;      // index of the primitive's leaf item
+  int32_t light;     // index in the light table (-1: not a light)
+  float n0[3], n1[3], n2[3];  // vertex normals (triangles with normals)
+  float pad;
+};
+#define PT_PRIM_SMOOTH 1
+#define PT_PRIM_FLIP 2
+
+// Material record: the C-ABI description plus constants derived once on the
+// host (Disney lobe weights, hair v[p], s, sin/cos 2^k alpha ...).
+struct alignas(16) MatRec {
+  int32_t type;
+  int32_t flags;
+  float p[30];
+  float d[32];  // derived
+};
+
+enum LightType : int32_t { LIGHT_QUAD = 0, LIGHT_SPHERE = 1, LIGHT_ENV = 2 };
+struct alignas(16) LightRec {
+  int32_t type;
+  int32_t prim;     // primitive id of the emitter (quads/spheres)
+  float intensity;
+  float area;
+  float v0[3];      // quad: vertices[0]; sphere: centre
+  float radius;
+  float e1[3];      // quad: vertices[1] - vertices[0]
+  float pad0;
+  float e2[3];      // quad: vertices[3] - vertices[0]
+  float pad1;
+  float normal[3];  // quad: normalize(cross(e1, e2))
+  float pad2;
+  float color[3];   // ConstantTexture colour
+  float pad3;
+};
+
+struct EnvMap {
+  const float4 *texels;   // width*height, [y][x], y = 0 bottom row
+  const float *alias_prob;// width*height
+  const int32_t *alias_idx;
+  const float *pdf;       // per texel, discrete probability
+  int32_t width, height;
+  float intensity;
+  int32_t present;
+};
+
+struct SceneView {
+  const Bvh4Node *nodes;
+  const Item *items;
+  const PrimShade *shade;
+  const MatRec *materials;
+  const LightRec *lights;
+  int32_t n_lights;
+  int32_t n_nodes;
+  int32_t n_prims;
+  EnvMap env;
+  float bg[3];
+  int32_t has_medium;
+  float sigma_a[3], sigma_s[3], sigma_t_max, medium_g;
+};
+
+// Camera constants of PerspectiveCamera (camera.cpp:7-35).
+struct CameraView {
+  float position[3];
+  float bottom_left[3];
+  float horizontal[3];
+  float vertical[3];
+  float h_vec[3];
+  float v_vec[3];
+  float lens_radius;
+};
+
+struct JobView {
+  int32_t width, height;
+  int32_t spp;            // spp_x * spp_y
+  int32_t spp_begin;      // first grid sample of this render
+  int32_t spp_x, spp_y;
+  int32_t max_depth;
+  int32_t rr_start;
+  int32_t estimator;
+  int32_t sampler;
+  int32_t env_sampling;
+  int32_t light_nx, light_ny;
+  uint32_t seed;
+  CameraView cam;
+  const float2 *offsets;  // per grid sample k: jittered pixel offset
+};
+
+}  // namespace pt

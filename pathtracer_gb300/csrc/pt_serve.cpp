@@ -1,0 +1,258 @@
+// pt_serve.cpp -- batched rendering and the request server of the C-ABI.
+//
+// pt_render_batch renders many jobs against resident scenes from one call.
+// The server admits requests while free HBM and slots allow, keeps each
+// request's film on the device, and in every scheduling pass adds
+// spp_per_pass samples to every active request (continuous batching: a
+// request submitted while others run joins at the next pass).  Each
+// request's result depends only on its own job (seed, sample range), never on
+// what else is in flight, so it is identical alone and in a mix.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <mutex>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "pt_host.h"
+
+namespace pt {
+
+struct PtErrorS : std::runtime_error {
+  int code;
+  PtErrorS(int c, const std::string &m) : std::runtime_error(m), code(c) {}
+};
+
+struct Request {
+  int64_t id;
+  pt_request_desc desc;
+  int state = 0;  // 0 queued, 1 running, 2 done, 3 cancelled, 4 failed
+  int spp_done = 0;
+  float *film_a = nullptr;  // sum of even passes
+  float *film_b = nullptr;  // sum of odd passes
+  int spp_a = 0, spp_b = 0;
+  size_t bytes = 0;
+  std::chrono::steady_clock::time_point t_submit, t_done;
+  std::vector<float> result;
+  std::string error;
+};
+
+struct Server {
+  Context *ctx;
+  int64_t budget;
+  int max_slots;
+  int64_t next_id = 1;
+  std::map<int64_t, Request> reqs;
+  std::deque<int64_t> queue;
+  std::vector<int64_t> active;
+  int64_t used = 0;
+};
+
+static void release_films(Request &r, Server &s) {
+  if (r.film_a) cudaFree(r.film_a);
+  if (r.film_b) cudaFree(r.film_b);
+  r.film_a = r.film_b = nullptr;
+  s.used -= (int64_t)r.bytes;
+  r.bytes = 0;
+}
+
+// RMSE of the mean image estimated from two independent halves:
+// E|A - B|^2 / 4 = var(mean of all samples) for equal halves.
+static double estimate_rmse(const Request &r, Server &s, std::vector<float> &ha, std::vector<float> &hb) {
+  if (r.spp_a == 0 || r.spp_b == 0) return INFINITY;
+  const size_t nf = (size_t)r.desc.job.width * r.desc.job.height * 3;
+  ha.resize(nf);
+  hb.resize(nf);
+  cudaMemcpyAsync(ha.data(), r.film_a, nf * 4, cudaMemcpyDeviceToHost, s.ctx->stream);
+  cudaMemcpyAsync(hb.data(), r.film_b, nf * 4, cudaMemcpyDeviceToHost, s.ctx->stream);
+  cudaStreamSynchronize(s.ctx->stream);
+  double acc = 0.0;
+  const double ia = 1.0 / r.spp_a, ib = 1.0 / r.spp_b;
+  for (size_t i = 0; i < nf; ++i) {
+    double d = ha[i] * ia - hb[i] * ib;
+    if (std::isfinite(d)) acc += d * d;
+  }
+  return 0.5 * std::sqrt(acc / (double)nf);
+}
+
+}  // namespace pt
+
+using namespace pt;
+
+static int serr(void *ctx, int code, const std::string &m) {
+  if (ctx) static_cast<Context *>(ctx)->last_error = m;
+  return code;
+}
+
+extern "C" {
+
+int pt_render_batch(void *ctx, const pt_job_desc *jobs, int32_t n_jobs, float **films, pt_stats *stats) {
+  if (!ctx || !jobs || n_jobs < 0 || (n_jobs > 0 && !films)) return serr(ctx, PT_ERR_INVALID, "bad batch args");
+  pt_stats total;
+  std::memset(&total, 0, sizeof total);
+  for (int k = 0; k < n_jobs; ++k) {
+    pt_stats st;
+    int rc = pt_render(ctx, &jobs[k], films[k], &st);
+    if (rc != PT_OK) return rc;
+    total.paths += st.paths;
+    total.segments += st.segments;
+    total.rays += st.rays;
+    total.shadow_rays += st.shadow_rays;
+    total.ms += st.ms;
+    total.algorithmic_bytes += st.algorithmic_bytes;
+  }
+  if (stats) *stats = total;
+  return PT_OK;
+}
+
+int pt_server_create(void *ctx, int64_t hbm_budget_bytes, int32_t max_slots, void **server) {
+  if (!ctx || !server || max_slots <= 0) return serr(ctx, PT_ERR_INVALID, "bad server args");
+  Server *s = new Server();
+  s->ctx = static_cast<Context *>(ctx);
+  s->budget = hbm_budget_bytes;
+  s->max_slots = max_slots;
+  *server = s;
+  return PT_OK;
+}
+
+int pt_server_destroy(void *server) {
+  if (!server) return PT_ERR_INVALID;
+  Server *s = static_cast<Server *>(server);
+  cudaStreamSynchronize(s->ctx->stream);
+  for (auto &kv : s->reqs) release_films(kv.second, *s);
+  delete s;
+  return PT_OK;
+}
+
+int pt_submit(void *server, const pt_request_desc *req, int64_t *request_id) {
+  if (!server || !req || !request_id) return PT_ERR_INVALID;
+  Server *s = static_cast<Server *>(server);
+  try {
+    validate_job(req->job);
+    s->ctx->scene(req->job.scene);
+  } catch (const std::exception &e) {
+    return serr(s->ctx, PT_ERR_INVALID, e.what());
+  }
+  if (req->spp_cap <= 0 || req->spp_per_pass <= 0) return serr(s->ctx, PT_ERR_INVALID, "bad spp cap / pass");
+  Request r;
+  r.id = s->next_id++;
+  r.desc = *req;
+  r.t_submit = std::chrono::steady_clock::now();
+  s->reqs[r.id] = r;
+  s->queue.push_back(r.id);
+  *request_id = r.id;
+  return PT_OK;
+}
+
+int pt_server_step(void *server, int32_t *active_out) {
+  if (!server) return PT_ERR_INVALID;
+  Server *s = static_cast<Server *>(server);
+  Context *c = s->ctx;
+  // admission: FIFO while slots and HBM allow
+  while (!s->queue.empty() && (int)s->active.size() < s->max_slots) {
+    Request &r = s->reqs[s->queue.front()];
+    if (r.state == 3) {
+      s->queue.pop_front();
+      continue;
+    }
+    const size_t nf = (size_t)r.desc.job.width * r.desc.job.height * 3;
+    const size_t need = 2 * nf * sizeof(float);
+    size_t free_b = 0, total_b = 0;
+    cudaMemGetInfo(&free_b, &total_b);
+    if ((int64_t)(s->used + need) > s->budget || need + (size_t)(256ull << 20) > free_b) break;
+    if (cudaMalloc(&r.film_a, nf * 4) != cudaSuccess || cudaMalloc(&r.film_b, nf * 4) != cudaSuccess) {
+      release_films(r, *s);
+      break;
+    }
+    cudaMemsetAsync(r.film_a, 0, nf * 4, c->stream);
+    cudaMemsetAsync(r.film_b, 0, nf * 4, c->stream);
+    r.bytes = need;
+    s->used += (int64_t)need;
+    r.state = 1;
+    s->active.push_back(r.id);
+    s->queue.pop_front();
+  }
+  // one pass over every active request
+  std::vector<float> ha, hb;
+  std::vector<int64_t> still;
+  for (int64_t id : s->active) {
+    Request &r = s->reqs[id];
+    if (r.state != 1) {
+      release_films(r, *s);
+      continue;
+    }
+    pt_job_desc j = r.desc.job;
+    const int spp_total = j.spp_x * j.spp_y;
+    const int cap = std::min(r.desc.spp_cap, spp_total);
+    const int b = r.spp_done, e = std::min(cap, b + r.desc.spp_per_pass);
+    j.spp_begin = b;
+    j.spp_end = e;
+    const bool to_a = ((b / std::max(1, r.desc.spp_per_pass)) % 2) == 0;
+    int rc = pt_render_device(c, &j, to_a ? r.film_a : r.film_b, 0, nullptr);
+    if (rc != PT_OK) {
+      r.state = 4;
+      r.error = c->last_error;
+      release_films(r, *s);
+      continue;
+    }
+    (to_a ? r.spp_a : r.spp_b) += e - b;
+    r.spp_done = e;
+    bool done = r.spp_done >= cap;
+    if (!done && r.desc.target_rmse > 0.f && r.spp_a > 0 && r.spp_b > 0) {
+      double est = estimate_rmse(r, *s, ha, hb);
+      if (est <= r.desc.target_rmse) done = true;
+    }
+    if (done) {
+      const size_t nf = (size_t)j.width * j.height * 3;
+      ha.resize(nf);
+      hb.resize(nf);
+      cudaMemcpyAsync(ha.data(), r.film_a, nf * 4, cudaMemcpyDeviceToHost, c->stream);
+      cudaMemcpyAsync(hb.data(), r.film_b, nf * 4, cudaMemcpyDeviceToHost, c->stream);
+      cudaStreamSynchronize(c->stream);
+      r.result.resize(nf);
+      const float inv = 1.f / (float)r.spp_done;
+      for (size_t i = 0; i < nf; ++i) r.result[i] = (ha[i] + hb[i]) * inv;
+      r.state = 2;
+      r.t_done = std::chrono::steady_clock::now();
+      release_films(r, *s);
+    } else {
+      still.push_back(id);
+    }
+  }
+  s->active = still;
+  cudaStreamSynchronize(c->stream);
+  if (active_out) *active_out = (int32_t)(s->active.size() + s->queue.size());
+  return PT_OK;
+}
+
+int pt_poll(void *server, int64_t request_id, int32_t *state, float *film, int32_t *spp_done, double *latency_ms) {
+  if (!server) return PT_ERR_INVALID;
+  Server *s = static_cast<Server *>(server);
+  auto it = s->reqs.find(request_id);
+  if (it == s->reqs.end()) return serr(s->ctx, PT_ERR_NOT_FOUND, "unknown request");
+  Request &r = it->second;
+  if (state) *state = r.state;
+  if (spp_done) *spp_done = r.spp_done;
+  if (latency_ms)
+    *latency_ms = r.state == 2 ? std::chrono::duration<double, std::milli>(r.t_done - r.t_submit).count() : -1.0;
+  if (film && r.state == 2) std::memcpy(film, r.result.data(), r.result.size() * sizeof(float));
+  if (r.state == 4) return serr(s->ctx, PT_ERR_DEVICE, r.error);
+  return PT_OK;
+}
+
+int pt_cancel(void *server, int64_t request_id) {
+  if (!server) return PT_ERR_INVALID;
+  Server *s = static_cast<Server *>(server);
+  auto it = s->reqs.find(request_id);
+  if (it == s->reqs.end()) return serr(s->ctx, PT_ERR_NOT_FOUND, "unknown request");
+  if (it->second.state <= 1) it->second.state = 3;
+  return PT_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,215 @@
+// pt_trace.cuh -- closest-hit and any-hit traversal of the BVH4.
+//
+// The BVH4 is collapsed from the reference's own binary trees (top level
+// BVHNode, bvh.hpp:46-102; per mesh MeshBVHNode, meshBVH.cpp:6-55), so the
+// leaves hold exactly the reference's leaf primitive sets.  Traversal is
+// near-to-far with a per-thread stack in SHARED memory (column per thread,
+// bank-conflict free).  Primitive tests restate the reference arithmetic
+// with rounded, never-fused operations so that hit distances match the
+// reference bit for bit:
+//   triangle  MeshBVHNode::hitTriangle  meshBVH.cpp:85-143
+//   rectangle AARectangle<axis>::intersect  primitive.cpp:31-122
+//   sphere    Sphere::intersect  primitive.hpp:124-170
+// Acceptance is inclusive (t == tmax accepted), so of two equal-t primitives
+// the later one tested wins, as in the reference leaf loop.
+#pragma once
+#include "pt_scene.cuh"
+
+namespace pt {
+
+#define PT_TRAVERSAL_CAP (1 << 22)
+
+struct HitRec {
+  float t;
+  int32_t prim;
+  float u, v;
+};
+
+// Leaf references on the stack: ~(first_item << 3 | count - 1), count <= 8.
+PT_HD int32_t leaf_ref(int32_t first, int32_t count) { return ~((first << 3) | (count - 1)); }
+
+// Moller-Trumbore exactly as hitTriangle orders it.
+__device__ __forceinline__ bool hit_triangle(const Item &it, V3 o, V3 d, float tmin, float tmax,
+                                             float &t_out, float &u_out, float &v_out) {
+  V3 p0 = v3(it.a[0], it.a[1], it.a[2]);
+  V3 e1 = v3(it.b[0], it.b[1], it.b[2]);
+  V3 e2 = v3(it.c[0], it.c[1], it.c[2]);
+  V3 P = xcross(d, e2);
+  float det = xdot(e1, P);
+  if (fabsf(det) < 1e-8f) return false;
+  float inv = xdiv(1.0f, det);
+  V3 T = xsubv(o, p0);
+  float u = xmul(xdot(T, P), inv);
+  if (u < 0.f || u > 1.f) return false;
+  V3 Q = xcross(T, e1);
+  float v = xmul(xdot(d, Q), inv);
+  if (v < 0.f || xadd(u, v) > 1.f) return false;
+  float t = xmul(xdot(e2, Q), inv);
+  if (t < tmin || t > tmax) return false;
+  t_out = t;
+  u_out = u;
+  v_out = v;
+  return true;
+}
+
+// AARectangle<axis>::intersect with the normalised direction dn.
+__device__ __forceinline__ bool hit_quad(const Item &it, V3 o, V3 dn, float tmin, float tmax,
+                                         float &t_out) {
+  const int axis = (int)it.b[2];
+  const float k = it.a[0], d0min = it.a[1], d0max = it.a[2];
+  const float d1min = it.b[0], d1max = it.b[1];
+  float oa, da, o0, d0_, o1, d1_;
+  if (axis == 0) {
+    oa = o.x; da = dn.x; o0 = o.y; d0_ = dn.y; o1 = o.z; d1_ = dn.z;
+  } else if (axis == 1) {
+    oa = o.y; da = dn.y; o0 = o.x; d0_ = dn.x; o1 = o.z; d1_ = dn.z;
+  } else {
+    oa = o.z; da = dn.z; o0 = o.x; d0_ = dn.x; o1 = o.y; d1_ = dn.y;
+  }
+  float t = xdiv(xsub(k, oa), da);
+  if (t < tmin || t > tmax) return false;
+  float a0 = xadd(o0, xmul(t, d0_));
+  float a1 = xadd(o1, xmul(t, d1_));
+  if (a0 < d0min || a0 > d0max || a1 < d1min || a1 > d1max) return false;
+  t_out = t;
+  return true;
+}
+
+// Sphere::intersect with the normalised direction dn.
+__device__ __forceinline__ bool hit_sphere(const Item &it, V3 o, V3 dn, float tmin, float tmax,
+                                           float &t_out) {
+  V3 c = v3(it.a[0], it.a[1], it.a[2]);
+  const float r = it.b[0];
+  V3 oc = xsubv(o, c);
+  float a = xdot(dn, dn);
+  float b = xmul(2.f, xdot(dn, oc));
+  float cc = xsub(xdot(oc, oc), xmul(r, r));
+  float disc = xsub(xmul(b, b), xmul(xmul(4.f, a), cc));
+  if (disc < 0.f) return false;
+  float delta = xsqrt(disc);
+  float t = xdiv(xsub(-b, delta), xmul(2.f, a));
+  if (t < tmin || t > tmax) {
+    t = xdiv(xadd(-b, delta), xmul(2.f, a));
+    if (t < tmin || t > tmax) return false;
+  }
+  t_out = t;
+  return true;
+}
+
+__device__ __forceinline__ Item load_item(const Item *items, int i) {
+  const float4 *p = reinterpret_cast<const float4 *>(items + i);
+  float4 a = __ldg(p), b = __ldg(p + 1), c = __ldg(p + 2);
+  Item it;
+  it.a[0] = a.x; it.a[1] = a.y; it.a[2] = a.z; it.a[3] = a.w;
+  it.b[0] = b.x; it.b[1] = b.y; it.b[2] = b.z; it.b[3] = b.w;
+  it.c[0] = c.x; it.c[1] = c.y; it.c[2] = c.z; it.c[3] = c.w;
+  return it;
+}
+
+// Tests one leaf; for ANY returns true on the first hit in [tmin, tmax].
+template <bool ANY>
+__device__ __forceinline__ bool test_leaf(const SceneView &S, int32_t ref, V3 o, V3 d, V3 dn,
+                                          float tmin, float &tmax, HitRec &hit) {
+  const int32_t code = ~ref;
+  const int first = code >> 3, count = (code & 7) + 1;
+  bool any = false;
+  for (int k = 0; k < count; ++k) {
+    Item it = load_item(S.items, first + k);
+    const int type = (int)f2u(it.b[3]);
+    float t, u = 0.f, v = 0.f;
+    bool h;
+    if (type == ITEM_TRI)
+      h = hit_triangle(it, o, d, tmin, tmax, t, u, v);
+    else if (type == ITEM_QUAD)
+      h = hit_quad(it, o, dn, tmin, tmax, t);
+    else
+      h = hit_sphere(it, o, dn, tmin, tmax, t);
+    if (h) {
+      if (ANY) return true;
+      tmax = t;
+      hit.t = t;
+      hit.prim = (int32_t)f2u(it.a[3]);
+      hit.u = u;
+      hit.v = v;
+      any = true;
+    }
+  }
+  return any;
+}
+
+// Generic traversal.  `stack` points at this thread's column of a shared
+// array laid out [PT_STACK][blockDim.x].  Returns: closest -> whether
+// anything was hit (hit filled); any -> occluded.  *err is set when the
+// stack would overflow or the iteration cap is reached (never expected).
+template <bool ANY>
+__device__ bool traverse(const SceneView &S, V3 o, V3 d, float tmin, float tmax, HitRec &hit,
+                         int32_t *stack, int stride, int *err) {
+  hit.t = FLT_MAX;
+  hit.prim = -1;
+  hit.u = hit.v = 0.f;
+  const V3 dn = xnormalize(d);
+  const V3 inv = v3(1.f / d.x, 1.f / d.y, 1.f / d.z);
+  const V3 oi = v3(-o.x * inv.x, -o.y * inv.y, -o.z * inv.z);
+  bool found = false;
+  int sp = 0;
+  int32_t ref = 0;  // node 0 is the root (the host always emits at least one node)
+  for (int iter = 0; iter < PT_TRAVERSAL_CAP; ++iter) {
+    if (ref >= 0) {
+      const float4 *np = reinterpret_cast<const float4 *>(S.nodes + ref);
+      float4 lx = __ldg(np + 0), hx = __ldg(np + 1), ly = __ldg(np + 2), hy = __ldg(np + 3);
+      float4 lz = __ldg(np + 4), hz = __ldg(np + 5);
+      int4 ch = __ldg(reinterpret_cast<const int4 *>(np + 6));
+      int4 cn = __ldg(reinterpret_cast<const int4 *>(np + 7));
+      const float lxa[4] = {lx.x, lx.y, lx.z, lx.w}, hxa[4] = {hx.x, hx.y, hx.z, hx.w};
+      const float lya[4] = {ly.x, ly.y, ly.z, ly.w}, hya[4] = {hy.x, hy.y, hy.z, hy.w};
+      const float lza[4] = {lz.x, lz.y, lz.z, lz.w}, hza[4] = {hz.x, hz.y, hz.z, hz.w};
+      const int cha[4] = {ch.x, ch.y, ch.z, ch.w}, cna[4] = {cn.x, cn.y, cn.z, cn.w};
+      float dist[4];
+      int32_t cref[4];
+      int nh = 0;
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        if (cna[c] < 0) continue;
+        float t0x = fmaf(lxa[c], inv.x, oi.x), t1x = fmaf(hxa[c], inv.x, oi.x);
+        float t0y = fmaf(lya[c], inv.y, oi.y), t1y = fmaf(hya[c], inv.y, oi.y);
+        float t0z = fmaf(lza[c], inv.z, oi.z), t1z = fmaf(hza[c], inv.z, oi.z);
+        float tn = fmaxf(fmaxf(fminf(t0x, t1x), fminf(t0y, t1y)), fmaxf(fminf(t0z, t1z), tmin));
+        float tf = fminf(fminf(fmaxf(t0x, t1x), fmaxf(t0y, t1y)), fminf(fmaxf(t0z, t1z), tmax));
+        if (tn <= tf) {
+          // insertion into a small sorted list (ascending distance)
+          int32_t r = cna[c] == 0 ? cha[c] : leaf_ref(cha[c], cna[c]);
+          int j = nh++;
+          while (j > 0 && dist[j - 1] > tn) {
+            dist[j] = dist[j - 1];
+            cref[j] = cref[j - 1];
+            --j;
+          }
+          dist[j] = tn;
+          cref[j] = r;
+        }
+      }
+      if (nh == 0) {
+        if (sp == 0) break;
+        ref = stack[(--sp) * stride];
+        continue;
+      }
+      if (sp + nh - 1 > PT_STACK) {
+        *err = 1;
+        break;
+      }
+      for (int j = nh - 1; j >= 1; --j) stack[(sp++) * stride] = cref[j];
+      ref = cref[0];
+    } else {
+      if (test_leaf<ANY>(S, ref, o, d, dn, tmin, tmax, hit)) {
+        found = true;
+        if (ANY) return true;
+      }
+      if (sp == 0) break;
+      ref = stack[(--sp) * stride];
+    }
+    if (iter == PT_TRAVERSAL_CAP - 1) *err = 2;
+  }
+  return found;
+}
+
+}  // namespace pt

@@ -1,0 +1,399 @@
+"""ctypes binding of the C-ABI in include/pathtracer_gb300.h.
+
+This is the Python face of the drop-in boundary: the structures mirror the C
+header field by field, and :class:`Renderer` wraps a ``pt_context``.  The
+library is loaded from the package's ``_lib`` directory; if it is missing
+the import fails loudly (there is no CPU fallback on the product path).
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+LIB_PATH = Path(__file__).resolve().parent / "_lib" / "libpathtracer_gb300.so"
+
+PT_OK = 0
+ERRORS = {
+    -1: "PT_ERR_INVALID", -2: "PT_ERR_CUDA", -3: "PT_ERR_NOMEM", -4: "PT_ERR_NOT_FOUND",
+    -5: "PT_ERR_DEVICE", -6: "PT_ERR_BUSY", -7: "PT_ERR_CANCELLED", -8: "PT_ERR_TOO_LARGE",
+}
+
+# material types (pathtracer_gb300.h)
+LAMBERTIAN, CONDUCTOR, MF_DIELECTRIC, THIN_DIELECTRIC, PHONG, DISNEY, HAIR, DIFFUSE_EMITTER = range(8)
+FLAG_SPLIT_RAY, FLAG_MELANIN = 1, 2
+OBJ_MESH, OBJ_QUAD, OBJ_SPHERE = 0, 1, 2
+EST_REF_NEE, EST_NEE_MIS = 0, 1
+SAMPLER_HALTON_NONE, SAMPLER_HALTON_PERMUTE, SAMPLER_HALTON_OWEN, SAMPLER_STRATIFIED = range(4)
+ENV_UNIFORM, ENV_ALIAS = 0, 1
+
+# exported symbols of the C-ABI, in header order
+EXPORTS = [
+    "pt_create", "pt_destroy", "pt_last_error", "pt_version", "pt_scene_upload", "pt_scene_release",
+    "pt_scene_info", "pt_render", "pt_render_device", "pt_tonemap", "pt_sampler_eval", "pt_trace_closest",
+    "pt_trace_any", "pt_bsdf_eval", "pt_bsdf_sample", "pt_render_batch", "pt_server_create",
+    "pt_server_destroy", "pt_submit", "pt_server_step", "pt_poll", "pt_cancel",
+]
+
+f32p = C.POINTER(C.c_float)
+i32p = C.POINTER(C.c_int32)
+u8p = C.POINTER(C.c_uint8)
+u32p = C.POINTER(C.c_uint32)
+
+
+class MaterialDesc(C.Structure):
+    _fields_ = [("type", C.c_int32), ("flags", C.c_int32), ("p", C.c_float * 30)]
+
+
+class MeshDesc(C.Structure):
+    _fields_ = [
+        ("positions", f32p), ("n_positions", C.c_int32),
+        ("normals", f32p), ("n_normals", C.c_int32),
+        ("uvs", f32p), ("n_uvs", C.c_int32),
+        ("indices", i32p), ("normal_indices", i32p), ("uv_indices", i32p),
+        ("n_triangles", C.c_int32), ("material", C.c_int32),
+    ]
+
+
+class QuadDesc(C.Structure):
+    _fields_ = [("axis", C.c_int32), ("k", C.c_float), ("d0_min", C.c_float), ("d0_max", C.c_float),
+                ("d1_min", C.c_float), ("d1_max", C.c_float), ("material", C.c_int32), ("flip_face", C.c_int32)]
+
+
+class SphereDesc(C.Structure):
+    _fields_ = [("center", C.c_float * 3), ("radius", C.c_float), ("material", C.c_int32),
+                ("flip_face", C.c_int32)]
+
+
+class ObjectDesc(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("index", C.c_int32)]
+
+
+class EnvDesc(C.Structure):
+    _fields_ = [("texels", f32p), ("width", C.c_int32), ("height", C.c_int32), ("intensity", C.c_float)]
+
+
+class MediumDesc(C.Structure):
+    _fields_ = [("sigma_a", C.c_float * 3), ("sigma_s", C.c_float * 3), ("g", C.c_float)]
+
+
+class SceneDesc(C.Structure):
+    _fields_ = [
+        ("materials", C.POINTER(MaterialDesc)), ("n_materials", C.c_int32),
+        ("meshes", C.POINTER(MeshDesc)), ("n_meshes", C.c_int32),
+        ("quads", C.POINTER(QuadDesc)), ("n_quads", C.c_int32),
+        ("spheres", C.POINTER(SphereDesc)), ("n_spheres", C.c_int32),
+        ("objects", C.POINTER(ObjectDesc)), ("n_objects", C.c_int32),
+        ("env", C.POINTER(EnvDesc)), ("medium", C.POINTER(MediumDesc)),
+        ("bg_color", C.c_float * 3), ("bvh_mode", C.c_int32),
+    ]
+
+
+class CameraDesc(C.Structure):
+    _fields_ = [("fov", C.c_float), ("aspect", C.c_float), ("focal_dist", C.c_float), ("aperture", C.c_float),
+                ("up", C.c_float * 3), ("front", C.c_float * 3), ("position", C.c_float * 3),
+                ("shutter", C.c_float)]
+
+
+class JobDesc(C.Structure):
+    _fields_ = [
+        ("scene", C.c_int32), ("width", C.c_int32), ("height", C.c_int32),
+        ("spp_x", C.c_int32), ("spp_y", C.c_int32), ("spp_begin", C.c_int32), ("spp_end", C.c_int32),
+        ("max_depth", C.c_int32), ("rr_start", C.c_int32), ("estimator", C.c_int32), ("sampler", C.c_int32),
+        ("env_sampling", C.c_int32), ("light_samples_x", C.c_int32), ("light_samples_y", C.c_int32),
+        ("seed", C.c_uint32), ("sampler_seed", C.c_uint32), ("camera", CameraDesc), ("gamma", C.c_float),
+        ("reserved", C.c_int32 * 4),
+    ]
+
+
+class Stats(C.Structure):
+    _fields_ = [("paths", C.c_uint64), ("segments", C.c_uint64), ("rays", C.c_uint64),
+                ("shadow_rays", C.c_uint64), ("ms", C.c_double), ("algorithmic_bytes", C.c_uint64)]
+
+
+class RequestDesc(C.Structure):
+    _fields_ = [("job", JobDesc), ("target_rmse", C.c_float), ("spp_cap", C.c_int32),
+                ("spp_per_pass", C.c_int32)]
+
+
+_lib = None
+
+
+def load() -> C.CDLL:
+    """Loads the native library (building nothing): raises if it is absent."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not LIB_PATH.exists():
+        raise ImportError(f"native library missing: {LIB_PATH} (run __graft_entry__.build())")
+    lib = C.CDLL(str(LIB_PATH))
+    vp = C.c_void_p
+    sig = {
+        "pt_create": [C.POINTER(vp), C.c_int],
+        "pt_destroy": [vp],
+        "pt_last_error": [vp, C.c_char_p, C.c_size_t],
+        "pt_version": [],
+        "pt_scene_upload": [vp, C.POINTER(SceneDesc), i32p],
+        "pt_scene_release": [vp, C.c_int32],
+        "pt_scene_info": [vp, C.c_int32, C.POINTER(C.c_int64)],
+        "pt_render": [vp, C.POINTER(JobDesc), f32p, C.POINTER(Stats)],
+        "pt_render_device": [vp, C.POINTER(JobDesc), vp, C.c_int, C.POINTER(Stats)],
+        "pt_tonemap": [vp, f32p, C.c_int32, C.c_int32, C.c_float, u8p],
+        "pt_sampler_eval": [vp, C.c_int32, C.c_uint32, C.c_uint32, C.c_int32, C.c_int32, f32p],
+        "pt_trace_closest": [vp, C.c_int32, f32p, C.c_int32, C.c_float, C.c_float, f32p, i32p, f32p],
+        "pt_trace_any": [vp, C.c_int32, f32p, f32p, C.c_int32, C.c_float, u8p],
+        "pt_bsdf_eval": [vp, C.POINTER(MaterialDesc), C.c_int32, f32p, f32p, f32p, u8p, f32p, f32p],
+        "pt_bsdf_sample": [vp, C.POINTER(MaterialDesc), C.c_int32, f32p, f32p, u8p, f32p, f32p, u8p, f32p,
+                           f32p, f32p, u32p],
+        "pt_render_batch": [vp, C.POINTER(JobDesc), C.c_int32, C.POINTER(f32p), C.POINTER(Stats)],
+        "pt_server_create": [vp, C.c_int64, C.c_int32, C.POINTER(vp)],
+        "pt_server_destroy": [vp],
+        "pt_submit": [vp, C.POINTER(RequestDesc), C.POINTER(C.c_int64)],
+        "pt_server_step": [vp, i32p],
+        "pt_poll": [vp, C.c_int64, i32p, f32p, i32p, C.POINTER(C.c_double)],
+        "pt_cancel": [vp, C.c_int64],
+    }
+    for name, args in sig.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = C.c_int
+    _lib = lib
+    return lib
+
+
+class PtError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+def _ptr(a: np.ndarray, ctype):
+    return a.ctypes.data_as(C.POINTER(ctype))
+
+
+def material(mtype: int, params, flags: int = 0) -> MaterialDesc:
+    m = MaterialDesc()
+    m.type = mtype
+    m.flags = flags
+    for i, v in enumerate(params):
+        m.p[i] = float(v)
+    return m
+
+
+class SceneBuffers:
+    """Keeps the numpy arrays alive that a SceneDesc points into."""
+
+    def __init__(self):
+        self.keep = []
+        self.desc = SceneDesc()
+
+    def hold(self, a):
+        self.keep.append(a)
+        return a
+
+
+def make_scene_desc(scene) -> SceneBuffers:
+    """Builds the C description of a :class:`pathtracer_gb300.scene.Scene`."""
+    sb = SceneBuffers()
+    d = sb.desc
+    mats = (MaterialDesc * max(1, len(scene.materials)))(*[material(*m) for m in scene.materials])
+    sb.hold(mats)
+    d.materials = mats
+    d.n_materials = len(scene.materials)
+    meshes = (MeshDesc * max(1, len(scene.meshes)))()
+    for i, m in enumerate(scene.meshes):
+        md = meshes[i]
+        pos = sb.hold(np.ascontiguousarray(m.positions, dtype=np.float32))
+        idx = sb.hold(np.ascontiguousarray(m.indices, dtype=np.int32))
+        md.positions = _ptr(pos, C.c_float)
+        md.n_positions = pos.shape[0]
+        md.indices = _ptr(idx, C.c_int32)
+        md.n_triangles = idx.shape[0]
+        if m.normals is not None:
+            nrm = sb.hold(np.ascontiguousarray(m.normals, dtype=np.float32))
+            md.normals = _ptr(nrm, C.c_float)
+            md.n_normals = nrm.shape[0]
+        md.material = m.material
+    sb.hold(meshes)
+    d.meshes = meshes
+    d.n_meshes = len(scene.meshes)
+    quads = (QuadDesc * max(1, len(scene.quads)))()
+    for i, q in enumerate(scene.quads):
+        quads[i] = QuadDesc(q[0], *[float(x) for x in q[1:6]], q[6], q[7] if len(q) > 7 else 0)
+    sb.hold(quads)
+    d.quads = quads
+    d.n_quads = len(scene.quads)
+    spheres = (SphereDesc * max(1, len(scene.spheres)))()
+    for i, s in enumerate(scene.spheres):
+        sd = spheres[i]
+        sd.center[:] = [float(x) for x in s[0]]
+        sd.radius = float(s[1])
+        sd.material = s[2]
+        sd.flip_face = s[3] if len(s) > 3 else 0
+    sb.hold(spheres)
+    d.spheres = spheres
+    d.n_spheres = len(scene.spheres)
+    objs = (ObjectDesc * max(1, len(scene.objects)))(*[ObjectDesc(k, i) for k, i in scene.objects])
+    sb.hold(objs)
+    d.objects = objs
+    d.n_objects = len(scene.objects)
+    if scene.env is not None:
+        tex = sb.hold(np.ascontiguousarray(scene.env, dtype=np.float32))
+        ed = EnvDesc(_ptr(tex, C.c_float), tex.shape[1], tex.shape[0], float(scene.env_intensity))
+        sb.hold(ed)
+        d.env = C.pointer(ed)
+    if scene.medium is not None:
+        sa, ss, g = scene.medium
+        md = MediumDesc((C.c_float * 3)(*sa), (C.c_float * 3)(*ss), float(g))
+        sb.hold(md)
+        d.medium = C.pointer(md)
+    d.bg_color[:] = [float(x) for x in scene.bg]
+    return sb
+
+
+def job_desc(scene_id: int, cam, width: int, height: int, spp_x: int, spp_y: int, max_depth: int,
+             estimator: int = EST_REF_NEE, sampler: int = SAMPLER_HALTON_OWEN, rr_start: int = -1,
+             env_sampling: int = ENV_UNIFORM, seed: int = 0, spp_begin: int = 0, spp_end: int = 0,
+             light_samples=(2, 2), sampler_seed: int = 0, gamma: float = 2.0) -> JobDesc:
+    j = JobDesc()
+    j.scene = scene_id
+    j.width, j.height = width, height
+    j.spp_x, j.spp_y = spp_x, spp_y
+    j.spp_begin, j.spp_end = spp_begin, spp_end
+    j.max_depth = max_depth
+    j.rr_start = rr_start
+    j.estimator = estimator
+    j.sampler = sampler
+    j.env_sampling = env_sampling
+    j.light_samples_x, j.light_samples_y = light_samples
+    j.seed = seed
+    j.sampler_seed = sampler_seed
+    j.camera = camera_desc(cam)
+    j.gamma = gamma
+    return j
+
+
+def camera_desc(cam) -> CameraDesc:
+    c = CameraDesc()
+    c.fov = float(cam["fov"])
+    c.aspect = float(cam["aspect"])
+    c.focal_dist = float(cam["focal_dist"])
+    c.aperture = float(cam["aperture"])
+    c.up[:] = [float(x) for x in cam["up"]]
+    c.front[:] = [float(x) for x in cam["front"]]
+    c.position[:] = [float(x) for x in cam["position"]]
+    c.shutter = float(cam.get("shutter", 0.0))
+    return c
+
+
+class Renderer:
+    """A pt_context on one CUDA device."""
+
+    def __init__(self, device: int = 0):
+        self.lib = load()
+        self.ctx = C.c_void_p()
+        self._check(self.lib.pt_create(C.byref(self.ctx), device), None)
+
+    def close(self):
+        if self.ctx:
+            self.lib.pt_destroy(self.ctx)
+            self.ctx = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc: int, ctx=-1):
+        if rc != PT_OK:
+            buf = C.create_string_buffer(512)
+            self.lib.pt_last_error(self.ctx if ctx == -1 else ctx, buf, 512)
+            raise PtError(rc, buf.value.decode())
+
+    # -- scenes
+    def upload(self, scene) -> int:
+        sb = make_scene_desc(scene)
+        sid = C.c_int32()
+        self._check(self.lib.pt_scene_upload(self.ctx, C.byref(sb.desc), C.byref(sid)))
+        return sid.value
+
+    def release(self, sid: int):
+        self._check(self.lib.pt_scene_release(self.ctx, sid))
+
+    def scene_info(self, sid: int):
+        out = (C.c_int64 * 6)()
+        self._check(self.lib.pt_scene_info(self.ctx, sid, out))
+        return dict(zip(["triangles", "quads", "spheres", "bvh4_nodes", "lights", "device_bytes"], list(out)))
+
+    # -- rendering
+    def render(self, job: JobDesc, stats: bool = False):
+        film = np.zeros((job.height, job.width, 3), np.float32)
+        st = Stats()
+        self._check(self.lib.pt_render(self.ctx, C.byref(job), _ptr(film, C.c_float), C.byref(st)))
+        return (film, st) if stats else film
+
+    def render_device(self, job: JobDesc, d_film_ptr: int, sync: bool = False, stats: bool = False):
+        st = Stats()
+        self._check(self.lib.pt_render_device(self.ctx, C.byref(job), C.c_void_p(d_film_ptr), int(sync),
+                                              C.byref(st) if stats else None))
+        return st
+
+    def tonemap(self, film: np.ndarray, gamma: float = 2.0) -> np.ndarray:
+        film = np.ascontiguousarray(film, dtype=np.float32)
+        h, w = film.shape[:2]
+        out = np.zeros((h, w, 3), np.uint8)
+        self._check(self.lib.pt_tonemap(self.ctx, _ptr(film, C.c_float), w, h, gamma, _ptr(out, C.c_uint8)))
+        return out
+
+    # -- batch test entry points
+    def sampler_eval(self, strategy: int, first_index: int, n: int, dims: int, seed: int = 0) -> np.ndarray:
+        out = np.zeros((n, dims), np.float32)
+        self._check(self.lib.pt_sampler_eval(self.ctx, strategy, seed, first_index, n, dims,
+                                             _ptr(out, C.c_float)))
+        return out
+
+    def trace_closest(self, sid: int, rays: np.ndarray, tmin: float = 1e-4, tmax: float = 1e5):
+        rays = np.ascontiguousarray(rays, dtype=np.float32)
+        n = rays.shape[0]
+        t = np.zeros(n, np.float32)
+        prim = np.zeros(n, np.int32)
+        uv = np.zeros((n, 2), np.float32)
+        self._check(self.lib.pt_trace_closest(self.ctx, sid, _ptr(rays, C.c_float), n, tmin, tmax,
+                                              _ptr(t, C.c_float), _ptr(prim, C.c_int32), _ptr(uv, C.c_float)))
+        return t, prim, uv
+
+    def trace_any(self, sid: int, rays: np.ndarray, tmax: np.ndarray, tmin: float = 1e-3):
+        rays = np.ascontiguousarray(rays, dtype=np.float32)
+        tmax = np.ascontiguousarray(tmax, dtype=np.float32)
+        occ = np.zeros(rays.shape[0], np.uint8)
+        self._check(self.lib.pt_trace_any(self.ctx, sid, _ptr(rays, C.c_float), _ptr(tmax, C.c_float),
+                                          rays.shape[0], tmin, _ptr(occ, C.c_uint8)))
+        return occ
+
+    def bsdf_eval(self, mat: MaterialDesc, wo, wi, normal, front):
+        wo, wi, normal = (np.ascontiguousarray(a, dtype=np.float32) for a in (wo, wi, normal))
+        front = np.ascontiguousarray(front, dtype=np.uint8)
+        n = wo.shape[0]
+        f = np.zeros((n, 3), np.float32)
+        pdf = np.zeros(n, np.float32)
+        self._check(self.lib.pt_bsdf_eval(self.ctx, C.byref(mat), n, _ptr(wo, C.c_float), _ptr(wi, C.c_float),
+                                          _ptr(normal, C.c_float), _ptr(front, C.c_uint8), _ptr(f, C.c_float),
+                                          _ptr(pdf, C.c_float)))
+        return f, pdf
+
+    def bsdf_sample(self, mat: MaterialDesc, wo, normal, front, uc, u):
+        wo, normal, uc, u = (np.ascontiguousarray(a, dtype=np.float32) for a in (wo, normal, uc, u))
+        front = np.ascontiguousarray(front, dtype=np.uint8)
+        n = wo.shape[0]
+        ok = np.zeros(n, np.uint8)
+        wi = np.zeros((n, 3), np.float32)
+        att = np.zeros((n, 3), np.float32)
+        pdf = np.zeros(n, np.float32)
+        ty = np.zeros(n, np.uint32)
+        self._check(self.lib.pt_bsdf_sample(self.ctx, C.byref(mat), n, _ptr(wo, C.c_float), _ptr(normal, C.c_float),
+                                            _ptr(front, C.c_uint8), _ptr(uc, C.c_float), _ptr(u, C.c_float),
+                                            _ptr(ok, C.c_uint8), _ptr(wi, C.c_float), _ptr(att, C.c_float),
+                                            _ptr(pdf, C.c_float), _ptr(ty, C.c_uint32)))
+        return ok.astype(bool), wi, att, pdf, ty

@@ -1,0 +1,146 @@
+"""Writes the golden fixtures of tests/golden/ by running the REFERENCE itself.
+
+Run in a container that has the reference sources, after
+``oracle/ref/build_ref.sh`` built ``oracle/_ref/libref_harness.so``:
+
+    python tests/golden/make_golden.py
+
+Every array written here comes out of the reference's own code (the
+HaltonSampler class, BVHNode/MeshBVHNode/AARectangle/Sphere intersection,
+Material::f / scatter_pdf / scatter, and getRayColor of
+include/integrator/maxdepth_nee.hpp), driven through the harness in
+oracle/ref/ref_harness.cpp.  Inputs are seeded, so the script is
+reproducible.
+"""
+from __future__ import annotations
+
+import math
+import sys
+from pathlib import Path
+
+import numpy as np
+
+REPO = Path(__file__).resolve().parents[2]
+sys.path.insert(0, str(REPO))
+
+from oracle.ref import refbind as R  # noqa: E402
+from pathtracer_gb300 import native as N  # noqa: E402
+from pathtracer_gb300 import scene as S  # noqa: E402
+
+OUT = Path(__file__).resolve().parent
+
+# Material parameter sets exercised by the BSDF fixtures: (name, type, params, flags)
+MATERIALS = [
+    ("lambertian", N.LAMBERTIAN, [0.63, 0.065, 0.05], 0),
+    ("conductor_gold_a03", N.CONDUCTOR, [*S.GOLD_ETA, *S.GOLD_K, 0.3, 0.3], 0),
+    ("conductor_silver_aniso", N.CONDUCTOR, [*S.SILVER_ETA, *S.SILVER_K, 0.05, 0.4], 0),
+    ("conductor_smooth", N.CONDUCTOR, [*S.GOLD_ETA, *S.GOLD_K, 1e-4, 1e-4], 0),
+    ("mfdielectric_a005", N.MF_DIELECTRIC, [1.5, 0.05, 0.05], 0),
+    ("mfdielectric_a04", N.MF_DIELECTRIC, [1.33, 0.4, 0.2], 0),
+    ("mfdielectric_smooth", N.MF_DIELECTRIC, [1.5, 0.0, 0.0], 0),
+    ("thindielectric", N.THIN_DIELECTRIC, [1.5], 0),
+    ("phong", N.PHONG, [0.5, 0.3, 0.2, 0.4, 0.4, 0.4, 0.0, 0.0, 0.0, 30.0], 0),
+    ("disney_a", N.DISNEY, [0.8, 0.3, 0.2, 0.3, 0.2, 0.5, 0.5, 0.4, 0.5, 0.3, 0.6, 0.5, 0.7, 0.4, 1.45], 0),
+    ("disney_b", N.DISNEY, [0.2, 0.6, 0.9, 0.0, 0.9, 0.0, 0.5, 0.15, 0.0, 0.8, 0.0, 0.0, 1.0, 0.9, 1.3], 0),
+    ("disney_c", N.DISNEY, [0.5, 0.5, 0.5, 0.9, 0.1, 0.2, 0.3, 0.6, 0.2, 0.0, 0.9, 0.9, 0.1, 0.5, 1.6], 0),
+    ("hair_a", N.HAIR, [0.419, 0.697, 1.37, 0.1, 1.55, 0.3, 0.3, math.radians(2.0)], 0),
+    ("hair_b", N.HAIR, [0.06, 0.1, 0.2, -0.4, 1.55, 0.15, 0.45, math.radians(3.0)], 0),
+    ("emitter", N.DIFFUSE_EMITTER, [17.0, 12.0, 4.0, 1.0], 0),
+]
+
+
+def unit(v):
+    return v / np.linalg.norm(v, axis=-1, keepdims=True)
+
+
+def bsdf_inputs(n, rng):
+    nrm = unit(rng.normal(size=(n, 3)))
+    # wo in the upper hemisphere of n (the integrator turns n towards the ray)
+    wo = unit(rng.normal(size=(n, 3)))
+    wo = np.where((np.sum(wo * nrm, 1) < 0)[:, None], -wo, wo)
+    wi = unit(rng.normal(size=(n, 3)))
+    # half of the wi in the upper hemisphere, half anywhere (transmission)
+    up = rng.uniform(size=n) < 0.5
+    wi = np.where((up & (np.sum(wi * nrm, 1) < 0))[:, None], -wi, wi)
+    front = (rng.uniform(size=n) < 0.5).astype(np.uint8)
+    uc = rng.uniform(size=n).astype(np.float32)
+    u = rng.uniform(size=(n, 2)).astype(np.float32)
+    return [a.astype(np.float32) for a in (wo, wi, nrm)] + [front, uc, u]
+
+
+def make_samplers():
+    out = {}
+    for name, strat, seed in [("none", N.SAMPLER_HALTON_NONE, 0), ("permute", N.SAMPLER_HALTON_PERMUTE, 0),
+                              ("permute7", N.SAMPLER_HALTON_PERMUTE, 7), ("owen", N.SAMPLER_HALTON_OWEN, 0)]:
+        blocks = []
+        for first, n in [(1, 512), (123457, 128), (100_000_000, 128), (4_000_000_000, 64)]:
+            blocks.append(R.sampler_eval(strat, first, n, 25, seed))
+            out[f"{name}_first_{first}"] = blocks[-1]
+    np.savez_compressed(OUT / "samplers.npz", **out)
+
+
+def cornell_rays(n, rng, cam):
+    # camera-like rays from the eye plus rays from random points in the box
+    o1 = np.tile(np.array(cam["position"], np.float32), (n // 2, 1))
+    tgt = np.stack([rng.uniform(0, 1, n // 2), rng.uniform(0, 1, n // 2), np.ones(n // 2)], 1)
+    d1 = unit(tgt - o1)
+    o2 = rng.uniform(0.02, 0.98, size=(n - n // 2, 3))
+    d2 = unit(rng.normal(size=(n - n // 2, 3)))
+    rays = np.concatenate([np.concatenate([o1, d1], 1), np.concatenate([o2, d2], 1)], 0)
+    return rays.astype(np.float32)
+
+
+def make_trace():
+    rng = np.random.default_rng(11)
+    sc, cam = S.cornell_icosphere(4)
+    rs = R.RefScene(sc)
+    rays = cornell_rays(4096, rng, cam)
+    t, prim, pos, nrm, front = rs.trace_closest(rays)
+    # shadow-ray intervals (maxdepth_nee.hpp:165-166): [0.001, len - 0.001]
+    tmax = rng.uniform(0.05, 1.5, size=rays.shape[0]).astype(np.float32)
+    occ = np.zeros(rays.shape[0], np.uint8)
+    for j in range(rays.shape[0]):
+        _, pp, _, _, _ = rs.trace_closest(rays[j:j + 1], tmin=0.001, tmax=float(tmax[j]))
+        occ[j] = 1 if pp[0] >= 0 else 0
+    np.savez_compressed(OUT / "trace_cornell.npz", rays=rays, t=t, prim=prim, pos=pos, nrm=nrm, front=front,
+                        shadow_tmax=tmax, occluded=occ)
+
+
+def make_bsdf():
+    rng = np.random.default_rng(5)
+    out = {}
+    for name, mtype, params, flags in MATERIALS:
+        mat = N.material(mtype, params, flags)
+        wo, wi, nrm, front, uc, u = bsdf_inputs(384, rng)
+        f, pdf = R.bsdf_eval(mat, wo, wi, nrm, front)
+        ok, swi, att, spdf, ty = R.bsdf_sample(mat, wo, nrm, front, uc, u)
+        out[name] = dict(type=mtype, flags=flags, params=np.array(params, np.float32), wo=wo, wi=wi, nrm=nrm,
+                         front=front, uc=uc, u=u, f=f, pdf=pdf, ok=ok, s_wi=swi, s_att=att, s_pdf=spdf, s_type=ty)
+    flat = {f"{k}__{kk}": vv for k, v in out.items() for kk, vv in v.items()}
+    np.savez_compressed(OUT / "bsdf.npz", **flat)
+
+
+def make_images():
+    # Cornell box + GGX gold icosphere, the reference integrator, 64 spp.
+    sc, cam = S.cornell_icosphere(4)
+    rs = R.RefScene(sc)
+    job = N.job_desc(0, cam, 64, 64, 8, 8, 8, seed=3)
+    mean, var = rs.render(job)
+    np.savez_compressed(OUT / "image_cornell.npz", mean=mean, var=var, width=64, height=64, spp=64, depth=8)
+    # Rough glass over a conductor ground, HDRI environment (small sizes).
+    sc, cam = S.rough_glass(subdiv=3, env_w=128, env_h=64, seed=2)
+    rs = R.RefScene(sc)
+    job = N.job_desc(0, cam, 48, 48, 4, 4, 6, seed=4)
+    mean, var = rs.render(job)
+    np.savez_compressed(OUT / "image_roughglass.npz", mean=mean, var=var, width=48, height=48, spp=16, depth=6)
+
+
+if __name__ == "__main__":
+    if not R.available():
+        raise SystemExit("build oracle/_ref first: oracle/ref/build_ref.sh")
+    make_samplers()
+    make_trace()
+    make_bsdf()
+    make_images()
+    for p in sorted(OUT.glob("*.npz")):
+        print(p.name, p.stat().st_size)
