@@ -63,6 +63,7 @@ PT_HD float logistic_(float x, float s) {
 PT_HD float logistic_cdf(float x, float s) { return 1.f / (1.f + expf(-x / s)); }
 PT_HD float hair_Np(float phi, int p, float s, float go, float gt) {
   float dphi = phi - hair_Phi(p, go, gt);
+  if (!(fabsf(dphi) < 1e4f)) return 0.f;  // bounds the wrap loops below
   while (dphi > (float)PT_PI) dphi -= 2.f * (float)PT_PI;
   while (dphi < -(float)PT_PI) dphi += 2.f * (float)PT_PI;
   const float a = -(float)PT_PI, b = (float)PT_PI;
