@@ -1,0 +1,357 @@
+"""Benchmark of the wavefront path integrator (one JSON line on rank 0).
+
+Workload (default): the rough-glass scene -- a seeded displaced icosphere of
+1,310,720 triangles (subdivision 8, radial noise 0.05) in rough glass (ior
+1.5, alpha 0.05) over a GGX conductor ground (alpha 0.2), lit by a seeded
+1024x512 FP32 HDRI (sky gradient + 3 Gaussian sun lobes, peak 5e3), rendered
+at 1024x1024, 256 spp (16x16 grid), depth 16, Russian roulette from depth 4,
+NEE+MIS with the luminance alias table, Owen-scrambled Halton sampler.
+One step = 16 of the 256 samples per pixel for every pixel (16.8 M paths).
+
+  value  paths/s with the scene resident in HBM, device film, device time
+         (CUDA events on the library's stream, max over ranks);
+  e2e    the same metric through the public C-ABI call pt_render with a
+         pinned HOST film: the job descriptor and offset table go host->device
+         and the 12.6 MB film device->host inside every step.
+
+``--impl reference`` times the reference algorithm on the host cores: the
+CPU restatement of the reference integrator (oracle/pt_oracle.cpp, REF_NEE,
+all hardware threads) on a bounded sample of the same workload.
+
+Multi-GPU (torchrun): the path is sample-parallel, every rank renders its own
+sample range of the same frame (replicas, no collective on the data path);
+``value`` = all ranks' paths / max-over-ranks time (weak scaling).
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+REPO = Path(__file__).resolve().parent
+sys.path.insert(0, str(REPO))
+
+import numpy as np  # noqa: E402
+
+PEAKS = REPO / "MEASURED_PEAKS.json"
+FALLBACK_HBM_GBS = 6800.0
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=8)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="rough_glass", choices=["rough_glass", "cornell", "divergence"])
+    ap.add_argument("--spp-per-step", type=int, default=16)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+WORKLOADS = {
+    # name: (width, height, spp_x, spp_y, depth, rr_start, estimator, sampler, env_sampling, description)
+    "rough_glass": dict(W=1024, H=1024, sx=16, sy=16, depth=16, rr=4, est=1, sampler=2, env=1,
+                        desc="rough-glass displaced icosphere (1,310,720 tris) + conductor ground + "
+                             "1024x512 HDRI, 1024x1024, 256 spp, depth 16, RR from 4"),
+    "cornell": dict(W=256, H=256, sx=8, sy=8, depth=8, rr=-1, est=1, sampler=2, env=0,
+                    desc="Cornell box + 5120-tri GGX gold icosphere, 256x256, 64 spp, depth 8"),
+    "divergence": dict(W=1920, H=1080, sx=16, sy=8, depth=12, rr=-1, est=1, sampler=3, env=0,
+                       desc="64 icospheres x 20480 tris, 5 material families, homogeneous medium, "
+                            "1920x1080, 128 spp, depth 12, stratified"),
+}
+
+
+def build_scene(name):
+    from pathtracer_gb300 import scene as S
+
+    if name == "rough_glass":
+        return S.rough_glass(8)
+    if name == "cornell":
+        return S.cornell_icosphere(4)
+    return S.material_divergence(5)
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle-reason sampling during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            p = [x.strip() for x in ln.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                mx = max(mx, float(p[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, p[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_paths_per_sec(osc, cam, wl, estimator, threads, target_s=12.0, max_px=1024):
+    """Times the CPU restatement of the reference integrator on a bounded
+    sample (a square crop-free frame of up to max_px^2 pixels at 1 spp of
+    the workload's sample grid), sized to about target_s of CPU work."""
+    from pathtracer_gb300 import native as N
+
+    res = 64
+    # calibrate the sample size to about target_s of CPU work
+    while True:
+        job = N.job_desc(0, cam, res, res, wl["sx"], wl["sy"], wl["depth"], estimator=estimator,
+                         sampler=wl["sampler"], rr_start=wl["rr"], env_sampling=0 if estimator == 0 else wl["env"],
+                         seed=7, spp_begin=0, spp_end=1)
+        t0 = time.perf_counter()
+        osc.render(job, threads=threads)
+        dt = time.perf_counter() - t0
+        if dt > target_s / 4 or res >= max_px:
+            break
+        res = min(max_px, int(res * max(1.5, min(4.0, (target_s / 4 / max(dt, 1e-3)) ** 0.5))))
+    t0 = time.perf_counter()
+    osc.render(job, threads=threads)
+    dt = time.perf_counter() - t0
+    return res * res / dt, f"{res}x{res} pixels x 1 spp of the workload's scene and camera", dt
+
+
+def run_reference(args, rank, world):
+    wl = WORKLOADS[args.workload]
+    if rank != 0:
+        return
+    from oracle import pyoracle as O
+
+    sc, cam = build_scene(args.workload)
+    osc = O.OracleScene(sc)
+    threads = os.cpu_count() or 1
+    vals = []
+    sample = ""
+    for i in range(args.warmup + args.steps):
+        v, sample, _ = cpu_paths_per_sec(osc, cam, wl, 0, threads,
+                                         target_s=max(4.0, 90.0 / (args.steps + args.warmup)))
+        if i >= args.warmup:
+            vals.append(v)
+    value = statistics.median(vals)
+    line = {
+        "impl": "reference", "metric": "paths/s", "value": value, "unit": "paths/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene generator)",
+        "config": {"workload": wl["desc"], "estimator": "REF_NEE (maxdepth_nee.hpp restated)"},
+        "cpu_baseline": {"value": value, "unit": "paths/s", "cores": threads, "kind": "port",
+                         "sample": sample + "; oracle/pt_oracle.cpp, the CPU restatement of the reference path"},
+        "e2e": {"value": value, "unit": "paths/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, rank, world, local_rank):
+    import torch
+
+    from pathtracer_gb300 import native as N
+
+    wl = WORKLOADS[args.workload]
+    torch.cuda.set_device(local_rank)
+    r = N.Renderer(local_rank)
+    sc, cam = build_scene(args.workload)
+    sid = r.upload(sc)
+    info = r.scene_info(sid)
+    W, H = wl["W"], wl["H"]
+    spp_total = wl["sx"] * wl["sy"]
+    k = args.spp_per_step
+
+    def job_for(step):
+        # each rank takes its own sample range of the frame; steps cycle
+        # through the frame's spp_total samples
+        chunk = (step * world + rank) % max(1, spp_total // k)
+        return N.job_desc(sid, cam, W, H, wl["sx"], wl["sy"], wl["depth"], rr_start=wl["rr"],
+                          estimator=wl["est"], sampler=wl["sampler"], env_sampling=wl["env"], seed=1,
+                          spp_begin=chunk * k, spp_end=chunk * k + k)
+
+    film = torch.zeros(H * W * 3, dtype=torch.float32, device=f"cuda:{local_rank}")
+    dist = world > 1
+
+    def barrier():
+        torch.cuda.synchronize()
+        if dist:
+            torch.distributed.barrier()
+
+    # ---- device-resident timing (value)
+    for i in range(args.warmup):
+        r.render_device(job_for(i), film.data_ptr(), sync=True)
+    barrier()
+    r.profile_begin()
+    stats = N.Stats()
+    tot = dict(paths=0, segments=0, rays=0, shadow=0, bytes=0)
+    t_dev = 0.0
+    with ClockSampler(local_rank) as clk:
+        barrier()
+        w0 = time.perf_counter()
+        for i in range(args.steps):
+            st = r.render_device(job_for(args.warmup + i), film.data_ptr(), sync=False, stats=True)
+            t_dev += st.ms
+            tot["paths"] += st.paths
+            tot["segments"] += st.segments
+            tot["rays"] += st.rays
+            tot["shadow"] += st.shadow_rays
+            tot["bytes"] += st.algorithmic_bytes
+        barrier()
+        wall = time.perf_counter() - w0
+    prof = r.profile_end()
+    del stats
+    t_max = t_dev / 1e3
+    paths_all = tot["paths"]
+    if dist:
+        tt = torch.tensor([t_max], device=f"cuda:{local_rank}", dtype=torch.float64)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        t_max = float(tt.item())
+        pt = torch.tensor([paths_all], device=f"cuda:{local_rank}", dtype=torch.float64)
+        torch.distributed.all_reduce(pt)
+        paths_all = int(pt.item())
+    value = paths_all / t_max
+
+    # ---- end-to-end through pt_render with a pinned host film
+    host = torch.empty((H, W, 3), dtype=torch.float32, pin_memory=True)
+    hp = host.numpy()
+    lib = N.load()
+    e2e_steps = max(2, args.steps // 2)
+    job = job_for(0)
+    lib.pt_render(r.ctx, C.byref(job), hp.ctypes.data_as(C.POINTER(C.c_float)), None)
+    barrier()
+    e0 = time.perf_counter()
+    e2e_paths = 0
+    for i in range(e2e_steps):
+        job = job_for(args.warmup + i)
+        rc = lib.pt_render(r.ctx, C.byref(job), hp.ctypes.data_as(C.POINTER(C.c_float)), None)
+        if rc != 0:
+            raise RuntimeError(f"pt_render failed: {rc}")
+        e2e_paths += W * H * k
+    barrier()
+    e2e_t = time.perf_counter() - e0
+    e2e_val = e2e_paths / e2e_t
+    if dist:
+        tt = torch.tensor([e2e_t], device=f"cuda:{local_rank}", dtype=torch.float64)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        e2e_val = e2e_paths * world / float(tt.item())
+    h2d = C.sizeof(N.JobDesc) + spp_total * 8
+    d2h = W * H * 3 * 4
+
+    if rank != 0:
+        return
+    # ---- roofline of the dominant kernel (CUDA events on the library stream)
+    dom = max(("trace", "shade", "shadow"), key=lambda s: prof[s][0])
+    peak = None
+    peak_src = "fallback"
+    if PEAKS.exists():
+        try:
+            peak = float(json.loads(PEAKS.read_text())["hbm_gbs"])
+            peak_src = "measured"
+        except (KeyError, ValueError):
+            peak = None
+    if peak is None:
+        peak = FALLBACK_HBM_GBS
+    # algorithmic bytes per unit (per ray for the traversal stages, per path
+    # vertex for shade): queue records read and written
+    per_unit = {"trace": 48.0, "shadow": 44.0 * 2, "shade": 192.0}
+    units = {"trace": tot["rays"], "shadow": tot["shadow"], "shade": tot["segments"]}
+    dom_ms = prof[dom][0]
+    achieved = per_unit[dom] * units[dom] / (dom_ms / 1e3) / 1e9
+    launches = sum(v[1] for v in prof.values())
+    step_bytes_gbs = tot["bytes"] / (t_dev / 1e3) / 1e9
+    line = {
+        "metric": "paths/s", "value": value, "unit": "paths/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t_dev / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene generator, no assets)",
+        "config": {"workload": wl["desc"], "step": f"{k} spp x {W}x{H} px = {W * H * k} paths",
+                   "estimator": "NEE+MIS", "triangles": info["triangles"], "bvh4_nodes": info["bvh4_nodes"],
+                   "l2": "inputs larger than L2: BVH + leaves "
+                         f"{info['device_bytes'] / 1e6:.0f} MB and ~{tot['bytes'] / args.steps / 1e9:.1f} GB of "
+                         "queue traffic per step (L2 129 MB)",
+                   "parallelism": f"replicas x{world} (sample ranges per rank)"},
+        "rays_per_s": (tot["rays"] + tot["shadow"]) * world / t_max,
+        "e2e": {"value": e2e_val, "unit": "paths/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "gpu_launches": int(launches),
+        "roofline": {"bound": "hbm", "kernel": f"k_{'trace_closest' if dom == 'trace' else 'trace_shadow' if dom == 'shadow' else 'shade'}",
+                     "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_source": peak_src, "traffic": None,
+                     "note": f"stage share {prof[dom][0] / sum(v[0] for v in prof.values()):.2f}; "
+                             f"whole-step queue bytes {step_bytes_gbs:.1f} GB/s"},
+        "stage_ms": {kk: round(v[0], 3) for kk, v in prof.items()},
+        "clocks": clk.summary(),
+        "wall_s": wall,
+    }
+    if not args.no_cpu_baseline:
+        from oracle import pyoracle as O
+
+        threads = os.cpu_count() or 1
+        v, sample, dt = cpu_paths_per_sec(O.OracleScene(sc), cam, wl, 0, threads)
+        line["cpu_baseline"] = {"value": v, "unit": "paths/s", "cores": threads, "kind": "port",
+                                "sample": sample + f" ({dt:.1f} s); REF_NEE restatement oracle/pt_oracle.cpp"}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+    if world > 1:
+        import torch
+
+        torch.cuda.set_device(local_rank)
+        torch.distributed.init_process_group("nccl")
+    run_ours(args, rank, world, local_rank)
+    if world > 1:
+        import torch
+
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

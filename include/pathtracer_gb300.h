@@ -263,6 +263,15 @@ int pt_render(void *ctx, const pt_job_desc *job, float *film_rgb,
 int pt_render_device(void *ctx, const pt_job_desc *job, float *d_film_sum,
                      int sync, pt_stats *stats);
 
+/* Per-stage device timing of the wave kernels (no counterpart in the
+ * reference, which times only the whole render, renderManager.hpp:164-173).
+ * pt_profile_begin clears and enables CUDA-event timing on the context's
+ * stream; pt_profile_end synchronises and returns, per stage (0 camera,
+ * 1 closest-hit trace, 2 material sort, 3 shade, 4 shadow trace, 5 film),
+ * the summed milliseconds and the number of kernel launches. */
+int pt_profile_begin(void *ctx);
+int pt_profile_end(void *ctx, double *stage_ms /*[6]*/, int64_t *stage_launches /*[6]*/);
+
 /* FrameBuffer::writeToFile pixel path (framebuffer.cpp:27-58): NaN -> 0,
  * pow(c, 1/gamma), clamp [0,1], *255 truncated to u8, rows flipped so that
  * row 0 of rgb8 is the top of the image.  Host buffers. */

@@ -729,6 +729,7 @@ Context::~Context() {
   if (d_offsets) cudaFree(d_offsets);
   if (d_scratch) cudaFree(d_scratch);
   if (d_err) cudaFree(d_err);
+  for (cudaEvent_t e : prof.pool) cudaEventDestroy(e);
   if (stream) cudaStreamDestroy(stream);
 }
 
@@ -899,7 +900,7 @@ void Context::render_device(const pt_job_desc &j, float *d_film, pt_stats *stats
   cudaEventRecord(e0, stream);
   for (long long g0 = 0; g0 < total; g0 += n) {
     int cnt = (int)std::min<long long>(n, total - g0);
-    launch_wave(S->view, J, Q, g0, cnt, d_film, cfg, stream);
+    launch_wave(S->view, J, Q, g0, cnt, d_film, cfg, stream, &prof);
   }
   cudaEventRecord(e1, stream);
   cuda_check(cudaGetLastError(), "launch");
@@ -1006,6 +1007,39 @@ int pt_last_error(void *ctx, char *buf, size_t n) {
   }
   std::snprintf(buf, n, "%s", m.c_str());
   return PT_OK;
+}
+
+int pt_profile_begin(void *ctx) {
+  Context *c = static_cast<Context *>(ctx);
+  PT_GUARD(c, {
+    c = as_ctx(ctx);
+    cuda_check(cudaStreamSynchronize(c->stream), "sync");
+    c->prof.used = 0;
+    c->prof.kinds.clear();
+    c->prof.on = true;
+  });
+}
+
+int pt_profile_end(void *ctx, double *stage_ms, int64_t *stage_launches) {
+  Context *c = static_cast<Context *>(ctx);
+  PT_GUARD(c, {
+    c = as_ctx(ctx);
+    cuda_check(cudaStreamSynchronize(c->stream), "sync");
+    for (int k = 0; k < STAGE_COUNT; ++k) {
+      if (stage_ms) stage_ms[k] = 0.0;
+      if (stage_launches) stage_launches[k] = 0;
+    }
+    for (size_t i = 0; i < c->prof.kinds.size(); ++i) {
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, c->prof.pool[2 * i], c->prof.pool[2 * i + 1]);
+      const int k = c->prof.kinds[i];
+      if (stage_ms) stage_ms[k] += ms;
+      if (stage_launches) stage_launches[k] += (k == STAGE_SORT) ? 2 : 1;
+    }
+    c->prof.on = false;
+    c->prof.used = 0;
+    c->prof.kinds.clear();
+  });
 }
 
 int pt_scene_upload(void *ctx, const pt_scene_desc *desc, int32_t *scene_id) {

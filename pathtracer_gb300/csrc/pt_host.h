@@ -62,6 +62,7 @@ struct Context {
   void *d_scratch = nullptr;
   size_t scratch_cap = 0;
   int *d_err = nullptr;
+  Profiler prof;
 
   explicit Context(int dev);
   ~Context();

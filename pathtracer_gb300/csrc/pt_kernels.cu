@@ -727,30 +727,44 @@ void launch_bsdf_sample(const MatRec *m, int n, const float *wo, const float *nr
 
 // One wave: camera, max_depth (+1 for MIS) bounces, film.
 void launch_wave(const SceneView &S, const DeviceJob &J, const Queues &Q, long long g0, int n,
-                 float *film, const LaunchCfg &cfg, cudaStream_t st) {
+                 float *film, const LaunchCfg &cfg, cudaStream_t st, Profiler *prof) {
   const int LN = J.job.light_nx * J.job.light_ny;
   const int bounces = J.job.max_depth + (J.job.estimator == PT_EST_NEE_MIS ? 1 : 0);
+  Profiler dummy;
+  Profiler &P = prof ? *prof : dummy;
+  P.begin(STAGE_CAMERA, st);
   k_camera<<<grid_for(n, 256, cfg.max_blocks_simple), 256, 0, st>>>(J, Q, g0, n);
+  P.end(st);
   int qsel = 0;
   for (int b = 0; b < bounces; ++b) {
     // reset next-queue and shadow counters (device side, graph friendly)
     cudaMemsetAsync(Q.counts + (qsel ^ 1), 0, sizeof(int), st);
     cudaMemsetAsync(Q.counts + 2, 0, sizeof(int), st);
+    P.begin(STAGE_TRACE, st);
     k_trace_closest<<<cfg.trace_blocks, 128, 0, st>>>(S, Q, qsel);
+    P.end(st);
     int use_order = 0;
     if (cfg.sort_by_material) {
       cudaMemsetAsync(Q.bins, 0, sizeof(int) * 2 * PT_SORT_BINS, st);
+      P.begin(STAGE_SORT, st);
       k_sort_hist<<<cfg.max_blocks_simple, 256, 0, st>>>(S, Q, qsel);
       k_sort_scatter<<<cfg.max_blocks_simple, 256, 0, st>>>(Q, qsel);
+      P.end(st);
       use_order = 1;
     }
+    P.begin(STAGE_SHADE, st);
     k_shade<<<cfg.shade_blocks, 128, 0, st>>>(S, J, Q, qsel, b, g0, use_order);
+    P.end(st);
+    P.begin(STAGE_SHADOW, st);
     k_trace_shadow<<<cfg.trace_blocks, 128, 0, st>>>(S, Q, LN);
+    P.end(st);
     qsel ^= 1;
   }
+  P.begin(STAGE_FILM, st);
   k_film<<<grid_for((int)std::min<long long>((long long)J.job.width * J.job.height, 1 << 30), 256,
                     cfg.max_blocks_simple),
            256, 0, st>>>(J, Q, g0, n, film);
+  P.end(st);
 }
 
 void launch_tonemap(const float *film, int W, int H, float gamma, uint8_t *out, cudaStream_t st) {

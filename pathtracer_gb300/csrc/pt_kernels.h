@@ -3,6 +3,7 @@
 #pragma once
 #include <cuda_runtime.h>
 #include <cstdint>
+#include <vector>
 #include "../../include/pathtracer_gb300.h"
 #include "pt_scene.cuh"
 
@@ -40,6 +41,32 @@ struct LaunchCfg {
   int sort_by_material;
 };
 
+// Per-stage CUDA-event timing of the wave kernels (pt_profile_begin/end).
+enum StageKind { STAGE_CAMERA = 0, STAGE_TRACE, STAGE_SORT, STAGE_SHADE, STAGE_SHADOW, STAGE_FILM, STAGE_COUNT };
+struct Profiler {
+  bool on = false;
+  std::vector<cudaEvent_t> pool;
+  size_t used = 0;
+  std::vector<int> kinds;  // per begin/end event pair
+  cudaEvent_t take() {
+    if (used == pool.size()) {
+      cudaEvent_t e;
+      cudaEventCreate(&e);
+      pool.push_back(e);
+    }
+    return pool[used++];
+  }
+  void begin(int kind, cudaStream_t st) {
+    if (!on) return;
+    cudaEventRecord(take(), st);
+    kinds.push_back(kind);
+  }
+  void end(cudaStream_t st) {
+    if (!on) return;
+    cudaEventRecord(take(), st);
+  }
+};
+
 struct KernelInfo {
   int trace_regs, shade_regs;
   int trace_blocks_per_sm, shade_blocks_per_sm, shadow_blocks_per_sm;
@@ -57,7 +84,7 @@ void launch_bsdf_sample(const MatRec *m, int n, const float *wo, const float *nr
                         const uint8_t *front, const float *uc, const float *u, uint8_t *ok,
                         float *wi, float *att, float *pdf, uint32_t *type, cudaStream_t st);
 void launch_wave(const SceneView &S, const DeviceJob &J, const Queues &Q, long long g0, int n,
-                 float *film, const LaunchCfg &cfg, cudaStream_t st);
+                 float *film, const LaunchCfg &cfg, cudaStream_t st, Profiler *prof);
 void launch_tonemap(const float *film, int W, int H, float gamma, uint8_t *out, cudaStream_t st);
 void kernel_attributes(KernelInfo *info);
 

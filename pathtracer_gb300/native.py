@@ -31,7 +31,7 @@ ENV_UNIFORM, ENV_ALIAS = 0, 1
 # exported symbols of the C-ABI, in header order
 EXPORTS = [
     "pt_create", "pt_destroy", "pt_last_error", "pt_version", "pt_scene_upload", "pt_scene_release",
-    "pt_scene_info", "pt_render", "pt_render_device", "pt_tonemap", "pt_sampler_eval", "pt_trace_closest",
+    "pt_scene_info", "pt_render", "pt_render_device", "pt_profile_begin", "pt_profile_end", "pt_tonemap", "pt_sampler_eval", "pt_trace_closest",
     "pt_trace_any", "pt_bsdf_eval", "pt_bsdf_sample", "pt_render_batch", "pt_server_create",
     "pt_server_destroy", "pt_submit", "pt_server_step", "pt_poll", "pt_cancel",
 ]
@@ -139,6 +139,8 @@ def load() -> C.CDLL:
         "pt_scene_info": [vp, C.c_int32, C.POINTER(C.c_int64)],
         "pt_render": [vp, C.POINTER(JobDesc), f32p, C.POINTER(Stats)],
         "pt_render_device": [vp, C.POINTER(JobDesc), vp, C.c_int, C.POINTER(Stats)],
+        "pt_profile_begin": [vp],
+        "pt_profile_end": [vp, C.POINTER(C.c_double), C.POINTER(C.c_int64)],
         "pt_tonemap": [vp, f32p, C.c_int32, C.c_int32, C.c_float, u8p],
         "pt_sampler_eval": [vp, C.c_int32, C.c_uint32, C.c_uint32, C.c_int32, C.c_int32, f32p],
         "pt_trace_closest": [vp, C.c_int32, f32p, C.c_int32, C.c_float, C.c_float, f32p, i32p, f32p],
@@ -339,6 +341,17 @@ class Renderer:
         self._check(self.lib.pt_render_device(self.ctx, C.byref(job), C.c_void_p(d_film_ptr), int(sync),
                                               C.byref(st) if stats else None))
         return st
+
+    STAGES = ["camera", "trace", "sort", "shade", "shadow", "film"]
+
+    def profile_begin(self):
+        self._check(self.lib.pt_profile_begin(self.ctx))
+
+    def profile_end(self) -> dict:
+        ms = (C.c_double * 6)()
+        nl = (C.c_int64 * 6)()
+        self._check(self.lib.pt_profile_end(self.ctx, ms, nl))
+        return {k: (ms[i], nl[i]) for i, k in enumerate(self.STAGES)}
 
     def tonemap(self, film: np.ndarray, gamma: float = 2.0) -> np.ndarray:
         film = np.ascontiguousarray(film, dtype=np.float32)

@@ -118,7 +118,7 @@ def test_bsdf_sample_matches_reference(renderer, name):
     # a sample on the boundary of a branch may flip; allow a handful
     assert (ok == okr).mean() > 0.99
     m = ok & okr & (ty == G["s_type"])
-    assert m.mean() > 0.97
+    assert m.sum() >= 0.97 * okr.sum()
     assert np.abs(wi[m] - G["s_wi"][m]).max(initial=0) < 2e-3
     close = np.isclose(att[m], G["s_att"][m], rtol=1e-3, atol=1e-4).all(1) & \
         np.isclose(pdf[m], G["s_pdf"][m], rtol=1e-3, atol=1e-4)
