@@ -109,7 +109,15 @@ def test_bsdf_eval_matches_reference(renderer, name):
     assert rel_close(pdf, G["pdf"], rtol=1e-4, atol=1e-5), np.abs(pdf - G["pdf"]).max()
 
 
-@pytest.mark.parametrize("name", sorted(n for n in CASES if n != "phong"))
+def test_emitter_does_not_scatter(renderer):
+    # DiffuseEmitter::scatter returns false (material.hpp:475-481)
+    G = CASES["emitter"]
+    mat = N.material(int(G["type"]), G["params"], int(G["flags"]))
+    ok, *_ = renderer.bsdf_sample(mat, G["wo"], G["nrm"], G["front"], G["uc"], G["u"])
+    assert not ok.any() and not G["ok"].any()
+
+
+@pytest.mark.parametrize("name", sorted(n for n in CASES if n not in ("phong", "emitter")))
 def test_bsdf_sample_matches_reference(renderer, name):
     G = CASES[name]
     mat = N.material(int(G["type"]), G["params"], int(G["flags"]))
