@@ -519,6 +519,62 @@ PT_HD float bsdf_pdf(const MatRec &m, V3 wo, V3 wi, V3 n, bool front) {
   default: return 0.f;
   }
 }
+// ---------------------------------------------------- fused f + pdf (NEE)
+// The same values as bsdf_f / bsdf_pdf, sharing the frame, half vector,
+// D, G and Fresnel terms between the two.
+PT_HD void cond_eval(const MatRec &m, V3 wo, V3 wi, V3 n, V3 &f, float &pdf) {
+  f = v3(0.f);
+  pdf = 0.f;
+  TR d = cond_tr(m);
+  if (tr_smooth(d)) return;
+  Onb b = make_onb(n);
+  V3 wol = to_local(b, normalize(wo)), wil = to_local(b, normalize(wi));
+  if (wil.z <= 0.f) return;
+  V3 ml = normalize(wol + wil);
+  float D = tr_D(d, ml);
+  float c = fabsf(dot(wol, ml));
+  float den = 4.f * c;
+  if (den >= 1e-6f) pdf = tr_G1(d, wol) / fabsf(wol.z) * D * c / den;
+  if (wol.z <= 0.f) return;
+  float G = tr_G(d, wol, wil);
+  V3 F = fresnel_complex(c, m.p, m.p + 3);
+  f = F * (D * G / (4.f * fabsf(wol.z) * fabsf(wil.z)));
+}
+PT_HD void mfd_eval_local(float eta, TR d, V3 wol, V3 wil, V3 tint, bool tinted, V3 &f, float &pdf) {
+  f = v3(0.f);
+  pdf = 0.f;
+  float co = wol.z, ci = wil.z;
+  if (ci == 0.f || co == 0.f) return;
+  bool refl = ci * co > 0.f;
+  float etap = 1.f;
+  if (!refl) etap = co > 0.f ? eta : (1.f / eta);
+  V3 wm = wil * etap + wol;
+  if (length(wm) == 0.f) return;
+  wm = face_forward(normalize(wm), v3(0.f, 0.f, 1.f));
+  const float dwi = dot(wm, wil), dwo = dot(wm, wol);
+  if (dwi * ci < 0.f || dwo * co < 0.f) return;
+  const float F = fresnel_dielectric(dwo, eta), R = F, T = 1.f - F;
+  const float D = tr_D(d, wm), G = tr_G(d, wol, wil);
+  const float Dw = tr_G1(d, wol) / fabsf(wol.z) * D * fabsf(dwo);
+  if (refl) {
+    float v = D * G * F / fabsf(4.f * ci * co);
+    f = tinted ? tint * v : v3(v);
+    pdf = Dw / (4.f * fabsf(dwo)) * R / (R + T);
+  } else {
+    float s = sqr(dwi + dwo / etap);
+    float ft = D * (1.f - F) * G * fabsf(dwi * dwo / (s * ci * co));
+    f = tinted ? v3(safe_sqrt(tint.x), safe_sqrt(tint.y), safe_sqrt(tint.z)) * ft : v3(ft);
+    pdf = Dw * (fabsf(dwi) / s) * T / (R + T);
+  }
+}
+
+// Compile-time material dispatch for the per-family shade kernels; T < 0
+// dispatches at run time.
+template <int T>
+PT_HD void bsdf_eval_t(const MatRec &m, V3 wo, V3 wi, V3 n, bool front, V3 &f, float &pdf);
+template <int T>
+PT_HD BsdfSample bsdf_sample_t(const MatRec &m, V3 wo, V3 n, bool front, float uc, float u0, float u1);
+
 PT_HD BsdfSample bsdf_sample(const MatRec &m, V3 wo, V3 n, bool front, float uc, float u0,
                              float u1) {
   switch (m.type) {
@@ -539,6 +595,58 @@ PT_HD BsdfSample bsdf_sample(const MatRec &m, V3 wo, V3 n, bool front, float uc,
     return s;
   }
   }
+}
+
+template <int T>
+PT_HD void bsdf_eval_t(const MatRec &m, V3 wo, V3 wi, V3 n, bool front, V3 &f, float &pdf) {
+  if constexpr (T == 0) {
+    f = lam_f(m);
+    pdf = cosine_pdf(n, wi);
+  } else if constexpr (T == 1) {
+    cond_eval(m, wo, wi, n, f, pdf);
+  } else if constexpr (T == 2) {
+    if (mfd_smooth(m)) {
+      f = v3(0.f);
+      pdf = 0.f;
+    } else {
+      Onb b = make_onb(n);
+      mfd_eval_local(m.p[0], TR{m.p[1], m.p[2]}, to_local(b, normalize(wo)), to_local(b, normalize(wi)),
+                     v3(1.f), false, f, pdf);
+    }
+  } else if constexpr (T == 3) {
+    f = v3(0.f);
+    pdf = 0.f;
+  } else if constexpr (T == 4) {
+    f = phong_f(m, wo, wi, n);
+    pdf = phong_pdf(m, wo, wi, n);
+  } else if constexpr (T == 5) {
+    if (front && !dis_glass_smooth(m)) {
+      Onb b = make_onb(n);
+      mfd_eval_local(m.p[14], dis_tr(m), to_local(b, normalize(wo)), to_local(b, normalize(wi)), dis_base(m),
+                     true, f, pdf);
+    } else {
+      f = disney_f(m, wo, wi, n, front);
+      pdf = disney_pdf(m, wo, wi, n, front);
+    }
+  } else if constexpr (T == 6) {
+    f = hair_f(m, wo, wi, n);
+    pdf = hair_pdf(m, wo, wi, n);
+  } else {
+    f = bsdf_f(m, wo, wi, n, front);
+    pdf = bsdf_pdf(m, wo, wi, n, front);
+  }
+}
+
+template <int T>
+PT_HD BsdfSample bsdf_sample_t(const MatRec &m, V3 wo, V3 n, bool front, float uc, float u0, float u1) {
+  if constexpr (T == 0) return lam_sample(m, n, u0, u1);
+  else if constexpr (T == 1) return cond_sample(m, wo, n, u0, u1);
+  else if constexpr (T == 2) return mfd_sample(m, wo, n, uc, u0, u1);
+  else if constexpr (T == 3) return thin_sample(m, wo, n, uc);
+  else if constexpr (T == 4) return phong_sample(m, wo, n, uc, u0, u1);
+  else if constexpr (T == 5) return disney_sample(m, wo, n, front, uc, u0, u1);
+  else if constexpr (T == 6) return hair_sample(m, wo, n, uc, u0, u1);
+  else return bsdf_sample(m, wo, n, front, uc, u0, u1);
 }
 
 }  // namespace pt

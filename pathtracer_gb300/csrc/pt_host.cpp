@@ -500,6 +500,15 @@ std::unique_ptr<Scene> build_scene(const pt_scene_desc *d, cudaStream_t st) {
       const pt_mesh_desc &m = d->meshes[prim_mesh[prim]];
       const int t = prim_tri[prim];
       ps.material = m.material;
+      ps.flags |= ITEM_TRI << 2;
+      {
+        const Item &it = items[prim_item[prim]];
+        V3 e1 = v3(it.b[0], it.b[1], it.b[2]), e2 = v3(it.c[0], it.c[1], it.c[2]);
+        V3 ng = cross(e1, e2);
+        ps.ng[0] = ng.x;
+        ps.ng[1] = ng.y;
+        ps.ng[2] = ng.z;
+      }
       if (m.normals && m.n_normals > 0) {
         const int32_t *ni = m.normal_indices ? m.normal_indices : m.indices;
         bool okn = true;
@@ -516,10 +525,13 @@ std::unique_ptr<Scene> build_scene(const pt_scene_desc *d, cudaStream_t st) {
     } else if (prim < B.n_tris + d->n_quads) {
       const pt_quad_desc &q = d->quads[prim - B.n_tris];
       ps.material = q.material;
+      ps.flags |= (ITEM_QUAD << 2) | (q.axis << 4);
       if (q.flip_face) ps.flags |= PT_PRIM_FLIP;
     } else {
       const pt_sphere_desc &s = d->spheres[prim - B.n_tris - d->n_quads];
       ps.material = s.material;
+      ps.flags |= ITEM_SPHERE << 2;
+      for (int a = 0; a < 3; ++a) ps.n0[a] = s.center[a];
       if (s.flip_face) ps.flags |= PT_PRIM_FLIP;
     }
   }
@@ -527,6 +539,10 @@ std::unique_ptr<Scene> build_scene(const pt_scene_desc *d, cudaStream_t st) {
   // materials
   std::vector<MatRec> mats;
   for (int i = 0; i < d->n_materials; ++i) mats.push_back(derive_material(d->materials[i]));
+  for (int prim = 0; prim < n_prims; ++prim) {
+    const int t = mats[shade[prim].material].type;
+    if (t < PT_MAT_DIFFUSE_EMITTER) S->family_mask |= 1u << t;
+  }
 
   // light discovery (lightDiscovery.hpp:5-81): emissive quads and spheres in
   // object order, then the environment light (renderManager.hpp:115-118).
@@ -711,7 +727,8 @@ Context::Context(int dev) : device(dev) {
   cfg.trace_blocks = num_sms * std::max(1, kinfo.trace_blocks_per_sm);
   cfg.shade_blocks = num_sms * std::max(1, kinfo.shade_blocks_per_sm);
   cfg.max_blocks_simple = num_sms * 8;
-  cfg.sort_by_material = 0;
+  cfg.sort_by_material = 1;
+  cfg.family_mask = 0x7f;
   const char *cap = std::getenv("PT_WAVE_PATHS");
   wave_cap = cap ? std::max(1024, std::atoi(cap)) : (1 << 22);
   const char *srt = std::getenv("PT_SORT_BY_MATERIAL");
@@ -766,6 +783,7 @@ void Context::ensure_queues(int cap, int ln) {
   Q.sort_key = (int *)alloc(c * 4);
   Q.order = (int *)alloc(c * 4);
   Q.bins = (int *)alloc(sizeof(int) * 2 * PT_SORT_BINS);
+  Q.seg = (int *)alloc(sizeof(int) * (PT_SORT_BINS + 1));
   Q.err = d_err;
   q_cap = cap;
   q_ln = ln;
@@ -898,9 +916,11 @@ void Context::render_device(const pt_job_desc &j, float *d_film, pt_stats *stats
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
   cudaEventRecord(e0, stream);
+  LaunchCfg lc = cfg;
+  lc.family_mask = S->family_mask;
   for (long long g0 = 0; g0 < total; g0 += n) {
     int cnt = (int)std::min<long long>(n, total - g0);
-    launch_wave(S->view, J, Q, g0, cnt, d_film, cfg, stream, &prof);
+    launch_wave(S->view, J, Q, g0, cnt, d_film, lc, stream, &prof);
   }
   cudaEventRecord(e1, stream);
   cuda_check(cudaGetLastError(), "launch");

@@ -33,6 +33,7 @@ struct Scene {
   std::vector<void *> owned;
   int n_tris = 0, n_quads = 0, n_spheres = 0, bvh_depth = 0;
   int env_w = 0, env_h = 0;
+  unsigned family_mask = 0;  // BSDF families (material types 0..6) present
   size_t device_bytes = 0;
   ~Scene();
 };

@@ -121,17 +121,23 @@ struct Surf {
 
 __device__ Surf surface_at(const SceneView &S, V3 o, V3 d, const HitRec &h) {
   Surf s;
-  const PrimShade ps = S.shade[h.prim];
+  const float4 *pp = reinterpret_cast<const float4 *>(S.shade + h.prim);
+  const float4 q0 = __ldg(pp), q1 = __ldg(pp + 1), q2 = __ldg(pp + 2), q3 = __ldg(pp + 3);
+  PrimShade ps;
+  ps.material = __float_as_int(q0.x);
+  ps.flags = __float_as_int(q0.y);
+  ps.light = __float_as_int(q0.w);
+  ps.n0[0] = q1.x; ps.n0[1] = q1.y; ps.n0[2] = q1.z;
+  ps.n1[0] = q1.w; ps.n1[1] = q2.x; ps.n1[2] = q2.y;
+  ps.n2[0] = q2.z; ps.n2[1] = q2.w; ps.n2[2] = q3.x;
+  ps.ng[0] = q3.y; ps.ng[1] = q3.z; ps.ng[2] = q3.w;
   s.mat = ps.material;
   s.light = ps.light;
-  // the leaf item of the primitive holds its geometry
-  Item it = load_item(S.items, ps.item);
-  const int type = (int)f2u(it.b[3]);
+  const int type = PT_PRIM_KIND(ps.flags);
   V3 n;
   if (type == ITEM_TRI) {
     // MeshBVHNode::hitTriangle (meshBVH.cpp:112-131) then TriangleMesh::intersect
-    V3 e1 = v3(it.b[0], it.b[1], it.b[2]), e2 = v3(it.c[0], it.c[1], it.c[2]);
-    V3 Ng = cross(e1, e2);
+    V3 Ng = v3(ps.ng[0], ps.ng[1], ps.ng[2]);
     if (ps.flags & PT_PRIM_SMOOTH) {
       float w = 1.f - h.u - h.v;
       n = normalize(w * v3(ps.n0[0], ps.n0[1], ps.n0[2]) + h.u * v3(ps.n1[0], ps.n1[1], ps.n1[2]) +
@@ -142,13 +148,13 @@ __device__ Surf surface_at(const SceneView &S, V3 o, V3 d, const HitRec &h) {
     if (dot(n, Ng) < 0.f) n = -n;
     s.p = xat(o, d, h.t);
   } else if (type == ITEM_QUAD) {
-    const int axis = (int)it.b[2];
+    const int axis = PT_PRIM_AXIS(ps.flags);
     n = v3(axis == 0 ? 1.f : 0.f, axis == 1 ? 1.f : 0.f, axis == 2 ? 1.f : 0.f);
     s.p = xat(o, xnormalize(d), h.t);
   } else {
     V3 dn = xnormalize(d);
     s.p = xat(o, dn, h.t);
-    n = normalize(s.p - v3(it.a[0], it.a[1], it.a[2]));
+    n = normalize(s.p - v3(ps.n0[0], ps.n0[1], ps.n0[2]));
   }
   s.ng = n;
   s.front = dot(d, n) < 0.f;  // set_normal (materialBase.hpp:48-52)
@@ -285,32 +291,54 @@ __global__ void k_camera(DeviceJob J, Queues Q, long long g0, int n) {
   }
 }
 
-__global__ void __launch_bounds__(128) k_trace_closest(SceneView S, Queues Q, int qsel) {
+// k_trace_closest: one ray per thread.  In a participating medium the
+// free-flight distance of the segment is drawn here (dimension dpb*bounce)
+// and used as tmax: a segment that reaches it without a surface hit is a
+// medium event (prim = PT_HIT_MEDIUM, t = free-flight distance).  That is
+// the same decision as comparing the distance with the closest hit.
+__global__ void __launch_bounds__(128) k_trace_closest(SceneView S, DeviceJob J, Queues Q, int qsel, int bounce,
+                                                       long long g0) {
   __shared__ int32_t stack[PT_STACK * 128];
   const int n = Q.counts[qsel];
+  const bool ff = S.has_medium && bounce < J.job.max_depth;
   int rays = 0;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     float4 ro = ld4(Q.ray_o[qsel] + i), rd = ld4(Q.ray_d[qsel] + i);
+    float tmax = 1e5f;
+    float t_s = INFINITY;
+    if (ff) {
+      PathId P = path_id(J, g0 + __float_as_int(ro.w));
+      float uf = sampler_dim(J, 4 * bounce, P.halton_index, P.key, P.q, P.k);
+      t_s = -logf(1.f - uf) / S.sigma_t_max;
+      tmax = fminf(tmax, t_s);
+    }
     HitRec h;
-    bool hit = traverse<false>(S, v3(ro.x, ro.y, ro.z), v3(rd.x, rd.y, rd.z), 1e-4f, 1e5f, h,
+    bool hit = traverse<false>(S, v3(ro.x, ro.y, ro.z), v3(rd.x, rd.y, rd.z), 1e-4f, tmax, h,
                                stack + threadIdx.x, blockDim.x, Q.err);
-    Q.hit[i] = make_float4(hit ? h.t : FLT_MAX, __int_as_float(hit ? h.prim : -1), h.u, h.v);
+    int prim = hit ? h.prim : (t_s < 1e5f ? PT_HIT_MEDIUM : -1);
+    float t = hit ? h.t : (prim == PT_HIT_MEDIUM ? t_s : FLT_MAX);
+    Q.hit[i] = make_float4(t, __int_as_float(prim), h.u, h.v);
     ++rays;
   }
   warp_count(&Q.stats[2], rays);
 }
 
-// Counting sort of the queue by material family: keys[i] = family of hit i
-// (misses last).  Two passes: histogram, then stable scatter of indices.
+// Sort keys: material type 0..7 of the surface hit, PT_KEY_MISS,
+// PT_KEY_MEDIUM.  Counting sort in two passes (histogram, scatter); the
+// second pass also publishes the segment bounds Q.seg[0..PT_SORT_BINS].
+__device__ __forceinline__ int sort_key(const SceneView &S, float4 hit) {
+  int prim = __float_as_int(hit.y);
+  if (prim == PT_HIT_MEDIUM) return PT_KEY_MEDIUM;
+  if (prim < 0) return PT_KEY_MISS;
+  return S.materials[__ldg(&S.shade[prim].material)].type;
+}
 __global__ void k_sort_hist(SceneView S, Queues Q, int qsel) {
   __shared__ int h[PT_SORT_BINS];
   for (int b = threadIdx.x; b < PT_SORT_BINS; b += blockDim.x) h[b] = 0;
   __syncthreads();
   const int n = Q.counts[qsel];
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    int prim = __float_as_int(ld4(Q.hit + i).y);
-    int key = PT_SORT_BINS - 1;
-    if (prim >= 0) key = S.materials[S.shade[prim].material].type;
+    int key = sort_key(S, ld4(Q.hit + i));
     Q.sort_key[i] = key;
     atomicAdd(&h[key], 1);
   }
@@ -319,13 +347,16 @@ __global__ void k_sort_hist(SceneView S, Queues Q, int qsel) {
     if (h[b]) atomicAdd(&Q.bins[b], h[b]);
 }
 __global__ void k_sort_scatter(Queues Q, int qsel) {
-  __shared__ int base[PT_SORT_BINS];
+  __shared__ int base[PT_SORT_BINS + 1];
   if (threadIdx.x == 0) {
     int acc = 0;
     for (int b = 0; b < PT_SORT_BINS; ++b) {
       base[b] = acc;
       acc += Q.bins[b];
     }
+    base[PT_SORT_BINS] = acc;
+    if (blockIdx.x == 0)
+      for (int b = 0; b <= PT_SORT_BINS; ++b) Q.seg[b] = base[b];
   }
   __syncthreads();
   const int n = Q.counts[qsel];
@@ -343,25 +374,129 @@ __device__ __forceinline__ float power_heuristic(float nf, float fpdf, float ng,
   return (f2 + g2) > 0.f ? f2 / (f2 + g2) : 0.f;
 }
 
-// k_shade: one path vertex per thread.  Correspondence with getRayColor
-// (maxdepth_nee.hpp):
-//   :16-17   depth limit          -> continuations are only queued while
-//                                    bounce + 1 < max_depth
+// Next-event estimation at one vertex (maxdepth_nee.hpp:89-232): LN light
+// samples on a stratified x-by-y grid, each a ShadowQueue entry with its
+// unoccluded contribution.  MED: the vertex is a medium scattering event
+// (isotropic phase function instead of a BSDF, no surface cosine).
+template <int FAM, bool MED>
+__device__ __forceinline__ void next_event(const SceneView &S, const DeviceJob &J, const Queues &Q, int sslot,
+                                           int path, uint64_t key, uint32_t rbase, const Surf &sf, int mat,
+                                           V3 wo, V3 beta, int LN, bool mis) {
+  const float phase = (float)(1.0 / (4.0 * PT_PI));
+  Q.sh_o[sslot] = make_float4(sf.p.x, sf.p.y, sf.p.z, __int_as_float(path));
+  const float inv_ln = 1.f / (float)LN;
+  const bool med = S.has_medium != 0;
+  for (int ls = 0; ls < LN; ++ls) {
+    float4 shd = make_float4(0.f, 0.f, 0.f, -1.f), shc = make_float4(0.f, 0.f, 0.f, 0.f);
+    // getOffsets(x, y): stratum (i, j), i outer (random.hpp:47-63)
+    const int si = ls / J.job.light_ny, sj = ls % J.job.light_ny;
+    float ox = ((float)si + rand01(key, rbase + 2u * ls)) / (float)J.job.light_nx;
+    float oy = ((float)sj + rand01(key, rbase + 2u * ls + 1u)) / (float)J.job.light_ny;
+    int li = (int)(rand01(key, rbase + 20u + ls) * S.n_lights) % S.n_lights;
+    const LightRec &Lr = S.lights[li];
+    V3 wl, Le;
+    float tmax, pdf_l, G, NoI, tr = 1.f;
+    bool valid = true;
+    if (Lr.type == LIGHT_ENV) {
+      float pdir;
+      if (J.job.env_sampling == PT_ENV_ALIAS) {
+        wl = env_alias_sample(S.env, ox, oy, rand01(key, rbase + 28u + ls), pdir);
+      } else {
+        // uniformSampleSphere * 1e5 (texture.hpp:120-124, envLight.hpp:26-43)
+        float z = 1.f - 2.f * ox;
+        float rr = sqrtf(fmaxf(0.f, 1.f - z * z));
+        float sp, cp;
+        sincospi_(2.f * oy, &sp, &cp);
+        V3 pinf = v3(rr * cp, rr * sp, z) * 1e5f;
+        wl = normalize(pinf - sf.p);
+        pdir = (float)(1.0 / (4.0 * PT_PI));
+      }
+      tmax = FLT_MAX;
+      pdf_l = pdir / (float)S.n_lights;
+      NoI = MED ? 1.f : fmaxf(0.f, dot(sf.n, wl));
+      G = NoI;
+      Le = env_lookup(S.env, wl);
+      valid = pdf_l > 1e-7f && !med;  // no light reaches through an infinite medium
+    } else {
+      V3 lp, ln;
+      if (Lr.type == LIGHT_QUAD) {
+        // QuadLight::get_sample / get_normal_at (light.hpp:131-147)
+        lp = v3(Lr.v0[0], Lr.v0[1], Lr.v0[2]) + ox * v3(Lr.e1[0], Lr.e1[1], Lr.e1[2]) +
+             oy * v3(Lr.e2[0], Lr.e2[1], Lr.e2[2]);
+        ln = v3(Lr.normal[0], Lr.normal[1], Lr.normal[2]);
+      } else {
+        // SphereLight::get_sample (light.hpp:254-264): the whole sphere
+        float sth, cth, sph, cph;
+        sincospi_(2.f * ox, &sth, &cth);
+        float phi = acosf(2.f * oy - 1.f);
+        sincos_(phi, &sph, &cph);
+        V3 c = v3(Lr.v0[0], Lr.v0[1], Lr.v0[2]);
+        lp = c + Lr.radius * v3(sph * cth, sph * sth, cph);
+        ln = normalize(lp - c);
+      }
+      V3 ld = lp - sf.p;
+      float len = length(ld);
+      wl = normalize(ld);
+      if (len < 0.001f) valid = false;
+      tmax = len - 0.001f;
+      pdf_l = (Lr.area <= 1e-7f) ? 0.f : 1.f / (Lr.area * (float)S.n_lights);
+      NoI = MED ? 1.f : fmaxf(0.f, dot(sf.n, wl));
+      float NoL = fmaxf(0.f, dot(ln, -wl));
+      float d2 = len * len;
+      G = (d2 < 1e-7f) ? 0.f : NoL * NoI / d2;
+      Le = (dot(ln, -wl) > 0.f) ? v3(Lr.color[0], Lr.color[1], Lr.color[2]) * Lr.intensity : v3(0.f);
+      if (!(pdf_l > 1e-7f)) valid = false;
+      if (mis && valid && NoL > 0.f) {
+        pdf_l = pdf_l * d2 / NoL;  // solid-angle pdf
+        G = NoI;
+      }
+      if (med) tr = expf(-S.sigma_t_max * len);
+    }
+    if (valid && G > 0.f) {
+      V3 f;
+      float pb;
+      if (MED) {
+        f = v3(phase);
+        pb = phase;
+      } else {
+        bsdf_eval_t<FAM>(S.materials[mat], wo, wl, sf.n, sf.front, f, pb);
+      }
+      float w = mis ? power_heuristic((float)LN, pdf_l, 1.f, pb) : 1.f;
+      V3 c = beta * (f * Le * (G / pdf_l * w * inv_ln)) * tr;
+      if (c.x != 0.f || c.y != 0.f || c.z != 0.f) {
+        shd = make_float4(wl.x, wl.y, wl.z, tmax);
+        shc = make_float4(c.x, c.y, c.z, 0.f);
+      }
+    }
+    Q.sh_d[(size_t)ls * Q.cap + sslot] = shd;
+    Q.sh_c[(size_t)ls * Q.cap + sslot] = shc;
+  }
+}
+
+// k_shade<FAM>: one path vertex per thread.  FAM 0..6 processes the
+// material-sorted segment of that BSDF family with its code compiled alone;
+// FAM PT_FAM_MISC the misses, emitter hits and medium events; FAM -1 the
+// whole unsorted queue with run-time dispatch.  Correspondence with
+// getRayColor (maxdepth_nee.hpp):
+//   :16-17   depth limit -> continuations are queued while bounce + 1 < max_depth
 //   :26-37   miss -> env / bg
 //   :44-45   scatter() false -> emit()
 //   :47-78   specular (delta) branches: no NEE, beta *= attenuation
-//   :91-232  NEE with LIGHT_SAMPLE_X*Y stratified light samples, one shadow
-//            ray each (ShadowQueue, resolved by k_trace_shadow)
+//   :91-232  NEE (next_event, resolved by k_trace_shadow)
 //   :238-247 continuation hitting an emitter is dropped (REF_NEE)
 //   :251-255 beta *= f * |cos| / pdf
 // NEE_MIS weights light and BSDF sampling with the power heuristic and
-// always performs NEE at non-delta vertices.
-//
-// The loop runs in three phases per iteration so that the queue slot
-// allocations (warp ballots) are reached by every lane of the warp.
-__global__ void __launch_bounds__(128) k_shade(SceneView S, DeviceJob J, Queues Q, int qsel,
-                                               int bounce, long long g0, int use_order) {
-  const int n = Q.counts[qsel];
+// always performs NEE at non-delta vertices.  The loop runs in phases so
+// that the queue slot allocations (warp ballots) see every lane.
+template <int FAM>
+__global__ void __launch_bounds__(128) k_shade(SceneView S, DeviceJob J, Queues Q, int qsel, int bounce,
+                                               long long g0) {
+  int lo = 0, hi = Q.counts[qsel];
+  if (FAM >= 0) {
+    lo = Q.seg[FAM];
+    hi = (FAM == PT_FAM_MISC) ? Q.seg[PT_KEY_MEDIUM + 1] : Q.seg[FAM + 1];
+  }
+  const int n = hi - lo;
   const int nq = qsel ^ 1;
   const int LN = J.job.light_nx * J.job.light_ny;
   const bool mis = J.job.estimator == PT_EST_NEE_MIS;
@@ -371,6 +506,8 @@ __global__ void __launch_bounds__(128) k_shade(SceneView S, DeviceJob J, Queues 
   const bool med = S.has_medium != 0;
   const int dpb = med ? 4 : 3;  // sampler dimensions per bounce
   const float phase = (float)(1.0 / (4.0 * PT_PI));  // isotropic Henyey-Greenstein, g = 0
+  constexpr bool DO_MISC = (FAM < 0 || FAM == PT_FAM_MISC);
+  constexpr bool DO_SURF = (FAM != PT_FAM_MISC);
   int segs = 0;
   const int stride = gridDim.x * blockDim.x;
   const int nround = (n + stride - 1) / stride * stride;
@@ -386,7 +523,7 @@ __global__ void __launch_bounds__(128) k_shade(SceneView S, DeviceJob J, Queues 
     float npdf = -1.f;
     uint64_t key = 0;
     if (ii < n) {
-      const int i = use_order ? Q.order[ii] : ii;
+      const int i = (FAM >= 0) ? Q.order[lo + ii] : ii;
       float4 ro = ld4(Q.ray_o[qsel] + i), rd = ld4(Q.ray_d[qsel] + i);
       float4 hh = ld4(Q.hit + i);
       path = __float_as_int(ro.w);
@@ -397,25 +534,13 @@ __global__ void __launch_bounds__(128) k_shade(SceneView S, DeviceJob J, Queues 
       PathId P = path_id(J, g0 + path);
       key = P.key;
       const int prim = __float_as_int(hh.y);
-      const float t_hit = prim >= 0 ? hh.x : INFINITY;
       V3 Ladd = v3(0.f);
-      // ---- homogeneous medium (extension): free-flight sampling
-      bool in_medium = false;
-      float t_s = 0.f;
-      if (med) {
-        if (bounce < max_depth) {
-          float uf = sampler_dim(J, dpb * bounce, P.halton_index, P.key, P.q, P.k);
-          t_s = -logf(1.f - uf) / S.sigma_t_max;
-          in_medium = t_s < t_hit;
-        } else {
-          beta = beta * expf(-S.sigma_t_max * t_hit);  // last MIS segment: transmittance
-        }
-      }
-      if (in_medium) {
+      if (med && bounce >= max_depth) beta = beta * expf(-S.sigma_t_max * (prim >= 0 ? hh.x : INFINITY));
+      if (DO_MISC && prim == PT_HIT_MEDIUM) {
+        // ---- medium scattering event (extension): weight sigma_s / sigma_t
         ++segs;
-        sf.p = o + t_s * normalize(d);
-        beta = beta * v3(S.sigma_s[0] / (S.sigma_a[0] + S.sigma_s[0]),
-                         S.sigma_s[1] / (S.sigma_a[1] + S.sigma_s[1]),
+        sf.p = o + hh.x * normalize(d);
+        beta = beta * v3(S.sigma_s[0] / (S.sigma_a[0] + S.sigma_s[0]), S.sigma_s[1] / (S.sigma_a[1] + S.sigma_s[1]),
                          S.sigma_s[2] / (S.sigma_a[2] + S.sigma_s[2]));
         do_nee = S.n_lights > 0;
         nee_medium = true;
@@ -430,21 +555,20 @@ __global__ void __launch_bounds__(128) k_shade(SceneView S, DeviceJob J, Queues 
           npdf = phase;
           push = true;
         }
-      } else if (prim < 0) {
+      } else if (DO_MISC && prim < 0) {
         // ---- miss (maxdepth_nee.hpp:26-37)
         if (S.env.present) {
           V3 Le = env_lookup(S.env, d);
           float w = 1.f;
           if (mis && prev_pdf >= 0.f && S.n_lights > 0) {
-            float pl = (J.job.env_sampling == PT_ENV_ALIAS) ? env_alias_pdf(S.env, d)
-                                                           : (float)(1.0 / (4.0 * PT_PI));
+            float pl = (J.job.env_sampling == PT_ENV_ALIAS) ? env_alias_pdf(S.env, d) : (float)(1.0 / (4.0 * PT_PI));
             w = power_heuristic(1.f, prev_pdf, (float)LN, pl / (float)S.n_lights);
           }
           Ladd = beta * Le * w;
         } else {
           Ladd = beta * v3(S.bg[0], S.bg[1], S.bg[2]);
         }
-      } else {
+      } else if (prim >= 0) {
         HitRec h;
         h.t = hh.x;
         h.prim = prim;
@@ -453,7 +577,7 @@ __global__ void __launch_bounds__(128) k_shade(SceneView S, DeviceJob J, Queues 
         sf = surface_at(S, o, d, h);
         mat = sf.mat;
         const MatRec &M = S.materials[mat];
-        if (mat_is_emitter(M)) {
+        if (DO_MISC && mat_is_emitter(M)) {
           // DiffuseEmitter: scatter() is false (material.hpp:475-481)
           if (prev_pdf < 0.f) {
             Ladd = beta * mat_emit(M, sf.n, d);
@@ -474,14 +598,14 @@ __global__ void __launch_bounds__(128) k_shade(SceneView S, DeviceJob J, Queues 
             }
           }
           // REF_NEE after a non-delta vertex: dropped (maxdepth_nee.hpp:246-247)
-        } else if (bounce < max_depth) {
+        } else if (DO_SURF && !mat_is_emitter(M) && bounce < max_depth) {
           ++segs;
           const int dim0 = dpb * bounce + (med ? 1 : 0);
           float uc = sampler_dim(J, dim0, P.halton_index, P.key, P.q, P.k);
           float u0 = sampler_dim(J, dim0 + 1, P.halton_index, P.key, P.q, P.k);
           float u1 = sampler_dim(J, dim0 + 2, P.halton_index, P.key, P.q, P.k);
           wo = -normalize(d);
-          BsdfSample bs = bsdf_sample(M, wo, sf.n, sf.front, uc, u0, u1);
+          BsdfSample bs = bsdf_sample_t<FAM>(M, wo, sf.n, sf.front, uc, u0, u1);
           const bool spec_r = (bs.type & BX_SPECULAR_R) == BX_SPECULAR_R;
           const bool spec_t = (bs.type & BX_SPECULAR_T) == BX_SPECULAR_T;
           if (bs.ok && (spec_r || spec_t)) {
@@ -526,103 +650,65 @@ __global__ void __launch_bounds__(128) k_shade(SceneView S, DeviceJob J, Queues 
       Q.ray_o[nq][slot] = make_float4(sf.p.x, sf.p.y, sf.p.z, __int_as_float(path));
       Q.ray_d[nq][slot] = make_float4(wi.x, wi.y, wi.z, 0.f);
     }
-    // ---------------- phase C: next-event estimation (maxdepth_nee.hpp:89-232)
+    // ---------------- phase C: next-event estimation
     if (do_nee) {
-      const MatRec &M = S.materials[mat];
-      Q.sh_o[sslot] = make_float4(sf.p.x, sf.p.y, sf.p.z, __int_as_float(path));
-      const float inv_ln = 1.f / (float)LN;
-      for (int ls = 0; ls < LN; ++ls) {
-        float4 shd = make_float4(0.f, 0.f, 0.f, -1.f), shc = make_float4(0.f, 0.f, 0.f, 0.f);
-        // getOffsets(x, y): stratum (i, j), i outer (random.hpp:47-63)
-        const int si = ls / J.job.light_ny, sj = ls % J.job.light_ny;
-        float ox = ((float)si + rand01(key, rbase + 2u * ls)) / (float)J.job.light_nx;
-        float oy = ((float)sj + rand01(key, rbase + 2u * ls + 1u)) / (float)J.job.light_ny;
-        int li = (int)(rand01(key, rbase + 20u + ls) * S.n_lights) % S.n_lights;
-        const LightRec &Lr = S.lights[li];
-        V3 wl, Le;
-        float tmax, pdf_l, G, NoI, tr = 1.f;
-        bool valid = true;
-        if (Lr.type == LIGHT_ENV) {
-          float pdir;
-          if (J.job.env_sampling == PT_ENV_ALIAS) {
-            wl = env_alias_sample(S.env, ox, oy, rand01(key, rbase + 28u + ls), pdir);
-          } else {
-            // uniformSampleSphere * 1e5 (texture.hpp:120-124, envLight.hpp:26-43)
-            float z = 1.f - 2.f * ox;
-            float rr = sqrtf(fmaxf(0.f, 1.f - z * z));
-            float sp, cp;
-            sincospi_(2.f * oy, &sp, &cp);
-            V3 pinf = v3(rr * cp, rr * sp, z) * 1e5f;
-            wl = normalize(pinf - sf.p);
-            pdir = (float)(1.0 / (4.0 * PT_PI));
-          }
-          tmax = FLT_MAX;
-          pdf_l = pdir / (float)S.n_lights;
-          NoI = nee_medium ? 1.f : fmaxf(0.f, dot(sf.n, wl));
-          G = NoI;
-          Le = env_lookup(S.env, wl);
-          valid = pdf_l > 1e-7f && !med;  // no light reaches through an infinite medium
-        } else {
-          V3 lp, ln;
-          if (Lr.type == LIGHT_QUAD) {
-            // QuadLight::get_sample / get_normal_at (light.hpp:131-147)
-            lp = v3(Lr.v0[0], Lr.v0[1], Lr.v0[2]) + ox * v3(Lr.e1[0], Lr.e1[1], Lr.e1[2]) +
-                 oy * v3(Lr.e2[0], Lr.e2[1], Lr.e2[2]);
-            ln = v3(Lr.normal[0], Lr.normal[1], Lr.normal[2]);
-          } else {
-            // SphereLight::get_sample (light.hpp:254-264): the whole sphere
-            float sth, cth, sph, cph;
-            sincospi_(2.f * ox, &sth, &cth);
-            float phi = acosf(2.f * oy - 1.f);
-            sincos_(phi, &sph, &cph);
-            V3 c = v3(Lr.v0[0], Lr.v0[1], Lr.v0[2]);
-            lp = c + Lr.radius * v3(sph * cth, sph * sth, cph);
-            ln = normalize(lp - c);
-          }
-          V3 ld = lp - sf.p;
-          float len = length(ld);
-          wl = normalize(ld);
-          if (len < 0.001f) valid = false;
-          tmax = len - 0.001f;
-          pdf_l = (Lr.area <= 1e-7f) ? 0.f : 1.f / (Lr.area * (float)S.n_lights);
-          NoI = nee_medium ? 1.f : fmaxf(0.f, dot(sf.n, wl));
-          float NoL = fmaxf(0.f, dot(ln, -wl));
-          float d2 = len * len;
-          G = (d2 < 1e-7f) ? 0.f : NoL * NoI / d2;
-          Le = (dot(ln, -wl) > 0.f) ? v3(Lr.color[0], Lr.color[1], Lr.color[2]) * Lr.intensity
-                                    : v3(0.f);
-          if (!(pdf_l > 1e-7f)) valid = false;
-          if (mis && valid && NoL > 0.f) {
-            pdf_l = pdf_l * d2 / NoL;  // solid-angle pdf
-            G = NoI;
-          }
-          if (med) tr = expf(-S.sigma_t_max * len);
-        }
-        if (valid && G > 0.f) {
-          V3 f = nee_medium ? v3(phase) : bsdf_f(M, wo, wl, sf.n, sf.front);
-          float w = 1.f;
-          if (mis) {
-            float pb = nee_medium ? phase : bsdf_pdf(M, wo, wl, sf.n, sf.front);
-            w = power_heuristic((float)LN, pdf_l, 1.f, pb);
-          }
-          V3 c = beta * (f * Le * (G / pdf_l * w * inv_ln)) * tr;
-          if (c.x != 0.f || c.y != 0.f || c.z != 0.f) {
-            shd = make_float4(wl.x, wl.y, wl.z, tmax);
-            shc = make_float4(c.x, c.y, c.z, 0.f);
-          }
-        }
-        Q.sh_d[(size_t)ls * Q.cap + sslot] = shd;
-        Q.sh_c[(size_t)ls * Q.cap + sslot] = shc;
-      }
+      if (DO_MISC && nee_medium)
+        next_event<FAM, true>(S, J, Q, sslot, path, key, rbase, sf, mat, wo, beta, LN, mis);
+      else if (DO_SURF)
+        next_event<FAM, false>(S, J, Q, sslot, path, key, rbase, sf, mat, wo, beta, LN, mis);
     }
   }
   warp_count(&Q.stats[1], segs);
 }
 
-// k_trace_shadow: one NEE vertex per thread; its light samples are tested
-// in order [0.001, tmax] and the visible terms are added to the path's L in
-// the same order (deterministic).
-__global__ void __launch_bounds__(128) k_trace_shadow(SceneView S, Queues Q, int LN) {
+// k_trace_shadow: one shadow ray per thread.  The LN rays of a vertex sit in
+// LN consecutive lanes (LN a power of two <= 32); their visible terms are
+// reduced with shuffles in a fixed order and the group's first lane adds the
+// sum to the path's L, so the result is deterministic.
+__global__ void __launch_bounds__(128) k_trace_shadow(SceneView S, Queues Q, int LN, int lg) {
+  __shared__ int32_t stack[PT_STACK * 128];
+  const int nv = Q.counts[2];
+  const long long n = (long long)nv << lg;
+  int rays = 0;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  const long long nround = (n + stride - 1) / stride * stride;
+  const int lane = threadIdx.x & 31;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < nround; t += stride) {
+    V3 acc = v3(0.f);
+    int v = (int)(t >> lg), ls = (int)(t & (LN - 1));
+    if (t < n) {
+      float4 dd = ld4(Q.sh_d + (size_t)ls * Q.cap + v);
+      if (dd.w >= 0.f) {
+        float4 so = ld4(Q.sh_o + v);
+        HitRec h;
+        ++rays;
+        bool occ = traverse<true>(S, v3(so.x, so.y, so.z), v3(dd.x, dd.y, dd.z), 0.001f, dd.w, h,
+                                  stack + threadIdx.x, blockDim.x, Q.err);
+        if (!occ) {
+          float4 cc = ld4(Q.sh_c + (size_t)ls * Q.cap + v);
+          acc = v3(cc.x, cc.y, cc.z);
+        }
+      }
+    }
+    // fixed-order tree reduction inside each group of LN lanes
+    for (int off = 1; off < LN; off <<= 1) {
+      float ox = __shfl_down_sync(0xffffffffu, acc.x, off);
+      float oy = __shfl_down_sync(0xffffffffu, acc.y, off);
+      float oz = __shfl_down_sync(0xffffffffu, acc.z, off);
+      if ((lane & (2 * off - 1)) == 0) acc = acc + v3(ox, oy, oz);
+    }
+    if (t < n && ls == 0 && (acc.x != 0.f || acc.y != 0.f || acc.z != 0.f)) {
+      int path = __float_as_int(ld4(Q.sh_o + v).w);
+      float4 L = Q.L[path];
+      Q.L[path] = make_float4(L.x + acc.x, L.y + acc.y, L.z + acc.z, 0.f);
+    }
+  }
+  warp_count(&Q.stats[3], rays);
+}
+
+// k_trace_shadow_serial: the same for light-sample counts that are not a
+// power of two: one vertex per thread, its rays in order.
+__global__ void __launch_bounds__(128) k_trace_shadow_serial(SceneView S, Queues Q, int LN) {
   __shared__ int32_t stack[PT_STACK * 128];
   const int n = Q.counts[2];
   int rays = 0;
@@ -637,8 +723,8 @@ __global__ void __launch_bounds__(128) k_trace_shadow(SceneView S, Queues Q, int
       float4 cc = ld4(Q.sh_c + (size_t)ls * Q.cap + i);
       HitRec h;
       ++rays;
-      bool occ = traverse<true>(S, o, v3(dd.x, dd.y, dd.z), 0.001f, dd.w, h, stack + threadIdx.x,
-                                blockDim.x, Q.err);
+      bool occ = traverse<true>(S, o, v3(dd.x, dd.y, dd.z), 0.001f, dd.w, h, stack + threadIdx.x, blockDim.x,
+                                Q.err);
       if (!occ) acc += v3(cc.x, cc.y, cc.z);
     }
     float4 L = Q.L[path];
@@ -741,22 +827,38 @@ void launch_wave(const SceneView &S, const DeviceJob &J, const Queues &Q, long l
     cudaMemsetAsync(Q.counts + (qsel ^ 1), 0, sizeof(int), st);
     cudaMemsetAsync(Q.counts + 2, 0, sizeof(int), st);
     P.begin(STAGE_TRACE, st);
-    k_trace_closest<<<cfg.trace_blocks, 128, 0, st>>>(S, Q, qsel);
+    k_trace_closest<<<cfg.trace_blocks, 128, 0, st>>>(S, J, Q, qsel, b, g0);
     P.end(st);
-    int use_order = 0;
     if (cfg.sort_by_material) {
+      // sort-by-material queues: one specialised shade kernel per family
       cudaMemsetAsync(Q.bins, 0, sizeof(int) * 2 * PT_SORT_BINS, st);
       P.begin(STAGE_SORT, st);
       k_sort_hist<<<cfg.max_blocks_simple, 256, 0, st>>>(S, Q, qsel);
       k_sort_scatter<<<cfg.max_blocks_simple, 256, 0, st>>>(Q, qsel);
       P.end(st);
-      use_order = 1;
+      P.begin(STAGE_SHADE, st);
+      if (cfg.family_mask & (1u << 0)) k_shade<0><<<cfg.shade_blocks, 128, 0, st>>>(S, J, Q, qsel, b, g0);
+      if (cfg.family_mask & (1u << 1)) k_shade<1><<<cfg.shade_blocks, 128, 0, st>>>(S, J, Q, qsel, b, g0);
+      if (cfg.family_mask & (1u << 2)) k_shade<2><<<cfg.shade_blocks, 128, 0, st>>>(S, J, Q, qsel, b, g0);
+      if (cfg.family_mask & (1u << 3)) k_shade<3><<<cfg.shade_blocks, 128, 0, st>>>(S, J, Q, qsel, b, g0);
+      if (cfg.family_mask & (1u << 4)) k_shade<4><<<cfg.shade_blocks, 128, 0, st>>>(S, J, Q, qsel, b, g0);
+      if (cfg.family_mask & (1u << 5)) k_shade<5><<<cfg.shade_blocks, 128, 0, st>>>(S, J, Q, qsel, b, g0);
+      if (cfg.family_mask & (1u << 6)) k_shade<6><<<cfg.shade_blocks, 128, 0, st>>>(S, J, Q, qsel, b, g0);
+      k_shade<PT_FAM_MISC><<<cfg.shade_blocks, 128, 0, st>>>(S, J, Q, qsel, b, g0);
+      P.end(st);
+    } else {
+      P.begin(STAGE_SHADE, st);
+      k_shade<-1><<<cfg.shade_blocks, 128, 0, st>>>(S, J, Q, qsel, b, g0);
+      P.end(st);
     }
-    P.begin(STAGE_SHADE, st);
-    k_shade<<<cfg.shade_blocks, 128, 0, st>>>(S, J, Q, qsel, b, g0, use_order);
-    P.end(st);
     P.begin(STAGE_SHADOW, st);
-    k_trace_shadow<<<cfg.trace_blocks, 128, 0, st>>>(S, Q, LN);
+    if ((LN & (LN - 1)) == 0 && LN <= 32) {
+      int lg = 0;
+      while ((1 << lg) < LN) ++lg;
+      k_trace_shadow<<<cfg.trace_blocks, 128, 0, st>>>(S, Q, LN, lg);
+    } else {
+      k_trace_shadow_serial<<<cfg.trace_blocks, 128, 0, st>>>(S, Q, LN);
+    }
     P.end(st);
     qsel ^= 1;
   }
@@ -775,12 +877,12 @@ void kernel_attributes(KernelInfo *info) {
   cudaFuncAttributes a;
   cudaFuncGetAttributes(&a, k_trace_closest);
   info->trace_regs = a.numRegs;
-  cudaFuncGetAttributes(&a, k_shade);
+  cudaFuncGetAttributes(&a, k_shade<-1>);
   info->shade_regs = a.numRegs;
   int nb = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_trace_closest, 128, 0);
   info->trace_blocks_per_sm = nb;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_shade, 128, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_shade<-1>, 128, 0);
   info->shade_blocks_per_sm = nb;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_trace_shadow, 128, 0);
   info->shadow_blocks_per_sm = nb;

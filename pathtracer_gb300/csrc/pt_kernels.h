@@ -9,6 +9,13 @@
 
 #define PT_MAX_LIGHT_SAMPLES 16
 #define PT_SORT_BINS 16
+// Sort keys: material type 0..7 of a surface hit, then misses and medium
+// events.  The shade kernel of family PT_FAM_MISC covers keys 7..9
+// (emitters, misses, medium events).
+#define PT_KEY_MISS 8
+#define PT_KEY_MEDIUM 9
+#define PT_FAM_MISC 7
+#define PT_HIT_MEDIUM (-2)
 
 namespace pt {
 
@@ -32,6 +39,7 @@ struct Queues {
   unsigned long long *stats;  // [0] paths [1] segments [2] rays [3] shadow rays
   int *err;           // device error flag (stack overflow / iteration cap)
   int *sort_key, *order, *bins;
+  int *seg;           // [PT_SORT_BINS + 1] segment bounds of the sorted order
 };
 
 struct LaunchCfg {
@@ -39,6 +47,7 @@ struct LaunchCfg {
   int shade_blocks;
   int max_blocks_simple;
   int sort_by_material;
+  unsigned family_mask;  // material types present in the scene (bit per type)
 };
 
 // Per-stage CUDA-event timing of the wave kernels (pt_profile_begin/end).

@@ -40,17 +40,24 @@ struct alignas(16) Item {
   float c[4];
 };
 
-// Shading record of a primitive (64 B).
+// Shading record of a primitive (64 B): everything the shade stage needs,
+// so a hit costs one dependent 64-byte load.
+//   triangle: n0..n2 vertex normals (if smooth), ng = cross(e1, e2)
+//   rectangle: axis in flags bits 4-5
+//   sphere: centre in n0
 struct alignas(16) PrimShade {
   int32_t material;
-  int32_t flags;     // bit0 smooth normals present, bit1 FlipFace
+  int32_t flags;     // bit0 smooth normals, bit1 FlipFace, bits 2-3 kind, bits 4-5 axis
   int32_t item;      // index of the primitive's leaf item
   int32_t light;     // index in the light table (-1: not a light)
-  float n0[3], n1[3], n2[3];  // vertex normals (triangles with normals)
-  float pad;
+  float n0[3], n1[3], n2[3];
+  float ng[3];
 };
+static_assert(sizeof(PrimShade) == 64, "PrimShade must be 64 bytes");
 #define PT_PRIM_SMOOTH 1
 #define PT_PRIM_FLIP 2
+#define PT_PRIM_KIND(f) (((f) >> 2) & 3)
+#define PT_PRIM_AXIS(f) (((f) >> 4) & 3)
 
 // Material record: the C-ABI description plus constants derived once on the
 // host (Disney lobe weights, hair v[p], s, sin/cos 2^k alpha ...).
