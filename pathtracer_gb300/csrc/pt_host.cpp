@@ -730,7 +730,7 @@ Context::Context(int dev) : device(dev) {
   cfg.sort_by_material = 1;
   cfg.family_mask = 0x7f;
   const char *cap = std::getenv("PT_WAVE_PATHS");
-  wave_cap = cap ? std::max(1024, std::atoi(cap)) : (1 << 22);
+  wave_cap = cap ? std::max(1024, std::atoi(cap)) : (1 << 24);
   const char *srt = std::getenv("PT_SORT_BY_MATERIAL");
   if (srt) cfg.sort_by_material = std::atoi(srt);
   cuda_check(cudaMalloc(&d_err, sizeof(int)), "cudaMalloc(err)");

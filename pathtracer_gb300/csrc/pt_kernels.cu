@@ -337,10 +337,19 @@ __global__ void k_sort_hist(SceneView S, Queues Q, int qsel) {
   for (int b = threadIdx.x; b < PT_SORT_BINS; b += blockDim.x) h[b] = 0;
   __syncthreads();
   const int n = Q.counts[qsel];
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    int key = sort_key(S, ld4(Q.hit + i));
-    Q.sort_key[i] = key;
-    atomicAdd(&h[key], 1);
+  const int lane = threadIdx.x & 31;
+  const int stride = gridDim.x * blockDim.x;
+  const int nround = (n + stride - 1) / stride * stride;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nround; i += stride) {
+    const bool act = i < n;
+    int key = -1;
+    if (act) {
+      key = sort_key(S, ld4(Q.hit + i));
+      Q.sort_key[i] = key;
+    }
+    // one shared atomic per (warp, key)
+    const unsigned peers = __match_any_sync(0xffffffffu, key);
+    if (act && lane == __ffs(peers) - 1) atomicAdd(&h[key], __popc(peers));
   }
   __syncthreads();
   for (int b = threadIdx.x; b < PT_SORT_BINS; b += blockDim.x)
@@ -359,11 +368,32 @@ __global__ void k_sort_scatter(Queues Q, int qsel) {
       for (int b = 0; b <= PT_SORT_BINS; ++b) Q.seg[b] = base[b];
   }
   __syncthreads();
+  // per tile of blockDim entries: warp-aggregated ranks in shared memory, one
+  // global atomic per (tile, key) to reserve the tile's range of each key
+  __shared__ int cnt[PT_SORT_BINS], gbase[PT_SORT_BINS];
   const int n = Q.counts[qsel];
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    int key = Q.sort_key[i];
-    int pos = base[key] + atomicAdd(&Q.bins[PT_SORT_BINS + key], 1);
-    Q.order[pos] = i;
+  const int lane = threadIdx.x & 31;
+  const int stride = gridDim.x * blockDim.x;
+  const int nround = (n + stride - 1) / stride * stride;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nround; i += stride) {
+    if (threadIdx.x < PT_SORT_BINS) cnt[threadIdx.x] = 0;
+    __syncthreads();
+    const bool act = i < n;
+    const int key = act ? Q.sort_key[i] : PT_SORT_BINS - 1;
+    const unsigned peers = __match_any_sync(0xffffffffu, act ? key : -1);
+    const int leader = __ffs(peers) - 1;
+    const int rank = __popc(peers & ((1u << lane) - 1u));
+    int wbase = 0;
+    if (act && lane == leader) wbase = atomicAdd(&cnt[key], __popc(peers));
+    wbase = __shfl_sync(0xffffffffu, wbase, leader);
+    __syncthreads();
+    if (threadIdx.x < PT_SORT_BINS) {
+      const int c = cnt[threadIdx.x];
+      gbase[threadIdx.x] = c ? atomicAdd(&Q.bins[PT_SORT_BINS + threadIdx.x], c) : 0;
+    }
+    __syncthreads();
+    if (act) Q.order[base[key] + gbase[key] + wbase + rank] = i;
+    __syncthreads();
   }
 }
 

@@ -164,30 +164,44 @@ __device__ bool traverse(const SceneView &S, V3 o, V3 d, float tmin, float tmax,
       const float lya[4] = {ly.x, ly.y, ly.z, ly.w}, hya[4] = {hy.x, hy.y, hy.z, hy.w};
       const float lza[4] = {lz.x, lz.y, lz.z, lz.w}, hza[4] = {hz.x, hz.y, hz.z, hz.w};
       const int cha[4] = {ch.x, ch.y, ch.z, ch.w}, cna[4] = {cn.x, cn.y, cn.z, cn.w};
-      float dist[4];
-      int32_t cref[4];
-      int nh = 0;
-#pragma unroll
-      for (int c = 0; c < 4; ++c) {
-        if (cna[c] < 0) continue;
-        float t0x = fmaf(lxa[c], inv.x, oi.x), t1x = fmaf(hxa[c], inv.x, oi.x);
-        float t0y = fmaf(lya[c], inv.y, oi.y), t1y = fmaf(hya[c], inv.y, oi.y);
-        float t0z = fmaf(lza[c], inv.z, oi.z), t1z = fmaf(hza[c], inv.z, oi.z);
-        float tn = fmaxf(fmaxf(fminf(t0x, t1x), fminf(t0y, t1y)), fmaxf(fminf(t0z, t1z), tmin));
-        float tf = fminf(fminf(fmaxf(t0x, t1x), fmaxf(t0y, t1y)), fminf(fmaxf(t0z, t1z), tmax));
-        if (tn <= tf) {
-          // insertion into a small sorted list (ascending distance)
-          int32_t r = cna[c] == 0 ? cha[c] : leaf_ref(cha[c], cna[c]);
-          int j = nh++;
-          while (j > 0 && dist[j - 1] > tn) {
-            dist[j] = dist[j - 1];
-            cref[j] = cref[j - 1];
-            --j;
-          }
-          dist[j] = tn;
-          cref[j] = r;
-        }
+      // entry distance per child (+inf when missed or empty), kept in
+      // registers; closest-hit visits near to far (sorting network),
+      // any-hit in node order.
+      float d0, d1, d2, d3;
+      int32_t r0, r1, r2, r3;
+#define PT_CHILD(c, dd, rr)                                                                          \
+  {                                                                                                  \
+    float t0x = fmaf(lxa[c], inv.x, oi.x), t1x = fmaf(hxa[c], inv.x, oi.x);                        \
+    float t0y = fmaf(lya[c], inv.y, oi.y), t1y = fmaf(hya[c], inv.y, oi.y);                        \
+    float t0z = fmaf(lza[c], inv.z, oi.z), t1z = fmaf(hza[c], inv.z, oi.z);                        \
+    float tn = fmaxf(fmaxf(fminf(t0x, t1x), fminf(t0y, t1y)), fmaxf(fminf(t0z, t1z), tmin));     \
+    float tf = fminf(fminf(fmaxf(t0x, t1x), fmaxf(t0y, t1y)), fminf(fmaxf(t0z, t1z), tmax));     \
+    dd = (cna[c] >= 0 && tn <= tf) ? tn : INFINITY;                                                 \
+    rr = cna[c] == 0 ? cha[c] : leaf_ref(cha[c], max(cna[c], 1));                                   \
+  }
+      PT_CHILD(0, d0, r0)
+      PT_CHILD(1, d1, r1)
+      PT_CHILD(2, d2, r2)
+      PT_CHILD(3, d3, r3)
+#undef PT_CHILD
+      if (!ANY) {
+#define PT_CSWAP(da, ra, db, rb)   \
+  if (db < da) {                   \
+    float tt = da;                 \
+    da = db;                       \
+    db = tt;                       \
+    int32_t tr = ra;               \
+    ra = rb;                       \
+    rb = tr;                       \
+  }
+        PT_CSWAP(d0, r0, d1, r1)
+        PT_CSWAP(d2, r2, d3, r3)
+        PT_CSWAP(d0, r0, d2, r2)
+        PT_CSWAP(d1, r1, d3, r3)
+        PT_CSWAP(d1, r1, d2, r2)
+#undef PT_CSWAP
       }
+      const int nh = (d0 < INFINITY) + (d1 < INFINITY) + (d2 < INFINITY) + (d3 < INFINITY);
       if (nh == 0) {
         if (sp == 0) break;
         ref = stack[(--sp) * stride];
@@ -197,8 +211,23 @@ __device__ bool traverse(const SceneView &S, V3 o, V3 d, float tmin, float tmax,
         *err = 1;
         break;
       }
-      for (int j = nh - 1; j >= 1; --j) stack[(sp++) * stride] = cref[j];
-      ref = cref[0];
+      // push the farther hits (far first), descend into the nearest
+      int32_t first = 0;
+      bool have = false;
+      if (ANY) {
+        // node order: descend into the first hit child, push the others
+        if (d3 < INFINITY) { first = r3; have = true; }
+        if (d2 < INFINITY) { if (have) stack[(sp++) * stride] = first; first = r2; have = true; }
+        if (d1 < INFINITY) { if (have) stack[(sp++) * stride] = first; first = r1; have = true; }
+        if (d0 < INFINITY) { if (have) stack[(sp++) * stride] = first; first = r0; have = true; }
+      } else {
+        if (d3 < INFINITY) stack[(sp++) * stride] = r3;
+        if (d2 < INFINITY) stack[(sp++) * stride] = r2;
+        if (d1 < INFINITY) stack[(sp++) * stride] = r1;
+        first = r0;  // d0 is the smallest and finite (nh > 0)
+        // r1..r3 were pushed only if hit; r0 is always the nearest hit
+      }
+      ref = first;
     } else {
       if (test_leaf<ANY>(S, ref, o, d, dn, tmin, tmax, hit)) {
         found = true;
