@@ -69,6 +69,24 @@ WORKLOADS = {
 }
 
 
+def sample_chunk(step: int, rank: int, world: int, n_chunks: int) -> int:
+    """Replica sharding: at each step every rank takes its own chunk of the
+    frame's sample grid (disjoint across ranks within a step; steps cycle
+    through the grid)."""
+    return (step * world + rank) % n_chunks
+
+
+def max_over_ranks(value: float, dist: bool, device=None) -> float:
+    """Max of a per-rank timing over all ranks (torch.distributed)."""
+    if not dist:
+        return value
+    import torch
+
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
 def build_scene(name):
     from pathtracer_gb300 import scene as S
 
@@ -204,9 +222,7 @@ def run_ours(args, rank, world, local_rank):
     k = args.spp_per_step
 
     def job_for(step):
-        # each rank takes its own sample range of the frame; steps cycle
-        # through the frame's spp_total samples
-        chunk = (step * world + rank) % max(1, spp_total // k)
+        chunk = sample_chunk(step, rank, world, max(1, spp_total // k))
         return N.job_desc(sid, cam, W, H, wl["sx"], wl["sy"], wl["depth"], rr_start=wl["rr"],
                           estimator=wl["est"], sampler=wl["sampler"], env_sampling=wl["env"], seed=1,
                           spp_begin=chunk * k, spp_end=chunk * k + k)
