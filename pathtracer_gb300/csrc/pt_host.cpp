@@ -27,11 +27,6 @@ namespace pt {
 static std::mutex g_err_mu;
 static std::string g_last_error;
 
-struct PtError : std::runtime_error {
-  int code;
-  PtError(int c, const std::string &m) : std::runtime_error(m), code(c) {}
-};
-
 void fail(int code, const std::string &msg) { throw PtError(code, msg); }
 void cuda_check(cudaError_t e, const char *what) {
   if (e != cudaSuccess) fail(PT_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));

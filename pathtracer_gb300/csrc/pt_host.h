@@ -4,6 +4,7 @@
 #include <cstddef>
 #include <map>
 #include <memory>
+#include <stdexcept>
 #include <string>
 #include <vector>
 
@@ -11,6 +12,12 @@
 #include "pt_kernels.h"
 
 namespace pt {
+
+// Error raised inside the library; the C-ABI turns it into its status code.
+struct PtError : std::runtime_error {
+  int code;
+  PtError(int c, const std::string &m) : std::runtime_error(m), code(c) {}
+};
 
 void fail(int code, const std::string &msg);
 void cuda_check(cudaError_t e, const char *what);

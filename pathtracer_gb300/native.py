@@ -31,7 +31,8 @@ ENV_UNIFORM, ENV_ALIAS = 0, 1
 # exported symbols of the C-ABI, in header order
 EXPORTS = [
     "pt_create", "pt_destroy", "pt_last_error", "pt_version", "pt_scene_upload", "pt_scene_release",
-    "pt_scene_info", "pt_render", "pt_render_device", "pt_profile_begin", "pt_profile_end", "pt_tonemap", "pt_sampler_eval", "pt_trace_closest",
+    "pt_scene_info", "pt_render", "pt_render_device", "pt_render_device_noalloc", "pt_profile_begin",
+    "pt_profile_end", "pt_tonemap", "pt_sampler_eval", "pt_trace_closest",
     "pt_trace_any", "pt_bsdf_eval", "pt_bsdf_sample", "pt_render_batch", "pt_server_create",
     "pt_server_destroy", "pt_submit", "pt_server_step", "pt_poll", "pt_cancel",
 ]
@@ -139,6 +140,7 @@ def load() -> C.CDLL:
         "pt_scene_info": [vp, C.c_int32, C.POINTER(C.c_int64)],
         "pt_render": [vp, C.POINTER(JobDesc), f32p, C.POINTER(Stats)],
         "pt_render_device": [vp, C.POINTER(JobDesc), vp, C.c_int, C.POINTER(Stats)],
+        "pt_render_device_noalloc": [vp, C.POINTER(JobDesc), vp, C.POINTER(Stats)],
         "pt_profile_begin": [vp],
         "pt_profile_end": [vp, C.POINTER(C.c_double), C.POINTER(C.c_int64)],
         "pt_tonemap": [vp, f32p, C.c_int32, C.c_int32, C.c_float, u8p],
