@@ -1,0 +1,485 @@
+// pathtracer_gb300.hpp -- C++ scene API over the C-ABI (header only).
+//
+// Mirrors the scene-building surface of 747745124/PathTracer so that a scene
+// function written against the reference compiles against this header with
+// `using namespace ptgb;`: materials (material.hpp:79-506, conductor.hpp,
+// dielectric.hpp, thinDielectric.hpp, disneyPrincipledBSDF.hpp,
+// hairMarsch.hpp), primitives (primitive.hpp:81-273, triangleMesh.hpp,
+// mesh_io/meshData.hpp), decorators (utils/objectTransform.hpp), lights
+// (envLight.hpp), the camera (base/camera.hpp) and SceneInfo
+// (render/renderManager.hpp:35-176).  SceneInfo::render flattens the object
+// list and renders it on the GPU through include/pathtracer_gb300.h instead
+// of looping over pixels with getRayColor.
+//
+// Transforms are baked into the uploaded geometry: Translate/Scale keep
+// rectangles axis aligned; a rotated rectangle becomes a two-triangle mesh.
+#pragma once
+#include <array>
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "pathtracer_gb300.h"
+
+namespace ptgb {
+
+struct vec3 {
+  float v[3] = {0, 0, 0};
+  vec3() = default;
+  explicit vec3(float s) : v{s, s, s} {}
+  vec3(float a, float b, float c) : v{a, b, c} {}
+  float x() const { return v[0]; }
+  float y() const { return v[1]; }
+  float z() const { return v[2]; }
+  float operator[](int i) const { return v[i]; }
+  float &operator[](int i) { return v[i]; }
+};
+inline vec3 operator+(vec3 a, vec3 b) { return {a[0] + b[0], a[1] + b[1], a[2] + b[2]}; }
+inline vec3 operator*(vec3 a, float s) { return {a[0] * s, a[1] * s, a[2] * s}; }
+struct vec2 {
+  float v[2] = {0, 0};
+  vec2() = default;
+  vec2(float a, float b) : v{a, b} {}
+};
+inline float to_radian(float deg) { return deg * 3.14159265358979323846f / 180.f; }
+
+enum class TransportMode { Radiance, Importance };
+enum class Axis { X = 0, Y = 1, Z = 2 };
+
+// ------------------------------------------------------------- materials
+class Material {
+ public:
+  virtual ~Material() = default;
+  virtual pt_material_desc desc() const = 0;
+  virtual bool is_emitter() const { return false; }
+};
+namespace detail {
+inline pt_material_desc make(int32_t type, std::initializer_list<float> p, int32_t flags = 0) {
+  pt_material_desc d{};
+  d.type = type;
+  d.flags = flags;
+  int i = 0;
+  for (float x : p) d.p[i++] = x;
+  return d;
+}
+}  // namespace detail
+
+class Lambertian : public Material {
+ public:
+  explicit Lambertian(vec3 albedo) : a(albedo) {}
+  pt_material_desc desc() const override { return detail::make(PT_MAT_LAMBERTIAN, {a[0], a[1], a[2]}); }
+  vec3 a;
+};
+class Conductor : public Material {
+ public:
+  Conductor(vec3 eta, vec3 k, float ax, float ay) : eta(eta), k(k), ax(ax), ay(ay) {}
+  pt_material_desc desc() const override {
+    return detail::make(PT_MAT_CONDUCTOR, {eta[0], eta[1], eta[2], k[0], k[1], k[2], ax, ay});
+  }
+  vec3 eta, k;
+  float ax, ay;
+};
+class MFDielectric : public Material {
+ public:
+  MFDielectric(float eta, float ax, float ay) : eta(eta), ax(ax), ay(ay) {}
+  pt_material_desc desc() const override { return detail::make(PT_MAT_MF_DIELECTRIC, {eta, ax, ay}); }
+  float eta, ax, ay;
+};
+class ThinDielectric : public Material {
+ public:
+  explicit ThinDielectric(float eta, bool split = false) : eta(eta), split(split) {}
+  pt_material_desc desc() const override {
+    return detail::make(PT_MAT_THIN_DIELECTRIC, {eta}, split ? PT_MAT_FLAG_SPLIT_RAY : 0);
+  }
+  float eta;
+  bool split;
+};
+class Phong : public Material {
+ public:
+  Phong(vec3 diffuse, vec3 specular, vec3 ambient, float shininess)
+      : d(diffuse), s(specular), a(ambient), n(shininess) {}
+  pt_material_desc desc() const override {
+    return detail::make(PT_MAT_PHONG, {d[0], d[1], d[2], s[0], s[1], s[2], a[0], a[1], a[2], n});
+  }
+  vec3 d, s, a;
+  float n;
+};
+class DisneyPrincipledBSDF : public Material {
+ public:
+  DisneyPrincipledBSDF(vec3 base, float specular_transmission, float metallic, float subsurface, float specular,
+                       float roughness, float specular_tint, float anisotropic, float sheen, float sheen_tint,
+                       float clearcoat, float clearcoat_gloss, float eta)
+      : p{base[0], base[1], base[2], specular_transmission, metallic, subsurface, specular, roughness,
+          specular_tint, anisotropic, sheen, sheen_tint, clearcoat, clearcoat_gloss, eta} {}
+  pt_material_desc desc() const override {
+    pt_material_desc d{};
+    d.type = PT_MAT_DISNEY;
+    for (int i = 0; i < 15; ++i) d.p[i] = p[i];
+    return d;
+  }
+  float p[15];
+};
+class HairMarschner : public Material {
+ public:
+  HairMarschner(vec3 sigma_a, float h, float eta, float beta_m, float beta_n, float alpha)
+      : p{sigma_a[0], sigma_a[1], sigma_a[2], h, eta, beta_m, beta_n, alpha} {}
+  pt_material_desc desc() const override {
+    pt_material_desc d{};
+    d.type = PT_MAT_HAIR;
+    for (int i = 0; i < 8; ++i) d.p[i] = p[i];
+    return d;
+  }
+  float p[8];
+};
+class DiffuseEmitter : public Material {
+ public:
+  explicit DiffuseEmitter(vec3 color, float intensity = 1.0f) : c(color), i(intensity) {}
+  pt_material_desc desc() const override { return detail::make(PT_MAT_DIFFUSE_EMITTER, {c[0], c[1], c[2], i}); }
+  bool is_emitter() const override { return true; }
+  vec3 c;
+  float i;
+};
+
+// ------------------------------------------------------------ geometry
+struct MeshData {  // mesh_io/meshData.hpp:6-13
+  std::vector<vec3> positions, normals;
+  std::vector<vec2> uvs;
+  std::vector<std::array<int, 3>> indices, normalIndices, uvIndices;
+};
+
+// Flattened geometry of one object, in world space.
+struct Flat {
+  enum Kind { MESH, QUAD, SPHERE } kind = MESH;
+  std::vector<float> pos, nrm;
+  std::vector<int32_t> idx;
+  pt_quad_desc quad{};
+  pt_sphere_desc sphere{};
+  std::shared_ptr<Material> mat;
+};
+
+class Hittable {
+ public:
+  virtual ~Hittable() = default;
+  virtual Flat flatten() const = 0;
+};
+
+class Sphere : public Hittable {
+ public:
+  Sphere(vec3 c, float r, std::shared_ptr<Material> m) : c(c), r(r), m(std::move(m)) {}
+  Flat flatten() const override {
+    Flat f;
+    f.kind = Flat::SPHERE;
+    f.sphere.center[0] = c[0];
+    f.sphere.center[1] = c[1];
+    f.sphere.center[2] = c[2];
+    f.sphere.radius = r;
+    f.mat = m;
+    return f;
+  }
+  vec3 c;
+  float r;
+  std::shared_ptr<Material> m;
+};
+
+template <Axis A>
+class AARectangle : public Hittable {
+ public:
+  AARectangle(float k, float d0_min, float d0_max, float d1_min, float d1_max, std::shared_ptr<Material> m)
+      : k(k), a0(d0_min), a1(d0_max), b0(d1_min), b1(d1_max), m(std::move(m)) {}
+  Flat flatten() const override {
+    Flat f;
+    f.kind = Flat::QUAD;
+    f.quad = pt_quad_desc{(int32_t)A, k, a0, a1, b0, b1, 0, 0};
+    f.mat = m;
+    return f;
+  }
+  float k, a0, a1, b0, b1;
+  std::shared_ptr<Material> m;
+};
+using XYRectangle = AARectangle<Axis::Z>;
+using XZRectangle = AARectangle<Axis::Y>;
+using YZRectangle = AARectangle<Axis::X>;
+
+class TriangleMesh : public Hittable {
+ public:
+  TriangleMesh(MeshData &&d, std::shared_ptr<Material> m) : d(std::move(d)), m(std::move(m)) {}
+  Flat flatten() const override {
+    Flat f;
+    f.kind = Flat::MESH;
+    for (auto &p : d.positions) f.pos.insert(f.pos.end(), {p[0], p[1], p[2]});
+    // per-corner normals (normalIndices) are expanded to the position layout
+    const bool has_n = !d.normals.empty() && d.normalIndices.size() == d.indices.size();
+    if (has_n) f.nrm.assign(f.pos.size(), 0.f);
+    for (size_t t = 0; t < d.indices.size(); ++t)
+      for (int k = 0; k < 3; ++k) {
+        f.idx.push_back(d.indices[t][k]);
+        if (has_n) {
+          const vec3 &n = d.normals[d.normalIndices[t][k]];
+          for (int c = 0; c < 3; ++c) f.nrm[3 * d.indices[t][k] + c] = n[c];
+        }
+      }
+    f.mat = m;
+    return f;
+  }
+  MeshData d;
+  std::shared_ptr<Material> m;
+};
+
+namespace detail {
+inline Flat quad_to_mesh(const Flat &q) {
+  Flat f;
+  f.kind = Flat::MESH;
+  f.mat = q.mat;
+  const pt_quad_desc &d = q.quad;
+  auto put = [&](float a, float b) {
+    float v[3];
+    v[d.axis] = d.k;
+    v[d.axis == 0 ? 1 : 0] = a;
+    v[d.axis == 2 ? 1 : 2] = b;
+    f.pos.insert(f.pos.end(), {v[0], v[1], v[2]});
+  };
+  put(d.d0_min, d.d1_min);
+  put(d.d0_max, d.d1_min);
+  put(d.d0_max, d.d1_max);
+  put(d.d0_min, d.d1_max);
+  f.idx = {0, 1, 2, 0, 2, 3};
+  return f;
+}
+}  // namespace detail
+
+// objectTransform.hpp decorators, baked into the flattened geometry
+class FlipFace : public Hittable {
+ public:
+  explicit FlipFace(std::shared_ptr<Hittable> o) : o(std::move(o)) {}
+  Flat flatten() const override {
+    Flat f = o->flatten();
+    if (f.kind == Flat::QUAD) f.quad.flip_face ^= 1;
+    if (f.kind == Flat::SPHERE) f.sphere.flip_face ^= 1;
+    if (f.kind == Flat::MESH)  // reversed winding toggles the front-face flag
+      for (size_t t = 0; t + 2 < f.idx.size(); t += 3) std::swap(f.idx[t + 1], f.idx[t + 2]);
+    return f;
+  }
+  std::shared_ptr<Hittable> o;
+};
+class Translate : public Hittable {
+ public:
+  Translate(std::shared_ptr<Hittable> o, vec3 off) : o(std::move(o)), off(off) {}
+  Flat flatten() const override {
+    Flat f = o->flatten();
+    if (f.kind == Flat::MESH)
+      for (size_t i = 0; i < f.pos.size(); ++i) f.pos[i] += off[(int)(i % 3)];
+    if (f.kind == Flat::SPHERE)
+      for (int c = 0; c < 3; ++c) f.sphere.center[c] += off[c];
+    if (f.kind == Flat::QUAD) {
+      const int a = f.quad.axis, a0 = a == 0 ? 1 : 0, a1 = a == 2 ? 1 : 2;
+      f.quad.k += off[a];
+      f.quad.d0_min += off[a0];
+      f.quad.d0_max += off[a0];
+      f.quad.d1_min += off[a1];
+      f.quad.d1_max += off[a1];
+    }
+    return f;
+  }
+  std::shared_ptr<Hittable> o;
+  vec3 off;
+};
+class Scale : public Hittable {
+ public:
+  Scale(std::shared_ptr<Hittable> o, float s) : o(std::move(o)), s(s) {}
+  Flat flatten() const override {
+    Flat f = o->flatten();
+    for (float &x : f.pos) x *= s;
+    if (f.kind == Flat::SPHERE) {
+      for (int c = 0; c < 3; ++c) f.sphere.center[c] *= s;
+      f.sphere.radius *= s;
+    }
+    if (f.kind == Flat::QUAD) {
+      f.quad.k *= s;
+      f.quad.d0_min *= s;
+      f.quad.d0_max *= s;
+      f.quad.d1_min *= s;
+      f.quad.d1_max *= s;
+    }
+    return f;
+  }
+  std::shared_ptr<Hittable> o;
+  float s;
+};
+template <Axis A>
+class Rotate : public Hittable {
+ public:
+  Rotate(std::shared_ptr<Hittable> o, float radians) : o(std::move(o)), r(radians) {}
+  Flat flatten() const override {
+    Flat f = o->flatten();
+    if (f.kind == Flat::QUAD) f = detail::quad_to_mesh(f);
+    const float c = std::cos(r), s = std::sin(r);
+    const int i = A == Axis::X ? 1 : A == Axis::Y ? 2 : 0, j = A == Axis::X ? 2 : A == Axis::Y ? 0 : 1;
+    auto rot = [&](float *p) {
+      float a = p[i], b = p[j];
+      p[i] = c * a - s * b;
+      p[j] = s * a + c * b;
+    };
+    for (size_t k = 0; k + 2 < f.pos.size(); k += 3) rot(&f.pos[k]);
+    for (size_t k = 0; k + 2 < f.nrm.size(); k += 3) rot(&f.nrm[k]);
+    if (f.kind == Flat::SPHERE) rot(f.sphere.center);
+    return f;
+  }
+  std::shared_ptr<Hittable> o;
+  float r;
+};
+
+class ObjectList {  // base/objectList.hpp
+ public:
+  void addObject(std::shared_ptr<Hittable> h) { objects.push_back(std::move(h)); }
+  const std::vector<std::shared_ptr<Hittable>> &getLists() const { return objects; }
+  std::vector<std::shared_ptr<Hittable>> objects;
+};
+
+// EnvironmentLight over texels given in memory (row 0 = bottom, RGB).
+class EnvironmentLight {
+ public:
+  EnvironmentLight(std::vector<float> texels, int width, int height, float intensity = 1.0f)
+      : texels(std::move(texels)), width(width), height(height), intensity(intensity) {}
+  std::vector<float> texels;
+  int width, height;
+  float intensity;
+};
+
+class PerspectiveCamera {  // base/camera.hpp
+ public:
+  PerspectiveCamera(float fov, float aspect, float focalDist, float aperture, vec3 up, vec3 front, vec3 position)
+      : fov(fov), aspect(aspect), focalDist(focalDist), aperture(aperture), up(up), front(front), position(position) {}
+  float fov, aspect, focalDist, aperture;
+  vec3 up, front, position;
+};
+
+// SceneInfo (render/renderManager.hpp:35-176): render() uploads the scene and
+// renders it through the C-ABI; the film and the tone-mapped bytes are kept.
+struct SceneInfo {
+  std::shared_ptr<PerspectiveCamera> camera;
+  ObjectList objects;
+  std::shared_ptr<EnvironmentLight> environment_light;
+  vec3 bg_color = vec3(0.7f, 0.8f, 1.0f);
+  uint32_t _width = 800, _height = 800, spp_x = 2, spp_y = 2;
+  float _gamma = 1.0f;
+  uint32_t max_depth = 10;                   // MAX_RAY_DEPTH (config.hpp:7)
+  int32_t estimator = PT_EST_NEE_MIS;
+  int32_t device = 0;
+  std::vector<float> film;                   // mean radiance [j][i][c], j = 0 bottom
+  std::vector<uint8_t> rgb8;                 // tone-mapped, row 0 top
+
+  void render(const std::string &out_path = "") {
+    if (!camera) throw std::runtime_error("Camera is not initialized!");
+    if (objects.getLists().empty()) throw std::runtime_error("No objects in the scene!");
+    std::vector<pt_material_desc> mats;
+    std::vector<Flat> flats;
+    std::vector<pt_mesh_desc> meshes;
+    std::vector<pt_quad_desc> quads;
+    std::vector<pt_sphere_desc> spheres;
+    std::vector<pt_object_desc> objs;
+    for (auto &h : objects.getLists()) flats.push_back(h->flatten());
+    meshes.reserve(flats.size());
+    for (auto &f : flats) {
+      mats.push_back(f.mat->desc());
+      const int32_t mi = (int32_t)mats.size() - 1;
+      if (f.kind == Flat::MESH) {
+        pt_mesh_desc m{};
+        m.positions = f.pos.data();
+        m.n_positions = (int32_t)(f.pos.size() / 3);
+        if (!f.nrm.empty()) {
+          m.normals = f.nrm.data();
+          m.n_normals = m.n_positions;
+        }
+        m.indices = f.idx.data();
+        m.n_triangles = (int32_t)(f.idx.size() / 3);
+        m.material = mi;
+        meshes.push_back(m);
+        objs.push_back({PT_OBJ_MESH, (int32_t)meshes.size() - 1});
+      } else if (f.kind == Flat::QUAD) {
+        f.quad.material = mi;
+        quads.push_back(f.quad);
+        objs.push_back({PT_OBJ_QUAD, (int32_t)quads.size() - 1});
+      } else {
+        f.sphere.material = mi;
+        spheres.push_back(f.sphere);
+        objs.push_back({PT_OBJ_SPHERE, (int32_t)spheres.size() - 1});
+      }
+    }
+    pt_scene_desc d{};
+    d.materials = mats.data();
+    d.n_materials = (int32_t)mats.size();
+    d.meshes = meshes.data();
+    d.n_meshes = (int32_t)meshes.size();
+    d.quads = quads.data();
+    d.n_quads = (int32_t)quads.size();
+    d.spheres = spheres.data();
+    d.n_spheres = (int32_t)spheres.size();
+    d.objects = objs.data();
+    d.n_objects = (int32_t)objs.size();
+    pt_env_desc env{};
+    if (environment_light) {
+      env = pt_env_desc{environment_light->texels.data(), environment_light->width, environment_light->height,
+                        environment_light->intensity};
+      d.env = &env;
+    }
+    for (int c = 0; c < 3; ++c) d.bg_color[c] = bg_color[c];
+    void *ctx = nullptr;
+    check(pt_create(&ctx, device), nullptr);
+    int32_t sid = 0;
+    try {
+      check(pt_scene_upload(ctx, &d, &sid), ctx);
+      pt_job_desc j{};
+      j.scene = sid;
+      j.width = (int32_t)_width;
+      j.height = (int32_t)_height;
+      j.spp_x = (int32_t)spp_x;
+      j.spp_y = (int32_t)spp_y;
+      j.max_depth = (int32_t)max_depth;
+      j.rr_start = -1;
+      j.estimator = estimator;
+      j.sampler = PT_SAMPLER_HALTON_OWEN;
+      j.env_sampling = estimator == PT_EST_NEE_MIS ? PT_ENV_ALIAS : PT_ENV_UNIFORM;
+      j.light_samples_x = 2;
+      j.light_samples_y = 2;
+      const PerspectiveCamera &c = *camera;
+      j.camera = pt_camera_desc{c.fov, c.aspect, c.focalDist, c.aperture, {c.up[0], c.up[1], c.up[2]},
+                                {c.front[0], c.front[1], c.front[2]},
+                                {c.position[0], c.position[1], c.position[2]}, 0.f};
+      j.gamma = _gamma;
+      film.assign((size_t)_width * _height * 3, 0.f);
+      check(pt_render(ctx, &j, film.data(), nullptr), ctx);
+      rgb8.assign(film.size(), 0);
+      check(pt_tonemap(ctx, film.data(), (int32_t)_width, (int32_t)_height, _gamma, rgb8.data()), ctx);
+      pt_scene_release(ctx, sid);
+    } catch (...) {
+      pt_destroy(ctx);
+      throw;
+    }
+    pt_destroy(ctx);
+    if (!out_path.empty()) write_ppm(out_path);
+  }
+
+  // Binary PPM of the tone-mapped image (PNG output is host I/O left to the caller).
+  void write_ppm(const std::string &path) const {
+    FILE *f = std::fopen(path.c_str(), "wb");
+    if (!f) throw std::runtime_error("cannot open " + path);
+    std::fprintf(f, "P6\n%u %u\n255\n", _width, _height);
+    std::fwrite(rgb8.data(), 1, rgb8.size(), f);
+    std::fclose(f);
+  }
+
+ private:
+  static void check(int rc, void *ctx) {
+    if (rc != PT_OK) {
+      char buf[512] = {0};
+      pt_last_error(ctx, buf, sizeof buf);
+      throw std::runtime_error(std::string("pathtracer_gb300: ") + buf);
+    }
+  }
+};
+
+}  // namespace ptgb
