@@ -129,6 +129,10 @@ enum { PT_OBJ_MESH = 0, PT_OBJ_QUAD = 1, PT_OBJ_SPHERE = 2 };
 typedef struct pt_object_desc {
   int32_t kind;
   int32_t index;
+  /* Extension (motion blur): linear velocity in scene units per unit of
+   * shutter time; the object sits at its described position + velocity * t
+   * for a ray of time t in [0, camera.shutter].  Zero: static. */
+  float velocity[3];
 } pt_object_desc;
 
 /* EnvironmentLight + HDRITexture (include/light/envLight.hpp:4,
@@ -165,6 +169,11 @@ typedef struct pt_scene_desc {
   const pt_medium_desc *medium; /* NULL: vacuum */
   float bg_color[3];            /* SceneInfo::bg_color, renderManager.hpp:41 */
   int32_t bvh_mode;             /* PT_BVH_REFERENCE (default) */
+  /* Extension (motion blur): the longest shutter a job may use on this
+   * scene; the BVH boxes of moving objects cover their motion over
+   * [0, shutter_max].  Jobs with camera.shutter > shutter_max are rejected
+   * when the scene has moving objects. */
+  float shutter_max;
 } pt_scene_desc;
 
 enum { PT_BVH_REFERENCE = 0 };
@@ -180,7 +189,9 @@ typedef struct pt_camera_desc {
   float up[3];
   float front[3];
   float position[3];
-  float shutter;    /* motion-blur shutter length (extension); 0 = off */
+  float shutter;    /* motion-blur shutter length (extension); 0 = off.  A
+                     * path's time is shutter * u, u from its own counter
+                     * stream, and every ray of the path uses it. */
 } pt_camera_desc;
 
 /* Estimator.  REF_NEE restates include/integrator/maxdepth_nee.hpp:9-256
@@ -336,6 +347,22 @@ int pt_bsdf_sample(void *ctx, const pt_material_desc *mat, int32_t n,
  * reference, which renders one scene per process. */
 int pt_render_batch(void *ctx, const pt_job_desc *jobs, int32_t n_jobs,
                     float **films, pt_stats *stats);
+
+/* Launch autotuner (extension): renders the batch under candidate launch
+ * configurations -- paths per wave of each job, material sorting on/off,
+ * blocks per SM of the traversal and shade kernels -- keeps the fastest for
+ * later renders on this context and reports it.  films of the tuning renders
+ * are discarded. */
+typedef struct pt_tuning {
+  int32_t wave_paths;
+  int32_t sort_by_material;
+  int32_t trace_blocks;
+  int32_t shade_blocks;
+  double best_ms;
+  double default_ms;
+  int32_t candidates;
+} pt_tuning;
+int pt_autotune(void *ctx, const pt_job_desc *jobs, int32_t n_jobs, pt_tuning *out);
 
 /* ------------------------------------------------------------- serving
  * A request loop over resident scenes with continuous batching.  Requests

@@ -692,6 +692,8 @@ struct MeshO {
 
 struct Obj {
   int kind, index;
+  V vel;               // motion blur (extension): position + vel * time
+  bool moving = false;
   Box box;
   int mat, flip, prim;
   int light = -1;
@@ -706,6 +708,8 @@ struct Obj {
 struct Light {
   int type;  // 0 quad, 1 sphere, 2 env
   V v0, e1, e2, normal, c, color;
+  V vel;
+  bool moving = false;
   float radius = 0, area = 0, intensity = 0;
 };
 
@@ -731,12 +735,17 @@ struct Scene {
   V sig_a, sig_s;
   float sig_t_max = 0.f;
 
-  // Sphere / AARectangle / TriangleMesh intersect (+ FlipFace, set_normal)
-  bool hit_obj(int oi, V o, V d, float tmin, float tmax, Hit &rec) const {
+  // Sphere / AARectangle / TriangleMesh intersect (+ FlipFace, set_normal).
+  // A moving object (extension) is intersected in its own frame at the ray's
+  // time: origin o - vel * time; the hit position is then taken on the world
+  // ray.
+  bool hit_obj(int oi, V o_w, V d, float tmin, float tmax, Hit &rec, float time) const {
     const Obj &ob = objs[oi];
+    const V o = ob.moving ? V(o_w.x - ob.vel.x * time, o_w.y - ob.vel.y * time, o_w.z - ob.vel.z * time) : o_w;
     if (ob.kind == PT_OBJ_MESH) {
       const MeshO &M = meshes[ob.index];
       if (!M.hit_node(0, o, d, tmin, tmax, rec)) return false;
+      if (ob.moving) rec.position = o_w + rec.t * d;
       rec.set_normal(d, rec.normal);
       rec.mat = M.mat;
       rec.light = -1;
@@ -750,7 +759,7 @@ struct Scene {
       float q0 = o[a0] + t * dn[a0], q1 = o[a1] + t * dn[a1];
       if (q0 < ob.d0min || q0 > ob.d0max || q1 < ob.d1min || q1 > ob.d1max) return false;
       rec.t = t;
-      rec.position = o + t * dn;
+      rec.position = o_w + t * dn;
       V nn(a == 0 ? 1.f : 0.f, a == 1 ? 1.f : 0.f, a == 2 ? 1.f : 0.f);
       rec.set_normal(d, nn);
     } else {  // primitive.hpp:124-170
@@ -765,8 +774,10 @@ struct Scene {
         if (t < tmin || t > tmax) return false;
       }
       rec.t = t;
-      rec.position = o + t * dn;
-      rec.set_normal(d, (rec.position - ob.c).normalize());
+      rec.position = o_w + t * dn;
+      const V c = ob.moving ? V(ob.c.x + ob.vel.x * time, ob.c.y + ob.vel.y * time, ob.c.z + ob.vel.z * time)
+                            : ob.c;
+      rec.set_normal(d, (rec.position - c).normalize());
     }
     if (ob.flip) rec.is_inside = !rec.is_inside;
     rec.mat = ob.mat;
@@ -774,17 +785,17 @@ struct Scene {
     rec.light = ob.light;
     return true;
   }
-  bool hit_ref(int ref, V o, V d, float tmin, float tmax, Hit &rec) const {
-    if (ref < 0) return hit_obj(~ref, o, d, tmin, tmax, rec);
+  bool hit_ref(int ref, V o, V d, float tmin, float tmax, Hit &rec, float time) const {
+    if (ref < 0) return hit_obj(~ref, o, d, tmin, tmax, rec, time);
     // BVHNode::intersect (bvh.hpp:27-41): left, then right with tmax = left.t
     const TNode &N = top[ref];
     if (!N.box.hit(o, d, tmin, tmax)) return false;
-    bool lh = hit_ref(N.left, o, d, tmin, tmax, rec);
-    bool rh = hit_ref(N.right, o, d, tmin, lh ? rec.t : tmax, rec);
+    bool lh = hit_ref(N.left, o, d, tmin, tmax, rec, time);
+    bool rh = hit_ref(N.right, o, d, tmin, lh ? rec.t : tmax, rec, time);
     return lh || rh;
   }
-  bool intersect(V o, V d, Hit &rec, float tmin = 0.0001f, float tmax = 1e5f) const {
-    return hit_ref(root, o, d, tmin, tmax, rec);
+  bool intersect(V o, V d, Hit &rec, float tmin = 0.0001f, float tmax = 1e5f, float time = 0.f) const {
+    return hit_ref(root, o, d, tmin, tmax, rec, time);
   }
   Box ref_box(int ref) const { return ref < 0 ? objs[~ref].box : top[ref].box; }
   // BVHNode ctor (bvh.hpp:46-102): halves of the insertion order, rand()
@@ -890,6 +901,8 @@ Scene *build_scene(const pt_scene_desc *d) {
     Obj ob{};
     ob.kind = od.kind;
     ob.index = od.index;
+    ob.vel = V(od.velocity[0], od.velocity[1], od.velocity[2]);
+    ob.moving = od.velocity[0] != 0.f || od.velocity[1] != 0.f || od.velocity[2] != 0.f;
     if (od.kind == PT_OBJ_MESH) {
       ob.box = S->meshes[od.index].aabb;
       ob.mat = d->meshes[od.index].material;
@@ -922,6 +935,10 @@ Scene *build_scene(const pt_scene_desc *d) {
       ob.prim = n_tris + d->n_quads + od.index;
       ob.box = Box{ob.c - V(s.radius), ob.c + V(s.radius)};
     }
+    if (ob.moving) {  // the box covers the motion over [0, shutter_max]
+      const V sw = ob.vel * std::max(0.f, d->shutter_max);
+      ob.box = merge(ob.box, Box{ob.box.lo + sw, ob.box.hi + sw});
+    }
     S->objs.push_back(ob);
   }
   std::srand(1);
@@ -934,6 +951,8 @@ Scene *build_scene(const pt_scene_desc *d) {
     Light L{};
     L.intensity = m.p[3];
     L.color = V(m.p[0], m.p[1], m.p[2]);
+    L.vel = ob.vel;
+    L.moving = ob.moving;
     if (ob.kind == PT_OBJ_QUAD) {
       auto put = [&](float a, float b) {
         V v;
@@ -1029,6 +1048,7 @@ struct PathCtx {
   uint64_t key;
   uint32_t halton_index;
   int pixel, k;
+  float time = 0.f;  // motion blur (extension): the path's time
 };
 
 static float dim_value(const PathCtx &P, int dim) {
@@ -1092,14 +1112,17 @@ static LightSample sample_light(const PathCtx &P, V x, V n, int bounce, int ls, 
     return r;
   }
   V lp, ln;
+  const float tm = P.time;
   if (L.type == 0) {  // QuadLight::get_sample / get_normal_at
     lp = L.v0 + ox * L.e1 + oy * L.e2;
+    if (L.moving) lp = V(lp.x + L.vel.x * tm, lp.y + L.vel.y * tm, lp.z + L.vel.z * tm);
     ln = L.normal;
   } else {  // SphereLight::get_sample
     float theta = (float)(2 * PI * ox);
     float phi = std::acos(2 * oy - 1);
-    lp = L.c + L.radius * V(std::sin(phi) * std::cos(theta), std::sin(phi) * std::sin(theta), std::cos(phi));
-    ln = (lp - L.c).normalize();
+    const V c = L.moving ? V(L.c.x + L.vel.x * tm, L.c.y + L.vel.y * tm, L.c.z + L.vel.z * tm) : L.c;
+    lp = c + L.radius * V(std::sin(phi) * std::cos(theta), std::sin(phi) * std::sin(theta), std::cos(phi));
+    ln = (lp - c).normalize();
   }
   V ld = lp - x;
   float len = ld.length();
@@ -1123,7 +1146,7 @@ static V ray_color_ref(const PathCtx &P, V o, V d, int depth, int bounce) {
   const pt_job_desc &j = *P.job;
   if (depth == 0) return V(0.f);
   Hit rec;
-  if (!S.intersect(o, d, rec)) {
+  if (!S.intersect(o, d, rec, 0.0001f, 1e5f, P.time)) {
     if (S.has_env) return S.env_le(d.normalize());
     return S.bg;
   }
@@ -1155,7 +1178,7 @@ static V ray_color_ref(const PathCtx &P, V o, V d, int depth, int bounce) {
       float V_ = 0.f;
       if (L.valid) {
         Hit sh;
-        V_ = S.intersect(rec.position, L.wl, sh, 0.001f, L.tmax) ? 0.f : 1.f;
+        V_ = S.intersect(rec.position, L.wl, sh, 0.001f, L.tmax, P.time) ? 0.f : 1.f;
       }
       if (V_ > 0.f && L.pdf > 1e-7f) light_term += mat_f(M, wo, L.wl, rec) * L.Le * L.G / L.pdf;
     }
@@ -1163,7 +1186,7 @@ static V ray_color_ref(const PathCtx &P, V o, V d, int depth, int bounce) {
   }
   if (depth - 1 == 0) return mat_emit(M, d, rec) + light_term;
   Hit next;
-  bool nh = S.intersect(rec.position, wi, next);
+  bool nh = S.intersect(rec.position, wi, next, 0.0001f, 1e5f, P.time);
   if (nh && S.mats[next.mat].type == PT_MAT_DIFFUSE_EMITTER) return mat_emit(M, d, rec) + light_term;
   V att = s.att;
   if (j.rr_start >= 0 && bounce >= j.rr_start) {  // roulette_naive.hpp:35-38 on the continuation
@@ -1188,7 +1211,7 @@ static V ray_color_iter(const PathCtx &P, V o, V d) {
   const int dpb = S.medium ? 4 : 3;
   for (int bounce = 0; bounce < limit; ++bounce) {
     Hit rec;
-    bool hit = S.intersect(o, d, rec);
+    bool hit = S.intersect(o, d, rec, 0.0001f, 1e5f, P.time);
     const uint32_t rbase = 64u + 32u * (uint32_t)bounce;
     bool in_medium = false;
     float t_s = 0.f;
@@ -1218,7 +1241,7 @@ static V ray_color_iter(const PathCtx &P, V o, V d) {
         }
         if (G <= 0.f) continue;
         Hit sh;
-        if (S.intersect(x, Ls.wl, sh, 0.001f, Ls.tmax)) continue;
+        if (S.intersect(x, Ls.wl, sh, 0.001f, Ls.tmax, P.time)) continue;
         float w = mis ? power_heuristic((float)LN, pl, 1.f, phase) : 1.f;
         float tr = std::exp(-S.sig_t_max * std::sqrt(Ls.d2));
         L += beta * Ls.Le * (phase * G / pl * w * tr / (float)LN);
@@ -1252,7 +1275,9 @@ static V ray_color_iter(const PathCtx &P, V o, V d) {
       } else if (mis) {
         if (rec.light >= 0) {
           const Light &Lt = S.lights[rec.light];
-          V ln = Lt.type == 0 ? Lt.normal : (rec.position - Lt.c).normalize();
+          const V lc = Lt.moving ? V(Lt.c.x + Lt.vel.x * P.time, Lt.c.y + Lt.vel.y * P.time, Lt.c.z + Lt.vel.z * P.time)
+                                 : Lt.c;
+          V ln = Lt.type == 0 ? Lt.normal : (rec.position - lc).normalize();
           float cl = dot(ln, -d.normalize());
           if (cl > 0.f) {
             float pl = rec.t * rec.t / (cl * Lt.area * (float)S.lights.size());
@@ -1298,7 +1323,7 @@ static V ray_color_iter(const PathCtx &P, V o, V d) {
         V c = f * Ls.Le * (G / pl * w / (float)LN);
         if (c.x == 0.f && c.y == 0.f && c.z == 0.f) continue;
         Hit sh;
-        if (S.intersect(rec.position, Ls.wl, sh, 0.001f, Ls.tmax)) continue;
+        if (S.intersect(rec.position, Ls.wl, sh, 0.001f, Ls.tmax, P.time)) continue;
         float tr = S.medium ? (Ls.env ? 0.f : std::exp(-S.sig_t_max * std::sqrt(Ls.d2))) : 1.f;
         lt += beta * c * tr;
       }
@@ -1436,6 +1461,7 @@ int or_render(void *s, const pt_job_desc *job, float *mean, float *var, int thre
         for (int k = b; k < e; ++k) {
           uint64_t lin = ((uint64_t)i * H + jj) * (uint64_t)Sn + k;
           PathCtx P{&S, &j, path_key(j.seed, lin), (uint32_t)(lin + 1u), jj * W + i, k};
+          P.time = j.camera.shutter > 0.f ? j.camera.shutter * rand01(P.key, 3u) : 0.f;
           float u = ((float)i + off[k].first) / (float)W, v = ((float)jj + off[k].second) / (float)H;
           float lx = -cam.r + (cam.r - -cam.r) * rand01(P.key, 1u);
           float ly = -cam.r + (cam.r - -cam.r) * rand01(P.key, 2u);

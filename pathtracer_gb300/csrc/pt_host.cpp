@@ -195,6 +195,7 @@ struct BNode {
 
 struct Builder {
   const pt_scene_desc *d;
+  float sweep[3] = {0.f, 0.f, 0.f};  // motion of the object being built over [0, shutter_max]
   std::vector<BNode> nodes;
   std::vector<int> leaf_prims;    // global prim ids in leaf order
   std::vector<int> tri_base;      // first global prim id of each mesh
@@ -224,7 +225,7 @@ struct Builder {
     }
     int me = (int)nodes.size();
     nodes.push_back(BNode());
-    nodes[me].box = pb;
+    nodes[me].box = swept(pb);
     int count = (int)ids.size();
     if (count <= 4) {
       nodes[me].first = (int)leaf_prims.size();
@@ -283,8 +284,19 @@ struct Builder {
     return b;
   }
 
+  // A moving object's boxes cover its whole motion: box | box + sweep.
+  Box swept(const Box &b) const {
+    Box r = b;
+    for (int a = 0; a < 3; ++a) {
+      r.lo[a] = std::min(b.lo[a], b.lo[a] + sweep[a]);
+      r.hi[a] = std::max(b.hi[a], b.hi[a] + sweep[a]);
+    }
+    return r;
+  }
+
   int object_subtree(int o) {
     const pt_object_desc &od = d->objects[o];
+    for (int a = 0; a < 3; ++a) sweep[a] = od.velocity[a] * std::max(0.f, d->shutter_max);
     if (od.kind == PT_OBJ_MESH) {
       const pt_mesh_desc &m = d->meshes[od.index];
       std::vector<int> ids(m.n_triangles);
@@ -293,7 +305,7 @@ struct Builder {
     }
     int me = (int)nodes.size();
     nodes.push_back(BNode());
-    nodes[me].box = object_box(o);
+    nodes[me].box = swept(object_box(o));
     nodes[me].first = (int)leaf_prims.size();
     nodes[me].count = 1;
     int prim = od.kind == PT_OBJ_QUAD ? n_tris + od.index : n_tris + d->n_quads + od.index;
@@ -431,6 +443,26 @@ std::unique_ptr<Scene> build_scene(const pt_scene_desc *d, cudaStream_t st) {
       fail(PT_ERR_INVALID, "bad object entry");
   }
   const int n_prims = B.n_tris + d->n_quads + d->n_spheres;
+  // motion blur: one motion record per moving object, index + 1 on its
+  // primitives (a mesh shared by several objects takes the last one's)
+  std::vector<float4> motion;
+  std::vector<int> prim_motion(n_prims, 0);
+  for (int o = 0; o < d->n_objects; ++o) {
+    const pt_object_desc &od = d->objects[o];
+    const float *v = od.velocity;
+    if (!std::isfinite(v[0]) || !std::isfinite(v[1]) || !std::isfinite(v[2]))
+      fail(PT_ERR_INVALID, "object velocity must be finite");
+    if (v[0] == 0.f && v[1] == 0.f && v[2] == 0.f) continue;
+    motion.push_back(make_float4(v[0], v[1], v[2], 0.f));
+    const int m = (int)motion.size();
+    if (od.kind == PT_OBJ_MESH) {
+      for (int t = 0; t < d->meshes[od.index].n_triangles; ++t) prim_motion[B.tri_base[od.index] + t] = m;
+    } else {
+      prim_motion[od.kind == PT_OBJ_QUAD ? B.n_tris + od.index : B.n_tris + d->n_quads + od.index] = m;
+    }
+  }
+  if (!motion.empty() && !(d->shutter_max > 0.f) )
+    fail(PT_ERR_INVALID, "moving objects need shutter_max > 0");
   std::srand(1);  // the reference's BVH build draws from rand() with its default seed
   int root = B.build_top(0, d->n_objects);
 
@@ -455,6 +487,7 @@ std::unique_ptr<Scene> build_scene(const pt_scene_desc *d, cudaStream_t st) {
     Item &it = items[k];
     std::memset(&it, 0, sizeof it);
     it.a[3] = u2f((uint32_t)prim);
+    it.c[3] = u2f((uint32_t)prim_motion[prim]);
     prim_item[prim] = (int)k;
     if (prim < B.n_tris) {
       const pt_mesh_desc &m = d->meshes[prim_mesh[prim]];
@@ -491,6 +524,7 @@ std::unique_ptr<Scene> build_scene(const pt_scene_desc *d, cudaStream_t st) {
     std::memset(&ps, 0, sizeof ps);
     ps.item = prim_item[prim];
     ps.light = -1;
+    ps.flags = prim_motion[prim] << 8;
     if (prim < B.n_tris) {
       const pt_mesh_desc &m = d->meshes[prim_mesh[prim]];
       const int t = prim_tri[prim];
@@ -583,6 +617,7 @@ std::unique_ptr<Scene> build_scene(const pt_scene_desc *d, cudaStream_t st) {
       L.radius = s.radius;
       L.area = (float)(4 * PT_PI * s.radius * s.radius);
     }
+    L.motion = prim_motion[L.prim];
     shade[L.prim].light = (int)lights.size();
     lights.push_back(L);
   }
@@ -681,6 +716,11 @@ std::unique_ptr<Scene> build_scene(const pt_scene_desc *d, cudaStream_t st) {
     V.env.intensity = d->env->intensity;
     V.env.present = 1;
   }
+  if (!motion.empty()) {
+    V.motion = dupload(motion, S->owned, st);
+    V.has_motion = 1;
+    S->shutter_max = d->shutter_max;
+  }
   if (d->medium) {
     V.has_medium = 1;
     float tmax = 0.f;
@@ -773,6 +813,7 @@ void Context::ensure_queues(int cap, int ln) {
   Q.sh_o = (float4 *)alloc(c * 16);
   Q.sh_d = (float4 *)alloc(c * 16 * ln);
   Q.sh_c = (float4 *)alloc(c * 16 * ln);
+  Q.sh_vis = (uint8_t *)alloc(c * ln);
   Q.counts = (int *)alloc(64);
   Q.stats = (unsigned long long *)alloc(64);
   Q.sort_key = (int *)alloc(c * 4);
@@ -859,6 +900,8 @@ void validate_job(const pt_job_desc &j) {
       j.env_sampling > 1)
     fail(PT_ERR_INVALID, "bad enum in job");
   if (j.camera.aperture == 0.f) fail(PT_ERR_INVALID, "camera aperture must be non-zero");
+  if (!(j.camera.shutter >= 0.f) || !std::isfinite(j.camera.shutter))
+    fail(PT_ERR_INVALID, "camera shutter must be finite and >= 0");
 }
 
 DeviceJob Context::device_job(const pt_job_desc &j, Scene *S) {
@@ -878,8 +921,11 @@ DeviceJob Context::device_job(const pt_job_desc &j, Scene *S) {
   J.job.light_nx = j.light_samples_x;
   J.job.light_ny = j.light_samples_y;
   J.job.seed = j.seed;
+  J.job.shutter = j.camera.shutter;
   J.job.cam = make_camera(j.camera);
   J.perm = j.sampler == PT_SAMPLER_HALTON_PERMUTE ? perm_for(j.sampler_seed) : nullptr;
+  if (S->view.has_motion && j.camera.shutter > S->shutter_max)
+    fail(PT_ERR_INVALID, "camera shutter longer than the scene's shutter_max");
   return J;
 }
 

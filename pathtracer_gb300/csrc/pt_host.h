@@ -41,11 +41,39 @@ struct Scene {
   int n_tris = 0, n_quads = 0, n_spheres = 0, bvh_depth = 0;
   int env_w = 0, env_h = 0;
   unsigned family_mask = 0;  // BSDF families (material types 0..6) present
+  float shutter_max = 0.f;   // moving objects' boxes cover [0, shutter_max]
   size_t device_bytes = 0;
   ~Scene();
 };
 
 std::unique_ptr<Scene> build_scene(const pt_scene_desc *d, cudaStream_t st);
+
+// Per-job device buffers of a batch, reused across batched renders.
+struct BatchSlot {
+  Queues Q{};
+  std::vector<void *> mem;
+  int cap = 0, ln = 0;
+  float2 *offsets = nullptr;
+  int offsets_cap = 0;
+  float *film = nullptr;
+  size_t film_cap = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t done = nullptr;
+  void ensure(int want_cap, int want_ln, size_t film_floats, int spp);
+  void release();
+};
+
+// A batch: one graph branch per job, captured once per composition.
+struct Batch {
+  std::vector<BatchSlot> slots;
+  cudaGraphExec_t exec = nullptr;
+  cudaEvent_t fork = nullptr;
+  std::string sig;
+  int captures = 0;  // graph instantiations
+  int updates = 0;   // in-place parameter updates of the executable graph
+  int launches = 0;  // graph launches
+  ~Batch();
+};
 
 struct Context {
   int device = 0;
@@ -71,6 +99,8 @@ struct Context {
   size_t scratch_cap = 0;
   int *d_err = nullptr;
   Profiler prof;
+  Batch batch;
+  int batch_wave_cap = 1 << 22;  // paths per wave of each batched job
 
   explicit Context(int dev);
   ~Context();

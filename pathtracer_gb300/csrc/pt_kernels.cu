@@ -119,7 +119,13 @@ struct Surf {
   int light;
 };
 
-__device__ Surf surface_at(const SceneView &S, V3 o, V3 d, const HitRec &h) {
+// Position of a moving object's point at `time` (rounded, never fused).
+__device__ __forceinline__ V3 moved_point(const SceneView &S, int motion, V3 p, float time) {
+  const float4 v = __ldg(S.motion + (motion - 1));
+  return v3(xadd(p.x, xmul(v.x, time)), xadd(p.y, xmul(v.y, time)), xadd(p.z, xmul(v.z, time)));
+}
+
+__device__ Surf surface_at(const SceneView &S, V3 o, V3 d, const HitRec &h, float time) {
   Surf s;
   const float4 *pp = reinterpret_cast<const float4 *>(S.shade + h.prim);
   const float4 q0 = __ldg(pp), q1 = __ldg(pp + 1), q2 = __ldg(pp + 2), q3 = __ldg(pp + 3);
@@ -154,7 +160,9 @@ __device__ Surf surface_at(const SceneView &S, V3 o, V3 d, const HitRec &h) {
   } else {
     V3 dn = xnormalize(d);
     s.p = xat(o, dn, h.t);
-    n = normalize(s.p - v3(ps.n0[0], ps.n0[1], ps.n0[2]));
+    V3 c = v3(ps.n0[0], ps.n0[1], ps.n0[2]);
+    if (PT_PRIM_MOTION(ps.flags)) c = moved_point(S, PT_PRIM_MOTION(ps.flags), c, time);
+    n = normalize(s.p - c);
   }
   s.ng = n;
   s.front = dot(d, n) < 0.f;  // set_normal (materialBase.hpp:48-52)
@@ -280,8 +288,10 @@ __global__ void k_camera(DeviceJob J, Queues Q, long long g0, int n) {
              u * v3(C.horizontal[0], C.horizontal[1], C.horizontal[2]) +
              v * v3(C.vertical[0], C.vertical[1], C.vertical[2]) - ps;
     dir = normalize(dir);
+    // motion blur: the path's time, used by every ray of the path
+    const float time = J.job.shutter > 0.f ? J.job.shutter * rand01(P.key, 3u) : 0.f;
     Q.ray_o[0][s] = make_float4(ps.x, ps.y, ps.z, __int_as_float(s));
-    Q.ray_d[0][s] = make_float4(dir.x, dir.y, dir.z, 0.f);
+    Q.ray_d[0][s] = make_float4(dir.x, dir.y, dir.z, time);
     Q.beta[s] = make_float4(1.f, 1.f, 1.f, -1.f);  // w < 0: previous vertex delta / camera
     Q.L[s] = make_float4(0.f, 0.f, 0.f, 0.f);
   }
@@ -291,34 +301,75 @@ __global__ void k_camera(DeviceJob J, Queues Q, long long g0, int n) {
   }
 }
 
-// k_trace_closest: one ray per thread.  In a participating medium the
-// free-flight distance of the segment is drawn here (dimension dpb*bounce)
-// and used as tmax: a segment that reaches it without a surface hit is a
-// medium event (prim = PT_HIT_MEDIUM, t = free-flight distance).  That is
-// the same decision as comparing the distance with the closest hit.
+// Persistent traversal warps with dynamic ray fetch (Aila and Laine,
+// "Understanding the efficiency of ray traversal on GPUs", HPG 2009, and the
+// 2012 addendum): each lane walks its ray one step at a time, and as soon as
+// PT_FETCH_IDLE lanes of a warp have finished, the warp claims that many new
+// rays from the queue with one atomic.  Incoherent rays of very different
+// lengths then no longer hold a warp until its longest ray ends.
+#define PT_FETCH_IDLE 16
+
+__device__ __forceinline__ unsigned lanemask_lt() {
+  return (1u << (threadIdx.x & 31)) - 1u;
+}
+
+// k_trace_closest: the RayQueue through the BVH.  In a participating medium
+// the free-flight distance of the segment is drawn when the ray is fetched
+// (dimension dpb*bounce) and used as tmax: a segment that reaches it without
+// a surface hit is a medium event (prim = PT_HIT_MEDIUM, t = free-flight
+// distance).  That is the same decision as comparing the distance with the
+// closest hit.
 __global__ void __launch_bounds__(128) k_trace_closest(SceneView S, DeviceJob J, Queues Q, int qsel, int bounce,
                                                        long long g0) {
   __shared__ int32_t stack[PT_STACK * 128];
   const int n = Q.counts[qsel];
+  int *fetch = Q.counts + 4;
   const bool ff = S.has_medium && bounce < J.job.max_depth;
-  int rays = 0;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    float4 ro = ld4(Q.ray_o[qsel] + i), rd = ld4(Q.ray_d[qsel] + i);
-    float tmax = 1e5f;
-    float t_s = INFINITY;
-    if (ff) {
-      PathId P = path_id(J, g0 + __float_as_int(ro.w));
-      float uf = sampler_dim(J, 4 * bounce, P.halton_index, P.key, P.q, P.k);
-      t_s = -logf(1.f - uf) / S.sigma_t_max;
-      tmax = fminf(tmax, t_s);
+  const int lane = threadIdx.x & 31;
+  int32_t *my_stack = stack + threadIdx.x;
+  TravRay R;
+  bool active = false, exhausted = false;
+  int ray = 0, rays = 0;
+  float t_s = INFINITY;
+  for (;;) {
+    unsigned idle = __ballot_sync(0xffffffffu, !active);
+    if (!exhausted && __popc(idle) >= PT_FETCH_IDLE) {
+      const int k = __popc(idle);
+      int base = 0;
+      if (lane == 0) base = atomicAdd(fetch, k);
+      base = __shfl_sync(0xffffffffu, base, 0);
+      if (base + k >= n) exhausted = true;
+      if (!active) {
+        const int r = base + __popc(idle & lanemask_lt());
+        if (r < n) {
+          float4 ro = ld4(Q.ray_o[qsel] + r), rd = ld4(Q.ray_d[qsel] + r);
+          float tmax = 1e5f;
+          t_s = INFINITY;
+          if (ff) {
+            PathId P = path_id(J, g0 + __float_as_int(ro.w));
+            float uf = sampler_dim(J, 4 * bounce, P.halton_index, P.key, P.q, P.k);
+            t_s = -logf(1.f - uf) / S.sigma_t_max;
+            tmax = fminf(tmax, t_s);
+          }
+          trav_init(R, v3(ro.x, ro.y, ro.z), v3(rd.x, rd.y, rd.z), 1e-4f, tmax, rd.w);
+          ray = r;
+          active = true;
+          ++rays;
+        }
+      }
+      idle = __ballot_sync(0xffffffffu, !active);
     }
-    HitRec h;
-    bool hit = traverse<false>(S, v3(ro.x, ro.y, ro.z), v3(rd.x, rd.y, rd.z), 1e-4f, tmax, h,
-                               stack + threadIdx.x, blockDim.x, Q.err);
-    int prim = hit ? h.prim : (t_s < 1e5f ? PT_HIT_MEDIUM : -1);
-    float t = hit ? h.t : (prim == PT_HIT_MEDIUM ? t_s : FLT_MAX);
-    Q.hit[i] = make_float4(t, __int_as_float(prim), h.u, h.v);
-    ++rays;
+    if (idle == 0xffffffffu) {
+      if (exhausted) break;
+      continue;
+    }
+    if (active && trav_step<false>(S, R, my_stack, blockDim.x, Q.err)) {
+      const bool hit = R.found;
+      int prim = hit ? R.hit.prim : (t_s < 1e5f ? PT_HIT_MEDIUM : -1);
+      float t = hit ? R.hit.t : (prim == PT_HIT_MEDIUM ? t_s : FLT_MAX);
+      Q.hit[ray] = make_float4(t, __int_as_float(prim), R.hit.u, R.hit.v);
+      active = false;
+    }
   }
   warp_count(&Q.stats[2], rays);
 }
@@ -411,7 +462,7 @@ __device__ __forceinline__ float power_heuristic(float nf, float fpdf, float ng,
 template <int FAM, bool MED>
 __device__ __forceinline__ void next_event(const SceneView &S, const DeviceJob &J, const Queues &Q, int sslot,
                                            int path, uint64_t key, uint32_t rbase, const Surf &sf, int mat,
-                                           V3 wo, V3 beta, int LN, bool mis) {
+                                           V3 wo, V3 beta, int LN, bool mis, float time) {
   const float phase = (float)(1.0 / (4.0 * PT_PI));
   Q.sh_o[sslot] = make_float4(sf.p.x, sf.p.y, sf.p.z, __int_as_float(path));
   const float inv_ln = 1.f / (float)LN;
@@ -453,6 +504,7 @@ __device__ __forceinline__ void next_event(const SceneView &S, const DeviceJob &
         // QuadLight::get_sample / get_normal_at (light.hpp:131-147)
         lp = v3(Lr.v0[0], Lr.v0[1], Lr.v0[2]) + ox * v3(Lr.e1[0], Lr.e1[1], Lr.e1[2]) +
              oy * v3(Lr.e2[0], Lr.e2[1], Lr.e2[2]);
+        if (Lr.motion) lp = moved_point(S, Lr.motion, lp, time);
         ln = v3(Lr.normal[0], Lr.normal[1], Lr.normal[2]);
       } else {
         // SphereLight::get_sample (light.hpp:254-264): the whole sphere
@@ -461,6 +513,7 @@ __device__ __forceinline__ void next_event(const SceneView &S, const DeviceJob &
         float phi = acosf(2.f * oy - 1.f);
         sincos_(phi, &sph, &cph);
         V3 c = v3(Lr.v0[0], Lr.v0[1], Lr.v0[2]);
+        if (Lr.motion) c = moved_point(S, Lr.motion, c, time);
         lp = c + Lr.radius * v3(sph * cth, sph * sth, cph);
         ln = normalize(lp - c);
       }
@@ -495,7 +548,7 @@ __device__ __forceinline__ void next_event(const SceneView &S, const DeviceJob &
       V3 c = beta * (f * Le * (G / pdf_l * w * inv_ln)) * tr;
       if (c.x != 0.f || c.y != 0.f || c.z != 0.f) {
         shd = make_float4(wl.x, wl.y, wl.z, tmax);
-        shc = make_float4(c.x, c.y, c.z, 0.f);
+        shc = make_float4(c.x, c.y, c.z, time);
       }
     }
     Q.sh_d[(size_t)ls * Q.cap + sslot] = shd;
@@ -552,11 +605,13 @@ __global__ void __launch_bounds__(128) k_shade(SceneView S, DeviceJob J, Queues 
     V3 wo = v3(0.f), beta = v3(0.f), wi = v3(0.f), nb = v3(0.f);
     float npdf = -1.f;
     uint64_t key = 0;
+    float time = 0.f;
     if (ii < n) {
       const int i = (FAM >= 0) ? Q.order[lo + ii] : ii;
       float4 ro = ld4(Q.ray_o[qsel] + i), rd = ld4(Q.ray_d[qsel] + i);
       float4 hh = ld4(Q.hit + i);
       path = __float_as_int(ro.w);
+      time = rd.w;
       V3 o = v3(ro.x, ro.y, ro.z), d = v3(rd.x, rd.y, rd.z);
       float4 b4 = Q.beta[path];
       beta = v3(b4.x, b4.y, b4.z);
@@ -604,7 +659,7 @@ __global__ void __launch_bounds__(128) k_shade(SceneView S, DeviceJob J, Queues 
         h.prim = prim;
         h.u = hh.z;
         h.v = hh.w;
-        sf = surface_at(S, o, d, h);
+        sf = surface_at(S, o, d, h, time);
         mat = sf.mat;
         const MatRec &M = S.materials[mat];
         if (DO_MISC && mat_is_emitter(M)) {
@@ -615,8 +670,9 @@ __global__ void __launch_bounds__(128) k_shade(SceneView S, DeviceJob J, Queues 
             if (sf.light >= 0) {
               const LightRec &Lr = S.lights[sf.light];
               // one-sided emission of the light, as NEE evaluates it
-              V3 ln = (Lr.type == LIGHT_QUAD) ? v3(Lr.normal[0], Lr.normal[1], Lr.normal[2])
-                                              : normalize(sf.p - v3(Lr.v0[0], Lr.v0[1], Lr.v0[2]));
+              V3 lc = v3(Lr.v0[0], Lr.v0[1], Lr.v0[2]);
+              if (Lr.motion) lc = moved_point(S, Lr.motion, lc, time);
+              V3 ln = (Lr.type == LIGHT_QUAD) ? v3(Lr.normal[0], Lr.normal[1], Lr.normal[2]) : normalize(sf.p - lc);
               float cl = dot(ln, -normalize(d));
               if (cl > 0.f) {
                 V3 Le = v3(Lr.color[0], Lr.color[1], Lr.color[2]) * Lr.intensity;
@@ -678,89 +734,91 @@ __global__ void __launch_bounds__(128) k_shade(SceneView S, DeviceJob J, Queues 
     const int slot = warp_alloc(&Q.counts[nq], push);
     if (push) {
       Q.ray_o[nq][slot] = make_float4(sf.p.x, sf.p.y, sf.p.z, __int_as_float(path));
-      Q.ray_d[nq][slot] = make_float4(wi.x, wi.y, wi.z, 0.f);
+      Q.ray_d[nq][slot] = make_float4(wi.x, wi.y, wi.z, time);
     }
     // ---------------- phase C: next-event estimation
     if (do_nee) {
       if (DO_MISC && nee_medium)
-        next_event<FAM, true>(S, J, Q, sslot, path, key, rbase, sf, mat, wo, beta, LN, mis);
+        next_event<FAM, true>(S, J, Q, sslot, path, key, rbase, sf, mat, wo, beta, LN, mis, time);
       else if (DO_SURF)
-        next_event<FAM, false>(S, J, Q, sslot, path, key, rbase, sf, mat, wo, beta, LN, mis);
+        next_event<FAM, false>(S, J, Q, sslot, path, key, rbase, sf, mat, wo, beta, LN, mis, time);
     }
   }
   warp_count(&Q.stats[1], segs);
 }
 
-// k_trace_shadow: one shadow ray per thread.  The LN rays of a vertex sit in
-// LN consecutive lanes (LN a power of two <= 32); their visible terms are
-// reduced with shuffles in a fixed order and the group's first lane adds the
-// sum to the path's L, so the result is deterministic.
-__global__ void __launch_bounds__(128) k_trace_shadow(SceneView S, Queues Q, int LN, int lg) {
+// k_trace_shadow: the ShadowQueue's rays (vertex v, light sample ls; ray
+// r = v * LN + ls) through the BVH, any-hit, with the persistent warps of
+// k_trace_closest.  Each ray's visibility goes to Q.sh_vis; k_shadow_resolve
+// then adds the visible terms of every vertex to its path in a fixed order,
+// so the result does not depend on which warp traced which ray.
+__global__ void __launch_bounds__(128) k_trace_shadow(SceneView S, Queues Q, int LN) {
   __shared__ int32_t stack[PT_STACK * 128];
-  const int nv = Q.counts[2];
-  const long long n = (long long)nv << lg;
-  int rays = 0;
-  const long long stride = (long long)gridDim.x * blockDim.x;
-  const long long nround = (n + stride - 1) / stride * stride;
+  const int n = Q.counts[2] * LN;
+  int *fetch = Q.counts + 3;
   const int lane = threadIdx.x & 31;
-  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < nround; t += stride) {
-    V3 acc = v3(0.f);
-    int v = (int)(t >> lg), ls = (int)(t & (LN - 1));
-    if (t < n) {
-      float4 dd = ld4(Q.sh_d + (size_t)ls * Q.cap + v);
-      if (dd.w >= 0.f) {
-        float4 so = ld4(Q.sh_o + v);
-        HitRec h;
-        ++rays;
-        bool occ = traverse<true>(S, v3(so.x, so.y, so.z), v3(dd.x, dd.y, dd.z), 0.001f, dd.w, h,
-                                  stack + threadIdx.x, blockDim.x, Q.err);
-        if (!occ) {
-          float4 cc = ld4(Q.sh_c + (size_t)ls * Q.cap + v);
-          acc = v3(cc.x, cc.y, cc.z);
+  int32_t *my_stack = stack + threadIdx.x;
+  TravRay R;
+  bool active = false, exhausted = false;
+  size_t slot = 0;
+  int rays = 0;
+  for (;;) {
+    unsigned idle = __ballot_sync(0xffffffffu, !active);
+    if (!exhausted && __popc(idle) >= PT_FETCH_IDLE) {
+      const int k = __popc(idle);
+      int base = 0;
+      if (lane == 0) base = atomicAdd(fetch, k);
+      base = __shfl_sync(0xffffffffu, base, 0);
+      if (base + k >= n) exhausted = true;
+      if (!active) {
+        const int r = base + __popc(idle & lanemask_lt());
+        if (r < n) {
+          const int v = r / LN, ls = r - v * LN;
+          slot = (size_t)ls * Q.cap + v;
+          float4 dd = ld4(Q.sh_d + slot);
+          if (dd.w >= 0.f) {
+            float4 so = ld4(Q.sh_o + v);
+            const float time = S.has_motion ? ld4(Q.sh_c + slot).w : 0.f;
+            trav_init(R, v3(so.x, so.y, so.z), v3(dd.x, dd.y, dd.z), 0.001f, dd.w, time);
+            active = true;
+            ++rays;
+          }
         }
       }
+      idle = __ballot_sync(0xffffffffu, !active);
     }
-    // fixed-order tree reduction inside each group of LN lanes
-    for (int off = 1; off < LN; off <<= 1) {
-      float ox = __shfl_down_sync(0xffffffffu, acc.x, off);
-      float oy = __shfl_down_sync(0xffffffffu, acc.y, off);
-      float oz = __shfl_down_sync(0xffffffffu, acc.z, off);
-      if ((lane & (2 * off - 1)) == 0) acc = acc + v3(ox, oy, oz);
+    if (idle == 0xffffffffu) {
+      if (exhausted) break;
+      continue;
     }
-    if (t < n && ls == 0 && (acc.x != 0.f || acc.y != 0.f || acc.z != 0.f)) {
-      int path = __float_as_int(ld4(Q.sh_o + v).w);
-      float4 L = Q.L[path];
-      Q.L[path] = make_float4(L.x + acc.x, L.y + acc.y, L.z + acc.z, 0.f);
+    if (active && trav_step<true>(S, R, my_stack, blockDim.x, Q.err)) {
+      Q.sh_vis[slot] = R.found ? 0 : 1;
+      active = false;
     }
   }
   warp_count(&Q.stats[3], rays);
 }
 
-// k_trace_shadow_serial: the same for light-sample counts that are not a
-// power of two: one vertex per thread, its rays in order.
-__global__ void __launch_bounds__(128) k_trace_shadow_serial(SceneView S, Queues Q, int LN) {
-  __shared__ int32_t stack[PT_STACK * 128];
+// k_shadow_resolve: per vertex, the visible NEE terms in light-sample order
+// added to the path's L.  Rays that were never traced (no contribution) have
+// a zero term, whatever their stale visibility byte says.
+__global__ void k_shadow_resolve(Queues Q, int LN) {
   const int n = Q.counts[2];
-  int rays = 0;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    float4 so = ld4(Q.sh_o + i);
-    V3 o = v3(so.x, so.y, so.z);
-    int path = __float_as_int(so.w);
+  for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
     V3 acc = v3(0.f);
     for (int ls = 0; ls < LN; ++ls) {
-      float4 dd = ld4(Q.sh_d + (size_t)ls * Q.cap + i);
-      if (dd.w < 0.f) continue;
-      float4 cc = ld4(Q.sh_c + (size_t)ls * Q.cap + i);
-      HitRec h;
-      ++rays;
-      bool occ = traverse<true>(S, o, v3(dd.x, dd.y, dd.z), 0.001f, dd.w, h, stack + threadIdx.x, blockDim.x,
-                                Q.err);
-      if (!occ) acc += v3(cc.x, cc.y, cc.z);
+      const size_t slot = (size_t)ls * Q.cap + v;
+      if (Q.sh_vis[slot]) {
+        float4 cc = ld4(Q.sh_c + slot);
+        acc += v3(cc.x, cc.y, cc.z);
+      }
     }
-    float4 L = Q.L[path];
-    Q.L[path] = make_float4(L.x + acc.x, L.y + acc.y, L.z + acc.z, 0.f);
+    if (acc.x != 0.f || acc.y != 0.f || acc.z != 0.f) {
+      const int path = __float_as_int(ld4(Q.sh_o + v).w);
+      float4 L = Q.L[path];
+      Q.L[path] = make_float4(L.x + acc.x, L.y + acc.y, L.z + acc.z, 0.f);
+    }
   }
-  warp_count(&Q.stats[3], rays);
 }
 
 // k_film: per pixel, adds the wave's paths in sample order (deterministic).
@@ -854,8 +912,9 @@ void launch_wave(const SceneView &S, const DeviceJob &J, const Queues &Q, long l
   int qsel = 0;
   for (int b = 0; b < bounces; ++b) {
     // reset next-queue and shadow counters (device side, graph friendly)
+    // ([2] shadow queue, [3] shadow fetch, [4] closest-hit fetch)
     cudaMemsetAsync(Q.counts + (qsel ^ 1), 0, sizeof(int), st);
-    cudaMemsetAsync(Q.counts + 2, 0, sizeof(int), st);
+    cudaMemsetAsync(Q.counts + 2, 0, 3 * sizeof(int), st);
     P.begin(STAGE_TRACE, st);
     k_trace_closest<<<cfg.trace_blocks, 128, 0, st>>>(S, J, Q, qsel, b, g0);
     P.end(st);
@@ -882,13 +941,8 @@ void launch_wave(const SceneView &S, const DeviceJob &J, const Queues &Q, long l
       P.end(st);
     }
     P.begin(STAGE_SHADOW, st);
-    if ((LN & (LN - 1)) == 0 && LN <= 32) {
-      int lg = 0;
-      while ((1 << lg) < LN) ++lg;
-      k_trace_shadow<<<cfg.trace_blocks, 128, 0, st>>>(S, Q, LN, lg);
-    } else {
-      k_trace_shadow_serial<<<cfg.trace_blocks, 128, 0, st>>>(S, Q, LN);
-    }
+    k_trace_shadow<<<cfg.trace_blocks, 128, 0, st>>>(S, Q, LN);
+    k_shadow_resolve<<<cfg.max_blocks_simple, 256, 0, st>>>(Q, LN);
     P.end(st);
     qsel ^= 1;
   }

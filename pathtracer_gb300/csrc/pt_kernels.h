@@ -35,7 +35,8 @@ struct Queues {
   float4 *sh_o;       // ShadowQueue: origin.xyz, path slot
   float4 *sh_d;       // [light sample][cap]: direction.xyz, tmax (<0: none)
   float4 *sh_c;       // [light sample][cap]: unoccluded contribution
-  int *counts;        // [0],[1] ray queues, [2] shadow queue
+  uint8_t *sh_vis;    // [light sample][cap]: 1 = the shadow ray reached the light
+  int *counts;        // [0],[1] ray queues, [2] shadow queue, [3] [4] fetch counters
   unsigned long long *stats;  // [0] paths [1] segments [2] rays [3] shadow rays
   int *err;           // device error flag (stack overflow / iteration cap)
   int *sort_key, *order, *bins;

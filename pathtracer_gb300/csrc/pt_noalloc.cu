@@ -80,8 +80,8 @@ void render_device_noalloc(Context *c, const pt_job_desc &j, float *d_film, pt_s
   uint16_t *d_perm = (uint16_t *)carve(perm.size() * sizeof(uint16_t) + 16);
   const int LN = j.light_samples_x * j.light_samples_y;
   off = align_up(off, 256);
-  const size_t per_path = 16 * 8 + 2 * 16 * (size_t)LN + 2 * 4;
-  const size_t avail = PT_NOALLOC_SCRATCH_BYTES - off - 16 * 256;  // alignment slack of 16 arrays
+  const size_t per_path = 16 * 8 + 2 * 16 * (size_t)LN + (size_t)LN + 2 * 4;
+  const size_t avail = PT_NOALLOC_SCRATCH_BYTES - off - 17 * 256;  // alignment slack of 17 arrays
   const int cap = (int)std::min<size_t>(avail / per_path, (size_t)1 << 30);
   if (cap < 1024) fail(PT_ERR_TOO_LARGE, "pt_render_device_noalloc: scratch too small for the light samples");
   const size_t c4 = (size_t)cap * 16;
@@ -96,6 +96,7 @@ void render_device_noalloc(Context *c, const pt_job_desc &j, float *d_film, pt_s
   Q.sh_o = (float4 *)carve(c4);
   Q.sh_d = (float4 *)carve(c4 * LN);
   Q.sh_c = (float4 *)carve(c4 * LN);
+  Q.sh_vis = (uint8_t *)carve((size_t)cap * LN);
   Q.sort_key = (int *)carve((size_t)cap * 4);
   Q.order = (int *)carve((size_t)cap * 4);
   if (off > PT_NOALLOC_SCRATCH_BYTES) fail(PT_ERR_TOO_LARGE, "pt_render_device_noalloc: scratch layout overflow");
@@ -117,6 +118,9 @@ void render_device_noalloc(Context *c, const pt_job_desc &j, float *d_film, pt_s
   J.job.light_nx = j.light_samples_x;
   J.job.light_ny = j.light_samples_y;
   J.job.seed = j.seed;
+  J.job.shutter = j.camera.shutter;
+  if (S->view.has_motion && j.camera.shutter > S->shutter_max)
+    fail(PT_ERR_INVALID, "camera shutter longer than the scene's shutter_max");
   J.job.cam = make_camera(j.camera);
   std::vector<float2> offs = make_offsets(j);
   cuda_check(cudaMemcpyAsync(d_off, offs.data(), offs.size() * sizeof(float2), cudaMemcpyHostToDevice, c->stream),

@@ -58,6 +58,7 @@ static_assert(sizeof(PrimShade) == 64, "PrimShade must be 64 bytes");
 #define PT_PRIM_FLIP 2
 #define PT_PRIM_KIND(f) (((f) >> 2) & 3)
 #define PT_PRIM_AXIS(f) (((f) >> 4) & 3)
+#define PT_PRIM_MOTION(f) ((f) >> 8)  // motion index + 1 (0: static)
 
 // Material record: the C-ABI description plus constants derived once on the
 // host (Disney lobe weights, hair v[p], s, sin/cos 2^k alpha ...).
@@ -77,7 +78,7 @@ struct alignas(16) LightRec {
   float v0[3];      // quad: vertices[0]; sphere: centre
   float radius;
   float e1[3];      // quad: vertices[1] - vertices[0]
-  float pad0;
+  int32_t motion;   // motion index + 1 (0: static)
   float e2[3];      // quad: vertices[3] - vertices[0]
   float pad1;
   float normal[3];  // quad: normalize(cross(e1, e2))
@@ -109,6 +110,10 @@ struct SceneView {
   float bg[3];
   int32_t has_medium;
   float sigma_a[3], sigma_s[3], sigma_t_max, medium_g;
+  // motion blur (extension): velocity per moving object; items, shading
+  // records and lights of a moving object carry its index + 1
+  const float4 *motion;
+  int32_t has_motion;
 };
 
 // Camera constants of PerspectiveCamera (camera.cpp:7-35).
@@ -134,6 +139,7 @@ struct JobView {
   int32_t env_sampling;
   int32_t light_nx, light_ny;
   uint32_t seed;
+  float shutter;          // motion blur: a path's time is shutter * u
   CameraView cam;
   const float2 *offsets;  // per grid sample k: jittered pixel offset
 };

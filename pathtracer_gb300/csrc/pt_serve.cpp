@@ -20,14 +20,9 @@
 
 #include <cuda_runtime.h>
 
-#include "pt_host.h"
+#include "pt_batch.h"
 
 namespace pt {
-
-struct PtErrorS : std::runtime_error {
-  int code;
-  PtErrorS(int c, const std::string &m) : std::runtime_error(m), code(c) {}
-};
 
 struct Request {
   int64_t id;
@@ -93,22 +88,32 @@ static int serr(void *ctx, int code, const std::string &m) {
 extern "C" {
 
 int pt_render_batch(void *ctx, const pt_job_desc *jobs, int32_t n_jobs, float **films, pt_stats *stats) {
-  if (!ctx || !jobs || n_jobs < 0 || (n_jobs > 0 && !films)) return serr(ctx, PT_ERR_INVALID, "bad batch args");
-  pt_stats total;
-  std::memset(&total, 0, sizeof total);
-  for (int k = 0; k < n_jobs; ++k) {
-    pt_stats st;
-    int rc = pt_render(ctx, &jobs[k], films[k], &st);
-    if (rc != PT_OK) return rc;
-    total.paths += st.paths;
-    total.segments += st.segments;
-    total.rays += st.rays;
-    total.shadow_rays += st.shadow_rays;
-    total.ms += st.ms;
-    total.algorithmic_bytes += st.algorithmic_bytes;
+  if (!ctx || !jobs || n_jobs < 0) return serr(ctx, PT_ERR_INVALID, "bad batch args");
+  if (n_jobs == 0) return PT_OK;
+  Context *c = static_cast<Context *>(ctx);
+  try {
+    cuda_check(cudaSetDevice(c->device), "cudaSetDevice");
+    render_batch(c, jobs, n_jobs, films, stats);
+    return PT_OK;
+  } catch (const PtError &e) {
+    return serr(ctx, e.code, e.what());
+  } catch (const std::exception &e) {
+    return serr(ctx, PT_ERR_INVALID, e.what());
   }
-  if (stats) *stats = total;
-  return PT_OK;
+}
+
+int pt_autotune(void *ctx, const pt_job_desc *jobs, int32_t n_jobs, pt_tuning *out) {
+  if (!ctx || !jobs || n_jobs <= 0) return serr(ctx, PT_ERR_INVALID, "bad autotune args");
+  Context *c = static_cast<Context *>(ctx);
+  try {
+    cuda_check(cudaSetDevice(c->device), "cudaSetDevice");
+    autotune(c, jobs, n_jobs, out);
+    return PT_OK;
+  } catch (const PtError &e) {
+    return serr(ctx, e.code, e.what());
+  } catch (const std::exception &e) {
+    return serr(ctx, PT_ERR_INVALID, e.what());
+  }
 }
 
 int pt_server_create(void *ctx, int64_t hbm_budget_bytes, int32_t max_slots, void **server) {
@@ -178,9 +183,14 @@ int pt_server_step(void *server, int32_t *active_out) {
     s->active.push_back(r.id);
     s->queue.pop_front();
   }
-  // one pass over every active request
+  // one pass over every active request: a batch with one job per request
+  // (its next spp_per_pass samples), rendered as one graph launch
   std::vector<float> ha, hb;
-  std::vector<int64_t> still;
+  std::vector<int64_t> still, live;
+  std::vector<pt_job_desc> jobs;
+  std::vector<float *> targets;
+  std::vector<int> ends;
+  std::vector<bool> to_a_v;
   for (int64_t id : s->active) {
     Request &r = s->reqs[id];
     if (r.state != 1) {
@@ -194,14 +204,33 @@ int pt_server_step(void *server, int32_t *active_out) {
     j.spp_begin = b;
     j.spp_end = e;
     const bool to_a = ((b / std::max(1, r.desc.spp_per_pass)) % 2) == 0;
-    int rc = pt_render_device(c, &j, to_a ? r.film_a : r.film_b, 0, nullptr);
-    if (rc != PT_OK) {
-      r.state = 4;
-      r.error = c->last_error;
-      release_films(r, *s);
-      continue;
+    jobs.push_back(j);
+    targets.push_back(to_a ? r.film_a : r.film_b);
+    ends.push_back(e);
+    to_a_v.push_back(to_a);
+    live.push_back(id);
+  }
+  if (!jobs.empty()) {
+    try {
+      render_batch(c, jobs.data(), (int)jobs.size(), nullptr, nullptr, targets.data());
+    } catch (const std::exception &ex) {
+      for (int64_t id : live) {
+        Request &r = s->reqs[id];
+        r.state = 4;
+        r.error = ex.what();
+        release_films(r, *s);
+      }
+      live.clear();
     }
-    (to_a ? r.spp_a : r.spp_b) += e - b;
+  }
+  for (size_t q = 0; q < live.size(); ++q) {
+    const int64_t id = live[q];
+    Request &r = s->reqs[id];
+    const pt_job_desc &j = jobs[q];
+    const int spp_total = j.spp_x * j.spp_y;
+    const int cap = std::min(r.desc.spp_cap, spp_total);
+    const int e = ends[q];
+    (to_a_v[q] ? r.spp_a : r.spp_b) += e - j.spp_begin;
     r.spp_done = e;
     bool done = r.spp_done >= cap;
     if (!done && r.desc.target_rmse > 0.f && r.spp_a > 0 && r.spp_b > 0) {

@@ -107,15 +107,24 @@ __device__ __forceinline__ Item load_item(const Item *items, int i) {
 }
 
 // Tests one leaf; for ANY returns true on the first hit in [tmin, tmax].
+// Origin of a ray of time `time` in the frame of a primitive moving with
+// velocity v: o - v * time (rounded, never fused).
+__device__ __forceinline__ V3 moved_origin(const SceneView &S, uint32_t motion, V3 o, float time) {
+  const float4 v = __ldg(S.motion + (motion - 1u));
+  return v3(xsub(o.x, xmul(v.x, time)), xsub(o.y, xmul(v.y, time)), xsub(o.z, xmul(v.z, time)));
+}
+
 template <bool ANY>
-__device__ __forceinline__ bool test_leaf(const SceneView &S, int32_t ref, V3 o, V3 d, V3 dn,
-                                          float tmin, float &tmax, HitRec &hit) {
+__device__ __forceinline__ bool test_leaf(const SceneView &S, int32_t ref, V3 o_w, V3 d, V3 dn,
+                                          float tmin, float &tmax, HitRec &hit, float time) {
   const int32_t code = ~ref;
   const int first = code >> 3, count = (code & 7) + 1;
   bool any = false;
   for (int k = 0; k < count; ++k) {
     Item it = load_item(S.items, first + k);
     const int type = (int)f2u(it.b[3]);
+    const uint32_t motion = f2u(it.c[3]);
+    const V3 o = motion ? moved_origin(S, motion, o_w, time) : o_w;
     float t, u = 0.f, v = 0.f;
     bool h;
     if (type == ITEM_TRI)
@@ -137,38 +146,66 @@ __device__ __forceinline__ bool test_leaf(const SceneView &S, int32_t ref, V3 o,
   return any;
 }
 
-// Generic traversal.  `stack` points at this thread's column of a shared
-// array laid out [PT_STACK][blockDim.x].  Returns: closest -> whether
-// anything was hit (hit filled); any -> occluded.  *err is set when the
-// stack would overflow or the iteration cap is reached (never expected).
+// Traversal state of one ray.  The walk is a sequence of steps (one node
+// visit or one leaf test each) so that a persistent warp can refill lanes
+// whose rays have finished while the others continue (trav_step).
+struct TravRay {
+  V3 o, d, dn, inv, oi;
+  float tmin, tmax;
+  int32_t ref;  // node index (>= 0) or leaf reference (< 0) visited next
+  int sp;       // stack depth
+  int iters;
+  float time;   // motion blur: the ray's time
+  bool found;
+  HitRec hit;
+};
+
+__device__ __forceinline__ void trav_init(TravRay &R, V3 o, V3 d, float tmin, float tmax, float time = 0.f) {
+  R.time = time;
+  R.o = o;
+  R.d = d;
+  R.dn = xnormalize(d);
+  R.inv = v3(1.f / d.x, 1.f / d.y, 1.f / d.z);
+  R.oi = v3(-o.x * R.inv.x, -o.y * R.inv.y, -o.z * R.inv.z);
+  R.tmin = tmin;
+  R.tmax = tmax;
+  R.ref = 0;  // node 0 is the root (the host always emits at least one node)
+  R.sp = 0;
+  R.iters = 0;
+  R.found = false;
+  R.hit.t = FLT_MAX;
+  R.hit.prim = -1;
+  R.hit.u = R.hit.v = 0.f;
+}
+
+// One traversal step.  `stack` points at this thread's column of a shared
+// array laid out [PT_STACK][stride].  Returns true when the ray is finished:
+// closest -> R.found / R.hit hold the nearest hit; any -> R.found = occluded.
+// *err is set when the stack would overflow or the iteration cap is reached
+// (never expected); the ray is then finished with what it has.
 template <bool ANY>
-__device__ bool traverse(const SceneView &S, V3 o, V3 d, float tmin, float tmax, HitRec &hit,
-                         int32_t *stack, int stride, int *err) {
-  hit.t = FLT_MAX;
-  hit.prim = -1;
-  hit.u = hit.v = 0.f;
-  const V3 dn = xnormalize(d);
-  const V3 inv = v3(1.f / d.x, 1.f / d.y, 1.f / d.z);
-  const V3 oi = v3(-o.x * inv.x, -o.y * inv.y, -o.z * inv.z);
-  bool found = false;
-  int sp = 0;
-  int32_t ref = 0;  // node 0 is the root (the host always emits at least one node)
-  for (int iter = 0; iter < PT_TRAVERSAL_CAP; ++iter) {
-    if (ref >= 0) {
-      const float4 *np = reinterpret_cast<const float4 *>(S.nodes + ref);
-      float4 lx = __ldg(np + 0), hx = __ldg(np + 1), ly = __ldg(np + 2), hy = __ldg(np + 3);
-      float4 lz = __ldg(np + 4), hz = __ldg(np + 5);
-      int4 ch = __ldg(reinterpret_cast<const int4 *>(np + 6));
-      int4 cn = __ldg(reinterpret_cast<const int4 *>(np + 7));
-      const float lxa[4] = {lx.x, lx.y, lx.z, lx.w}, hxa[4] = {hx.x, hx.y, hx.z, hx.w};
-      const float lya[4] = {ly.x, ly.y, ly.z, ly.w}, hya[4] = {hy.x, hy.y, hy.z, hy.w};
-      const float lza[4] = {lz.x, lz.y, lz.z, lz.w}, hza[4] = {hz.x, hz.y, hz.z, hz.w};
-      const int cha[4] = {ch.x, ch.y, ch.z, ch.w}, cna[4] = {cn.x, cn.y, cn.z, cn.w};
-      // entry distance per child (+inf when missed or empty), kept in
-      // registers; closest-hit visits near to far (sorting network),
-      // any-hit in node order.
-      float d0, d1, d2, d3;
-      int32_t r0, r1, r2, r3;
+__device__ __forceinline__ bool trav_step(const SceneView &S, TravRay &R, int32_t *stack, int stride, int *err) {
+  if (++R.iters > PT_TRAVERSAL_CAP) {
+    *err = 2;
+    return true;
+  }
+  if (R.ref >= 0) {
+    const float4 *np = reinterpret_cast<const float4 *>(S.nodes + R.ref);
+    float4 lx = __ldg(np + 0), hx = __ldg(np + 1), ly = __ldg(np + 2), hy = __ldg(np + 3);
+    float4 lz = __ldg(np + 4), hz = __ldg(np + 5);
+    int4 ch = __ldg(reinterpret_cast<const int4 *>(np + 6));
+    int4 cn = __ldg(reinterpret_cast<const int4 *>(np + 7));
+    const float lxa[4] = {lx.x, lx.y, lx.z, lx.w}, hxa[4] = {hx.x, hx.y, hx.z, hx.w};
+    const float lya[4] = {ly.x, ly.y, ly.z, ly.w}, hya[4] = {hy.x, hy.y, hy.z, hy.w};
+    const float lza[4] = {lz.x, lz.y, lz.z, lz.w}, hza[4] = {hz.x, hz.y, hz.z, hz.w};
+    const int cha[4] = {ch.x, ch.y, ch.z, ch.w}, cna[4] = {cn.x, cn.y, cn.z, cn.w};
+    const V3 inv = R.inv, oi = R.oi;
+    const float tmin = R.tmin, tmax = R.tmax;
+    // entry distance per child (+inf when missed or empty), kept in
+    // registers; closest-hit visits near to far (sorting network), any-hit
+    // in node order.
+    float d0, d1, d2, d3;
+    int32_t r0, r1, r2, r3;
 #define PT_CHILD(c, dd, rr)                                                                          \
   {                                                                                                  \
     float t0x = fmaf(lxa[c], inv.x, oi.x), t1x = fmaf(hxa[c], inv.x, oi.x);                        \
@@ -179,12 +216,12 @@ __device__ bool traverse(const SceneView &S, V3 o, V3 d, float tmin, float tmax,
     dd = (cna[c] >= 0 && tn <= tf) ? tn : INFINITY;                                                 \
     rr = cna[c] == 0 ? cha[c] : leaf_ref(cha[c], max(cna[c], 1));                                   \
   }
-      PT_CHILD(0, d0, r0)
-      PT_CHILD(1, d1, r1)
-      PT_CHILD(2, d2, r2)
-      PT_CHILD(3, d3, r3)
+    PT_CHILD(0, d0, r0)
+    PT_CHILD(1, d1, r1)
+    PT_CHILD(2, d2, r2)
+    PT_CHILD(3, d3, r3)
 #undef PT_CHILD
-      if (!ANY) {
+    if (!ANY) {
 #define PT_CSWAP(da, ra, db, rb)   \
   if (db < da) {                   \
     float tt = da;                 \
@@ -194,51 +231,62 @@ __device__ bool traverse(const SceneView &S, V3 o, V3 d, float tmin, float tmax,
     ra = rb;                       \
     rb = tr;                       \
   }
-        PT_CSWAP(d0, r0, d1, r1)
-        PT_CSWAP(d2, r2, d3, r3)
-        PT_CSWAP(d0, r0, d2, r2)
-        PT_CSWAP(d1, r1, d3, r3)
-        PT_CSWAP(d1, r1, d2, r2)
+      PT_CSWAP(d0, r0, d1, r1)
+      PT_CSWAP(d2, r2, d3, r3)
+      PT_CSWAP(d0, r0, d2, r2)
+      PT_CSWAP(d1, r1, d3, r3)
+      PT_CSWAP(d1, r1, d2, r2)
 #undef PT_CSWAP
-      }
-      const int nh = (d0 < INFINITY) + (d1 < INFINITY) + (d2 < INFINITY) + (d3 < INFINITY);
-      if (nh == 0) {
-        if (sp == 0) break;
-        ref = stack[(--sp) * stride];
-        continue;
-      }
-      if (sp + nh - 1 > PT_STACK) {
-        *err = 1;
-        break;
-      }
-      // push the farther hits (far first), descend into the nearest
-      int32_t first = 0;
-      bool have = false;
-      if (ANY) {
-        // node order: descend into the first hit child, push the others
-        if (d3 < INFINITY) { first = r3; have = true; }
-        if (d2 < INFINITY) { if (have) stack[(sp++) * stride] = first; first = r2; have = true; }
-        if (d1 < INFINITY) { if (have) stack[(sp++) * stride] = first; first = r1; have = true; }
-        if (d0 < INFINITY) { if (have) stack[(sp++) * stride] = first; first = r0; have = true; }
-      } else {
-        if (d3 < INFINITY) stack[(sp++) * stride] = r3;
-        if (d2 < INFINITY) stack[(sp++) * stride] = r2;
-        if (d1 < INFINITY) stack[(sp++) * stride] = r1;
-        first = r0;  // d0 is the smallest and finite (nh > 0)
-        // r1..r3 were pushed only if hit; r0 is always the nearest hit
-      }
-      ref = first;
-    } else {
-      if (test_leaf<ANY>(S, ref, o, d, dn, tmin, tmax, hit)) {
-        found = true;
-        if (ANY) return true;
-      }
-      if (sp == 0) break;
-      ref = stack[(--sp) * stride];
     }
-    if (iter == PT_TRAVERSAL_CAP - 1) *err = 2;
+    const int nh = (d0 < INFINITY) + (d1 < INFINITY) + (d2 < INFINITY) + (d3 < INFINITY);
+    if (nh == 0) {
+      if (R.sp == 0) return true;
+      R.ref = stack[(--R.sp) * stride];
+      return false;
+    }
+    if (R.sp + nh - 1 > PT_STACK) {
+      *err = 1;
+      return true;
+    }
+    // push the farther hits (far first), descend into the nearest
+    int32_t first = 0;
+    int sp = R.sp;
+    if (ANY) {
+      // node order: descend into the first hit child, push the others
+      bool have = false;
+      if (d3 < INFINITY) { first = r3; have = true; }
+      if (d2 < INFINITY) { if (have) stack[(sp++) * stride] = first; first = r2; have = true; }
+      if (d1 < INFINITY) { if (have) stack[(sp++) * stride] = first; first = r1; have = true; }
+      if (d0 < INFINITY) { if (have) stack[(sp++) * stride] = first; first = r0; have = true; }
+    } else {
+      if (d3 < INFINITY) stack[(sp++) * stride] = r3;
+      if (d2 < INFINITY) stack[(sp++) * stride] = r2;
+      if (d1 < INFINITY) stack[(sp++) * stride] = r1;
+      first = r0;  // d0 is the smallest and finite (nh > 0)
+    }
+    R.sp = sp;
+    R.ref = first;
+    return false;
   }
-  return found;
+  if (test_leaf<ANY>(S, R.ref, R.o, R.d, R.dn, R.tmin, R.tmax, R.hit, R.time)) {
+    R.found = true;
+    if (ANY) return true;
+  }
+  if (R.sp == 0) return true;
+  R.ref = stack[(--R.sp) * stride];
+  return false;
+}
+
+// Whole traversal of one ray by one thread (batch test kernels).
+template <bool ANY>
+__device__ bool traverse(const SceneView &S, V3 o, V3 d, float tmin, float tmax, HitRec &hit,
+                         int32_t *stack, int stride, int *err, float time = 0.f) {
+  TravRay R;
+  trav_init(R, o, d, tmin, tmax, time);
+  while (!trav_step<ANY>(S, R, stack, stride, err)) {
+  }
+  hit = R.hit;
+  return R.found;
 }
 
 }  // namespace pt

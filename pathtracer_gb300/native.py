@@ -33,7 +33,7 @@ EXPORTS = [
     "pt_create", "pt_destroy", "pt_last_error", "pt_version", "pt_scene_upload", "pt_scene_release",
     "pt_scene_info", "pt_render", "pt_render_device", "pt_render_device_noalloc", "pt_profile_begin",
     "pt_profile_end", "pt_tonemap", "pt_sampler_eval", "pt_trace_closest",
-    "pt_trace_any", "pt_bsdf_eval", "pt_bsdf_sample", "pt_render_batch", "pt_server_create",
+    "pt_trace_any", "pt_bsdf_eval", "pt_bsdf_sample", "pt_render_batch", "pt_autotune", "pt_server_create",
     "pt_server_destroy", "pt_submit", "pt_server_step", "pt_poll", "pt_cancel",
 ]
 
@@ -68,7 +68,7 @@ class SphereDesc(C.Structure):
 
 
 class ObjectDesc(C.Structure):
-    _fields_ = [("kind", C.c_int32), ("index", C.c_int32)]
+    _fields_ = [("kind", C.c_int32), ("index", C.c_int32), ("velocity", C.c_float * 3)]
 
 
 class EnvDesc(C.Structure):
@@ -87,7 +87,7 @@ class SceneDesc(C.Structure):
         ("spheres", C.POINTER(SphereDesc)), ("n_spheres", C.c_int32),
         ("objects", C.POINTER(ObjectDesc)), ("n_objects", C.c_int32),
         ("env", C.POINTER(EnvDesc)), ("medium", C.POINTER(MediumDesc)),
-        ("bg_color", C.c_float * 3), ("bvh_mode", C.c_int32),
+        ("bg_color", C.c_float * 3), ("bvh_mode", C.c_int32), ("shutter_max", C.c_float),
     ]
 
 
@@ -111,6 +111,12 @@ class JobDesc(C.Structure):
 class Stats(C.Structure):
     _fields_ = [("paths", C.c_uint64), ("segments", C.c_uint64), ("rays", C.c_uint64),
                 ("shadow_rays", C.c_uint64), ("ms", C.c_double), ("algorithmic_bytes", C.c_uint64)]
+
+
+class Tuning(C.Structure):
+    _fields_ = [("wave_paths", C.c_int32), ("sort_by_material", C.c_int32), ("trace_blocks", C.c_int32),
+                ("shade_blocks", C.c_int32), ("best_ms", C.c_double), ("default_ms", C.c_double),
+                ("candidates", C.c_int32)]
 
 
 class RequestDesc(C.Structure):
@@ -151,6 +157,7 @@ def load() -> C.CDLL:
         "pt_bsdf_sample": [vp, C.POINTER(MaterialDesc), C.c_int32, f32p, f32p, u8p, f32p, f32p, u8p, f32p,
                            f32p, f32p, u32p],
         "pt_render_batch": [vp, C.POINTER(JobDesc), C.c_int32, C.POINTER(f32p), C.POINTER(Stats)],
+        "pt_autotune": [vp, C.POINTER(JobDesc), C.c_int32, C.POINTER(Tuning)],
         "pt_server_create": [vp, C.c_int64, C.c_int32, C.POINTER(vp)],
         "pt_server_destroy": [vp],
         "pt_submit": [vp, C.POINTER(RequestDesc), C.POINTER(C.c_int64)],
@@ -238,7 +245,9 @@ def make_scene_desc(scene) -> SceneBuffers:
     sb.hold(spheres)
     d.spheres = spheres
     d.n_spheres = len(scene.spheres)
-    objs = (ObjectDesc * max(1, len(scene.objects)))(*[ObjectDesc(k, i) for k, i in scene.objects])
+    objs = (ObjectDesc * max(1, len(scene.objects)))(
+        *[ObjectDesc(o[0], o[1], (C.c_float * 3)(*[float(x) for x in (o[2] if len(o) > 2 else (0, 0, 0))]))
+          for o in scene.objects])
     sb.hold(objs)
     d.objects = objs
     d.n_objects = len(scene.objects)
@@ -253,6 +262,7 @@ def make_scene_desc(scene) -> SceneBuffers:
         sb.hold(md)
         d.medium = C.pointer(md)
     d.bg_color[:] = [float(x) for x in scene.bg]
+    d.shutter_max = float(getattr(scene, "shutter_max", 0.0))
     return sb
 
 
@@ -363,6 +373,23 @@ class Renderer:
         return out
 
     # -- batch test entry points
+    def render_batch(self, jobs, stats: bool = False):
+        """pt_render_batch: one graph launch for all jobs; returns the mean films."""
+        n = len(jobs)
+        arr = (JobDesc * n)(*jobs)
+        films = [np.zeros((j.height, j.width, 3), np.float32) for j in jobs]
+        ptrs = (f32p * n)(*[_ptr(f, C.c_float) for f in films])
+        st = Stats()
+        self._check(self.lib.pt_render_batch(self.ctx, arr, n, ptrs, C.byref(st)))
+        return (films, st) if stats else films
+
+    def autotune(self, jobs) -> dict:
+        n = len(jobs)
+        arr = (JobDesc * n)(*jobs)
+        t = Tuning()
+        self._check(self.lib.pt_autotune(self.ctx, arr, n, C.byref(t)))
+        return {k: getattr(t, k) for k, _ in Tuning._fields_}
+
     def sampler_eval(self, strategy: int, first_index: int, n: int, dims: int, seed: int = 0) -> np.ndarray:
         out = np.zeros((n, dims), np.float32)
         self._check(self.lib.pt_sampler_eval(self.ctx, strategy, seed, first_index, n, dims,
@@ -412,3 +439,56 @@ class Renderer:
                                             _ptr(ok, C.c_uint8), _ptr(wi, C.c_float), _ptr(att, C.c_float),
                                             _ptr(pdf, C.c_float), _ptr(ty, C.c_uint32)))
         return ok.astype(bool), wi, att, pdf, ty
+
+
+REQ_QUEUED, REQ_RUNNING, REQ_DONE, REQ_CANCELLED, REQ_FAILED = range(5)
+
+
+class Server:
+    """Request loop over a :class:`Renderer` (pt_server_* / pt_submit / pt_poll).
+
+    Each ``step()`` admits queued requests while slots and the HBM budget
+    allow, then adds ``spp_per_pass`` samples to every active request in one
+    batched launch.
+    """
+
+    def __init__(self, renderer: Renderer, hbm_budget: int = 8 << 30, max_slots: int = 64):
+        self.r = renderer
+        self.lib = renderer.lib
+        self.handle = C.c_void_p()
+        renderer._check(self.lib.pt_server_create(renderer.ctx, hbm_budget, max_slots, C.byref(self.handle)))
+        self.shapes = {}
+
+    def close(self):
+        if self.handle:
+            self.lib.pt_server_destroy(self.handle)
+            self.handle = C.c_void_p()
+
+    def submit(self, job: JobDesc, target_rmse: float = 0.0, spp_cap: int = 0, spp_per_pass: int = 1) -> int:
+        req = RequestDesc()
+        req.job = job
+        req.target_rmse = target_rmse
+        req.spp_cap = spp_cap if spp_cap > 0 else job.spp_x * job.spp_y
+        req.spp_per_pass = spp_per_pass
+        rid = C.c_int64()
+        self.r._check(self.lib.pt_submit(self.handle, C.byref(req), C.byref(rid)))
+        self.shapes[rid.value] = (job.height, job.width, 3)
+        return rid.value
+
+    def step(self) -> int:
+        active = C.c_int32()
+        self.r._check(self.lib.pt_server_step(self.handle, C.byref(active)))
+        return active.value
+
+    def poll(self, rid: int):
+        """(state, film or None, spp_done, latency_ms)."""
+        st = C.c_int32()
+        done = C.c_int32()
+        lat = C.c_double()
+        film = np.zeros(self.shapes[rid], np.float32)
+        self.r._check(self.lib.pt_poll(self.handle, rid, C.byref(st), _ptr(film, C.c_float), C.byref(done),
+                                       C.byref(lat)))
+        return st.value, (film if st.value == REQ_DONE else None), done.value, lat.value
+
+    def cancel(self, rid: int):
+        self.r._check(self.lib.pt_cancel(self.handle, rid))

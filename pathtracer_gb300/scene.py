@@ -41,27 +41,32 @@ class Scene:
     meshes: list = field(default_factory=list)
     quads: list = field(default_factory=list)       # (axis, k, d0min, d0max, d1min, d1max, material, flip)
     spheres: list = field(default_factory=list)     # ((cx, cy, cz), r, material, flip)
-    objects: list = field(default_factory=list)     # (kind, index)
+    objects: list = field(default_factory=list)     # (kind, index, velocity)
     env: np.ndarray | None = None                   # (H, W, 3), row 0 = bottom
     env_intensity: float = 1.0
     medium: tuple | None = None                     # (sigma_a[3], sigma_s[3], g)
     bg: tuple = (0.0, 0.0, 0.0)
+    shutter_max: float = 0.0                        # motion blur: longest shutter of any job
 
     def add_material(self, mtype: int, params, flags: int = 0) -> int:
         self.materials.append((mtype, list(params), flags))
         return len(self.materials) - 1
 
-    def add_mesh(self, mesh: Mesh):
+    def add_mesh(self, mesh: Mesh, velocity=(0.0, 0.0, 0.0)):
         self.meshes.append(mesh)
-        self.objects.append((N.OBJ_MESH, len(self.meshes) - 1))
+        self.objects.append((N.OBJ_MESH, len(self.meshes) - 1, tuple(velocity)))
 
-    def add_quad(self, axis, k, d0min, d0max, d1min, d1max, material, flip=0):
+    def add_quad(self, axis, k, d0min, d0max, d1min, d1max, material, flip=0, velocity=(0.0, 0.0, 0.0)):
         self.quads.append((axis, k, d0min, d0max, d1min, d1max, material, flip))
-        self.objects.append((N.OBJ_QUAD, len(self.quads) - 1))
+        self.objects.append((N.OBJ_QUAD, len(self.quads) - 1, tuple(velocity)))
 
-    def add_sphere(self, center, radius, material, flip=0):
+    def add_sphere(self, center, radius, material, flip=0, velocity=(0.0, 0.0, 0.0)):
         self.spheres.append((tuple(center), radius, material, flip))
-        self.objects.append((N.OBJ_SPHERE, len(self.spheres) - 1))
+        self.objects.append((N.OBJ_SPHERE, len(self.spheres) - 1, tuple(velocity)))
+
+    @property
+    def has_motion(self) -> bool:
+        return any(len(o) > 2 and any(v != 0.0 for v in o[2]) for o in self.objects)
 
     @property
     def n_triangles(self) -> int:

@@ -1,0 +1,165 @@
+"""Batched and served forms (pt_render_batch, pt_autotune, pt_server_*).
+
+A path's sample streams depend only on its own job (seed, pixel, sample
+index), so a job rendered in a batch, or a request served among others, gives
+the same film as the job rendered alone: bit for bit when the per-pixel
+summation is grouped the same way, otherwise within FP32 summation rounding
+(relative 1e-5).
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from pathtracer_gb300 import native as N
+from pathtracer_gb300 import scene as S
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def scenes(renderer):
+    cb, cam_cb = S.cornell_icosphere(3)
+    rg, cam_rg = S.rough_glass(subdiv=3, env_w=128, env_h=64, seed=2)
+    md, cam_md = S.material_divergence(subdiv=2, seed=3, aspect=1.0)
+    ids = [renderer.upload(cb), renderer.upload(rg), renderer.upload(md)]
+    yield list(zip(ids, [cam_cb, cam_rg, cam_md]))
+    for sid in ids:
+        renderer.release(sid)
+
+
+def _jobs(scenes):
+    (s0, c0), (s1, c1), (s2, c2) = scenes
+    return [
+        N.job_desc(s0, c0, 48, 40, 4, 2, 8, seed=1, estimator=N.EST_NEE_MIS),
+        N.job_desc(s1, c1, 32, 32, 2, 2, 12, seed=2, estimator=N.EST_NEE_MIS, env_sampling=N.ENV_ALIAS,
+                   rr_start=4),
+        N.job_desc(s2, c2, 40, 24, 4, 4, 6, seed=3, estimator=N.EST_NEE_MIS, sampler=N.SAMPLER_STRATIFIED),
+        N.job_desc(s0, c0, 16, 16, 8, 8, 8, seed=4, estimator=N.EST_REF_NEE),
+    ]
+
+
+def test_batch_matches_individual(renderer, scenes):
+    jobs = _jobs(scenes)
+    films, st = renderer.render_batch(jobs, stats=True)
+    assert st.paths == sum(j.width * j.height * j.spp_x * j.spp_y for j in jobs)
+    for j, f in zip(jobs, films):
+        alone = renderer.render(j)
+        assert np.isfinite(f).all()
+        assert np.allclose(f, alone, rtol=1e-5, atol=1e-7), np.abs(f - alone).max()
+
+
+def test_batch_graph_replay_identical(renderer, scenes):
+    jobs = _jobs(scenes)
+    a = renderer.render_batch(jobs)
+    b = renderer.render_batch(jobs)  # replay of the captured graph
+    c = renderer.render_batch(jobs[::-1])[::-1]  # another composition
+    for x, y, z in zip(a, b, c):
+        assert np.array_equal(x, y)
+        assert np.array_equal(x, z)
+
+
+def test_batch_empty_and_invalid(renderer, scenes):
+    assert renderer.render_batch([]) == []
+    bad = _jobs(scenes)[:1]
+    bad[0].scene = 999
+    with pytest.raises(N.PtError):
+        renderer.render_batch(bad)
+
+
+def test_autotune_picks_a_candidate(scenes):
+    # a context of its own: the tuned launch configuration stays with it
+    r = N.Renderer(0)
+    cb, cam_cb = S.cornell_icosphere(3)
+    md, cam_md = S.material_divergence(subdiv=2, seed=3, aspect=1.0)
+    a, b = r.upload(cb), r.upload(md)
+    jobs = [N.job_desc(a, cam_cb, 64, 48, 4, 4, 8, seed=1, estimator=N.EST_NEE_MIS),
+            N.job_desc(b, cam_md, 32, 32, 2, 4, 6, seed=3, estimator=N.EST_NEE_MIS,
+                       sampler=N.SAMPLER_STRATIFIED)]
+    renderer = r
+    ref = renderer.render_batch(jobs)
+    t = renderer.autotune(jobs)
+    assert t["candidates"] == 24
+    assert t["wave_paths"] in (1 << 20, 1 << 22, 1 << 24)
+    assert t["sort_by_material"] in (0, 1)
+    assert 0.0 < t["best_ms"] <= t["default_ms"] + 1e-9
+    after = renderer.render_batch(jobs)
+    # the tuned configuration may shade through the generic kernel instead of
+    # the per-family ones (separately compiled arithmetic, so a rare path can
+    # branch differently): the images agree statistically, nearly all pixels
+    # to rounding
+    for x, y in zip(ref, after):
+        close = np.isclose(x, y, rtol=1e-4, atol=1e-6).all(-1)
+        assert close.mean() > 0.95, close.mean()
+        assert abs(float(x.mean()) - float(y.mean())) <= 2e-2 * float(x.mean())
+    r.close()
+
+
+def _serve_until_done(srv, ids, max_steps=10000):
+    for _ in range(max_steps):
+        if srv.step() == 0:
+            break
+    out = {}
+    for rid in ids:
+        st, film, spp, lat = srv.poll(rid)
+        assert st == N.REQ_DONE, st
+        assert lat >= 0.0
+        out[rid] = (film, spp)
+    return out
+
+
+def test_served_same_alone_and_in_mix(renderer, scenes):
+    jobs = _jobs(scenes)
+    probe = jobs[0]
+    # alone
+    srv = N.Server(renderer, hbm_budget=1 << 30, max_slots=8)
+    rid = srv.submit(probe, spp_per_pass=2)
+    alone, spp_alone = _serve_until_done(srv, [rid])[rid]
+    srv.close()
+    assert spp_alone == probe.spp_x * probe.spp_y
+    # in a mix: one request already running, others arriving mid-flight
+    srv = N.Server(renderer, hbm_budget=1 << 30, max_slots=8)
+    first = srv.submit(jobs[1], spp_per_pass=1)
+    srv.step()
+    rid = srv.submit(probe, spp_per_pass=2)
+    srv.step()
+    late = [srv.submit(jobs[2], spp_per_pass=4), srv.submit(jobs[3], spp_per_pass=8)]
+    res = _serve_until_done(srv, [first, rid] + late)
+    srv.close()
+    mixed, spp_mixed = res[rid]
+    assert spp_mixed == spp_alone
+    assert np.array_equal(alone, mixed)
+    # and the served film is the job's film (pass sums grouped differently)
+    ref = renderer.render(probe)
+    assert np.allclose(mixed, ref, rtol=1e-5, atol=1e-7)
+    for r, j in zip([first] + late, [jobs[1], jobs[2], jobs[3]]):
+        assert np.allclose(res[r][0], renderer.render(j), rtol=1e-5, atol=1e-7)
+
+
+def test_served_rmse_target_and_cap(renderer, scenes):
+    jobs = _jobs(scenes)
+    srv = N.Server(renderer, hbm_budget=1 << 30, max_slots=4)
+    easy = srv.submit(jobs[0], target_rmse=1e9, spp_per_pass=1)  # met once both halves have a pass
+    capped = srv.submit(jobs[3], spp_cap=6, spp_per_pass=4)
+    res = _serve_until_done(srv, [easy, capped])
+    srv.close()
+    assert res[easy][1] == 2
+    assert res[capped][1] == 6
+
+
+def test_server_admission_by_budget_and_cancel(renderer, scenes):
+    jobs = _jobs(scenes)
+    j = jobs[0]
+    film_bytes = 2 * j.width * j.height * 3 * 4
+    srv = N.Server(renderer, hbm_budget=film_bytes, max_slots=8)  # one request's films at a time
+    a = srv.submit(j, spp_per_pass=8)
+    b = srv.submit(j, spp_per_pass=8)
+    c = srv.submit(j, spp_per_pass=8)
+    srv.cancel(c)
+    srv.step()
+    st_b = srv.poll(b)[0]
+    assert st_b == N.REQ_QUEUED  # no room until a's films are released
+    res = _serve_until_done(srv, [a, b])
+    assert srv.poll(c)[0] == N.REQ_CANCELLED
+    srv.close()
+    assert np.array_equal(res[a][0], res[b][0])
