@@ -53,6 +53,10 @@ def parse():
     ap.add_argument("--workload", default="rough_glass", choices=["rough_glass", "cornell", "divergence"])
     ap.add_argument("--spp-per-step", type=int, default=16)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-forms", action="store_true", help="skip the batched and served forms")
+    ap.add_argument("--batch-jobs", type=int, default=96)
+    ap.add_argument("--serve-seconds", type=float, default=10.0)
+    ap.add_argument("--serve-rate", type=float, default=20.0, help="Poisson arrivals per second")
     return ap.parse_args()
 
 
@@ -175,6 +179,188 @@ def cpu_paths_per_sec(osc, cam, wl, estimator, threads, target_s=12.0, max_px=10
     osc.render(job, threads=threads)
     dt = time.perf_counter() - t0
     return res * res / dt, f"{res}x{res} pixels x 1 spp of the workload's scene and camera", dt
+
+
+def form_scenes(r, with_big: bool):
+    """The resident scenes of the batched and served forms: the three
+    workloads with seeded per-object motion (meshes and spheres move, walls,
+    ground and area lights stay), plus for serving the 5,242,880-triangle
+    displaced-sphere variant of the rough-glass scene.  Values: (scene id,
+    camera, focus distance)."""
+    from pathtracer_gb300 import scene as S
+
+    out = {}
+    t0 = time.perf_counter()
+    sc, cam = S.cornell_icosphere(4)
+    out["cornell"] = (r.upload(S.with_motion(sc, seed=21)), cam, 1.9)
+    sc, cam = S.rough_glass(8)
+    out["rough_glass"] = (r.upload(S.with_motion(sc, seed=22)), cam, 4.24)
+    sc, cam = S.material_divergence(5)
+    out["divergence"] = (r.upload(S.with_motion(sc, seed=23)), cam, 11.9)
+    big = None
+    if with_big:
+        sc, cam = S.rough_glass(9, seed=5)
+        big = (r.upload(S.with_motion(sc, seed=24)), cam, 4.24)
+    return out, big, time.perf_counter() - t0
+
+
+def run_batched(r, scenes, n_jobs: int, seed: int = 11):
+    """Config-3 job mix: one pt_render_batch call (one CUDA-graph launch)
+    against the plain wavefront drop-in (pt_render per job, one after the
+    other); both with host films, so both are end to end.  The two arms
+    render the same samples, so their images (and RMSE) are equal; the
+    largest relative film difference is reported."""
+    from pathtracer_gb300 import scene as S
+
+    jobs = S.job_mix(scenes, n_jobs, seed=seed)
+    paths = sum(j.width * j.height * j.spp_x * j.spp_y for j in jobs)
+    # autotune the batch launch on a small sample of the mix (first 8 jobs, 4 spp)
+    tj = []
+    for j in jobs[:8]:
+        jj = type(j).from_buffer_copy(j)
+        jj.spp_x, jj.spp_y, jj.spp_begin, jj.spp_end = 2, 2, 0, 0
+        tj.append(jj)
+    t0 = time.perf_counter()
+    tuning = r.autotune(tj)
+    tune_s = time.perf_counter() - t0
+    # warm: queue allocation and graph capture
+    r.render_batch(jobs)
+    t0 = time.perf_counter()
+    films_b, st = r.render_batch(jobs, stats=True)
+    t_batch = time.perf_counter() - t0
+    # plain wavefront, one job after the other (warm the context's queues first)
+    r.render(jobs[0])
+    t0 = time.perf_counter()
+    films_p = [r.render(j) for j in jobs]
+    t_plain = time.perf_counter() - t0
+    rel = 0.0
+    for a, b in zip(films_b, films_p):
+        d = np.abs(a - b).max() / max(1e-12, float(np.abs(b).max()))
+        rel = max(rel, float(d))
+    res = sorted(j.width for j in jobs)
+    return {
+        "jobs": n_jobs, "paths": paths, "paths_per_s": paths / t_batch, "plain_paths_per_s": paths / t_plain,
+        "speedup_vs_plain": t_plain / t_batch, "batch_s": t_batch, "plain_s": t_plain,
+        "graph_device_ms": st.ms, "max_rel_film_diff_vs_plain": rel,
+        "equal_rmse": "same samples in both arms: identical images up to FP32 summation order",
+        "mix": f"{n_jobs} jobs over cornell/rough_glass/divergence with per-object motion; square resolution "
+               f"log-uniform 64..1024 (median {res[len(res) // 2]}), spp U{{4..256}}, lens diameter U[0,0.05], "
+               "shutter U[0,0.5], NEE+MIS",
+        "autotune": {k: tuning[k] for k in ("wave_paths", "sort_by_material", "trace_blocks", "shade_blocks")} |
+                    {"candidates": tuning["candidates"], "seconds": tune_s},
+    }
+
+
+def run_served(r, scenes, big, seconds: float, rate: float, seed: int = 12):
+    """Serving: Poisson arrivals at `rate` req/s for `seconds` over the
+    resident scenes; each request a seeded camera, square resolution
+    log-uniform 128..512, an spp cap U{16..128} and a target RMSE of 0.02
+    (whichever comes first), 8 spp per scheduling pass.  Latency is from the
+    request's arrival to its completion.  The plain arm renders the same
+    requests (same samples, spp as served) one after the other through
+    pt_render."""
+    from pathtracer_gb300 import native as N
+    from pathtracer_gb300 import scene as S
+
+    rng = np.random.default_rng(seed)
+    pool = dict(scenes)
+    if big is not None:
+        pool["rough_glass_5m"] = big
+    names = sorted(pool)
+    reqs = []
+    t = 0.0
+    while True:
+        t += float(rng.exponential(1.0 / rate))
+        if t > seconds:
+            break
+        name = names[int(rng.integers(len(names)))]
+        key = "rough_glass" if name == "rough_glass_5m" else name
+        sid, cam, focus = pool[name]
+        side = int(round(np.exp(rng.uniform(np.log(128), np.log(512)))))
+        cap = int(rng.integers(16, 129))
+        job = S.job_mix({key: (sid, cam, focus)}, 1, seed=int(rng.integers(1 << 30)), res=(side, side),
+                        spp=(cap, cap))[0]
+        reqs.append((t, job, cap))
+    srv = N.Server(r, hbm_budget=32 << 30, max_slots=64)
+    lat, spp_done = {}, {}
+    arrival = {}
+    outstanding = set()
+    busy = 0.0
+    k = 0
+    t0 = time.perf_counter()
+    while k < len(reqs) or outstanding:
+        now = time.perf_counter() - t0
+        while k < len(reqs) and reqs[k][0] <= now:
+            rid = srv.submit(reqs[k][1], target_rmse=0.02, spp_cap=reqs[k][2], spp_per_pass=8)
+            arrival[rid] = (reqs[k][0], k)
+            outstanding.add(rid)
+            k += 1
+        if not outstanding:
+            time.sleep(max(0.0, reqs[k][0] - (time.perf_counter() - t0)))
+            continue
+        s0 = time.perf_counter()
+        srv.step()
+        busy += time.perf_counter() - s0
+        now = time.perf_counter() - t0
+        for rid in list(outstanding):
+            st, n = srv.state(rid)
+            if st >= N.REQ_DONE:
+                outstanding.discard(rid)
+                lat[rid] = (now - arrival[rid][0]) * 1e3
+                spp_done[arrival[rid][1]] = n
+    wall = time.perf_counter() - t0
+    srv.close()
+    served_paths = sum(reqs[i][1].width * reqs[i][1].height * n for i, n in spp_done.items())
+    # plain arm: the same requests at the spp they were served with
+    t0 = time.perf_counter()
+    for i, n in spp_done.items():
+        j = reqs[i][1]
+        j.spp_begin, j.spp_end = 0, n
+        r.render(j)
+    t_plain = time.perf_counter() - t0
+    ls = sorted(lat.values())
+    pct = lambda q: ls[min(len(ls) - 1, int(q * len(ls)))] if ls else None
+    return {
+        "requests": len(reqs), "completed": len(lat), "rate_req_s": rate, "seconds": seconds,
+        "p50_ms": pct(0.50), "p99_ms": pct(0.99), "max_ms": ls[-1] if ls else None,
+        "paths": served_paths, "paths_per_s_busy": served_paths / busy if busy else None,
+        "paths_per_s_wall": served_paths / wall, "plain_paths_per_s": served_paths / t_plain,
+        "speedup_vs_plain": t_plain / busy if busy else None,
+        "mean_spp": float(np.mean(list(spp_done.values()))) if spp_done else None,
+        "mix": "4 resident scenes (cornell, rough_glass 1.3M tris, divergence, rough_glass 5.2M tris) with motion; "
+               "res log-uniform 128..512, spp cap U{16..128}, target RMSE 0.02, 8 spp per pass",
+    }
+
+
+def converged_rmse(r, sid, cam, wl, k_step: int, win: int = 64, ref_grid: int = 256):
+    """RMSE of the workload's render against a converged reference on the
+    frame's centre window: the reference is the GPU render of that window at
+    ref_grid^2 = 65536 spp (a window job has the full frame's sample
+    streams; the GPU against the oracle at high spp on small windows is
+    tests/test_gpu_converged.py).  Reported for one bench step (k_step spp)
+    and for the workload's full spp."""
+    from pathtracer_gb300 import native as N
+
+    W, H = wl["W"], wl["H"]
+    x0, y0 = (W - win) // 2, (H - win) // 2
+
+    def job(sx, sy, begin=0, end=0, seed=1):
+        j = N.job_desc(sid, cam, win, win, sx, sy, wl["depth"], rr_start=wl["rr"], estimator=wl["est"],
+                       sampler=wl["sampler"], env_sampling=wl["env"], seed=seed, spp_begin=begin, spp_end=end)
+        j.crop_x, j.crop_y, j.full_width, j.full_height = x0, y0, W, H
+        return j
+
+    t0 = time.perf_counter()
+    ref = r.render(job(ref_grid, ref_grid, seed=977))
+    ref_s = time.perf_counter() - t0
+    full = r.render(job(wl["sx"], wl["sy"]))
+    step = r.render(job(wl["sx"], wl["sy"], 0, k_step))
+    rm = lambda a: float(np.sqrt(np.mean((a.astype(np.float64) - ref) ** 2)))
+    return {"reference": f"GPU {ref_grid * ref_grid} spp on the {win}x{win} centre window of the "
+                         f"{W}x{H} frame (independent seed); oracle spot-check in tests/test_gpu_converged.py",
+            "rmse_full_spp": rm(full), "full_spp": wl["sx"] * wl["sy"], "rmse_step_spp": rm(step),
+            "step_spp": k_step, "reference_seconds": ref_s,
+            "equal_rmse_forms": "batched and served jobs render the same samples as the plain path"}
 
 
 def run_reference(args, rank, world):
@@ -339,6 +525,14 @@ def run_ours(args, rank, world, local_rank):
         "clocks": clk.summary(),
         "wall_s": wall,
     }
+    if world == 1:
+        line["rmse"] = converged_rmse(r, sid, cam, wl, k)
+    if world == 1 and not args.no_forms:
+        fs, big, build_s = form_scenes(r, with_big=True)
+        forms = {"scene_build_s": build_s}
+        forms["batched"] = run_batched(r, fs, args.batch_jobs)
+        forms["served"] = run_served(r, fs, big, args.serve_seconds, args.serve_rate)
+        line["forms"] = forms
     if not args.no_cpu_baseline:
         from oracle import pyoracle as O
 

@@ -230,7 +230,13 @@ typedef struct pt_job_desc {
   uint32_t sampler_seed;     /* HaltonSampler seed (PermuteDigits only) */
   pt_camera_desc camera;
   float gamma;               /* GAMMA, config.hpp:10 */
-  int32_t reserved[4];
+  /* Window of a larger frame (extension; converged references, tiles): the
+   * job renders pixels [crop_x, crop_x + width) x [crop_y, crop_y + height)
+   * of a full_width x full_height frame with the sample streams of the full
+   * frame's pixels, so a window equals the same pixels of the full render.
+   * full_width = full_height = 0: the job is the whole frame. */
+  int32_t crop_x, crop_y;
+  int32_t full_width, full_height;
 } pt_job_desc;
 
 typedef struct pt_stats {

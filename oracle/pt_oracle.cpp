@@ -1450,6 +1450,11 @@ int or_render(void *s, const pt_job_desc *job, float *mean, float *var, int thre
   Camera cam(j.camera);
   auto off = offsets(j);
   const int W = j.width, H = j.height, Sn = j.spp_x * j.spp_y;
+  // window of a larger frame (pt_job_desc crop fields): frame coordinates
+  // drive the camera and the sample streams
+  const bool win = j.full_width > 0 || j.full_height > 0;
+  const int X0 = win ? j.crop_x : 0, Y0 = win ? j.crop_y : 0;
+  const int FW = win ? j.full_width : W, FH = win ? j.full_height : H;
   const int b = j.spp_begin, e = j.spp_end ? j.spp_end : Sn;
   if (threads <= 0) threads = (int)std::max(1u, std::thread::hardware_concurrency());
   const bool use_rec = recursive && !S.medium && j.estimator == PT_EST_REF_NEE;
@@ -1458,11 +1463,12 @@ int or_render(void *s, const pt_job_desc *job, float *mean, float *var, int thre
     for (int i = next_col++; i < W; i = next_col++) {
       for (int jj = 0; jj < H; ++jj) {
         double sum[3] = {0, 0, 0}, sq[3] = {0, 0, 0};
+        const int gi = X0 + i, gj = Y0 + jj;
         for (int k = b; k < e; ++k) {
-          uint64_t lin = ((uint64_t)i * H + jj) * (uint64_t)Sn + k;
-          PathCtx P{&S, &j, path_key(j.seed, lin), (uint32_t)(lin + 1u), jj * W + i, k};
+          uint64_t lin = ((uint64_t)gi * FH + gj) * (uint64_t)Sn + k;
+          PathCtx P{&S, &j, path_key(j.seed, lin), (uint32_t)(lin + 1u), gj * FW + gi, k};
           P.time = j.camera.shutter > 0.f ? j.camera.shutter * rand01(P.key, 3u) : 0.f;
-          float u = ((float)i + off[k].first) / (float)W, v = ((float)jj + off[k].second) / (float)H;
+          float u = ((float)gi + off[k].first) / (float)FW, v = ((float)gj + off[k].second) / (float)FH;
           float lx = -cam.r + (cam.r - -cam.r) * rand01(P.key, 1u);
           float ly = -cam.r + (cam.r - -cam.r) * rand01(P.key, 2u);
           V ps = cam.pos + (cam.hv * lx + cam.vv * ly);

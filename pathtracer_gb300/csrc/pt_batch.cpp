@@ -1,20 +1,27 @@
-// pt_batch.cpp -- batched rendering: many jobs (different scenes, sizes, spp)
-// in ONE CUDA-graph launch.
+// pt_batch.cpp -- batched rendering: many jobs (different scenes, sizes, spp,
+// cameras) in ONE CUDA-graph launch of merged waves.
 //
-// Every job of a batch gets its own work queues, offset table and device
-// film (reused across calls) and its own branch of the graph: the branch runs
-// the job's waves (camera, bounces of trace / sort / shade / shadow, film) on
-// a stream forked from the context's stream, so the jobs' kernels run
-// concurrently on the device and share the resident scenes' BVHs.  The graph
-// is captured once per batch composition and replayed while the composition
-// is unchanged.  Results per job are independent of the batch: a path's
-// sample streams depend only on its own job.
+// The jobs are grouped by scene and light-sample count.  A group's jobs are
+// concatenated into one sequence of paths (job k owns merged indices
+// [start[k], start[k+1])) and rendered in waves over that sequence: every
+// kernel of a bounce processes the paths of all the group's jobs at once,
+// looking up each path's job in a table in HBM, so a small job costs its
+// paths and not a chain of kernel launches of its own.  Each group runs on
+// its own branch of the graph (a stream forked from the context's stream);
+// the groups share nothing but the resident scenes.  The graph is captured
+// per batch composition and updated in place when only parameters change.
+//
+// A job's result does not depend on the batch: a path's sample streams depend
+// only on its own job, and films add samples one by one in sample order
+// whatever the wave boundaries.
 #include <cuda_runtime.h>
 
 #include <algorithm>
 #include <chrono>
 #include <cstring>
+#include <map>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "pt_batch.h"
@@ -31,19 +38,23 @@ void BatchSlot::release() {
   for (void *p : mem) cudaFree(p);
   mem.clear();
   cap = ln = 0;
-  if (offsets) cudaFree(offsets);
-  offsets = nullptr;
-  offsets_cap = 0;
-  if (film) cudaFree(film);
-  film = nullptr;
-  film_cap = 0;
+  auto fr = [](auto *&p) {
+    if (p) cudaFree(p);
+    p = nullptr;
+  };
+  fr(d_jobs);
+  fr(d_start);
+  fr(offsets);
+  fr(films);
+  jobs_cap = 0;
+  offsets_cap = films_cap = 0;
   if (stream) cudaStreamDestroy(stream);
   stream = nullptr;
   if (done) cudaEventDestroy(done);
   done = nullptr;
 }
 
-void BatchSlot::ensure(int want_cap, int want_ln, size_t film_floats, int spp) {
+void BatchSlot::ensure(int want_cap, int want_ln, int n_jobs, size_t n_offsets, size_t film_floats) {
   if (!stream) cuda_check(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "cudaStreamCreate");
   if (!done) cuda_check(cudaEventCreateWithFlags(&done, cudaEventDisableTiming), "cudaEventCreate");
   if (want_cap > cap || want_ln > ln) {
@@ -73,93 +84,154 @@ void BatchSlot::ensure(int want_cap, int want_ln, size_t film_floats, int spp) {
     Q.err = (int *)alloc(16);
     Q.sort_key = (int *)alloc(c * 4);
     Q.order = (int *)alloc(c * 4);
+    Q.job = (int *)alloc(c * 4);
     Q.bins = (int *)alloc(sizeof(int) * 2 * PT_SORT_BINS);
     Q.seg = (int *)alloc(sizeof(int) * (PT_SORT_BINS + 1));
     cuda_check(cudaMemset(Q.err, 0, 16), "memset err");
     cap = want_cap;
     ln = want_ln;
   }
-  if (spp > offsets_cap) {
+  if (n_jobs > jobs_cap) {
+    if (d_jobs) cudaFree(d_jobs);
+    if (d_start) cudaFree(d_start);
+    d_jobs = nullptr;
+    d_start = nullptr;
+    cuda_check(cudaMalloc(&d_jobs, sizeof(DeviceJob) * n_jobs), "cudaMalloc(batch jobs)");
+    cuda_check(cudaMalloc(&d_start, sizeof(long long) * (n_jobs + 1)), "cudaMalloc(batch starts)");
+    jobs_cap = n_jobs;
+  }
+  if (n_offsets > offsets_cap) {
     if (offsets) cudaFree(offsets);
     offsets = nullptr;
-    cuda_check(cudaMalloc(&offsets, sizeof(float2) * spp), "cudaMalloc(batch offsets)");
-    offsets_cap = spp;
+    cuda_check(cudaMalloc(&offsets, sizeof(float2) * n_offsets), "cudaMalloc(batch offsets)");
+    offsets_cap = n_offsets;
   }
-  if (film_floats > film_cap) {
-    if (film) cudaFree(film);
-    film = nullptr;
-    cuda_check(cudaMalloc(&film, film_floats * sizeof(float)), "cudaMalloc(batch film)");
-    film_cap = film_floats;
+  if (film_floats > films_cap) {
+    if (films) cudaFree(films);
+    films = nullptr;
+    cuda_check(cudaMalloc(&films, film_floats * sizeof(float)), "cudaMalloc(batch films)");
+    films_cap = film_floats;
   }
 }
 
-static std::string signature(const pt_job_desc *jobs, int n, const LaunchCfg &cfg, int per_job_cap,
+// One merged group: the jobs (indices into the batch) of one scene and one
+// light-sample count, in batch order.
+struct Group {
+  int scene;
+  int ln;
+  std::vector<int> members;
+  MergedJobs M;
+  long long total = 0;
+  int wave = 0;
+  std::vector<size_t> film_off;  // offset of each member's film in the slot's film array
+  size_t film_floats = 0;
+};
+
+static std::string signature(const pt_job_desc *jobs, int n, const LaunchCfg &cfg, int per_group_cap,
                              float **targets) {
   std::string s((const char *)jobs, (const char *)(jobs + n));
   s.append((const char *)&cfg, sizeof cfg);
-  s.append((const char *)&per_job_cap, sizeof per_job_cap);
+  s.append((const char *)&per_group_cap, sizeof per_group_cap);
   if (targets) s.append((const char *)targets, sizeof(float *) * n);
   return s;
 }
 
-// Renders the batch; films[k] (host, may be null) receive job k's mean image.
+// Renders the batch; films[k] (host, may be null) receive job k's mean image;
+// with targets, job k's samples are added onto the device film targets[k].
 void render_batch(Context *c, const pt_job_desc *jobs, int n, float **films, pt_stats *stats,
                   float **targets) {
   Batch &B = c->batch;
   if (!B.fork) cuda_check(cudaEventCreateWithFlags(&B.fork, cudaEventDisableTiming), "cudaEventCreate");
-  if ((int)B.slots.size() < n) B.slots.resize(n);
-  std::vector<DeviceJob> dj(n);
-  std::vector<Scene *> scenes(n);
-  std::vector<long long> total(n);
-  std::vector<int> wave(n);
+  // ---- groups
+  std::vector<Group> groups;
+  std::map<std::pair<int, int>, int> gidx;
   for (int k = 0; k < n; ++k) {
     const pt_job_desc &j = jobs[k];
     validate_job(j);
-    scenes[k] = c->scene(j.scene);
-    dj[k] = c->device_job(j, scenes[k]);
-    const long long npix = (long long)j.width * j.height;
-    const int e = j.spp_end ? j.spp_end : j.spp_x * j.spp_y;
-    total[k] = npix * (e - j.spp_begin);
-    int w = c->batch_wave_cap;
-    if (npix <= w) w = (int)((w / npix) * npix);
-    if ((long long)w > total[k]) w = (int)total[k];
-    wave[k] = w;
-    BatchSlot &s = B.slots[k];
-    s.ensure(w, j.light_samples_x * j.light_samples_y, (size_t)npix * 3, j.spp_x * j.spp_y);
-    std::vector<float2> off = make_offsets(j);
-    cuda_check(cudaMemcpyAsync(s.offsets, off.data(), off.size() * sizeof(float2), cudaMemcpyHostToDevice,
+    c->scene(j.scene);
+    const int ln = j.light_samples_x * j.light_samples_y;
+    auto key = std::make_pair(j.scene, ln);
+    auto it = gidx.find(key);
+    if (it == gidx.end()) {
+      it = gidx.emplace(key, (int)groups.size()).first;
+      groups.push_back(Group{j.scene, ln, {}, {}, 0, 0, {}, 0});
+    }
+    groups[it->second].members.push_back(k);
+  }
+  if ((int)B.slots.size() < (int)groups.size()) B.slots.resize(groups.size());
+  // ---- tables
+  for (size_t gi = 0; gi < groups.size(); ++gi) {
+    Group &G = groups[gi];
+    Scene *S = c->scene(G.scene);
+    MergedJobs &M = G.M;
+    M.LN = G.ln;
+    M.start.push_back(0);
+    size_t n_off = 0, film_floats = 0;
+    for (int k : G.members) {
+      const pt_job_desc &j = jobs[k];
+      const long long npix = (long long)j.width * j.height;
+      const int e = j.spp_end ? j.spp_end : j.spp_x * j.spp_y;
+      M.start.push_back(M.start.back() + npix * (e - j.spp_begin));
+      M.bounces = std::max(M.bounces, j.max_depth + (j.estimator == PT_EST_NEE_MIS ? 1 : 0));
+      n_off += (size_t)j.spp_x * j.spp_y;
+      G.film_off.push_back(film_floats);
+      film_floats += (size_t)npix * 3;
+    }
+    G.total = M.start.back();
+    G.film_floats = film_floats;
+    G.wave = (int)std::min<long long>(c->batch_wave_cap, G.total);
+    BatchSlot &slot = B.slots[gi];
+    slot.ensure(G.wave, G.ln, (int)G.members.size(), n_off, targets ? 1 : film_floats);
+    std::vector<float2> offs;
+    offs.reserve(n_off);
+    for (size_t m = 0; m < G.members.size(); ++m) {
+      const pt_job_desc &j = jobs[G.members[m]];
+      DeviceJob dj = c->device_job(j, S);
+      dj.job.offsets = slot.offsets + offs.size();
+      std::vector<float2> o = make_offsets(j);
+      offs.insert(offs.end(), o.begin(), o.end());
+      M.jobs.push_back(dj);
+      M.films.push_back(targets ? targets[G.members[m]] : slot.films + G.film_off[m]);
+    }
+    cuda_check(cudaMemcpyAsync(slot.offsets, offs.data(), offs.size() * sizeof(float2), cudaMemcpyHostToDevice,
                                c->stream),
                "upload offsets");
-    dj[k].job.offsets = s.offsets;
+    cuda_check(cudaMemcpyAsync(slot.d_jobs, M.jobs.data(), sizeof(DeviceJob) * M.jobs.size(),
+                               cudaMemcpyHostToDevice, c->stream),
+               "upload job table");
+    cuda_check(cudaMemcpyAsync(slot.d_start, M.start.data(), sizeof(long long) * M.start.size(),
+                               cudaMemcpyHostToDevice, c->stream),
+               "upload job starts");
+    M.T = JobTable{slot.d_jobs, slot.d_start, (int)G.members.size()};
   }
   cuda_check(cudaStreamSynchronize(c->stream), "batch set-up");
+  // ---- graph
   const std::string sig = signature(jobs, n, c->cfg, c->batch_wave_cap, targets);
   if (!B.exec || sig != B.sig) {
     cudaGraph_t graph = nullptr;
     cuda_check(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal), "begin capture");
     cudaEventRecord(B.fork, c->stream);
-    for (int k = 0; k < n; ++k) {
-      BatchSlot &s = B.slots[k];
-      const pt_job_desc &j = jobs[k];
-      cudaStreamWaitEvent(s.stream, B.fork, 0);
-      cudaMemsetAsync(s.Q.stats, 0, 64, s.stream);
-      // targets: device films the samples are added onto; else the slot film
-      float *dst = targets ? targets[k] : s.film;
-      if (!targets) cudaMemsetAsync(s.film, 0, sizeof(float) * (size_t)j.width * j.height * 3, s.stream);
+    for (size_t gi = 0; gi < groups.size(); ++gi) {
+      Group &G = groups[gi];
+      BatchSlot &slot = B.slots[gi];
+      Scene *S = c->scene(G.scene);
+      cudaStreamWaitEvent(slot.stream, B.fork, 0);
+      cudaMemsetAsync(slot.Q.stats, 0, 64, slot.stream);
+      if (!targets) cudaMemsetAsync(slot.films, 0, sizeof(float) * G.film_floats, slot.stream);
       LaunchCfg lc = c->cfg;
-      lc.family_mask = scenes[k]->family_mask;
-      for (long long g0 = 0; g0 < total[k]; g0 += wave[k]) {
-        int cnt = (int)std::min<long long>(wave[k], total[k] - g0);
-        launch_wave(scenes[k]->view, dj[k], s.Q, g0, cnt, dst, lc, s.stream, nullptr);
+      lc.family_mask = S->family_mask;
+      for (long long g0 = 0; g0 < G.total; g0 += G.wave) {
+        const int cnt = (int)std::min<long long>(G.wave, G.total - g0);
+        launch_wave_multi(S->view, G.M, slot.Q, g0, cnt, lc, slot.stream, nullptr);
       }
-      cudaEventRecord(s.done, s.stream);
-      cudaStreamWaitEvent(c->stream, s.done, 0);
+      cudaEventRecord(slot.done, slot.stream);
+      cudaStreamWaitEvent(c->stream, slot.done, 0);
     }
     cudaError_t ce = cudaStreamEndCapture(c->stream, &graph);
     cuda_check(ce, "end capture");
-    // Same topology (e.g. the next pass of the same requests, only sample
-    // ranges and films changed): update the executable graph's parameters in
-    // place; otherwise instantiate anew.
+    // Same topology (e.g. the server's next pass of the same requests: only
+    // sample ranges and target films changed): update the executable graph's
+    // parameters in place; otherwise instantiate anew.
     bool updated = false;
     if (B.exec) {
       cudaGraphExecUpdateResultInfo info;
@@ -196,26 +268,32 @@ void render_batch(Context *c, const pt_job_desc *jobs, int n, float **films, pt_
   cudaEventElapsedTime(&ms, e0, e1);
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
+  // ---- results
   pt_stats tot;
   std::memset(&tot, 0, sizeof tot);
-  for (int k = 0; k < n; ++k) {
-    BatchSlot &s = B.slots[k];
+  for (size_t gi = 0; gi < groups.size(); ++gi) {
+    Group &G = groups[gi];
+    BatchSlot &slot = B.slots[gi];
     int herr = 0;
-    cuda_check(cudaMemcpy(&herr, s.Q.err, sizeof(int), cudaMemcpyDeviceToHost), "read err");
+    cuda_check(cudaMemcpy(&herr, slot.Q.err, sizeof(int), cudaMemcpyDeviceToHost), "read err");
     if (herr) {
-      cudaMemset(s.Q.err, 0, sizeof(int));
-      fail(PT_ERR_DEVICE, "device traversal error flag in batch job " + std::to_string(k));
+      cudaMemset(slot.Q.err, 0, sizeof(int));
+      fail(PT_ERR_DEVICE, "device traversal error flag in batch group " + std::to_string(gi));
     }
     unsigned long long h[4];
-    cuda_check(cudaMemcpy(h, s.Q.stats, sizeof h, cudaMemcpyDeviceToHost), "read stats");
+    cuda_check(cudaMemcpy(h, slot.Q.stats, sizeof h, cudaMemcpyDeviceToHost), "read stats");
     tot.paths += h[0];
     tot.segments += h[1];
     tot.rays += h[2];
     tot.shadow_rays += h[3];
-    const pt_job_desc &j = jobs[k];
-    if (!targets && films && films[k]) {
+    if (targets || !films) continue;
+    for (size_t m = 0; m < G.members.size(); ++m) {
+      const int k = G.members[m];
+      if (!films[k]) continue;
+      const pt_job_desc &j = jobs[k];
       const size_t nf = (size_t)j.width * j.height * 3;
-      cuda_check(cudaMemcpy(films[k], s.film, nf * sizeof(float), cudaMemcpyDeviceToHost), "film d2h");
+      cuda_check(cudaMemcpy(films[k], slot.films + G.film_off[m], nf * sizeof(float), cudaMemcpyDeviceToHost),
+                 "film d2h");
       const int e = j.spp_end ? j.spp_end : j.spp_x * j.spp_y;
       const float inv = 1.f / (float)(e - j.spp_begin);
       for (size_t i = 0; i < nf; ++i) films[k][i] *= inv;
@@ -227,8 +305,9 @@ void render_batch(Context *c, const pt_job_desc *jobs, int n, float **films, pt_
 }
 
 // Autotuner: renders the batch under candidate launch configurations
-// (wave capacity per job, material sorting, blocks per SM of the traversal
-// and shade kernels), keeps the fastest in the context and reports it.
+// (merged wave capacity per group, material sorting, blocks per SM of the
+// traversal and shade kernels), keeps the fastest in the context and
+// reports it.
 void autotune(Context *c, const pt_job_desc *jobs, int n, pt_tuning *out) {
   const LaunchCfg base = c->cfg;
   const int base_wave = c->batch_wave_cap;

@@ -195,8 +195,9 @@ struct BNode {
 
 struct Builder {
   const pt_scene_desc *d;
-  float sweep[3] = {0.f, 0.f, 0.f};  // motion of the object being built over [0, shutter_max]
+  std::vector<int> obj_motion;   // per object: motion index + 1 (0: static)
   std::vector<BNode> nodes;
+  std::vector<int> inst_motion;  // per node: motion index + 1 if it roots a moving object's subtree
   std::vector<int> leaf_prims;    // global prim ids in leaf order
   std::vector<int> tri_base;      // first global prim id of each mesh
   int n_tris = 0;
@@ -225,7 +226,7 @@ struct Builder {
     }
     int me = (int)nodes.size();
     nodes.push_back(BNode());
-    nodes[me].box = swept(pb);
+    nodes[me].box = pb;
     int count = (int)ids.size();
     if (count <= 4) {
       nodes[me].first = (int)leaf_prims.size();
@@ -284,32 +285,40 @@ struct Builder {
     return b;
   }
 
-  // A moving object's boxes cover its whole motion: box | box + sweep.
-  Box swept(const Box &b) const {
-    Box r = b;
+  // Motion blur: a moving object's subtree keeps its boxes at rest (it is
+  // traversed in the object's frame at the ray's time); only its root box,
+  // seen from the world, covers the motion over [0, shutter_max].
+  void sweep_root(int root, int o) {
+    if (!obj_motion[o]) return;
+    const float *v = d->objects[o].velocity;
+    Box &b = nodes[root].box;
     for (int a = 0; a < 3; ++a) {
-      r.lo[a] = std::min(b.lo[a], b.lo[a] + sweep[a]);
-      r.hi[a] = std::max(b.hi[a], b.hi[a] + sweep[a]);
+      const float s = v[a] * d->shutter_max;
+      b.lo[a] = std::min(b.lo[a], b.lo[a] + s);
+      b.hi[a] = std::max(b.hi[a], b.hi[a] + s);
     }
-    return r;
+    if (nodes[root].left >= 0) inst_motion[root] = obj_motion[o];
   }
 
   int object_subtree(int o) {
     const pt_object_desc &od = d->objects[o];
-    for (int a = 0; a < 3; ++a) sweep[a] = od.velocity[a] * std::max(0.f, d->shutter_max);
+    int me;
     if (od.kind == PT_OBJ_MESH) {
       const pt_mesh_desc &m = d->meshes[od.index];
       std::vector<int> ids(m.n_triangles);
       std::iota(ids.begin(), ids.end(), 0);
-      return build_mesh(od.index, ids);
+      me = build_mesh(od.index, ids);
+    } else {
+      me = (int)nodes.size();
+      nodes.push_back(BNode());
+      nodes[me].box = object_box(o);
+      nodes[me].first = (int)leaf_prims.size();
+      nodes[me].count = 1;
+      int prim = od.kind == PT_OBJ_QUAD ? n_tris + od.index : n_tris + d->n_quads + od.index;
+      leaf_prims.push_back(prim);
     }
-    int me = (int)nodes.size();
-    nodes.push_back(BNode());
-    nodes[me].box = swept(object_box(o));
-    nodes[me].first = (int)leaf_prims.size();
-    nodes[me].count = 1;
-    int prim = od.kind == PT_OBJ_QUAD ? n_tris + od.index : n_tris + d->n_quads + od.index;
-    leaf_prims.push_back(prim);
+    inst_motion.resize(nodes.size(), 0);
+    sweep_root(me, o);
     return me;
   }
 
@@ -347,11 +356,21 @@ struct Builder {
 
 struct Bvh4Out {
   std::vector<Bvh4Node> nodes;
-  std::vector<int> leaf_order;  // leaf prims in item order
+  std::vector<int> node_motion;   // per node: motion index + 1 of the moving object it roots
+  std::vector<int> leaf_order;    // leaf prims in item order
+  std::vector<char> leaf_world;   // per item: tested from the world frame (not inside a moving subtree)
   int max_depth = 0;
 };
 
-static void collapse(const Builder &B, int bn, Bvh4Out &out, int depth, int me) {
+static int motion_of(const Builder &B, int bn) {
+  return bn < (int)B.inst_motion.size() ? B.inst_motion[bn] : 0;
+}
+
+// Collapses the binary tree under `bn` into BVH4 node `me`.  A moving
+// object's subtree root met from the world frame is never merged into a world
+// node: it becomes a child of its own (reference flagged PT_INST_BIT) whose
+// subtree is traversed in the object's frame.
+static void collapse(const Builder &B, int bn, Bvh4Out &out, int depth, int me, bool in_inst) {
   // gather up to 4 children by expanding the largest internal child
   std::vector<int> ch = {B.nodes[bn].left, B.nodes[bn].right};
   if (B.nodes[bn].left < 0) ch = {bn};  // a leaf as the root
@@ -360,7 +379,7 @@ static void collapse(const Builder &B, int bn, Bvh4Out &out, int depth, int me) 
     float ba = -1.f;
     for (size_t k = 0; k < ch.size(); ++k) {
       const BNode &c = B.nodes[ch[k]];
-      if (c.left >= 0 && box_area(c.box) > ba) {
+      if (c.left >= 0 && (in_inst || !motion_of(B, ch[k])) && box_area(c.box) > ba) {
         ba = box_area(c.box);
         best = (int)k;
       }
@@ -390,13 +409,19 @@ static void collapse(const Builder &B, int bn, Bvh4Out &out, int depth, int me) 
     if (c.left < 0) {
       N.child[k] = (int)out.leaf_order.size();
       N.count[k] = c.count;
-      for (int t = 0; t < c.count; ++t) out.leaf_order.push_back(B.leaf_prims[c.first + t]);
+      for (int t = 0; t < c.count; ++t) {
+        out.leaf_order.push_back(B.leaf_prims[c.first + t]);
+        out.leaf_world.push_back(in_inst ? 0 : 1);
+      }
     } else {
       int idx = (int)out.nodes.size();
       out.nodes.push_back(Bvh4Node());
-      out.nodes[me].child[k] = idx;
+      out.node_motion.push_back(0);
+      const bool enter = !in_inst && motion_of(B, ch[k]);
+      out.nodes[me].child[k] = enter ? (idx | PT_INST_BIT) : idx;
       out.nodes[me].count[k] = 0;
-      collapse(B, ch[k], out, depth + 1, idx);
+      if (enter) out.node_motion[idx] = motion_of(B, ch[k]);
+      collapse(B, ch[k], out, depth + 1, idx, in_inst || enter);
     }
   }
 }
@@ -447,6 +472,7 @@ std::unique_ptr<Scene> build_scene(const pt_scene_desc *d, cudaStream_t st) {
   // primitives (a mesh shared by several objects takes the last one's)
   std::vector<float4> motion;
   std::vector<int> prim_motion(n_prims, 0);
+  B.obj_motion.assign(d->n_objects, 0);
   for (int o = 0; o < d->n_objects; ++o) {
     const pt_object_desc &od = d->objects[o];
     const float *v = od.velocity;
@@ -455,6 +481,7 @@ std::unique_ptr<Scene> build_scene(const pt_scene_desc *d, cudaStream_t st) {
     if (v[0] == 0.f && v[1] == 0.f && v[2] == 0.f) continue;
     motion.push_back(make_float4(v[0], v[1], v[2], 0.f));
     const int m = (int)motion.size();
+    B.obj_motion[o] = m;
     if (od.kind == PT_OBJ_MESH) {
       for (int t = 0; t < d->meshes[od.index].n_triangles; ++t) prim_motion[B.tri_base[od.index] + t] = m;
     } else {
@@ -466,10 +493,33 @@ std::unique_ptr<Scene> build_scene(const pt_scene_desc *d, cudaStream_t st) {
   std::srand(1);  // the reference's BVH build draws from rand() with its default seed
   int root = B.build_top(0, d->n_objects);
 
+  B.inst_motion.resize(B.nodes.size(), 0);
   Bvh4Out out;
   out.nodes.push_back(Bvh4Node());
-  collapse(B, root, out, 0, 0);
-  if (3 * out.max_depth + 1 > PT_STACK)
+  out.node_motion.push_back(0);
+  if (motion_of(B, root)) {
+    // the whole scene is one moving object: a world node above its subtree
+    Bvh4Node &R = out.nodes[0];
+    for (int k = 0; k < 4; ++k) {
+      R.lo_x[k] = R.lo_y[k] = R.lo_z[k] = INFINITY;
+      R.hi_x[k] = R.hi_y[k] = R.hi_z[k] = -INFINITY;
+      R.child[k] = 0;
+      R.count[k] = -1;
+    }
+    const Box &b = B.nodes[root].box;
+    R.lo_x[0] = b.lo[0]; R.lo_y[0] = b.lo[1]; R.lo_z[0] = b.lo[2];
+    R.hi_x[0] = b.hi[0]; R.hi_y[0] = b.hi[1]; R.hi_z[0] = b.hi[2];
+    R.child[0] = 1 | PT_INST_BIT;
+    R.count[0] = 0;
+    out.nodes.push_back(Bvh4Node());
+    out.node_motion.push_back(motion_of(B, root));
+    collapse(B, root, out, 1, 1, true);
+  } else {
+    collapse(B, root, out, 0, 0, false);
+  }
+  if (out.nodes.size() >= (size_t)PT_INST_BIT) fail(PT_ERR_TOO_LARGE, "too many BVH nodes");
+  if (out.leaf_order.size() >= ((size_t)1 << 28) - 8) fail(PT_ERR_TOO_LARGE, "too many leaf items");
+  if (3 * out.max_depth + 2 > PT_STACK)
     fail(PT_ERR_TOO_LARGE, "BVH deeper than the traversal stack (" + std::to_string(out.max_depth) + ")");
 
   // leaf items and shading records
@@ -487,7 +537,9 @@ std::unique_ptr<Scene> build_scene(const pt_scene_desc *d, cudaStream_t st) {
     Item &it = items[k];
     std::memset(&it, 0, sizeof it);
     it.a[3] = u2f((uint32_t)prim);
-    it.c[3] = u2f((uint32_t)prim_motion[prim]);
+    // a moving primitive tested from the world frame moves itself; inside a
+    // moving object's subtree the ray is already in the object's frame
+    it.c[3] = u2f((uint32_t)(out.leaf_world[k] ? prim_motion[prim] : 0));
     prim_item[prim] = (int)k;
     if (prim < B.n_tris) {
       const pt_mesh_desc &m = d->meshes[prim_mesh[prim]];
@@ -718,6 +770,7 @@ std::unique_ptr<Scene> build_scene(const pt_scene_desc *d, cudaStream_t st) {
   }
   if (!motion.empty()) {
     V.motion = dupload(motion, S->owned, st);
+    V.node_motion = dupload(out.node_motion, S->owned, st);
     V.has_motion = 1;
     S->shutter_max = d->shutter_max;
   }
@@ -758,6 +811,7 @@ Context::Context(int dev) : device(dev) {
   num_sms = prop.multiProcessorCount;
   halton = make_halton_tables();
   upload_halton_tables(halton, stream);
+  upload_halton_tables_multi(halton, stream);
   kernel_attributes(&kinfo);
   cfg.trace_blocks = num_sms * std::max(1, kinfo.trace_blocks_per_sm);
   cfg.shade_blocks = num_sms * std::max(1, kinfo.shade_blocks_per_sm);
@@ -820,6 +874,7 @@ void Context::ensure_queues(int cap, int ln) {
   Q.order = (int *)alloc(c * 4);
   Q.bins = (int *)alloc(sizeof(int) * 2 * PT_SORT_BINS);
   Q.seg = (int *)alloc(sizeof(int) * (PT_SORT_BINS + 1));
+  Q.job = (int *)alloc(c * 4);
   Q.err = d_err;
   q_cap = cap;
   q_ln = ln;
@@ -902,13 +957,29 @@ void validate_job(const pt_job_desc &j) {
   if (j.camera.aperture == 0.f) fail(PT_ERR_INVALID, "camera aperture must be non-zero");
   if (!(j.camera.shutter >= 0.f) || !std::isfinite(j.camera.shutter))
     fail(PT_ERR_INVALID, "camera shutter must be finite and >= 0");
+  if (j.full_width > 0 || j.full_height > 0) {
+    if (j.crop_x < 0 || j.crop_y < 0 || (int64_t)j.crop_x + j.width > j.full_width ||
+        (int64_t)j.crop_y + j.height > j.full_height)
+      fail(PT_ERR_INVALID, "window outside the frame");
+  } else if (j.crop_x != 0 || j.crop_y != 0) {
+    fail(PT_ERR_INVALID, "window origin without a frame size");
+  }
+}
+
+void set_window(JobView &v, const pt_job_desc &j) {
+  v.width = j.width;
+  v.height = j.height;
+  const bool win = j.full_width > 0 || j.full_height > 0;
+  v.crop_x = win ? j.crop_x : 0;
+  v.crop_y = win ? j.crop_y : 0;
+  v.full_w = win ? j.full_width : j.width;
+  v.full_h = win ? j.full_height : j.height;
 }
 
 DeviceJob Context::device_job(const pt_job_desc &j, Scene *S) {
   DeviceJob J;
   std::memset(&J, 0, sizeof J);
-  J.job.width = j.width;
-  J.job.height = j.height;
+  set_window(J.job, j);
   J.job.spp_x = j.spp_x;
   J.job.spp_y = j.spp_y;
   J.job.spp = j.spp_x * j.spp_y;

@@ -27,6 +27,7 @@ std::vector<uint16_t> make_digit_permutations(const HaltonTables &T, uint32_t se
 MatRec derive_material(const pt_material_desc &m);
 CameraView make_camera(const pt_camera_desc &c);
 std::vector<float2> make_offsets(const pt_job_desc &j);
+void set_window(JobView &v, const pt_job_desc &j);
 void validate_job(const pt_job_desc &j);
 
 // A flattened scene resident in HBM.
@@ -48,22 +49,27 @@ struct Scene {
 
 std::unique_ptr<Scene> build_scene(const pt_scene_desc *d, cudaStream_t st);
 
-// Per-job device buffers of a batch, reused across batched renders.
+// Device buffers of one merged group of a batch (the jobs of one scene with
+// the same light-sample count), reused across batched renders.
 struct BatchSlot {
   Queues Q{};
   std::vector<void *> mem;
   int cap = 0, ln = 0;
-  float2 *offsets = nullptr;
-  int offsets_cap = 0;
-  float *film = nullptr;
-  size_t film_cap = 0;
+  DeviceJob *d_jobs = nullptr;  // job table
+  long long *d_start = nullptr;
+  int jobs_cap = 0;
+  float2 *offsets = nullptr;    // the jobs' offset tables, concatenated
+  size_t offsets_cap = 0;
+  float *films = nullptr;       // the jobs' films (when no targets are given), concatenated
+  size_t films_cap = 0;
   cudaStream_t stream = nullptr;
   cudaEvent_t done = nullptr;
-  void ensure(int want_cap, int want_ln, size_t film_floats, int spp);
+  void ensure(int want_cap, int want_ln, int n_jobs, size_t n_offsets, size_t film_floats);
   void release();
 };
 
-// A batch: one graph branch per job, captured once per composition.
+// A batch: one graph branch per merged group, captured per composition and
+// updated in place when only parameters change.
 struct Batch {
   std::vector<BatchSlot> slots;
   cudaGraphExec_t exec = nullptr;

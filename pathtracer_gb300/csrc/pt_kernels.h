@@ -24,6 +24,14 @@ struct DeviceJob {
   const uint16_t *perm;  // PermuteDigits tables for job.sampler_seed
 };
 
+// Jobs of a merged wave (batched and served forms): the merged path index
+// g in [start[k], start[k+1]) is path g - start[k] of job k.
+struct JobTable {
+  const DeviceJob *jobs;   // [n]
+  const long long *start;  // [n + 1], start[0] = 0
+  int n;
+};
+
 // Work queues of one context, sized for `cap` paths per wave (SoA in HBM).
 struct Queues {
   int cap;
@@ -39,6 +47,7 @@ struct Queues {
   int *counts;        // [0],[1] ray queues, [2] shadow queue, [3] [4] fetch counters
   unsigned long long *stats;  // [0] paths [1] segments [2] rays [3] shadow rays
   int *err;           // device error flag (stack overflow / iteration cap)
+  int *job;           // [cap] merged waves: job index of the path in each slot
   int *sort_key, *order, *bins;
   int *seg;           // [PT_SORT_BINS + 1] segment bounds of the sorted order
 };
@@ -95,7 +104,39 @@ void launch_bsdf_sample(const MatRec *m, int n, const float *wo, const float *nr
                         float *wi, float *att, float *pdf, uint32_t *type, cudaStream_t st);
 void launch_wave(const SceneView &S, const DeviceJob &J, const Queues &Q, long long g0, int n,
                  float *film, const LaunchCfg &cfg, cudaStream_t st, Profiler *prof);
+// Job-independent stages (pt_kernels.cu), also used by merged waves.
+void launch_sort(const SceneView &S, const Queues &Q, int qsel, const LaunchCfg &cfg, cudaStream_t st);
+void launch_shadow(const SceneView &S, const Queues &Q, int LN, const LaunchCfg &cfg, cudaStream_t st);
+// Adds paths [lo, lo + cnt) of job J (held in wave slots slot0..) to its
+// film, per pixel in sample order.
+void launch_film(const DeviceJob &J, const Queues &Q, long long lo, int cnt, long long slot0, float *film,
+                 const LaunchCfg &cfg, cudaStream_t st);
+
+// A merged wave over the jobs of one scene (pt_kernels_multi.cu): device job
+// table + host copies for the per-job film stage.
+struct MergedJobs {
+  JobTable T;                    // device pointers
+  std::vector<DeviceJob> jobs;   // host copies
+  std::vector<long long> start;  // host copy, n + 1 entries
+  std::vector<float *> films;    // device film of each job (samples are added)
+  int bounces = 0;               // max over the jobs of max_depth (+1 with MIS)
+  int LN = 1;                    // light samples per vertex (equal for all jobs)
+};
+void launch_wave_multi(const SceneView &S, const MergedJobs &M, const Queues &Q, long long g0, int n,
+                       const LaunchCfg &cfg, cudaStream_t st, Profiler *prof);
+void upload_halton_tables_multi(const HaltonTables &T, cudaStream_t st);
 void launch_tonemap(const float *film, int W, int H, float gamma, uint8_t *out, cudaStream_t st);
+
+// Serving: RMSE estimates from half films (see k_film_rmse) and the final
+// mean image.  partials holds PT_RMSE_BLOCKS doubles per pair.
+#define PT_RMSE_BLOCKS 64
+struct FilmPair {
+  const float *a, *b;
+  double ia, ib;  // 1 / samples in a, b
+  long long n;    // floats per film
+};
+void launch_film_rmse(const FilmPair *pairs, int npairs, double *partials, double *out, cudaStream_t st);
+void launch_film_combine(float *a, const float *b, float inv, long long n, cudaStream_t st);
 void kernel_attributes(KernelInfo *info);
 
 }  // namespace pt

@@ -80,8 +80,8 @@ void render_device_noalloc(Context *c, const pt_job_desc &j, float *d_film, pt_s
   uint16_t *d_perm = (uint16_t *)carve(perm.size() * sizeof(uint16_t) + 16);
   const int LN = j.light_samples_x * j.light_samples_y;
   off = align_up(off, 256);
-  const size_t per_path = 16 * 8 + 2 * 16 * (size_t)LN + (size_t)LN + 2 * 4;
-  const size_t avail = PT_NOALLOC_SCRATCH_BYTES - off - 17 * 256;  // alignment slack of 17 arrays
+  const size_t per_path = 16 * 8 + 2 * 16 * (size_t)LN + (size_t)LN + 3 * 4;
+  const size_t avail = PT_NOALLOC_SCRATCH_BYTES - off - 18 * 256;  // alignment slack of 18 arrays
   const int cap = (int)std::min<size_t>(avail / per_path, (size_t)1 << 30);
   if (cap < 1024) fail(PT_ERR_TOO_LARGE, "pt_render_device_noalloc: scratch too small for the light samples");
   const size_t c4 = (size_t)cap * 16;
@@ -99,13 +99,13 @@ void render_device_noalloc(Context *c, const pt_job_desc &j, float *d_film, pt_s
   Q.sh_vis = (uint8_t *)carve((size_t)cap * LN);
   Q.sort_key = (int *)carve((size_t)cap * 4);
   Q.order = (int *)carve((size_t)cap * 4);
+  Q.job = (int *)carve((size_t)cap * 4);
   if (off > PT_NOALLOC_SCRATCH_BYTES) fail(PT_ERR_TOO_LARGE, "pt_render_device_noalloc: scratch layout overflow");
 
   // ---- job constants (as Context::device_job, with the tables in scratch)
   DeviceJob J;
   std::memset(&J, 0, sizeof J);
-  J.job.width = j.width;
-  J.job.height = j.height;
+  set_window(J.job, j);
   J.job.spp_x = j.spp_x;
   J.job.spp_y = j.spp_y;
   J.job.spp = spp;

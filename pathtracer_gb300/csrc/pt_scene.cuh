@@ -113,8 +113,16 @@ struct SceneView {
   // motion blur (extension): velocity per moving object; items, shading
   // records and lights of a moving object carry its index + 1
   const float4 *motion;
+  const int32_t *node_motion;  // per BVH4 node: motion index + 1 of the moving object it roots
   int32_t has_motion;
 };
+
+// Child references of a BVH4 node entering a moving object's subtree carry
+// PT_INST_BIT; the traversal then pushes PT_FRAME_END (never a leaf
+// reference: items < 2^28 - 8) and continues in the object's frame until it
+// pops it.
+#define PT_INST_BIT (1 << 30)
+#define PT_FRAME_END ((int32_t)0x80000000)
 
 // Camera constants of PerspectiveCamera (camera.cpp:7-35).
 struct CameraView {
@@ -128,7 +136,9 @@ struct CameraView {
 };
 
 struct JobView {
-  int32_t width, height;
+  int32_t width, height;  // the rendered window (the film)
+  int32_t crop_x, crop_y; // window origin in the frame
+  int32_t full_w, full_h; // the frame: camera and sample streams
   int32_t spp;            // spp_x * spp_y
   int32_t spp_begin;      // first grid sample of this render
   int32_t spp_x, spp_y;

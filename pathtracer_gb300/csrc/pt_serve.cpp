@@ -36,6 +36,7 @@ struct Request {
   std::chrono::steady_clock::time_point t_submit, t_done;
   std::vector<float> result;
   std::string error;
+  double last_rmse = INFINITY;  // latest estimate of the mean image's RMSE
 };
 
 struct Server {
@@ -47,6 +48,26 @@ struct Server {
   std::deque<int64_t> queue;
   std::vector<int64_t> active;
   int64_t used = 0;
+  // device scratch of the RMSE estimates: pairs, partial sums, results
+  FilmPair *d_pairs = nullptr;
+  double *d_partials = nullptr, *d_out = nullptr;
+  int pairs_cap = 0;
+  void ensure_pairs(int n) {
+    if (n <= pairs_cap) return;
+    free_pairs();
+    cuda_check(cudaMalloc(&d_pairs, sizeof(FilmPair) * n), "cudaMalloc(rmse pairs)");
+    cuda_check(cudaMalloc(&d_partials, sizeof(double) * PT_RMSE_BLOCKS * n), "cudaMalloc(rmse partials)");
+    cuda_check(cudaMalloc(&d_out, sizeof(double) * n), "cudaMalloc(rmse out)");
+    pairs_cap = n;
+  }
+  void free_pairs() {
+    if (d_pairs) cudaFree(d_pairs);
+    if (d_partials) cudaFree(d_partials);
+    if (d_out) cudaFree(d_out);
+    d_pairs = nullptr;
+    d_partials = d_out = nullptr;
+    pairs_cap = 0;
+  }
 };
 
 static void release_films(Request &r, Server &s) {
@@ -55,25 +76,6 @@ static void release_films(Request &r, Server &s) {
   r.film_a = r.film_b = nullptr;
   s.used -= (int64_t)r.bytes;
   r.bytes = 0;
-}
-
-// RMSE of the mean image estimated from two independent halves:
-// E|A - B|^2 / 4 = var(mean of all samples) for equal halves.
-static double estimate_rmse(const Request &r, Server &s, std::vector<float> &ha, std::vector<float> &hb) {
-  if (r.spp_a == 0 || r.spp_b == 0) return INFINITY;
-  const size_t nf = (size_t)r.desc.job.width * r.desc.job.height * 3;
-  ha.resize(nf);
-  hb.resize(nf);
-  cudaMemcpyAsync(ha.data(), r.film_a, nf * 4, cudaMemcpyDeviceToHost, s.ctx->stream);
-  cudaMemcpyAsync(hb.data(), r.film_b, nf * 4, cudaMemcpyDeviceToHost, s.ctx->stream);
-  cudaStreamSynchronize(s.ctx->stream);
-  double acc = 0.0;
-  const double ia = 1.0 / r.spp_a, ib = 1.0 / r.spp_b;
-  for (size_t i = 0; i < nf; ++i) {
-    double d = ha[i] * ia - hb[i] * ib;
-    if (std::isfinite(d)) acc += d * d;
-  }
-  return 0.5 * std::sqrt(acc / (double)nf);
 }
 
 }  // namespace pt
@@ -131,6 +133,7 @@ int pt_server_destroy(void *server) {
   Server *s = static_cast<Server *>(server);
   cudaStreamSynchronize(s->ctx->stream);
   for (auto &kv : s->reqs) release_films(kv.second, *s);
+  s->free_pairs();
   delete s;
   return PT_OK;
 }
@@ -185,7 +188,6 @@ int pt_server_step(void *server, int32_t *active_out) {
   }
   // one pass over every active request: a batch with one job per request
   // (its next spp_per_pass samples), rendered as one graph launch
-  std::vector<float> ha, hb;
   std::vector<int64_t> still, live;
   std::vector<pt_job_desc> jobs;
   std::vector<float *> targets;
@@ -223,31 +225,63 @@ int pt_server_step(void *server, int32_t *active_out) {
       live.clear();
     }
   }
+  // bookkeeping; RMSE estimates of the requests that have a target, on the
+  // device in one launch (the mean image's RMSE from the two half films:
+  // E|A - B|^2 / 4 = var(mean of all samples) for equal halves)
+  std::vector<FilmPair> pairs;
+  std::vector<int> pair_of(live.size(), -1);
+  for (size_t q = 0; q < live.size(); ++q) {
+    Request &r = s->reqs[live[q]];
+    const pt_job_desc &j = jobs[q];
+    (to_a_v[q] ? r.spp_a : r.spp_b) += ends[q] - j.spp_begin;
+    r.spp_done = ends[q];
+    const int cap = std::min(r.desc.spp_cap, j.spp_x * j.spp_y);
+    if (r.spp_done < cap && r.desc.target_rmse > 0.f && r.spp_a > 0 && r.spp_b > 0) {
+      pair_of[q] = (int)pairs.size();
+      pairs.push_back(FilmPair{r.film_a, r.film_b, 1.0 / r.spp_a, 1.0 / r.spp_b, (long long)j.width * j.height * 3});
+    }
+  }
+  std::vector<double> est(pairs.size());
+  try {
+    if (!pairs.empty()) {
+      s->ensure_pairs((int)pairs.size());
+      cuda_check(cudaMemcpyAsync(s->d_pairs, pairs.data(), sizeof(FilmPair) * pairs.size(), cudaMemcpyHostToDevice,
+                                 c->stream),
+                 "upload rmse pairs");
+      launch_film_rmse(s->d_pairs, (int)pairs.size(), s->d_partials, s->d_out, c->stream);
+      cuda_check(cudaMemcpyAsync(est.data(), s->d_out, sizeof(double) * pairs.size(), cudaMemcpyDeviceToHost,
+                                 c->stream),
+                 "read rmse");
+      cuda_check(cudaStreamSynchronize(c->stream), "rmse estimate");
+    }
+  } catch (const std::exception &ex) {
+    for (int64_t id : live) {
+      Request &r = s->reqs[id];
+      r.state = 4;
+      r.error = ex.what();
+      release_films(r, *s);
+    }
+    live.clear();
+  }
   for (size_t q = 0; q < live.size(); ++q) {
     const int64_t id = live[q];
     Request &r = s->reqs[id];
     const pt_job_desc &j = jobs[q];
-    const int spp_total = j.spp_x * j.spp_y;
-    const int cap = std::min(r.desc.spp_cap, spp_total);
-    const int e = ends[q];
-    (to_a_v[q] ? r.spp_a : r.spp_b) += e - j.spp_begin;
-    r.spp_done = e;
-    bool done = r.spp_done >= cap;
-    if (!done && r.desc.target_rmse > 0.f && r.spp_a > 0 && r.spp_b > 0) {
-      double est = estimate_rmse(r, *s, ha, hb);
-      if (est <= r.desc.target_rmse) done = true;
-    }
+    const int cap = std::min(r.desc.spp_cap, j.spp_x * j.spp_y);
+    r.last_rmse = pair_of[q] >= 0 ? est[pair_of[q]] : r.last_rmse;
+    bool done = r.spp_done >= cap || (pair_of[q] >= 0 && est[pair_of[q]] <= r.desc.target_rmse);
     if (done) {
-      const size_t nf = (size_t)j.width * j.height * 3;
-      ha.resize(nf);
-      hb.resize(nf);
-      cudaMemcpyAsync(ha.data(), r.film_a, nf * 4, cudaMemcpyDeviceToHost, c->stream);
-      cudaMemcpyAsync(hb.data(), r.film_b, nf * 4, cudaMemcpyDeviceToHost, c->stream);
-      cudaStreamSynchronize(c->stream);
-      r.result.resize(nf);
-      const float inv = 1.f / (float)r.spp_done;
-      for (size_t i = 0; i < nf; ++i) r.result[i] = (ha[i] + hb[i]) * inv;
-      r.state = 2;
+      const long long nf = (long long)j.width * j.height * 3;
+      r.result.resize((size_t)nf);
+      launch_film_combine(r.film_a, r.film_b, 1.f / (float)r.spp_done, nf, c->stream);
+      cudaMemcpyAsync(r.result.data(), r.film_a, (size_t)nf * 4, cudaMemcpyDeviceToHost, c->stream);
+      cudaError_t e = cudaStreamSynchronize(c->stream);
+      if (e != cudaSuccess) {
+        r.state = 4;
+        r.error = cudaGetErrorString(e);
+      } else {
+        r.state = 2;
+      }
       r.t_done = std::chrono::steady_clock::now();
       release_films(r, *s);
     } else {

@@ -150,7 +150,8 @@ __device__ __forceinline__ bool test_leaf(const SceneView &S, int32_t ref, V3 o_
 // visit or one leaf test each) so that a persistent warp can refill lanes
 // whose rays have finished while the others continue (trav_step).
 struct TravRay {
-  V3 o, d, dn, inv, oi;
+  V3 o, d, dn, inv, oi;  // o, oi: the current frame (world, or a moving object's)
+  V3 ow;                 // world origin
   float tmin, tmax;
   int32_t ref;  // node index (>= 0) or leaf reference (< 0) visited next
   int sp;       // stack depth
@@ -163,6 +164,7 @@ struct TravRay {
 __device__ __forceinline__ void trav_init(TravRay &R, V3 o, V3 d, float tmin, float tmax, float time = 0.f) {
   R.time = time;
   R.o = o;
+  R.ow = o;
   R.d = d;
   R.dn = xnormalize(d);
   R.inv = v3(1.f / d.x, 1.f / d.y, 1.f / d.z);
@@ -188,6 +190,26 @@ __device__ __forceinline__ bool trav_step(const SceneView &S, TravRay &R, int32_
   if (++R.iters > PT_TRAVERSAL_CAP) {
     *err = 2;
     return true;
+  }
+  if (R.ref == PT_FRAME_END) {
+    // leaving a moving object's subtree: back to the world frame
+    R.o = R.ow;
+    R.oi = v3(-R.o.x * R.inv.x, -R.o.y * R.inv.y, -R.o.z * R.inv.z);
+    if (R.sp == 0) return true;
+    R.ref = stack[(--R.sp) * stride];
+    return false;
+  }
+  if (R.ref >= 0 && (R.ref & PT_INST_BIT)) {
+    // entering a moving object's subtree: the ray in the object's frame at
+    // its time, until PT_FRAME_END comes off the stack
+    R.ref &= ~PT_INST_BIT;
+    if (R.sp + 1 > PT_STACK) {
+      *err = 1;
+      return true;
+    }
+    stack[(R.sp++) * stride] = PT_FRAME_END;
+    R.o = moved_origin(S, (uint32_t)__ldg(S.node_motion + R.ref), R.ow, R.time);
+    R.oi = v3(-R.o.x * R.inv.x, -R.o.y * R.inv.y, -R.o.z * R.inv.z);
   }
   if (R.ref >= 0) {
     const float4 *np = reinterpret_cast<const float4 *>(S.nodes + R.ref);

@@ -1,0 +1,697 @@
+// pt_wave.cuh -- device code of the wavefront stages whose work depends on
+// the job of each path: camera, closest-hit traversal (medium free flight)
+// and shading.  Included by pt_kernels.cu (single-job waves, MJ = false: the
+// job is a kernel argument) and by pt_kernels_multi.cu (merged waves of many
+// jobs, MJ = true: a job table in HBM and a job index per path); the two
+// translation units compile in parallel.  The estimator restates getRayColor
+// (maxdepth_nee.hpp:9-256) iteratively; see k_shade for the correspondence.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include "pt_bsdf.cuh"
+#include "pt_trace.cuh"
+#include "pt_kernels.h"
+
+namespace pt {
+
+// Halton tables in constant memory, one copy per translation unit (each
+// unit's upload function fills its own).
+static __constant__ HaltonTables c_halton;
+
+// ---------------------------------------------------------------- helpers
+__device__ __forceinline__ float4 ld4(const float4 *p) { return __ldg(p); }
+
+// Warp-aggregated slot allocation in a queue counter.
+__device__ __forceinline__ int warp_alloc(int *counter, bool want) {
+  unsigned mask = __ballot_sync(0xffffffffu, want);
+  if (!mask) return -1;
+  int lane = threadIdx.x & 31;
+  int leader = __ffs(mask) - 1;
+  int base = 0;
+  if (lane == leader) base = atomicAdd(counter, __popc(mask));
+  base = __shfl_sync(0xffffffffu, base, leader);
+  return want ? base + __popc(mask & ((1u << lane) - 1u)) : -1;
+}
+__device__ __forceinline__ void warp_count(unsigned long long *counter, int n) {
+  // sums n over the warp, one atomic per warp
+  for (int off = 16; off > 0; off >>= 1) n += __shfl_down_sync(0xffffffffu, n, off);
+  if ((threadIdx.x & 31) == 0 && n) atomicAdd(counter, (unsigned long long)n);
+}
+
+__device__ __forceinline__ float sampler_dim(const DeviceJob &J, int dim, uint32_t index,
+                                             uint64_t key, int pixel, int k) {
+  switch (J.job.sampler) {
+  case PT_SAMPLER_HALTON_NONE: return radical_inverse(c_halton, dim, index);
+  case PT_SAMPLER_HALTON_PERMUTE: return permuted_radical_inverse(c_halton, J.perm, dim, index);
+  case PT_SAMPLER_STRATIFIED: {
+    // Jittered strata over the pixel's spp samples, permuted per (pixel,
+    // dimension) with the reference's permutationElement.
+    const uint32_t S = (uint32_t)J.job.spp;
+    uint32_t h = (uint32_t)mix_bits(((uint64_t)pixel << 20) ^ ((uint64_t)dim << 8) ^ J.job.seed);
+    uint32_t stratum = permutation_element((uint32_t)k, S, h);
+    float jit = rand01(key, 4096u + (uint32_t)dim);
+    return fminf(((float)stratum + jit) / (float)S, 0x1.fffffep-1f);
+  }
+  default: return owen_radical_inverse(c_halton, dim, index);
+  }
+}
+
+// HDRITexture::getTexelColor(dir) (texture.hpp:105-115) with
+// ImageTexture's bilinear lookup (texture.cpp:112-143, including its clamp
+// of the cell index to width-2 / height-2 after the fraction is taken).
+__device__ inline V3 env_lookup(const EnvMap &E, V3 dir) {
+  V3 dn = normalize(dir);
+  float theta = acosf(-dn.y);
+  float phi = atan2f(-dn.z, dn.x) + (float)PT_PI;
+  float u = phi / (2.0f * (float)PT_PI), v = theta / (float)PT_PI;
+  const int W = E.width, H = E.height;
+  float fu = u * W, fv = v * H;
+  unsigned x = (unsigned)fu, y = (unsigned)fv;
+  float x1 = fu - (float)x, y1 = fv - (float)y;
+  x = min(x, (unsigned)(W - 2));
+  y = min(y, (unsigned)(H - 2));
+  float x2 = 1.0f - x1, y2 = 1.0f - y1;
+  float4 c1 = __ldg(E.texels + y * W + x), c2 = __ldg(E.texels + y * W + x + 1);
+  float4 c3 = __ldg(E.texels + (y + 1) * W + x), c4 = __ldg(E.texels + (y + 1) * W + x + 1);
+  V3 c12 = v3(c1.x, c1.y, c1.z) * x2 + v3(c2.x, c2.y, c2.z) * x1;
+  V3 c34 = v3(c3.x, c3.y, c3.z) * x2 + v3(c4.x, c4.y, c4.z) * x1;
+  return (c12 * y2 + c34 * y1) * E.intensity;
+}
+
+// Luminance alias-table sampling of the environment (extension).
+__device__ inline V3 env_alias_sample(const EnvMap &E, float u0, float u1, float u2, float &pdf) {
+  const int N = E.width * E.height;
+  float f = u0 * N;
+  int i = min((int)f, N - 1);
+  float r = f - (float)i;
+  int cell = (r < __ldg(E.alias_prob + i)) ? i : __ldg(E.alias_idx + i);
+  int cx = cell % E.width, cy = cell / E.width;
+  float u = (cx + u1) / E.width, v = (cy + u2) / E.height;
+  float theta = v * (float)PT_PI;
+  float st, ct, sp, cp;
+  sincospi_(v, &st, &ct);
+  sincospi_(2.f * u, &sp, &cp);
+  (void)theta;
+  V3 d = v3(-st * cp, -ct, st * sp);
+  pdf = (st > 0.f) ? __ldg(E.pdf + cell) * (float)N / (2.f * (float)(PT_PI * PT_PI) * st) : 0.f;
+  return d;
+}
+__device__ inline float env_alias_pdf(const EnvMap &E, V3 dir) {
+  V3 dn = normalize(dir);
+  float theta = acosf(fminf(fmaxf(-dn.y, -1.f), 1.f));
+  float phi = atan2f(-dn.z, dn.x) + (float)PT_PI;
+  float u = phi / (2.f * (float)PT_PI), v = theta / (float)PT_PI;
+  int cx = min((int)(u * E.width), E.width - 1), cy = min((int)(v * E.height), E.height - 1);
+  float st = sinf(theta);
+  if (st <= 0.f) return 0.f;
+  const int N = E.width * E.height;
+  return __ldg(E.pdf + cy * E.width + cx) * (float)N / (2.f * (float)(PT_PI * PT_PI) * st);
+}
+
+// Surface record at a hit (HitRecord after intersect + set_normal).
+struct Surf {
+  V3 p;       // position
+  V3 n;       // shading normal, turned towards the ray
+  V3 ng;      // un-flipped geometric/analytic normal (for emitter-side tests)
+  bool front; // HitRecord::is_inside (front-face flag; FlipFace toggles it)
+  int mat;
+  int light;
+};
+
+// Position of a moving object's point at `time` (rounded, never fused).
+__device__ __forceinline__ V3 moved_point(const SceneView &S, int motion, V3 p, float time) {
+  const float4 v = __ldg(S.motion + (motion - 1));
+  return v3(xadd(p.x, xmul(v.x, time)), xadd(p.y, xmul(v.y, time)), xadd(p.z, xmul(v.z, time)));
+}
+
+__device__ inline Surf surface_at(const SceneView &S, V3 o, V3 d, const HitRec &h, float time) {
+  Surf s;
+  const float4 *pp = reinterpret_cast<const float4 *>(S.shade + h.prim);
+  const float4 q0 = __ldg(pp), q1 = __ldg(pp + 1), q2 = __ldg(pp + 2), q3 = __ldg(pp + 3);
+  PrimShade ps;
+  ps.material = __float_as_int(q0.x);
+  ps.flags = __float_as_int(q0.y);
+  ps.light = __float_as_int(q0.w);
+  ps.n0[0] = q1.x; ps.n0[1] = q1.y; ps.n0[2] = q1.z;
+  ps.n1[0] = q1.w; ps.n1[1] = q2.x; ps.n1[2] = q2.y;
+  ps.n2[0] = q2.z; ps.n2[1] = q2.w; ps.n2[2] = q3.x;
+  ps.ng[0] = q3.y; ps.ng[1] = q3.z; ps.ng[2] = q3.w;
+  s.mat = ps.material;
+  s.light = ps.light;
+  const int type = PT_PRIM_KIND(ps.flags);
+  V3 n;
+  if (type == ITEM_TRI) {
+    // MeshBVHNode::hitTriangle (meshBVH.cpp:112-131) then TriangleMesh::intersect
+    V3 Ng = v3(ps.ng[0], ps.ng[1], ps.ng[2]);
+    if (ps.flags & PT_PRIM_SMOOTH) {
+      float w = 1.f - h.u - h.v;
+      n = normalize(w * v3(ps.n0[0], ps.n0[1], ps.n0[2]) + h.u * v3(ps.n1[0], ps.n1[1], ps.n1[2]) +
+                    h.v * v3(ps.n2[0], ps.n2[1], ps.n2[2]));
+    } else {
+      n = normalize(Ng);
+    }
+    if (dot(n, Ng) < 0.f) n = -n;
+    s.p = xat(o, d, h.t);
+  } else if (type == ITEM_QUAD) {
+    const int axis = PT_PRIM_AXIS(ps.flags);
+    n = v3(axis == 0 ? 1.f : 0.f, axis == 1 ? 1.f : 0.f, axis == 2 ? 1.f : 0.f);
+    s.p = xat(o, xnormalize(d), h.t);
+  } else {
+    V3 dn = xnormalize(d);
+    s.p = xat(o, dn, h.t);
+    V3 c = v3(ps.n0[0], ps.n0[1], ps.n0[2]);
+    if (PT_PRIM_MOTION(ps.flags)) c = moved_point(S, PT_PRIM_MOTION(ps.flags), c, time);
+    n = normalize(s.p - c);
+  }
+  s.ng = n;
+  s.front = dot(d, n) < 0.f;  // set_normal (materialBase.hpp:48-52)
+  s.n = s.front ? n : -n;
+  if (ps.flags & PT_PRIM_FLIP) s.front = !s.front;
+  return s;
+}
+
+// ---------------------------------------------------------- wavefront
+// Path identity inside a wave: slot -> global path g = g0 + slot,
+// pixel q = g % npix, grid sample k = spp_begin + g / npix.
+struct PathId {
+  int q, i, j, k;  // film pixel, frame column / row, grid sample
+  int pix;         // frame pixel index j * full_w + i
+  uint32_t halton_index;
+  uint64_t key;
+};
+__device__ __forceinline__ PathId path_id(const DeviceJob &J, long long g) {
+  PathId P;
+  const long long npix = (long long)J.job.width * J.job.height;
+  P.q = (int)(g % npix);
+  P.k = J.job.spp_begin + (int)(g / npix);
+  P.i = J.job.crop_x + P.q % J.job.width;
+  P.j = J.job.crop_y + P.q / J.job.width;
+  P.pix = P.j * J.job.full_w + P.i;
+  // single-thread order of renderManager.hpp:99-115: i outer, j, k inner
+  uint64_t lin = ((uint64_t)P.i * J.job.full_h + P.j) * (uint64_t)J.job.spp + P.k;
+  P.halton_index = (uint32_t)(lin + 1u);
+  P.key = path_key(J.job.seed, lin);
+  return P;
+}
+
+// The job of a path.  Single-job waves (MJ = false): the kernel's DeviceJob
+// and the path's index g0 + slot.  Merged waves of many jobs (MJ = true):
+// the job index k_camera stored for the path's slot and the path's index
+// within its job.
+template <bool MJ>
+__device__ __forceinline__ const DeviceJob &path_job(const DeviceJob &J, const JobTable &T, const Queues &Q,
+                                                     int slot, long long g0, long long &g) {
+  if (!MJ) {
+    g = g0 + slot;
+    return J;
+  }
+  const int k = Q.job[slot];
+  g = g0 + slot - __ldg(T.start + k);
+  return T.jobs[k];
+}
+
+// k_camera: PerspectiveCamera::generateRay (camera.cpp:42-56) for every path
+// of the wave; the direction is normalised (the one documented deviation:
+// it makes hit distances of every primitive kind comparable).
+// Merged waves: the path's job by binary search of the jobs' first merged
+// indices (start[0] = 0 <= g < start[n]), stored for the later stages.
+template <bool MJ>
+__global__ void k_camera(DeviceJob J0, JobTable T, Queues Q, long long g0, int n) {
+  for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x) {
+    long long g = g0 + s;
+    int jk = 0;
+    if (MJ) {
+      int lo = 0, hi = T.n;
+      while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (__ldg(T.start + mid) <= g) lo = mid;
+        else hi = mid;
+      }
+      jk = lo;
+      Q.job[s] = jk;
+      g -= __ldg(T.start + jk);
+    }
+    const DeviceJob &J = MJ ? T.jobs[jk] : J0;
+    PathId P = path_id(J, g);
+    const CameraView &C = J.job.cam;
+    float2 off = __ldg(J.job.offsets + P.k);
+    float u = ((float)P.i + off.x) / (float)J.job.full_w;
+    float v = ((float)P.j + off.y) / (float)J.job.full_h;
+    const float r = C.lens_radius;
+    float lx = -r + (r - -r) * rand01(P.key, 1u);
+    float ly = -r + (r - -r) * rand01(P.key, 2u);
+    V3 hv = v3(C.h_vec[0], C.h_vec[1], C.h_vec[2]), vv = v3(C.v_vec[0], C.v_vec[1], C.v_vec[2]);
+    V3 ps = v3(C.position[0], C.position[1], C.position[2]) + (hv * lx + vv * ly);
+    V3 dir = v3(C.bottom_left[0], C.bottom_left[1], C.bottom_left[2]) +
+             u * v3(C.horizontal[0], C.horizontal[1], C.horizontal[2]) +
+             v * v3(C.vertical[0], C.vertical[1], C.vertical[2]) - ps;
+    dir = normalize(dir);
+    // motion blur: the path's time, used by every ray of the path
+    const float time = J.job.shutter > 0.f ? J.job.shutter * rand01(P.key, 3u) : 0.f;
+    Q.ray_o[0][s] = make_float4(ps.x, ps.y, ps.z, __int_as_float(s));
+    Q.ray_d[0][s] = make_float4(dir.x, dir.y, dir.z, time);
+    Q.beta[s] = make_float4(1.f, 1.f, 1.f, -1.f);  // w < 0: previous vertex delta / camera
+    Q.L[s] = make_float4(0.f, 0.f, 0.f, 0.f);
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    Q.counts[0] = n;
+    atomicAdd(&Q.stats[0], (unsigned long long)n);
+  }
+}
+
+// Persistent traversal warps with dynamic ray fetch (Aila and Laine,
+// "Understanding the efficiency of ray traversal on GPUs", HPG 2009, and the
+// 2012 addendum): each lane walks its ray one step at a time, and as soon as
+// PT_FETCH_IDLE lanes of a warp have finished, the warp claims that many new
+// rays from the queue with one atomic.  Incoherent rays of very different
+// lengths then no longer hold a warp until its longest ray ends.
+#define PT_FETCH_IDLE 16
+
+__device__ __forceinline__ unsigned lanemask_lt() {
+  return (1u << (threadIdx.x & 31)) - 1u;
+}
+
+// k_trace_closest: the RayQueue through the BVH.  In a participating medium
+// the free-flight distance of the segment is drawn when the ray is fetched
+// (dimension dpb*bounce) and used as tmax: a segment that reaches it without
+// a surface hit is a medium event (prim = PT_HIT_MEDIUM, t = free-flight
+// distance).  That is the same decision as comparing the distance with the
+// closest hit.
+template <bool MJ>
+__global__ void __launch_bounds__(128) k_trace_closest(SceneView S, DeviceJob J, JobTable T, Queues Q, int qsel,
+                                                       int bounce, long long g0) {
+  __shared__ int32_t stack[PT_STACK * 128];
+  const int n = Q.counts[qsel];
+  int *fetch = Q.counts + 4;
+  const int lane = threadIdx.x & 31;
+  int32_t *my_stack = stack + threadIdx.x;
+  TravRay R;
+  bool active = false, exhausted = false;
+  int ray = 0, rays = 0;
+  float t_s = INFINITY;
+  for (;;) {
+    unsigned idle = __ballot_sync(0xffffffffu, !active);
+    if (!exhausted && __popc(idle) >= PT_FETCH_IDLE) {
+      const int k = __popc(idle);
+      int base = 0;
+      if (lane == 0) base = atomicAdd(fetch, k);
+      base = __shfl_sync(0xffffffffu, base, 0);
+      if (base + k >= n) exhausted = true;
+      if (!active) {
+        const int r = base + __popc(idle & lanemask_lt());
+        if (r < n) {
+          float4 ro = ld4(Q.ray_o[qsel] + r), rd = ld4(Q.ray_d[qsel] + r);
+          float tmax = 1e5f;
+          t_s = INFINITY;
+          if (S.has_medium) {
+            long long g;
+            const DeviceJob &Jp = path_job<MJ>(J, T, Q, __float_as_int(ro.w), g0, g);
+            if (bounce < Jp.job.max_depth) {
+              PathId P = path_id(Jp, g);
+              float uf = sampler_dim(Jp, 4 * bounce, P.halton_index, P.key, P.pix, P.k);
+              t_s = -logf(1.f - uf) / S.sigma_t_max;
+              tmax = fminf(tmax, t_s);
+            }
+          }
+          trav_init(R, v3(ro.x, ro.y, ro.z), v3(rd.x, rd.y, rd.z), 1e-4f, tmax, rd.w);
+          ray = r;
+          active = true;
+          ++rays;
+        }
+      }
+      idle = __ballot_sync(0xffffffffu, !active);
+    }
+    if (idle == 0xffffffffu) {
+      if (exhausted) break;
+      continue;
+    }
+    if (active && trav_step<false>(S, R, my_stack, blockDim.x, Q.err)) {
+      const bool hit = R.found;
+      int prim = hit ? R.hit.prim : (t_s < 1e5f ? PT_HIT_MEDIUM : -1);
+      float t = hit ? R.hit.t : (prim == PT_HIT_MEDIUM ? t_s : FLT_MAX);
+      Q.hit[ray] = make_float4(t, __int_as_float(prim), R.hit.u, R.hit.v);
+      active = false;
+    }
+  }
+  warp_count(&Q.stats[2], rays);
+}
+
+__device__ __forceinline__ float power_heuristic(float nf, float fpdf, float ng, float gpdf) {
+  float f = nf * fpdf, g = ng * gpdf;  // maxdepth_mis.hpp:10-15 with sample counts
+  if (isinf(f)) return 1.f;
+  float f2 = f * f, g2 = g * g;
+  return (f2 + g2) > 0.f ? f2 / (f2 + g2) : 0.f;
+}
+
+// Next-event estimation at one vertex (maxdepth_nee.hpp:89-232): LN light
+// samples on a stratified x-by-y grid, each a ShadowQueue entry with its
+// unoccluded contribution.  MED: the vertex is a medium scattering event
+// (isotropic phase function instead of a BSDF, no surface cosine).
+template <int FAM, bool MED>
+__device__ __forceinline__ void next_event(const SceneView &S, const DeviceJob &J, const Queues &Q, int sslot,
+                                           int path, uint64_t key, uint32_t rbase, const Surf &sf, int mat,
+                                           V3 wo, V3 beta, int LN, bool mis, float time) {
+  const float phase = (float)(1.0 / (4.0 * PT_PI));
+  Q.sh_o[sslot] = make_float4(sf.p.x, sf.p.y, sf.p.z, __int_as_float(path));
+  const float inv_ln = 1.f / (float)LN;
+  const bool med = S.has_medium != 0;
+  for (int ls = 0; ls < LN; ++ls) {
+    float4 shd = make_float4(0.f, 0.f, 0.f, -1.f), shc = make_float4(0.f, 0.f, 0.f, 0.f);
+    // getOffsets(x, y): stratum (i, j), i outer (random.hpp:47-63)
+    const int si = ls / J.job.light_ny, sj = ls % J.job.light_ny;
+    float ox = ((float)si + rand01(key, rbase + 2u * ls)) / (float)J.job.light_nx;
+    float oy = ((float)sj + rand01(key, rbase + 2u * ls + 1u)) / (float)J.job.light_ny;
+    int li = (int)(rand01(key, rbase + 20u + ls) * S.n_lights) % S.n_lights;
+    const LightRec &Lr = S.lights[li];
+    V3 wl, Le;
+    float tmax, pdf_l, G, NoI, tr = 1.f;
+    bool valid = true;
+    if (Lr.type == LIGHT_ENV) {
+      float pdir;
+      if (J.job.env_sampling == PT_ENV_ALIAS) {
+        wl = env_alias_sample(S.env, ox, oy, rand01(key, rbase + 28u + ls), pdir);
+      } else {
+        // uniformSampleSphere * 1e5 (texture.hpp:120-124, envLight.hpp:26-43)
+        float z = 1.f - 2.f * ox;
+        float rr = sqrtf(fmaxf(0.f, 1.f - z * z));
+        float sp, cp;
+        sincospi_(2.f * oy, &sp, &cp);
+        V3 pinf = v3(rr * cp, rr * sp, z) * 1e5f;
+        wl = normalize(pinf - sf.p);
+        pdir = (float)(1.0 / (4.0 * PT_PI));
+      }
+      tmax = FLT_MAX;
+      pdf_l = pdir / (float)S.n_lights;
+      NoI = MED ? 1.f : fmaxf(0.f, dot(sf.n, wl));
+      G = NoI;
+      Le = env_lookup(S.env, wl);
+      valid = pdf_l > 1e-7f && !med;  // no light reaches through an infinite medium
+    } else {
+      V3 lp, ln;
+      if (Lr.type == LIGHT_QUAD) {
+        // QuadLight::get_sample / get_normal_at (light.hpp:131-147)
+        lp = v3(Lr.v0[0], Lr.v0[1], Lr.v0[2]) + ox * v3(Lr.e1[0], Lr.e1[1], Lr.e1[2]) +
+             oy * v3(Lr.e2[0], Lr.e2[1], Lr.e2[2]);
+        if (Lr.motion) lp = moved_point(S, Lr.motion, lp, time);
+        ln = v3(Lr.normal[0], Lr.normal[1], Lr.normal[2]);
+      } else {
+        // SphereLight::get_sample (light.hpp:254-264): the whole sphere
+        float sth, cth, sph, cph;
+        sincospi_(2.f * ox, &sth, &cth);
+        float phi = acosf(2.f * oy - 1.f);
+        sincos_(phi, &sph, &cph);
+        V3 c = v3(Lr.v0[0], Lr.v0[1], Lr.v0[2]);
+        if (Lr.motion) c = moved_point(S, Lr.motion, c, time);
+        lp = c + Lr.radius * v3(sph * cth, sph * sth, cph);
+        ln = normalize(lp - c);
+      }
+      V3 ld = lp - sf.p;
+      float len = length(ld);
+      wl = normalize(ld);
+      if (len < 0.001f) valid = false;
+      tmax = len - 0.001f;
+      pdf_l = (Lr.area <= 1e-7f) ? 0.f : 1.f / (Lr.area * (float)S.n_lights);
+      NoI = MED ? 1.f : fmaxf(0.f, dot(sf.n, wl));
+      float NoL = fmaxf(0.f, dot(ln, -wl));
+      float d2 = len * len;
+      G = (d2 < 1e-7f) ? 0.f : NoL * NoI / d2;
+      Le = (dot(ln, -wl) > 0.f) ? v3(Lr.color[0], Lr.color[1], Lr.color[2]) * Lr.intensity : v3(0.f);
+      if (!(pdf_l > 1e-7f)) valid = false;
+      if (mis && valid && NoL > 0.f) {
+        pdf_l = pdf_l * d2 / NoL;  // solid-angle pdf
+        G = NoI;
+      }
+      if (med) tr = expf(-S.sigma_t_max * len);
+    }
+    if (valid && G > 0.f) {
+      V3 f;
+      float pb;
+      if (MED) {
+        f = v3(phase);
+        pb = phase;
+      } else {
+        bsdf_eval_t<FAM>(S.materials[mat], wo, wl, sf.n, sf.front, f, pb);
+      }
+      float w = mis ? power_heuristic((float)LN, pdf_l, 1.f, pb) : 1.f;
+      V3 c = beta * (f * Le * (G / pdf_l * w * inv_ln)) * tr;
+      if (c.x != 0.f || c.y != 0.f || c.z != 0.f) {
+        shd = make_float4(wl.x, wl.y, wl.z, tmax);
+        shc = make_float4(c.x, c.y, c.z, time);
+      }
+    }
+    Q.sh_d[(size_t)ls * Q.cap + sslot] = shd;
+    Q.sh_c[(size_t)ls * Q.cap + sslot] = shc;
+  }
+}
+
+// k_shade<FAM>: one path vertex per thread.  FAM 0..6 processes the
+// material-sorted segment of that BSDF family with its code compiled alone;
+// FAM PT_FAM_MISC the misses, emitter hits and medium events; FAM -1 the
+// whole unsorted queue with run-time dispatch.  Correspondence with
+// getRayColor (maxdepth_nee.hpp):
+//   :16-17   depth limit -> continuations are queued while bounce + 1 < max_depth
+//   :26-37   miss -> env / bg
+//   :44-45   scatter() false -> emit()
+//   :47-78   specular (delta) branches: no NEE, beta *= attenuation
+//   :91-232  NEE (next_event, resolved by k_trace_shadow)
+//   :238-247 continuation hitting an emitter is dropped (REF_NEE)
+//   :251-255 beta *= f * |cos| / pdf
+// NEE_MIS weights light and BSDF sampling with the power heuristic and
+// always performs NEE at non-delta vertices.  The loop runs in phases so
+// that the queue slot allocations (warp ballots) see every lane.
+template <int FAM, bool MJ>
+__global__ void __launch_bounds__(128) k_shade(SceneView S, DeviceJob J, JobTable T, Queues Q, int qsel, int bounce,
+                                               long long g0) {
+  int lo = 0, hi = Q.counts[qsel];
+  if (FAM >= 0) {
+    lo = Q.seg[FAM];
+    hi = (FAM == PT_FAM_MISC) ? Q.seg[PT_KEY_MEDIUM + 1] : Q.seg[FAM + 1];
+  }
+  const int n = hi - lo;
+  const int nq = qsel ^ 1;
+  const uint32_t rbase = 64u + 32u * (uint32_t)bounce;
+  const bool med = S.has_medium != 0;
+  const int dpb = med ? 4 : 3;  // sampler dimensions per bounce
+  const float phase = (float)(1.0 / (4.0 * PT_PI));  // isotropic Henyey-Greenstein, g = 0
+  constexpr bool DO_MISC = (FAM < 0 || FAM == PT_FAM_MISC);
+  constexpr bool DO_SURF = (FAM != PT_FAM_MISC);
+  int segs = 0;
+  const int stride = gridDim.x * blockDim.x;
+  const int nround = (n + stride - 1) / stride * stride;
+  for (int ii = blockIdx.x * blockDim.x + threadIdx.x; ii < nround; ii += stride) {
+    // ---------------- phase A: hit logic and BSDF sampling
+    bool do_nee = false, push = false, nee_medium = false;
+    int path = 0, mat = 0;
+    Surf sf;
+    sf.p = v3(0.f);
+    sf.n = v3(0.f, 0.f, 1.f);
+    sf.front = false;
+    V3 wo = v3(0.f), beta = v3(0.f), wi = v3(0.f), nb = v3(0.f);
+    float npdf = -1.f;
+    uint64_t key = 0;
+    float time = 0.f;
+    int LN = 1;
+    bool mis = false;
+    if (ii < n) {
+      const int i = (FAM >= 0) ? Q.order[lo + ii] : ii;
+      float4 ro = ld4(Q.ray_o[qsel] + i), rd = ld4(Q.ray_d[qsel] + i);
+      float4 hh = ld4(Q.hit + i);
+      path = __float_as_int(ro.w);
+      time = rd.w;
+      V3 o = v3(ro.x, ro.y, ro.z), d = v3(rd.x, rd.y, rd.z);
+      float4 b4 = Q.beta[path];
+      beta = v3(b4.x, b4.y, b4.z);
+      const float prev_pdf = b4.w;  // < 0: camera ray or previous vertex delta
+      long long g;
+      const DeviceJob &Jp = path_job<MJ>(J, T, Q, path, g0, g);
+      LN = Jp.job.light_nx * Jp.job.light_ny;
+      mis = Jp.job.estimator == PT_EST_NEE_MIS;
+      const int max_depth = Jp.job.max_depth;
+      const int limit = mis ? max_depth + 1 : max_depth;
+      PathId P = path_id(Jp, g);
+      key = P.key;
+      const int prim = __float_as_int(hh.y);
+      V3 Ladd = v3(0.f);
+      if (med && bounce >= max_depth) beta = beta * expf(-S.sigma_t_max * (prim >= 0 ? hh.x : INFINITY));
+      if (DO_MISC && prim == PT_HIT_MEDIUM) {
+        // ---- medium scattering event (extension): weight sigma_s / sigma_t
+        ++segs;
+        sf.p = o + hh.x * normalize(d);
+        beta = beta * v3(S.sigma_s[0] / (S.sigma_a[0] + S.sigma_s[0]), S.sigma_s[1] / (S.sigma_a[1] + S.sigma_s[1]),
+                         S.sigma_s[2] / (S.sigma_a[2] + S.sigma_s[2]));
+        do_nee = S.n_lights > 0;
+        nee_medium = true;
+        if (bounce + 1 < limit) {
+          float u0 = sampler_dim(Jp, dpb * bounce + 2, P.halton_index, P.key, P.pix, P.k);
+          float u1 = sampler_dim(Jp, dpb * bounce + 3, P.halton_index, P.key, P.pix, P.k);
+          float z = 1.f - 2.f * u0, rr = sqrtf(fmaxf(0.f, 1.f - z * z));
+          float sp, cp;
+          sincospi_(2.f * u1, &sp, &cp);
+          wi = v3(rr * cp, rr * sp, z);
+          nb = beta;
+          npdf = phase;
+          push = true;
+        }
+      } else if (DO_MISC && prim < 0) {
+        // ---- miss (maxdepth_nee.hpp:26-37)
+        if (S.env.present) {
+          V3 Le = env_lookup(S.env, d);
+          float w = 1.f;
+          if (mis && prev_pdf >= 0.f && S.n_lights > 0) {
+            float pl = (Jp.job.env_sampling == PT_ENV_ALIAS) ? env_alias_pdf(S.env, d) : (float)(1.0 / (4.0 * PT_PI));
+            w = power_heuristic(1.f, prev_pdf, (float)LN, pl / (float)S.n_lights);
+          }
+          Ladd = beta * Le * w;
+        } else {
+          Ladd = beta * v3(S.bg[0], S.bg[1], S.bg[2]);
+        }
+      } else if (prim >= 0) {
+        HitRec h;
+        h.t = hh.x;
+        h.prim = prim;
+        h.u = hh.z;
+        h.v = hh.w;
+        sf = surface_at(S, o, d, h, time);
+        mat = sf.mat;
+        const MatRec &M = S.materials[mat];
+        if (DO_MISC && mat_is_emitter(M)) {
+          // DiffuseEmitter: scatter() is false (material.hpp:475-481)
+          if (prev_pdf < 0.f) {
+            Ladd = beta * mat_emit(M, sf.n, d);
+          } else if (mis) {
+            if (sf.light >= 0) {
+              const LightRec &Lr = S.lights[sf.light];
+              // one-sided emission of the light, as NEE evaluates it
+              V3 lc = v3(Lr.v0[0], Lr.v0[1], Lr.v0[2]);
+              if (Lr.motion) lc = moved_point(S, Lr.motion, lc, time);
+              V3 ln = (Lr.type == LIGHT_QUAD) ? v3(Lr.normal[0], Lr.normal[1], Lr.normal[2]) : normalize(sf.p - lc);
+              float cl = dot(ln, -normalize(d));
+              if (cl > 0.f) {
+                V3 Le = v3(Lr.color[0], Lr.color[1], Lr.color[2]) * Lr.intensity;
+                float pl = h.t * h.t / (cl * Lr.area * (float)S.n_lights);
+                Ladd = beta * Le * power_heuristic(1.f, prev_pdf, (float)LN, pl);
+              }
+            } else {
+              Ladd = beta * mat_emit(M, sf.n, d);
+            }
+          }
+          // REF_NEE after a non-delta vertex: dropped (maxdepth_nee.hpp:246-247)
+        } else if (DO_SURF && !mat_is_emitter(M) && bounce < max_depth) {
+          ++segs;
+          const int dim0 = dpb * bounce + (med ? 1 : 0);
+          float uc = sampler_dim(Jp, dim0, P.halton_index, P.key, P.pix, P.k);
+          float u0 = sampler_dim(Jp, dim0 + 1, P.halton_index, P.key, P.pix, P.k);
+          float u1 = sampler_dim(Jp, dim0 + 2, P.halton_index, P.key, P.pix, P.k);
+          wo = -normalize(d);
+          BsdfSample bs = bsdf_sample_t<FAM>(M, wo, sf.n, sf.front, uc, u0, u1);
+          const bool spec_r = (bs.type & BX_SPECULAR_R) == BX_SPECULAR_R;
+          const bool spec_t = (bs.type & BX_SPECULAR_T) == BX_SPECULAR_T;
+          if (bs.ok && (spec_r || spec_t)) {
+            // specular: emit + attenuation * L(next) (maxdepth_nee.hpp:47-78);
+            // the split-ray case follows one child chosen with probability R
+            // (thin_sample), the expectation of the two-child sum.
+            if (bounce + 1 < limit) {
+              push = true;
+              wi = bs.wi;
+              nb = beta * ((spec_r && spec_t) ? v3(1.f) : bs.att);
+              npdf = -1.f;
+            }
+          } else if (bs.ok || mis) {
+            do_nee = S.n_lights > 0;
+            if (bs.ok && bounce + 1 < limit) {
+              // ---- continuation (maxdepth_nee.hpp:234-255)
+              wi = normalize(bs.wi);
+              float c = fabsf(dot(sf.n, wi));
+              nb = beta * bs.att * (c / bs.pdf);
+              npdf = bs.pdf;
+              push = true;
+              if (Jp.job.rr_start >= 0 && bounce >= Jp.job.rr_start) {
+                // roulette_naive.hpp:35-38 applied to the continuation
+                float q = clampf(max_comp(bs.att), 0.5f, 1.0f);
+                if (rand01(P.key, rbase + 31u) > q) push = false;
+                nb = nb * (1.f / q);
+              }
+            }
+          }
+        }
+      }
+      if (Ladd.x != 0.f || Ladd.y != 0.f || Ladd.z != 0.f) {
+        float4 L4 = Q.L[path];
+        Q.L[path] = make_float4(L4.x + Ladd.x, L4.y + Ladd.y, L4.z + Ladd.z, 0.f);
+      }
+      if (push) Q.beta[path] = make_float4(nb.x, nb.y, nb.z, npdf);
+    }
+    // ---------------- phase B: queue slots (all lanes)
+    const int sslot = warp_alloc(&Q.counts[2], do_nee);
+    const int slot = warp_alloc(&Q.counts[nq], push);
+    if (push) {
+      Q.ray_o[nq][slot] = make_float4(sf.p.x, sf.p.y, sf.p.z, __int_as_float(path));
+      Q.ray_d[nq][slot] = make_float4(wi.x, wi.y, wi.z, time);
+    }
+    // ---------------- phase C: next-event estimation
+    if (do_nee) {
+      long long g;
+      const DeviceJob &Jp = path_job<MJ>(J, T, Q, path, g0, g);
+      if (DO_MISC && nee_medium)
+        next_event<FAM, true>(S, Jp, Q, sslot, path, key, rbase, sf, mat, wo, beta, LN, mis, time);
+      else if (DO_SURF)
+        next_event<FAM, false>(S, Jp, Q, sslot, path, key, rbase, sf, mat, wo, beta, LN, mis, time);
+    }
+  }
+  warp_count(&Q.stats[1], segs);
+}
+
+static inline int grid_for(long long n, int block, int max_blocks) {
+  long long b = (n + block - 1) / block;
+  if (b < 1) b = 1;
+  if (b > max_blocks) b = max_blocks;
+  return (int)b;
+}
+
+// Camera and the bounces of one wave (single job or merged jobs):
+// trace -> [sort] -> shade -> shadow per bounce.
+template <bool MJ>
+void launch_wave_stages(const SceneView &S, const DeviceJob &J, const JobTable &T, const Queues &Q, long long g0,
+                        int n, int LN, int bounces, const LaunchCfg &cfg, cudaStream_t st, Profiler &P) {
+  P.begin(STAGE_CAMERA, st);
+  k_camera<MJ><<<grid_for(n, 256, cfg.max_blocks_simple), 256, 0, st>>>(J, T, Q, g0, n);
+  P.end(st);
+  int qsel = 0;
+  for (int b = 0; b < bounces; ++b) {
+    // reset next-queue and shadow counters (device side, graph friendly)
+    // ([2] shadow queue, [3] shadow fetch, [4] closest-hit fetch)
+    cudaMemsetAsync(Q.counts + (qsel ^ 1), 0, sizeof(int), st);
+    cudaMemsetAsync(Q.counts + 2, 0, 3 * sizeof(int), st);
+    P.begin(STAGE_TRACE, st);
+    k_trace_closest<MJ><<<cfg.trace_blocks, 128, 0, st>>>(S, J, T, Q, qsel, b, g0);
+    P.end(st);
+    if (cfg.sort_by_material) {
+      // sort-by-material queues: one specialised shade kernel per family
+      P.begin(STAGE_SORT, st);
+      launch_sort(S, Q, qsel, cfg, st);
+      P.end(st);
+      P.begin(STAGE_SHADE, st);
+      if (cfg.family_mask & (1u << 0)) k_shade<0, MJ><<<cfg.shade_blocks, 128, 0, st>>>(S, J, T, Q, qsel, b, g0);
+      if (cfg.family_mask & (1u << 1)) k_shade<1, MJ><<<cfg.shade_blocks, 128, 0, st>>>(S, J, T, Q, qsel, b, g0);
+      if (cfg.family_mask & (1u << 2)) k_shade<2, MJ><<<cfg.shade_blocks, 128, 0, st>>>(S, J, T, Q, qsel, b, g0);
+      if (cfg.family_mask & (1u << 3)) k_shade<3, MJ><<<cfg.shade_blocks, 128, 0, st>>>(S, J, T, Q, qsel, b, g0);
+      if (cfg.family_mask & (1u << 4)) k_shade<4, MJ><<<cfg.shade_blocks, 128, 0, st>>>(S, J, T, Q, qsel, b, g0);
+      if (cfg.family_mask & (1u << 5)) k_shade<5, MJ><<<cfg.shade_blocks, 128, 0, st>>>(S, J, T, Q, qsel, b, g0);
+      if (cfg.family_mask & (1u << 6)) k_shade<6, MJ><<<cfg.shade_blocks, 128, 0, st>>>(S, J, T, Q, qsel, b, g0);
+      k_shade<PT_FAM_MISC, MJ><<<cfg.shade_blocks, 128, 0, st>>>(S, J, T, Q, qsel, b, g0);
+      P.end(st);
+    } else {
+      P.begin(STAGE_SHADE, st);
+      k_shade<-1, MJ><<<cfg.shade_blocks, 128, 0, st>>>(S, J, T, Q, qsel, b, g0);
+      P.end(st);
+    }
+    P.begin(STAGE_SHADOW, st);
+    launch_shadow(S, Q, LN, cfg, st);
+    P.end(st);
+    qsel ^= 1;
+  }
+}
+
+}  // namespace pt

@@ -104,7 +104,7 @@ class JobDesc(C.Structure):
         ("max_depth", C.c_int32), ("rr_start", C.c_int32), ("estimator", C.c_int32), ("sampler", C.c_int32),
         ("env_sampling", C.c_int32), ("light_samples_x", C.c_int32), ("light_samples_y", C.c_int32),
         ("seed", C.c_uint32), ("sampler_seed", C.c_uint32), ("camera", CameraDesc), ("gamma", C.c_float),
-        ("reserved", C.c_int32 * 4),
+        ("crop_x", C.c_int32), ("crop_y", C.c_int32), ("full_width", C.c_int32), ("full_height", C.c_int32),
     ]
 
 
@@ -489,6 +489,13 @@ class Server:
         self.r._check(self.lib.pt_poll(self.handle, rid, C.byref(st), _ptr(film, C.c_float), C.byref(done),
                                        C.byref(lat)))
         return st.value, (film if st.value == REQ_DONE else None), done.value, lat.value
+
+    def state(self, rid: int):
+        """(state, spp_done) without copying the film."""
+        st = C.c_int32()
+        done = C.c_int32()
+        self.r._check(self.lib.pt_poll(self.handle, rid, C.byref(st), None, C.byref(done), None))
+        return st.value, done.value
 
     def cancel(self, rid: int):
         self.r._check(self.lib.pt_cancel(self.handle, rid))

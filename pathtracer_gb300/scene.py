@@ -249,3 +249,83 @@ def material_divergence(subdiv: int = 5, seed: int = 0, aspect: float = 16 / 9) 
     sc.medium = ((0.005, 0.005, 0.005), (0.045, 0.045, 0.045), 0.0)
     cam = camera((0.0, 5.5, -10.5), (0.0, -0.45, 1.0), 45.0, aspect)
     return sc, cam
+
+
+# --------------------------------------------------- batched / served mixes
+def with_motion(sc: Scene, seed: int, speed: float = 0.4, shutter_max: float = 0.5,
+                kinds=(N.OBJ_MESH, N.OBJ_SPHERE)) -> Scene:
+    """Gives the scene's meshes and spheres seeded linear velocities
+    (|v| uniform in [0, speed] scene units per unit time, random direction);
+    walls, ground and area lights stay put.  Jobs may then use a shutter up
+    to ``shutter_max``."""
+    rng = np.random.default_rng(seed)
+    objs = []
+    for o in sc.objects:
+        if o[0] in kinds:
+            v = rng.normal(size=3)
+            v = v / np.linalg.norm(v) * rng.uniform(0.0, speed)
+            objs.append((o[0], o[1], tuple(float(x) for x in v)))
+        else:
+            objs.append(o)
+    sc.objects = objs
+    sc.shutter_max = shutter_max
+    return sc
+
+
+def with_lens(cam: dict, lens_diameter: float, focal_dist: float | None = None) -> dict:
+    """Depth of field in the reference's camera terms: PerspectiveCamera's
+    lens radius is focalDist / aperture * 0.5 (camera.cpp:44), so a lens of
+    diameter D takes aperture = focalDist / D (D = 0: a pinhole)."""
+    c = dict(cam)
+    if focal_dist is not None:
+        c["focal_dist"] = float(focal_dist)
+    c["aperture"] = c["focal_dist"] / lens_diameter if lens_diameter > 0 else 1e9
+    return c
+
+
+# per workload: depth, RR start, sampler, env sampling of its plain config
+MIX_SETTINGS = {
+    "cornell": dict(max_depth=8, rr_start=-1, sampler=N.SAMPLER_HALTON_OWEN, env_sampling=N.ENV_UNIFORM),
+    "rough_glass": dict(max_depth=16, rr_start=4, sampler=N.SAMPLER_HALTON_OWEN, env_sampling=N.ENV_ALIAS),
+    "divergence": dict(max_depth=12, rr_start=-1, sampler=N.SAMPLER_STRATIFIED, env_sampling=N.ENV_UNIFORM),
+}
+
+
+def _spp_grid(spp: int) -> tuple[int, int]:
+    x = int(math.isqrt(spp))
+    while spp % x:
+        x -= 1
+    return spp // x, x
+
+
+def job_mix(scenes: dict, n_jobs: int, seed: int, res=(64, 1024), spp=(4, 256), lens_max: float = 0.05,
+            shutter_max: float = 0.5) -> list:
+    """Seeded render jobs over resident scenes: square resolution
+    log-uniform in ``res``, spp uniform in ``spp``, a seeded camera (position
+    and direction jitter around the scene's own), a lens of diameter
+    U[0, lens_max] focused on the scene centre, and a shutter U[0,
+    shutter_max].  ``scenes`` maps a workload name (cornell, rough_glass,
+    divergence) to (scene id, base camera, focus distance)."""
+    rng = np.random.default_rng(seed)
+    names = sorted(scenes)
+    jobs = []
+    for k in range(n_jobs):
+        name = names[int(rng.integers(len(names)))]
+        sid, cam, focus = scenes[name]
+        side = int(round(math.exp(rng.uniform(math.log(res[0]), math.log(res[1])))))
+        s = int(rng.integers(spp[0], spp[1] + 1))
+        sx, sy = _spp_grid(s)
+        c = dict(cam)
+        c["aspect"] = 1.0
+        scale = 0.02 * focus
+        c["position"] = tuple(float(p + rng.uniform(-scale, scale)) for p in cam["position"])
+        fr = np.asarray(cam["front"], np.float64)
+        fr = fr / np.linalg.norm(fr) + rng.uniform(-0.02, 0.02, size=3)
+        c["front"] = tuple(float(x) for x in fr)
+        c = with_lens(c, float(rng.uniform(0.0, lens_max)), focal_dist=focus)
+        c["shutter"] = float(rng.uniform(0.0, shutter_max))
+        st = MIX_SETTINGS[name]
+        jobs.append(N.job_desc(sid, c, side, side, sx, sy, st["max_depth"], estimator=N.EST_NEE_MIS,
+                               sampler=st["sampler"], rr_start=st["rr_start"], env_sampling=st["env_sampling"],
+                               seed=seed * 1000 + k))
+    return jobs
