@@ -42,6 +42,11 @@ import numpy as np  # noqa: E402
 
 PEAKS = REPO / "MEASURED_PEAKS.json"
 FALLBACK_HBM_GBS = 6800.0
+# DRAM bytes (read + write) per launch of the traversal kernels on the
+# default workload at 16 spp per step, from one single-pass ncu capture of
+# the 17 launches of a timed step (profiles/ncu_traffic_rough_glass_1024_16spp.md);
+# scaled by the paths per step for other step sizes.
+NCU_TRAFFIC_PER_LAUNCH_16SPP = {"shadow": 3.630e9 / 17, "trace": 3.376e9 / 17}
 
 
 def parse():
@@ -54,6 +59,7 @@ def parse():
     ap.add_argument("--spp-per-step", type=int, default=16)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-forms", action="store_true", help="skip the batched and served forms")
+    ap.add_argument("--no-rmse", action="store_true", help="skip the converged-reference RMSE")
     ap.add_argument("--batch-jobs", type=int, default=96)
     ap.add_argument("--serve-seconds", type=float, default=10.0)
     ap.add_argument("--serve-rate", type=float, default=20.0, help="Poisson arrivals per second")
@@ -204,7 +210,7 @@ def form_scenes(r, with_big: bool):
     return out, big, time.perf_counter() - t0
 
 
-def run_batched(r, scenes, n_jobs: int, seed: int = 11):
+def run_batched(r, scenes, n_jobs: int, seed: int = 11, res=(64, 1024), spp=(4, 256), tune: bool = True):
     """Config-3 job mix: one pt_render_batch call (one CUDA-graph launch)
     against the plain wavefront drop-in (pt_render per job, one after the
     other); both with host films, so both are end to end.  The two arms
@@ -212,17 +218,19 @@ def run_batched(r, scenes, n_jobs: int, seed: int = 11):
     largest relative film difference is reported."""
     from pathtracer_gb300 import scene as S
 
-    jobs = S.job_mix(scenes, n_jobs, seed=seed)
+    jobs = S.job_mix(scenes, n_jobs, seed=seed, res=res, spp=spp)
     paths = sum(j.width * j.height * j.spp_x * j.spp_y for j in jobs)
-    # autotune the batch launch on a small sample of the mix (first 8 jobs, 4 spp)
-    tj = []
-    for j in jobs[:8]:
-        jj = type(j).from_buffer_copy(j)
-        jj.spp_x, jj.spp_y, jj.spp_begin, jj.spp_end = 2, 2, 0, 0
-        tj.append(jj)
-    t0 = time.perf_counter()
-    tuning = r.autotune(tj)
-    tune_s = time.perf_counter() - t0
+    tuning, tune_s = None, 0.0
+    if tune:
+        # autotune the batch launch on a small sample of the mix (first 8 jobs, 4 spp)
+        tj = []
+        for j in jobs[:8]:
+            jj = type(j).from_buffer_copy(j)
+            jj.spp_x, jj.spp_y, jj.spp_begin, jj.spp_end = 2, 2, 0, 0
+            tj.append(jj)
+        t0 = time.perf_counter()
+        tuning = r.autotune(tj)
+        tune_s = time.perf_counter() - t0
     # warm: queue allocation and graph capture
     r.render_batch(jobs)
     t0 = time.perf_counter()
@@ -237,17 +245,17 @@ def run_batched(r, scenes, n_jobs: int, seed: int = 11):
     for a, b in zip(films_b, films_p):
         d = np.abs(a - b).max() / max(1e-12, float(np.abs(b).max()))
         rel = max(rel, float(d))
-    res = sorted(j.width for j in jobs)
+    sides = sorted(j.width for j in jobs)
     return {
         "jobs": n_jobs, "paths": paths, "paths_per_s": paths / t_batch, "plain_paths_per_s": paths / t_plain,
         "speedup_vs_plain": t_plain / t_batch, "batch_s": t_batch, "plain_s": t_plain,
         "graph_device_ms": st.ms, "max_rel_film_diff_vs_plain": rel,
         "equal_rmse": "same samples in both arms: identical images up to FP32 summation order",
         "mix": f"{n_jobs} jobs over cornell/rough_glass/divergence with per-object motion; square resolution "
-               f"log-uniform 64..1024 (median {res[len(res) // 2]}), spp U{{4..256}}, lens diameter U[0,0.05], "
-               "shutter U[0,0.5], NEE+MIS",
-        "autotune": {k: tuning[k] for k in ("wave_paths", "sort_by_material", "trace_blocks", "shade_blocks")} |
-                    {"candidates": tuning["candidates"], "seconds": tune_s},
+               f"log-uniform {res[0]}..{res[1]} (median {sides[len(sides) // 2]}), spp U{{{spp[0]}..{spp[1]}}}, "
+               "lens diameter U[0,0.05], shutter U[0,0.5], NEE+MIS",
+        "autotune": ({k: tuning[k] for k in ("wave_paths", "sort_by_material", "trace_blocks", "shade_blocks")} |
+                     {"candidates": tuning["candidates"], "seconds": tune_s}) if tuning else "as tuned above",
     }
 
 
@@ -518,19 +526,27 @@ def run_ours(args, rank, world, local_rank):
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "kernel": f"k_{'trace_closest' if dom == 'trace' else 'trace_shadow' if dom == 'shadow' else 'shade'}",
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "peak_source": peak_src, "traffic": None,
+                     "peak_source": peak_src,
+                     "traffic": (NCU_TRAFFIC_PER_LAUNCH_16SPP[dom] * k / 16.0
+                                 if args.workload == "rough_glass" and dom in NCU_TRAFFIC_PER_LAUNCH_16SPP else None),
+                     "traffic_note": "ncu dram__bytes_read.sum + dram__bytes_write.sum per launch (average over "
+                                     "a 16-spp step's launches, scaled to this step), bytes",
                      "note": f"stage share {prof[dom][0] / sum(v[0] for v in prof.values()):.2f}; "
                              f"whole-step queue bytes {step_bytes_gbs:.1f} GB/s"},
         "stage_ms": {kk: round(v[0], 3) for kk, v in prof.items()},
         "clocks": clk.summary(),
         "wall_s": wall,
     }
-    if world == 1:
+    if world == 1 and not args.no_rmse:
         line["rmse"] = converged_rmse(r, sid, cam, wl, k)
     if world == 1 and not args.no_forms:
         fs, big, build_s = form_scenes(r, with_big=True)
         forms = {"scene_build_s": build_s}
         forms["batched"] = run_batched(r, fs, args.batch_jobs)
+        # the regime batching exists for: many jobs far below one GPU's worth
+        # of paths each (same scenes and cameras, smaller frames and spp)
+        forms["batched_small_jobs"] = run_batched(r, fs, args.batch_jobs, seed=13, res=(64, 256), spp=(4, 32),
+                                                  tune=False)
         forms["served"] = run_served(r, fs, big, args.serve_seconds, args.serve_rate)
         line["forms"] = forms
     if not args.no_cpu_baseline:

@@ -1166,7 +1166,10 @@ int pt_profile_end(void *ctx, double *stage_ms, int64_t *stage_launches) {
       cudaEventElapsedTime(&ms, c->prof.pool[2 * i], c->prof.pool[2 * i + 1]);
       const int k = c->prof.kinds[i];
       if (stage_ms) stage_ms[k] += ms;
-      if (stage_launches) stage_launches[k] += (k == STAGE_SORT) ? 2 : 1;
+    }
+    for (int k = 0; k < STAGE_COUNT; ++k) {
+      if (stage_launches) stage_launches[k] = c->prof.kernels[k];
+      c->prof.kernels[k] = 0;
     }
     c->prof.on = false;
     c->prof.used = 0;

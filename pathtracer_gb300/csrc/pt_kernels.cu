@@ -368,6 +368,7 @@ void launch_wave(const SceneView &S, const DeviceJob &J, const Queues &Q, long l
   P.begin(STAGE_FILM, st);
   launch_film(J, Q, g0, n, 0, film, cfg, st);
   P.end(st);
+  P.count(STAGE_FILM, 1);
 }
 
 void launch_sort(const SceneView &S, const Queues &Q, int qsel, const LaunchCfg &cfg, cudaStream_t st) {

@@ -67,6 +67,10 @@ struct Profiler {
   std::vector<cudaEvent_t> pool;
   size_t used = 0;
   std::vector<int> kinds;  // per begin/end event pair
+  long long kernels[STAGE_COUNT] = {};  // kernel launches per stage while on
+  void count(int kind, int n) {
+    if (on) kernels[kind] += n;
+  }
   cudaEvent_t take() {
     if (used == pool.size()) {
       cudaEvent_t e;

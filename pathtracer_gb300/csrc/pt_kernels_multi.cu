@@ -25,6 +25,7 @@ void launch_wave_multi(const SceneView &S, const MergedJobs &M, const Queues &Q,
     const long long a = std::max(g0, M.start[k]), b = std::min(g1, M.start[k + 1]);
     if (a >= b) continue;
     launch_film(M.jobs[k], Q, a - M.start[k], (int)(b - a), a - g0, M.films[k], cfg, st);
+    P.count(STAGE_FILM, 1);
   }
   P.end(st);
 }

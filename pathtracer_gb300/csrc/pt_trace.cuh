@@ -146,20 +146,27 @@ __device__ __forceinline__ bool test_leaf(const SceneView &S, int32_t ref, V3 o_
   return any;
 }
 
-// Traversal state of one ray.  The walk is a sequence of steps (one node
-// visit or one leaf test each) so that a persistent warp can refill lanes
-// whose rays have finished while the others continue (trav_step).
+// Traversal state of one ray.  The walk is a sequence of node visits and
+// leaf tests (trav_step) so that a persistent warp can refill lanes whose
+// rays have finished while the others continue.
 struct TravRay {
   V3 o, d, dn, inv, oi;  // o, oi: the current frame (world, or a moving object's)
   V3 ow;                 // world origin
   float tmin, tmax;
-  int32_t ref;  // node index (>= 0) or leaf reference (< 0) visited next
-  int sp;       // stack depth
+  int32_t ref;   // next reference: node (>= 0, PT_INST_BIT: entering a moving
+                 // object), leaf (< 0), PT_FRAME_END or PT_REF_EMPTY
+  int sp;        // stack depth
   int iters;
-  float time;   // motion blur: the ray's time
+  float time;    // motion blur: the ray's time
   bool found;
   HitRec hit;
 };
+
+// The stack is empty: the ray is finished once no leaf is pending.
+#define PT_REF_EMPTY ((int32_t)0x80000001)
+
+__device__ __forceinline__ bool ref_is_node(int32_t r) { return r >= 0 || r == PT_FRAME_END; }
+__device__ __forceinline__ bool ref_is_leaf(int32_t r) { return r < 0 && r != PT_FRAME_END && r != PT_REF_EMPTY; }
 
 __device__ __forceinline__ void trav_init(TravRay &R, V3 o, V3 d, float tmin, float tmax, float time = 0.f) {
   R.time = time;
@@ -180,54 +187,51 @@ __device__ __forceinline__ void trav_init(TravRay &R, V3 o, V3 d, float tmin, fl
   R.hit.u = R.hit.v = 0.f;
 }
 
-// One traversal step.  `stack` points at this thread's column of a shared
-// array laid out [PT_STACK][stride].  Returns true when the ray is finished:
-// closest -> R.found / R.hit hold the nearest hit; any -> R.found = occluded.
-// *err is set when the stack would overflow or the iteration cap is reached
-// (never expected); the ray is then finished with what it has.
+__device__ __forceinline__ int32_t trav_pop(TravRay &R, const int32_t *stack, int stride) {
+  return R.sp == 0 ? PT_REF_EMPTY : stack[(--R.sp) * stride];
+}
+
+// One node visit (or frame change).  R.ref must satisfy ref_is_node; after it
+// R.ref is the next reference (the nearest hit child for closest hit, the
+// first hit child in node order for any hit, else the top of the stack).
+// `stack` points at this thread's column of a shared array laid out
+// [PT_STACK][stride].  Returns false on a stack overflow (error flag set).
 template <bool ANY>
-__device__ __forceinline__ bool trav_step(const SceneView &S, TravRay &R, int32_t *stack, int stride, int *err) {
-  if (++R.iters > PT_TRAVERSAL_CAP) {
-    *err = 2;
-    return true;
-  }
+__device__ __forceinline__ bool trav_node(const SceneView &S, TravRay &R, int32_t *stack, int stride, int *err) {
   if (R.ref == PT_FRAME_END) {
     // leaving a moving object's subtree: back to the world frame
     R.o = R.ow;
     R.oi = v3(-R.o.x * R.inv.x, -R.o.y * R.inv.y, -R.o.z * R.inv.z);
-    if (R.sp == 0) return true;
-    R.ref = stack[(--R.sp) * stride];
-    return false;
+    R.ref = trav_pop(R, stack, stride);
+    return true;
   }
-  if (R.ref >= 0 && (R.ref & PT_INST_BIT)) {
+  if (R.ref & PT_INST_BIT) {
     // entering a moving object's subtree: the ray in the object's frame at
     // its time, until PT_FRAME_END comes off the stack
     R.ref &= ~PT_INST_BIT;
     if (R.sp + 1 > PT_STACK) {
       *err = 1;
-      return true;
+      return false;
     }
     stack[(R.sp++) * stride] = PT_FRAME_END;
     R.o = moved_origin(S, (uint32_t)__ldg(S.node_motion + R.ref), R.ow, R.time);
     R.oi = v3(-R.o.x * R.inv.x, -R.o.y * R.inv.y, -R.o.z * R.inv.z);
   }
-  if (R.ref >= 0) {
-    const float4 *np = reinterpret_cast<const float4 *>(S.nodes + R.ref);
-    float4 lx = __ldg(np + 0), hx = __ldg(np + 1), ly = __ldg(np + 2), hy = __ldg(np + 3);
-    float4 lz = __ldg(np + 4), hz = __ldg(np + 5);
-    int4 ch = __ldg(reinterpret_cast<const int4 *>(np + 6));
-    int4 cn = __ldg(reinterpret_cast<const int4 *>(np + 7));
-    const float lxa[4] = {lx.x, lx.y, lx.z, lx.w}, hxa[4] = {hx.x, hx.y, hx.z, hx.w};
-    const float lya[4] = {ly.x, ly.y, ly.z, ly.w}, hya[4] = {hy.x, hy.y, hy.z, hy.w};
-    const float lza[4] = {lz.x, lz.y, lz.z, lz.w}, hza[4] = {hz.x, hz.y, hz.z, hz.w};
-    const int cha[4] = {ch.x, ch.y, ch.z, ch.w}, cna[4] = {cn.x, cn.y, cn.z, cn.w};
-    const V3 inv = R.inv, oi = R.oi;
-    const float tmin = R.tmin, tmax = R.tmax;
-    // entry distance per child (+inf when missed or empty), kept in
-    // registers; closest-hit visits near to far (sorting network), any-hit
-    // in node order.
-    float d0, d1, d2, d3;
-    int32_t r0, r1, r2, r3;
+  const float4 *np = reinterpret_cast<const float4 *>(S.nodes + R.ref);
+  float4 lx = __ldg(np + 0), hx = __ldg(np + 1), ly = __ldg(np + 2), hy = __ldg(np + 3);
+  float4 lz = __ldg(np + 4), hz = __ldg(np + 5);
+  int4 ch = __ldg(reinterpret_cast<const int4 *>(np + 6));
+  int4 cn = __ldg(reinterpret_cast<const int4 *>(np + 7));
+  const float lxa[4] = {lx.x, lx.y, lx.z, lx.w}, hxa[4] = {hx.x, hx.y, hx.z, hx.w};
+  const float lya[4] = {ly.x, ly.y, ly.z, ly.w}, hya[4] = {hy.x, hy.y, hy.z, hy.w};
+  const float lza[4] = {lz.x, lz.y, lz.z, lz.w}, hza[4] = {hz.x, hz.y, hz.z, hz.w};
+  const int cha[4] = {ch.x, ch.y, ch.z, ch.w}, cna[4] = {cn.x, cn.y, cn.z, cn.w};
+  const V3 inv = R.inv, oi = R.oi;
+  const float tmin = R.tmin, tmax = R.tmax;
+  // entry distance per child (+inf when missed or empty), kept in registers;
+  // closest-hit visits near to far (sorting network), any-hit in node order.
+  float d0, d1, d2, d3;
+  int32_t r0, r1, r2, r3;
 #define PT_CHILD(c, dd, rr)                                                                          \
   {                                                                                                  \
     float t0x = fmaf(lxa[c], inv.x, oi.x), t1x = fmaf(hxa[c], inv.x, oi.x);                        \
@@ -238,12 +242,12 @@ __device__ __forceinline__ bool trav_step(const SceneView &S, TravRay &R, int32_
     dd = (cna[c] >= 0 && tn <= tf) ? tn : INFINITY;                                                 \
     rr = cna[c] == 0 ? cha[c] : leaf_ref(cha[c], max(cna[c], 1));                                   \
   }
-    PT_CHILD(0, d0, r0)
-    PT_CHILD(1, d1, r1)
-    PT_CHILD(2, d2, r2)
-    PT_CHILD(3, d3, r3)
+  PT_CHILD(0, d0, r0)
+  PT_CHILD(1, d1, r1)
+  PT_CHILD(2, d2, r2)
+  PT_CHILD(3, d3, r3)
 #undef PT_CHILD
-    if (!ANY) {
+  if (!ANY) {
 #define PT_CSWAP(da, ra, db, rb)   \
   if (db < da) {                   \
     float tt = da;                 \
@@ -253,49 +257,61 @@ __device__ __forceinline__ bool trav_step(const SceneView &S, TravRay &R, int32_
     ra = rb;                       \
     rb = tr;                       \
   }
-      PT_CSWAP(d0, r0, d1, r1)
-      PT_CSWAP(d2, r2, d3, r3)
-      PT_CSWAP(d0, r0, d2, r2)
-      PT_CSWAP(d1, r1, d3, r3)
-      PT_CSWAP(d1, r1, d2, r2)
+    PT_CSWAP(d0, r0, d1, r1)
+    PT_CSWAP(d2, r2, d3, r3)
+    PT_CSWAP(d0, r0, d2, r2)
+    PT_CSWAP(d1, r1, d3, r3)
+    PT_CSWAP(d1, r1, d2, r2)
 #undef PT_CSWAP
-    }
-    const int nh = (d0 < INFINITY) + (d1 < INFINITY) + (d2 < INFINITY) + (d3 < INFINITY);
-    if (nh == 0) {
-      if (R.sp == 0) return true;
-      R.ref = stack[(--R.sp) * stride];
-      return false;
-    }
-    if (R.sp + nh - 1 > PT_STACK) {
-      *err = 1;
-      return true;
-    }
-    // push the farther hits (far first), descend into the nearest
-    int32_t first = 0;
-    int sp = R.sp;
-    if (ANY) {
-      // node order: descend into the first hit child, push the others
-      bool have = false;
-      if (d3 < INFINITY) { first = r3; have = true; }
-      if (d2 < INFINITY) { if (have) stack[(sp++) * stride] = first; first = r2; have = true; }
-      if (d1 < INFINITY) { if (have) stack[(sp++) * stride] = first; first = r1; have = true; }
-      if (d0 < INFINITY) { if (have) stack[(sp++) * stride] = first; first = r0; have = true; }
-    } else {
-      if (d3 < INFINITY) stack[(sp++) * stride] = r3;
-      if (d2 < INFINITY) stack[(sp++) * stride] = r2;
-      if (d1 < INFINITY) stack[(sp++) * stride] = r1;
-      first = r0;  // d0 is the smallest and finite (nh > 0)
-    }
-    R.sp = sp;
-    R.ref = first;
+  }
+  const int nh = (d0 < INFINITY) + (d1 < INFINITY) + (d2 < INFINITY) + (d3 < INFINITY);
+  if (nh == 0) {
+    R.ref = trav_pop(R, stack, stride);
+    return true;
+  }
+  if (R.sp + nh - 1 > PT_STACK) {
+    *err = 1;
     return false;
   }
+  // push the farther hits (far first), descend into the nearest
+  int32_t first = 0;
+  int sp = R.sp;
+  if (ANY) {
+    // node order: descend into the first hit child, push the others
+    bool have = false;
+    if (d3 < INFINITY) { first = r3; have = true; }
+    if (d2 < INFINITY) { if (have) stack[(sp++) * stride] = first; first = r2; have = true; }
+    if (d1 < INFINITY) { if (have) stack[(sp++) * stride] = first; first = r1; have = true; }
+    if (d0 < INFINITY) { if (have) stack[(sp++) * stride] = first; first = r0; have = true; }
+  } else {
+    if (d3 < INFINITY) stack[(sp++) * stride] = r3;
+    if (d2 < INFINITY) stack[(sp++) * stride] = r2;
+    if (d1 < INFINITY) stack[(sp++) * stride] = r1;
+    first = r0;  // d0 is the smallest and finite (nh > 0)
+  }
+  R.sp = sp;
+  R.ref = first;
+  return true;
+}
+
+// One traversal step of one ray: a node visit or a leaf test.  Returns true
+// when the ray is finished: closest -> R.found / R.hit hold the nearest hit;
+// any -> R.found = occluded.  *err is set when the stack would overflow or
+// the iteration cap is reached (never expected); the ray is then finished
+// with what it has.
+template <bool ANY>
+__device__ __forceinline__ bool trav_step(const SceneView &S, TravRay &R, int32_t *stack, int stride, int *err) {
+  if (++R.iters > PT_TRAVERSAL_CAP) {
+    *err = 2;
+    return true;
+  }
+  if (R.ref == PT_REF_EMPTY) return true;
+  if (ref_is_node(R.ref)) return !trav_node<ANY>(S, R, stack, stride, err);
   if (test_leaf<ANY>(S, R.ref, R.o, R.d, R.dn, R.tmin, R.tmax, R.hit, R.time)) {
     R.found = true;
     if (ANY) return true;
   }
-  if (R.sp == 0) return true;
-  R.ref = stack[(--R.sp) * stride];
+  R.ref = trav_pop(R, stack, stride);
   return false;
 }
 

@@ -658,6 +658,7 @@ void launch_wave_stages(const SceneView &S, const DeviceJob &J, const JobTable &
   P.begin(STAGE_CAMERA, st);
   k_camera<MJ><<<grid_for(n, 256, cfg.max_blocks_simple), 256, 0, st>>>(J, T, Q, g0, n);
   P.end(st);
+  P.count(STAGE_CAMERA, 1);
   int qsel = 0;
   for (int b = 0; b < bounces; ++b) {
     // reset next-queue and shadow counters (device side, graph friendly)
@@ -667,11 +668,13 @@ void launch_wave_stages(const SceneView &S, const DeviceJob &J, const JobTable &
     P.begin(STAGE_TRACE, st);
     k_trace_closest<MJ><<<cfg.trace_blocks, 128, 0, st>>>(S, J, T, Q, qsel, b, g0);
     P.end(st);
+    P.count(STAGE_TRACE, 1);
     if (cfg.sort_by_material) {
       // sort-by-material queues: one specialised shade kernel per family
       P.begin(STAGE_SORT, st);
       launch_sort(S, Q, qsel, cfg, st);
       P.end(st);
+      P.count(STAGE_SORT, 2);
       P.begin(STAGE_SHADE, st);
       if (cfg.family_mask & (1u << 0)) k_shade<0, MJ><<<cfg.shade_blocks, 128, 0, st>>>(S, J, T, Q, qsel, b, g0);
       if (cfg.family_mask & (1u << 1)) k_shade<1, MJ><<<cfg.shade_blocks, 128, 0, st>>>(S, J, T, Q, qsel, b, g0);
@@ -682,14 +685,17 @@ void launch_wave_stages(const SceneView &S, const DeviceJob &J, const JobTable &
       if (cfg.family_mask & (1u << 6)) k_shade<6, MJ><<<cfg.shade_blocks, 128, 0, st>>>(S, J, T, Q, qsel, b, g0);
       k_shade<PT_FAM_MISC, MJ><<<cfg.shade_blocks, 128, 0, st>>>(S, J, T, Q, qsel, b, g0);
       P.end(st);
+      P.count(STAGE_SHADE, 1 + __builtin_popcount(cfg.family_mask & 0x7fu));
     } else {
       P.begin(STAGE_SHADE, st);
       k_shade<-1, MJ><<<cfg.shade_blocks, 128, 0, st>>>(S, J, T, Q, qsel, b, g0);
       P.end(st);
+      P.count(STAGE_SHADE, 1);
     }
     P.begin(STAGE_SHADOW, st);
     launch_shadow(S, Q, LN, cfg, st);
     P.end(st);
+    P.count(STAGE_SHADOW, 2);
     qsel ^= 1;
   }
 }
