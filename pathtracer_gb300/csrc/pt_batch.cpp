@@ -32,6 +32,7 @@ Batch::~Batch() {
   if (exec) cudaGraphExecDestroy(exec);
   for (auto &s : slots) s.release();
   if (fork) cudaEventDestroy(fork);
+  for (cudaEvent_t e : film_events) cudaEventDestroy(e);
 }
 
 void BatchSlot::release() {
@@ -48,15 +49,19 @@ void BatchSlot::release() {
   fr(films);
   jobs_cap = 0;
   offsets_cap = films_cap = 0;
-  if (stream) cudaStreamDestroy(stream);
-  stream = nullptr;
-  if (done) cudaEventDestroy(done);
-  done = nullptr;
+  for (int h = 0; h < 2; ++h) {
+    if (stream[h]) cudaStreamDestroy(stream[h]);
+    stream[h] = nullptr;
+    if (done[h]) cudaEventDestroy(done[h]);
+    done[h] = nullptr;
+  }
 }
 
 void BatchSlot::ensure(int want_cap, int want_ln, int n_jobs, size_t n_offsets, size_t film_floats) {
-  if (!stream) cuda_check(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "cudaStreamCreate");
-  if (!done) cuda_check(cudaEventCreateWithFlags(&done, cudaEventDisableTiming), "cudaEventCreate");
+  for (int h = 0; h < 2; ++h) {
+    if (!stream[h]) cuda_check(cudaStreamCreateWithFlags(&stream[h], cudaStreamNonBlocking), "cudaStreamCreate");
+    if (!done[h]) cuda_check(cudaEventCreateWithFlags(&done[h], cudaEventDisableTiming), "cudaEventCreate");
+  }
   if (want_cap > cap || want_ln > ln) {
     for (void *p : mem) cudaFree(p);
     mem.clear();
@@ -67,27 +72,30 @@ void BatchSlot::ensure(int want_cap, int want_ln, int n_jobs, size_t n_offsets, 
       return p;
     };
     const size_t c = (size_t)want_cap;
-    Q.cap = want_cap;
-    Q.beta = (float4 *)alloc(c * 16);
-    Q.L = (float4 *)alloc(c * 16);
-    Q.ray_o[0] = (float4 *)alloc(c * 16);
-    Q.ray_o[1] = (float4 *)alloc(c * 16);
-    Q.ray_d[0] = (float4 *)alloc(c * 16);
-    Q.ray_d[1] = (float4 *)alloc(c * 16);
-    Q.hit = (float4 *)alloc(c * 16);
-    Q.sh_o = (float4 *)alloc(c * 16);
-    Q.sh_d = (float4 *)alloc(c * 16 * want_ln);
-    Q.sh_c = (float4 *)alloc(c * 16 * want_ln);
-    Q.sh_vis = (uint8_t *)alloc(c * want_ln);
-    Q.counts = (int *)alloc(64);
-    Q.stats = (unsigned long long *)alloc(64);
-    Q.err = (int *)alloc(16);
-    Q.sort_key = (int *)alloc(c * 4);
-    Q.order = (int *)alloc(c * 4);
-    Q.job = (int *)alloc(c * 4);
-    Q.bins = (int *)alloc(sizeof(int) * 2 * PT_SORT_BINS);
-    Q.seg = (int *)alloc(sizeof(int) * (PT_SORT_BINS + 1));
-    cuda_check(cudaMemset(Q.err, 0, 16), "memset err");
+    for (int h = 0; h < 2; ++h) {
+      Queues &Q = this->Q[h];
+      Q.cap = want_cap;
+      Q.beta = (float4 *)alloc(c * 16);
+      Q.L = (float4 *)alloc(c * 16);
+      Q.ray_o[0] = (float4 *)alloc(c * 16);
+      Q.ray_o[1] = (float4 *)alloc(c * 16);
+      Q.ray_d[0] = (float4 *)alloc(c * 16);
+      Q.ray_d[1] = (float4 *)alloc(c * 16);
+      Q.hit = (float4 *)alloc(c * 16);
+      Q.sh_o = (float4 *)alloc(c * 16);
+      Q.sh_d = (float4 *)alloc(c * 16 * want_ln);
+      Q.sh_c = (float4 *)alloc(c * 16 * want_ln);
+      Q.sh_vis = (uint8_t *)alloc(c * want_ln);
+      Q.counts = (int *)alloc(64);
+      Q.stats = (unsigned long long *)alloc(64);
+      Q.err = (int *)alloc(16);
+      Q.sort_key = (int *)alloc(c * 4);
+      Q.order = (int *)alloc(c * 4);
+      Q.job = (int *)alloc(c * 4);
+      Q.bins = (int *)alloc(sizeof(int) * 2 * PT_SORT_BINS);
+      Q.seg = (int *)alloc(sizeof(int) * (PT_SORT_BINS + 1));
+      cuda_check(cudaMemset(Q.err, 0, 16), "memset err");
+    }
     cap = want_cap;
     ln = want_ln;
   }
@@ -211,21 +219,47 @@ void render_batch(Context *c, const pt_job_desc *jobs, int n, float **films, pt_
     cudaGraph_t graph = nullptr;
     cuda_check(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal), "begin capture");
     cudaEventRecord(B.fork, c->stream);
+    size_t n_events = 0;
+    for (const Group &G : groups) n_events += (size_t)((G.total + G.wave - 1) / G.wave);
+    while (B.film_events.size() < n_events) {
+      cudaEvent_t e;
+      cuda_check(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "cudaEventCreate");
+      B.film_events.push_back(e);
+    }
+    size_t ev = 0;
     for (size_t gi = 0; gi < groups.size(); ++gi) {
       Group &G = groups[gi];
       BatchSlot &slot = B.slots[gi];
       Scene *S = c->scene(G.scene);
-      cudaStreamWaitEvent(slot.stream, B.fork, 0);
-      cudaMemsetAsync(slot.Q.stats, 0, 64, slot.stream);
-      if (!targets) cudaMemsetAsync(slot.films, 0, sizeof(float) * G.film_floats, slot.stream);
+      for (int h = 0; h < 2; ++h) {
+        cudaStreamWaitEvent(slot.stream[h], B.fork, 0);
+        cudaMemsetAsync(slot.Q[h].stats, 0, 64, slot.stream[h]);
+      }
+      if (!targets) cudaMemsetAsync(slot.films, 0, sizeof(float) * G.film_floats, slot.stream[0]);
       LaunchCfg lc = c->cfg;
       lc.family_mask = S->family_mask;
-      for (long long g0 = 0; g0 < G.total; g0 += G.wave) {
+      // consecutive waves alternate between two queue sets on two streams,
+      // so one wave's sparse last bounces overlap the next wave's first
+      // ones; the film stages stay in wave order (event chain), which keeps
+      // every pixel's samples added in sample order
+      cudaEvent_t prev = nullptr;
+      int w = 0;
+      for (long long g0 = 0; g0 < G.total; g0 += G.wave, ++w) {
         const int cnt = (int)std::min<long long>(G.wave, G.total - g0);
-        launch_wave_multi(S->view, G.M, slot.Q, g0, cnt, lc, slot.stream, nullptr);
+        const int h = w & 1;
+        if (w == 1 && !targets) {
+          // the film clear on stream 0 precedes every film stage
+          cudaEventRecord(slot.done[0], slot.stream[0]);
+          cudaStreamWaitEvent(slot.stream[1], slot.done[0], 0);
+        }
+        cudaEvent_t mine = B.film_events[ev++];
+        launch_wave_multi(S->view, G.M, slot.Q[h], g0, cnt, lc, slot.stream[h], nullptr, prev, mine);
+        prev = mine;
       }
-      cudaEventRecord(slot.done, slot.stream);
-      cudaStreamWaitEvent(c->stream, slot.done, 0);
+      for (int h = 0; h < 2; ++h) {
+        cudaEventRecord(slot.done[h], slot.stream[h]);
+        cudaStreamWaitEvent(c->stream, slot.done[h], 0);
+      }
     }
     cudaError_t ce = cudaStreamEndCapture(c->stream, &graph);
     cuda_check(ce, "end capture");
@@ -274,18 +308,20 @@ void render_batch(Context *c, const pt_job_desc *jobs, int n, float **films, pt_
   for (size_t gi = 0; gi < groups.size(); ++gi) {
     Group &G = groups[gi];
     BatchSlot &slot = B.slots[gi];
-    int herr = 0;
-    cuda_check(cudaMemcpy(&herr, slot.Q.err, sizeof(int), cudaMemcpyDeviceToHost), "read err");
-    if (herr) {
-      cudaMemset(slot.Q.err, 0, sizeof(int));
-      fail(PT_ERR_DEVICE, "device traversal error flag in batch group " + std::to_string(gi));
+    for (int q = 0; q < 2; ++q) {
+      int herr = 0;
+      cuda_check(cudaMemcpy(&herr, slot.Q[q].err, sizeof(int), cudaMemcpyDeviceToHost), "read err");
+      if (herr) {
+        cudaMemset(slot.Q[q].err, 0, sizeof(int));
+        fail(PT_ERR_DEVICE, "device traversal error flag in batch group " + std::to_string(gi));
+      }
+      unsigned long long h[4];
+      cuda_check(cudaMemcpy(h, slot.Q[q].stats, sizeof h, cudaMemcpyDeviceToHost), "read stats");
+      tot.paths += h[0];
+      tot.segments += h[1];
+      tot.rays += h[2];
+      tot.shadow_rays += h[3];
     }
-    unsigned long long h[4];
-    cuda_check(cudaMemcpy(h, slot.Q.stats, sizeof h, cudaMemcpyDeviceToHost), "read stats");
-    tot.paths += h[0];
-    tot.segments += h[1];
-    tot.rays += h[2];
-    tot.shadow_rays += h[3];
     if (targets || !films) continue;
     for (size_t m = 0; m < G.members.size(); ++m) {
       const int k = G.members[m];

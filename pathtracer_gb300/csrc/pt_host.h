@@ -52,7 +52,7 @@ std::unique_ptr<Scene> build_scene(const pt_scene_desc *d, cudaStream_t st);
 // Device buffers of one merged group of a batch (the jobs of one scene with
 // the same light-sample count), reused across batched renders.
 struct BatchSlot {
-  Queues Q{};
+  Queues Q[2]{};                // two queue sets: consecutive waves overlap
   std::vector<void *> mem;
   int cap = 0, ln = 0;
   DeviceJob *d_jobs = nullptr;  // job table
@@ -62,8 +62,8 @@ struct BatchSlot {
   size_t offsets_cap = 0;
   float *films = nullptr;       // the jobs' films (when no targets are given), concatenated
   size_t films_cap = 0;
-  cudaStream_t stream = nullptr;
-  cudaEvent_t done = nullptr;
+  cudaStream_t stream[2] = {nullptr, nullptr};
+  cudaEvent_t done[2] = {nullptr, nullptr};
   void ensure(int want_cap, int want_ln, int n_jobs, size_t n_offsets, size_t film_floats);
   void release();
 };
@@ -74,6 +74,7 @@ struct Batch {
   std::vector<BatchSlot> slots;
   cudaGraphExec_t exec = nullptr;
   cudaEvent_t fork = nullptr;
+  std::vector<cudaEvent_t> film_events;  // per wave: its films are done
   std::string sig;
   int captures = 0;  // graph instantiations
   int updates = 0;   // in-place parameter updates of the executable graph

@@ -126,8 +126,12 @@ struct MergedJobs {
   int bounces = 0;               // max over the jobs of max_depth (+1 with MIS)
   int LN = 1;                    // light samples per vertex (equal for all jobs)
 };
+// film_after (may be null): the film stage waits for it (the previous
+// wave's films, on another stream); film_done (may be null) is recorded after
+// this wave's films.
 void launch_wave_multi(const SceneView &S, const MergedJobs &M, const Queues &Q, long long g0, int n,
-                       const LaunchCfg &cfg, cudaStream_t st, Profiler *prof);
+                       const LaunchCfg &cfg, cudaStream_t st, Profiler *prof, cudaEvent_t film_after = nullptr,
+                       cudaEvent_t film_done = nullptr);
 void upload_halton_tables_multi(const HaltonTables &T, cudaStream_t st);
 void launch_tonemap(const float *film, int W, int H, float gamma, uint8_t *out, cudaStream_t st);
 

@@ -13,12 +13,14 @@ void upload_halton_tables_multi(const HaltonTables &T, cudaStream_t st) {
 }
 
 void launch_wave_multi(const SceneView &S, const MergedJobs &M, const Queues &Q, long long g0, int n,
-                       const LaunchCfg &cfg, cudaStream_t st, Profiler *prof) {
+                       const LaunchCfg &cfg, cudaStream_t st, Profiler *prof, cudaEvent_t film_after,
+                       cudaEvent_t film_done) {
   Profiler dummy;
   Profiler &P = prof ? *prof : dummy;
   DeviceJob none;
   std::memset(&none, 0, sizeof none);
   launch_wave_stages<true>(S, none, M.T, Q, g0, n, M.LN, M.bounces, cfg, st, P);
+  if (film_after) cudaStreamWaitEvent(st, film_after, 0);
   P.begin(STAGE_FILM, st);
   const long long g1 = g0 + n;
   for (size_t k = 0; k + 1 < M.start.size(); ++k) {
@@ -28,6 +30,7 @@ void launch_wave_multi(const SceneView &S, const MergedJobs &M, const Queues &Q,
     P.count(STAGE_FILM, 1);
   }
   P.end(st);
+  if (film_done) cudaEventRecord(film_done, st);
 }
 
 }  // namespace pt
