@@ -261,6 +261,14 @@ int pt_version(void);
  * light discovery).  Host arrays are copied; the caller keeps ownership. */
 int pt_scene_upload(void *ctx, const pt_scene_desc *desc, int32_t *scene_id);
 int pt_scene_release(void *ctx, int32_t scene_id);
+
+/* Host-only build of a scene's BVH (no device, no context; no reference
+ * counterpart): validates the description and builds the BVH4 exactly as
+ * pt_scene_upload does, with `threads` workers for the mesh BVHs (0: all
+ * hardware threads).  out5: BVH4 nodes, leaf items, depth, a 64-bit content
+ * hash of nodes and items (same hash, same tree, whatever the thread count),
+ * build time in microseconds.  Errors: pt_last_error(NULL, ...). */
+int pt_bvh_build(const pt_scene_desc *desc, int32_t threads, int64_t *out5);
 /* Counts of the flattened scene: [0] triangles, [1] quads, [2] spheres,
  * [3] BVH4 nodes, [4] lights, [5] device bytes. */
 int pt_scene_info(void *ctx, int32_t scene_id, int64_t *out6);

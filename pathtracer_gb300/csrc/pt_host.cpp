@@ -13,6 +13,7 @@
 #include <memory>
 #include <mutex>
 #include <numeric>
+#include <thread>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -195,6 +196,7 @@ struct BNode {
 
 struct Builder {
   const pt_scene_desc *d;
+  int threads = 0;               // mesh BVH build workers (0: hardware threads)
   std::vector<int> obj_motion;   // per object: motion index + 1 (0: static)
   std::vector<BNode> nodes;
   std::vector<int> inst_motion;  // per node: motion index + 1 if it roots a moving object's subtree
@@ -207,7 +209,29 @@ struct Builder {
   // MeshBVHNode (meshBVH.cpp:6-55): box of the triangles +- 1e-3; leaf at
   // <= 4 triangles; otherwise split at the median of the centroids along
   // the longest axis, sorted with std::sort and the reference's comparator.
-  int build_mesh(int mesh, std::vector<int> ids) {
+  // The centroids are computed once per mesh with the comparator's own
+  // arithmetic ((v0 + v1 + v2) / 3.0f per component), so the sort sees the
+  // same comparisons and gives the same order.  Large subtrees are built on
+  // worker threads into their own arrays and spliced back in preorder: the
+  // tree (node numbering, leaf order) is the one the sequential recursion
+  // builds.
+  struct Part {
+    std::vector<BNode> nodes;
+    std::vector<int> prims;
+  };
+
+  void mesh_centroids(int mesh, std::vector<float> cen[3]) const {
+    const pt_mesh_desc &m = d->meshes[mesh];
+    for (int a = 0; a < 3; ++a) cen[a].resize(m.n_triangles);
+    for (int t = 0; t < m.n_triangles; ++t) {
+      const float *p0 = pos(mesh, m.indices[3 * t]), *p1 = pos(mesh, m.indices[3 * t + 1]),
+                  *p2 = pos(mesh, m.indices[3 * t + 2]);
+      for (int a = 0; a < 3; ++a) cen[a][t] = ((p0[a] + p1[a]) + p2[a]) / 3.0f;
+    }
+  }
+
+  void build_mesh_part(int mesh, std::vector<int> ids, const std::vector<float> *cen, Part &out,
+                       int par_depth) const {
     const pt_mesh_desc &m = d->meshes[mesh];
     Box b = box_empty();
     for (int id : ids)
@@ -224,31 +248,89 @@ struct Builder {
       pb.lo[a] = b.lo[a] - eps;
       pb.hi[a] = b.hi[a] + eps;
     }
-    int me = (int)nodes.size();
-    nodes.push_back(BNode());
-    nodes[me].box = pb;
-    int count = (int)ids.size();
+    const int me = (int)out.nodes.size();
+    out.nodes.push_back(BNode());
+    out.nodes[me].box = pb;
+    const int count = (int)ids.size();
     if (count <= 4) {
-      nodes[me].first = (int)leaf_prims.size();
-      nodes[me].count = count;
-      for (int id : ids) leaf_prims.push_back(tri_base[mesh] + id);
-      return me;
+      out.nodes[me].first = (int)out.prims.size();
+      out.nodes[me].count = count;
+      for (int id : ids) out.prims.push_back(tri_base[mesh] + id);
+      return;
     }
     float ext[3] = {b.hi[0] - b.lo[0], b.hi[1] - b.lo[1], b.hi[2] - b.lo[2]};
-    int axis = ext[0] > ext[1] && ext[0] > ext[2] ? 0 : ext[1] > ext[2] ? 1 : 2;
-    auto centroid = [&](int t) {
-      // (v0 + v1 + v2) / 3.0f, component-wise as the reference's vec ops
-      const float *a = pos(mesh, m.indices[3 * t]), *bb = pos(mesh, m.indices[3 * t + 1]),
-                  *c = pos(mesh, m.indices[3 * t + 2]);
-      return ((a[axis] + bb[axis]) + c[axis]) / 3.0f;
+    const int axis = ext[0] > ext[1] && ext[0] > ext[2] ? 0 : ext[1] > ext[2] ? 1 : 2;
+    const std::vector<float> &c = cen[axis];
+    std::sort(ids.begin(), ids.end(), [&](int x, int y) { return c[x] < c[y]; });
+    const int mid = count / 2;
+    std::vector<int> lids(ids.begin(), ids.begin() + mid), rids(ids.begin() + mid, ids.end());
+    ids.clear();
+    ids.shrink_to_fit();
+    if (par_depth > 0 && count > (1 << 15)) {
+      Part lp, rp;
+      std::thread th([&] { build_mesh_part(mesh, std::move(lids), cen, lp, par_depth - 1); });
+      build_mesh_part(mesh, std::move(rids), cen, rp, par_depth - 1);
+      th.join();
+      splice(out, me, lp, rp);
+    } else {
+      const int l = (int)out.nodes.size();
+      build_mesh_part(mesh, std::move(lids), cen, out, 0);
+      const int r = (int)out.nodes.size();
+      build_mesh_part(mesh, std::move(rids), cen, out, 0);
+      out.nodes[me].left = l;
+      out.nodes[me].right = r;
+    }
+  }
+
+  // Appends the left then the right subtree (each rooted at its index 0)
+  // behind node `me`, renumbering nodes and leaf ranges.
+  static void splice(Part &out, int me, const Part &lp, const Part &rp) {
+    auto append = [&](const Part &p) {
+      const int nb = (int)out.nodes.size(), pb = (int)out.prims.size();
+      for (BNode n : p.nodes) {
+        if (n.left >= 0) {
+          n.left += nb;
+          n.right += nb;
+        } else {
+          n.first += pb;
+        }
+        out.nodes.push_back(n);
+      }
+      out.prims.insert(out.prims.end(), p.prims.begin(), p.prims.end());
+      return nb;
     };
-    std::sort(ids.begin(), ids.end(), [&](int x, int y) { return centroid(x) < centroid(y); });
-    int mid = count / 2;
-    int l = build_mesh(mesh, std::vector<int>(ids.begin(), ids.begin() + mid));
-    int r = build_mesh(mesh, std::vector<int>(ids.begin() + mid, ids.end()));
-    nodes[me].left = l;
-    nodes[me].right = r;
-    return me;
+    const int l = append(lp);
+    const int r = append(rp);
+    out.nodes[me].left = l;
+    out.nodes[me].right = r;
+  }
+
+  int build_mesh(int mesh, std::vector<int> ids) {
+    std::vector<float> cen[3];
+    mesh_centroids(mesh, cen);
+    unsigned hw = threads > 0 ? (unsigned)threads : std::max(1u, std::thread::hardware_concurrency());
+    int par_depth = 0;
+    while ((1u << par_depth) < hw && par_depth < 6) ++par_depth;
+    if (ids.size() <= (1u << 16)) par_depth = 0;
+    Part p;
+    build_mesh_part(mesh, std::move(ids), cen, p, par_depth);
+    Part top;
+    top.nodes = std::move(nodes);
+    top.prims = std::move(leaf_prims);
+    const int root = (int)top.nodes.size(), pb = (int)top.prims.size();
+    for (BNode n : p.nodes) {
+      if (n.left >= 0) {
+        n.left += root;
+        n.right += root;
+      } else {
+        n.first += pb;
+      }
+      top.nodes.push_back(n);
+    }
+    top.prims.insert(top.prims.end(), p.prims.begin(), p.prims.end());
+    nodes = std::move(top.nodes);
+    leaf_prims = std::move(top.prims);
+    return root;
   }
 
   Box object_box(int o) const {
@@ -437,12 +519,22 @@ static T *dupload(const std::vector<T> &v, std::vector<void *> &owned, cudaStrea
   return static_cast<T *>(p);
 }
 
-std::unique_ptr<Scene> build_scene(const pt_scene_desc *d, cudaStream_t st) {
+static uint64_t fnv1a(const void *p, size_t n, uint64_t h) {
+  const unsigned char *b = static_cast<const unsigned char *>(p);
+  for (size_t i = 0; i < n; ++i) h = (h ^ b[i]) * 0x100000001b3ull;
+  return h;
+}
+
+// Builds a scene; with device = false only the host part (validation, BVH,
+// tables) runs, without touching the GPU.  threads: worker threads of the
+// mesh BVH build (0: all hardware threads).
+std::unique_ptr<Scene> build_scene(const pt_scene_desc *d, cudaStream_t st, bool device, int threads) {
   if (!d) fail(PT_ERR_INVALID, "null scene description");
   if (d->n_objects <= 0) fail(PT_ERR_INVALID, "scene has no objects");  // renderManager.hpp:64
   auto S = std::make_unique<Scene>();
   Builder B;
   B.d = d;
+  B.threads = threads;
   for (int m = 0; m < d->n_meshes; ++m) {
     const pt_mesh_desc &md = d->meshes[m];
     if (md.n_triangles < 0 || (md.n_triangles > 0 && (!md.positions || !md.indices)))
@@ -741,12 +833,19 @@ std::unique_ptr<Scene> build_scene(const pt_scene_desc *d, cudaStream_t st) {
     S->env_h = H;
   }
 
+  // content hash of the BVH (nodes and leaf items): equal hashes, equal trees
+  S->bvh_hash = fnv1a(items.data(), items.size() * sizeof(Item),
+                      fnv1a(out.nodes.data(), out.nodes.size() * sizeof(Bvh4Node), 0xcbf29ce484222325ull));
+  S->n_nodes = (int64_t)out.nodes.size();
+  S->n_items = (int64_t)items.size();
+
   // upload
-  S->nodes = dupload(out.nodes, S->owned, st);
-  S->items = dupload(items, S->owned, st);
-  S->shade = dupload(shade, S->owned, st);
-  S->materials = dupload(mats, S->owned, st);
-  S->lights = dupload(lights, S->owned, st);
+  auto up = [&](const auto &v) { return device ? dupload(v, S->owned, st) : nullptr; };
+  S->nodes = up(out.nodes);
+  S->items = up(items);
+  S->shade = up(shade);
+  S->materials = up(mats);
+  S->lights = up(lights);
   SceneView &V = S->view;
   std::memset(&V, 0, sizeof V);
   V.nodes = S->nodes;
@@ -759,18 +858,18 @@ std::unique_ptr<Scene> build_scene(const pt_scene_desc *d, cudaStream_t st) {
   V.n_prims = n_prims;
   for (int c = 0; c < 3; ++c) V.bg[c] = d->bg_color[c];
   if (d->env) {
-    V.env.texels = dupload(tex, S->owned, st);
-    V.env.alias_prob = dupload(aprob, S->owned, st);
-    V.env.alias_idx = dupload(aidx, S->owned, st);
-    V.env.pdf = dupload(apdf, S->owned, st);
+    V.env.texels = up(tex);
+    V.env.alias_prob = up(aprob);
+    V.env.alias_idx = up(aidx);
+    V.env.pdf = up(apdf);
     V.env.width = d->env->width;
     V.env.height = d->env->height;
     V.env.intensity = d->env->intensity;
     V.env.present = 1;
   }
   if (!motion.empty()) {
-    V.motion = dupload(motion, S->owned, st);
-    V.node_motion = dupload(out.node_motion, S->owned, st);
+    V.motion = up(motion);
+    V.node_motion = up(out.node_motion);
     V.has_motion = 1;
     S->shutter_max = d->shutter_max;
   }
@@ -794,7 +893,7 @@ std::unique_ptr<Scene> build_scene(const pt_scene_desc *d, cudaStream_t st) {
   bytes += mats.size() * sizeof(MatRec) + lights.size() * sizeof(LightRec);
   bytes += tex.size() * sizeof(float4) + aprob.size() * 12;
   S->device_bytes = bytes;
-  cuda_check(cudaStreamSynchronize(st), "scene upload");
+  if (device) cuda_check(cudaStreamSynchronize(st), "scene upload");
   return S;
 }
 
@@ -1183,7 +1282,7 @@ int pt_scene_upload(void *ctx, const pt_scene_desc *desc, int32_t *scene_id) {
     c = as_ctx(ctx);
     if (!scene_id) fail(PT_ERR_INVALID, "null scene_id");
     cuda_check(cudaSetDevice(c->device), "cudaSetDevice");
-    auto S = build_scene(desc, c->stream);
+    auto S = build_scene(desc, c->stream, true, 0);
     int id = c->next_scene++;
     c->scenes[id] = std::move(S);
     *scene_id = id;
@@ -1210,6 +1309,21 @@ int pt_scene_info(void *ctx, int32_t scene_id, int64_t *out6) {
     out6[3] = S->view.n_nodes;
     out6[4] = S->view.n_lights;
     out6[5] = (int64_t)S->device_bytes;
+  });
+}
+
+int pt_bvh_build(const pt_scene_desc *desc, int32_t threads, int64_t *out5) {
+  PT_GUARD(nullptr, {
+    if (!out5) fail(PT_ERR_INVALID, "null output");
+    auto t0 = std::chrono::steady_clock::now();
+    auto S = build_scene(desc, nullptr, false, threads);
+    auto t1 = std::chrono::steady_clock::now();
+    out5[0] = S->n_nodes;
+    out5[1] = S->n_items;
+    out5[2] = S->bvh_depth;
+    uint64_t h = S->bvh_hash;
+    std::memcpy(&out5[3], &h, sizeof h);
+    out5[4] = (int64_t)std::chrono::duration_cast<std::chrono::microseconds>(t1 - t0).count();
   });
 }
 

@@ -44,10 +44,12 @@ struct Scene {
   unsigned family_mask = 0;  // BSDF families (material types 0..6) present
   float shutter_max = 0.f;   // moving objects' boxes cover [0, shutter_max]
   size_t device_bytes = 0;
+  uint64_t bvh_hash = 0;     // content hash of the BVH4 nodes and leaf items
+  int64_t n_nodes = 0, n_items = 0;
   ~Scene();
 };
 
-std::unique_ptr<Scene> build_scene(const pt_scene_desc *d, cudaStream_t st);
+std::unique_ptr<Scene> build_scene(const pt_scene_desc *d, cudaStream_t st, bool device, int threads);
 
 // Device buffers of one merged group of a batch (the jobs of one scene with
 // the same light-sample count), reused across batched renders.

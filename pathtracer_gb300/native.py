@@ -31,7 +31,8 @@ ENV_UNIFORM, ENV_ALIAS = 0, 1
 # exported symbols of the C-ABI, in header order
 EXPORTS = [
     "pt_create", "pt_destroy", "pt_last_error", "pt_version", "pt_scene_upload", "pt_scene_release",
-    "pt_scene_info", "pt_render", "pt_render_device", "pt_render_device_noalloc", "pt_profile_begin",
+    "pt_bvh_build", "pt_scene_info", "pt_render", "pt_render_device", "pt_render_device_noalloc",
+    "pt_profile_begin",
     "pt_profile_end", "pt_tonemap", "pt_sampler_eval", "pt_trace_closest",
     "pt_trace_any", "pt_bsdf_eval", "pt_bsdf_sample", "pt_render_batch", "pt_autotune", "pt_server_create",
     "pt_server_destroy", "pt_submit", "pt_server_step", "pt_poll", "pt_cancel",
@@ -143,6 +144,7 @@ def load() -> C.CDLL:
         "pt_version": [],
         "pt_scene_upload": [vp, C.POINTER(SceneDesc), i32p],
         "pt_scene_release": [vp, C.c_int32],
+        "pt_bvh_build": [C.POINTER(SceneDesc), C.c_int32, C.POINTER(C.c_int64)],
         "pt_scene_info": [vp, C.c_int32, C.POINTER(C.c_int64)],
         "pt_render": [vp, C.POINTER(JobDesc), f32p, C.POINTER(Stats)],
         "pt_render_device": [vp, C.POINTER(JobDesc), vp, C.c_int, C.POINTER(Stats)],
@@ -439,6 +441,20 @@ class Renderer:
                                             _ptr(ok, C.c_uint8), _ptr(wi, C.c_float), _ptr(att, C.c_float),
                                             _ptr(pdf, C.c_float), _ptr(ty, C.c_uint32)))
         return ok.astype(bool), wi, att, pdf, ty
+
+
+def bvh_build(scene, threads: int = 0) -> dict:
+    """pt_bvh_build: the scene's BVH4 built on the host only (no GPU)."""
+    lib = load()
+    sb = make_scene_desc(scene)
+    out = (C.c_int64 * 5)()
+    rc = lib.pt_bvh_build(C.byref(sb.desc), threads, out)
+    if rc != PT_OK:
+        buf = C.create_string_buffer(512)
+        lib.pt_last_error(None, buf, 512)
+        raise PtError(rc, buf.value.decode())
+    return {"nodes": out[0], "items": out[1], "depth": out[2], "hash": out[3] & 0xffffffffffffffff,
+            "build_us": out[4]}
 
 
 REQ_QUEUED, REQ_RUNNING, REQ_DONE, REQ_CANCELLED, REQ_FAILED = range(5)

@@ -1,0 +1,38 @@
+"""Host BVH build (pt_bvh_build, no GPU): the parallel mesh build gives the
+tree the sequential recursion gives, and invalid scenes fail loudly."""
+from __future__ import annotations
+
+import pytest
+
+from pathtracer_gb300 import native as N
+from pathtracer_gb300 import scene as S
+
+
+def test_parallel_build_equals_sequential():
+    sc, _ = S.rough_glass(subdiv=7, env_w=16, env_h=8, seed=3)
+    one = N.bvh_build(sc, threads=1)
+    many = N.bvh_build(sc, threads=8)
+    assert one["hash"] == many["hash"]
+    assert (one["nodes"], one["items"], one["depth"]) == (many["nodes"], many["items"], many["depth"])
+    assert one["items"] == 327680 + 1  # every triangle and the ground quad, once
+
+
+def test_build_is_deterministic_and_sees_motion():
+    static, _ = S.material_divergence(subdiv=1, seed=2)
+    a = N.bvh_build(static)
+    b = N.bvh_build(static)
+    assert a["hash"] == b["hash"]
+    moving, _ = S.material_divergence(subdiv=1, seed=2)
+    S.with_motion(moving, seed=4)
+    c = N.bvh_build(moving)
+    assert c["hash"] != a["hash"]  # swept root boxes, per-object subtrees
+
+
+def test_invalid_scene_fails():
+    sc, _ = S.cornell_icosphere(1)
+    sc.meshes[0].indices[0, 0] = 10 ** 6  # vertex index out of range
+    with pytest.raises(N.PtError):
+        N.bvh_build(sc)
+    empty = S.Scene()
+    with pytest.raises(N.PtError):
+        N.bvh_build(empty)
