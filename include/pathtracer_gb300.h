@@ -269,6 +269,19 @@ int pt_scene_release(void *ctx, int32_t scene_id);
  * hash of nodes and items (same hash, same tree, whatever the thread count),
  * build time in microseconds.  Errors: pt_last_error(NULL, ...). */
 int pt_bvh_build(const pt_scene_desc *desc, int32_t threads, int64_t *out5);
+
+/* OBJ ingest: loadOBJMesh (src/mesh_io/meshLoader.cpp:7-58), which reads the
+ * file with tinyobjloader.  "v", "vn", "vt" and "f" records; face vertices
+ * "v", "v/vt", "v//vn", "v/vt/vn" with 1-based or negative indices; an
+ * absent normal / uv index is -1 (a face without normals is shaded flat);
+ * quads split along the shorter diagonal as tinyobjloader does, longer
+ * polygons fanned from their first vertex; other records ignored.  Fills
+ * *mesh (material = -1, to be set by the caller) with arrays owned by the
+ * library until pt_obj_free.  No context; errors (missing file:
+ * PT_ERR_NOT_FOUND, malformed record or out-of-range index:
+ * PT_ERR_INVALID) through pt_last_error(NULL, ...). */
+int pt_obj_load(const char *path, pt_mesh_desc *mesh);
+int pt_obj_free(pt_mesh_desc *mesh);
 /* Counts of the flattened scene: [0] triangles, [1] quads, [2] spheres,
  * [3] BVH4 nodes, [4] lights, [5] device bytes. */
 int pt_scene_info(void *ctx, int32_t scene_id, int64_t *out6);

@@ -929,6 +929,11 @@ Context::Context(int dev) : device(dev) {
 Context::~Context() {
   cudaSetDevice(device);
   free_queues();
+  for (void *p : qmem2) cudaFree(p);
+  if (stream2) cudaStreamDestroy(stream2);
+  if (ev_fork) cudaEventDestroy(ev_fork);
+  if (ev_join) cudaEventDestroy(ev_join);
+  for (cudaEvent_t e : film_ev) cudaEventDestroy(e);
   for (auto &kv : perms) cudaFree(kv.second);
   if (d_film) cudaFree(d_film);
   if (d_offsets) cudaFree(d_offsets);
@@ -945,13 +950,14 @@ void Context::free_queues() {
   q_ln = 0;
 }
 
-void Context::ensure_queues(int cap, int ln) {
-  if (cap <= q_cap && ln <= q_ln) return;
-  free_queues();
+// Work queues for `cap` paths per wave and `ln` light samples per vertex.
+static void alloc_queues(Queues &Q, std::vector<void *> &mem, int cap, int ln, int *d_err) {
+  for (void *p : mem) cudaFree(p);
+  mem.clear();
   auto alloc = [&](size_t bytes) {
     void *p = nullptr;
     cuda_check(cudaMalloc(&p, bytes), "cudaMalloc(queues)");
-    qmem.push_back(p);
+    mem.push_back(p);
     return p;
   };
   const size_t c = (size_t)cap;
@@ -975,8 +981,24 @@ void Context::ensure_queues(int cap, int ln) {
   Q.seg = (int *)alloc(sizeof(int) * (PT_SORT_BINS + 1));
   Q.job = (int *)alloc(c * 4);
   Q.err = d_err;
+}
+
+void Context::ensure_queues(int cap, int ln) {
+  if (cap <= q_cap && ln <= q_ln) return;
+  free_queues();
+  alloc_queues(Q, qmem, cap, ln, d_err);
   q_cap = cap;
   q_ln = ln;
+}
+
+void Context::ensure_queues2(int cap, int ln) {
+  if (!stream2) cuda_check(cudaStreamCreateWithFlags(&stream2, cudaStreamNonBlocking), "cudaStreamCreate");
+  if (!ev_fork) cuda_check(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming), "cudaEventCreate");
+  if (!ev_join) cuda_check(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming), "cudaEventCreate");
+  if (cap <= q2_cap && ln <= q2_ln) return;
+  alloc_queues(Q2, qmem2, cap, ln, d_err);
+  q2_cap = cap;
+  q2_ln = ln;
 }
 
 const uint16_t *Context::perm_for(uint32_t seed) {
@@ -1129,9 +1151,31 @@ void Context::render_device(const pt_job_desc &j, float *d_film, pt_stats *stats
   cudaEventRecord(e0, stream);
   LaunchCfg lc = cfg;
   lc.family_mask = S->family_mask;
-  for (long long g0 = 0; g0 < total; g0 += n) {
-    int cnt = (int)std::min<long long>(n, total - g0);
-    launch_wave(S->view, J, Q, g0, cnt, d_film, lc, stream, &prof);
+  const long long waves = (total + n - 1) / n;
+  if (waves == 1) {
+    launch_wave(S->view, J, Q, 0, (int)total, d_film, lc, stream, &prof);
+  } else {
+    // consecutive waves alternate between two queue sets on two streams so
+    // that one wave's sparse last bounces overlap the next wave's first ones;
+    // the film stages stay in wave order (event chain)
+    ensure_queues2(n, LN);
+    while ((long long)film_ev.size() < waves) {
+      cudaEvent_t ev;
+      cuda_check(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "cudaEventCreate");
+      film_ev.push_back(ev);
+    }
+    cuda_check(cudaMemsetAsync(Q2.stats, 0, 64, stream), "memset stats");
+    cudaEventRecord(ev_fork, stream);
+    cudaStreamWaitEvent(stream2, ev_fork, 0);
+    int w = 0;
+    for (long long g0 = 0; g0 < total; g0 += n, ++w) {
+      const int cnt = (int)std::min<long long>(n, total - g0);
+      const bool odd = (w & 1) != 0;
+      launch_wave(S->view, J, odd ? Q2 : Q, g0, cnt, d_film, lc, odd ? stream2 : stream, &prof,
+                  w > 0 ? film_ev[w - 1] : nullptr, film_ev[w]);
+    }
+    cudaEventRecord(ev_join, stream2);
+    cudaStreamWaitEvent(stream, ev_join, 0);
   }
   cudaEventRecord(e1, stream);
   cuda_check(cudaGetLastError(), "launch");
@@ -1147,6 +1191,11 @@ void Context::render_device(const pt_job_desc &j, float *d_film, pt_stats *stats
   if (stats) {
     unsigned long long h[4];
     cuda_check(cudaMemcpy(h, Q.stats, sizeof h, cudaMemcpyDeviceToHost), "read stats");
+    if (waves > 1) {
+      unsigned long long h2[4];
+      cuda_check(cudaMemcpy(h2, Q2.stats, sizeof h2, cudaMemcpyDeviceToHost), "read stats");
+      for (int k = 0; k < 4; ++k) h[k] += h2[k];
+    }
     float ms = 0.f;
     cudaEventElapsedTime(&ms, e0, e1);
     stats->paths = h[0];
@@ -1192,6 +1241,10 @@ static int set_error(Context *c, int code, const std::string &msg) {
   g_last_error = msg;
   return code;
 }
+
+namespace pt {
+int record_error(int code, const std::string &msg) { return set_error(nullptr, code, msg); }
+}  // namespace pt
 
 #define PT_GUARD(ctxptr, body)                                   \
   try {                                                          \

@@ -28,6 +28,9 @@ MatRec derive_material(const pt_material_desc &m);
 CameraView make_camera(const pt_camera_desc &c);
 std::vector<float2> make_offsets(const pt_job_desc &j);
 void set_window(JobView &v, const pt_job_desc &j);
+// Records an error for pt_last_error(NULL, ...) (entry points without a
+// context); returns code.
+int record_error(int code, const std::string &msg);
 void validate_job(const pt_job_desc &j);
 
 // A flattened scene resident in HBM.
@@ -100,6 +103,14 @@ struct Context {
   Queues Q{};
   std::vector<void *> qmem;
   int q_cap = 0, q_ln = 0;
+  // second queue set and stream: consecutive waves of one render overlap
+  Queues Q2{};
+  std::vector<void *> qmem2;
+  int q2_cap = 0, q2_ln = 0;
+  cudaStream_t stream2 = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  std::vector<cudaEvent_t> film_ev;
+  void ensure_queues2(int cap, int ln);
   float *d_film = nullptr;
   size_t film_cap = 0;
   float2 *d_offsets = nullptr;

@@ -106,8 +106,11 @@ void launch_bsdf_eval(const MatRec *m, int n, const float *wo, const float *wi, 
 void launch_bsdf_sample(const MatRec *m, int n, const float *wo, const float *nrm,
                         const uint8_t *front, const float *uc, const float *u, uint8_t *ok,
                         float *wi, float *att, float *pdf, uint32_t *type, cudaStream_t st);
+// film_after (may be null): the film stage waits for it; film_done (may be
+// null) is recorded after this wave's film stage (wave order across streams).
 void launch_wave(const SceneView &S, const DeviceJob &J, const Queues &Q, long long g0, int n,
-                 float *film, const LaunchCfg &cfg, cudaStream_t st, Profiler *prof);
+                 float *film, const LaunchCfg &cfg, cudaStream_t st, Profiler *prof,
+                 cudaEvent_t film_after = nullptr, cudaEvent_t film_done = nullptr);
 // Job-independent stages (pt_kernels.cu), also used by merged waves.
 void launch_sort(const SceneView &S, const Queues &Q, int qsel, const LaunchCfg &cfg, cudaStream_t st);
 void launch_shadow(const SceneView &S, const Queues &Q, int LN, const LaunchCfg &cfg, cudaStream_t st);

@@ -31,7 +31,7 @@ ENV_UNIFORM, ENV_ALIAS = 0, 1
 # exported symbols of the C-ABI, in header order
 EXPORTS = [
     "pt_create", "pt_destroy", "pt_last_error", "pt_version", "pt_scene_upload", "pt_scene_release",
-    "pt_bvh_build", "pt_scene_info", "pt_render", "pt_render_device", "pt_render_device_noalloc",
+    "pt_bvh_build", "pt_obj_load", "pt_obj_free", "pt_scene_info", "pt_render", "pt_render_device", "pt_render_device_noalloc",
     "pt_profile_begin",
     "pt_profile_end", "pt_tonemap", "pt_sampler_eval", "pt_trace_closest",
     "pt_trace_any", "pt_bsdf_eval", "pt_bsdf_sample", "pt_render_batch", "pt_autotune", "pt_server_create",
@@ -145,6 +145,8 @@ def load() -> C.CDLL:
         "pt_scene_upload": [vp, C.POINTER(SceneDesc), i32p],
         "pt_scene_release": [vp, C.c_int32],
         "pt_bvh_build": [C.POINTER(SceneDesc), C.c_int32, C.POINTER(C.c_int64)],
+        "pt_obj_load": [C.c_char_p, C.POINTER(MeshDesc)],
+        "pt_obj_free": [C.POINTER(MeshDesc)],
         "pt_scene_info": [vp, C.c_int32, C.POINTER(C.c_int64)],
         "pt_render": [vp, C.POINTER(JobDesc), f32p, C.POINTER(Stats)],
         "pt_render_device": [vp, C.POINTER(JobDesc), vp, C.c_int, C.POINTER(Stats)],
@@ -455,6 +457,31 @@ def bvh_build(scene, threads: int = 0) -> dict:
         raise PtError(rc, buf.value.decode())
     return {"nodes": out[0], "items": out[1], "depth": out[2], "hash": out[3] & 0xffffffffffffffff,
             "build_us": out[4]}
+
+
+def obj_load(path) -> dict:
+    """pt_obj_load: an OBJ file as numpy arrays (positions, normals, uvs,
+    indices, normal_indices, uv_indices; -1 where a face has no normal/uv)."""
+    lib = load()
+    md = MeshDesc()
+    rc = lib.pt_obj_load(str(path).encode(), C.byref(md))
+    if rc != PT_OK:
+        buf = C.create_string_buffer(512)
+        lib.pt_last_error(None, buf, 512)
+        raise PtError(rc, buf.value.decode())
+    try:
+        def arr(ptr, n, w, dt):
+            if not ptr or n == 0:
+                return np.zeros((0, w), dt)
+            return np.ctypeslib.as_array(ptr, shape=(n * w,)).reshape(n, w).astype(dt, copy=True)
+        return {"positions": arr(md.positions, md.n_positions, 3, np.float32),
+                "normals": arr(md.normals, md.n_normals, 3, np.float32),
+                "uvs": arr(md.uvs, md.n_uvs, 2, np.float32),
+                "indices": arr(md.indices, md.n_triangles, 3, np.int32),
+                "normal_indices": arr(md.normal_indices, md.n_triangles, 3, np.int32),
+                "uv_indices": arr(md.uv_indices, md.n_triangles, 3, np.int32)}
+    finally:
+        lib.pt_obj_free(C.byref(md))
 
 
 REQ_QUEUED, REQ_RUNNING, REQ_DONE, REQ_CANCELLED, REQ_FAILED = range(5)

@@ -163,3 +163,26 @@ def test_server_admission_by_budget_and_cancel(renderer, scenes):
     assert srv.poll(c)[0] == N.REQ_CANCELLED
     srv.close()
     assert np.array_equal(res[a][0], res[b][0])
+
+
+def test_multi_wave_render_equals_single_wave(renderer, scenes, monkeypatch):
+    # a context with a tiny wave capacity renders the job in many waves that
+    # overlap on two queue sets; films add samples in sample order, so the
+    # result has the single-wave bits
+    monkeypatch.setenv("PT_WAVE_PATHS", "4096")
+    small = N.Renderer(0)
+    monkeypatch.delenv("PT_WAVE_PATHS")
+    cb, cam = S.cornell_icosphere(3)
+    md, cam_md = S.material_divergence(subdiv=2, seed=3, aspect=1.0)
+    for sc, c, kw in ((cb, cam, {}), (md, cam_md, {"sampler": N.SAMPLER_STRATIFIED})):
+        a_id, b_id = renderer.upload(sc), small.upload(sc)
+        ja = N.job_desc(a_id, c, 40, 36, 4, 2, 6, seed=8, estimator=N.EST_NEE_MIS, **kw)
+        jb = N.job_desc(b_id, c, 40, 36, 4, 2, 6, seed=8, estimator=N.EST_NEE_MIS, **kw)
+        one, st1 = renderer.render(ja, stats=True)
+        many, st2 = small.render(jb, stats=True)
+        assert st1.paths == st2.paths == 40 * 36 * 8
+        assert st1.rays == st2.rays and st1.shadow_rays == st2.shadow_rays
+        assert np.array_equal(one, many)
+        renderer.release(a_id)
+        small.release(b_id)
+    small.close()
