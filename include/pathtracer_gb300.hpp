@@ -154,8 +154,9 @@ struct MeshData {  // mesh_io/meshData.hpp:6-13
 // Flattened geometry of one object, in world space.
 struct Flat {
   enum Kind { MESH, QUAD, SPHERE } kind = MESH;
-  std::vector<float> pos, nrm;
-  std::vector<int32_t> idx;
+  std::vector<float> pos, nrm;   // positions; normals (a list, see nidx)
+  std::vector<int32_t> idx;      // 3 position indices per triangle
+  std::vector<int32_t> nidx;     // 3 normal indices per triangle (-1: none)
   pt_quad_desc quad{};
   pt_sphere_desc sphere{};
   std::shared_ptr<Material> mat;
@@ -211,16 +212,15 @@ class TriangleMesh : public Hittable {
     Flat f;
     f.kind = Flat::MESH;
     for (auto &p : d.positions) f.pos.insert(f.pos.end(), {p[0], p[1], p[2]});
-    // per-corner normals (normalIndices) are expanded to the position layout
+    // normals stay a list indexed per corner (normalIndices; -1: the face
+    // has none and is shaded with its geometric normal)
     const bool has_n = !d.normals.empty() && d.normalIndices.size() == d.indices.size();
-    if (has_n) f.nrm.assign(f.pos.size(), 0.f);
+    if (has_n)
+      for (auto &n : d.normals) f.nrm.insert(f.nrm.end(), {n[0], n[1], n[2]});
     for (size_t t = 0; t < d.indices.size(); ++t)
       for (int k = 0; k < 3; ++k) {
         f.idx.push_back(d.indices[t][k]);
-        if (has_n) {
-          const vec3 &n = d.normals[d.normalIndices[t][k]];
-          for (int c = 0; c < 3; ++c) f.nrm[3 * d.indices[t][k] + c] = n[c];
-        }
+        if (has_n) f.nidx.push_back(d.normalIndices[t][k]);
       }
     f.mat = m;
     return f;
@@ -332,6 +332,29 @@ class Rotate : public Hittable {
   float r;
 };
 
+// loadOBJMesh (src/mesh_io/meshLoader.cpp:7-58) through pt_obj_load.
+inline std::shared_ptr<TriangleMesh> loadOBJMesh(const std::string &path, std::shared_ptr<Material> mat) {
+  pt_mesh_desc m{};
+  if (pt_obj_load(path.c_str(), &m) != PT_OK) {
+    char buf[512] = {0};
+    pt_last_error(nullptr, buf, sizeof buf);
+    throw std::runtime_error(buf);
+  }
+  MeshData d;
+  for (int i = 0; i < m.n_positions; ++i)
+    d.positions.push_back(vec3{m.positions[3 * i], m.positions[3 * i + 1], m.positions[3 * i + 2]});
+  for (int i = 0; i < m.n_normals; ++i)
+    d.normals.push_back(vec3{m.normals[3 * i], m.normals[3 * i + 1], m.normals[3 * i + 2]});
+  for (int i = 0; i < m.n_uvs; ++i) d.uvs.push_back(vec2{m.uvs[2 * i], m.uvs[2 * i + 1]});
+  for (int t = 0; t < m.n_triangles; ++t) {
+    d.indices.push_back({m.indices[3 * t], m.indices[3 * t + 1], m.indices[3 * t + 2]});
+    d.normalIndices.push_back({m.normal_indices[3 * t], m.normal_indices[3 * t + 1], m.normal_indices[3 * t + 2]});
+    d.uvIndices.push_back({m.uv_indices[3 * t], m.uv_indices[3 * t + 1], m.uv_indices[3 * t + 2]});
+  }
+  pt_obj_free(&m);
+  return std::make_shared<TriangleMesh>(std::move(d), std::move(mat));
+}
+
 class ObjectList {  // base/objectList.hpp
  public:
   void addObject(std::shared_ptr<Hittable> h) { objects.push_back(std::move(h)); }
@@ -392,7 +415,8 @@ struct SceneInfo {
         m.n_positions = (int32_t)(f.pos.size() / 3);
         if (!f.nrm.empty()) {
           m.normals = f.nrm.data();
-          m.n_normals = m.n_positions;
+          m.n_normals = (int32_t)(f.nrm.size() / 3);
+          m.normal_indices = f.nidx.data();
         }
         m.indices = f.idx.data();
         m.n_triangles = (int32_t)(f.idx.size() / 3);
