@@ -528,7 +528,8 @@ static uint64_t fnv1a(const void *p, size_t n, uint64_t h) {
 // Builds a scene; with device = false only the host part (validation, BVH,
 // tables) runs, without touching the GPU.  threads: worker threads of the
 // mesh BVH build (0: all hardware threads).
-std::unique_ptr<Scene> build_scene(const pt_scene_desc *d, cudaStream_t st, bool device, int threads) {
+std::unique_ptr<Scene> build_scene(const pt_scene_desc *d, cudaStream_t st, bool device, int threads,
+                                   int trav_cap) {
   if (!d) fail(PT_ERR_INVALID, "null scene description");
   if (d->n_objects <= 0) fail(PT_ERR_INVALID, "scene has no objects");  // renderManager.hpp:64
   auto S = std::make_unique<Scene>();
@@ -856,6 +857,7 @@ std::unique_ptr<Scene> build_scene(const pt_scene_desc *d, cudaStream_t st, bool
   V.n_lights = (int)lights.size();
   V.n_nodes = (int)out.nodes.size();
   V.n_prims = n_prims;
+  V.trav_cap = trav_cap > 0 ? trav_cap : PT_TRAVERSAL_CAP;
   for (int c = 0; c < 3; ++c) V.bg[c] = d->bg_color[c];
   if (d->env) {
     V.env.texels = up(tex);
@@ -919,6 +921,10 @@ Context::Context(int dev) : device(dev) {
   cfg.family_mask = 0x7f;
   const char *cap = std::getenv("PT_WAVE_PATHS");
   wave_cap = cap ? std::max(1024, std::atoi(cap)) : (1 << 24);
+  // bound on one ray's traversal steps (scenes uploaded by this context);
+  // exceeding it sets the device error flag, reported as PT_ERR_DEVICE
+  const char *tc = std::getenv("PT_TRAVERSAL_CAP");
+  trav_cap = tc ? std::max(1, std::atoi(tc)) : 0;
   const char *srt = std::getenv("PT_SORT_BY_MATERIAL");
   if (srt) cfg.sort_by_material = std::atoi(srt);
   cuda_check(cudaMalloc(&d_err, sizeof(int)), "cudaMalloc(err)");
@@ -1335,7 +1341,7 @@ int pt_scene_upload(void *ctx, const pt_scene_desc *desc, int32_t *scene_id) {
     c = as_ctx(ctx);
     if (!scene_id) fail(PT_ERR_INVALID, "null scene_id");
     cuda_check(cudaSetDevice(c->device), "cudaSetDevice");
-    auto S = build_scene(desc, c->stream, true, 0);
+    auto S = build_scene(desc, c->stream, true, 0, c->trav_cap);
     int id = c->next_scene++;
     c->scenes[id] = std::move(S);
     *scene_id = id;
@@ -1369,7 +1375,7 @@ int pt_bvh_build(const pt_scene_desc *desc, int32_t threads, int64_t *out5) {
   PT_GUARD(nullptr, {
     if (!out5) fail(PT_ERR_INVALID, "null output");
     auto t0 = std::chrono::steady_clock::now();
-    auto S = build_scene(desc, nullptr, false, threads);
+    auto S = build_scene(desc, nullptr, false, threads, 0);
     auto t1 = std::chrono::steady_clock::now();
     out5[0] = S->n_nodes;
     out5[1] = S->n_items;

@@ -52,7 +52,8 @@ struct Scene {
   ~Scene();
 };
 
-std::unique_ptr<Scene> build_scene(const pt_scene_desc *d, cudaStream_t st, bool device, int threads);
+std::unique_ptr<Scene> build_scene(const pt_scene_desc *d, cudaStream_t st, bool device, int threads,
+                                   int trav_cap);
 
 // Device buffers of one merged group of a batch (the jobs of one scene with
 // the same light-sample count), reused across batched renders.
@@ -95,6 +96,7 @@ struct Context {
   KernelInfo kinfo;
   LaunchCfg cfg;
   int wave_cap = 1 << 22;
+  int trav_cap = 0;  // 0: PT_TRAVERSAL_CAP
   std::string last_error;
   std::map<int, std::unique_ptr<Scene>> scenes;
   int next_scene = 1;

@@ -115,6 +115,7 @@ struct SceneView {
   const float4 *motion;
   const int32_t *node_motion;  // per BVH4 node: motion index + 1 of the moving object it roots
   int32_t has_motion;
+  int32_t trav_cap;  // steps one ray's traversal may take before the device error flag is set
 };
 
 // Child references of a BVH4 node entering a moving object's subtree carry
@@ -122,6 +123,8 @@ struct SceneView {
 // reference: items < 2^28 - 8) and continues in the object's frame until it
 // pops it.
 #define PT_INST_BIT (1 << 30)
+// Default bound on the steps of one ray's traversal (SceneView::trav_cap).
+#define PT_TRAVERSAL_CAP (1 << 22)
 #define PT_FRAME_END ((int32_t)0x80000000)
 
 // Camera constants of PerspectiveCamera (camera.cpp:7-35).

@@ -17,7 +17,6 @@
 
 namespace pt {
 
-#define PT_TRAVERSAL_CAP (1 << 22)
 
 struct HitRec {
   float t;
@@ -301,7 +300,7 @@ __device__ __forceinline__ bool trav_node(const SceneView &S, TravRay &R, int32_
 // with what it has.
 template <bool ANY>
 __device__ __forceinline__ bool trav_step(const SceneView &S, TravRay &R, int32_t *stack, int stride, int *err) {
-  if (++R.iters > PT_TRAVERSAL_CAP) {
+  if (++R.iters > S.trav_cap) {
     *err = 2;
     return true;
   }

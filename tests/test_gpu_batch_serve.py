@@ -186,3 +186,30 @@ def test_multi_wave_render_equals_single_wave(renderer, scenes, monkeypatch):
         renderer.release(a_id)
         small.release(b_id)
     small.close()
+
+
+def test_traversal_cap_reports_device_error_and_context_survives(monkeypatch):
+    # failure detection without a fault: a context whose traversal step bound
+    # is tiny makes every ray hit it; the kernels set the device error flag
+    # and return, the call reports PT_ERR_DEVICE, and the context (and the
+    # GPU) stay usable
+    monkeypatch.setenv("PT_TRAVERSAL_CAP", "2")
+    r = N.Renderer(0)
+    monkeypatch.delenv("PT_TRAVERSAL_CAP")
+    sc, cam = S.cornell_icosphere(2)
+    sid = r.upload(sc)
+    job = N.job_desc(sid, cam, 16, 16, 1, 1, 4)
+    with pytest.raises(N.PtError) as e:
+        r.render(job)
+    assert e.value.code == -5
+    with pytest.raises(N.PtError):
+        r.render_batch([job])
+    v = r.sampler_eval(N.SAMPLER_HALTON_NONE, 1, 4, 2)  # the context still works
+    assert np.allclose(v[:, 0], [0.5, 0.25, 0.75, 0.125])
+    r.release(sid)
+    r.close()
+    ok = N.Renderer(0)  # and so does a fresh one
+    sid = ok.upload(sc)
+    assert np.isfinite(ok.render(N.job_desc(sid, cam, 16, 16, 1, 1, 4))).all()
+    ok.release(sid)
+    ok.close()
