@@ -334,6 +334,20 @@ int pt_profile_end(void *ctx, double *stage_ms /*[6]*/, int64_t *stage_launches 
 int pt_tonemap(void *ctx, const float *film_rgb, int32_t width, int32_t height,
                float gamma, uint8_t *rgb8);
 
+/* FrameBuffer::gaussianBlur (framebuffer.cpp:60-129): a k x k Gaussian of
+ * standard deviation sigma (normalised weights, clamp to edge) over the film,
+ * on the GPU; film_out may equal film_in.  Host buffers.  As the reference,
+ * k even or < 3 or sigma < 0 leave the film unchanged (PT_OK); sigma = 0 is
+ * also left unchanged (the reference divides by zero). */
+int pt_gaussian_blur(void *ctx, const float *film_in, float *film_out, int32_t width,
+                     int32_t height, int32_t kernel, float sigma);
+
+/* FrameBuffer::writeToFile's file step (framebuffer.cpp:47-49, stb's PNG
+ * writer): rgb8 as pt_tonemap gives it (row 0 = top) to an 8-bit RGB PNG
+ * (uncompressed deflate blocks).  No context; errors through
+ * pt_last_error(NULL, ...). */
+int pt_write_png(const char *path, const uint8_t *rgb8, int32_t width, int32_t height);
+
 /* ------------------------------------------------- batch test entry points
  * Sampler sequences (HaltonSampler::SampleDimension, sampler.hpp:54-73):
  * out[i * dims + d] = sample of dimension d at sample index first_index + i. */

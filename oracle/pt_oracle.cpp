@@ -1444,6 +1444,39 @@ void or_bsdf_sample(const pt_material_desc *md, int n, const float *wo, const fl
 
 // Renders the job; mean/var are width*height*3, [j][i][c].  recursive != 0
 // selects the recursive REF_NEE restatement (scenes without a medium).
+// FrameBuffer::gaussianBlur (framebuffer.cpp:60-129) over a film laid out
+// [row][column][rgb] (row 0 = bottom, as pixel_color[j][i]).  Returns 0 when
+// it blurred, 1 when the reference would refuse the arguments (film copied).
+int or_gaussian_blur(const float *in, float *out, int W, int H, int kernel, float sigma) {
+  if (kernel % 2 == 0 || kernel < 3 || !(sigma > 0.0f)) {
+    std::memcpy(out, in, sizeof(float) * 3 * (size_t)W * H);
+    return 1;
+  }
+  std::vector<std::vector<float>> k2(kernel, std::vector<float>(kernel));
+  float sum = 0.0f;
+  for (int x = -kernel / 2; x <= kernel / 2; x++)
+    for (int y = -kernel / 2; y <= kernel / 2; y++) {
+      float r = (float)std::sqrt((double)(x * x + y * y));
+      float e = std::exp(-(r * r) / (2 * sigma * sigma));
+      k2[x + kernel / 2][y + kernel / 2] = (float)((double)e / (2 * M_PI * sigma * sigma));
+      sum += k2[x + kernel / 2][y + kernel / 2];
+    }
+  for (auto &row : k2)
+    for (float &v : row) v /= sum;
+  for (int i = 0; i < H; i++)
+    for (int j = 0; j < W; j++) {
+      float c[3] = {0.f, 0.f, 0.f};
+      for (int s = 0; s < kernel; s++)
+        for (int t = 0; t < kernel; t++) {
+          int ix = std::min(std::max(i - kernel / 2 + s, 0), H - 1);
+          int iy = std::min(std::max(j - kernel / 2 + t, 0), W - 1);
+          for (int ch = 0; ch < 3; ++ch) c[ch] += in[3 * ((size_t)ix * W + iy) + ch] * k2[s][t];
+        }
+      for (int ch = 0; ch < 3; ++ch) out[3 * ((size_t)i * W + j) + ch] = c[ch];
+    }
+  return 0;
+}
+
 int or_render(void *s, const pt_job_desc *job, float *mean, float *var, int threads, int recursive) {
   const Scene &S = *static_cast<Scene *>(s);
   const pt_job_desc &j = *job;

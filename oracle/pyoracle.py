@@ -37,6 +37,7 @@ def load():
         lib.or_bsdf_sample.argtypes = [C.POINTER(N.MaterialDesc), C.c_int, f32p, f32p, u8p, f32p, f32p, u8p, f32p,
                                        f32p, f32p, u32p]
         lib.or_render.argtypes = [C.c_void_p, C.POINTER(N.JobDesc), f32p, f32p, C.c_int, C.c_int]
+        lib.or_gaussian_blur.argtypes = [f32p, f32p, C.c_int, C.c_int, C.c_int, C.c_float]
         _lib = lib
     return _lib
 
@@ -107,3 +108,12 @@ def bsdf_sample(mat, wo, nrm, front, uc, u):
                           _p(uc, C.c_float), _p(u, C.c_float), _p(ok, C.c_uint8), _p(wi, C.c_float),
                           _p(att, C.c_float), _p(pdf, C.c_float), _p(ty, C.c_uint32))
     return ok, wi, att, pdf, ty
+
+
+def gaussian_blur(film, kernel, sigma):
+    """FrameBuffer::gaussianBlur restated on the CPU (or_gaussian_blur)."""
+    lib = load()
+    f = np.ascontiguousarray(film, dtype=np.float32)
+    out = np.empty_like(f)
+    lib.or_gaussian_blur(_p(f, C.c_float), _p(out, C.c_float), f.shape[1], f.shape[0], kernel, sigma)
+    return out

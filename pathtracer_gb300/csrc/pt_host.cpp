@@ -519,6 +519,107 @@ static T *dupload(const std::vector<T> &v, std::vector<void *> &owned, cudaStrea
   return static_cast<T *>(p);
 }
 
+// FrameBuffer::gaussianBlur's kernel (framebuffer.cpp:60-87): k x k weights
+// exp(-r^2 / (2 sigma^2)) / (2 pi sigma^2), r = sqrt(x^2 + y^2), divided by
+// their float sum; row-major [s][t].  Empty when the reference refuses the
+// arguments (k even or < 3, sigma < 0; sigma = 0 divides by zero there and
+// is refused here too).
+std::vector<float> gaussian_weights(int k, float sigma) {
+  std::vector<float> w;
+  if (k % 2 == 0 || k < 3 || !(sigma > 0.f)) return w;
+  w.resize((size_t)k * k);
+  float sum = 0.0f;
+  for (int x = -k / 2; x <= k / 2; x++)
+    for (int y = -k / 2; y <= k / 2; y++) {
+      float r = (float)std::sqrt((double)(x * x + y * y));
+      float e = std::exp(-(r * r) / (2 * sigma * sigma));
+      float v = (float)((double)e / (2 * M_PI * sigma * sigma));
+      w[(size_t)(x + k / 2) * k + (y + k / 2)] = v;
+      sum += v;
+    }
+  for (float &v : w) v /= sum;
+  return w;
+}
+
+// Minimal PNG encoder: 8-bit RGB, filter 0 rows, zlib stream of stored
+// (uncompressed) deflate blocks, CRC-32 and Adler-32 from their published
+// definitions (PNG spec, RFC 1950/1951).
+static uint32_t crc32_update(uint32_t c, const unsigned char *p, size_t n) {
+  static uint32_t table[256];
+  static bool init = false;
+  if (!init) {
+    for (uint32_t i = 0; i < 256; ++i) {
+      uint32_t v = i;
+      for (int k = 0; k < 8; ++k) v = (v & 1) ? 0xEDB88320u ^ (v >> 1) : v >> 1;
+      table[i] = v;
+    }
+    init = true;
+  }
+  for (size_t i = 0; i < n; ++i) c = table[(c ^ p[i]) & 0xff] ^ (c >> 8);
+  return c;
+}
+
+void write_png(const char *path, const uint8_t *rgb, int W, int H) {
+  std::vector<unsigned char> raw;
+  raw.reserve((size_t)H * (3 * W + 1));
+  for (int y = 0; y < H; ++y) {
+    raw.push_back(0);
+    raw.insert(raw.end(), rgb + (size_t)y * W * 3, rgb + (size_t)(y + 1) * W * 3);
+  }
+  std::vector<unsigned char> z = {0x78, 0x01};
+  uint32_t a = 1, b = 0;
+  for (unsigned char ch : raw) {
+    a = (a + ch) % 65521u;
+    b = (b + a) % 65521u;
+  }
+  for (size_t off = 0; off < raw.size() || off == 0;) {
+    const size_t len = std::min<size_t>(65535, raw.size() - off);
+    const bool last = off + len >= raw.size();
+    z.push_back(last ? 1 : 0);
+    z.push_back((unsigned char)(len & 0xff));
+    z.push_back((unsigned char)(len >> 8));
+    z.push_back((unsigned char)(~len & 0xff));
+    z.push_back((unsigned char)((~len >> 8) & 0xff));
+    z.insert(z.end(), raw.begin() + off, raw.begin() + off + len);
+    off += len;
+    if (last) break;
+  }
+  const uint32_t adler = (b << 16) | a;
+  for (int s = 24; s >= 0; s -= 8) z.push_back((unsigned char)(adler >> s));
+  FILE *f = std::fopen(path, "wb");
+  if (!f) fail(PT_ERR_INVALID, std::string("cannot write ") + path);
+  auto be32 = [](unsigned char *o, uint32_t v) {
+    o[0] = (unsigned char)(v >> 24); o[1] = (unsigned char)(v >> 16); o[2] = (unsigned char)(v >> 8); o[3] = (unsigned char)v;
+  };
+  auto chunk = [&](const char *type, const unsigned char *data, size_t n) {
+    unsigned char hdr[8];
+    be32(hdr, (uint32_t)n);
+    std::memcpy(hdr + 4, type, 4);
+    uint32_t c = crc32_update(0xffffffffu, hdr + 4, 4);
+    c = crc32_update(c, data, n) ^ 0xffffffffu;
+    unsigned char tail[4];
+    be32(tail, c);
+    std::fwrite(hdr, 1, 8, f);
+    if (n) std::fwrite(data, 1, n, f);
+    std::fwrite(tail, 1, 4, f);
+  };
+  static const unsigned char sig[8] = {0x89, 'P', 'N', 'G', 0x0d, 0x0a, 0x1a, 0x0a};
+  std::fwrite(sig, 1, 8, f);
+  unsigned char ihdr[13];
+  be32(ihdr, (uint32_t)W);
+  be32(ihdr + 4, (uint32_t)H);
+  ihdr[8] = 8;   // bit depth
+  ihdr[9] = 2;   // colour type RGB
+  ihdr[10] = 0;  // deflate
+  ihdr[11] = 0;  // filter method 0
+  ihdr[12] = 0;  // no interlace
+  chunk("IHDR", ihdr, 13);
+  chunk("IDAT", z.data(), z.size());
+  chunk("IEND", nullptr, 0);
+  const bool ok = std::fclose(f) == 0;
+  if (!ok) fail(PT_ERR_INVALID, std::string("cannot write ") + path);
+}
+
 static uint64_t fnv1a(const void *p, size_t n, uint64_t h) {
   const unsigned char *b = static_cast<const unsigned char *>(p);
   for (size_t i = 0; i < n; ++i) h = (h ^ b[i]) * 0x100000001b3ull;
@@ -1434,6 +1535,38 @@ int pt_tonemap(void *ctx, const float *film_rgb, int32_t width, int32_t height, 
     launch_tonemap(df, width, height, gamma, d8, c->stream);
     cuda_check(cudaMemcpyAsync(rgb8, d8, nf, cudaMemcpyDeviceToHost, c->stream), "d2h");
     cuda_check(cudaStreamSynchronize(c->stream), "tonemap");
+  });
+}
+
+int pt_gaussian_blur(void *ctx, const float *film_in, float *film_out, int32_t width, int32_t height, int32_t kernel,
+                     float sigma) {
+  Context *c = static_cast<Context *>(ctx);
+  PT_GUARD(c, {
+    c = as_ctx(ctx);
+    if (!film_in || !film_out || width <= 0 || height <= 0) fail(PT_ERR_INVALID, "bad blur args");
+    const size_t nf = (size_t)width * height * 3;
+    std::vector<float> w = gaussian_weights(kernel, sigma);
+    if (w.empty()) {
+      // FrameBuffer::gaussianBlur returns without blurring (framebuffer.cpp:62-67)
+      if (film_out != film_in) std::memcpy(film_out, film_in, nf * sizeof(float));
+      return PT_OK;
+    }
+    char *buf = (char *)c->scratch(nf * 8 + w.size() * 4);
+    float *din = (float *)buf;
+    float *dout = din + nf;
+    float *dw = dout + nf;
+    cuda_check(cudaMemcpyAsync(din, film_in, nf * 4, cudaMemcpyHostToDevice, c->stream), "h2d");
+    cuda_check(cudaMemcpyAsync(dw, w.data(), w.size() * 4, cudaMemcpyHostToDevice, c->stream), "h2d");
+    launch_gaussian_blur(din, dout, width, height, kernel, dw, c->stream);
+    cuda_check(cudaMemcpyAsync(film_out, dout, nf * 4, cudaMemcpyDeviceToHost, c->stream), "d2h");
+    cuda_check(cudaStreamSynchronize(c->stream), "blur");
+  });
+}
+
+int pt_write_png(const char *path, const uint8_t *rgb8, int32_t width, int32_t height) {
+  PT_GUARD(nullptr, {
+    if (!path || !rgb8 || width <= 0 || height <= 0) fail(PT_ERR_INVALID, "bad png args");
+    write_png(path, rgb8, width, height);
   });
 }
 

@@ -31,6 +31,8 @@ void set_window(JobView &v, const pt_job_desc &j);
 // Records an error for pt_last_error(NULL, ...) (entry points without a
 // context); returns code.
 int record_error(int code, const std::string &msg);
+std::vector<float> gaussian_weights(int k, float sigma);
+void write_png(const char *path, const uint8_t *rgb, int W, int H);
 void validate_job(const pt_job_desc &j);
 
 // A flattened scene resident in HBM.

@@ -308,6 +308,31 @@ __global__ void k_film_combine(float *a, const float *b, float inv, long long n)
     a[i] = (a[i] + b[i]) * inv;
 }
 
+// FrameBuffer::gaussianBlur (framebuffer.cpp:60-129): the full k x k kernel
+// (weights computed on the host exactly as the reference does) over the film
+// with clamp-to-edge, taps summed row-major in the reference's order with
+// rounded, never-fused operations, one thread per pixel.
+__global__ void k_gaussian_blur(const float *in, float *out, int W, int H, int K, const float *w) {
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < W * H; p += gridDim.x * blockDim.x) {
+    const int i = p / W, j = p % W;  // row, column (row 0 = bottom, as the film)
+    float cx = 0.f, cy = 0.f, cz = 0.f;
+    for (int s = 0; s < K; ++s) {
+      const int ix = min(max(i - K / 2 + s, 0), H - 1);
+      for (int t = 0; t < K; ++t) {
+        const int iy = min(max(j - K / 2 + t, 0), W - 1);
+        const float wt = __ldg(w + s * K + t);
+        const float *q = in + 3 * ((size_t)ix * W + iy);
+        cx = __fadd_rn(cx, __fmul_rn(__ldg(q), wt));
+        cy = __fadd_rn(cy, __fmul_rn(__ldg(q + 1), wt));
+        cz = __fadd_rn(cz, __fmul_rn(__ldg(q + 2), wt));
+      }
+    }
+    out[3 * (size_t)p] = cx;
+    out[3 * (size_t)p + 1] = cy;
+    out[3 * (size_t)p + 2] = cz;
+  }
+}
+
 // FrameBuffer::writeToFile pixel path (framebuffer.cpp:27-58).
 __global__ void k_tonemap(const float *film, int W, int H, float inv_gamma, uint8_t *out) {
   for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < W * H * 3; t += gridDim.x * blockDim.x) {
@@ -399,6 +424,10 @@ void launch_film_rmse(const FilmPair *pairs, int npairs, double *partials, doubl
 }
 void launch_film_combine(float *a, const float *b, float inv, long long n, cudaStream_t st) {
   k_film_combine<<<grid_for((int)std::min<long long>(n, 1 << 30), 256, 152 * 8), 256, 0, st>>>(a, b, inv, n);
+}
+
+void launch_gaussian_blur(const float *in, float *out, int W, int H, int K, const float *w, cudaStream_t st) {
+  k_gaussian_blur<<<grid_for((long long)W * H, 128, 152 * 16), 128, 0, st>>>(in, out, W, H, K, w);
 }
 
 void launch_tonemap(const float *film, int W, int H, float gamma, uint8_t *out, cudaStream_t st) {

@@ -137,6 +137,7 @@ void launch_wave_multi(const SceneView &S, const MergedJobs &M, const Queues &Q,
                        cudaEvent_t film_done = nullptr);
 void upload_halton_tables_multi(const HaltonTables &T, cudaStream_t st);
 void launch_tonemap(const float *film, int W, int H, float gamma, uint8_t *out, cudaStream_t st);
+void launch_gaussian_blur(const float *in, float *out, int W, int H, int K, const float *w, cudaStream_t st);
 
 // Serving: RMSE estimates from half films (see k_film_rmse) and the final
 // mean image.  partials holds PT_RMSE_BLOCKS doubles per pair.

@@ -33,7 +33,7 @@ EXPORTS = [
     "pt_create", "pt_destroy", "pt_last_error", "pt_version", "pt_scene_upload", "pt_scene_release",
     "pt_bvh_build", "pt_obj_load", "pt_obj_free", "pt_scene_info", "pt_render", "pt_render_device", "pt_render_device_noalloc",
     "pt_profile_begin",
-    "pt_profile_end", "pt_tonemap", "pt_sampler_eval", "pt_trace_closest",
+    "pt_profile_end", "pt_tonemap", "pt_gaussian_blur", "pt_write_png", "pt_sampler_eval", "pt_trace_closest",
     "pt_trace_any", "pt_bsdf_eval", "pt_bsdf_sample", "pt_render_batch", "pt_autotune", "pt_server_create",
     "pt_server_destroy", "pt_submit", "pt_server_step", "pt_poll", "pt_cancel",
 ]
@@ -154,6 +154,8 @@ def load() -> C.CDLL:
         "pt_profile_begin": [vp],
         "pt_profile_end": [vp, C.POINTER(C.c_double), C.POINTER(C.c_int64)],
         "pt_tonemap": [vp, f32p, C.c_int32, C.c_int32, C.c_float, u8p],
+        "pt_gaussian_blur": [vp, f32p, f32p, C.c_int32, C.c_int32, C.c_int32, C.c_float],
+        "pt_write_png": [C.c_char_p, u8p, C.c_int32, C.c_int32],
         "pt_sampler_eval": [vp, C.c_int32, C.c_uint32, C.c_uint32, C.c_int32, C.c_int32, f32p],
         "pt_trace_closest": [vp, C.c_int32, f32p, C.c_int32, C.c_float, C.c_float, f32p, i32p, f32p],
         "pt_trace_any": [vp, C.c_int32, f32p, f32p, C.c_int32, C.c_float, u8p],
@@ -369,6 +371,14 @@ class Renderer:
         self._check(self.lib.pt_profile_end(self.ctx, ms, nl))
         return {k: (ms[i], nl[i]) for i, k in enumerate(self.STAGES)}
 
+    def gaussian_blur(self, film: np.ndarray, kernel: int, sigma: float) -> np.ndarray:
+        """pt_gaussian_blur of an (H, W, 3) float32 film."""
+        f = np.ascontiguousarray(film, dtype=np.float32)
+        out = np.empty_like(f)
+        self._check(self.lib.pt_gaussian_blur(self.ctx, _ptr(f, C.c_float), _ptr(out, C.c_float), f.shape[1],
+                                              f.shape[0], kernel, sigma))
+        return out
+
     def tonemap(self, film: np.ndarray, gamma: float = 2.0) -> np.ndarray:
         film = np.ascontiguousarray(film, dtype=np.float32)
         h, w = film.shape[:2]
@@ -443,6 +453,17 @@ class Renderer:
                                             _ptr(ok, C.c_uint8), _ptr(wi, C.c_float), _ptr(att, C.c_float),
                                             _ptr(pdf, C.c_float), _ptr(ty, C.c_uint32)))
         return ok.astype(bool), wi, att, pdf, ty
+
+
+def write_png(path, rgb8: np.ndarray) -> None:
+    """pt_write_png of an (H, W, 3) uint8 image (row 0 = top)."""
+    lib = load()
+    a = np.ascontiguousarray(rgb8, dtype=np.uint8)
+    rc = lib.pt_write_png(str(path).encode(), _ptr(a, C.c_uint8), a.shape[1], a.shape[0])
+    if rc != PT_OK:
+        buf = C.create_string_buffer(512)
+        lib.pt_last_error(None, buf, 512)
+        raise PtError(rc, buf.value.decode())
 
 
 def bvh_build(scene, threads: int = 0) -> dict:

@@ -72,3 +72,18 @@ def test_converged_window_spot_check(renderer, workload):
     assert np.all(np.abs(z) < 3.0), z
     close = np.isclose(g, m_o, rtol=1e-2, atol=1e-3).all(-1)
     assert close.mean() > 0.9, close.mean()
+
+
+@pytest.mark.parametrize("k,sigma", [(3, 0.8), (7, 2.0), (15, 5.0)])
+def test_gaussian_blur_matches_oracle(renderer, k, sigma):
+    rng = np.random.default_rng(k)
+    film = (rng.random((23, 37, 3)) ** 3 * 20).astype(np.float32)
+    got = renderer.gaussian_blur(film, k, sigma)
+    want = O.gaussian_blur(film, k, sigma)
+    assert np.array_equal(got, want)  # same weights, same tap order, no fused operations
+
+
+def test_gaussian_blur_refused_arguments(renderer):
+    film = np.random.default_rng(3).random((8, 8, 3)).astype(np.float32)
+    for k, s in ((4, 1.0), (1, 1.0), (5, -1.0), (5, 0.0)):
+        assert np.array_equal(renderer.gaussian_blur(film, k, s), film)
