@@ -77,6 +77,28 @@ enum {
 };
 #define PT_MAT_FLAG_SPLIT_RAY 1
 #define PT_MAT_FLAG_MELANIN 2
+/* ColorVariant (include/texture/texture.hpp:134-163): a Lambertian albedo or
+ * a DiffuseEmitter colour given by a texture instead of p[0..2]: flags bits
+ * 8..31 hold the texture's index in pt_scene_desc.textures + 1 (0: the
+ * constant colour p[0..2]). */
+#define PT_MAT_TEXTURE_SHIFT 8
+
+/* Texture2D kinds (include/texture/texture.hpp:20-95, texture.cpp:95-193):
+ * CONSTANT color1; CHECKER color1 where sin(u*scale)*sin(v*scale) < 0 else
+ * color2; NOISE the fractal 2-D Perlin noise of pattern.hpp:72-114 at
+ * (u*scale, v*scale) with `fractal` octaves, grey; IMAGE bilinear lookup of
+ * width*height RGB texels stored as ImageTexture's texels[x][y]:
+ * texels[(y*width + x)*3 + c]. */
+enum { PT_TEX_CONSTANT = 0, PT_TEX_CHECKER = 1, PT_TEX_NOISE = 2, PT_TEX_IMAGE = 3 };
+typedef struct pt_texture_desc {
+  int32_t kind;
+  float color1[3];
+  float color2[3];
+  float scale;
+  int32_t fractal;
+  const float *texels; /* IMAGE only */
+  int32_t width, height;
+} pt_texture_desc;
 
 typedef struct pt_material_desc {
   int32_t type;
@@ -174,6 +196,9 @@ typedef struct pt_scene_desc {
    * [0, shutter_max].  Jobs with camera.shutter > shutter_max are rejected
    * when the scene has moving objects. */
   float shutter_max;
+  /* Textures referenced by materials (PT_MAT_TEXTURE_SHIFT). */
+  const pt_texture_desc *textures;
+  int32_t n_textures;
 } pt_scene_desc;
 
 enum { PT_BVH_REFERENCE = 0 };

@@ -599,7 +599,8 @@ static Box merge(const Box &a, const Box &b) {
 
 struct MeshO {
   std::vector<V> pos, nrm;
-  std::vector<std::array<int, 3>> tri, ntri;
+  std::vector<std::array<int, 3>> tri, ntri, uvtri;
+  std::vector<std::array<float, 2>> uv;
   int mat = 0, prim_base = 0;
   Box aabb;
   struct Node {
@@ -666,6 +667,8 @@ struct MeshO {
     rec.t = t;
     rec.position = o + t * d;
     rec.prim = prim_base + id;
+    rec.bu = u;
+    rec.bv = v;
     return true;
   }
   bool hit_node(int ni, V o, V d, float tmin, float tmax, Hit &rec) const {  // meshBVH.cpp:57-83
@@ -710,11 +713,108 @@ struct Light {
   V v0, e1, e2, normal, c, color;
   V vel;
   bool moving = false;
+  int texture = 0;  // texture index + 1 of the colour (0: color)
   float radius = 0, area = 0, intensity = 0;
 };
 
+// Surface textures (texture.hpp:20-95, texture.cpp:95-193, pattern.hpp:8-114).
+struct Tex {
+  int kind = 0, fractal = 1, w = 0, h = 0;
+  V c1, c2;
+  float scale = 10.f;
+  std::vector<V> texels;  // [y][x]
+};
+
+static const unsigned char kPerlin[256] = {  // Ken Perlin, "Improving Noise" (2002)
+    151, 160, 137, 91,  90,  15,  131, 13,  201, 95,  96,  53,  194, 233, 7,   225, 140, 36,  103, 30,  69,  142,
+    8,   99,  37,  240, 21,  10,  23,  190, 6,   148, 247, 120, 234, 75,  0,   26,  197, 62,  94,  252, 219, 203,
+    117, 35,  11,  32,  57,  177, 33,  88,  237, 149, 56,  87,  174, 20,  125, 136, 171, 168, 68,  175, 74,  165,
+    71,  134, 139, 48,  27,  166, 77,  146, 158, 231, 83,  111, 229, 122, 60,  211, 133, 230, 220, 105, 92,  41,
+    55,  46,  245, 40,  244, 102, 143, 54,  65,  25,  63,  161, 1,   216, 80,  73,  209, 76,  132, 187, 208, 89,
+    18,  169, 200, 196, 135, 130, 116, 188, 159, 86,  164, 100, 109, 198, 173, 186, 3,   64,  52,  217, 226, 250,
+    124, 123, 5,   202, 38,  147, 118, 126, 255, 82,  85,  212, 207, 206, 59,  227, 47,  16,  58,  17,  182, 189,
+    28,  42,  223, 183, 170, 213, 119, 248, 152, 2,   44,  154, 163, 70,  221, 153, 101, 155, 167, 43,  172, 9,
+    129, 22,  39,  253, 19,  98,  108, 110, 79,  113, 224, 232, 178, 185, 112, 104, 218, 246, 97,  228, 251, 34,
+    242, 193, 238, 210, 144, 12,  191, 179, 162, 241, 81,  51,  145, 235, 249, 14,  239, 107, 49,  192, 214, 31,
+    181, 199, 106, 157, 184, 84,  204, 176, 115, 121, 50,  45,  127, 4,   150, 254, 138, 236, 205, 93,  222, 114,
+    67,  29,  24,  72,  243, 141, 128, 195, 78,  66,  215, 61,  156, 180};
+
+static float perlin_grad(int hash, float x, float y) {  // pattern.hpp:43-66
+  switch (hash & 7) {
+  case 0: return x + y;
+  case 1: return -x + y;
+  case 2: return x - y;
+  case 3: return -x - y;
+  case 4: return x;
+  case 5: return -x;
+  case 6: return y;
+  default: return -y;
+  }
+}
+static float perlin_2d(float ux, float uy) {  // perlin_noise_2D, pattern.hpp:72-98
+  float x = std::fmod(ux, 256.f), y = std::fmod(uy, 256.f);
+  const int X = (int)std::floor(x) & 255, Y = (int)std::floor(y) & 255;
+  x = x - std::floor(x);
+  y = y - std::floor(y);
+  auto smooth = [](float t) {
+    t = std::clamp(t, 0.f, 1.f);
+    return t * t * t * (t * (t * 6.f - 15.f) + 10.f);
+  };
+  const float u = smooth(x), v = smooth(y);
+  auto P = [](int i) { return (int)kPerlin[i & 255]; };
+  const int X1 = (X + 1) % 256, Y1 = (Y + 1) % 256;
+  const int aa = P(P(X) + Y), ab = P(P(X) + Y1), ba = P(P(X1) + Y), bb = P(P(X1) + Y1);
+  auto lerp = [](float a, float b, float t) { return a + t * (b - a); };
+  const float x1 = lerp(perlin_grad(aa, x, y), perlin_grad(ba, x - 1.f, y), u);
+  const float x2 = lerp(perlin_grad(ab, x, y - 1.f), perlin_grad(bb, x - 1.f, y - 1.f), u);
+  return (lerp(x1, x2, v) + 1.f) * 0.5f;
+}
+static V tex_eval(const Tex &T, float u, float v) {
+  switch (T.kind) {
+  case PT_TEX_CHECKER: {  // texture.cpp:164-181
+    const float s = std::sin(u * T.scale) * std::sin(v * T.scale);
+    return s < 0.f ? T.c1 : T.c2;
+  }
+  case PT_TEX_NOISE: {  // fractal_perlin_2D, pattern.hpp:100-114
+    float total = 0.f, amp = 1.f, freq = 1.f;
+    for (int i = 0; i < T.fractal && i < 32; ++i) {
+      total += amp * perlin_2d(u * T.scale * freq, v * T.scale * freq);
+      amp *= 0.5f;
+      freq *= 2.f;
+    }
+    return V(std::clamp(std::fabs(total), 0.f, 1.f));
+  }
+  case PT_TEX_IMAGE: {  // ImageTexture::getTexelColor, bilinear (texture.cpp:112-143)
+    unsigned x = (unsigned)(u * T.w), y = (unsigned)(v * T.h);
+    float x1 = (u * T.w) - x, y1 = (v * T.h) - y;
+    x = std::min(x, (unsigned)T.w - 2);
+    y = std::min(y, (unsigned)T.h - 2);
+    float x2 = 1.0f - x1, y2 = 1.0f - y1;
+    V a = T.texels[y * T.w + x], b = T.texels[y * T.w + x + 1];
+    V c = T.texels[(y + 1) * T.w + x], e = T.texels[(y + 1) * T.w + x + 1];
+    V ab = a * x2 + b * x1, ce = c * x2 + e * x1;
+    return ab * y2 + ce * y1;
+  }
+  default: return T.c1;
+  }
+}
+
 struct Scene {
   std::vector<Material> mats;
+  std::vector<Tex> texs;
+  // The material at a hit, with a textured colour (ColorVariant, Lambertian
+  // albedo / DiffuseEmitter colour) looked up at the hit's texCoords.
+  Material shade_mat(const Hit &rec) const {
+    Material m = mats[rec.mat];
+    const int ti = (int)((uint32_t)m.flags >> PT_MAT_TEXTURE_SHIFT);
+    if (ti && (m.type == PT_MAT_LAMBERTIAN || m.type == PT_MAT_DIFFUSE_EMITTER)) {
+      V c = tex_eval(texs[ti - 1], rec.tu, rec.tv);
+      m.p[0] = c.x;
+      m.p[1] = c.y;
+      m.p[2] = c.z;
+    }
+    return m;
+  }
   std::vector<MeshO> meshes;
   std::vector<Obj> objs;
   struct TNode {
@@ -735,6 +835,29 @@ struct Scene {
   V sig_a, sig_s;
   float sig_t_max = 0.f;
 
+  // HitRecord::texCoords of a triangle hit: the interpolated uvs
+  // (meshBVH.cpp:134-138) or, for a mesh without uvs, the planar fallback of
+  // TriangleMesh::intersect over the mesh's box (triangleMesh.cpp:39-51);
+  // p is the hit point in the mesh's frame.
+  static void mesh_uv(const MeshO &M, Hit &rec, V p) {
+    const int id = rec.prim - M.prim_base;
+    if (!M.uv.empty()) {
+      const auto &ui = M.uvtri[id];
+      if (ui[0] < 0 || ui[1] < 0 || ui[2] < 0) return;  // (0, 0)
+      const float w = 1.f - rec.bu - rec.bv;
+      rec.tu = w * M.uv[ui[0]][0] + rec.bu * M.uv[ui[1]][0] + rec.bv * M.uv[ui[2]][0];
+      rec.tv = w * M.uv[ui[0]][1] + rec.bu * M.uv[ui[1]][1] + rec.bv * M.uv[ui[2]][1];
+      return;
+    }
+    const V n(std::fabs(rec.normal.x), std::fabs(rec.normal.y), std::fabs(rec.normal.z));
+    const int au = (n.x > n.y && n.x > n.z) ? 1 : 0;
+    const int av = (au == 1) ? 2 : (n.y > n.z ? 2 : 1);
+    const float u = (p[au] - M.aabb.lo[au]) / (M.aabb.hi[au] - M.aabb.lo[au]);
+    const float v = (p[av] - M.aabb.lo[av]) / (M.aabb.hi[av] - M.aabb.lo[av]);
+    rec.tu = std::clamp(u, 0.f, 1.f);
+    rec.tv = std::clamp(v, 0.f, 1.f);
+  }
+
   // Sphere / AARectangle / TriangleMesh intersect (+ FlipFace, set_normal).
   // A moving object (extension) is intersected in its own frame at the ray's
   // time: origin o - vel * time; the hit position is then taken on the world
@@ -745,8 +868,10 @@ struct Scene {
     if (ob.kind == PT_OBJ_MESH) {
       const MeshO &M = meshes[ob.index];
       if (!M.hit_node(0, o, d, tmin, tmax, rec)) return false;
+      const V p_obj = rec.position;
       if (ob.moving) rec.position = o_w + rec.t * d;
       rec.set_normal(d, rec.normal);
+      mesh_uv(M, rec, p_obj);
       rec.mat = M.mat;
       rec.light = -1;
       return true;
@@ -760,6 +885,9 @@ struct Scene {
       if (q0 < ob.d0min || q0 > ob.d0max || q1 < ob.d1min || q1 > ob.d1max) return false;
       rec.t = t;
       rec.position = o_w + t * dn;
+      // AARectangle texCoords (primitive.cpp:55-57)
+      rec.tu = (q0 - ob.d0min) / (ob.d0max - ob.d0min);
+      rec.tv = (q1 - ob.d1min) / (ob.d1max - ob.d1min);
       V nn(a == 0 ? 1.f : 0.f, a == 1 ? 1.f : 0.f, a == 2 ? 1.f : 0.f);
       rec.set_normal(d, nn);
     } else {  // primitive.hpp:124-170
@@ -778,6 +906,11 @@ struct Scene {
       const V c = ob.moving ? V(ob.c.x + ob.vel.x * time, ob.c.y + ob.vel.y * time, ob.c.z + ob.vel.z * time)
                             : ob.c;
       rec.set_normal(d, (rec.position - c).normalize());
+      // Sphere texCoords (primitive.hpp:158-164), in the object's frame
+      const V q = ((o + t * dn) - ob.c).normalize();
+      const float phi = std::atan2(q.z, q.x), theta = std::asin(std::clamp(q.y, -1.f, 1.f));
+      rec.tu = std::fmod(1.f - (phi + (float)PI) / (2.f * (float)PI) + 0.75f, 1.0f);
+      rec.tv = (theta + (float)(PI / 2)) / (float)PI;
     }
     if (ob.flip) rec.is_inside = !rec.is_inside;
     rec.mat = ob.mat;
@@ -885,6 +1018,16 @@ Scene *build_scene(const pt_scene_desc *d) {
       M.ntri.push_back({ni[3 * t], ni[3 * t + 1], ni[3 * t + 2]});
     }
     M.mat = md.material;
+    if (md.uvs && md.n_uvs > 0) {
+      for (int i = 0; i < md.n_uvs; ++i) M.uv.push_back({md.uvs[2 * i], md.uvs[2 * i + 1]});
+      const int32_t *ui = md.uv_indices ? md.uv_indices : md.indices;
+      for (int t = 0; t < md.n_triangles; ++t) {
+        std::array<int, 3> u3 = {ui[3 * t], ui[3 * t + 1], ui[3 * t + 2]};
+        for (int k = 0; k < 3; ++k)
+          if (u3[k] >= md.n_uvs) u3[k] = -1;
+        M.uvtri.push_back(u3);
+      }
+    }
     M.prim_base = tri_base[m];
     V mn(INFINITY), mx(-INFINITY);
     for (auto &p : M.pos) {
@@ -950,6 +1093,7 @@ Scene *build_scene(const pt_scene_desc *d) {
     if (m.type != PT_MAT_DIFFUSE_EMITTER || m.p[3] <= 0.f) continue;
     Light L{};
     L.intensity = m.p[3];
+    L.texture = (int)((uint32_t)m.flags >> PT_MAT_TEXTURE_SHIFT);
     L.color = V(m.p[0], m.p[1], m.p[2]);
     L.vel = ob.vel;
     L.moving = ob.moving;
@@ -1030,6 +1174,22 @@ Scene *build_scene(const pt_scene_desc *d) {
     L.type = 2;
     L.intensity = d->env->intensity;
     S->lights.push_back(L);
+  }
+  for (int k = 0; d->textures && k < d->n_textures; ++k) {
+    const pt_texture_desc &t = d->textures[k];
+    Tex T;
+    T.kind = t.kind;
+    T.fractal = t.fractal;
+    T.scale = t.scale;
+    T.c1 = V(t.color1[0], t.color1[1], t.color1[2]);
+    T.c2 = V(t.color2[0], t.color2[1], t.color2[2]);
+    if (t.kind == PT_TEX_IMAGE) {
+      T.w = t.width;
+      T.h = t.height;
+      for (int i = 0; i < t.width * t.height; ++i)
+        T.texels.emplace_back(t.texels[3 * i], t.texels[3 * i + 1], t.texels[3 * i + 2]);
+    }
+    S->texs.push_back(T);
   }
   S->bg = V(d->bg_color[0], d->bg_color[1], d->bg_color[2]);
   if (d->medium) {
@@ -1134,7 +1294,10 @@ static LightSample sample_light(const PathCtx &P, V x, V n, int bounce, int ls, 
   r.NoL = std::max(0.f, dot(ln, -r.wl));
   r.d2 = len * len;
   r.G = (r.d2 < 1e-7f) ? 0.f : r.NoL * r.NoI / r.d2;
-  r.Le = (dot(ln, -r.wl) > 0.0f) ? L.color * L.intensity : V(0.f);
+  // L_emit (light.hpp:157-165, 296-303); a textured light at the sample's
+  // offsets (maxdepth_nee.hpp:175-176)
+  const V lcol = L.texture ? tex_eval(S.texs[L.texture - 1], ox, oy) : L.color;
+  r.Le = (dot(ln, -r.wl) > 0.0f) ? lcol * L.intensity : V(0.f);
   if (!(r.pdf > 1e-7f)) r.valid = false;
   return r;
 }
@@ -1150,7 +1313,7 @@ static V ray_color_ref(const PathCtx &P, V o, V d, int depth, int bounce) {
     if (S.has_env) return S.env_le(d.normalize());
     return S.bg;
   }
-  const Material &M = S.mats[rec.mat];
+  const Material M = S.shade_mat(rec);
   const int dim0 = 3 * bounce;
   float uc = dim_value(P, dim0), u0 = dim_value(P, dim0 + 1), u1 = dim_value(P, dim0 + 2);
   Scatter s;
@@ -1268,7 +1431,7 @@ static V ray_color_iter(const PathCtx &P, V o, V d) {
       }
       break;
     }
-    const Material &M = S.mats[rec.mat];
+    const Material M = S.shade_mat(rec);
     if (M.type == PT_MAT_DIFFUSE_EMITTER) {
       if (prev_pdf < 0.f) {
         L += beta * mat_emit(M, d, rec);
@@ -1281,7 +1444,8 @@ static V ray_color_iter(const PathCtx &P, V o, V d) {
           float cl = dot(ln, -d.normalize());
           if (cl > 0.f) {
             float pl = rec.t * rec.t / (cl * Lt.area * (float)S.lights.size());
-            L += beta * Lt.color * Lt.intensity * power_heuristic(1.f, prev_pdf, (float)LN, pl);
+            const V lcol = Lt.texture ? tex_eval(S.texs[Lt.texture - 1], rec.tu, rec.tv) : Lt.color;
+            L += beta * lcol * Lt.intensity * power_heuristic(1.f, prev_pdf, (float)LN, pl);
           }
         } else {
           L += beta * mat_emit(M, d, rec);

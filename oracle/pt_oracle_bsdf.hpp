@@ -17,6 +17,8 @@ struct Hit {  // HitRecord (materialBase.hpp:32-53)
   int mat = -1;
   int prim = -1;
   int light = -1;
+  float bu = 0.f, bv = 0.f;  // triangle barycentrics of the hit
+  float tu = 0.f, tv = 0.f;  // HitRecord::texCoords
   void set_normal(V dir, V n) {
     is_inside = dot(dir, n) < 0;
     normal = is_inside ? n : -n;

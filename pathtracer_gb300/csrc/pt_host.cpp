@@ -819,6 +819,89 @@ std::unique_ptr<Scene> build_scene(const pt_scene_desc *d, cudaStream_t st, bool
     if (t < PT_MAT_DIFFUSE_EMITTER) S->family_mask |= 1u << t;
   }
 
+  // textures (ColorVariant): the table, an image texel pool, and per
+  // primitive texture-coordinate records when a material uses one
+  const int n_tex = d->textures ? d->n_textures : 0;
+  if (n_tex < 0) fail(PT_ERR_INVALID, "negative texture count");
+  std::vector<TexRec> texs(n_tex);
+  std::vector<float4> texel_pool;
+  std::vector<size_t> texel_off(n_tex, 0);
+  for (int k = 0; k < n_tex; ++k) {
+    const pt_texture_desc &t = d->textures[k];
+    TexRec &T = texs[k];
+    std::memset(&T, 0, sizeof T);
+    if (t.kind < PT_TEX_CONSTANT || t.kind > PT_TEX_IMAGE) fail(PT_ERR_INVALID, "bad texture kind");
+    T.kind = t.kind;
+    T.fractal = t.fractal;
+    T.scale = t.scale;
+    for (int c = 0; c < 3; ++c) {
+      T.c1[c] = t.color1[c];
+      T.c2[c] = t.color2[c];
+    }
+    if (t.kind == PT_TEX_IMAGE) {
+      if (!t.texels || t.width < 2 || t.height < 2) fail(PT_ERR_INVALID, "image texture smaller than 2x2");
+      T.width = t.width;
+      T.height = t.height;
+      texel_off[k] = texel_pool.size();
+      for (size_t i = 0; i < (size_t)t.width * t.height; ++i)
+        texel_pool.push_back(make_float4(t.texels[3 * i], t.texels[3 * i + 1], t.texels[3 * i + 2], 0.f));
+    }
+  }
+  bool any_textured = false;
+  for (const MatRec &m : mats) {
+    const int ti = (int)((uint32_t)m.flags >> PT_MAT_TEXTURE_SHIFT);
+    if (ti > n_tex) fail(PT_ERR_INVALID, "material texture index out of range");
+    if (ti && (m.type == PT_MAT_LAMBERTIAN || m.type == PT_MAT_DIFFUSE_EMITTER)) any_textured = true;
+  }
+  std::vector<float4> prim_uv;
+  if (any_textured) {
+    prim_uv.assign(2 * (size_t)n_prims, make_float4(0.f, 0.f, 0.f, 0.f));
+    for (int prim = 0; prim < n_prims; ++prim) {
+      float4 &a = prim_uv[2 * prim], &b = prim_uv[2 * prim + 1];
+      if (prim < B.n_tris) {
+        const int mi = prim_mesh[prim], t = prim_tri[prim];
+        const pt_mesh_desc &m = d->meshes[mi];
+        if (m.uvs && m.n_uvs > 0) {
+          // MeshBVHNode::hitTriangle's uv interpolation (meshBVH.cpp:134-138);
+          // a face without valid uv indices keeps (0, 0)
+          const int32_t *ui = m.uv_indices ? m.uv_indices : m.indices;
+          bool ok = true;
+          for (int k = 0; k < 3; ++k) ok = ok && ui[3 * t + k] >= 0 && ui[3 * t + k] < m.n_uvs;
+          if (ok) {
+            const float *u0 = m.uvs + 2 * ui[3 * t], *u1 = m.uvs + 2 * ui[3 * t + 1], *u2 = m.uvs + 2 * ui[3 * t + 2];
+            a = make_float4(u0[0], u0[1], u1[0], u1[1]);
+            b = make_float4(u2[0], u2[1], (float)PT_UV_TRI, 0.f);
+          } else {
+            b = make_float4(0.f, 0.f, (float)PT_UV_TRI, 0.f);
+          }
+        } else {
+          // TriangleMesh::intersect's planar fallback over the mesh's box
+          // (triangleMesh.cpp:39-51, box as triangleMesh.cpp:10-18)
+          float mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
+          for (int v = 0; v < m.n_positions; ++v)
+            for (int c = 0; c < 3; ++c) {
+              mn[c] = std::min(mn[c], m.positions[3 * v + c]);
+              mx[c] = std::max(mx[c], m.positions[3 * v + c]);
+            }
+          for (int c = 0; c < 3; ++c) {
+            mn[c] -= 1e-3f;
+            mx[c] += 1e-3f;
+          }
+          a = make_float4(mn[0], mn[1], mn[2], mx[0]);
+          b = make_float4(mx[1], mx[2], (float)PT_UV_PLANAR, 0.f);
+        }
+      } else if (prim < B.n_tris + d->n_quads) {
+        const pt_quad_desc &q = d->quads[prim - B.n_tris];
+        a = make_float4(q.d0_min, q.d0_max, q.d1_min, q.d1_max);
+        b = make_float4(0.f, 0.f, (float)PT_UV_QUAD, (float)q.axis);
+      } else {
+        const pt_sphere_desc &sp = d->spheres[prim - B.n_tris - d->n_quads];
+        a = make_float4(sp.center[0], sp.center[1], sp.center[2], sp.radius);
+        b = make_float4(0.f, 0.f, (float)PT_UV_SPHERE, 0.f);
+      }
+    }
+  }
+
   // light discovery (lightDiscovery.hpp:5-81): emissive quads and spheres in
   // object order, then the environment light (renderManager.hpp:115-118).
   std::vector<LightRec> lights;
@@ -864,6 +947,7 @@ std::unique_ptr<Scene> build_scene(const pt_scene_desc *d, cudaStream_t st, bool
       L.area = (float)(4 * PT_PI * s.radius * s.radius);
     }
     L.motion = prim_motion[L.prim];
+    L.texture = (int32_t)((uint32_t)md.flags >> PT_MAT_TEXTURE_SHIFT);
     shade[L.prim].light = (int)lights.size();
     lights.push_back(L);
   }
@@ -970,6 +1054,14 @@ std::unique_ptr<Scene> build_scene(const pt_scene_desc *d, cudaStream_t st, bool
     V.env.intensity = d->env->intensity;
     V.env.present = 1;
   }
+  if (!texs.empty()) {
+    const float4 *pool = up(texel_pool);
+    for (int k = 0; k < n_tex; ++k)
+      if (texs[k].kind == PT_TEX_IMAGE) texs[k].texels = pool ? pool + texel_off[k] : nullptr;
+    V.textures = up(texs);
+    V.n_textures = n_tex;
+  }
+  if (!prim_uv.empty()) V.prim_uv = up(prim_uv);
   if (!motion.empty()) {
     V.motion = up(motion);
     V.node_motion = up(out.node_motion);

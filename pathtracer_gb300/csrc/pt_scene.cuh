@@ -84,7 +84,7 @@ struct alignas(16) LightRec {
   float normal[3];  // quad: normalize(cross(e1, e2))
   float pad2;
   float color[3];   // ConstantTexture colour
-  float pad3;
+  int32_t texture;  // texture index + 1 of the emitter's colour (0: color)
 };
 
 struct EnvMap {
@@ -96,6 +96,19 @@ struct EnvMap {
   float intensity;
   int32_t present;
 };
+
+// A surface texture (pt_texture_desc), image texels as float4.
+struct alignas(16) TexRec {
+  int32_t kind, fractal, width, height;
+  float c1[3], scale;
+  float c2[3], pad;
+  const float4 *texels;
+  const float4 *pad_ptr;
+};
+
+// Texture-coordinate records (2 x float4 per primitive, only for scenes with
+// textured materials): kind in the second record's z.
+enum UvKind : int32_t { PT_UV_TRI = 1, PT_UV_PLANAR = 2, PT_UV_QUAD = 3, PT_UV_SPHERE = 4 };
 
 struct SceneView {
   const Bvh4Node *nodes;
@@ -116,6 +129,9 @@ struct SceneView {
   const int32_t *node_motion;  // per BVH4 node: motion index + 1 of the moving object it roots
   int32_t has_motion;
   int32_t trav_cap;  // steps one ray's traversal may take before the device error flag is set
+  const TexRec *textures;  // surface textures (materials' flags >> PT_MAT_TEXTURE_SHIFT)
+  const float4 *prim_uv;   // per primitive texture-coordinate records (null: no textures)
+  int32_t n_textures;
 };
 
 // Child references of a BVH4 node entering a moving object's subtree carry

@@ -13,6 +13,7 @@
 #include "pt_bsdf.cuh"
 #include "pt_trace.cuh"
 #include "pt_kernels.h"
+#include "pt_texture.cuh"
 
 namespace pt {
 
@@ -118,6 +119,7 @@ struct Surf {
   bool front; // HitRecord::is_inside (front-face flag; FlipFace toggles it)
   int mat;
   int light;
+  int motion;  // motion index + 1 of the primitive (0: static)
 };
 
 // Position of a moving object's point at `time` (rounded, never fused).
@@ -140,6 +142,7 @@ __device__ inline Surf surface_at(const SceneView &S, V3 o, V3 d, const HitRec &
   ps.ng[0] = q3.y; ps.ng[1] = q3.z; ps.ng[2] = q3.w;
   s.mat = ps.material;
   s.light = ps.light;
+  s.motion = PT_PRIM_MOTION(ps.flags);
   const int type = PT_PRIM_KIND(ps.flags);
   V3 n;
   if (type == ITEM_TRI) {
@@ -338,6 +341,26 @@ __global__ void __launch_bounds__(128) k_trace_closest(SceneView S, DeviceJob J,
   warp_count(&Q.stats[2], rays);
 }
 
+// The hit point in its object's rest frame (texture coordinates of moving
+// objects follow the object).
+__device__ __forceinline__ V3 uv_point(const SceneView &S, const Surf &sf, float time) {
+  return sf.motion ? moved_point(S, sf.motion, sf.p, -time) : sf.p;
+}
+
+// Texture index + 1 of a material's colour (0: the constant p[0..2]).
+__device__ __forceinline__ int mat_texture(const MatRec &M) { return (int)((uint32_t)M.flags >> PT_MAT_TEXTURE_SHIFT); }
+
+// DiffuseEmitter::emit (material.hpp:483-488) with its colour texture looked
+// up at the hit's texture coordinates.
+__device__ __forceinline__ V3 emit_at(const SceneView &S, const MatRec &M, const Surf &sf, V3 d, const HitRec &h,
+                                      float time) {
+  const int ti = mat_texture(M);
+  if (!ti) return mat_emit(M, sf.n, d);
+  if (!(dot(sf.n, -d) > 0.f)) return v3(0.f);
+  const float2 uv = surface_uv(S, h.prim, uv_point(S, sf, time), sf.n, h.u, h.v);
+  return tex_eval(S.textures[ti - 1], uv.x, uv.y) * M.p[3];
+}
+
 __device__ __forceinline__ float power_heuristic(float nf, float fpdf, float ng, float gpdf) {
   float f = nf * fpdf, g = ng * gpdf;  // maxdepth_mis.hpp:10-15 with sample counts
   if (isinf(f)) return 1.f;
@@ -352,7 +375,8 @@ __device__ __forceinline__ float power_heuristic(float nf, float fpdf, float ng,
 template <int FAM, bool MED>
 __device__ __forceinline__ void next_event(const SceneView &S, const DeviceJob &J, const Queues &Q, int sslot,
                                            int path, uint64_t key, uint32_t rbase, const Surf &sf, int mat,
-                                           V3 wo, V3 beta, int LN, bool mis, float time) {
+                                           V3 wo, V3 beta, int LN, bool mis, float time, bool tex_alb,
+                                           V3 alb) {
   const float phase = (float)(1.0 / (4.0 * PT_PI));
   Q.sh_o[sslot] = make_float4(sf.p.x, sf.p.y, sf.p.z, __int_as_float(path));
   const float inv_ln = 1.f / (float)LN;
@@ -417,7 +441,11 @@ __device__ __forceinline__ void next_event(const SceneView &S, const DeviceJob &
       float NoL = fmaxf(0.f, dot(ln, -wl));
       float d2 = len * len;
       G = (d2 < 1e-7f) ? 0.f : NoL * NoI / d2;
-      Le = (dot(ln, -wl) > 0.f) ? v3(Lr.color[0], Lr.color[1], Lr.color[2]) * Lr.intensity : v3(0.f);
+      // L_emit of the light (light.hpp:157-165, 296-303); a textured light
+      // is looked up at the sample's offsets (maxdepth_nee.hpp:175-176)
+      const V3 lcol = Lr.texture ? tex_eval(S.textures[Lr.texture - 1], ox, oy)
+                                 : v3(Lr.color[0], Lr.color[1], Lr.color[2]);
+      Le = (dot(ln, -wl) > 0.f) ? lcol * Lr.intensity : v3(0.f);
       if (!(pdf_l > 1e-7f)) valid = false;
       if (mis && valid && NoL > 0.f) {
         pdf_l = pdf_l * d2 / NoL;  // solid-angle pdf
@@ -433,6 +461,7 @@ __device__ __forceinline__ void next_event(const SceneView &S, const DeviceJob &
         pb = phase;
       } else {
         bsdf_eval_t<FAM>(S.materials[mat], wo, wl, sf.n, sf.front, f, pb);
+        if ((FAM == 0 || FAM < 0) && tex_alb) f = alb * PT_INV_PI_F;  // textured Lambertian albedo
       }
       float w = mis ? power_heuristic((float)LN, pdf_l, 1.f, pb) : 1.f;
       V3 c = beta * (f * Le * (G / pdf_l * w * inv_ln)) * tr;
@@ -494,6 +523,8 @@ __global__ void __launch_bounds__(128) k_shade(SceneView S, DeviceJob J, JobTabl
     float time = 0.f;
     int LN = 1;
     bool mis = false;
+    bool tex_alb = false;  // textured Lambertian albedo of this vertex
+    V3 alb = v3(0.f);
     if (ii < n) {
       const int i = (FAM >= 0) ? Q.order[lo + ii] : ii;
       float4 ro = ld4(Q.ray_o[qsel] + i), rd = ld4(Q.ray_d[qsel] + i);
@@ -559,7 +590,7 @@ __global__ void __launch_bounds__(128) k_shade(SceneView S, DeviceJob J, JobTabl
         if (DO_MISC && mat_is_emitter(M)) {
           // DiffuseEmitter: scatter() is false (material.hpp:475-481)
           if (prev_pdf < 0.f) {
-            Ladd = beta * mat_emit(M, sf.n, d);
+            Ladd = beta * emit_at(S, M, sf, d, h, time);
           } else if (mis) {
             if (sf.light >= 0) {
               const LightRec &Lr = S.lights[sf.light];
@@ -569,12 +600,17 @@ __global__ void __launch_bounds__(128) k_shade(SceneView S, DeviceJob J, JobTabl
               V3 ln = (Lr.type == LIGHT_QUAD) ? v3(Lr.normal[0], Lr.normal[1], Lr.normal[2]) : normalize(sf.p - lc);
               float cl = dot(ln, -normalize(d));
               if (cl > 0.f) {
-                V3 Le = v3(Lr.color[0], Lr.color[1], Lr.color[2]) * Lr.intensity;
+                V3 lcol = v3(Lr.color[0], Lr.color[1], Lr.color[2]);
+                if (Lr.texture) {
+                  const float2 uv = surface_uv(S, h.prim, uv_point(S, sf, time), sf.n, h.u, h.v);
+                  lcol = tex_eval(S.textures[Lr.texture - 1], uv.x, uv.y);
+                }
+                V3 Le = lcol * Lr.intensity;
                 float pl = h.t * h.t / (cl * Lr.area * (float)S.n_lights);
                 Ladd = beta * Le * power_heuristic(1.f, prev_pdf, (float)LN, pl);
               }
             } else {
-              Ladd = beta * mat_emit(M, sf.n, d);
+              Ladd = beta * emit_at(S, M, sf, d, h, time);
             }
           }
           // REF_NEE after a non-delta vertex: dropped (maxdepth_nee.hpp:246-247)
@@ -586,6 +622,14 @@ __global__ void __launch_bounds__(128) k_shade(SceneView S, DeviceJob J, JobTabl
           float u1 = sampler_dim(Jp, dim0 + 2, P.halton_index, P.key, P.pix, P.k);
           wo = -normalize(d);
           BsdfSample bs = bsdf_sample_t<FAM>(M, wo, sf.n, sf.front, uc, u0, u1);
+          if ((FAM == 0 || FAM < 0) && M.type == PT_MAT_LAMBERTIAN && mat_texture(M)) {
+            // Lambertian with a ColorVariant texture: albedo at the hit's
+            // texCoords (material.hpp:100, 133)
+            const float2 uv = surface_uv(S, prim, uv_point(S, sf, time), sf.n, h.u, h.v);
+            tex_alb = true;
+            alb = tex_eval(S.textures[mat_texture(M) - 1], uv.x, uv.y);
+            bs.att = alb * PT_INV_PI_F;
+          }
           const bool spec_r = (bs.type & BX_SPECULAR_R) == BX_SPECULAR_R;
           const bool spec_t = (bs.type & BX_SPECULAR_T) == BX_SPECULAR_T;
           if (bs.ok && (spec_r || spec_t)) {
@@ -635,9 +679,9 @@ __global__ void __launch_bounds__(128) k_shade(SceneView S, DeviceJob J, JobTabl
       long long g;
       const DeviceJob &Jp = path_job<MJ>(J, T, Q, path, g0, g);
       if (DO_MISC && nee_medium)
-        next_event<FAM, true>(S, Jp, Q, sslot, path, key, rbase, sf, mat, wo, beta, LN, mis, time);
+        next_event<FAM, true>(S, Jp, Q, sslot, path, key, rbase, sf, mat, wo, beta, LN, mis, time, false, alb);
       else if (DO_SURF)
-        next_event<FAM, false>(S, Jp, Q, sslot, path, key, rbase, sf, mat, wo, beta, LN, mis, time);
+        next_event<FAM, false>(S, Jp, Q, sslot, path, key, rbase, sf, mat, wo, beta, LN, mis, time, tex_alb, alb);
     }
   }
   warp_count(&Q.stats[1], segs);

@@ -44,6 +44,16 @@ u8p = C.POINTER(C.c_uint8)
 u32p = C.POINTER(C.c_uint32)
 
 
+class TextureDesc(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("color1", C.c_float * 3), ("color2", C.c_float * 3), ("scale", C.c_float),
+                ("fractal", C.c_int32), ("texels", C.POINTER(C.c_float)), ("width", C.c_int32),
+                ("height", C.c_int32)]
+
+
+TEX_CONSTANT, TEX_CHECKER, TEX_NOISE, TEX_IMAGE = range(4)
+MAT_TEXTURE_SHIFT = 8
+
+
 class MaterialDesc(C.Structure):
     _fields_ = [("type", C.c_int32), ("flags", C.c_int32), ("p", C.c_float * 30)]
 
@@ -89,6 +99,7 @@ class SceneDesc(C.Structure):
         ("objects", C.POINTER(ObjectDesc)), ("n_objects", C.c_int32),
         ("env", C.POINTER(EnvDesc)), ("medium", C.POINTER(MediumDesc)),
         ("bg_color", C.c_float * 3), ("bvh_mode", C.c_int32), ("shutter_max", C.c_float),
+        ("textures", C.POINTER(TextureDesc)), ("n_textures", C.c_int32),
     ]
 
 
@@ -231,6 +242,10 @@ def make_scene_desc(scene) -> SceneBuffers:
             nrm = sb.hold(np.ascontiguousarray(m.normals, dtype=np.float32))
             md.normals = _ptr(nrm, C.c_float)
             md.n_normals = nrm.shape[0]
+        if getattr(m, "uvs", None) is not None:
+            uv = sb.hold(np.ascontiguousarray(m.uvs, dtype=np.float32))
+            md.uvs = _ptr(uv, C.c_float)
+            md.n_uvs = uv.shape[0]
         md.material = m.material
     sb.hold(meshes)
     d.meshes = meshes
@@ -269,6 +284,23 @@ def make_scene_desc(scene) -> SceneBuffers:
         d.medium = C.pointer(md)
     d.bg_color[:] = [float(x) for x in scene.bg]
     d.shutter_max = float(getattr(scene, "shutter_max", 0.0))
+    texs = getattr(scene, "textures", [])
+    if texs:
+        arr = (TextureDesc * len(texs))()
+        for i, t in enumerate(texs):
+            td = arr[i]
+            td.kind = t["kind"]
+            td.color1[:] = [float(x) for x in t.get("color1", (0, 0, 0))]
+            td.color2[:] = [float(x) for x in t.get("color2", (1, 1, 1))]
+            td.scale = float(t.get("scale", 10.0))
+            td.fractal = int(t.get("fractal", 1))
+            if t["kind"] == TEX_IMAGE:
+                img = sb.hold(np.ascontiguousarray(t["texels"], dtype=np.float32))
+                td.texels = _ptr(img, C.c_float)
+                td.height, td.width = img.shape[0], img.shape[1]
+        sb.hold(arr)
+        d.textures = arr
+        d.n_textures = len(texs)
     return sb
 
 

@@ -33,6 +33,7 @@ class Mesh:
     indices: np.ndarray              # (T, 3) int32
     normals: np.ndarray | None       # (V, 3) float32, indexed like positions
     material: int
+    uvs: np.ndarray | None = None    # (V, 2) float32 texture coordinates, indexed like positions
 
 
 @dataclass
@@ -47,10 +48,24 @@ class Scene:
     medium: tuple | None = None                     # (sigma_a[3], sigma_s[3], g)
     bg: tuple = (0.0, 0.0, 0.0)
     shutter_max: float = 0.0                        # motion blur: longest shutter of any job
+    textures: list = field(default_factory=list)    # dicts: kind, color1, color2, scale, fractal, texels
 
-    def add_material(self, mtype: int, params, flags: int = 0) -> int:
+    def add_material(self, mtype: int, params, flags: int = 0, texture: int | None = None) -> int:
+        """A material; `texture` (an index from add_texture) replaces the
+        Lambertian albedo / DiffuseEmitter colour p[0..2] (ColorVariant)."""
+        if texture is not None:
+            flags |= (texture + 1) << N.MAT_TEXTURE_SHIFT
         self.materials.append((mtype, list(params), flags))
         return len(self.materials) - 1
+
+    def add_texture(self, kind: int, color1=(0.0, 0.0, 0.0), color2=(1.0, 1.0, 1.0), scale: float = 10.0,
+                    fractal: int = 1, texels=None) -> int:
+        """CheckerTexture(color1, color2, scale), NoiseTexture(scale, fractal),
+        ConstantTexture(color1) or an image (texels (H, W, 3), row y as
+        ImageTexture's texels[x][y])."""
+        self.textures.append({"kind": kind, "color1": tuple(color1), "color2": tuple(color2), "scale": scale,
+                              "fractal": fractal, "texels": texels})
+        return len(self.textures) - 1
 
     def add_mesh(self, mesh: Mesh, velocity=(0.0, 0.0, 0.0)):
         self.meshes.append(mesh)
@@ -329,3 +344,39 @@ def job_mix(scenes: dict, n_jobs: int, seed: int, res=(64, 1024), spp=(4, 256), 
                                sampler=st["sampler"], rr_start=st["rr_start"], env_sampling=st["env_sampling"],
                                seed=seed * 1000 + k))
     return jobs
+
+
+def textured_cornell(subdiv: int = 3, seed: int = 0) -> tuple[Scene, dict]:
+    """The Cornell box with ColorVariant textures: a checker floor, a noise
+    back wall, an image on the left wall, a checker-textured light, and the
+    sphere a Lambertian mesh with per-vertex uvs (spherical mapping) under a
+    noise texture."""
+    rng = np.random.default_rng(seed)
+    sc = Scene()
+    checker = sc.add_texture(N.TEX_CHECKER, (0.1, 0.1, 0.1), (0.8, 0.8, 0.8), scale=40.0)
+    noise = sc.add_texture(N.TEX_NOISE, scale=8.0, fractal=4)
+    img = (rng.random((16, 24, 3)) * 0.8 + 0.1).astype(np.float32)
+    image = sc.add_texture(N.TEX_IMAGE, texels=img)
+    lchk = sc.add_texture(N.TEX_CHECKER, (4.0, 2.0, 0.5), (20.0, 14.0, 5.0), scale=30.0)
+    snoise = sc.add_texture(N.TEX_NOISE, scale=20.0, fractal=2)
+    white = sc.add_material(N.LAMBERTIAN, [0.75, 0.75, 0.75])
+    floor = sc.add_material(N.LAMBERTIAN, [0, 0, 0], texture=checker)
+    back = sc.add_material(N.LAMBERTIAN, [0, 0, 0], texture=noise)
+    left = sc.add_material(N.LAMBERTIAN, [0, 0, 0], texture=image)
+    green = sc.add_material(N.LAMBERTIAN, [0.14, 0.45, 0.09])
+    light = sc.add_material(N.DIFFUSE_EMITTER, [0, 0, 0, 1.0], texture=lchk)
+    ball = sc.add_material(N.LAMBERTIAN, [0, 0, 0], texture=snoise)
+    sc.add_quad(1, 0.999, 0.3, 0.7, 0.3, 0.7, light)
+    sc.add_quad(0, 1.0, 0.0, 1.0, 0.0, 1.0, left)
+    sc.add_quad(0, 0.0, 0.0, 1.0, 0.0, 1.0, green)
+    sc.add_quad(1, 0.0, 0.0, 1.0, 0.0, 1.0, floor)
+    sc.add_quad(1, 1.0, 0.0, 1.0, 0.0, 1.0, white)
+    sc.add_quad(2, 1.0, 0.0, 1.0, 0.0, 1.0, back)
+    m = sphere_mesh(subdiv, (0.5, 0.3, 0.55), 0.25, ball)
+    d = m.normals.astype(np.float64)
+    uvs = np.stack([0.5 + np.arctan2(d[:, 2], d[:, 0]) / (2 * math.pi), 0.5 + np.arcsin(np.clip(d[:, 1], -1, 1)) / math.pi],
+                   axis=1).astype(np.float32)
+    m.uvs = uvs
+    sc.add_mesh(m)
+    cam = camera((0.5, 0.5, -1.4), (0.0, 0.0, 1.0), 40.0, 1.0)
+    return sc, cam

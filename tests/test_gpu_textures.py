@@ -1,0 +1,60 @@
+"""Surface textures (ColorVariant): checker, Perlin noise and image textures
+on Lambertian albedos and on a light's colour, with texture coordinates from
+rectangles, spheres, meshes with uvs and the planar fallback.  GPU images
+against the oracle on the same sample streams."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from oracle import pyoracle as O
+from pathtracer_gb300 import native as N
+from pathtracer_gb300 import scene as S
+
+pytestmark = pytest.mark.gpu
+
+
+def _z(mean_a, var_a, mean_b, var_b, spp):
+    se = np.sqrt((var_a + var_b).reshape(-1, 3).sum(0) / spp) / (mean_a.shape[0] * mean_a.shape[1])
+    return (mean_a.reshape(-1, 3).mean(0) - mean_b.reshape(-1, 3).mean(0)) / se
+
+
+def _compare(renderer, sc, job, spp, frac=0.9):
+    sid = renderer.upload(sc)
+    job.scene = sid
+    film = renderer.render(job)
+    renderer.release(sid)
+    job.scene = 0
+    m_o, v_o = O.render(sc, job)
+    assert np.isfinite(film).all()
+    z = _z(film, v_o, m_o, v_o, spp)
+    assert np.all(np.abs(z) < 3.0), z
+    close = np.isclose(film, m_o, rtol=1e-3, atol=1e-3).all(-1)
+    assert close.mean() > frac, close.mean()
+    return film
+
+
+@pytest.mark.parametrize("estimator", [N.EST_REF_NEE, N.EST_NEE_MIS])
+def test_textured_cornell_matches_oracle(renderer, estimator):
+    sc, cam = S.textured_cornell(3)
+    job = N.job_desc(0, cam, 48, 48, 4, 4, 6, seed=4, estimator=estimator)
+    _compare(renderer, sc, job, 16)
+
+
+def test_planar_fallback_and_spheres(renderer):
+    sc, cam = S.textured_cornell(2)
+    # the ball without uvs (planar fallback over its box) and a textured sphere light
+    sc.meshes[0].uvs = None
+    sc.add_sphere((0.25, 0.8, 0.4), 0.08, sc.add_material(N.DIFFUSE_EMITTER, [0, 0, 0, 3.0],
+                                                          texture=sc.add_texture(N.TEX_CHECKER, (1, 1, 1),
+                                                                                 (6, 5, 4), 12.0)))
+    sc.add_sphere((0.75, 0.15, 0.3), 0.12, sc.add_material(N.LAMBERTIAN, [0, 0, 0], texture=0))
+    job = N.job_desc(0, cam, 40, 40, 4, 4, 6, seed=9, estimator=N.EST_NEE_MIS)
+    _compare(renderer, sc, job, 16)
+
+
+def test_textures_move_with_objects(renderer):
+    sc, cam = S.textured_cornell(2)
+    S.with_motion(sc, seed=3, speed=0.5)
+    job = N.job_desc(0, dict(cam, shutter=0.4), 40, 40, 4, 4, 6, seed=2, estimator=N.EST_NEE_MIS)
+    _compare(renderer, sc, job, 16)
