@@ -51,11 +51,78 @@ enum class TransportMode { Radiance, Importance };
 enum class Axis { X = 0, Y = 1, Z = 2 };
 
 // ------------------------------------------------------------- materials
+// ------------------------------------------------------------ textures
+// Texture2D and its kinds (texture/texture.hpp:20-95); an ImageTexture takes
+// its texels in memory ([y][x] RGB, as ImageTexture's texels[x][y]).
+class Texture2D {
+ public:
+  virtual ~Texture2D() = default;
+  virtual pt_texture_desc desc() const = 0;
+};
+class ConstantTexture : public Texture2D {
+ public:
+  explicit ConstantTexture(vec3 c) : c(c) {}
+  pt_texture_desc desc() const override {
+    pt_texture_desc d{};
+    d.kind = PT_TEX_CONSTANT;
+    for (int k = 0; k < 3; ++k) d.color1[k] = c[k];
+    return d;
+  }
+  vec3 c;
+};
+class CheckerTexture : public Texture2D {
+ public:
+  explicit CheckerTexture(float scale = 10.f) : c1(0.f), c2(1.f), scale(scale) {}
+  CheckerTexture(vec3 color1, vec3 color2, float scale = 10.f) : c1(color1), c2(color2), scale(scale) {}
+  pt_texture_desc desc() const override {
+    pt_texture_desc d{};
+    d.kind = PT_TEX_CHECKER;
+    for (int k = 0; k < 3; ++k) {
+      d.color1[k] = c1[k];
+      d.color2[k] = c2[k];
+    }
+    d.scale = scale;
+    return d;
+  }
+  vec3 c1, c2;
+  float scale;
+};
+class NoiseTexture : public Texture2D {
+ public:
+  NoiseTexture(float scale, int fractal = 1) : scale(scale), fractal(fractal) {}
+  pt_texture_desc desc() const override {
+    pt_texture_desc d{};
+    d.kind = PT_TEX_NOISE;
+    d.scale = scale;
+    d.fractal = fractal;
+    return d;
+  }
+  float scale;
+  int fractal;
+};
+class ImageTexture : public Texture2D {
+ public:
+  ImageTexture(std::vector<float> texels, int width, int height)
+      : texels(std::move(texels)), width(width), height(height) {}
+  pt_texture_desc desc() const override {
+    pt_texture_desc d{};
+    d.kind = PT_TEX_IMAGE;
+    d.texels = texels.data();
+    d.width = width;
+    d.height = height;
+    return d;
+  }
+  std::vector<float> texels;
+  int width, height;
+};
+
 class Material {
  public:
   virtual ~Material() = default;
   virtual pt_material_desc desc() const = 0;
   virtual bool is_emitter() const { return false; }
+  // ColorVariant: the texture of the albedo / emission colour, if any
+  virtual std::shared_ptr<Texture2D> texture() const { return nullptr; }
 };
 namespace detail {
 inline pt_material_desc make(int32_t type, std::initializer_list<float> p, int32_t flags = 0) {
@@ -71,8 +138,11 @@ inline pt_material_desc make(int32_t type, std::initializer_list<float> p, int32
 class Lambertian : public Material {
  public:
   explicit Lambertian(vec3 albedo) : a(albedo) {}
+  explicit Lambertian(std::shared_ptr<Texture2D> t) : a(0.f), tex(std::move(t)) {}
   pt_material_desc desc() const override { return detail::make(PT_MAT_LAMBERTIAN, {a[0], a[1], a[2]}); }
+  std::shared_ptr<Texture2D> texture() const override { return tex; }
   vec3 a;
+  std::shared_ptr<Texture2D> tex;
 };
 class Conductor : public Material {
  public:
@@ -138,10 +208,13 @@ class HairMarschner : public Material {
 class DiffuseEmitter : public Material {
  public:
   explicit DiffuseEmitter(vec3 color, float intensity = 1.0f) : c(color), i(intensity) {}
+  DiffuseEmitter(std::shared_ptr<Texture2D> t, float intensity = 1.0f) : c(0.f), i(intensity), tex(std::move(t)) {}
   pt_material_desc desc() const override { return detail::make(PT_MAT_DIFFUSE_EMITTER, {c[0], c[1], c[2], i}); }
   bool is_emitter() const override { return true; }
+  std::shared_ptr<Texture2D> texture() const override { return tex; }
   vec3 c;
   float i;
+  std::shared_ptr<Texture2D> tex;
 };
 
 // ------------------------------------------------------------ geometry
@@ -157,6 +230,8 @@ struct Flat {
   std::vector<float> pos, nrm;   // positions; normals (a list, see nidx)
   std::vector<int32_t> idx;      // 3 position indices per triangle
   std::vector<int32_t> nidx;     // 3 normal indices per triangle (-1: none)
+  std::vector<float> uv;         // texture coordinates (a list, see uvidx)
+  std::vector<int32_t> uvidx;    // 3 uv indices per triangle (-1: none)
   pt_quad_desc quad{};
   pt_sphere_desc sphere{};
   std::shared_ptr<Material> mat;
@@ -217,10 +292,14 @@ class TriangleMesh : public Hittable {
     const bool has_n = !d.normals.empty() && d.normalIndices.size() == d.indices.size();
     if (has_n)
       for (auto &n : d.normals) f.nrm.insert(f.nrm.end(), {n[0], n[1], n[2]});
+    const bool has_uv = !d.uvs.empty() && d.uvIndices.size() == d.indices.size();
+    if (has_uv)
+      for (auto &u : d.uvs) f.uv.insert(f.uv.end(), {u.v[0], u.v[1]});
     for (size_t t = 0; t < d.indices.size(); ++t)
       for (int k = 0; k < 3; ++k) {
         f.idx.push_back(d.indices[t][k]);
         if (has_n) f.nidx.push_back(d.normalIndices[t][k]);
+        if (has_uv) f.uvidx.push_back(d.uvIndices[t][k]);
       }
     f.mat = m;
     return f;
@@ -404,11 +483,24 @@ struct SceneInfo {
     std::vector<pt_quad_desc> quads;
     std::vector<pt_sphere_desc> spheres;
     std::vector<pt_object_desc> objs;
+    std::vector<pt_texture_desc> texs;
+    std::vector<std::shared_ptr<Texture2D>> tex_objs;
     for (auto &h : objects.getLists()) flats.push_back(h->flatten());
     meshes.reserve(flats.size());
     for (auto &f : flats) {
       mats.push_back(f.mat->desc());
       const int32_t mi = (int32_t)mats.size() - 1;
+      if (auto t = f.mat->texture()) {
+        int ti = -1;
+        for (size_t k = 0; k < tex_objs.size(); ++k)
+          if (tex_objs[k] == t) ti = (int)k;
+        if (ti < 0) {
+          ti = (int)tex_objs.size();
+          tex_objs.push_back(t);
+          texs.push_back(t->desc());
+        }
+        mats[mi].flags |= (ti + 1) << PT_MAT_TEXTURE_SHIFT;
+      }
       if (f.kind == Flat::MESH) {
         pt_mesh_desc m{};
         m.positions = f.pos.data();
@@ -417,6 +509,11 @@ struct SceneInfo {
           m.normals = f.nrm.data();
           m.n_normals = (int32_t)(f.nrm.size() / 3);
           m.normal_indices = f.nidx.data();
+        }
+        if (!f.uv.empty()) {
+          m.uvs = f.uv.data();
+          m.n_uvs = (int32_t)(f.uv.size() / 2);
+          m.uv_indices = f.uvidx.data();
         }
         m.indices = f.idx.data();
         m.n_triangles = (int32_t)(f.idx.size() / 3);
@@ -444,6 +541,8 @@ struct SceneInfo {
     d.n_spheres = (int32_t)spheres.size();
     d.objects = objs.data();
     d.n_objects = (int32_t)objs.size();
+    d.textures = texs.data();
+    d.n_textures = (int32_t)texs.size();
     pt_env_desc env{};
     if (environment_light) {
       env = pt_env_desc{environment_light->texels.data(), environment_light->width, environment_light->height,

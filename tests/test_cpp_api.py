@@ -15,16 +15,54 @@ SRC = REPO / "tests" / "cpp" / "cornell_example.cpp"
 LIBDIR = REPO / "pathtracer_gb300" / "_lib"
 
 
-def _build(tmp_path):
-    exe = tmp_path / "cornell_example"
-    subprocess.run(["g++", "-std=c++17", "-O2", "-I", str(REPO / "include"), str(SRC), "-o", str(exe),
+def _build(tmp_path, src=SRC):
+    exe = tmp_path / src.stem
+    subprocess.run(["g++", "-std=c++17", "-O2", "-I", str(REPO / "include"), str(src), "-o", str(exe),
                     "-L", str(LIBDIR), "-lpathtracer_gb300", f"-Wl,-rpath,{LIBDIR}"], check=True)
     return exe
+
+
+TEXTURED = REPO / "tests" / "cpp" / "textured_example.cpp"
 
 
 @pytest.mark.skipif(shutil.which("g++") is None, reason="needs g++")
 def test_cpp_scene_compiles_and_links(tmp_path):
     assert _build(tmp_path).exists()
+    assert _build(tmp_path, TEXTURED).exists()
+
+
+@pytest.mark.gpu
+def test_cpp_textured_scene_renders_like_python(tmp_path):
+    from pathtracer_gb300 import native as N
+    from pathtracer_gb300 import scene as S
+
+    out = subprocess.run([str(_build(tmp_path, TEXTURED))], capture_output=True, text=True, check=True).stdout
+    cpp_mean = np.array([float(x) for x in out.split()])
+    sc = S.Scene()
+    checker = sc.add_texture(N.TEX_CHECKER, (0.1, 0.1, 0.1), (0.8, 0.8, 0.8), scale=40.0)
+    noise = sc.add_texture(N.TEX_NOISE, scale=8.0, fractal=4)
+    lchk = sc.add_texture(N.TEX_CHECKER, (4.0, 2.0, 0.5), (20.0, 14.0, 5.0), scale=30.0)
+    # materials in object order, as the C++ SceneInfo flattens them (one per object)
+    m_light = sc.add_material(N.DIFFUSE_EMITTER, [0, 0, 0, 1.0], texture=lchk)
+    m_w1 = sc.add_material(N.LAMBERTIAN, [0.75, 0.75, 0.75])
+    m_green = sc.add_material(N.LAMBERTIAN, [0.14, 0.45, 0.09])
+    m_floor = sc.add_material(N.LAMBERTIAN, [0, 0, 0], texture=checker)
+    m_w2 = sc.add_material(N.LAMBERTIAN, [0.75, 0.75, 0.75])
+    m_back = sc.add_material(N.LAMBERTIAN, [0, 0, 0], texture=noise)
+    m_ball = sc.add_material(N.LAMBERTIAN, [0, 0, 0], texture=noise)
+    sc.add_quad(1, 0.999, 0.3, 0.7, 0.3, 0.7, m_light)
+    sc.add_quad(0, 1.0, 0.0, 1.0, 0.0, 1.0, m_w1)
+    sc.add_quad(0, 0.0, 0.0, 1.0, 0.0, 1.0, m_green)
+    sc.add_quad(1, 0.0, 0.0, 1.0, 0.0, 1.0, m_floor)
+    sc.add_quad(1, 1.0, 0.0, 1.0, 0.0, 1.0, m_w2)
+    sc.add_quad(2, 1.0, 0.0, 1.0, 0.0, 1.0, m_back)
+    sc.add_sphere((0.5, 0.3, 0.55), 0.25, m_ball)
+    cam = S.camera((0.5, 0.5, -1.4), (0.0, 0.0, 1.0), 40.0, 1.0)
+    r = N.Renderer(0)
+    sid = r.upload(sc)
+    film = r.render(N.job_desc(sid, cam, 48, 48, 4, 4, 6, estimator=N.EST_NEE_MIS, env_sampling=N.ENV_ALIAS))
+    r.close()
+    np.testing.assert_allclose(cpp_mean, film.reshape(-1, 3).mean(0), rtol=1e-5)
 
 
 @pytest.mark.gpu
