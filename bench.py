@@ -210,7 +210,8 @@ def form_scenes(r, with_big: bool):
     return out, big, time.perf_counter() - t0
 
 
-def run_batched(r, scenes, n_jobs: int, seed: int = 11, res=(64, 1024), spp=(4, 256), tune: bool = True):
+def run_batched(r, scenes, n_jobs: int, seed: int = 11, res=(64, 1024), spp=(4, 256), tune: bool = True,
+                tune_sample: int = 8, tune_spp: int = 4):
     """Config-3 job mix: one pt_render_batch call (one CUDA-graph launch)
     against the plain wavefront drop-in (pt_render per job, one after the
     other); both with host films, so both are end to end.  The two arms
@@ -222,11 +223,13 @@ def run_batched(r, scenes, n_jobs: int, seed: int = 11, res=(64, 1024), spp=(4, 
     paths = sum(j.width * j.height * j.spp_x * j.spp_y for j in jobs)
     tuning, tune_s = None, 0.0
     if tune:
-        # autotune the batch launch on a small sample of the mix (first 8 jobs, 4 spp)
+        # autotune the batch launch on a sample of the mix (the first jobs,
+        # their spp capped at tune_spp)
         tj = []
-        for j in jobs[:8]:
+        for j in jobs[:tune_sample]:
             jj = type(j).from_buffer_copy(j)
-            jj.spp_x, jj.spp_y, jj.spp_begin, jj.spp_end = 2, 2, 0, 0
+            if jj.spp_x * jj.spp_y > tune_spp:
+                jj.spp_begin, jj.spp_end = 0, tune_spp
             tj.append(jj)
         t0 = time.perf_counter()
         tuning = r.autotune(tj)
@@ -546,7 +549,7 @@ def run_ours(args, rank, world, local_rank):
         # the regime batching exists for: many jobs far below one GPU's worth
         # of paths each (same scenes and cameras, smaller frames and spp)
         forms["batched_small_jobs"] = run_batched(r, fs, args.batch_jobs, seed=13, res=(64, 256), spp=(4, 32),
-                                                  tune=False)
+                                                  tune_sample=32, tune_spp=32)
         forms["served"] = run_served(r, fs, big, args.serve_seconds, args.serve_rate)
         line["forms"] = forms
     if not args.no_cpu_baseline:

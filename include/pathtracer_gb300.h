@@ -147,7 +147,17 @@ typedef struct pt_sphere_desc {
 /* Entry of the scene's ObjectList in insertion order (objectList.hpp:176).
  * The order fixes the top-level BVH build (bvh.hpp:46-102) and light
  * discovery order (lightDiscovery.hpp:5-81). */
-enum { PT_OBJ_MESH = 0, PT_OBJ_QUAD = 1, PT_OBJ_SPHERE = 2 };
+enum { PT_OBJ_MESH = 0, PT_OBJ_QUAD = 1, PT_OBJ_SPHERE = 2, PT_OBJ_BOX = 3 };
+
+/* Box(min_xyz, max_xyz, material) (include/primitives/box.hpp:5-53): one
+ * object of six rectangles, x1, x0, y1, y0, z1, z0 faces in that order,
+ * intersected as its ObjectList (closest of the six); its faces are not
+ * discovered as lights. */
+typedef struct pt_box_desc {
+  float min_xyz[3];
+  float max_xyz[3];
+  int32_t material;
+} pt_box_desc;
 typedef struct pt_object_desc {
   int32_t kind;
   int32_t index;
@@ -199,6 +209,8 @@ typedef struct pt_scene_desc {
   /* Textures referenced by materials (PT_MAT_TEXTURE_SHIFT). */
   const pt_texture_desc *textures;
   int32_t n_textures;
+  const pt_box_desc *boxes;     /* objects of kind PT_OBJ_BOX index these */
+  int32_t n_boxes;
 } pt_scene_desc;
 
 enum { PT_BVH_REFERENCE = 0 };

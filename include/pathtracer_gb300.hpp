@@ -226,7 +226,7 @@ struct MeshData {  // mesh_io/meshData.hpp:6-13
 
 // Flattened geometry of one object, in world space.
 struct Flat {
-  enum Kind { MESH, QUAD, SPHERE } kind = MESH;
+  enum Kind { MESH, QUAD, SPHERE, BOX } kind = MESH;
   std::vector<float> pos, nrm;   // positions; normals (a list, see nidx)
   std::vector<int32_t> idx;      // 3 position indices per triangle
   std::vector<int32_t> nidx;     // 3 normal indices per triangle (-1: none)
@@ -234,6 +234,7 @@ struct Flat {
   std::vector<int32_t> uvidx;    // 3 uv indices per triangle (-1: none)
   pt_quad_desc quad{};
   pt_sphere_desc sphere{};
+  pt_box_desc box{};
   std::shared_ptr<Material> mat;
 };
 
@@ -328,7 +329,45 @@ inline Flat quad_to_mesh(const Flat &q) {
   f.idx = {0, 1, 2, 0, 2, 3};
   return f;
 }
+// A Box as a mesh of its six faces (x1, x0, y1, y0, z1, z0), for rotations.
+inline Flat box_to_mesh(const Flat &b) {
+  Flat f;
+  f.kind = Flat::MESH;
+  f.mat = b.mat;
+  const float *lo = b.box.min_xyz, *hi = b.box.max_xyz;
+  const pt_quad_desc faces[6] = {{0, hi[0], lo[1], hi[1], lo[2], hi[2], 0, 0}, {0, lo[0], lo[1], hi[1], lo[2], hi[2], 0, 0},
+                                 {1, hi[1], lo[0], hi[0], lo[2], hi[2], 0, 0}, {1, lo[1], lo[0], hi[0], lo[2], hi[2], 0, 0},
+                                 {2, hi[2], lo[0], hi[0], lo[1], hi[1], 0, 0}, {2, lo[2], lo[0], hi[0], lo[1], hi[1], 0, 0}};
+  for (const pt_quad_desc &q : faces) {
+    Flat qf;
+    qf.kind = Flat::QUAD;
+    qf.quad = q;
+    Flat m = quad_to_mesh(qf);
+    const int32_t base = (int32_t)(f.pos.size() / 3);
+    f.pos.insert(f.pos.end(), m.pos.begin(), m.pos.end());
+    for (int32_t i : m.idx) f.idx.push_back(base + i);
+  }
+  return f;
+}
 }  // namespace detail
+
+// Box(min_xyz, max_xyz, material) (primitives/box.hpp:5-53).
+class Box : public Hittable {
+ public:
+  Box(vec3 min_xyz, vec3 max_xyz, std::shared_ptr<Material> m) : lo(min_xyz), hi(max_xyz), m(std::move(m)) {}
+  Flat flatten() const override {
+    Flat f;
+    f.kind = Flat::BOX;
+    for (int c = 0; c < 3; ++c) {
+      f.box.min_xyz[c] = lo[c];
+      f.box.max_xyz[c] = hi[c];
+    }
+    f.mat = m;
+    return f;
+  }
+  vec3 lo, hi;
+  std::shared_ptr<Material> m;
+};
 
 // objectTransform.hpp decorators, baked into the flattened geometry
 class FlipFace : public Hittable {
@@ -336,6 +375,7 @@ class FlipFace : public Hittable {
   explicit FlipFace(std::shared_ptr<Hittable> o) : o(std::move(o)) {}
   Flat flatten() const override {
     Flat f = o->flatten();
+    if (f.kind == Flat::BOX) f = detail::box_to_mesh(f);
     if (f.kind == Flat::QUAD) f.quad.flip_face ^= 1;
     if (f.kind == Flat::SPHERE) f.sphere.flip_face ^= 1;
     if (f.kind == Flat::MESH)  // reversed winding toggles the front-face flag
@@ -353,6 +393,11 @@ class Translate : public Hittable {
       for (size_t i = 0; i < f.pos.size(); ++i) f.pos[i] += off[(int)(i % 3)];
     if (f.kind == Flat::SPHERE)
       for (int c = 0; c < 3; ++c) f.sphere.center[c] += off[c];
+    if (f.kind == Flat::BOX)
+      for (int c = 0; c < 3; ++c) {
+        f.box.min_xyz[c] += off[c];
+        f.box.max_xyz[c] += off[c];
+      }
     if (f.kind == Flat::QUAD) {
       const int a = f.quad.axis, a0 = a == 0 ? 1 : 0, a1 = a == 2 ? 1 : 2;
       f.quad.k += off[a];
@@ -376,6 +421,11 @@ class Scale : public Hittable {
       for (int c = 0; c < 3; ++c) f.sphere.center[c] *= s;
       f.sphere.radius *= s;
     }
+    if (f.kind == Flat::BOX)
+      for (int c = 0; c < 3; ++c) {
+        f.box.min_xyz[c] *= s;
+        f.box.max_xyz[c] *= s;
+      }
     if (f.kind == Flat::QUAD) {
       f.quad.k *= s;
       f.quad.d0_min *= s;
@@ -395,6 +445,7 @@ class Rotate : public Hittable {
   Flat flatten() const override {
     Flat f = o->flatten();
     if (f.kind == Flat::QUAD) f = detail::quad_to_mesh(f);
+    if (f.kind == Flat::BOX) f = detail::box_to_mesh(f);
     const float c = std::cos(r), s = std::sin(r);
     const int i = A == Axis::X ? 1 : A == Axis::Y ? 2 : 0, j = A == Axis::X ? 2 : A == Axis::Y ? 0 : 1;
     auto rot = [&](float *p) {
@@ -483,6 +534,7 @@ struct SceneInfo {
     std::vector<pt_quad_desc> quads;
     std::vector<pt_sphere_desc> spheres;
     std::vector<pt_object_desc> objs;
+    std::vector<pt_box_desc> boxes;
     std::vector<pt_texture_desc> texs;
     std::vector<std::shared_ptr<Texture2D>> tex_objs;
     for (auto &h : objects.getLists()) flats.push_back(h->flatten());
@@ -520,6 +572,10 @@ struct SceneInfo {
         m.material = mi;
         meshes.push_back(m);
         objs.push_back({PT_OBJ_MESH, (int32_t)meshes.size() - 1});
+      } else if (f.kind == Flat::BOX) {
+        f.box.material = mi;
+        boxes.push_back(f.box);
+        objs.push_back({PT_OBJ_BOX, (int32_t)boxes.size() - 1});
       } else if (f.kind == Flat::QUAD) {
         f.quad.material = mi;
         quads.push_back(f.quad);
@@ -543,6 +599,8 @@ struct SceneInfo {
     d.n_objects = (int32_t)objs.size();
     d.textures = texs.data();
     d.n_textures = (int32_t)texs.size();
+    d.boxes = boxes.data();
+    d.n_boxes = (int32_t)boxes.size();
     pt_env_desc env{};
     if (environment_light) {
       env = pt_env_desc{environment_light->texels.data(), environment_light->width, environment_light->height,

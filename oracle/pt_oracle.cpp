@@ -802,6 +802,7 @@ static V tex_eval(const Tex &T, float u, float v) {
 struct Scene {
   std::vector<Material> mats;
   std::vector<Tex> texs;
+  std::vector<struct Obj> box_faces;  // six rectangles per Box object
   // The material at a hit, with a textured colour (ColorVariant, Lambertian
   // albedo / DiffuseEmitter colour) looked up at the hit's texCoords.
   Material shade_mat(const Hit &rec) const {
@@ -864,6 +865,22 @@ struct Scene {
   // ray.
   bool hit_obj(int oi, V o_w, V d, float tmin, float tmax, Hit &rec, float time) const {
     const Obj &ob = objs[oi];
+    if (ob.kind == PT_OBJ_BOX) {  // Box::intersect: its ObjectList, closest face (objectList.hpp:84-105)
+      bool hit = false;
+      float closest = tmax;
+      for (int k = 0; k < 6; ++k) {
+        Hit tmp;
+        if (hit_objref(box_faces[ob.index * 6 + k], o_w, d, tmin, closest, tmp, time)) {
+          hit = true;
+          closest = tmp.t;
+          rec = tmp;
+        }
+      }
+      return hit;
+    }
+    return hit_objref(ob, o_w, d, tmin, tmax, rec, time);
+  }
+  bool hit_objref(const Obj &ob, V o_w, V d, float tmin, float tmax, Hit &rec, float time) const {
     const V o = ob.moving ? V(o_w.x - ob.vel.x * time, o_w.y - ob.vel.y * time, o_w.z - ob.vel.z * time) : o_w;
     if (ob.kind == PT_OBJ_MESH) {
       const MeshO &M = meshes[ob.index];
@@ -1069,13 +1086,37 @@ Scene *build_scene(const pt_scene_desc *d) {
       lo[a1] = q.d1_min;
       hi[a1] = q.d1_max;
       ob.box = Box{lo, hi};
+    } else if (od.kind == PT_OBJ_BOX) {  // Box (box.hpp:5-53): six faces x1, x0, y1, y0, z1, z0
+      const pt_box_desc &bx = d->boxes[od.index];
+      const float *lo = bx.min_xyz, *hi = bx.max_xyz;
+      const float f[6][6] = {{0, hi[0], lo[1], hi[1], lo[2], hi[2]}, {0, lo[0], lo[1], hi[1], lo[2], hi[2]},
+                             {1, hi[1], lo[0], hi[0], lo[2], hi[2]}, {1, lo[1], lo[0], hi[0], lo[2], hi[2]},
+                             {2, hi[2], lo[0], hi[0], lo[1], hi[1]}, {2, lo[2], lo[0], hi[0], lo[1], hi[1]}};
+      ob.mat = bx.material;
+      ob.box = Box{V(lo[0], lo[1], lo[2]), V(hi[0], hi[1], hi[2])};
+      if ((int)S->box_faces.size() < 6 * (od.index + 1)) S->box_faces.resize(6 * (od.index + 1));
+      for (int k = 0; k < 6; ++k) {
+        Obj q{};
+        q.kind = PT_OBJ_QUAD;
+        q.axis = (int)f[k][0];
+        q.k = f[k][1];
+        q.d0min = f[k][2];
+        q.d0max = f[k][3];
+        q.d1min = f[k][4];
+        q.d1max = f[k][5];
+        q.mat = bx.material;
+        q.prim = n_tris + d->n_quads + 6 * od.index + k;
+        q.vel = ob.vel;
+        q.moving = ob.moving;
+        S->box_faces[6 * od.index + k] = q;
+      }
     } else {
       const pt_sphere_desc &s = d->spheres[od.index];
       ob.c = V(s.center[0], s.center[1], s.center[2]);
       ob.r = s.radius;
       ob.mat = s.material;
       ob.flip = s.flip_face;
-      ob.prim = n_tris + d->n_quads + od.index;
+      ob.prim = n_tris + d->n_quads + 6 * (d->boxes ? d->n_boxes : 0) + od.index;
       ob.box = Box{ob.c - V(s.radius), ob.c + V(s.radius)};
     }
     if (ob.moving) {  // the box covers the motion over [0, shutter_max]
@@ -1088,7 +1129,7 @@ Scene *build_scene(const pt_scene_desc *d) {
   S->root = S->build_top(0, (int)S->objs.size());
   // lights (lightDiscovery.hpp:5-81, light.hpp:55-306)
   for (auto &ob : S->objs) {
-    if (ob.kind == PT_OBJ_MESH) continue;
+    if (ob.kind == PT_OBJ_MESH || ob.kind == PT_OBJ_BOX) continue;
     const Material &m = S->mats[ob.mat];
     if (m.type != PT_MAT_DIFFUSE_EMITTER || m.p[3] <= 0.f) continue;
     Light L{};

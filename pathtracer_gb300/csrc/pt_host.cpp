@@ -196,6 +196,7 @@ struct BNode {
 
 struct Builder {
   const pt_scene_desc *d;
+  int box_quad_base = 0;          // first rectangle of the boxes' faces
   int threads = 0;               // mesh BVH build workers (0: hardware threads)
   std::vector<int> obj_motion;   // per object: motion index + 1 (0: static)
   std::vector<BNode> nodes;
@@ -348,6 +349,12 @@ struct Builder {
         b.lo[a] -= 1e-3f;
         b.hi[a] += 1e-3f;
       }
+    } else if (od.kind == PT_OBJ_BOX) {  // Box::getAABB (box.hpp:36)
+      const pt_box_desc &bx = d->boxes[od.index];
+      for (int a = 0; a < 3; ++a) {
+        b.lo[a] = bx.min_xyz[a];
+        b.hi[a] = bx.max_xyz[a];
+      }
     } else if (od.kind == PT_OBJ_QUAD) {  // AARectangle::getAABB (primitive.cpp:6-28)
       const pt_quad_desc &q = d->quads[od.index];
       int a0 = q.axis == 0 ? 1 : 0, a1 = q.axis == 2 ? 1 : 2;
@@ -395,9 +402,14 @@ struct Builder {
       nodes.push_back(BNode());
       nodes[me].box = object_box(o);
       nodes[me].first = (int)leaf_prims.size();
-      nodes[me].count = 1;
-      int prim = od.kind == PT_OBJ_QUAD ? n_tris + od.index : n_tris + d->n_quads + od.index;
-      leaf_prims.push_back(prim);
+      if (od.kind == PT_OBJ_BOX) {  // one leaf: the six faces in the box's order
+        nodes[me].count = 6;
+        for (int k = 0; k < 6; ++k) leaf_prims.push_back(n_tris + box_quad_base + 6 * od.index + k);
+      } else {
+        nodes[me].count = 1;
+        int prim = od.kind == PT_OBJ_QUAD ? n_tris + od.index : n_tris + d->n_quads + od.index;
+        leaf_prims.push_back(prim);
+      }
     }
     inst_motion.resize(nodes.size(), 0);
     sweep_root(me, o);
@@ -629,14 +641,39 @@ static uint64_t fnv1a(const void *p, size_t n, uint64_t h) {
 // Builds a scene; with device = false only the host part (validation, BVH,
 // tables) runs, without touching the GPU.  threads: worker threads of the
 // mesh BVH build (0: all hardware threads).
-std::unique_ptr<Scene> build_scene(const pt_scene_desc *d, cudaStream_t st, bool device, int threads,
+// Box faces (box.hpp:16-33): YZ at x1, x0; XZ at y1, y0; XY at z1, z0.
+static void box_faces(const pt_box_desc &b, std::vector<pt_quad_desc> &out) {
+  const float *lo = b.min_xyz, *hi = b.max_xyz;
+  out.push_back(pt_quad_desc{0, hi[0], lo[1], hi[1], lo[2], hi[2], b.material, 0});
+  out.push_back(pt_quad_desc{0, lo[0], lo[1], hi[1], lo[2], hi[2], b.material, 0});
+  out.push_back(pt_quad_desc{1, hi[1], lo[0], hi[0], lo[2], hi[2], b.material, 0});
+  out.push_back(pt_quad_desc{1, lo[1], lo[0], hi[0], lo[2], hi[2], b.material, 0});
+  out.push_back(pt_quad_desc{2, hi[2], lo[0], hi[0], lo[1], hi[1], b.material, 0});
+  out.push_back(pt_quad_desc{2, lo[2], lo[0], hi[0], lo[1], hi[1], b.material, 0});
+}
+
+std::unique_ptr<Scene> build_scene(const pt_scene_desc *d_in, cudaStream_t st, bool device, int threads,
                                    int trav_cap) {
-  if (!d) fail(PT_ERR_INVALID, "null scene description");
+  if (!d_in) fail(PT_ERR_INVALID, "null scene description");
+  // boxes become six rectangles each, after the scene's own rectangles
+  pt_scene_desc aug = *d_in;
+  std::vector<pt_quad_desc> all_quads;
+  const int n_boxes = d_in->boxes ? d_in->n_boxes : 0;
+  if (n_boxes < 0) fail(PT_ERR_INVALID, "negative box count");
+  if (n_boxes > 0) {
+    all_quads.assign(d_in->quads, d_in->quads + std::max(0, d_in->n_quads));
+    for (int b = 0; b < n_boxes; ++b) box_faces(d_in->boxes[b], all_quads);
+    aug.quads = all_quads.data();
+    aug.n_quads = (int32_t)all_quads.size();
+  }
+  const pt_scene_desc *d = &aug;
+  const int n_user_quads = d_in->n_quads;
   if (d->n_objects <= 0) fail(PT_ERR_INVALID, "scene has no objects");  // renderManager.hpp:64
   auto S = std::make_unique<Scene>();
   Builder B;
   B.d = d;
   B.threads = threads;
+  B.box_quad_base = n_user_quads;
   for (int m = 0; m < d->n_meshes; ++m) {
     const pt_mesh_desc &md = d->meshes[m];
     if (md.n_triangles < 0 || (md.n_triangles > 0 && (!md.positions || !md.indices)))
@@ -657,8 +694,11 @@ std::unique_ptr<Scene> build_scene(const pt_scene_desc *d, cudaStream_t st, bool
       fail(PT_ERR_INVALID, "bad sphere");
   for (int o = 0; o < d->n_objects; ++o) {
     const pt_object_desc &od = d->objects[o];
-    int lim = od.kind == PT_OBJ_MESH ? d->n_meshes : od.kind == PT_OBJ_QUAD ? d->n_quads : d->n_spheres;
-    if (od.kind < 0 || od.kind > 2 || od.index < 0 || od.index >= lim)
+    int lim = od.kind == PT_OBJ_MESH ? d->n_meshes
+              : od.kind == PT_OBJ_QUAD ? n_user_quads
+              : od.kind == PT_OBJ_BOX  ? n_boxes
+                                       : d->n_spheres;
+    if (od.kind < 0 || od.kind > 3 || od.index < 0 || od.index >= lim)
       fail(PT_ERR_INVALID, "bad object entry");
   }
   const int n_prims = B.n_tris + d->n_quads + d->n_spheres;
@@ -679,7 +719,10 @@ std::unique_ptr<Scene> build_scene(const pt_scene_desc *d, cudaStream_t st, bool
     if (od.kind == PT_OBJ_MESH) {
       for (int t = 0; t < d->meshes[od.index].n_triangles; ++t) prim_motion[B.tri_base[od.index] + t] = m;
     } else {
-      prim_motion[od.kind == PT_OBJ_QUAD ? B.n_tris + od.index : B.n_tris + d->n_quads + od.index] = m;
+      if (od.kind == PT_OBJ_BOX)
+        for (int k = 0; k < 6; ++k) prim_motion[B.n_tris + n_user_quads + 6 * od.index + k] = m;
+      else
+        prim_motion[od.kind == PT_OBJ_QUAD ? B.n_tris + od.index : B.n_tris + d->n_quads + od.index] = m;
     }
   }
   if (!motion.empty() && !(d->shutter_max > 0.f) )
@@ -907,7 +950,7 @@ std::unique_ptr<Scene> build_scene(const pt_scene_desc *d, cudaStream_t st, bool
   std::vector<LightRec> lights;
   for (int o = 0; o < d->n_objects; ++o) {
     const pt_object_desc &od = d->objects[o];
-    if (od.kind == PT_OBJ_MESH) continue;  // meshes are not discovered as lights
+    if (od.kind == PT_OBJ_MESH || od.kind == PT_OBJ_BOX) continue;  // not discovered as lights
     int mi = od.kind == PT_OBJ_QUAD ? d->quads[od.index].material : d->spheres[od.index].material;
     const pt_material_desc &md = d->materials[mi];
     if (md.type != PT_MAT_DIFFUSE_EMITTER || md.p[3] <= 0.f) continue;

@@ -23,7 +23,7 @@ ERRORS = {
 # material types (pathtracer_gb300.h)
 LAMBERTIAN, CONDUCTOR, MF_DIELECTRIC, THIN_DIELECTRIC, PHONG, DISNEY, HAIR, DIFFUSE_EMITTER = range(8)
 FLAG_SPLIT_RAY, FLAG_MELANIN = 1, 2
-OBJ_MESH, OBJ_QUAD, OBJ_SPHERE = 0, 1, 2
+OBJ_MESH, OBJ_QUAD, OBJ_SPHERE, OBJ_BOX = 0, 1, 2, 3
 EST_REF_NEE, EST_NEE_MIS = 0, 1
 SAMPLER_HALTON_NONE, SAMPLER_HALTON_PERMUTE, SAMPLER_HALTON_OWEN, SAMPLER_STRATIFIED = range(4)
 ENV_UNIFORM, ENV_ALIAS = 0, 1
@@ -82,6 +82,10 @@ class ObjectDesc(C.Structure):
     _fields_ = [("kind", C.c_int32), ("index", C.c_int32), ("velocity", C.c_float * 3)]
 
 
+class BoxDesc(C.Structure):
+    _fields_ = [("min_xyz", C.c_float * 3), ("max_xyz", C.c_float * 3), ("material", C.c_int32)]
+
+
 class EnvDesc(C.Structure):
     _fields_ = [("texels", f32p), ("width", C.c_int32), ("height", C.c_int32), ("intensity", C.c_float)]
 
@@ -100,6 +104,7 @@ class SceneDesc(C.Structure):
         ("env", C.POINTER(EnvDesc)), ("medium", C.POINTER(MediumDesc)),
         ("bg_color", C.c_float * 3), ("bvh_mode", C.c_int32), ("shutter_max", C.c_float),
         ("textures", C.POINTER(TextureDesc)), ("n_textures", C.c_int32),
+        ("boxes", C.POINTER(BoxDesc)), ("n_boxes", C.c_int32),
     ]
 
 
@@ -284,6 +289,13 @@ def make_scene_desc(scene) -> SceneBuffers:
         d.medium = C.pointer(md)
     d.bg_color[:] = [float(x) for x in scene.bg]
     d.shutter_max = float(getattr(scene, "shutter_max", 0.0))
+    boxes = getattr(scene, "boxes", [])
+    if boxes:
+        barr = (BoxDesc * len(boxes))(*[BoxDesc((C.c_float * 3)(*[float(x) for x in b[0]]),
+                                                (C.c_float * 3)(*[float(x) for x in b[1]]), b[2]) for b in boxes])
+        sb.hold(barr)
+        d.boxes = barr
+        d.n_boxes = len(boxes)
     texs = getattr(scene, "textures", [])
     if texs:
         arr = (TextureDesc * len(texs))()

@@ -49,6 +49,7 @@ class Scene:
     bg: tuple = (0.0, 0.0, 0.0)
     shutter_max: float = 0.0                        # motion blur: longest shutter of any job
     textures: list = field(default_factory=list)    # dicts: kind, color1, color2, scale, fractal, texels
+    boxes: list = field(default_factory=list)       # (min_xyz, max_xyz, material)
 
     def add_material(self, mtype: int, params, flags: int = 0, texture: int | None = None) -> int:
         """A material; `texture` (an index from add_texture) replaces the
@@ -78,6 +79,11 @@ class Scene:
     def add_sphere(self, center, radius, material, flip=0, velocity=(0.0, 0.0, 0.0)):
         self.spheres.append((tuple(center), radius, material, flip))
         self.objects.append((N.OBJ_SPHERE, len(self.spheres) - 1, tuple(velocity)))
+
+    def add_box(self, min_xyz, max_xyz, material, velocity=(0.0, 0.0, 0.0)):
+        """Box(min_xyz, max_xyz, material): one object of six rectangles."""
+        self.boxes.append((tuple(min_xyz), tuple(max_xyz), material))
+        self.objects.append((N.OBJ_BOX, len(self.boxes) - 1, tuple(velocity)))
 
     @property
     def has_motion(self) -> bool:

@@ -58,3 +58,25 @@ def test_textures_move_with_objects(renderer):
     S.with_motion(sc, seed=3, speed=0.5)
     job = N.job_desc(0, dict(cam, shutter=0.4), 40, 40, 4, 4, 6, seed=2, estimator=N.EST_NEE_MIS)
     _compare(renderer, sc, job, 16)
+
+
+def test_box_matches_oracle(renderer):
+    sc, cam = S.cornell_icosphere(2)
+    tex = sc.add_texture(N.TEX_CHECKER, (0.1, 0.2, 0.6), (0.9, 0.8, 0.2), 25.0)
+    sc.add_box((0.15, 0.0, 0.5), (0.45, 0.35, 0.8), sc.add_material(N.LAMBERTIAN, [0, 0, 0], texture=tex))
+    sc.add_box((0.6, 0.0, 0.15), (0.85, 0.2, 0.4), sc.add_material(N.CONDUCTOR, [*S.GOLD_ETA, *S.GOLD_K, 0.2, 0.2]))
+    job = N.job_desc(0, cam, 40, 40, 4, 4, 6, seed=3, estimator=N.EST_NEE_MIS)
+    _compare(renderer, sc, job, 16)
+    # closest-hit ids: the boxes' faces follow the scene's rectangles
+    rng = np.random.default_rng(5)
+    o = np.tile([0.5, 0.5, -1.0], (2048, 1)) + rng.normal(0, 0.02, (2048, 3))
+    d = np.stack([rng.uniform(-0.35, 0.35, 2048), rng.uniform(-0.4, 0.2, 2048), np.ones(2048)], 1)
+    rays = np.concatenate([o, d], 1).astype(np.float32)
+    sid = renderer.upload(sc)
+    t, prim, _ = renderer.trace_closest(sid, rays)
+    renderer.release(sid)
+    osc = O.OracleScene(sc)
+    t_o, prim_o = osc.trace_closest(rays)
+    assert (prim == prim_o).mean() > 0.999
+    both = (prim == prim_o) & (prim >= 0)
+    assert np.allclose(t[both], t_o[both], rtol=1e-5)
