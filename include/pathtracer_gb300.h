@@ -147,7 +147,18 @@ typedef struct pt_sphere_desc {
 /* Entry of the scene's ObjectList in insertion order (objectList.hpp:176).
  * The order fixes the top-level BVH build (bvh.hpp:46-102) and light
  * discovery order (lightDiscovery.hpp:5-81). */
-enum { PT_OBJ_MESH = 0, PT_OBJ_QUAD = 1, PT_OBJ_SPHERE = 2, PT_OBJ_BOX = 3 };
+enum { PT_OBJ_MESH = 0, PT_OBJ_QUAD = 1, PT_OBJ_SPHERE = 2, PT_OBJ_BOX = 3, PT_OBJ_CURVE = 4 };
+
+/* Curve(cps, width0, width1, material) (include/primitives/curve.hpp:13-157):
+ * a cubic Bezier intersected as 8 cylinder segments, radius the mean of the
+ * linearly interpolated width at the segment's ends; its hit carries the
+ * curve tangent (HitRecord::hair_tangent), which HairMarschner uses as its
+ * frame.  Not discovered as a light. */
+typedef struct pt_curve_desc {
+  float cps[4][3];
+  float width0, width1;
+  int32_t material;
+} pt_curve_desc;
 
 /* Box(min_xyz, max_xyz, material) (include/primitives/box.hpp:5-53): one
  * object of six rectangles, x1, x0, y1, y0, z1, z0 faces in that order,
@@ -211,6 +222,8 @@ typedef struct pt_scene_desc {
   int32_t n_textures;
   const pt_box_desc *boxes;     /* objects of kind PT_OBJ_BOX index these */
   int32_t n_boxes;
+  const pt_curve_desc *curves;  /* objects of kind PT_OBJ_CURVE index these */
+  int32_t n_curves;
 } pt_scene_desc;
 
 enum { PT_BVH_REFERENCE = 0 };

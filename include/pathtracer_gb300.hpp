@@ -226,7 +226,7 @@ struct MeshData {  // mesh_io/meshData.hpp:6-13
 
 // Flattened geometry of one object, in world space.
 struct Flat {
-  enum Kind { MESH, QUAD, SPHERE, BOX } kind = MESH;
+  enum Kind { MESH, QUAD, SPHERE, BOX, CURVE } kind = MESH;
   std::vector<float> pos, nrm;   // positions; normals (a list, see nidx)
   std::vector<int32_t> idx;      // 3 position indices per triangle
   std::vector<int32_t> nidx;     // 3 normal indices per triangle (-1: none)
@@ -235,6 +235,7 @@ struct Flat {
   pt_quad_desc quad{};
   pt_sphere_desc sphere{};
   pt_box_desc box{};
+  pt_curve_desc curve{};
   std::shared_ptr<Material> mat;
 };
 
@@ -351,6 +352,27 @@ inline Flat box_to_mesh(const Flat &b) {
 }
 }  // namespace detail
 
+// Curve(cps, width0, width1, CurveType::Cylinder, material)
+// (primitives/curve.hpp:13-157).
+class Curve : public Hittable {
+ public:
+  Curve(const std::array<vec3, 4> &cps, float width0, float width1, std::shared_ptr<Material> m)
+      : cps(cps), w0(width0), w1(width1), m(std::move(m)) {}
+  Flat flatten() const override {
+    Flat f;
+    f.kind = Flat::CURVE;
+    for (int k = 0; k < 4; ++k)
+      for (int c = 0; c < 3; ++c) f.curve.cps[k][c] = cps[k][c];
+    f.curve.width0 = w0;
+    f.curve.width1 = w1;
+    f.mat = m;
+    return f;
+  }
+  std::array<vec3, 4> cps;
+  float w0, w1;
+  std::shared_ptr<Material> m;
+};
+
 // Box(min_xyz, max_xyz, material) (primitives/box.hpp:5-53).
 class Box : public Hittable {
  public:
@@ -398,6 +420,9 @@ class Translate : public Hittable {
         f.box.min_xyz[c] += off[c];
         f.box.max_xyz[c] += off[c];
       }
+    if (f.kind == Flat::CURVE)
+      for (int k = 0; k < 4; ++k)
+        for (int c = 0; c < 3; ++c) f.curve.cps[k][c] += off[c];
     if (f.kind == Flat::QUAD) {
       const int a = f.quad.axis, a0 = a == 0 ? 1 : 0, a1 = a == 2 ? 1 : 2;
       f.quad.k += off[a];
@@ -426,6 +451,12 @@ class Scale : public Hittable {
         f.box.min_xyz[c] *= s;
         f.box.max_xyz[c] *= s;
       }
+    if (f.kind == Flat::CURVE) {
+      for (int k = 0; k < 4; ++k)
+        for (int c = 0; c < 3; ++c) f.curve.cps[k][c] *= s;
+      f.curve.width0 *= s;
+      f.curve.width1 *= s;
+    }
     if (f.kind == Flat::QUAD) {
       f.quad.k *= s;
       f.quad.d0_min *= s;
@@ -456,6 +487,8 @@ class Rotate : public Hittable {
     for (size_t k = 0; k + 2 < f.pos.size(); k += 3) rot(&f.pos[k]);
     for (size_t k = 0; k + 2 < f.nrm.size(); k += 3) rot(&f.nrm[k]);
     if (f.kind == Flat::SPHERE) rot(f.sphere.center);
+    if (f.kind == Flat::CURVE)
+      for (int k = 0; k < 4; ++k) rot(f.curve.cps[k]);
     return f;
   }
   std::shared_ptr<Hittable> o;
@@ -535,6 +568,7 @@ struct SceneInfo {
     std::vector<pt_sphere_desc> spheres;
     std::vector<pt_object_desc> objs;
     std::vector<pt_box_desc> boxes;
+    std::vector<pt_curve_desc> curves;
     std::vector<pt_texture_desc> texs;
     std::vector<std::shared_ptr<Texture2D>> tex_objs;
     for (auto &h : objects.getLists()) flats.push_back(h->flatten());
@@ -572,6 +606,10 @@ struct SceneInfo {
         m.material = mi;
         meshes.push_back(m);
         objs.push_back({PT_OBJ_MESH, (int32_t)meshes.size() - 1});
+      } else if (f.kind == Flat::CURVE) {
+        f.curve.material = mi;
+        curves.push_back(f.curve);
+        objs.push_back({PT_OBJ_CURVE, (int32_t)curves.size() - 1});
       } else if (f.kind == Flat::BOX) {
         f.box.material = mi;
         boxes.push_back(f.box);
@@ -601,6 +639,8 @@ struct SceneInfo {
     d.n_textures = (int32_t)texs.size();
     d.boxes = boxes.data();
     d.n_boxes = (int32_t)boxes.size();
+    d.curves = curves.data();
+    d.n_curves = (int32_t)curves.size();
     pt_env_desc env{};
     if (environment_light) {
       env = pt_env_desc{environment_light->texels.data(), environment_light->width, environment_light->height,

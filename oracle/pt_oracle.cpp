@@ -283,7 +283,8 @@ static float hair_at(const Material &m, V wol, V wil) {  // hairPDF.cpp:101-152
 }
 
 bool mat_scatter(const Material &m, V ray_dir, const Hit &rec, Scatter &s, float uc, float u0, float u1) {
-  const V n = rec.normal;
+  // HairMarschner's frame is the hair tangent when set (hairMarsch.cpp:12-19)
+  const V n = (m.type == PT_MAT_HAIR && rec.has_tangent) ? rec.tangent : rec.normal;
   const V wo = -ray_dir.normalize();
   switch (m.type) {
   case PT_MAT_LAMBERTIAN: {  // material.hpp:88-105
@@ -464,7 +465,8 @@ bool mat_scatter(const Material &m, V ray_dir, const Hit &rec, Scatter &s, float
 }
 
 V mat_f(const Material &m, V wo, V wi, const Hit &rec) {
-  const V n = rec.normal;
+  // HairMarschner's frame is the hair tangent when set (hairMarsch.cpp:12-19)
+  const V n = (m.type == PT_MAT_HAIR && rec.has_tangent) ? rec.tangent : rec.normal;
   switch (m.type) {
   case PT_MAT_LAMBERTIAN:
     return base_color(m) * (float)(1.0f / PI);
@@ -514,7 +516,8 @@ V mat_f(const Material &m, V wo, V wi, const Hit &rec) {
 }
 
 float mat_pdf(const Material &m, V wo, V wi, const Hit &rec) {
-  const V n = rec.normal;
+  // HairMarschner's frame is the hair tangent when set (hairMarsch.cpp:12-19)
+  const V n = (m.type == PT_MAT_HAIR && rec.has_tangent) ? rec.tangent : rec.normal;
   switch (m.type) {
   case PT_MAT_LAMBERTIAN:
     return cosine_pdf_at(n, wi);
@@ -695,6 +698,8 @@ struct MeshO {
 
 struct Obj {
   int kind, index;
+  V cps[4];            // curve control points
+  float w0 = 0, w1 = 0;  // curve widths
   V vel;               // motion blur (extension): position + vel * time
   bool moving = false;
   Box box;
@@ -865,6 +870,7 @@ struct Scene {
   // ray.
   bool hit_obj(int oi, V o_w, V d, float tmin, float tmax, Hit &rec, float time) const {
     const Obj &ob = objs[oi];
+    if (ob.kind == PT_OBJ_CURVE) return hit_curve(ob, o_w, d, tmin, tmax, rec, time);
     if (ob.kind == PT_OBJ_BOX) {  // Box::intersect: its ObjectList, closest face (objectList.hpp:84-105)
       bool hit = false;
       float closest = tmax;
@@ -880,6 +886,70 @@ struct Scene {
     }
     return hit_objref(ob, o_w, d, tmin, tmax, rec, time);
   }
+  static V bezier(const V *c, float u) {  // bezier.hpp:10-18
+    float u1 = 1.0f - u;
+    float b0 = u1 * u1 * u1, b1 = 3.0f * u * u1 * u1, b2 = 3.0f * u * u * u1, b3 = u * u * u;
+    return c[0] * b0 + c[1] * b1 + c[2] * b2 + c[3] * b3;
+  }
+  static V bezier_d(const V *c, float u) {  // bezier.hpp:24-36
+    V d0 = 3.0f * (c[1] - c[0]), d1 = 3.0f * (c[2] - c[1]), d2 = 3.0f * (c[3] - c[2]);
+    float u1 = 1.0f - u;
+    return d0 * (u1 * u1) + d1 * (2.0f * u * u1) + d2 * (u * u);
+  }
+  // Curve::intersect (curve.hpp:48-129), in the curve's frame at the ray's time
+  bool hit_curve(const Obj &ob, V o_w, V d, float tmin, float tmax, Hit &rec, float time) const {
+    const V o = ob.moving ? V(o_w.x - ob.vel.x * time, o_w.y - ob.vel.y * time, o_w.z - ob.vel.z * time) : o_w;
+    const int N = 8;
+    float bestT = tmax;
+    bool found = false;
+    V bestP, bestN, bestT3;
+    for (int i = 0; i < N; ++i) {
+      const V pa = bezier(ob.cps, float(i) / N), pb = bezier(ob.cps, float(i + 1) / N);
+      const float u0 = float(i) / N, u1 = float(i + 1) / N;
+      const float r0 = ob.w0 + (ob.w1 - ob.w0) * u0, r1 = ob.w0 + (ob.w1 - ob.w0) * u1;
+      const float radius = 0.5f * (r0 + r1);
+      const float segLen = (pb - pa).length();
+      const V axis = (pb - pa) / segLen;
+      const V d_perp = d - dot(d, axis) * axis;
+      const V delta = o - pa;
+      const V o_perp = delta - dot(delta, axis) * axis;
+      const float A = dot(d_perp, d_perp), B = 2.0f * dot(d_perp, o_perp);
+      const float C = dot(o_perp, o_perp) - radius * radius;
+      const float disc = B * B - 4 * A * C;  // gl::solveQuadratic (utility.hpp:112-124)
+      if (disc < 0) continue;
+      const float sq = std::sqrt(disc);
+      const float q = B < 0 ? -0.5f * (B - sq) : -0.5f * (B + sq);
+      float roots[2] = {q / A, C / q};
+      if (roots[0] > roots[1]) std::swap(roots[0], roots[1]);
+      const int nr = roots[0] == roots[1] ? 1 : 2;
+      for (int r = 0; r < nr; ++r) {
+        const float t = roots[r];
+        if (t < tmin || t > bestT) continue;
+        const V hp = o + t * d;
+        const float proj = dot(hp - pa, axis);
+        if (proj < 0.0f || proj > segLen) continue;
+        bestT = t;
+        bestP = hp;
+        const float uu = proj / segLen;
+        const V d0 = bezier_d(ob.cps, u0), d1 = bezier_d(ob.cps, u1);
+        bestT3 = (d0 + (d1 - d0) * uu).normalize();
+        const V v = hp - (pa + axis * proj);
+        bestN = (v - dot(v, bestT3) * bestT3).normalize();
+        found = true;
+      }
+    }
+    if (!found) return false;
+    rec.t = bestT;
+    rec.position = o_w + bestT * d;
+    rec.tangent = bestT3;
+    rec.has_tangent = true;
+    rec.set_normal(d, bestN);
+    rec.mat = ob.mat;
+    rec.prim = ob.prim;
+    rec.light = -1;
+    return true;
+  }
+
   bool hit_objref(const Obj &ob, V o_w, V d, float tmin, float tmax, Hit &rec, float time) const {
     const V o = ob.moving ? V(o_w.x - ob.vel.x * time, o_w.y - ob.vel.y * time, o_w.z - ob.vel.z * time) : o_w;
     if (ob.kind == PT_OBJ_MESH) {
@@ -1086,6 +1156,20 @@ Scene *build_scene(const pt_scene_desc *d) {
       lo[a1] = q.d1_min;
       hi[a1] = q.d1_max;
       ob.box = Box{lo, hi};
+    } else if (od.kind == PT_OBJ_CURVE) {  // Curve (curve.hpp:13-46)
+      const pt_curve_desc &cv = d->curves[od.index];
+      V mn(INFINITY), mx(-INFINITY);
+      for (int k = 0; k < 4; ++k) {
+        ob.cps[k] = V(cv.cps[k][0], cv.cps[k][1], cv.cps[k][2]);
+        mn = V(std::min(mn.x, ob.cps[k].x), std::min(mn.y, ob.cps[k].y), std::min(mn.z, ob.cps[k].z));
+        mx = V(std::max(mx.x, ob.cps[k].x), std::max(mx.y, ob.cps[k].y), std::max(mx.z, ob.cps[k].z));
+      }
+      ob.w0 = cv.width0;
+      ob.w1 = cv.width1;
+      ob.mat = cv.material;
+      const float r = std::max(cv.width0, cv.width1);
+      ob.box = Box{mn - V(r), mx + V(r)};
+      ob.prim = n_tris + d->n_quads + 6 * (d->boxes ? d->n_boxes : 0) + d->n_spheres + od.index;
     } else if (od.kind == PT_OBJ_BOX) {  // Box (box.hpp:5-53): six faces x1, x0, y1, y0, z1, z0
       const pt_box_desc &bx = d->boxes[od.index];
       const float *lo = bx.min_xyz, *hi = bx.max_xyz;
@@ -1129,7 +1213,7 @@ Scene *build_scene(const pt_scene_desc *d) {
   S->root = S->build_top(0, (int)S->objs.size());
   // lights (lightDiscovery.hpp:5-81, light.hpp:55-306)
   for (auto &ob : S->objs) {
-    if (ob.kind == PT_OBJ_MESH || ob.kind == PT_OBJ_BOX) continue;
+    if (ob.kind == PT_OBJ_MESH || ob.kind == PT_OBJ_BOX || ob.kind == PT_OBJ_CURVE) continue;
     const Material &m = S->mats[ob.mat];
     if (m.type != PT_MAT_DIFFUSE_EMITTER || m.p[3] <= 0.f) continue;
     Light L{};

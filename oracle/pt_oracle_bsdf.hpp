@@ -18,6 +18,8 @@ struct Hit {  // HitRecord (materialBase.hpp:32-53)
   int prim = -1;
   int light = -1;
   float bu = 0.f, bv = 0.f;  // triangle barycentrics of the hit
+  bool has_tangent = false;  // a curve hit: HitRecord::hair_tangent
+  V tangent;
   float tu = 0.f, tv = 0.f;  // HitRecord::texCoords
   void set_normal(V dir, V n) {
     is_inside = dot(dir, n) < 0;

@@ -197,6 +197,7 @@ struct BNode {
 struct Builder {
   const pt_scene_desc *d;
   int box_quad_base = 0;          // first rectangle of the boxes' faces
+  int curve_base = 0;             // first curve primitive
   int threads = 0;               // mesh BVH build workers (0: hardware threads)
   std::vector<int> obj_motion;   // per object: motion index + 1 (0: static)
   std::vector<BNode> nodes;
@@ -349,6 +350,19 @@ struct Builder {
         b.lo[a] -= 1e-3f;
         b.hi[a] += 1e-3f;
       }
+    } else if (od.kind == PT_OBJ_CURVE) {  // Curve::getAABB (curve.hpp:33-46)
+      const pt_curve_desc &cv = d->curves[od.index];
+      b = box_empty();
+      for (int k = 0; k < 4; ++k)
+        for (int a = 0; a < 3; ++a) {
+          b.lo[a] = std::min(b.lo[a], cv.cps[k][a]);
+          b.hi[a] = std::max(b.hi[a], cv.cps[k][a]);
+        }
+      const float r = std::max(cv.width0, cv.width1);
+      for (int a = 0; a < 3; ++a) {
+        b.lo[a] -= r;
+        b.hi[a] += r;
+      }
     } else if (od.kind == PT_OBJ_BOX) {  // Box::getAABB (box.hpp:36)
       const pt_box_desc &bx = d->boxes[od.index];
       for (int a = 0; a < 3; ++a) {
@@ -402,7 +416,10 @@ struct Builder {
       nodes.push_back(BNode());
       nodes[me].box = object_box(o);
       nodes[me].first = (int)leaf_prims.size();
-      if (od.kind == PT_OBJ_BOX) {  // one leaf: the six faces in the box's order
+      if (od.kind == PT_OBJ_CURVE) {
+        nodes[me].count = 1;
+        leaf_prims.push_back(curve_base + od.index);
+      } else if (od.kind == PT_OBJ_BOX) {  // one leaf: the six faces in the box's order
         nodes[me].count = 6;
         for (int k = 0; k < 6; ++k) leaf_prims.push_back(n_tris + box_quad_base + 6 * od.index + k);
       } else {
@@ -692,16 +709,23 @@ std::unique_ptr<Scene> build_scene(const pt_scene_desc *d_in, cudaStream_t st, b
   for (int s = 0; s < d->n_spheres; ++s)
     if (d->spheres[s].material < 0 || d->spheres[s].material >= d->n_materials)
       fail(PT_ERR_INVALID, "bad sphere");
+  const int n_curves = d->curves ? d->n_curves : 0;
+  if (n_curves < 0) fail(PT_ERR_INVALID, "negative curve count");
   for (int o = 0; o < d->n_objects; ++o) {
     const pt_object_desc &od = d->objects[o];
-    int lim = od.kind == PT_OBJ_MESH ? d->n_meshes
-              : od.kind == PT_OBJ_QUAD ? n_user_quads
-              : od.kind == PT_OBJ_BOX  ? n_boxes
-                                       : d->n_spheres;
-    if (od.kind < 0 || od.kind > 3 || od.index < 0 || od.index >= lim)
+    int lim = od.kind == PT_OBJ_MESH  ? d->n_meshes
+              : od.kind == PT_OBJ_QUAD  ? n_user_quads
+              : od.kind == PT_OBJ_BOX   ? n_boxes
+              : od.kind == PT_OBJ_CURVE ? n_curves
+                                        : d->n_spheres;
+    if (od.kind < 0 || od.kind > 4 || od.index < 0 || od.index >= lim)
       fail(PT_ERR_INVALID, "bad object entry");
   }
-  const int n_prims = B.n_tris + d->n_quads + d->n_spheres;
+  for (int c = 0; c < n_curves; ++c)
+    if (d->curves[c].material < 0 || d->curves[c].material >= d->n_materials) fail(PT_ERR_INVALID, "bad curve");
+  const int curve_base = B.n_tris + d->n_quads + d->n_spheres;  // first curve primitive
+  B.curve_base = curve_base;
+  const int n_prims = curve_base + n_curves;
   // motion blur: one motion record per moving object, index + 1 on its
   // primitives (a mesh shared by several objects takes the last one's)
   std::vector<float4> motion;
@@ -721,6 +745,8 @@ std::unique_ptr<Scene> build_scene(const pt_scene_desc *d_in, cudaStream_t st, b
     } else {
       if (od.kind == PT_OBJ_BOX)
         for (int k = 0; k < 6; ++k) prim_motion[B.n_tris + n_user_quads + 6 * od.index + k] = m;
+      else if (od.kind == PT_OBJ_CURVE)
+        prim_motion[curve_base + od.index] = m;
       else
         prim_motion[od.kind == PT_OBJ_QUAD ? B.n_tris + od.index : B.n_tris + d->n_quads + od.index] = m;
     }
@@ -799,6 +825,9 @@ std::unique_ptr<Scene> build_scene(const pt_scene_desc *d_in, cudaStream_t st, b
       it.b[1] = q.d1_max;
       it.b[2] = (float)q.axis;
       it.b[3] = u2f(ITEM_QUAD);
+    } else if (prim >= curve_base) {
+      it.a[0] = u2f((uint32_t)(prim - curve_base));
+      it.b[3] = u2f(ITEM_CURVE);
     } else {
       const pt_sphere_desc &s = d->spheres[prim - B.n_tris - d->n_quads];
       it.a[0] = s.center[0];
@@ -845,6 +874,10 @@ std::unique_ptr<Scene> build_scene(const pt_scene_desc *d_in, cudaStream_t st, b
       ps.material = q.material;
       ps.flags |= (ITEM_QUAD << 2) | (q.axis << 4);
       if (q.flip_face) ps.flags |= PT_PRIM_FLIP;
+    } else if (prim >= curve_base) {
+      ps.material = d->curves[prim - curve_base].material;
+      ps.flags |= ITEM_CURVE << 2;
+      ps.n0[0] = u2f((uint32_t)(prim - curve_base));
     } else {
       const pt_sphere_desc &s = d->spheres[prim - B.n_tris - d->n_quads];
       ps.material = s.material;
@@ -937,6 +970,8 @@ std::unique_ptr<Scene> build_scene(const pt_scene_desc *d_in, cudaStream_t st, b
         const pt_quad_desc &q = d->quads[prim - B.n_tris];
         a = make_float4(q.d0_min, q.d0_max, q.d1_min, q.d1_max);
         b = make_float4(0.f, 0.f, (float)PT_UV_QUAD, (float)q.axis);
+      } else if (prim >= curve_base) {
+        b = make_float4(0.f, 0.f, (float)PT_UV_TRI, 0.f);  // Curve sets no texCoords: (0, 0)
       } else {
         const pt_sphere_desc &sp = d->spheres[prim - B.n_tris - d->n_quads];
         a = make_float4(sp.center[0], sp.center[1], sp.center[2], sp.radius);
@@ -950,7 +985,7 @@ std::unique_ptr<Scene> build_scene(const pt_scene_desc *d_in, cudaStream_t st, b
   std::vector<LightRec> lights;
   for (int o = 0; o < d->n_objects; ++o) {
     const pt_object_desc &od = d->objects[o];
-    if (od.kind == PT_OBJ_MESH || od.kind == PT_OBJ_BOX) continue;  // not discovered as lights
+    if (od.kind == PT_OBJ_MESH || od.kind == PT_OBJ_BOX || od.kind == PT_OBJ_CURVE) continue;  // not lights
     int mi = od.kind == PT_OBJ_QUAD ? d->quads[od.index].material : d->spheres[od.index].material;
     const pt_material_desc &md = d->materials[mi];
     if (md.type != PT_MAT_DIFFUSE_EMITTER || md.p[3] <= 0.f) continue;
@@ -1105,6 +1140,16 @@ std::unique_ptr<Scene> build_scene(const pt_scene_desc *d_in, cudaStream_t st, b
     V.n_textures = n_tex;
   }
   if (!prim_uv.empty()) V.prim_uv = up(prim_uv);
+  if (n_curves > 0) {
+    std::vector<float4> cv(4 * (size_t)n_curves);
+    for (int c = 0; c < n_curves; ++c) {
+      const pt_curve_desc &k = d->curves[c];
+      for (int j = 0; j < 4; ++j)
+        cv[4 * c + j] = make_float4(k.cps[j][0], k.cps[j][1], k.cps[j][2],
+                                    j == 0 ? k.width0 : j == 1 ? k.width1 : 0.f);
+    }
+    V.curves = up(cv);
+  }
   if (!motion.empty()) {
     V.motion = up(motion);
     V.node_motion = up(out.node_motion);

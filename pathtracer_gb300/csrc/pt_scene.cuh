@@ -21,7 +21,7 @@
 
 namespace pt {
 
-enum ItemType : int32_t { ITEM_TRI = 0, ITEM_QUAD = 1, ITEM_SPHERE = 2 };
+enum ItemType : int32_t { ITEM_TRI = 0, ITEM_QUAD = 1, ITEM_SPHERE = 2, ITEM_CURVE = 3 };
 
 struct alignas(128) Bvh4Node {
   float lo_x[4], hi_x[4];
@@ -132,6 +132,7 @@ struct SceneView {
   const TexRec *textures;  // surface textures (materials' flags >> PT_MAT_TEXTURE_SHIFT)
   const float4 *prim_uv;   // per primitive texture-coordinate records (null: no textures)
   int32_t n_textures;
+  const float4 *curves;    // per curve: (cp0, width0), (cp1, width1), (cp2, 0), (cp3, 0)
 };
 
 // Child references of a BVH4 node entering a moving object's subtree carry

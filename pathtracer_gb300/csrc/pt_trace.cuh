@@ -95,6 +95,76 @@ __device__ __forceinline__ bool hit_sphere(const Item &it, V3 o, V3 dn, float tm
   return true;
 }
 
+// Cubic Bezier point and derivative (primitives/bezier.hpp:10-36).
+__device__ __forceinline__ V3 bezier_point(const float4 *cp, float u) {
+  const float u1 = 1.0f - u;
+  const float b0 = u1 * u1 * u1, b1 = 3.0f * u * u1 * u1, b2 = 3.0f * u * u * u1, b3 = u * u * u;
+  const float4 c0 = __ldg(cp), c1 = __ldg(cp + 1), c2 = __ldg(cp + 2), c3 = __ldg(cp + 3);
+  return v3(c0.x, c0.y, c0.z) * b0 + v3(c1.x, c1.y, c1.z) * b1 + v3(c2.x, c2.y, c2.z) * b2 +
+         v3(c3.x, c3.y, c3.z) * b3;
+}
+__device__ __forceinline__ V3 bezier_tangent(const float4 *cp, float u) {
+  const float4 c0 = __ldg(cp), c1 = __ldg(cp + 1), c2 = __ldg(cp + 2), c3 = __ldg(cp + 3);
+  const V3 d0 = 3.0f * (v3(c1.x, c1.y, c1.z) - v3(c0.x, c0.y, c0.z));
+  const V3 d1 = 3.0f * (v3(c2.x, c2.y, c2.z) - v3(c1.x, c1.y, c1.z));
+  const V3 d2 = 3.0f * (v3(c3.x, c3.y, c3.z) - v3(c2.x, c2.y, c2.z));
+  const float u1 = 1.0f - u;
+  return d0 * (u1 * u1) + d1 * (2.0f * u * u1) + d2 * (u * u);
+}
+
+// Curve::intersect (primitives/curve.hpp:48-129): the Bezier split into 8
+// segments, each an infinite cylinder of the segment's mean radius cut at its
+// ends; roots from gl::solveQuadratic (utility.hpp:112-124).  Returns the
+// segment in u and the position along it in v (fraction of its length).
+__device__ __forceinline__ bool hit_curve(const float4 *cp, V3 o, V3 d, float tmin, float tmax, float &t_out,
+                                          float &u_out, float &v_out) {
+  const int N = 8;
+  const float w0 = __ldg(cp).w, w1 = __ldg(cp + 1).w;
+  float best = tmax;
+  bool found = false;
+  V3 pa = bezier_point(cp, 0.f);
+  for (int i = 0; i < N; ++i) {
+    const float u0 = float(i) / N, u1 = float(i + 1) / N;
+    const V3 pb = bezier_point(cp, u1);
+    const float r0 = w0 + (w1 - w0) * u0, r1 = w0 + (w1 - w0) * u1;
+    const float radius = 0.5f * (r0 + r1);
+    const V3 ab = pb - pa;
+    const float seg_len = length(ab);
+    const V3 axis = ab / seg_len;
+    const V3 d_perp = d - dot(d, axis) * axis;
+    const V3 delta = o - pa;
+    const V3 o_perp = delta - dot(delta, axis) * axis;
+    const float A = dot(d_perp, d_perp), B = 2.0f * dot(d_perp, o_perp);
+    const float C = dot(o_perp, o_perp) - radius * radius;
+    const float disc = B * B - 4 * A * C;
+    if (disc >= 0.f) {
+      const float sq = sqrtf(disc);
+      const float q = B < 0 ? -0.5f * (B - sq) : -0.5f * (B + sq);
+      float ra = q / A, rb = C / q;
+      if (ra > rb) {
+        const float tt = ra;
+        ra = rb;
+        rb = tt;
+      }
+      const int nr = ra == rb ? 1 : 2;
+      for (int r = 0; r < nr; ++r) {
+        const float t = r == 0 ? ra : rb;
+        if (t < tmin || t > best) continue;
+        const V3 hp = o + t * d;
+        const float proj = dot(hp - pa, axis);
+        if (proj < 0.0f || proj > seg_len) continue;
+        best = t;
+        u_out = (float)i;
+        v_out = proj / seg_len;
+        found = true;
+      }
+    }
+    pa = pb;
+  }
+  if (found) t_out = best;
+  return found;
+}
+
 __device__ __forceinline__ Item load_item(const Item *items, int i) {
   const float4 *p = reinterpret_cast<const float4 *>(items + i);
   float4 a = __ldg(p), b = __ldg(p + 1), c = __ldg(p + 2);
@@ -130,8 +200,10 @@ __device__ __forceinline__ bool test_leaf(const SceneView &S, int32_t ref, V3 o_
       h = hit_triangle(it, o, d, tmin, tmax, t, u, v);
     else if (type == ITEM_QUAD)
       h = hit_quad(it, o, dn, tmin, tmax, t);
-    else
+    else if (type == ITEM_SPHERE)
       h = hit_sphere(it, o, dn, tmin, tmax, t);
+    else
+      h = hit_curve(S.curves + 4 * (size_t)f2u(it.a[0]), o, d, tmin, tmax, t, u, v);
     if (h) {
       if (ANY) return true;
       tmax = t;

@@ -120,6 +120,8 @@ struct Surf {
   int mat;
   int light;
   int motion;  // motion index + 1 of the primitive (0: static)
+  bool has_tan;  // a curve hit: HitRecord::hair_tangent is set
+  V3 tan;        // the curve tangent (HairMarschner's frame)
 };
 
 // Position of a moving object's point at `time` (rounded, never fused).
@@ -143,6 +145,8 @@ __device__ inline Surf surface_at(const SceneView &S, V3 o, V3 d, const HitRec &
   s.mat = ps.material;
   s.light = ps.light;
   s.motion = PT_PRIM_MOTION(ps.flags);
+  s.has_tan = false;
+  s.tan = v3(0.f);
   const int type = PT_PRIM_KIND(ps.flags);
   V3 n;
   if (type == ITEM_TRI) {
@@ -161,6 +165,25 @@ __device__ inline Surf surface_at(const SceneView &S, V3 o, V3 d, const HitRec &
     const int axis = PT_PRIM_AXIS(ps.flags);
     n = v3(axis == 0 ? 1.f : 0.f, axis == 1 ? 1.f : 0.f, axis == 2 ? 1.f : 0.f);
     s.p = xat(o, xnormalize(d), h.t);
+  } else if (type == ITEM_CURVE) {
+    // Curve::intersect's hit record (curve.hpp:104-121): tangent from the two
+    // Bezier derivatives at the segment's ends, normal from the segment's
+    // axis to the hit point, in the curve's frame (h.u segment, h.v
+    // fraction of its length)
+    s.p = xat(o, d, h.t);
+    const float4 *cp = S.curves + 4 * (size_t)f2u(ps.n0[0]);
+    const V3 hp = s.motion ? moved_point(S, s.motion, s.p, -time) : s.p;
+    const int i = (int)h.u;
+    const float u0 = float(i) / 8, u1 = float(i + 1) / 8;
+    const V3 pa = bezier_point(cp, u0), pb = bezier_point(cp, u1);
+    const V3 ab = pb - pa;
+    const V3 axis = ab / length(ab);
+    const float proj = dot(hp - pa, axis);
+    const V3 d0 = bezier_tangent(cp, u0), d1 = bezier_tangent(cp, u1);
+    s.tan = normalize(d0 + (d1 - d0) * h.v);
+    s.has_tan = true;
+    const V3 rv = hp - (pa + axis * proj);
+    n = normalize(rv - dot(rv, s.tan) * s.tan);
   } else {
     V3 dn = xnormalize(d);
     s.p = xat(o, dn, h.t);
@@ -460,7 +483,10 @@ __device__ __forceinline__ void next_event(const SceneView &S, const DeviceJob &
         f = v3(phase);
         pb = phase;
       } else {
-        bsdf_eval_t<FAM>(S.materials[mat], wo, wl, sf.n, sf.front, f, pb);
+        // HairMarschner on a curve uses the curve tangent as its frame
+        // (hairMarsch.cpp:12-19), every other BSDF the shading normal
+        const V3 bn = ((FAM == 6 || FAM < 0) && sf.has_tan && S.materials[mat].type == PT_MAT_HAIR) ? sf.tan : sf.n;
+        bsdf_eval_t<FAM>(S.materials[mat], wo, wl, bn, sf.front, f, pb);
         if ((FAM == 0 || FAM < 0) && tex_alb) f = alb * PT_INV_PI_F;  // textured Lambertian albedo
       }
       float w = mis ? power_heuristic((float)LN, pdf_l, 1.f, pb) : 1.f;
@@ -621,7 +647,8 @@ __global__ void __launch_bounds__(128) k_shade(SceneView S, DeviceJob J, JobTabl
           float u0 = sampler_dim(Jp, dim0 + 1, P.halton_index, P.key, P.pix, P.k);
           float u1 = sampler_dim(Jp, dim0 + 2, P.halton_index, P.key, P.pix, P.k);
           wo = -normalize(d);
-          BsdfSample bs = bsdf_sample_t<FAM>(M, wo, sf.n, sf.front, uc, u0, u1);
+          const V3 bn = ((FAM == 6 || FAM < 0) && sf.has_tan && M.type == PT_MAT_HAIR) ? sf.tan : sf.n;
+          BsdfSample bs = bsdf_sample_t<FAM>(M, wo, bn, sf.front, uc, u0, u1);
           if ((FAM == 0 || FAM < 0) && M.type == PT_MAT_LAMBERTIAN && mat_texture(M)) {
             // Lambertian with a ColorVariant texture: albedo at the hit's
             // texCoords (material.hpp:100, 133)

@@ -23,7 +23,7 @@ ERRORS = {
 # material types (pathtracer_gb300.h)
 LAMBERTIAN, CONDUCTOR, MF_DIELECTRIC, THIN_DIELECTRIC, PHONG, DISNEY, HAIR, DIFFUSE_EMITTER = range(8)
 FLAG_SPLIT_RAY, FLAG_MELANIN = 1, 2
-OBJ_MESH, OBJ_QUAD, OBJ_SPHERE, OBJ_BOX = 0, 1, 2, 3
+OBJ_MESH, OBJ_QUAD, OBJ_SPHERE, OBJ_BOX, OBJ_CURVE = 0, 1, 2, 3, 4
 EST_REF_NEE, EST_NEE_MIS = 0, 1
 SAMPLER_HALTON_NONE, SAMPLER_HALTON_PERMUTE, SAMPLER_HALTON_OWEN, SAMPLER_STRATIFIED = range(4)
 ENV_UNIFORM, ENV_ALIAS = 0, 1
@@ -86,6 +86,10 @@ class BoxDesc(C.Structure):
     _fields_ = [("min_xyz", C.c_float * 3), ("max_xyz", C.c_float * 3), ("material", C.c_int32)]
 
 
+class CurveDesc(C.Structure):
+    _fields_ = [("cps", (C.c_float * 3) * 4), ("width0", C.c_float), ("width1", C.c_float), ("material", C.c_int32)]
+
+
 class EnvDesc(C.Structure):
     _fields_ = [("texels", f32p), ("width", C.c_int32), ("height", C.c_int32), ("intensity", C.c_float)]
 
@@ -105,6 +109,7 @@ class SceneDesc(C.Structure):
         ("bg_color", C.c_float * 3), ("bvh_mode", C.c_int32), ("shutter_max", C.c_float),
         ("textures", C.POINTER(TextureDesc)), ("n_textures", C.c_int32),
         ("boxes", C.POINTER(BoxDesc)), ("n_boxes", C.c_int32),
+        ("curves", C.POINTER(CurveDesc)), ("n_curves", C.c_int32),
     ]
 
 
@@ -296,6 +301,16 @@ def make_scene_desc(scene) -> SceneBuffers:
         sb.hold(barr)
         d.boxes = barr
         d.n_boxes = len(boxes)
+    curves = getattr(scene, "curves", [])
+    if curves:
+        carr = (CurveDesc * len(curves))()
+        for i, (cps, w0, w1, mat) in enumerate(curves):
+            for k in range(4):
+                carr[i].cps[k][:] = [float(x) for x in cps[k]]
+            carr[i].width0, carr[i].width1, carr[i].material = float(w0), float(w1), mat
+        sb.hold(carr)
+        d.curves = carr
+        d.n_curves = len(curves)
     texs = getattr(scene, "textures", [])
     if texs:
         arr = (TextureDesc * len(texs))()

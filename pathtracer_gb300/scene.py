@@ -50,6 +50,7 @@ class Scene:
     shutter_max: float = 0.0                        # motion blur: longest shutter of any job
     textures: list = field(default_factory=list)    # dicts: kind, color1, color2, scale, fractal, texels
     boxes: list = field(default_factory=list)       # (min_xyz, max_xyz, material)
+    curves: list = field(default_factory=list)      # (4 control points, width0, width1, material)
 
     def add_material(self, mtype: int, params, flags: int = 0, texture: int | None = None) -> int:
         """A material; `texture` (an index from add_texture) replaces the
@@ -84,6 +85,11 @@ class Scene:
         """Box(min_xyz, max_xyz, material): one object of six rectangles."""
         self.boxes.append((tuple(min_xyz), tuple(max_xyz), material))
         self.objects.append((N.OBJ_BOX, len(self.boxes) - 1, tuple(velocity)))
+
+    def add_curve(self, cps, width0, width1, material, velocity=(0.0, 0.0, 0.0)):
+        """Curve(cps, width0, width1, CurveType::Cylinder, material)."""
+        self.curves.append(([tuple(float(x) for x in p) for p in cps], width0, width1, material))
+        self.objects.append((N.OBJ_CURVE, len(self.curves) - 1, tuple(velocity)))
 
     @property
     def has_motion(self) -> bool:
@@ -385,4 +391,30 @@ def textured_cornell(subdiv: int = 3, seed: int = 0) -> tuple[Scene, dict]:
     m.uvs = uvs
     sc.add_mesh(m)
     cam = camera((0.5, 0.5, -1.4), (0.0, 0.0, 1.0), 40.0, 1.0)
+    return sc, cam
+
+
+def hair_curves(n: int = 200, seed: int = 0) -> tuple[Scene, dict]:
+    """Strands of cubic Bezier curves (Curve, cylinder segments) in
+    Marschner hair of seeded melanin over a Lambertian ground, lit by a quad
+    light and a sphere light: the hair BSDF's frame is the curve tangent."""
+    rng = np.random.default_rng(seed)
+    sc = Scene()
+    ground = sc.add_material(N.LAMBERTIAN, [0.5, 0.45, 0.4])
+    light = sc.add_material(N.DIFFUSE_EMITTER, [1.0, 0.95, 0.9, 12.0])
+    mats = [sc.add_material(N.HAIR, [0, 0, 0, 0.0, 1.55, float(rng.uniform(0.2, 0.4)), float(rng.uniform(0.2, 0.4)),
+                                     math.radians(2.0), float(rng.uniform(0.3, 2.5)), 0.0], N.FLAG_MELANIN)
+            for _ in range(4)]
+    sc.add_quad(1, 0.0, -2.0, 2.0, -2.0, 2.0, ground)
+    sc.add_quad(1, 2.5, -0.5, 0.5, -0.5, 0.5, light)
+    sc.add_sphere((1.5, 1.5, -1.0), 0.2, light)
+    for _ in range(n):
+        base = np.array([rng.uniform(-0.8, 0.8), 0.0, rng.uniform(-0.8, 0.8)])
+        lean = rng.normal(0, 0.25, size=3)
+        lean[1] = 0.0
+        h = rng.uniform(0.6, 1.2)
+        cps = [base, base + np.array([0, h / 3, 0]) + lean * 0.2, base + np.array([0, 2 * h / 3, 0]) + lean * 0.6,
+               base + np.array([0, h, 0]) + lean]
+        sc.add_curve(cps, 0.012, 0.004, mats[int(rng.integers(len(mats)))])
+    cam = camera((0.0, 0.7, -3.0), (0.0, -0.1, 1.0), 40.0, 1.0)
     return sc, cam

@@ -80,3 +80,24 @@ def test_box_matches_oracle(renderer):
     assert (prim == prim_o).mean() > 0.999
     both = (prim == prim_o) & (prim >= 0)
     assert np.allclose(t[both], t_o[both], rtol=1e-5)
+
+
+@pytest.mark.parametrize("estimator", [N.EST_REF_NEE, N.EST_NEE_MIS])
+def test_hair_curves_match_oracle(renderer, estimator):
+    sc, cam = S.hair_curves(120, seed=4)
+    job = N.job_desc(0, cam, 40, 40, 4, 4, 6, seed=5, estimator=estimator)
+    _compare(renderer, sc, job, 16, frac=0.85)
+    # closest hits on curves: same primitive, t within 1e-5
+    rng = np.random.default_rng(7)
+    o = np.tile([0.0, 0.7, -3.0], (4096, 1))
+    d = np.stack([rng.uniform(-0.3, 0.3, 4096), rng.uniform(-0.35, 0.15, 4096), np.ones(4096)], 1)
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    rays = np.concatenate([o, d], 1).astype(np.float32)
+    sid = renderer.upload(sc)
+    t, prim, _ = renderer.trace_closest(sid, rays)
+    renderer.release(sid)
+    t_o, prim_o = O.OracleScene(sc).trace_closest(rays)
+    assert (prim == prim_o).mean() > 0.995
+    both = (prim == prim_o) & (prim >= 0)
+    assert np.allclose(t[both], t_o[both], rtol=1e-5)
+    assert (prim >= 3).sum() > 100  # the rays do hit curves

@@ -63,3 +63,20 @@ def test_box_is_its_six_faces():
     b, _ = O.render(b_sc, job)
     # same surfaces, different top-level tree: only exact edge ties may differ
     assert np.isclose(a, b, rtol=1e-5, atol=1e-6).all(-1).mean() > 0.99
+
+
+def test_curves_build_and_render():
+    sc, cam = S.hair_curves(40, seed=2)
+    info = N.bvh_build(sc)
+    assert info["items"] == 2 + 1 + 40
+    job = N.job_desc(0, cam, 24, 24, 2, 2, 5, seed=1, estimator=N.EST_NEE_MIS)
+    a, _ = O.render(sc, job)
+    assert np.isfinite(a).all() and a.mean() > 0
+    # rays straight down onto a strand's root hit it
+    rays = []
+    for cps, w0, w1, _ in sc.curves[:10]:
+        x, _, z = cps[0]
+        rays.append([x, 0.05, z - 1.0, 0.0, 0.0, 1.0])
+    t, prim = O.OracleScene(sc).trace_closest(np.array(rays, np.float32))
+    curve_prims = set(range(3, 3 + 40))  # after the two rectangles and the sphere
+    assert sum(int(p) in curve_prims for p in prim) >= 8
