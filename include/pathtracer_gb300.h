@@ -332,6 +332,18 @@ int pt_bvh_build(const pt_scene_desc *desc, int32_t threads, int64_t *out5);
  * PT_ERR_INVALID) through pt_last_error(NULL, ...). */
 int pt_obj_load(const char *path, pt_mesh_desc *mesh);
 int pt_obj_free(pt_mesh_desc *mesh);
+
+/* Image file -> texels, the ImageTexture(filename, flip_y, isHDR)
+ * constructor (src/texture/texture.cpp:3-93, decoding through stb_image):
+ * *texels = width*height*3 floats laid out as the reference's texels[x][y],
+ * y = 0 the image's bottom row (its top row with flip_y) -- the layout of
+ * pt_env_desc and pt_texture_desc image texels.  Radiance RGBE (.hdr, flat or
+ * RLE scanlines) and PNG (every colour type / bit depth, Adam7); LDR texels
+ * are byte / 255, is_hdr linearises LDR files as stbi_loadf does.  Free with
+ * pt_free_image.  No context; errors through pt_last_error(NULL, ...). */
+int pt_load_image(const char *path, int32_t flip_y, int32_t is_hdr, float **texels, int32_t *width,
+                  int32_t *height);
+int pt_free_image(float *texels);
 /* Counts of the flattened scene: [0] triangles, [1] quads, [2] spheres,
  * [3] BVH4 nodes, [4] lights, [5] device bytes. */
 int pt_scene_info(void *ctx, int32_t scene_id, int64_t *out6);

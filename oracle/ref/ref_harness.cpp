@@ -372,4 +372,22 @@ double ref_render_time(void *s, const pt_job_desc *job, int threads) {
   return std::chrono::duration<double>(t1 - t0).count();
 }
 
+// ImageTexture(filename, flip_y, isHDR) (texture.cpp:3-93) sampled by its
+// own getTexelColor at n points (u, v); returns -1 when the constructor
+// throws (file missing or undecodable).
+int ref_image_texels(const char *path, int flip_y, int is_hdr, int n, const float *uv, float *rgb) {
+  try {
+    ImageTexture tex(path, flip_y != 0, is_hdr != 0);
+    for (int k = 0; k < n; ++k) {
+      gl::vec3 c = tex.getTexelColor(uv[2 * k], uv[2 * k + 1]);
+      rgb[3 * k] = c[0];
+      rgb[3 * k + 1] = c[1];
+      rgb[3 * k + 2] = c[2];
+    }
+    return 0;
+  } catch (...) {
+    return -1;
+  }
+}
+
 }  // extern "C"

@@ -48,6 +48,7 @@ def load():
         lib.ref_render.argtypes = [C.c_void_p, C.POINTER(N.JobDesc), f32p, f32p, C.c_int]
         lib.ref_render_time.argtypes = [C.c_void_p, C.POINTER(N.JobDesc), C.c_int]
         lib.ref_render_time.restype = C.c_double
+        lib.ref_image_texels.argtypes = [C.c_char_p, C.c_int, C.c_int, C.c_int, f32p, f32p]
         _lib = lib
     return _lib
 
@@ -123,4 +124,15 @@ def sampler_eval(strategy, first_index, n, dims, seed=0):
     lib = load()
     out = np.zeros((n, dims), np.float32)
     lib.ref_sampler_eval(strategy, seed, first_index, n, dims, _p(out, C.c_float))
+    return out
+
+
+def image_texels(path, flip_y: bool, is_hdr: bool, uv: np.ndarray) -> np.ndarray:
+    """ImageTexture(path, flip_y, is_hdr).getTexelColor at each (u, v)."""
+    uv = np.ascontiguousarray(uv, np.float32).reshape(-1, 2)
+    out = np.zeros((uv.shape[0], 3), np.float32)
+    rc = load().ref_image_texels(str(path).encode(), int(flip_y), int(is_hdr), uv.shape[0], _p(uv, C.c_float),
+                                 _p(out, C.c_float))
+    if rc != 0:
+        raise RuntimeError(f"reference ImageTexture failed to load {path}")
     return out

@@ -436,12 +436,12 @@ void launch_tonemap(const float *film, int W, int H, float gamma, uint8_t *out, 
 
 void kernel_attributes(KernelInfo *info) {
   cudaFuncAttributes a;
-  cudaFuncGetAttributes(&a, k_trace_closest<false>);
+  cudaFuncGetAttributes(&a, k_trace_closest<false, false>);
   info->trace_regs = a.numRegs;
   cudaFuncGetAttributes(&a, k_shade<-1, false>);
   info->shade_regs = a.numRegs;
   int nb = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_trace_closest<false>, 128, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_trace_closest<false, false>, 128, 0);
   info->trace_blocks_per_sm = nb;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_shade<-1, false>, 128, 0);
   info->shade_blocks_per_sm = nb;

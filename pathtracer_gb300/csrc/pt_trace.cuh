@@ -96,12 +96,17 @@ __device__ __forceinline__ bool hit_sphere(const Item &it, V3 o, V3 dn, float tm
 }
 
 // Cubic Bezier point and derivative (primitives/bezier.hpp:10-36).
+// Bezier point with every operation separately rounded (never fused), in
+// bezier.hpp:10-18's order, so that curve hits round like the reference's.
 __device__ __forceinline__ V3 bezier_point(const float4 *cp, float u) {
-  const float u1 = 1.0f - u;
-  const float b0 = u1 * u1 * u1, b1 = 3.0f * u * u1 * u1, b2 = 3.0f * u * u * u1, b3 = u * u * u;
+  const float u1 = xsub(1.0f, u);
+  const float b0 = xmul(xmul(u1, u1), u1), b1 = xmul(xmul(xmul(3.0f, u), u1), u1);
+  const float b2 = xmul(xmul(xmul(3.0f, u), u), u1), b3 = xmul(xmul(u, u), u);
   const float4 c0 = __ldg(cp), c1 = __ldg(cp + 1), c2 = __ldg(cp + 2), c3 = __ldg(cp + 3);
-  return v3(c0.x, c0.y, c0.z) * b0 + v3(c1.x, c1.y, c1.z) * b1 + v3(c2.x, c2.y, c2.z) * b2 +
-         v3(c3.x, c3.y, c3.z) * b3;
+  auto comb = [&](float a0, float a1, float a2, float a3) {
+    return xadd(xadd(xadd(xmul(a0, b0), xmul(a1, b1)), xmul(a2, b2)), xmul(a3, b3));
+  };
+  return v3(comb(c0.x, c1.x, c2.x, c3.x), comb(c0.y, c1.y, c2.y, c3.y), comb(c0.z, c1.z, c2.z, c3.z));
 }
 __device__ __forceinline__ V3 bezier_tangent(const float4 *cp, float u) {
   const float4 c0 = __ldg(cp), c1 = __ldg(cp + 1), c2 = __ldg(cp + 2), c3 = __ldg(cp + 3);
@@ -119,28 +124,36 @@ __device__ __forceinline__ V3 bezier_tangent(const float4 *cp, float u) {
 __device__ __forceinline__ bool hit_curve(const float4 *cp, V3 o, V3 d, float tmin, float tmax, float &t_out,
                                           float &u_out, float &v_out) {
   const int N = 8;
-  const float w0 = __ldg(cp).w, w1 = __ldg(cp + 1).w;
   float best = tmax;
   bool found = false;
-  V3 pa = bezier_point(cp, 0.f);
+  // Exact (never fused) arithmetic throughout: the cylinder quadratic is
+  // ill-conditioned for grazing rays (C is a difference of near-equal
+  // squares), so contracted multiply-adds would move t by ~1e-5 relative.
+  auto axpy = [](V3 a, float k, V3 b) {  // a - k b
+    return v3(xsub(a.x, xmul(k, b.x)), xsub(a.y, xmul(k, b.y)), xsub(a.z, xmul(k, b.z)));
+  };
+  // the end points are recomputed per segment (as the reference does) and
+  // the widths reloaded, which keeps fewer values live in the traversal loop
+#pragma unroll 1
   for (int i = 0; i < N; ++i) {
     const float u0 = float(i) / N, u1 = float(i + 1) / N;
-    const V3 pb = bezier_point(cp, u1);
-    const float r0 = w0 + (w1 - w0) * u0, r1 = w0 + (w1 - w0) * u1;
-    const float radius = 0.5f * (r0 + r1);
-    const V3 ab = pb - pa;
-    const float seg_len = length(ab);
-    const V3 axis = ab / seg_len;
-    const V3 d_perp = d - dot(d, axis) * axis;
-    const V3 delta = o - pa;
-    const V3 o_perp = delta - dot(delta, axis) * axis;
-    const float A = dot(d_perp, d_perp), B = 2.0f * dot(d_perp, o_perp);
-    const float C = dot(o_perp, o_perp) - radius * radius;
-    const float disc = B * B - 4 * A * C;
+    const V3 pa = bezier_point(cp, u0), pb = bezier_point(cp, u1);
+    const float w0 = __ldg(cp).w, w1 = __ldg(cp + 1).w;
+    const float r0 = xadd(w0, xmul(xsub(w1, w0), u0)), r1 = xadd(w0, xmul(xsub(w1, w0), u1));
+    const float radius = xmul(0.5f, xadd(r0, r1));
+    const V3 ab = xsubv(pb, pa);
+    const float seg_len = xsqrt(xdot(ab, ab));
+    const V3 axis = v3(xdiv(ab.x, seg_len), xdiv(ab.y, seg_len), xdiv(ab.z, seg_len));
+    const V3 d_perp = axpy(d, xdot(d, axis), axis);
+    const V3 delta = xsubv(o, pa);
+    const V3 o_perp = axpy(delta, xdot(delta, axis), axis);
+    const float A = xdot(d_perp, d_perp), B = xmul(2.0f, xdot(d_perp, o_perp));
+    const float C = xsub(xdot(o_perp, o_perp), xmul(radius, radius));
+    const float disc = xsub(xmul(B, B), xmul(xmul(4.0f, A), C));
     if (disc >= 0.f) {
-      const float sq = sqrtf(disc);
-      const float q = B < 0 ? -0.5f * (B - sq) : -0.5f * (B + sq);
-      float ra = q / A, rb = C / q;
+      const float sq = xsqrt(disc);
+      const float q = B < 0 ? xmul(-0.5f, xsub(B, sq)) : xmul(-0.5f, xadd(B, sq));
+      float ra = xdiv(q, A), rb = xdiv(C, q);
       if (ra > rb) {
         const float tt = ra;
         ra = rb;
@@ -150,16 +163,15 @@ __device__ __forceinline__ bool hit_curve(const float4 *cp, V3 o, V3 d, float tm
       for (int r = 0; r < nr; ++r) {
         const float t = r == 0 ? ra : rb;
         if (t < tmin || t > best) continue;
-        const V3 hp = o + t * d;
-        const float proj = dot(hp - pa, axis);
+        const V3 hp = v3(xadd(o.x, xmul(t, d.x)), xadd(o.y, xmul(t, d.y)), xadd(o.z, xmul(t, d.z)));
+        const float proj = xdot(xsubv(hp, pa), axis);
         if (proj < 0.0f || proj > seg_len) continue;
         best = t;
         u_out = (float)i;
-        v_out = proj / seg_len;
+        v_out = xdiv(proj, seg_len);
         found = true;
       }
     }
-    pa = pb;
   }
   if (found) t_out = best;
   return found;
@@ -183,7 +195,9 @@ __device__ __forceinline__ V3 moved_origin(const SceneView &S, uint32_t motion, 
   return v3(xsub(o.x, xmul(v.x, time)), xsub(o.y, xmul(v.y, time)), xsub(o.z, xmul(v.z, time)));
 }
 
-template <bool ANY>
+// CURVES = false compiles the curve test out (curve items then never hit):
+// the closest-hit kernel of a scene without curves keeps 8 fewer registers.
+template <bool ANY, bool CURVES = true>
 __device__ __forceinline__ bool test_leaf(const SceneView &S, int32_t ref, V3 o_w, V3 d, V3 dn,
                                           float tmin, float &tmax, HitRec &hit, float time) {
   const int32_t code = ~ref;
@@ -202,8 +216,10 @@ __device__ __forceinline__ bool test_leaf(const SceneView &S, int32_t ref, V3 o_
       h = hit_quad(it, o, dn, tmin, tmax, t);
     else if (type == ITEM_SPHERE)
       h = hit_sphere(it, o, dn, tmin, tmax, t);
-    else
+    else if (CURVES)
       h = hit_curve(S.curves + 4 * (size_t)f2u(it.a[0]), o, d, tmin, tmax, t, u, v);
+    else
+      h = false;
     if (h) {
       if (ANY) return true;
       tmax = t;
@@ -370,7 +386,7 @@ __device__ __forceinline__ bool trav_node(const SceneView &S, TravRay &R, int32_
 // any -> R.found = occluded.  *err is set when the stack would overflow or
 // the iteration cap is reached (never expected); the ray is then finished
 // with what it has.
-template <bool ANY>
+template <bool ANY, bool CURVES = true>
 __device__ __forceinline__ bool trav_step(const SceneView &S, TravRay &R, int32_t *stack, int stride, int *err) {
   if (++R.iters > S.trav_cap) {
     *err = 2;
@@ -378,7 +394,7 @@ __device__ __forceinline__ bool trav_step(const SceneView &S, TravRay &R, int32_
   }
   if (R.ref == PT_REF_EMPTY) return true;
   if (ref_is_node(R.ref)) return !trav_node<ANY>(S, R, stack, stride, err);
-  if (test_leaf<ANY>(S, R.ref, R.o, R.d, R.dn, R.tmin, R.tmax, R.hit, R.time)) {
+  if (test_leaf<ANY, CURVES>(S, R.ref, R.o, R.d, R.dn, R.tmin, R.tmax, R.hit, R.time)) {
     R.found = true;
     if (ANY) return true;
   }

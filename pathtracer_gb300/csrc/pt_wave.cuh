@@ -305,7 +305,7 @@ __device__ __forceinline__ unsigned lanemask_lt() {
 // a surface hit is a medium event (prim = PT_HIT_MEDIUM, t = free-flight
 // distance).  That is the same decision as comparing the distance with the
 // closest hit.
-template <bool MJ>
+template <bool MJ, bool CURVES>
 __global__ void __launch_bounds__(128) k_trace_closest(SceneView S, DeviceJob J, JobTable T, Queues Q, int qsel,
                                                        int bounce, long long g0) {
   __shared__ int32_t stack[PT_STACK * 128];
@@ -353,7 +353,7 @@ __global__ void __launch_bounds__(128) k_trace_closest(SceneView S, DeviceJob J,
       if (exhausted) break;
       continue;
     }
-    if (active && trav_step<false>(S, R, my_stack, blockDim.x, Q.err)) {
+    if (active && trav_step<false, CURVES>(S, R, my_stack, blockDim.x, Q.err)) {
       const bool hit = R.found;
       int prim = hit ? R.hit.prim : (t_s < 1e5f ? PT_HIT_MEDIUM : -1);
       float t = hit ? R.hit.t : (prim == PT_HIT_MEDIUM ? t_s : FLT_MAX);
@@ -737,7 +737,10 @@ void launch_wave_stages(const SceneView &S, const DeviceJob &J, const JobTable &
     cudaMemsetAsync(Q.counts + (qsel ^ 1), 0, sizeof(int), st);
     cudaMemsetAsync(Q.counts + 2, 0, 3 * sizeof(int), st);
     P.begin(STAGE_TRACE, st);
-    k_trace_closest<MJ><<<cfg.trace_blocks, 128, 0, st>>>(S, J, T, Q, qsel, b, g0);
+    if (S.curves)
+      k_trace_closest<MJ, true><<<cfg.trace_blocks, 128, 0, st>>>(S, J, T, Q, qsel, b, g0);
+    else
+      k_trace_closest<MJ, false><<<cfg.trace_blocks, 128, 0, st>>>(S, J, T, Q, qsel, b, g0);
     P.end(st);
     P.count(STAGE_TRACE, 1);
     if (cfg.sort_by_material) {

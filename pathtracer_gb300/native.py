@@ -31,7 +31,7 @@ ENV_UNIFORM, ENV_ALIAS = 0, 1
 # exported symbols of the C-ABI, in header order
 EXPORTS = [
     "pt_create", "pt_destroy", "pt_last_error", "pt_version", "pt_scene_upload", "pt_scene_release",
-    "pt_bvh_build", "pt_obj_load", "pt_obj_free", "pt_scene_info", "pt_render", "pt_render_device", "pt_render_device_noalloc",
+    "pt_bvh_build", "pt_obj_load", "pt_obj_free", "pt_load_image", "pt_free_image", "pt_scene_info", "pt_render", "pt_render_device", "pt_render_device_noalloc",
     "pt_profile_begin",
     "pt_profile_end", "pt_tonemap", "pt_gaussian_blur", "pt_write_png", "pt_sampler_eval", "pt_trace_closest",
     "pt_trace_any", "pt_bsdf_eval", "pt_bsdf_sample", "pt_render_batch", "pt_autotune", "pt_server_create",
@@ -168,6 +168,9 @@ def load() -> C.CDLL:
         "pt_bvh_build": [C.POINTER(SceneDesc), C.c_int32, C.POINTER(C.c_int64)],
         "pt_obj_load": [C.c_char_p, C.POINTER(MeshDesc)],
         "pt_obj_free": [C.POINTER(MeshDesc)],
+        "pt_load_image": [C.c_char_p, C.c_int32, C.c_int32, C.POINTER(f32p), C.POINTER(C.c_int32),
+                          C.POINTER(C.c_int32)],
+        "pt_free_image": [f32p],
         "pt_scene_info": [vp, C.c_int32, C.POINTER(C.c_int64)],
         "pt_render": [vp, C.POINTER(JobDesc), f32p, C.POINTER(Stats)],
         "pt_render_device": [vp, C.POINTER(JobDesc), vp, C.c_int, C.POINTER(Stats)],
@@ -512,6 +515,24 @@ class Renderer:
                                             _ptr(ok, C.c_uint8), _ptr(wi, C.c_float), _ptr(att, C.c_float),
                                             _ptr(pdf, C.c_float), _ptr(ty, C.c_uint32)))
         return ok.astype(bool), wi, att, pdf, ty
+
+
+def load_image(path, flip_y: bool = False, hdr: bool = False) -> np.ndarray:
+    """pt_load_image, ImageTexture(path, flip_y, isHDR)'s texels: (H, W, 3)
+    float32 whose row y is the reference's texels[x][y] (y = 0 the bottom row
+    of the image, its top row with flip_y)."""
+    lib = load()
+    p = f32p()
+    w, h = C.c_int32(), C.c_int32()
+    rc = lib.pt_load_image(str(path).encode(), int(flip_y), int(hdr), C.byref(p), C.byref(w), C.byref(h))
+    if rc != PT_OK:
+        buf = C.create_string_buffer(512)
+        lib.pt_last_error(None, buf, 512)
+        raise PtError(rc, buf.value.decode())
+    try:
+        return np.ctypeslib.as_array(p, shape=(h.value * w.value * 3,)).reshape(h.value, w.value, 3).copy()
+    finally:
+        lib.pt_free_image(p)
 
 
 def write_png(path, rgb8: np.ndarray) -> None:

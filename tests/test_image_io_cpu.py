@@ -54,3 +54,256 @@ def test_oracle_blur_properties():
         assert np.array_equal(O.gaussian_blur(film, k, s), film)
     blurred = O.gaussian_blur(film, 3, 0.8)
     assert blurred.std() < film.std()
+
+
+# ---------------------------------------------------------------- Radiance HDR
+def _rle_channel(b: bytes) -> bytes:
+    """Adaptive run-length encoding of one scanline channel (runs of 3+)."""
+    out, i, n = bytearray(), 0, len(b)
+    while i < n:
+        j = i
+        while j < n and j - i < 127 and b[j] == b[i]:
+            j += 1
+        if j - i >= 3:
+            out += bytes([128 + j - i, b[i]])
+            i = j
+            continue
+        k = i
+        while k < n and k - i < 128 and not (k + 2 < n and b[k] == b[k + 1] == b[k + 2]):
+            k += 1
+        out += bytes([k - i]) + b[i:k]
+        i = k
+    return bytes(out)
+
+
+def _write_hdr(path, rgbe: np.ndarray, rle: bool, magic=b"#?RADIANCE"):
+    h, w, _ = rgbe.shape
+    data = bytearray(magic + b"\n# made by the test\nFORMAT=32-bit_rle_rgbe\nEXPOSURE=1.0\n\n")
+    data += f"-Y {h} +X {w}\n".encode()
+    for y in range(h):
+        if rle:
+            data += bytes([2, 2, w >> 8, w & 255])
+            for c in range(4):
+                data += _rle_channel(rgbe[y, :, c].tobytes())
+        else:
+            data += rgbe[y].tobytes()
+    path.write_bytes(bytes(data))
+
+
+def _rgbe_to_float(rgbe: np.ndarray) -> np.ndarray:
+    e = rgbe[..., 3].astype(np.int32)
+    s = np.where(e > 0, np.ldexp(np.float32(1), e - 136), 0).astype(np.float32)
+    return rgbe[..., :3].astype(np.float32) * s[..., None]
+
+
+def _random_rgbe(rng, h, w):
+    rgbe = rng.integers(0, 256, (h, w, 4), dtype=np.uint8)
+    rgbe[..., 3] = rng.integers(100, 160, (h, w))
+    rgbe[h // 2, : w // 2] = rgbe[h // 2, 0]  # long runs for the RLE encoder
+    rgbe[0, 0, 3] = 0                          # exponent 0: black
+    return rgbe
+
+
+def test_hdr_load_flat_and_rle(tmp_path):
+    rng = np.random.default_rng(5)
+    for (h, w), rle, magic in (((3, 5), False, b"#?RGBE"), ((16, 40), True, b"#?RADIANCE"),
+                               ((9, 300), True, b"#?RADIANCE"), ((4, 7), True, b"#?RADIANCE")):
+        rgbe = _random_rgbe(rng, h, w)
+        p = tmp_path / f"img_{h}x{w}.hdr"
+        _write_hdr(p, rgbe, rle and w >= 8, magic)
+        want = _rgbe_to_float(rgbe)            # file rows, top first
+        top_first = N.load_image(p, flip_y=True, hdr=True)
+        bottom_first = N.load_image(p, flip_y=False, hdr=True)
+        assert top_first.shape == (h, w, 3) and top_first.dtype == np.float32
+        assert np.array_equal(top_first, want)
+        assert np.array_equal(bottom_first, want[::-1])
+
+
+def test_hdr_load_errors(tmp_path):
+    import pytest
+    with pytest.raises(N.PtError):
+        N.load_image(tmp_path / "missing.hdr", hdr=True)
+    bad = tmp_path / "bad.hdr"
+    bad.write_bytes(b"P6\n1 1\n255\n\0\0\0")
+    with pytest.raises(N.PtError):
+        N.load_image(bad, hdr=True)
+    rgbe = _random_rgbe(np.random.default_rng(0), 8, 16)
+    _write_hdr(bad, rgbe, True)
+    bad.write_bytes(bad.read_bytes()[:-9])  # truncated last run
+    with pytest.raises(N.PtError):
+        N.load_image(bad, hdr=True)
+
+
+def test_hdr_texels_match_reference_image_texture(tmp_path):
+    """Texel layout against the reference's own ImageTexture(isHDR = true)
+    (stbi_loadf) through the reference harness, where it is built: at the
+    lattice points u = x / W, v = y / H its bilinear getTexelColor returns
+    texel (x, y) itself."""
+    import pytest
+    from oracle.ref import refbind
+    if not refbind.available():
+        pytest.skip("reference harness not built")
+    rng = np.random.default_rng(9)
+    h, w = 8, 16
+    rgbe = _random_rgbe(rng, h, w)
+    p = tmp_path / "env.hdr"
+    _write_hdr(p, rgbe, True)
+    xs, ys = np.meshgrid(np.arange(w - 1), np.arange(h - 1))
+    uv = np.stack([xs.ravel() / w, ys.ravel() / h], 1).astype(np.float32)
+    for flip in (False, True):
+        ours = N.load_image(p, flip_y=flip, hdr=True)
+        ref = refbind.image_texels(p, flip, True, uv)
+        assert np.array_equal(ours[ys.ravel(), xs.ravel()], ref)
+
+
+# ---------------------------------------------------------------- PNG reading
+_CHANNELS = {0: 1, 2: 3, 3: 1, 4: 2, 6: 4}
+_ADAM7 = ((0, 0, 8, 8), (4, 0, 8, 8), (0, 4, 4, 8), (2, 0, 4, 4), (0, 2, 2, 4), (1, 0, 2, 2), (0, 1, 1, 2))
+
+
+def _pack_row(samples: np.ndarray, depth: int) -> bytes:
+    if depth == 16:
+        return samples.astype(">u2").tobytes()
+    if depth == 8:
+        return samples.astype(np.uint8).tobytes()
+    bits = np.unpackbits(samples.astype(np.uint8)[:, None], axis=1)[:, 8 - depth:].ravel()
+    return np.packbits(bits).tobytes()
+
+
+def _filter_row(raw: bytes, prev: bytes, bpp: int, f: int) -> bytes:
+    out = bytearray([f])
+    for i, x in enumerate(raw):
+        a = raw[i - bpp] if i >= bpp else 0
+        b = prev[i]
+        c = prev[i - bpp] if i >= bpp else 0
+        if f == 0:
+            pred = 0
+        elif f == 1:
+            pred = a
+        elif f == 2:
+            pred = b
+        elif f == 3:
+            pred = (a + b) >> 1
+        else:
+            p = a + b - c
+            pa, pb, pc = abs(p - a), abs(p - b), abs(p - c)
+            pred = a if pa <= pb and pa <= pc else (b if pb <= pc else c)
+        out.append((x - pred) & 255)
+    return bytes(out)
+
+
+def _write_png_file(path, samples: np.ndarray, ctype: int, depth: int, interlace: bool, level: int, rng,
+                    palette: np.ndarray | None = None):
+    """samples: (H, W, channels) integers; every scanline gets a random filter."""
+    h, w, ch = samples.shape
+    bpp = max(1, ch * depth // 8)
+    raw = bytearray()
+    passes = _ADAM7 if interlace else ((0, 0, 1, 1),)
+    for x0, y0, dx, dy in passes:
+        sub = samples[y0::dy, x0::dx]
+        if sub.size == 0:
+            continue
+        prev = bytes(len(_pack_row(sub[0].ravel(), depth)))
+        for r in range(sub.shape[0]):
+            row = _pack_row(sub[r].ravel(), depth)
+            raw += _filter_row(row, prev, bpp, int(rng.integers(0, 5)))
+            prev = row
+
+    def chunk(t, body):
+        return struct.pack(">I", len(body)) + t + body + struct.pack(">I", zlib.crc32(t + body) & 0xffffffff)
+    data = b"\x89PNG\r\n\x1a\n" + chunk(b"IHDR", struct.pack(">IIBBBBB", w, h, depth, ctype, 0, 0, int(interlace)))
+    data += chunk(b"tEXt", b"Comment\0made by the test")
+    if palette is not None:
+        data += chunk(b"PLTE", palette.astype(np.uint8).tobytes())
+    z = zlib.compress(bytes(raw), level)
+    for k in range(0, len(z), 97):  # several IDAT chunks
+        data += chunk(b"IDAT", z[k:k + 97])
+    data += chunk(b"IEND", b"")
+    path.write_bytes(data)
+
+
+def _expected_rgb8(samples, ctype, depth, palette):
+    if ctype == 3:
+        return palette[samples[..., 0]].astype(np.uint8)
+    s = samples.astype(np.uint32)
+    s = s >> 8 if depth == 16 else s * {1: 255, 2: 0x55, 4: 0x11, 8: 1}[depth]
+    if ctype in (0, 4):
+        return np.repeat(s[..., :1], 3, axis=2).astype(np.uint8)
+    return s[..., :3].astype(np.uint8)
+
+
+def _png_cases():
+    for ctype, depths in ((0, (1, 2, 4, 8, 16)), (2, (8, 16)), (3, (1, 2, 4, 8)), (4, (8, 16)), (6, (8, 16))):
+        for depth in depths:
+            yield ctype, depth
+
+
+def test_png_load_every_colour_type_depth_and_filter(tmp_path):
+    rng = np.random.default_rng(11)
+    for ctype, depth in _png_cases():
+        for (h, w), interlace, level in (((13, 21), False, 6), ((11, 17), True, 9), ((5, 3), True, 0),
+                                         ((1, 1), False, 1)):
+            ch = _CHANNELS[ctype]
+            samples = rng.integers(0, 1 << depth, (h, w, ch))
+            palette = None
+            if ctype == 3:
+                samples = samples % min(1 << depth, 40)
+                palette = rng.integers(0, 256, (min(1 << depth, 40), 3))
+            p = tmp_path / f"c{ctype}_d{depth}_{h}x{w}_{int(interlace)}.png"
+            _write_png_file(p, samples, ctype, depth, interlace, level, rng, palette)
+            want = _expected_rgb8(samples, ctype, depth, palette).astype(np.float32) / np.float32(255)
+            got = N.load_image(p, flip_y=True)
+            assert got.shape == (h, w, 3), (ctype, depth)
+            assert np.array_equal(got, want), (ctype, depth, interlace, level)
+            assert np.array_equal(N.load_image(p, flip_y=False), want[::-1])
+
+
+def test_png_writer_reader_round_trip(tmp_path):
+    rng = np.random.default_rng(3)
+    img = rng.integers(0, 256, (70, 45, 3), dtype=np.uint8)
+    p = tmp_path / "rt.png"
+    N.write_png(p, img)
+    assert np.array_equal(N.load_image(p, flip_y=True), img.astype(np.float32) / np.float32(255))
+
+
+def test_png_load_errors(tmp_path):
+    import pytest
+    rng = np.random.default_rng(4)
+    p = tmp_path / "ok.png"
+    _write_png_file(p, rng.integers(0, 256, (9, 9, 3)), 2, 8, False, 6, rng)
+    good = p.read_bytes()
+    cases = {
+        "crc": good[:40] + bytes([good[40] ^ 1]) + good[41:],
+        "truncated": good[: len(good) // 2],
+        "signature": b"\x89PNX" + good[4:],
+    }
+    for name, data in cases.items():
+        q = tmp_path / f"{name}.png"
+        q.write_bytes(data)
+        with pytest.raises(N.PtError):
+            N.load_image(q)
+
+
+def test_png_texels_match_reference_image_texture(tmp_path):
+    """PNG texels against the reference's ImageTexture (stbi_load /
+    stbi_loadf) through the reference harness, where it is built: RGB 8- and
+    16-bit, palette and Adam7 files (the three-component files the reference
+    indexes correctly), LDR exact, isHDR within float rounding of powf."""
+    import pytest
+    from oracle.ref import refbind
+    if not refbind.available():
+        pytest.skip("reference harness not built")
+    rng = np.random.default_rng(21)
+    h, w = 16, 32
+    xs, ys = np.meshgrid(np.arange(w - 1), np.arange(h - 1))
+    uv = np.stack([xs.ravel() / w, ys.ravel() / h], 1).astype(np.float32)
+    for ctype, depth, interlace in ((2, 8, False), (2, 16, False), (2, 8, True), (3, 4, False)):
+        samples = rng.integers(0, 1 << depth, (h, w, _CHANNELS[ctype]))
+        palette = rng.integers(0, 256, (16, 3)) if ctype == 3 else None
+        p = tmp_path / f"ref_{ctype}_{depth}_{int(interlace)}.png"
+        _write_png_file(p, samples, ctype, depth, interlace, 6, rng, palette)
+        for flip in (False, True):
+            ours = N.load_image(p, flip_y=flip)[ys.ravel(), xs.ravel()]
+            assert np.array_equal(ours, refbind.image_texels(p, flip, False, uv)), (ctype, depth, flip)
+            lin = N.load_image(p, flip_y=flip, hdr=True)[ys.ravel(), xs.ravel()]
+            np.testing.assert_allclose(lin, refbind.image_texels(p, flip, True, uv), rtol=2e-7, atol=0)
