@@ -100,10 +100,32 @@ class NoiseTexture : public Texture2D {
   float scale;
   int fractal;
 };
+namespace detail {
+// ImageTexture(filename, flip_y, isHDR)'s texels (texture.cpp:3-93) through
+// pt_load_image; throws std::runtime_error like the reference.
+inline std::vector<float> load_texels(const std::string &path, bool flip_y, bool is_hdr, int &w, int &h) {
+  float *p = nullptr;
+  int32_t W = 0, H = 0;
+  if (pt_load_image(path.c_str(), flip_y, is_hdr, &p, &W, &H) != PT_OK) {
+    char buf[512] = {0};
+    pt_last_error(nullptr, buf, sizeof buf);
+    throw std::runtime_error(buf);
+  }
+  std::vector<float> v(p, p + (size_t)W * H * 3);
+  pt_free_image(p);
+  w = W;
+  h = H;
+  return v;
+}
+}  // namespace detail
+
 class ImageTexture : public Texture2D {
  public:
   ImageTexture(std::vector<float> texels, int width, int height)
       : texels(std::move(texels)), width(width), height(height) {}
+  // texture.hpp:55: a PNG or Radiance HDR file
+  explicit ImageTexture(const std::string &filename, bool flip_y = false, bool isHDR = false)
+      : texels(detail::load_texels(filename, flip_y, isHDR, width, height)) {}
   pt_texture_desc desc() const override {
     pt_texture_desc d{};
     d.kind = PT_TEX_IMAGE;
@@ -525,11 +547,15 @@ class ObjectList {  // base/objectList.hpp
   std::vector<std::shared_ptr<Hittable>> objects;
 };
 
-// EnvironmentLight over texels given in memory (row 0 = bottom, RGB).
+// EnvironmentLight over texels given in memory (row 0 = bottom, RGB) or
+// loaded from an HDR image file.
 class EnvironmentLight {
  public:
   EnvironmentLight(std::vector<float> texels, int width, int height, float intensity = 1.0f)
       : texels(std::move(texels)), width(width), height(height), intensity(intensity) {}
+  // envLight.hpp:7: HDRITexture(hdri_filepath, flip_y = false, isHDR = true)
+  explicit EnvironmentLight(const std::string &hdri_filepath, float intensity_scale = 1.0f)
+      : texels(detail::load_texels(hdri_filepath, false, true, width, height)), intensity(intensity_scale) {}
   std::vector<float> texels;
   int width, height;
   float intensity;

@@ -69,6 +69,16 @@ class Scene:
                               "fractal": fractal, "texels": texels})
         return len(self.textures) - 1
 
+    def add_image_texture(self, path, flip_y: bool = False, hdr: bool = False) -> int:
+        """ImageTexture(filename, flip_y, isHDR): a PNG or Radiance HDR file."""
+        return self.add_texture(N.TEX_IMAGE, texels=N.load_image(path, flip_y, hdr))
+
+    def set_environment(self, path, intensity: float = 1.0) -> None:
+        """EnvironmentLight(hdri_filepath, intensity_scale): HDRITexture with
+        flip_y = false, isHDR = true."""
+        self.env = N.load_image(path, flip_y=False, hdr=True)
+        self.env_intensity = float(intensity)
+
     def add_mesh(self, mesh: Mesh, velocity=(0.0, 0.0, 0.0)):
         self.meshes.append(mesh)
         self.objects.append((N.OBJ_MESH, len(self.meshes) - 1, tuple(velocity)))

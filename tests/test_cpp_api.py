@@ -91,3 +91,28 @@ def test_cpp_scene_renders_like_python(tmp_path):
     film = r.render(N.job_desc(sid, cam, 48, 48, 4, 4, 8, estimator=N.EST_NEE_MIS, env_sampling=N.ENV_ALIAS))
     r.close()
     np.testing.assert_allclose(cpp_mean, film.reshape(-1, 3).mean(0), rtol=1e-5)
+
+
+@pytest.mark.skipif(shutil.which("g++") is None, reason="needs g++")
+def test_cpp_image_files_load_like_python(tmp_path):
+    """ImageTexture(filename, flip_y) and EnvironmentLight(hdri_filepath) in
+    the C++ API load the same texels as pathtracer_gb300.native.load_image."""
+    from pathtracer_gb300 import native as N
+    rng = np.random.default_rng(2)
+    img = rng.integers(0, 256, (9, 14, 3), dtype=np.uint8)
+    png = tmp_path / "tex.png"
+    N.write_png(png, img)
+    hdr = tmp_path / "env.hdr"
+    rgbe = rng.integers(0, 256, (6, 10, 4), dtype=np.uint8)
+    hdr.write_bytes(b"#?RADIANCE\nFORMAT=32-bit_rle_rgbe\n\n-Y 6 +X 10\n" + rgbe.tobytes())
+    exe = _build(tmp_path, REPO / "tests" / "cpp" / "image_files_example.cpp")
+    lines = subprocess.run([str(exe), str(png), str(hdr)], capture_output=True, text=True, check=True).stdout.split("\n")
+    w, h = map(int, lines[0].split())
+    got_png = np.array(lines[1:1 + w * h * 3], np.float32).reshape(h, w, 3)
+    k = 1 + w * h * 3
+    w2, h2 = map(int, lines[k].split())
+    got_env = np.array(lines[k + 1:k + 1 + w2 * h2 * 3], np.float32).reshape(h2, w2, 3)
+    assert (w, h, w2, h2) == (14, 9, 10, 6)
+    assert np.array_equal(got_png, N.load_image(png, flip_y=True))
+    assert np.array_equal(got_env, N.load_image(hdr, flip_y=False, hdr=True))
+    assert lines[k + 1 + w2 * h2 * 3] == "missing-file error"

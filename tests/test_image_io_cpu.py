@@ -307,3 +307,19 @@ def test_png_texels_match_reference_image_texture(tmp_path):
             assert np.array_equal(ours, refbind.image_texels(p, flip, False, uv)), (ctype, depth, flip)
             lin = N.load_image(p, flip_y=flip, hdr=True)[ys.ravel(), xs.ravel()]
             np.testing.assert_allclose(lin, refbind.image_texels(p, flip, True, uv), rtol=2e-7, atol=0)
+
+
+def test_scene_image_texture_and_environment_from_files(tmp_path):
+    from pathtracer_gb300 import scene as S
+    rng = np.random.default_rng(8)
+    png = tmp_path / "albedo.png"
+    img = rng.integers(0, 256, (12, 20, 3), dtype=np.uint8)
+    N.write_png(png, img)
+    hdr = tmp_path / "sky.hdr"
+    _write_hdr(hdr, _random_rgbe(rng, 16, 32), True)
+    sc = S.Scene()
+    t = sc.add_image_texture(png, flip_y=False)
+    sc.set_environment(hdr, intensity=1.5)
+    assert np.array_equal(sc.textures[t]["texels"], (img.astype(np.float32) / np.float32(255))[::-1])
+    assert sc.env.shape == (16, 32, 3) and sc.env_intensity == 1.5
+    assert np.array_equal(sc.env, N.load_image(hdr, hdr=True))
