@@ -320,6 +320,20 @@ int pt_scene_release(void *ctx, int32_t scene_id);
  * build time in microseconds.  Errors: pt_last_error(NULL, ...). */
 int pt_bvh_build(const pt_scene_desc *desc, int32_t threads, int64_t *out5);
 
+/* Mesh BVH builder of a context's later pt_scene_upload calls (no reference
+ * counterpart: the reference builds on the host).  PT_BVH_BUILD_HOST
+ * (default) is the reference's recursion (MeshBVHNode, meshBVH.cpp:6-55) on
+ * host threads; PT_BVH_BUILD_DEVICE builds meshes of >= 16384 triangles on
+ * the GPU with the same split rule, level by level: the same tree whenever
+ * no two centroids of a node tie along its split axis (ties: by triangle
+ * index), i.e. the same hits, found faster for large meshes. */
+#define PT_BVH_BUILD_HOST 0
+#define PT_BVH_BUILD_DEVICE 1
+int pt_set_bvh_builder(void *ctx, int32_t builder);
+/* pt_bvh_build with the context's device builder for large meshes: the
+ * scene is validated and built (BVH4, items) but not kept.  Same out5. */
+int pt_bvh_build_device(void *ctx, const pt_scene_desc *desc, int64_t *out5);
+
 /* OBJ ingest: loadOBJMesh (src/mesh_io/meshLoader.cpp:7-58), which reads the
  * file with tinyobjloader.  "v", "vn", "vt" and "f" records; face vertices
  * "v", "v/vt", "v//vn", "v/vt/vn" with 1-based or negative indices; an

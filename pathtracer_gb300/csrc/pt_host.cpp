@@ -21,6 +21,7 @@
 #include <cuda_runtime.h>
 
 #include "pt_host.h"
+#include "pt_bvh_gpu.h"
 
 namespace pt {
 
@@ -199,6 +200,8 @@ struct Builder {
   int box_quad_base = 0;          // first rectangle of the boxes' faces
   int curve_base = 0;             // first curve primitive
   int threads = 0;               // mesh BVH build workers (0: hardware threads)
+  bool gpu_bvh = false;          // large meshes built by the device builder
+  cudaStream_t gpu_stream = nullptr;
   std::vector<int> obj_motion;   // per object: motion index + 1 (0: static)
   std::vector<BNode> nodes;
   std::vector<int> inst_motion;  // per node: motion index + 1 if it roots a moving object's subtree
@@ -316,6 +319,57 @@ struct Builder {
     if (ids.size() <= (1u << 16)) par_depth = 0;
     Part p;
     build_mesh_part(mesh, std::move(ids), cen, p, par_depth);
+    return append_part(p);
+  }
+
+  // The same tree from the device builder (pt_bvh_gpu.cu), renumbered in
+  // the host recursion's preorder.
+  int build_mesh_gpu(int mesh) {
+    const pt_mesh_desc &m = d->meshes[mesh];
+    std::vector<GpuBvhNode> g;
+    std::vector<int32_t> perm;
+    try {
+      gpu_mesh_bvh(m.positions, m.n_positions, m.indices, m.n_triangles, gpu_stream, g, perm);
+    } catch (const GpuBvhError &e) {
+      fail(PT_ERR_CUDA, e.what());
+    }
+    Part p;
+    p.nodes.reserve(g.size());
+    p.prims.resize(perm.size());
+    for (size_t k = 0; k < perm.size(); ++k) p.prims[k] = tri_base[mesh] + perm[k];
+    // preorder: node, left subtree, right subtree (explicit stack of
+    // (device node, parent slot to patch))
+    std::vector<std::pair<int, int>> stack = {{0, -1}};
+    while (!stack.empty()) {
+      auto [x, parent] = stack.back();
+      stack.pop_back();
+      if (x < 0 || x >= (int)g.size()) fail(PT_ERR_CUDA, "device BVH: bad child index");
+      const GpuBvhNode &G = g[x];
+      const int me = (int)p.nodes.size();
+      p.nodes.push_back(BNode());
+      BNode &N = p.nodes[me];
+      for (int a = 0; a < 3; ++a) {
+        N.box.lo[a] = G.lo[a];
+        N.box.hi[a] = G.hi[a];
+      }
+      if (parent >= 0) {  // parent slot: 2 * node + side
+        BNode &P = p.nodes[parent >> 1];
+        (parent & 1 ? P.right : P.left) = me;
+      }
+      if (G.left < 0) {
+        if (G.count < 1 || G.count > 4) fail(PT_ERR_CUDA, "device BVH: bad leaf");
+        N.first = G.start;
+        N.count = G.count;
+      } else {
+        stack.push_back({G.left + 1, 2 * me + 1});  // right after the whole left subtree
+        stack.push_back({G.left, 2 * me});
+      }
+    }
+    return append_part(p);
+  }
+
+  // Appends a mesh tree (rooted at its index 0) to the scene's nodes.
+  int append_part(Part &p) {
     Part top;
     top.nodes = std::move(nodes);
     top.prims = std::move(leaf_prims);
@@ -410,7 +464,7 @@ struct Builder {
       const pt_mesh_desc &m = d->meshes[od.index];
       std::vector<int> ids(m.n_triangles);
       std::iota(ids.begin(), ids.end(), 0);
-      me = build_mesh(od.index, ids);
+      me = gpu_bvh && m.n_triangles >= PT_GPU_BVH_MIN ? build_mesh_gpu(od.index) : build_mesh(od.index, ids);
     } else {
       me = (int)nodes.size();
       nodes.push_back(BNode());
@@ -670,7 +724,7 @@ static void box_faces(const pt_box_desc &b, std::vector<pt_quad_desc> &out) {
 }
 
 std::unique_ptr<Scene> build_scene(const pt_scene_desc *d_in, cudaStream_t st, bool device, int threads,
-                                   int trav_cap) {
+                                   int trav_cap, bool gpu_bvh) {
   if (!d_in) fail(PT_ERR_INVALID, "null scene description");
   // boxes become six rectangles each, after the scene's own rectangles
   pt_scene_desc aug = *d_in;
@@ -690,6 +744,8 @@ std::unique_ptr<Scene> build_scene(const pt_scene_desc *d_in, cudaStream_t st, b
   Builder B;
   B.d = d;
   B.threads = threads;
+  B.gpu_bvh = gpu_bvh;
+  B.gpu_stream = st;
   B.box_quad_base = n_user_quads;
   for (int m = 0; m < d->n_meshes; ++m) {
     const pt_mesh_desc &md = d->meshes[m];
@@ -1622,7 +1678,7 @@ int pt_scene_upload(void *ctx, const pt_scene_desc *desc, int32_t *scene_id) {
     c = as_ctx(ctx);
     if (!scene_id) fail(PT_ERR_INVALID, "null scene_id");
     cuda_check(cudaSetDevice(c->device), "cudaSetDevice");
-    auto S = build_scene(desc, c->stream, true, 0, c->trav_cap);
+    auto S = build_scene(desc, c->stream, true, 0, c->trav_cap, c->bvh_builder == PT_BVH_BUILD_DEVICE);
     int id = c->next_scene++;
     c->scenes[id] = std::move(S);
     *scene_id = id;
@@ -1657,6 +1713,33 @@ int pt_bvh_build(const pt_scene_desc *desc, int32_t threads, int64_t *out5) {
     if (!out5) fail(PT_ERR_INVALID, "null output");
     auto t0 = std::chrono::steady_clock::now();
     auto S = build_scene(desc, nullptr, false, threads, 0);
+    auto t1 = std::chrono::steady_clock::now();
+    out5[0] = S->n_nodes;
+    out5[1] = S->n_items;
+    out5[2] = S->bvh_depth;
+    uint64_t h = S->bvh_hash;
+    std::memcpy(&out5[3], &h, sizeof h);
+    out5[4] = (int64_t)std::chrono::duration_cast<std::chrono::microseconds>(t1 - t0).count();
+  });
+}
+
+int pt_set_bvh_builder(void *ctx, int32_t builder) {
+  Context *c = static_cast<Context *>(ctx);
+  PT_GUARD(c, {
+    c = as_ctx(ctx);
+    if (builder != PT_BVH_BUILD_HOST && builder != PT_BVH_BUILD_DEVICE) fail(PT_ERR_INVALID, "unknown BVH builder");
+    c->bvh_builder = builder;
+  });
+}
+
+int pt_bvh_build_device(void *ctx, const pt_scene_desc *desc, int64_t *out5) {
+  Context *c = static_cast<Context *>(ctx);
+  PT_GUARD(c, {
+    c = as_ctx(ctx);
+    if (!out5) fail(PT_ERR_INVALID, "null output");
+    cuda_check(cudaSetDevice(c->device), "cudaSetDevice");
+    auto t0 = std::chrono::steady_clock::now();
+    auto S = build_scene(desc, c->stream, false, 0, 0, true);
     auto t1 = std::chrono::steady_clock::now();
     out5[0] = S->n_nodes;
     out5[1] = S->n_items;

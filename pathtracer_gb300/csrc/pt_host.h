@@ -54,8 +54,11 @@ struct Scene {
   ~Scene();
 };
 
+// gpu_bvh: meshes of at least PT_GPU_BVH_MIN triangles get their BVH from
+// the device builder (on st's device) instead of the host recursion.
 std::unique_ptr<Scene> build_scene(const pt_scene_desc *d, cudaStream_t st, bool device, int threads,
-                                   int trav_cap);
+                                   int trav_cap, bool gpu_bvh = false);
+constexpr int PT_GPU_BVH_MIN = 1 << 14;
 
 // Device buffers of one merged group of a batch (the jobs of one scene with
 // the same light-sample count), reused across batched renders.
@@ -99,6 +102,7 @@ struct Context {
   LaunchCfg cfg;
   int wave_cap = 1 << 22;
   int trav_cap = 0;  // 0: PT_TRAVERSAL_CAP
+  int bvh_builder = PT_BVH_BUILD_HOST;
   std::string last_error;
   std::map<int, std::unique_ptr<Scene>> scenes;
   int next_scene = 1;

@@ -27,11 +27,12 @@ OBJ_MESH, OBJ_QUAD, OBJ_SPHERE, OBJ_BOX, OBJ_CURVE = 0, 1, 2, 3, 4
 EST_REF_NEE, EST_NEE_MIS = 0, 1
 SAMPLER_HALTON_NONE, SAMPLER_HALTON_PERMUTE, SAMPLER_HALTON_OWEN, SAMPLER_STRATIFIED = range(4)
 ENV_UNIFORM, ENV_ALIAS = 0, 1
+BVH_BUILD_HOST, BVH_BUILD_DEVICE = 0, 1
 
 # exported symbols of the C-ABI, in header order
 EXPORTS = [
     "pt_create", "pt_destroy", "pt_last_error", "pt_version", "pt_scene_upload", "pt_scene_release",
-    "pt_bvh_build", "pt_obj_load", "pt_obj_free", "pt_load_image", "pt_free_image", "pt_scene_info", "pt_render", "pt_render_device", "pt_render_device_noalloc",
+    "pt_bvh_build", "pt_set_bvh_builder", "pt_bvh_build_device", "pt_obj_load", "pt_obj_free", "pt_load_image", "pt_free_image", "pt_scene_info", "pt_render", "pt_render_device", "pt_render_device_noalloc",
     "pt_profile_begin",
     "pt_profile_end", "pt_tonemap", "pt_gaussian_blur", "pt_write_png", "pt_sampler_eval", "pt_trace_closest",
     "pt_trace_any", "pt_bsdf_eval", "pt_bsdf_sample", "pt_render_batch", "pt_autotune", "pt_server_create",
@@ -166,6 +167,8 @@ def load() -> C.CDLL:
         "pt_scene_upload": [vp, C.POINTER(SceneDesc), i32p],
         "pt_scene_release": [vp, C.c_int32],
         "pt_bvh_build": [C.POINTER(SceneDesc), C.c_int32, C.POINTER(C.c_int64)],
+        "pt_set_bvh_builder": [C.c_void_p, C.c_int32],
+        "pt_bvh_build_device": [C.c_void_p, C.POINTER(SceneDesc), C.POINTER(C.c_int64)],
         "pt_obj_load": [C.c_char_p, C.POINTER(MeshDesc)],
         "pt_obj_free": [C.POINTER(MeshDesc)],
         "pt_load_image": [C.c_char_p, C.c_int32, C.c_int32, C.POINTER(f32p), C.POINTER(C.c_int32),
@@ -403,6 +406,20 @@ class Renderer:
 
     def release(self, sid: int):
         self._check(self.lib.pt_scene_release(self.ctx, sid))
+
+    def set_bvh_builder(self, builder: int):
+        """BVH_BUILD_HOST (the reference's recursion, default) or
+        BVH_BUILD_DEVICE (large meshes built on the GPU) for later uploads."""
+        self._check(self.lib.pt_set_bvh_builder(self.ctx, int(builder)))
+
+    def bvh_build_device(self, scene) -> dict:
+        """pt_bvh_build_device: the scene's BVH4 with large meshes built on the
+        GPU, not kept (same keys as bvh_build)."""
+        sb = make_scene_desc(scene)
+        out = (C.c_int64 * 5)()
+        self._check(self.lib.pt_bvh_build_device(self.ctx, C.byref(sb.desc), out))
+        return {"nodes": out[0], "items": out[1], "depth": out[2], "hash": out[3] & 0xffffffffffffffff,
+                "build_us": out[4]}
 
     def scene_info(self, sid: int):
         out = (C.c_int64 * 6)()
