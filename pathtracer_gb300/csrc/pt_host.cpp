@@ -162,6 +162,26 @@ MatRec derive_material(const pt_material_desc &m) {
   return r;
 }
 
+// Runs f(i) for i in [0, n) on up to `threads` host threads (0: all
+// hardware threads), in contiguous chunks; f must touch disjoint state per i.
+template <class F>
+static void parallel_for(size_t n, int threads, F f) {
+  unsigned hw = threads > 0 ? (unsigned)threads : std::max(1u, std::thread::hardware_concurrency());
+  const size_t grain = 1 << 15;
+  const unsigned nt = (unsigned)std::min<size_t>(hw, (n + grain - 1) / grain);
+  if (nt <= 1) {
+    for (size_t i = 0; i < n; ++i) f(i);
+    return;
+  }
+  std::vector<std::thread> pool;
+  for (unsigned w = 0; w < nt; ++w)
+    pool.emplace_back([&, w] {
+      const size_t b = n * w / nt, e = n * (w + 1) / nt;
+      for (size_t i = b; i < e; ++i) f(i);
+    });
+  for (auto &t : pool) t.join();
+}
+
 // ---------------------------------------------------------------- scene
 struct Box {
   float lo[3], hi[3];
@@ -537,22 +557,29 @@ static int motion_of(const Builder &B, int bn) {
 // subtree is traversed in the object's frame.
 static void collapse(const Builder &B, int bn, Bvh4Out &out, int depth, int me, bool in_inst) {
   // gather up to 4 children by expanding the largest internal child
-  std::vector<int> ch = {B.nodes[bn].left, B.nodes[bn].right};
-  if (B.nodes[bn].left < 0) ch = {bn};  // a leaf as the root
-  while (ch.size() < 4) {
+  int ch[4], nch = 2;
+  ch[0] = B.nodes[bn].left;
+  ch[1] = B.nodes[bn].right;
+  if (B.nodes[bn].left < 0) {  // a leaf as the root
+    ch[0] = bn;
+    nch = 1;
+  }
+  while (nch < 4) {
     int best = -1;
     float ba = -1.f;
-    for (size_t k = 0; k < ch.size(); ++k) {
+    for (int k = 0; k < nch; ++k) {
       const BNode &c = B.nodes[ch[k]];
       if (c.left >= 0 && (in_inst || !motion_of(B, ch[k])) && box_area(c.box) > ba) {
         ba = box_area(c.box);
-        best = (int)k;
+        best = k;
       }
     }
     if (best < 0) break;
-    int x = ch[best];
+    const int x = ch[best];
+    for (int k = nch; k > best + 1; --k) ch[k] = ch[k - 1];
     ch[best] = B.nodes[x].left;
-    ch.insert(ch.begin() + best + 1, B.nodes[x].right);
+    ch[best + 1] = B.nodes[x].right;
+    ++nch;
   }
   out.max_depth = std::max(out.max_depth, depth + 1);
   Bvh4Node &N0 = out.nodes[me];
@@ -562,7 +589,7 @@ static void collapse(const Builder &B, int bn, Bvh4Out &out, int depth, int me, 
     N0.child[k] = 0;
     N0.count[k] = -1;
   }
-  for (size_t k = 0; k < ch.size(); ++k) {
+  for (int k = 0; k < nch; ++k) {
     const BNode &c = B.nodes[ch[k]];
     Bvh4Node &N = out.nodes[me];
     N.lo_x[k] = c.box.lo[0];
@@ -724,7 +751,7 @@ static void box_faces(const pt_box_desc &b, std::vector<pt_quad_desc> &out) {
 }
 
 std::unique_ptr<Scene> build_scene(const pt_scene_desc *d_in, cudaStream_t st, bool device, int threads,
-                                   int trav_cap, bool gpu_bvh) {
+                                   int trav_cap, bool gpu_bvh, bool want_hash) {
   if (!d_in) fail(PT_ERR_INVALID, "null scene description");
   // boxes become six rectangles each, after the scene's own rectangles
   pt_scene_desc aug = *d_in;
@@ -851,7 +878,7 @@ std::unique_ptr<Scene> build_scene(const pt_scene_desc *d_in, cudaStream_t st, b
       prim_mesh[B.tri_base[m] + t] = m;
       prim_tri[B.tri_base[m] + t] = t;
     }
-  for (size_t k = 0; k < out.leaf_order.size(); ++k) {
+  parallel_for(out.leaf_order.size(), threads, [&](size_t k) {
     const int prim = out.leaf_order[k];
     Item &it = items[k];
     std::memset(&it, 0, sizeof it);
@@ -892,8 +919,9 @@ std::unique_ptr<Scene> build_scene(const pt_scene_desc *d_in, cudaStream_t st, b
       it.b[0] = s.radius;
       it.b[3] = u2f(ITEM_SPHERE);
     }
-  }
-  for (int prim = 0; prim < n_prims; ++prim) {
+  });
+  parallel_for((size_t)n_prims, threads, [&](size_t pi) {
+    const int prim = (int)pi;
     PrimShade &ps = shade[prim];
     std::memset(&ps, 0, sizeof ps);
     ps.item = prim_item[prim];
@@ -941,7 +969,7 @@ std::unique_ptr<Scene> build_scene(const pt_scene_desc *d_in, cudaStream_t st, b
       for (int a = 0; a < 3; ++a) ps.n0[a] = s.center[a];
       if (s.flip_face) ps.flags |= PT_PRIM_FLIP;
     }
-  }
+  });
 
   // materials
   std::vector<MatRec> mats;
@@ -1154,8 +1182,9 @@ std::unique_ptr<Scene> build_scene(const pt_scene_desc *d_in, cudaStream_t st, b
   }
 
   // content hash of the BVH (nodes and leaf items): equal hashes, equal trees
-  S->bvh_hash = fnv1a(items.data(), items.size() * sizeof(Item),
-                      fnv1a(out.nodes.data(), out.nodes.size() * sizeof(Bvh4Node), 0xcbf29ce484222325ull));
+  if (want_hash)
+    S->bvh_hash = fnv1a(items.data(), items.size() * sizeof(Item),
+                        fnv1a(out.nodes.data(), out.nodes.size() * sizeof(Bvh4Node), 0xcbf29ce484222325ull));
   S->n_nodes = (int64_t)out.nodes.size();
   S->n_items = (int64_t)items.size();
 
@@ -1712,7 +1741,7 @@ int pt_bvh_build(const pt_scene_desc *desc, int32_t threads, int64_t *out5) {
   PT_GUARD(nullptr, {
     if (!out5) fail(PT_ERR_INVALID, "null output");
     auto t0 = std::chrono::steady_clock::now();
-    auto S = build_scene(desc, nullptr, false, threads, 0);
+    auto S = build_scene(desc, nullptr, false, threads, 0, false, true);
     auto t1 = std::chrono::steady_clock::now();
     out5[0] = S->n_nodes;
     out5[1] = S->n_items;
@@ -1739,7 +1768,7 @@ int pt_bvh_build_device(void *ctx, const pt_scene_desc *desc, int64_t *out5) {
     if (!out5) fail(PT_ERR_INVALID, "null output");
     cuda_check(cudaSetDevice(c->device), "cudaSetDevice");
     auto t0 = std::chrono::steady_clock::now();
-    auto S = build_scene(desc, c->stream, false, 0, 0, true);
+    auto S = build_scene(desc, c->stream, false, 0, 0, true, true);
     auto t1 = std::chrono::steady_clock::now();
     out5[0] = S->n_nodes;
     out5[1] = S->n_items;
