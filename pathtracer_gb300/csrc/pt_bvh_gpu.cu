@@ -197,14 +197,7 @@ __global__ void __launch_bounds__(RADIX_THREADS) k_radix_scatter(const uint32_t 
 }
 
 // ------------------------------------------------------------ levels
-struct DNode {
-  float lo[3], hi[3];  // padded box
-  int start, count;
-  int left;            // first of the two children, -1 for a leaf
-  int axis;            // split axis (internal nodes)
-  int paxis;           // the parent's split axis (-1 for the root)
-  int pad;
-};
+using DNode = GpuBvhNode;
 
 __global__ void k_level_init(DNode *nodes, int b, int e, uint32_t *bkey) {
   for (int x = b + blockIdx.x * blockDim.x + threadIdx.x; x < e; x += gridDim.x * blockDim.x) {
@@ -450,22 +443,12 @@ void gpu_mesh_bvh(const float *positions, int n_positions, const int32_t *indice
     b = e;
     e = total;
   }
-  std::vector<DNode> h(total);
-  check(cudaMemcpyAsync(h.data(), nodes.p, sizeof(DNode) * (size_t)total, cudaMemcpyDeviceToHost, st), "nodes");
+  out_nodes.resize(total);
+  check(cudaMemcpyAsync(out_nodes.data(), nodes.p, sizeof(DNode) * (size_t)total, cudaMemcpyDeviceToHost, st),
+        "nodes");
   leaf_perm.resize(n);
   check(cudaMemcpyAsync(leaf_perm.data(), perm.p, sizeof(int32_t) * (size_t)n, cudaMemcpyDeviceToHost, st), "perm");
   check(cudaStreamSynchronize(st), "BVH download");
-  out_nodes.resize(total);
-  for (int x = 0; x < total; ++x) {
-    GpuBvhNode &o = out_nodes[x];
-    for (int a = 0; a < 3; ++a) {
-      o.lo[a] = h[x].lo[a];
-      o.hi[a] = h[x].hi[a];
-    }
-    o.start = h[x].start;
-    o.count = h[x].count;
-    o.left = h[x].left;
-  }
 }
 
 }  // namespace pt

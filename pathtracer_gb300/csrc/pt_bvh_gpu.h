@@ -17,7 +17,11 @@ struct GpuBvhError : std::runtime_error {
 // leaf order, and its first child (the second is left + 1; -1: a leaf).
 struct GpuBvhNode {
   float lo[3], hi[3];
-  int start, count, left;
+  int start, count;
+  int left;
+  int axis;   // split axis (internal nodes)
+  int paxis;  // the parent's split axis (-1: the root)
+  int pad;
 };
 
 // Builds the median-split BVH of one triangle mesh on the current device.

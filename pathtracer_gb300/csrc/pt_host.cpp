@@ -353,39 +353,39 @@ struct Builder {
     } catch (const GpuBvhError &e) {
       fail(PT_ERR_CUDA, e.what());
     }
-    Part p;
-    p.nodes.reserve(g.size());
-    p.prims.resize(perm.size());
-    for (size_t k = 0; k < perm.size(); ++k) p.prims[k] = tri_base[mesh] + perm[k];
-    // preorder: node, left subtree, right subtree (explicit stack of
-    // (device node, parent slot to patch))
+    // appended to the scene's nodes in preorder (node, left subtree, right
+    // subtree; an explicit stack of (device node, parent slot to patch))
+    const int root = (int)nodes.size(), pb = (int)leaf_prims.size();
+    nodes.reserve(nodes.size() + g.size());
+    leaf_prims.resize(pb + perm.size());
+    for (size_t k = 0; k < perm.size(); ++k) leaf_prims[pb + k] = tri_base[mesh] + perm[k];
     std::vector<std::pair<int, int>> stack = {{0, -1}};
     while (!stack.empty()) {
       auto [x, parent] = stack.back();
       stack.pop_back();
       if (x < 0 || x >= (int)g.size()) fail(PT_ERR_CUDA, "device BVH: bad child index");
       const GpuBvhNode &G = g[x];
-      const int me = (int)p.nodes.size();
-      p.nodes.push_back(BNode());
-      BNode &N = p.nodes[me];
+      const int me = (int)nodes.size();
+      nodes.push_back(BNode());
+      BNode &N = nodes[me];
       for (int a = 0; a < 3; ++a) {
         N.box.lo[a] = G.lo[a];
         N.box.hi[a] = G.hi[a];
       }
       if (parent >= 0) {  // parent slot: 2 * node + side
-        BNode &P = p.nodes[parent >> 1];
+        BNode &P = nodes[parent >> 1];
         (parent & 1 ? P.right : P.left) = me;
       }
       if (G.left < 0) {
         if (G.count < 1 || G.count > 4) fail(PT_ERR_CUDA, "device BVH: bad leaf");
-        N.first = G.start;
+        N.first = pb + G.start;
         N.count = G.count;
       } else {
         stack.push_back({G.left + 1, 2 * me + 1});  // right after the whole left subtree
         stack.push_back({G.left, 2 * me});
       }
     }
-    return append_part(p);
+    return root;
   }
 
   // Appends a mesh tree (rooted at its index 0) to the scene's nodes.
