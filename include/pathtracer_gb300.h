@@ -329,6 +329,12 @@ int pt_bvh_build(const pt_scene_desc *desc, int32_t threads, int64_t *out5);
  * index), i.e. the same hits, found faster for large meshes. */
 #define PT_BVH_BUILD_HOST 0
 #define PT_BVH_BUILD_DEVICE 1
+/* Binned-SAH trees (meshes and the object level) on host threads: not the
+ * reference's tree -- the same hits (up to exact ties in t), fewer node
+ * visits where the reference's median / insertion-order splits are poor. */
+#define PT_BVH_BUILD_SAH 2
+/* pt_bvh_build with PT_BVH_BUILD_SAH trees (host only, no context). */
+int pt_bvh_build_sah(const pt_scene_desc *desc, int32_t threads, int64_t *out5);
 int pt_set_bvh_builder(void *ctx, int32_t builder);
 /* pt_bvh_build with the context's device builder for large meshes: the
  * scene is validated and built (BVH4, items) but not kept.  Same out5. */

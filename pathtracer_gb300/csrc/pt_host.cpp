@@ -221,6 +221,7 @@ struct Builder {
   int curve_base = 0;             // first curve primitive
   int threads = 0;               // mesh BVH build workers (0: hardware threads)
   bool gpu_bvh = false;          // large meshes built by the device builder
+  bool sah = false;              // SAH trees instead of the reference's
   cudaStream_t gpu_stream = nullptr;
   std::vector<int> obj_motion;   // per object: motion index + 1 (0: static)
   std::vector<BNode> nodes;
@@ -388,6 +389,202 @@ struct Builder {
     return root;
   }
 
+  // ------------------------------------------------------------ SAH trees
+  // Binned surface-area-heuristic build (16 bins per axis over the centroid
+  // box; cost 1 per node visit + 1 per item, leaves of up to 8 items).  Not
+  // the reference's tree: the hits are the same (a BVH only decides which
+  // boxes are visited), found with fewer visits where the median split of
+  // the reference is far from the cost optimum.
+  struct SahInput {
+    const float *lo[3], *hi[3], *c[3];  // per item: box and centroid
+  };
+  static constexpr int SAH_BINS = 16, SAH_LEAF_MAX = 8;
+
+  void sah_part(const SahInput &in, int *ids, int n, Part &out, int par_depth) const {
+    Box b = box_empty(), cb = box_empty();
+    for (int k = 0; k < n; ++k) {
+      const int i = ids[k];
+      for (int a = 0; a < 3; ++a) {
+        b.lo[a] = std::min(b.lo[a], in.lo[a][i]);
+        b.hi[a] = std::max(b.hi[a], in.hi[a][i]);
+        cb.lo[a] = std::min(cb.lo[a], in.c[a][i]);
+        cb.hi[a] = std::max(cb.hi[a], in.c[a][i]);
+      }
+    }
+    const int me = (int)out.nodes.size();
+    out.nodes.push_back(BNode());
+    for (int a = 0; a < 3; ++a) {
+      out.nodes[me].box.lo[a] = b.lo[a] - 1e-3f;
+      out.nodes[me].box.hi[a] = b.hi[a] + 1e-3f;
+    }
+    auto make_leaf = [&] {
+      out.nodes[me].first = (int)out.prims.size();
+      out.nodes[me].count = n;
+      for (int k = 0; k < n; ++k) out.prims.push_back(ids[k]);
+    };
+    if (n <= 2) return make_leaf();
+    // best split over the three axes' bin boundaries
+    float best = INFINITY;
+    int best_axis = -1, best_bin = -1;
+    for (int a = 0; a < 3; ++a) {
+      const float ext = cb.hi[a] - cb.lo[a];
+      if (!(ext > 0.f)) continue;
+      Box bb[SAH_BINS];
+      int cnt[SAH_BINS] = {0};
+      for (int k = 0; k < SAH_BINS; ++k) bb[k] = box_empty();
+      const float scale = SAH_BINS / ext;
+      for (int k = 0; k < n; ++k) {
+        const int i = ids[k];
+        const int bin = std::min(SAH_BINS - 1, (int)((in.c[a][i] - cb.lo[a]) * scale));
+        ++cnt[bin];
+        for (int q = 0; q < 3; ++q) {
+          bb[bin].lo[q] = std::min(bb[bin].lo[q], in.lo[q][i]);
+          bb[bin].hi[q] = std::max(bb[bin].hi[q], in.hi[q][i]);
+        }
+      }
+      float right_area[SAH_BINS];
+      int right_cnt[SAH_BINS];
+      Box acc = box_empty();
+      int ac = 0;
+      for (int k = SAH_BINS - 1; k > 0; --k) {
+        acc = box_merge(acc, bb[k]);
+        ac += cnt[k];
+        right_area[k] = box_area(acc);
+        right_cnt[k] = ac;
+      }
+      acc = box_empty();
+      ac = 0;
+      for (int k = 0; k < SAH_BINS - 1; ++k) {
+        acc = box_merge(acc, bb[k]);
+        ac += cnt[k];
+        if (ac == 0 || right_cnt[k + 1] == 0) continue;
+        const float cost = box_area(acc) * ac + right_area[k + 1] * right_cnt[k + 1];
+        if (cost < best) {
+          best = cost;
+          best_axis = a;
+          best_bin = k;
+        }
+      }
+    }
+    const float parent_area = std::max(box_area(b), 1e-30f);
+    const float split_cost = 1.f + best / parent_area;
+    if (best_axis < 0 || (n <= SAH_LEAF_MAX && split_cost >= (float)n)) {
+      if (n <= SAH_LEAF_MAX) return make_leaf();
+    }
+    int mid;
+    if (best_axis < 0) {  // all centroids equal: halves
+      mid = n / 2;
+    } else {
+      const float ext = cb.hi[best_axis] - cb.lo[best_axis], scale = SAH_BINS / ext;
+      int *p = std::partition(ids, ids + n, [&](int i) {
+        return std::min(SAH_BINS - 1, (int)((in.c[best_axis][i] - cb.lo[best_axis]) * scale)) <= best_bin;
+      });
+      mid = (int)(p - ids);
+      if (mid == 0 || mid == n) mid = n / 2;
+    }
+    if (par_depth > 0 && n > (1 << 15)) {
+      Part lp, rp;
+      std::thread th([&] { sah_part(in, ids, mid, lp, par_depth - 1); });
+      sah_part(in, ids + mid, n - mid, rp, par_depth - 1);
+      th.join();
+      splice(out, me, lp, rp);
+    } else {
+      const int l = (int)out.nodes.size();
+      sah_part(in, ids, mid, out, 0);
+      const int r = (int)out.nodes.size();
+      sah_part(in, ids + mid, n - mid, out, 0);
+      out.nodes[me].left = l;
+      out.nodes[me].right = r;
+    }
+  }
+
+  int build_mesh_sah(int mesh) {
+    const pt_mesh_desc &m = d->meshes[mesh];
+    const int n = m.n_triangles;
+    std::vector<float> arr(9 * (size_t)n);
+    SahInput in;
+    for (int a = 0; a < 3; ++a) {
+      in.lo[a] = arr.data() + (size_t)a * n;
+      in.hi[a] = arr.data() + (size_t)(3 + a) * n;
+      in.c[a] = arr.data() + (size_t)(6 + a) * n;
+    }
+    parallel_for((size_t)n, threads, [&](size_t t) {
+      const float *p0 = pos(mesh, m.indices[3 * t]), *p1 = pos(mesh, m.indices[3 * t + 1]),
+                  *p2 = pos(mesh, m.indices[3 * t + 2]);
+      for (int a = 0; a < 3; ++a) {
+        arr[(size_t)a * n + t] = std::min(std::min(p0[a], p1[a]), p2[a]);
+        arr[(size_t)(3 + a) * n + t] = std::max(std::max(p0[a], p1[a]), p2[a]);
+        arr[(size_t)(6 + a) * n + t] = ((p0[a] + p1[a]) + p2[a]) / 3.0f;
+      }
+    });
+    std::vector<int> ids(n);
+    std::iota(ids.begin(), ids.end(), 0);
+    unsigned hw = threads > 0 ? (unsigned)threads : std::max(1u, std::thread::hardware_concurrency());
+    int par_depth = 0;
+    while ((1u << par_depth) < hw && par_depth < 6) ++par_depth;
+    Part p;
+    sah_part(in, ids.data(), n, p, n > (1 << 16) ? par_depth : 0);
+    for (int &x : p.prims) x += tri_base[mesh];
+    return append_part(p);
+  }
+
+  // Top level over objects with the same heuristic (object boxes); its
+  // leaves are the objects' subtrees.
+  int sah_top(std::vector<int> objs) {
+    if (objs.size() == 1) return object_subtree(objs[0]);
+    Box cb = box_empty();
+    std::vector<Box> ob(objs.size());
+    for (size_t k = 0; k < objs.size(); ++k) {
+      ob[k] = object_box(objs[k]);
+      for (int a = 0; a < 3; ++a) {
+        const float c = 0.5f * (ob[k].lo[a] + ob[k].hi[a]);
+        cb.lo[a] = std::min(cb.lo[a], c);
+        cb.hi[a] = std::max(cb.hi[a], c);
+      }
+    }
+    // exact sweep over the sorted order of each axis (object counts are small)
+    float best = INFINITY;
+    int best_axis = -1, best_k = -1;
+    std::vector<int> order(objs.size());
+    const int n = (int)objs.size();
+    for (int a = 0; a < 3; ++a) {
+      std::iota(order.begin(), order.end(), 0);
+      std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
+        return ob[x].lo[a] + ob[x].hi[a] < ob[y].lo[a] + ob[y].hi[a];
+      });
+      std::vector<float> ra(n);
+      Box acc = box_empty();
+      for (int k = n - 1; k > 0; --k) {
+        acc = box_merge(acc, ob[order[k]]);
+        ra[k] = box_area(acc);
+      }
+      acc = box_empty();
+      for (int k = 0; k < n - 1; ++k) {
+        acc = box_merge(acc, ob[order[k]]);
+        const float cost = box_area(acc) * (k + 1) + ra[k + 1] * (n - k - 1);
+        if (cost < best) {
+          best = cost;
+          best_axis = a;
+          best_k = k;
+        }
+      }
+    }
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
+      return ob[x].lo[best_axis] + ob[x].hi[best_axis] < ob[y].lo[best_axis] + ob[y].hi[best_axis];
+    });
+    std::vector<int> lo_objs, hi_objs;
+    for (int k = 0; k < n; ++k) (k <= best_k ? lo_objs : hi_objs).push_back(objs[order[k]]);
+    const int l = sah_top(std::move(lo_objs));
+    const int r = sah_top(std::move(hi_objs));
+    const int me = (int)nodes.size();
+    nodes.push_back(BNode());
+    nodes[me].left = l;
+    nodes[me].right = r;
+    nodes[me].box = box_merge(nodes[l].box, nodes[r].box);
+    return me;
+  }
+
   // Appends a mesh tree (rooted at its index 0) to the scene's nodes.
   int append_part(Part &p) {
     Part top;
@@ -484,7 +681,12 @@ struct Builder {
       const pt_mesh_desc &m = d->meshes[od.index];
       std::vector<int> ids(m.n_triangles);
       std::iota(ids.begin(), ids.end(), 0);
-      me = gpu_bvh && m.n_triangles >= PT_GPU_BVH_MIN ? build_mesh_gpu(od.index) : build_mesh(od.index, ids);
+      if (sah && m.n_triangles > 4)
+        me = build_mesh_sah(od.index);
+      else if (gpu_bvh && m.n_triangles >= PT_GPU_BVH_MIN)
+        me = build_mesh_gpu(od.index);
+      else
+        me = build_mesh(od.index, ids);
     } else {
       me = (int)nodes.size();
       nodes.push_back(BNode());
@@ -751,7 +953,7 @@ static void box_faces(const pt_box_desc &b, std::vector<pt_quad_desc> &out) {
 }
 
 std::unique_ptr<Scene> build_scene(const pt_scene_desc *d_in, cudaStream_t st, bool device, int threads,
-                                   int trav_cap, bool gpu_bvh, bool want_hash) {
+                                   int trav_cap, int builder, bool want_hash) {
   if (!d_in) fail(PT_ERR_INVALID, "null scene description");
   // boxes become six rectangles each, after the scene's own rectangles
   pt_scene_desc aug = *d_in;
@@ -771,7 +973,8 @@ std::unique_ptr<Scene> build_scene(const pt_scene_desc *d_in, cudaStream_t st, b
   Builder B;
   B.d = d;
   B.threads = threads;
-  B.gpu_bvh = gpu_bvh;
+  B.gpu_bvh = builder == PT_BVH_BUILD_DEVICE;
+  B.sah = builder == PT_BVH_BUILD_SAH;
   B.gpu_stream = st;
   B.box_quad_base = n_user_quads;
   for (int m = 0; m < d->n_meshes; ++m) {
@@ -837,7 +1040,14 @@ std::unique_ptr<Scene> build_scene(const pt_scene_desc *d_in, cudaStream_t st, b
   if (!motion.empty() && !(d->shutter_max > 0.f) )
     fail(PT_ERR_INVALID, "moving objects need shutter_max > 0");
   std::srand(1);  // the reference's BVH build draws from rand() with its default seed
-  int root = B.build_top(0, d->n_objects);
+  int root;
+  if (B.sah) {
+    std::vector<int> all(d->n_objects);
+    std::iota(all.begin(), all.end(), 0);
+    root = B.sah_top(std::move(all));
+  } else {
+    root = B.build_top(0, d->n_objects);
+  }
 
   B.inst_motion.resize(B.nodes.size(), 0);
   Bvh4Out out;
@@ -1707,7 +1917,7 @@ int pt_scene_upload(void *ctx, const pt_scene_desc *desc, int32_t *scene_id) {
     c = as_ctx(ctx);
     if (!scene_id) fail(PT_ERR_INVALID, "null scene_id");
     cuda_check(cudaSetDevice(c->device), "cudaSetDevice");
-    auto S = build_scene(desc, c->stream, true, 0, c->trav_cap, c->bvh_builder == PT_BVH_BUILD_DEVICE);
+    auto S = build_scene(desc, c->stream, true, 0, c->trav_cap, c->bvh_builder);
     int id = c->next_scene++;
     c->scenes[id] = std::move(S);
     *scene_id = id;
@@ -1741,7 +1951,22 @@ int pt_bvh_build(const pt_scene_desc *desc, int32_t threads, int64_t *out5) {
   PT_GUARD(nullptr, {
     if (!out5) fail(PT_ERR_INVALID, "null output");
     auto t0 = std::chrono::steady_clock::now();
-    auto S = build_scene(desc, nullptr, false, threads, 0, false, true);
+    auto S = build_scene(desc, nullptr, false, threads, 0, PT_BVH_BUILD_HOST, true);
+    auto t1 = std::chrono::steady_clock::now();
+    out5[0] = S->n_nodes;
+    out5[1] = S->n_items;
+    out5[2] = S->bvh_depth;
+    uint64_t h = S->bvh_hash;
+    std::memcpy(&out5[3], &h, sizeof h);
+    out5[4] = (int64_t)std::chrono::duration_cast<std::chrono::microseconds>(t1 - t0).count();
+  });
+}
+
+int pt_bvh_build_sah(const pt_scene_desc *desc, int32_t threads, int64_t *out5) {
+  PT_GUARD(nullptr, {
+    if (!out5) fail(PT_ERR_INVALID, "null output");
+    auto t0 = std::chrono::steady_clock::now();
+    auto S = build_scene(desc, nullptr, false, threads, 0, PT_BVH_BUILD_SAH, true);
     auto t1 = std::chrono::steady_clock::now();
     out5[0] = S->n_nodes;
     out5[1] = S->n_items;
@@ -1756,7 +1981,8 @@ int pt_set_bvh_builder(void *ctx, int32_t builder) {
   Context *c = static_cast<Context *>(ctx);
   PT_GUARD(c, {
     c = as_ctx(ctx);
-    if (builder != PT_BVH_BUILD_HOST && builder != PT_BVH_BUILD_DEVICE) fail(PT_ERR_INVALID, "unknown BVH builder");
+    if (builder != PT_BVH_BUILD_HOST && builder != PT_BVH_BUILD_DEVICE && builder != PT_BVH_BUILD_SAH)
+      fail(PT_ERR_INVALID, "unknown BVH builder");
     c->bvh_builder = builder;
   });
 }
@@ -1768,7 +1994,7 @@ int pt_bvh_build_device(void *ctx, const pt_scene_desc *desc, int64_t *out5) {
     if (!out5) fail(PT_ERR_INVALID, "null output");
     cuda_check(cudaSetDevice(c->device), "cudaSetDevice");
     auto t0 = std::chrono::steady_clock::now();
-    auto S = build_scene(desc, c->stream, false, 0, 0, true, true);
+    auto S = build_scene(desc, c->stream, false, 0, 0, PT_BVH_BUILD_DEVICE, true);
     auto t1 = std::chrono::steady_clock::now();
     out5[0] = S->n_nodes;
     out5[1] = S->n_items;

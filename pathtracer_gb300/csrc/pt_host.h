@@ -54,10 +54,11 @@ struct Scene {
   ~Scene();
 };
 
-// gpu_bvh: meshes of at least PT_GPU_BVH_MIN triangles get their BVH from
-// the device builder (on st's device) instead of the host recursion.
+// builder: PT_BVH_BUILD_HOST (the reference's trees), PT_BVH_BUILD_DEVICE
+// (meshes of at least PT_GPU_BVH_MIN triangles built on st's device with the
+// same rule), PT_BVH_BUILD_SAH (binned-SAH trees on the host).
 std::unique_ptr<Scene> build_scene(const pt_scene_desc *d, cudaStream_t st, bool device, int threads,
-                                   int trav_cap, bool gpu_bvh = false, bool want_hash = false);
+                                   int trav_cap, int builder = PT_BVH_BUILD_HOST, bool want_hash = false);
 constexpr int PT_GPU_BVH_MIN = 1 << 14;
 
 // Device buffers of one merged group of a batch (the jobs of one scene with

@@ -170,6 +170,7 @@ __global__ void k_sort_scatter(Queues Q, int qsel) {
 // k_trace_closest.  Each ray's visibility goes to Q.sh_vis; k_shadow_resolve
 // then adds the visible terms of every vertex to its path in a fixed order,
 // so the result does not depend on which warp traced which ray.
+template <bool CURVES>
 __global__ void __launch_bounds__(128) k_trace_shadow(SceneView S, Queues Q, int LN) {
   __shared__ int32_t stack[PT_STACK * 128];
   const int n = Q.counts[2] * LN;
@@ -209,7 +210,7 @@ __global__ void __launch_bounds__(128) k_trace_shadow(SceneView S, Queues Q, int
       if (exhausted) break;
       continue;
     }
-    if (active && trav_step<true>(S, R, my_stack, blockDim.x, Q.err)) {
+    if (active && trav_step<true, CURVES>(S, R, my_stack, blockDim.x, Q.err)) {
       Q.sh_vis[slot] = R.found ? 0 : 1;
       active = false;
     }
@@ -406,7 +407,10 @@ void launch_sort(const SceneView &S, const Queues &Q, int qsel, const LaunchCfg 
 }
 
 void launch_shadow(const SceneView &S, const Queues &Q, int LN, const LaunchCfg &cfg, cudaStream_t st) {
-  k_trace_shadow<<<cfg.trace_blocks, 128, 0, st>>>(S, Q, LN);
+  if (S.curves)
+    k_trace_shadow<true><<<cfg.trace_blocks, 128, 0, st>>>(S, Q, LN);
+  else
+    k_trace_shadow<false><<<cfg.trace_blocks, 128, 0, st>>>(S, Q, LN);
   k_shadow_resolve<<<cfg.max_blocks_simple, 256, 0, st>>>(Q, LN);
 }
 
@@ -445,7 +449,7 @@ void kernel_attributes(KernelInfo *info) {
   info->trace_blocks_per_sm = nb;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_shade<-1, false>, 128, 0);
   info->shade_blocks_per_sm = nb;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_trace_shadow, 128, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_trace_shadow<false>, 128, 0);
   info->shadow_blocks_per_sm = nb;
 }
 

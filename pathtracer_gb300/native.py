@@ -27,12 +27,12 @@ OBJ_MESH, OBJ_QUAD, OBJ_SPHERE, OBJ_BOX, OBJ_CURVE = 0, 1, 2, 3, 4
 EST_REF_NEE, EST_NEE_MIS = 0, 1
 SAMPLER_HALTON_NONE, SAMPLER_HALTON_PERMUTE, SAMPLER_HALTON_OWEN, SAMPLER_STRATIFIED = range(4)
 ENV_UNIFORM, ENV_ALIAS = 0, 1
-BVH_BUILD_HOST, BVH_BUILD_DEVICE = 0, 1
+BVH_BUILD_HOST, BVH_BUILD_DEVICE, BVH_BUILD_SAH = 0, 1, 2
 
 # exported symbols of the C-ABI, in header order
 EXPORTS = [
     "pt_create", "pt_destroy", "pt_last_error", "pt_version", "pt_scene_upload", "pt_scene_release",
-    "pt_bvh_build", "pt_set_bvh_builder", "pt_bvh_build_device", "pt_obj_load", "pt_obj_free", "pt_load_image", "pt_free_image", "pt_scene_info", "pt_render", "pt_render_device", "pt_render_device_noalloc",
+    "pt_bvh_build", "pt_set_bvh_builder", "pt_bvh_build_device", "pt_bvh_build_sah", "pt_obj_load", "pt_obj_free", "pt_load_image", "pt_free_image", "pt_scene_info", "pt_render", "pt_render_device", "pt_render_device_noalloc",
     "pt_profile_begin",
     "pt_profile_end", "pt_tonemap", "pt_gaussian_blur", "pt_write_png", "pt_sampler_eval", "pt_trace_closest",
     "pt_trace_any", "pt_bsdf_eval", "pt_bsdf_sample", "pt_render_batch", "pt_autotune", "pt_server_create",
@@ -168,6 +168,7 @@ def load() -> C.CDLL:
         "pt_scene_release": [vp, C.c_int32],
         "pt_bvh_build": [C.POINTER(SceneDesc), C.c_int32, C.POINTER(C.c_int64)],
         "pt_set_bvh_builder": [C.c_void_p, C.c_int32],
+        "pt_bvh_build_sah": [C.POINTER(SceneDesc), C.c_int32, C.POINTER(C.c_int64)],
         "pt_bvh_build_device": [C.c_void_p, C.POINTER(SceneDesc), C.POINTER(C.c_int64)],
         "pt_obj_load": [C.c_char_p, C.POINTER(MeshDesc)],
         "pt_obj_free": [C.POINTER(MeshDesc)],
@@ -563,12 +564,13 @@ def write_png(path, rgb8: np.ndarray) -> None:
         raise PtError(rc, buf.value.decode())
 
 
-def bvh_build(scene, threads: int = 0) -> dict:
-    """pt_bvh_build: the scene's BVH4 built on the host only (no GPU)."""
+def bvh_build(scene, threads: int = 0, sah: bool = False) -> dict:
+    """pt_bvh_build (the reference's trees) or pt_bvh_build_sah: the scene's
+    BVH4 built on the host only (no GPU)."""
     lib = load()
     sb = make_scene_desc(scene)
     out = (C.c_int64 * 5)()
-    rc = lib.pt_bvh_build(C.byref(sb.desc), threads, out)
+    rc = (lib.pt_bvh_build_sah if sah else lib.pt_bvh_build)(C.byref(sb.desc), threads, out)
     if rc != PT_OK:
         buf = C.create_string_buffer(512)
         lib.pt_last_error(None, buf, 512)
