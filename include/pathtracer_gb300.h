@@ -320,13 +320,16 @@ int pt_scene_release(void *ctx, int32_t scene_id);
  * build time in microseconds.  Errors: pt_last_error(NULL, ...). */
 int pt_bvh_build(const pt_scene_desc *desc, int32_t threads, int64_t *out5);
 
-/* Mesh BVH builder of a context's later pt_scene_upload calls (no reference
- * counterpart: the reference builds on the host).  PT_BVH_BUILD_HOST
- * (default) is the reference's recursion (MeshBVHNode, meshBVH.cpp:6-55) on
- * host threads; PT_BVH_BUILD_DEVICE builds meshes of >= 16384 triangles on
- * the GPU with the same split rule, level by level: the same tree whenever
- * no two centroids of a node tie along its split axis (ties: by triangle
- * index), i.e. the same hits, found faster for large meshes. */
+/* BVH builder of a context's later pt_scene_upload calls (the reference
+ * builds one way only, on the host).  A BVH decides which boxes a ray visits,
+ * not what it hits: every builder gives the same closest hits up to exact
+ * ties in t.  PT_BVH_BUILD_SAH (default): binned-SAH trees, fewest node
+ * visits.  PT_BVH_BUILD_HOST: the reference's own trees (MeshBVHNode,
+ * meshBVH.cpp:6-55; BVHNode, bvh.hpp:46-102) on host threads.
+ * PT_BVH_BUILD_DEVICE: meshes of >= 16384 triangles built on the GPU with the
+ * reference's split rule, level by level -- the reference's tree whenever no
+ * two centroids of a node tie along its split axis (ties: by triangle
+ * index); the fastest upload of large meshes. */
 #define PT_BVH_BUILD_HOST 0
 #define PT_BVH_BUILD_DEVICE 1
 /* Binned-SAH trees (meshes and the object level) on host threads: not the

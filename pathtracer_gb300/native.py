@@ -409,8 +409,10 @@ class Renderer:
         self._check(self.lib.pt_scene_release(self.ctx, sid))
 
     def set_bvh_builder(self, builder: int):
-        """BVH_BUILD_HOST (the reference's recursion, default) or
-        BVH_BUILD_DEVICE (large meshes built on the GPU) for later uploads."""
+        """BVH_BUILD_SAH (binned-SAH trees, default), BVH_BUILD_HOST (the
+        reference's trees) or BVH_BUILD_DEVICE (the reference's split rule,
+        large meshes built on the GPU) for later uploads; all give the same
+        hits up to exact ties in t."""
         self._check(self.lib.pt_set_bvh_builder(self.ctx, int(builder)))
 
     def bvh_build_device(self, scene) -> dict:

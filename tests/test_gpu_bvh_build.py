@@ -1,9 +1,10 @@
-"""The device BVH builder (pt_set_bvh_builder / pt_bvh_build_device): the
-reference's median-split tree built level by level on the GPU.  Where no
-two centroids of a node tie along its split axis it is the host recursion's
-tree node for node (equal content hash); with ties it is another valid tree
-of the same split rule (same closest hits).  Renders through it equal the
-host-built scene's."""
+"""BVH builders (pt_set_bvh_builder).  The device builder
+(pt_bvh_build_device) builds the reference's median-split tree level by
+level on the GPU: where no two centroids of a node tie along its split axis
+it is the host recursion's tree node for node (equal content hash); with
+ties it is another valid tree of the same split rule.  The SAH builder (the
+default) builds other trees.  Every builder finds the same closest hits and
+renders the same images as the reference's tree."""
 from __future__ import annotations
 
 import numpy as np
@@ -13,6 +14,15 @@ from pathtracer_gb300 import native as N
 from pathtracer_gb300 import scene as S
 
 pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ref_tree():
+    """A context that uploads with the reference's trees."""
+    r = N.Renderer(0)
+    r.set_bvh_builder(N.BVH_BUILD_HOST)
+    yield r
+    r.close()
 
 
 def _soup(n, seed):
@@ -50,7 +60,8 @@ def test_device_tree_on_a_displaced_sphere(renderer):
     assert abs(dev["depth"] - host["depth"]) <= 1
 
 
-def test_device_tree_with_ties_traces_like_host_tree(renderer):
+def test_device_tree_with_ties_traces_like_host_tree(ref_tree):
+    renderer = ref_tree
     # an undisplaced icosphere: symmetric triangles share centroid coordinates
     sc, cam = S.cornell_icosphere(7)
     r_dev = N.Renderer(0)
@@ -76,7 +87,8 @@ def test_device_tree_with_ties_traces_like_host_tree(renderer):
         r_dev.close()
 
 
-def test_device_built_scene_renders_identically(renderer):
+def test_device_built_scene_renders_identically(ref_tree):
+    renderer = ref_tree
     sc = _soup_scene(60000, seed=4)
     cam = S.camera((0.0, 0.0, -3.5), (0.0, 0.0, 1.0), 45.0, 1.0)
     r_dev = N.Renderer(0)
@@ -94,3 +106,33 @@ def test_device_built_scene_renders_identically(renderer):
 def test_builder_selection_is_validated(renderer):
     with pytest.raises(N.PtError):
         renderer.set_bvh_builder(7)
+
+
+def test_sah_trees_find_the_same_hits(ref_tree):
+    renderer = ref_tree
+    """PT_BVH_BUILD_SAH: another tree over the same primitives (meshes and
+    the object level): the same closest hits and the same image."""
+    sc, cam = S.material_divergence(3)
+    r_sah = N.Renderer(0)
+    r_sah.set_bvh_builder(N.BVH_BUILD_SAH)
+    try:
+        s_ref, s_sah = renderer.upload(sc), r_sah.upload(sc)
+        rng = np.random.default_rng(5)
+        n = 1 << 15
+        o = np.tile(cam["position"], (n, 1)) + rng.normal(0, 0.05, (n, 3))
+        d = rng.normal(0, 1, (n, 3)) * [0.4, 0.3, 0.0] + np.asarray(cam["front"])
+        rays = np.concatenate([o, d / np.linalg.norm(d, axis=1, keepdims=True)], 1).astype(np.float32)
+        t_r, p_r, _ = renderer.trace_closest(s_ref, rays)
+        t_s, p_s, _ = r_sah.trace_closest(s_sah, rays)
+        assert (p_r == p_s).mean() > 0.9999
+        same = p_r == p_s
+        assert np.array_equal(t_r[same], t_s[same])
+        job_r = N.job_desc(s_ref, cam, 64, 36, 4, 2, 8, seed=4, estimator=N.EST_NEE_MIS,
+                           sampler=N.SAMPLER_STRATIFIED)
+        job_s = N.job_desc(s_sah, cam, 64, 36, 4, 2, 8, seed=4, estimator=N.EST_NEE_MIS,
+                           sampler=N.SAMPLER_STRATIFIED)
+        f_r, f_s = renderer.render(job_r), r_sah.render(job_s)
+        assert (f_r == f_s).mean() > 0.999
+        renderer.release(s_ref)
+    finally:
+        r_sah.close()
