@@ -46,7 +46,7 @@ FALLBACK_HBM_GBS = 6800.0
 # default workload at 16 spp per step, from one single-pass ncu capture of
 # the 17 launches of a timed step (profiles/ncu_traffic_rough_glass_1024_16spp.md);
 # scaled by the paths per step for other step sizes.
-NCU_TRAFFIC_PER_LAUNCH_16SPP = {"shadow": 3.630e9 / 17, "trace": 3.376e9 / 17}
+NCU_TRAFFIC_PER_LAUNCH_16SPP = {"shadow": 4.146e9 / 17, "trace": 3.561e9 / 17}
 
 
 def parse():
