@@ -985,16 +985,27 @@ std::unique_ptr<Scene> build_scene(const pt_scene_desc *d_in, cudaStream_t st, b
     for (int t = 0; t < 3 * md.n_triangles; ++t)
       if (md.indices[t] < 0 || md.indices[t] >= md.n_positions)
         fail(PT_ERR_INVALID, "mesh index out of range");
+    for (int v = 0; v < 3 * md.n_positions; ++v)
+      if (!std::isfinite(md.positions[v])) fail(PT_ERR_INVALID, "mesh position not finite");
     B.tri_base.push_back(B.n_tris);
     B.n_tris += md.n_triangles;
   }
-  for (int q = 0; q < d->n_quads; ++q)
-    if (d->quads[q].material < 0 || d->quads[q].material >= d->n_materials || d->quads[q].axis < 0 ||
-        d->quads[q].axis > 2)
+  auto finite = [](std::initializer_list<float> xs) {
+    for (float x : xs)
+      if (!std::isfinite(x)) return false;
+    return true;
+  };
+  for (int q = 0; q < d->n_quads; ++q) {
+    const pt_quad_desc &Q = d->quads[q];
+    if (Q.material < 0 || Q.material >= d->n_materials || Q.axis < 0 || Q.axis > 2 ||
+        !finite({Q.k, Q.d0_min, Q.d0_max, Q.d1_min, Q.d1_max}))
       fail(PT_ERR_INVALID, "bad quad");
-  for (int s = 0; s < d->n_spheres; ++s)
-    if (d->spheres[s].material < 0 || d->spheres[s].material >= d->n_materials)
+  }
+  for (int s = 0; s < d->n_spheres; ++s) {
+    const pt_sphere_desc &P = d->spheres[s];
+    if (P.material < 0 || P.material >= d->n_materials || !finite({P.center[0], P.center[1], P.center[2], P.radius}))
       fail(PT_ERR_INVALID, "bad sphere");
+  }
   const int n_curves = d->curves ? d->n_curves : 0;
   if (n_curves < 0) fail(PT_ERR_INVALID, "negative curve count");
   for (int o = 0; o < d->n_objects; ++o) {
@@ -1007,8 +1018,12 @@ std::unique_ptr<Scene> build_scene(const pt_scene_desc *d_in, cudaStream_t st, b
     if (od.kind < 0 || od.kind > 4 || od.index < 0 || od.index >= lim)
       fail(PT_ERR_INVALID, "bad object entry");
   }
-  for (int c = 0; c < n_curves; ++c)
-    if (d->curves[c].material < 0 || d->curves[c].material >= d->n_materials) fail(PT_ERR_INVALID, "bad curve");
+  for (int c = 0; c < n_curves; ++c) {
+    const pt_curve_desc &K = d->curves[c];
+    bool ok = K.material >= 0 && K.material < d->n_materials && finite({K.width0, K.width1});
+    for (int k = 0; k < 4; ++k) ok = ok && finite({K.cps[k][0], K.cps[k][1], K.cps[k][2]});
+    if (!ok) fail(PT_ERR_INVALID, "bad curve");
+  }
   const int curve_base = B.n_tris + d->n_quads + d->n_spheres;  // first curve primitive
   B.curve_base = curve_base;
   const int n_prims = curve_base + n_curves;

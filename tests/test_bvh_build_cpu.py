@@ -2,6 +2,7 @@
 tree the sequential recursion gives, and invalid scenes fail loudly."""
 from __future__ import annotations
 
+import numpy as np
 import pytest
 
 from pathtracer_gb300 import native as N
@@ -36,3 +37,29 @@ def test_invalid_scene_fails():
     empty = S.Scene()
     with pytest.raises(N.PtError):
         N.bvh_build(empty)
+
+
+def test_non_finite_geometry_is_rejected():
+    """NaN / inf positions, centres, radii or rectangle bounds are refused at
+    build time (every builder bins or sorts by them)."""
+    import pytest
+    sc, _ = S.cornell_icosphere(1)
+    pos = sc.meshes[0].positions.copy()
+    pos[3, 1] = np.nan
+    bad = S.Scene(materials=sc.materials, meshes=[S.Mesh(pos, sc.meshes[0].indices, None, sc.meshes[0].material)],
+                  quads=sc.quads, spheres=sc.spheres, objects=sc.objects)
+    for sah in (False, True):
+        with pytest.raises(N.PtError):
+            N.bvh_build(bad, sah=sah)
+    sc2, _ = S.cornell_icosphere(1)
+    sc2.add_sphere((0.5, np.inf, 0.5), 0.1, 0)
+    with pytest.raises(N.PtError):
+        N.bvh_build(sc2)
+
+
+def test_sah_tree_holds_every_item_once():
+    """The SAH builder places every primitive in exactly one leaf."""
+    sc, _ = S.material_divergence(2)
+    ref, sah = N.bvh_build(sc), N.bvh_build(sc, sah=True)
+    assert sah["items"] == ref["items"]
+    assert sah["depth"] <= 15
