@@ -46,7 +46,7 @@ FALLBACK_HBM_GBS = 6800.0
 # default workload at 16 spp per step, from one single-pass ncu capture of
 # the 17 launches of a timed step (profiles/ncu_traffic_rough_glass_1024_16spp.md);
 # scaled by the paths per step for other step sizes.
-NCU_TRAFFIC_PER_LAUNCH_16SPP = {"shadow": 4.146e9 / 17, "trace": 3.561e9 / 17}
+NCU_TRAFFIC_PER_LAUNCH_16SPP = {"shadow": 3.630e9 / 17, "trace": 3.376e9 / 17}
 
 
 def parse():
@@ -221,7 +221,7 @@ def form_scenes(r, with_big: bool):
         t1 = time.perf_counter()
         big = (r.upload(sc), cam, 4.24)
         upload_s["device_builder"] = round(time.perf_counter() - t1, 3)
-        r.set_bvh_builder(N.BVH_BUILD_SAH)
+        r.set_bvh_builder(N.BVH_BUILD_HOST)
     return out, big, time.perf_counter() - t0, upload_s
 
 
@@ -433,9 +433,10 @@ def run_ours(args, rank, world, local_rank):
     spp_total = wl["sx"] * wl["sy"]
     k = args.spp_per_step
 
-    def job_for(step):
+    def job_for(step, scene_id=None):
         chunk = sample_chunk(step, rank, world, max(1, spp_total // k))
-        return N.job_desc(sid, cam, W, H, wl["sx"], wl["sy"], wl["depth"], rr_start=wl["rr"],
+        return N.job_desc(sid if scene_id is None else scene_id, cam, W, H, wl["sx"], wl["sy"], wl["depth"],
+                          rr_start=wl["rr"],
                           estimator=wl["est"], sampler=wl["sampler"], env_sampling=wl["env"], seed=1,
                           spp_begin=chunk * k, spp_end=chunk * k + k)
 
@@ -535,7 +536,7 @@ def run_ours(args, rank, world, local_rank):
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene generator, no assets)",
         "config": {"workload": wl["desc"], "step": f"{k} spp x {W}x{H} px = {W * H * k} paths",
                    "estimator": "NEE+MIS", "triangles": info["triangles"], "bvh4_nodes": info["bvh4_nodes"],
-                   "bvh": "binned-SAH BVH4 (the library default; same hits as the reference's median-split tree)",
+                   "bvh": "BVH4 collapsed from the reference's own trees (the library default)",
                    "l2": "inputs larger than L2: BVH + leaves "
                          f"{info['device_bytes'] / 1e6:.0f} MB and ~{tot['bytes'] / args.steps / 1e9:.1f} GB of "
                          "queue traffic per step (L2 129 MB)",
@@ -558,6 +559,22 @@ def run_ours(args, rank, world, local_rank):
     }
     if world == 1 and not args.no_rmse:
         line["rmse"] = converged_rmse(r, sid, cam, wl, k)
+    if world == 1 and not args.no_forms:
+        # the same steps through the opt-in SAH trees (same hits, other tree)
+        r.set_bvh_builder(N.BVH_BUILD_SAH)
+        sid_sah = r.upload(sc)
+        r.set_bvh_builder(N.BVH_BUILD_HOST)
+        for i in range(args.warmup):
+            r.render_device(job_for(i, sid_sah), film.data_ptr(), sync=True)
+        t_sah, p_sah = 0.0, 0
+        for i in range(args.steps):
+            st = r.render_device(job_for(args.warmup + i, sid_sah), film.data_ptr(), sync=False, stats=True)
+            t_sah += st.ms
+            p_sah += st.paths
+        r.release(sid_sah)
+        line["bvh_variants"] = {"reference_tree": value, "sah_tree": p_sah / (t_sah / 1e3),
+                                "unit": "paths/s",
+                                "note": "PT_BVH_BUILD_SAH: binned-SAH BVH4, same steps and samples, device time"}
     if world == 1 and not args.no_forms:
         fs, big, build_s, upload_s = form_scenes(r, with_big=True)
         forms = {"scene_build_s": build_s,

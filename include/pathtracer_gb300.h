@@ -323,13 +323,13 @@ int pt_bvh_build(const pt_scene_desc *desc, int32_t threads, int64_t *out5);
 /* BVH builder of a context's later pt_scene_upload calls (the reference
  * builds one way only, on the host).  A BVH decides which boxes a ray visits,
  * not what it hits: every builder gives the same closest hits up to exact
- * ties in t.  PT_BVH_BUILD_SAH (default): binned-SAH trees, fewest node
- * visits.  PT_BVH_BUILD_HOST: the reference's own trees (MeshBVHNode,
- * meshBVH.cpp:6-55; BVHNode, bvh.hpp:46-102) on host threads.
+ * ties in t.  PT_BVH_BUILD_HOST (default): the reference's own trees
+ * (MeshBVHNode, meshBVH.cpp:6-55; BVHNode, bvh.hpp:46-102) on host threads.
  * PT_BVH_BUILD_DEVICE: meshes of >= 16384 triangles built on the GPU with the
  * reference's split rule, level by level -- the reference's tree whenever no
  * two centroids of a node tie along its split axis (ties: by triangle
- * index); the fastest upload of large meshes. */
+ * index); the fastest upload of large meshes.  PT_BVH_BUILD_SAH: binned-SAH
+ * trees instead of the reference's, fewer node visits per ray. */
 #define PT_BVH_BUILD_HOST 0
 #define PT_BVH_BUILD_DEVICE 1
 /* Binned-SAH trees (meshes and the object level) on host threads: not the

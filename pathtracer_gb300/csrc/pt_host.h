@@ -103,7 +103,7 @@ struct Context {
   LaunchCfg cfg;
   int wave_cap = 1 << 22;
   int trav_cap = 0;  // 0: PT_TRAVERSAL_CAP
-  int bvh_builder = PT_BVH_BUILD_SAH;
+  int bvh_builder = PT_BVH_BUILD_HOST;
   std::string last_error;
   std::map<int, std::unique_ptr<Scene>> scenes;
   int next_scene = 1;

@@ -409,9 +409,9 @@ class Renderer:
         self._check(self.lib.pt_scene_release(self.ctx, sid))
 
     def set_bvh_builder(self, builder: int):
-        """BVH_BUILD_SAH (binned-SAH trees, default), BVH_BUILD_HOST (the
-        reference's trees) or BVH_BUILD_DEVICE (the reference's split rule,
-        large meshes built on the GPU) for later uploads; all give the same
+        """BVH_BUILD_HOST (the reference's trees, default), BVH_BUILD_DEVICE
+        (the reference's split rule, large meshes built on the GPU) or
+        BVH_BUILD_SAH (binned-SAH trees) for later uploads; all give the same
         hits up to exact ties in t."""
         self._check(self.lib.pt_set_bvh_builder(self.ctx, int(builder)))
 
