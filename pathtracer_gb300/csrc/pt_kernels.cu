@@ -38,7 +38,7 @@ __global__ void __launch_bounds__(128) k_trace_test(SceneView S, const float *ra
                                                     int n, float tmin, float tmax, float *t_out,
                                                     int *prim_out, float *uv_out, uint8_t *occ,
                                                     int *err) {
-  __shared__ int32_t stack[PT_STACK_SMEM * 128];
+  __shared__ int32_t stack[PT_STACK * 128];
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     V3 o = v3(rays[6 * i], rays[6 * i + 1], rays[6 * i + 2]);
     V3 d = v3(rays[6 * i + 3], rays[6 * i + 4], rays[6 * i + 5]);
@@ -172,12 +172,11 @@ __global__ void k_sort_scatter(Queues Q, int qsel) {
 // so the result does not depend on which warp traced which ray.
 template <bool CURVES>
 __global__ void __launch_bounds__(128) k_trace_shadow(SceneView S, Queues Q, int LN) {
-  __shared__ int32_t stack[PT_STACK_SMEM * 128];
+  __shared__ int32_t stack[PT_STACK * 128];
   const int n = Q.counts[2] * LN;
   int *fetch = Q.counts + 3;
   const int lane = threadIdx.x & 31;
-  int32_t ovf[PT_STACK - PT_STACK_SMEM];  // deep stack entries (local memory)
-  const TStack TS{stack + threadIdx.x, (int)blockDim.x, ovf};
+  int32_t *my_stack = stack + threadIdx.x;
   TravRay R;
   bool active = false, exhausted = false;
   size_t slot = 0;
@@ -211,7 +210,7 @@ __global__ void __launch_bounds__(128) k_trace_shadow(SceneView S, Queues Q, int
       if (exhausted) break;
       continue;
     }
-    if (active && trav_step<true, CURVES>(S, R, TS, Q.err)) {
+    if (active && trav_step<true, CURVES>(S, R, my_stack, blockDim.x, Q.err)) {
       Q.sh_vis[slot] = R.found ? 0 : 1;
       active = false;
     }

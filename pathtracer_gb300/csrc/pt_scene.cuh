@@ -15,13 +15,6 @@
 
 // Entries of the per-thread traversal stack (shared memory).  A BVH4 of
 // depth D needs at most 3 * D + 1 entries; scene upload rejects deeper trees.
-// Traversal stack: PT_STACK entries per ray, the first PT_STACK_SMEM in
-// shared memory ([entry][thread] in the block's array), the rest -- used
-// only by unusually deep descents -- in the thread's local memory.  Fewer
-// shared-memory entries leave more of the SM's L1 for BVH nodes.
-#ifndef PT_STACK_SMEM
-#define PT_STACK_SMEM 32
-#endif
 #ifndef PT_STACK
 #define PT_STACK 48
 #endif

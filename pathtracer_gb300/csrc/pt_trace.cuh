@@ -249,14 +249,6 @@ struct TravRay {
   HitRec hit;
 };
 
-// A ray's traversal stack: entries [0, PT_STACK_SMEM) at s[entry * stride]
-// (shared memory), the rest in ovf (the thread's local memory).
-struct TStack {
-  int32_t *s;
-  int stride;
-  int32_t *ovf;
-};
-
 // The stack is empty: the ray is finished once no leaf is pending.
 #define PT_REF_EMPTY ((int32_t)0x80000001)
 
@@ -282,17 +274,8 @@ __device__ __forceinline__ void trav_init(TravRay &R, V3 o, V3 d, float tmin, fl
   R.hit.u = R.hit.v = 0.f;
 }
 
-__device__ __forceinline__ void stack_put(const TStack &T, int at, int32_t v) {
-  if (at < PT_STACK_SMEM)
-    T.s[at * T.stride] = v;
-  else
-    T.ovf[at - PT_STACK_SMEM] = v;
-}
-
-__device__ __forceinline__ int32_t trav_pop(TravRay &R, const TStack &T) {
-  if (R.sp == 0) return PT_REF_EMPTY;
-  --R.sp;
-  return R.sp < PT_STACK_SMEM ? T.s[R.sp * T.stride] : T.ovf[R.sp - PT_STACK_SMEM];
+__device__ __forceinline__ int32_t trav_pop(TravRay &R, const int32_t *stack, int stride) {
+  return R.sp == 0 ? PT_REF_EMPTY : stack[(--R.sp) * stride];
 }
 
 // One node visit (or frame change).  R.ref must satisfy ref_is_node; after it
@@ -301,12 +284,12 @@ __device__ __forceinline__ int32_t trav_pop(TravRay &R, const TStack &T) {
 // `stack` points at this thread's column of a shared array laid out
 // [PT_STACK][stride].  Returns false on a stack overflow (error flag set).
 template <bool ANY>
-__device__ __forceinline__ bool trav_node(const SceneView &S, TravRay &R, const TStack &T, int *err) {
+__device__ __forceinline__ bool trav_node(const SceneView &S, TravRay &R, int32_t *stack, int stride, int *err) {
   if (R.ref == PT_FRAME_END) {
     // leaving a moving object's subtree: back to the world frame
     R.o = R.ow;
     R.oi = v3(-R.o.x * R.inv.x, -R.o.y * R.inv.y, -R.o.z * R.inv.z);
-    R.ref = trav_pop(R, T);
+    R.ref = trav_pop(R, stack, stride);
     return true;
   }
   if (R.ref & PT_INST_BIT) {
@@ -317,7 +300,7 @@ __device__ __forceinline__ bool trav_node(const SceneView &S, TravRay &R, const 
       *err = 1;
       return false;
     }
-    stack_put(T, R.sp++, PT_FRAME_END);
+    stack[(R.sp++) * stride] = PT_FRAME_END;
     R.o = moved_origin(S, (uint32_t)__ldg(S.node_motion + R.ref), R.ow, R.time);
     R.oi = v3(-R.o.x * R.inv.x, -R.o.y * R.inv.y, -R.o.z * R.inv.z);
   }
@@ -370,7 +353,7 @@ __device__ __forceinline__ bool trav_node(const SceneView &S, TravRay &R, const 
   }
   const int nh = (d0 < INFINITY) + (d1 < INFINITY) + (d2 < INFINITY) + (d3 < INFINITY);
   if (nh == 0) {
-    R.ref = trav_pop(R, T);
+    R.ref = trav_pop(R, stack, stride);
     return true;
   }
   if (R.sp + nh - 1 > PT_STACK) {
@@ -384,13 +367,13 @@ __device__ __forceinline__ bool trav_node(const SceneView &S, TravRay &R, const 
     // node order: descend into the first hit child, push the others
     bool have = false;
     if (d3 < INFINITY) { first = r3; have = true; }
-    if (d2 < INFINITY) { if (have) stack_put(T, sp++, first); first = r2; have = true; }
-    if (d1 < INFINITY) { if (have) stack_put(T, sp++, first); first = r1; have = true; }
-    if (d0 < INFINITY) { if (have) stack_put(T, sp++, first); first = r0; have = true; }
+    if (d2 < INFINITY) { if (have) stack[(sp++) * stride] = first; first = r2; have = true; }
+    if (d1 < INFINITY) { if (have) stack[(sp++) * stride] = first; first = r1; have = true; }
+    if (d0 < INFINITY) { if (have) stack[(sp++) * stride] = first; first = r0; have = true; }
   } else {
-    if (d3 < INFINITY) stack_put(T, sp++, r3);
-    if (d2 < INFINITY) stack_put(T, sp++, r2);
-    if (d1 < INFINITY) stack_put(T, sp++, r1);
+    if (d3 < INFINITY) stack[(sp++) * stride] = r3;
+    if (d2 < INFINITY) stack[(sp++) * stride] = r2;
+    if (d1 < INFINITY) stack[(sp++) * stride] = r1;
     first = r0;  // d0 is the smallest and finite (nh > 0)
   }
   R.sp = sp;
@@ -404,18 +387,18 @@ __device__ __forceinline__ bool trav_node(const SceneView &S, TravRay &R, const 
 // the iteration cap is reached (never expected); the ray is then finished
 // with what it has.
 template <bool ANY, bool CURVES = true>
-__device__ __forceinline__ bool trav_step(const SceneView &S, TravRay &R, const TStack &T, int *err) {
+__device__ __forceinline__ bool trav_step(const SceneView &S, TravRay &R, int32_t *stack, int stride, int *err) {
   if (++R.iters > S.trav_cap) {
     *err = 2;
     return true;
   }
   if (R.ref == PT_REF_EMPTY) return true;
-  if (ref_is_node(R.ref)) return !trav_node<ANY>(S, R, T, err);
+  if (ref_is_node(R.ref)) return !trav_node<ANY>(S, R, stack, stride, err);
   if (test_leaf<ANY, CURVES>(S, R.ref, R.o, R.d, R.dn, R.tmin, R.tmax, R.hit, R.time)) {
     R.found = true;
     if (ANY) return true;
   }
-  R.ref = trav_pop(R, T);
+  R.ref = trav_pop(R, stack, stride);
   return false;
 }
 
@@ -425,9 +408,7 @@ __device__ bool traverse(const SceneView &S, V3 o, V3 d, float tmin, float tmax,
                          int32_t *stack, int stride, int *err, float time = 0.f) {
   TravRay R;
   trav_init(R, o, d, tmin, tmax, time);
-  int32_t ovf[PT_STACK - PT_STACK_SMEM];
-  const TStack T{stack, stride, ovf};
-  while (!trav_step<ANY>(S, R, T, err)) {
+  while (!trav_step<ANY>(S, R, stack, stride, err)) {
   }
   hit = R.hit;
   return R.found;

@@ -308,12 +308,11 @@ __device__ __forceinline__ unsigned lanemask_lt() {
 template <bool MJ, bool CURVES>
 __global__ void __launch_bounds__(128) k_trace_closest(SceneView S, DeviceJob J, JobTable T, Queues Q, int qsel,
                                                        int bounce, long long g0) {
-  __shared__ int32_t stack[PT_STACK_SMEM * 128];
+  __shared__ int32_t stack[PT_STACK * 128];
   const int n = Q.counts[qsel];
   int *fetch = Q.counts + 4;
   const int lane = threadIdx.x & 31;
-  int32_t ovf[PT_STACK - PT_STACK_SMEM];  // deep stack entries (local memory)
-  const TStack TS{stack + threadIdx.x, (int)blockDim.x, ovf};
+  int32_t *my_stack = stack + threadIdx.x;
   TravRay R;
   bool active = false, exhausted = false;
   int ray = 0, rays = 0;
@@ -354,7 +353,7 @@ __global__ void __launch_bounds__(128) k_trace_closest(SceneView S, DeviceJob J,
       if (exhausted) break;
       continue;
     }
-    if (active && trav_step<false, CURVES>(S, R, TS, Q.err)) {
+    if (active && trav_step<false, CURVES>(S, R, my_stack, blockDim.x, Q.err)) {
       const bool hit = R.found;
       int prim = hit ? R.hit.prim : (t_s < 1e5f ? PT_HIT_MEDIUM : -1);
       float t = hit ? R.hit.t : (prim == PT_HIT_MEDIUM ? t_s : FLT_MAX);
