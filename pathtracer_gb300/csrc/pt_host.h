@@ -19,7 +19,7 @@ struct PtError : std::runtime_error {
   PtError(int c, const std::string &m) : std::runtime_error(m), code(c) {}
 };
 
-void fail(int code, const std::string &msg);
+[[noreturn]] void fail(int code, const std::string &msg);
 void cuda_check(cudaError_t e, const char *what);
 
 HaltonTables make_halton_tables();

@@ -407,7 +407,7 @@ void decode_png(const std::string &path, const std::vector<unsigned char> &d, st
       in += row;
       for (size_t i = 0; i < row; ++i) {
         const int a = i >= (size_t)bpp ? cur[i - bpp] : 0, b = prev[i], c = i >= (size_t)bpp ? prev[i - bpp] : 0;
-        int v;
+        int v = 0;
         switch (f) {
         case 0: v = 0; break;
         case 1: v = a; break;

@@ -90,11 +90,9 @@ __device__ inline V3 env_alias_sample(const EnvMap &E, float u0, float u1, float
   int cell = (r < __ldg(E.alias_prob + i)) ? i : __ldg(E.alias_idx + i);
   int cx = cell % E.width, cy = cell / E.width;
   float u = (cx + u1) / E.width, v = (cy + u2) / E.height;
-  float theta = v * (float)PT_PI;
-  float st, ct, sp, cp;
+  float st, ct, sp, cp;  // theta = pi v, phi = 2 pi u
   sincospi_(v, &st, &ct);
   sincospi_(2.f * u, &sp, &cp);
-  (void)theta;
   V3 d = v3(-st * cp, -ct, st * sp);
   pdf = (st > 0.f) ? __ldg(E.pdf + cell) * (float)N / (2.f * (float)(PT_PI * PT_PI) * st) : 0.f;
   return d;
