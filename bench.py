@@ -63,6 +63,7 @@ def parse():
     ap.add_argument("--batch-jobs", type=int, default=96)
     ap.add_argument("--serve-seconds", type=float, default=10.0)
     ap.add_argument("--serve-rate", type=float, default=20.0, help="Poisson arrivals per second")
+    ap.add_argument("--serve-pass-spp", type=int, default=8, help="samples per request per scheduling pass")
     return ap.parse_args()
 
 
@@ -277,7 +278,7 @@ def run_batched(r, scenes, n_jobs: int, seed: int = 11, res=(64, 1024), spp=(4, 
     }
 
 
-def run_served(r, scenes, big, seconds: float, rate: float, seed: int = 12):
+def run_served(r, scenes, big, seconds: float, rate: float, seed: int = 12, pass_spp: int = 8):
     """Serving: Poisson arrivals at `rate` req/s for `seconds` over the
     resident scenes; each request a seeded camera, square resolution
     log-uniform 128..512, an spp cap U{16..128} and a target RMSE of 0.02
@@ -317,7 +318,7 @@ def run_served(r, scenes, big, seconds: float, rate: float, seed: int = 12):
     while k < len(reqs) or outstanding:
         now = time.perf_counter() - t0
         while k < len(reqs) and reqs[k][0] <= now:
-            rid = srv.submit(reqs[k][1], target_rmse=0.02, spp_cap=reqs[k][2], spp_per_pass=8)
+            rid = srv.submit(reqs[k][1], target_rmse=0.02, spp_cap=reqs[k][2], spp_per_pass=pass_spp)
             arrival[rid] = (reqs[k][0], k)
             outstanding.add(rid)
             k += 1
@@ -354,7 +355,7 @@ def run_served(r, scenes, big, seconds: float, rate: float, seed: int = 12):
         "speedup_vs_plain": t_plain / busy if busy else None,
         "mean_spp": float(np.mean(list(spp_done.values()))) if spp_done else None,
         "mix": "4 resident scenes (cornell, rough_glass 1.3M tris, divergence, rough_glass 5.2M tris) with motion; "
-               "res log-uniform 128..512, spp cap U{16..128}, target RMSE 0.02, 8 spp per pass",
+               f"res log-uniform 128..512, spp cap U{{16..128}}, target RMSE 0.02, {pass_spp} spp per pass",
     }
 
 
@@ -584,7 +585,7 @@ def run_ours(args, rank, world, local_rank):
         # of paths each (same scenes and cameras, smaller frames and spp)
         forms["batched_small_jobs"] = run_batched(r, fs, args.batch_jobs, seed=13, res=(64, 256), spp=(4, 32),
                                                   tune_sample=32, tune_spp=32)
-        forms["served"] = run_served(r, fs, big, args.serve_seconds, args.serve_rate)
+        forms["served"] = run_served(r, fs, big, args.serve_seconds, args.serve_rate, pass_spp=args.serve_pass_spp)
         line["forms"] = forms
     if not args.no_cpu_baseline:
         from oracle import pyoracle as O
