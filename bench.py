@@ -63,7 +63,7 @@ def parse():
     ap.add_argument("--batch-jobs", type=int, default=96)
     ap.add_argument("--serve-seconds", type=float, default=10.0)
     ap.add_argument("--serve-rate", type=float, default=20.0, help="Poisson arrivals per second")
-    ap.add_argument("--serve-pass-spp", type=int, default=8, help="samples per request per scheduling pass")
+    ap.add_argument("--serve-pass-spp", type=int, default=16, help="samples per request per scheduling pass")
     return ap.parse_args()
 
 
@@ -282,7 +282,7 @@ def run_served(r, scenes, big, seconds: float, rate: float, seed: int = 12, pass
     """Serving: Poisson arrivals at `rate` req/s for `seconds` over the
     resident scenes; each request a seeded camera, square resolution
     log-uniform 128..512, an spp cap U{16..128} and a target RMSE of 0.02
-    (whichever comes first), 8 spp per scheduling pass.  Latency is from the
+    (whichever comes first), `pass_spp` spp per scheduling pass.  Latency is from the
     request's arrival to its completion.  The plain arm renders the same
     requests (same samples, spp as served) one after the other through
     pt_render."""
