@@ -362,6 +362,7 @@ void autotune(Context *c, const pt_job_desc *jobs, int n, pt_tuning *out) {
     c->cfg.sort_by_material = cd.sort;
     c->cfg.trace_blocks = base.trace_blocks * cd.tmul;
     c->cfg.shade_blocks = base.shade_blocks * cd.smul;
+    for (int f = 0; f < PT_FAM_MISC + 2; ++f) c->cfg.shade_fam_blocks[f] = base.shade_fam_blocks[f] * cd.smul;
     c->batch_wave_cap = cd.wave;
     pt_stats st;
     render_batch(c, jobs, n, nullptr, &st);  // capture + warm
@@ -380,6 +381,7 @@ void autotune(Context *c, const pt_job_desc *jobs, int n, pt_tuning *out) {
   c->cfg.sort_by_material = bc.sort;
   c->cfg.trace_blocks = base.trace_blocks * bc.tmul;
   c->cfg.shade_blocks = base.shade_blocks * bc.smul;
+  for (int f = 0; f < PT_FAM_MISC + 2; ++f) c->cfg.shade_fam_blocks[f] = base.shade_fam_blocks[f] * bc.smul;
   c->batch_wave_cap = bc.wave;
   if (out) {
     out->wave_paths = bc.wave;

@@ -1507,6 +1507,8 @@ Context::Context(int dev) : device(dev) {
   kernel_attributes(&kinfo);
   cfg.trace_blocks = num_sms * std::max(1, kinfo.trace_blocks_per_sm);
   cfg.shade_blocks = num_sms * std::max(1, kinfo.shade_blocks_per_sm);
+  for (int f = 0; f < PT_FAM_MISC + 2; ++f)
+    cfg.shade_fam_blocks[f] = num_sms * std::max(1, kinfo.shade_fam_blocks_per_sm[f]);
   cfg.max_blocks_simple = num_sms * 8;
   cfg.sort_by_material = 1;
   cfg.family_mask = 0x7f;

@@ -451,6 +451,16 @@ void kernel_attributes(KernelInfo *info) {
   info->shade_blocks_per_sm = nb;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_trace_shadow<false>, 128, 0);
   info->shadow_blocks_per_sm = nb;
+  int *fb = info->shade_fam_blocks_per_sm;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fb[0], k_shade<0, false>, 128, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fb[1], k_shade<1, false>, 128, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fb[2], k_shade<2, false>, 128, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fb[3], k_shade<3, false>, 128, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fb[4], k_shade<4, false>, 128, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fb[5], k_shade<5, false>, 128, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fb[6], k_shade<6, false>, 128, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fb[PT_FAM_MISC], k_shade<PT_FAM_MISC, false>, 128, 0);
+  fb[PT_FAM_MISC + 1] = info->shade_blocks_per_sm;
 }
 
 }  // namespace pt

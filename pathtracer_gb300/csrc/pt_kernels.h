@@ -54,7 +54,8 @@ struct Queues {
 
 struct LaunchCfg {
   int trace_blocks;
-  int shade_blocks;
+  int shade_blocks;                       // grid of the generic shade kernel
+  int shade_fam_blocks[PT_FAM_MISC + 2];  // grid per family (0..PT_FAM_MISC), generic last
   int max_blocks_simple;
   int sort_by_material;
   unsigned family_mask;  // material types present in the scene (bit per type)
@@ -93,6 +94,7 @@ struct Profiler {
 struct KernelInfo {
   int trace_regs, shade_regs;
   int trace_blocks_per_sm, shade_blocks_per_sm, shadow_blocks_per_sm;
+  int shade_fam_blocks_per_sm[PT_FAM_MISC + 2];  // per family, generic last
 };
 
 void upload_halton_tables(const HaltonTables &T, cudaStream_t st);

@@ -514,8 +514,18 @@ __device__ __forceinline__ void next_event(const SceneView &S, const DeviceJob &
 // NEE_MIS weights light and BSDF sampling with the power heuristic and
 // always performs NEE at non-delta vertices.  The loop runs in phases so
 // that the queue slot allocations (warp ballots) see every lane.
+// Resident blocks per SM a shade kernel is compiled for: families whose BSDF
+// code fits 102 registers without spilling run 5 blocks of 128 threads per
+// SM (the compiler's default allocation gave them 96-128 registers, 4-5
+// blocks); the Disney and hair kernels and the generic one, which spill
+// below 128 registers, run 4.  Single-job and merged-wave variants get the
+// same bound: a tighter one (6 blocks, 80 registers) changes how the
+// compiler contracts multiply-adds, and the two variants must compute the
+// same bits (a batched job equals its plain render).
+constexpr int shade_min_blocks(int fam, bool) { return (fam == 5 || fam == 6 || fam < 0) ? 4 : 5; }
+
 template <int FAM, bool MJ>
-__global__ void __launch_bounds__(128) k_shade(SceneView S, DeviceJob J, JobTable T, Queues Q, int qsel, int bounce,
+__global__ void __launch_bounds__(128, shade_min_blocks(FAM, MJ)) k_shade(SceneView S, DeviceJob J, JobTable T, Queues Q, int qsel, int bounce,
                                                long long g0) {
   int lo = 0, hi = Q.counts[qsel];
   if (FAM >= 0) {
@@ -748,19 +758,19 @@ void launch_wave_stages(const SceneView &S, const DeviceJob &J, const JobTable &
       P.end(st);
       P.count(STAGE_SORT, 2);
       P.begin(STAGE_SHADE, st);
-      if (cfg.family_mask & (1u << 0)) k_shade<0, MJ><<<cfg.shade_blocks, 128, 0, st>>>(S, J, T, Q, qsel, b, g0);
-      if (cfg.family_mask & (1u << 1)) k_shade<1, MJ><<<cfg.shade_blocks, 128, 0, st>>>(S, J, T, Q, qsel, b, g0);
-      if (cfg.family_mask & (1u << 2)) k_shade<2, MJ><<<cfg.shade_blocks, 128, 0, st>>>(S, J, T, Q, qsel, b, g0);
-      if (cfg.family_mask & (1u << 3)) k_shade<3, MJ><<<cfg.shade_blocks, 128, 0, st>>>(S, J, T, Q, qsel, b, g0);
-      if (cfg.family_mask & (1u << 4)) k_shade<4, MJ><<<cfg.shade_blocks, 128, 0, st>>>(S, J, T, Q, qsel, b, g0);
-      if (cfg.family_mask & (1u << 5)) k_shade<5, MJ><<<cfg.shade_blocks, 128, 0, st>>>(S, J, T, Q, qsel, b, g0);
-      if (cfg.family_mask & (1u << 6)) k_shade<6, MJ><<<cfg.shade_blocks, 128, 0, st>>>(S, J, T, Q, qsel, b, g0);
-      k_shade<PT_FAM_MISC, MJ><<<cfg.shade_blocks, 128, 0, st>>>(S, J, T, Q, qsel, b, g0);
+      if (cfg.family_mask & (1u << 0)) k_shade<0, MJ><<<cfg.shade_fam_blocks[0], 128, 0, st>>>(S, J, T, Q, qsel, b, g0);
+      if (cfg.family_mask & (1u << 1)) k_shade<1, MJ><<<cfg.shade_fam_blocks[1], 128, 0, st>>>(S, J, T, Q, qsel, b, g0);
+      if (cfg.family_mask & (1u << 2)) k_shade<2, MJ><<<cfg.shade_fam_blocks[2], 128, 0, st>>>(S, J, T, Q, qsel, b, g0);
+      if (cfg.family_mask & (1u << 3)) k_shade<3, MJ><<<cfg.shade_fam_blocks[3], 128, 0, st>>>(S, J, T, Q, qsel, b, g0);
+      if (cfg.family_mask & (1u << 4)) k_shade<4, MJ><<<cfg.shade_fam_blocks[4], 128, 0, st>>>(S, J, T, Q, qsel, b, g0);
+      if (cfg.family_mask & (1u << 5)) k_shade<5, MJ><<<cfg.shade_fam_blocks[5], 128, 0, st>>>(S, J, T, Q, qsel, b, g0);
+      if (cfg.family_mask & (1u << 6)) k_shade<6, MJ><<<cfg.shade_fam_blocks[6], 128, 0, st>>>(S, J, T, Q, qsel, b, g0);
+      k_shade<PT_FAM_MISC, MJ><<<cfg.shade_fam_blocks[PT_FAM_MISC], 128, 0, st>>>(S, J, T, Q, qsel, b, g0);
       P.end(st);
       P.count(STAGE_SHADE, 1 + __builtin_popcount(cfg.family_mask & 0x7fu));
     } else {
       P.begin(STAGE_SHADE, st);
-      k_shade<-1, MJ><<<cfg.shade_blocks, 128, 0, st>>>(S, J, T, Q, qsel, b, g0);
+      k_shade<-1, MJ><<<cfg.shade_fam_blocks[PT_FAM_MISC + 1], 128, 0, st>>>(S, J, T, Q, qsel, b, g0);
       P.end(st);
       P.count(STAGE_SHADE, 1);
     }
