@@ -413,6 +413,9 @@ void launch_shadow(const SceneView &S, const Queues &Q, int LN, const LaunchCfg 
     k_trace_shadow<false><<<cfg.trace_blocks, 128, 0, st>>>(S, Q, LN);
   k_shadow_resolve<<<cfg.max_blocks_simple, 256, 0, st>>>(Q, LN);
 }
+void launch_shadow_resolve(const Queues &Q, int LN, const LaunchCfg &cfg, cudaStream_t st) {
+  k_shadow_resolve<<<cfg.max_blocks_simple, 256, 0, st>>>(Q, LN);
+}
 
 void launch_film(const DeviceJob &J, const Queues &Q, long long lo, int cnt, long long slot0, float *film,
                  const LaunchCfg &cfg, cudaStream_t st) {

@@ -59,6 +59,8 @@ struct LaunchCfg {
   int max_blocks_simple;
   int sort_by_material;
   unsigned family_mask;  // material types present in the scene (bit per type)
+  int pair_trace;        // waves of at most this many paths trace the shadow rays of
+                         // bounce b with the closest rays of b + 1 (0: never)
 };
 
 // Per-stage CUDA-event timing of the wave kernels (pt_profile_begin/end).
@@ -116,6 +118,7 @@ void launch_wave(const SceneView &S, const DeviceJob &J, const Queues &Q, long l
 // Job-independent stages (pt_kernels.cu), also used by merged waves.
 void launch_sort(const SceneView &S, const Queues &Q, int qsel, const LaunchCfg &cfg, cudaStream_t st);
 void launch_shadow(const SceneView &S, const Queues &Q, int LN, const LaunchCfg &cfg, cudaStream_t st);
+void launch_shadow_resolve(const Queues &Q, int LN, const LaunchCfg &cfg, cudaStream_t st);
 // Adds paths [lo, lo + cnt) of job J (held in wave slots slot0..) to its
 // film, per pixel in sample order.
 void launch_film(const DeviceJob &J, const Queues &Q, long long lo, int cnt, long long slot0, float *film,

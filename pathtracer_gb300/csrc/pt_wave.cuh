@@ -362,6 +362,95 @@ __global__ void __launch_bounds__(128) k_trace_closest(SceneView S, DeviceJob J,
   warp_count(&Q.stats[2], rays);
 }
 
+// k_trace_pair: the closest-hit rays of bounce `bounce` (RayQueue qsel)
+// and the shadow rays of the bounce before it (ShadowQueue, LN light
+// samples per vertex) in ONE persistent launch.  Both queues come from the
+// same shade pass and neither reads the other's output, so one index space
+// [0, n_closest + n_shadow) is fetched with one counter (Q.counts[4]):
+// closest rays first (the sort and shade passes wait on them), then shadow
+// rays.  A bounce then has one sparse tail instead of two.  Per ray the work
+// is exactly k_trace_closest's or k_trace_shadow's, so results are the same;
+// the shadow terms are still added (k_shadow_resolve) before the next shade
+// pass, in the same order.
+template <bool MJ, bool CURVES>
+__global__ void __launch_bounds__(128, 7) k_trace_pair(SceneView S, DeviceJob J, JobTable T, Queues Q, int qsel,
+                                                    int bounce, long long g0, int LN) {
+  __shared__ int32_t stack[PT_STACK * 128];
+  const int nc = Q.counts[qsel];
+  const int n = nc + Q.counts[2] * LN;
+  int *fetch = Q.counts + 4;
+  const int lane = threadIdx.x & 31;
+  int32_t *my_stack = stack + threadIdx.x;
+  TravRay R;
+  bool active = false, exhausted = false, shadow = false;
+  size_t slot = 0;  // closest: ray index; shadow: ShadowQueue slot
+  int crays = 0, srays = 0;
+  float t_s = INFINITY;
+  for (;;) {
+    unsigned idle = __ballot_sync(0xffffffffu, !active);
+    if (!exhausted && __popc(idle) >= PT_FETCH_IDLE) {
+      const int k = __popc(idle);
+      int base = 0;
+      if (lane == 0) base = atomicAdd(fetch, k);
+      base = __shfl_sync(0xffffffffu, base, 0);
+      if (base + k >= n) exhausted = true;
+      if (!active) {
+        const int r = base + __popc(idle & lanemask_lt());
+        if (r < nc) {
+          float4 ro = ld4(Q.ray_o[qsel] + r), rd = ld4(Q.ray_d[qsel] + r);
+          float tmax = 1e5f;
+          t_s = INFINITY;
+          if (S.has_medium) {
+            long long g;
+            const DeviceJob &Jp = path_job<MJ>(J, T, Q, __float_as_int(ro.w), g0, g);
+            if (bounce < Jp.job.max_depth) {
+              PathId P = path_id(Jp, g);
+              float uf = sampler_dim(Jp, 4 * bounce, P.halton_index, P.key, P.pix, P.k);
+              t_s = -logf(1.f - uf) / S.sigma_t_max;
+              tmax = fminf(tmax, t_s);
+            }
+          }
+          trav_init(R, v3(ro.x, ro.y, ro.z), v3(rd.x, rd.y, rd.z), 1e-4f, tmax, rd.w);
+          slot = (size_t)r;
+          shadow = false;
+          active = true;
+          ++crays;
+        } else if (r < n) {
+          const int v = (r - nc) / LN, ls = (r - nc) - v * LN;
+          slot = (size_t)ls * Q.cap + v;
+          float4 dd = ld4(Q.sh_d + slot);
+          if (dd.w >= 0.f) {
+            float4 so = ld4(Q.sh_o + v);
+            const float time = S.has_motion ? ld4(Q.sh_c + slot).w : 0.f;
+            trav_init(R, v3(so.x, so.y, so.z), v3(dd.x, dd.y, dd.z), 0.001f, dd.w, time);
+            shadow = true;
+            active = true;
+            ++srays;
+          }
+        }
+      }
+      idle = __ballot_sync(0xffffffffu, !active);
+    }
+    if (idle == 0xffffffffu) {
+      if (exhausted) break;
+      continue;
+    }
+    if (active && !shadow && trav_step<false, CURVES>(S, R, my_stack, blockDim.x, Q.err)) {
+      const bool hit = R.found;
+      int prim = hit ? R.hit.prim : (t_s < 1e5f ? PT_HIT_MEDIUM : -1);
+      float t = hit ? R.hit.t : (prim == PT_HIT_MEDIUM ? t_s : FLT_MAX);
+      Q.hit[slot] = make_float4(t, __int_as_float(prim), R.hit.u, R.hit.v);
+      active = false;
+    }
+    if (active && shadow && trav_step<true, CURVES>(S, R, my_stack, blockDim.x, Q.err)) {
+      Q.sh_vis[slot] = R.found ? 0 : 1;
+      active = false;
+    }
+  }
+  warp_count(&Q.stats[2], crays);
+  warp_count(&Q.stats[3], srays);
+}
+
 // The hit point in its object's rest frame (texture coordinates of moving
 // objects follow the object).
 __device__ __forceinline__ V3 uv_point(const SceneView &S, const Surf &sf, float time) {
@@ -739,18 +828,37 @@ void launch_wave_stages(const SceneView &S, const DeviceJob &J, const JobTable &
   P.end(st);
   P.count(STAGE_CAMERA, 1);
   int qsel = 0;
+  const bool pair = n <= cfg.pair_trace;
   for (int b = 0; b < bounces; ++b) {
-    // reset next-queue and shadow counters (device side, graph friendly)
+    // reset next-queue and fetch counters (device side, graph friendly)
     // ([2] shadow queue, [3] shadow fetch, [4] closest-hit fetch)
     cudaMemsetAsync(Q.counts + (qsel ^ 1), 0, sizeof(int), st);
-    cudaMemsetAsync(Q.counts + 2, 0, 3 * sizeof(int), st);
-    P.begin(STAGE_TRACE, st);
-    if (S.curves)
-      k_trace_closest<MJ, true><<<cfg.trace_blocks, 128, 0, st>>>(S, J, T, Q, qsel, b, g0);
+    if (!pair || b == 0)
+      cudaMemsetAsync(Q.counts + 2, 0, 3 * sizeof(int), st);
     else
+      cudaMemsetAsync(Q.counts + 4, 0, sizeof(int), st);
+    P.begin(STAGE_TRACE, st);
+    if (pair) {
+      // this bounce's closest rays with the previous bounce's shadow rays
+      if (S.curves)
+        k_trace_pair<MJ, true><<<cfg.trace_blocks, 128, 0, st>>>(S, J, T, Q, qsel, b, g0, LN);
+      else
+        k_trace_pair<MJ, false><<<cfg.trace_blocks, 128, 0, st>>>(S, J, T, Q, qsel, b, g0, LN);
+    } else if (S.curves) {
+      k_trace_closest<MJ, true><<<cfg.trace_blocks, 128, 0, st>>>(S, J, T, Q, qsel, b, g0);
+    } else {
       k_trace_closest<MJ, false><<<cfg.trace_blocks, 128, 0, st>>>(S, J, T, Q, qsel, b, g0);
+    }
     P.end(st);
     P.count(STAGE_TRACE, 1);
+    if (pair && b > 0) {
+      // the previous bounce's shadow terms, before this bounce's shading
+      P.begin(STAGE_SHADOW, st);
+      launch_shadow_resolve(Q, LN, cfg, st);
+      cudaMemsetAsync(Q.counts + 2, 0, 2 * sizeof(int), st);
+      P.end(st);
+      P.count(STAGE_SHADOW, 1);
+    }
     if (cfg.sort_by_material) {
       // sort-by-material queues: one specialised shade kernel per family
       P.begin(STAGE_SORT, st);
@@ -774,10 +882,12 @@ void launch_wave_stages(const SceneView &S, const DeviceJob &J, const JobTable &
       P.end(st);
       P.count(STAGE_SHADE, 1);
     }
-    P.begin(STAGE_SHADOW, st);
-    launch_shadow(S, Q, LN, cfg, st);
-    P.end(st);
-    P.count(STAGE_SHADOW, 2);
+    if (!pair || b + 1 == bounces) {
+      P.begin(STAGE_SHADOW, st);
+      launch_shadow(S, Q, LN, cfg, st);
+      P.end(st);
+      P.count(STAGE_SHADOW, 2);
+    }
     qsel ^= 1;
   }
 }

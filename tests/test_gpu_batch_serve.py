@@ -188,6 +188,29 @@ def test_multi_wave_render_equals_single_wave(renderer, scenes, monkeypatch):
     small.close()
 
 
+def test_paired_tracing_equals_separate_tracing(renderer, scenes, monkeypatch):
+    # small waves trace bounce b's shadow rays with bounce b + 1's closest
+    # rays in one launch; the shadow terms are still added before the next
+    # shade pass, so the film has the bits of separate launches
+    monkeypatch.setenv("PT_PAIR_TRACE", "0")
+    sep = N.Renderer(0)
+    monkeypatch.delenv("PT_PAIR_TRACE")
+    for sc, c, kw in ((S.cornell_icosphere(3)[0], S.cornell_icosphere(3)[1], {}),
+                      (*S.material_divergence(subdiv=2, seed=3, aspect=1.0), {"sampler": N.SAMPLER_STRATIFIED}),
+                      (*S.rough_glass(subdiv=4, env_w=256, env_h=128, seed=2),
+                       {"rr_start": 4, "env_sampling": N.ENV_ALIAS})):
+        a_id, b_id = renderer.upload(sc), sep.upload(sc)
+        ja = N.job_desc(a_id, c, 48, 40, 4, 4, 8, seed=6, estimator=N.EST_NEE_MIS, **kw)
+        jb = N.job_desc(b_id, c, 48, 40, 4, 4, 8, seed=6, estimator=N.EST_NEE_MIS, **kw)
+        paired, st1 = renderer.render(ja, stats=True)
+        separate, st2 = sep.render(jb, stats=True)
+        assert st1.rays == st2.rays and st1.shadow_rays == st2.shadow_rays
+        assert np.array_equal(paired, separate)
+        renderer.release(a_id)
+        sep.release(b_id)
+    sep.close()
+
+
 def test_traversal_cap_reports_device_error_and_context_survives(monkeypatch):
     # failure detection without a fault: a context whose traversal step bound
     # is tiny makes every ray hit it; the kernels set the device error flag
