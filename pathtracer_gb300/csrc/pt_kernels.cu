@@ -10,7 +10,8 @@
 //   k_trace_shadow   ShadowQueue any-hit visibility
 //   k_shadow_resolve visible NEE terms added to L in a fixed order
 // and once per wave k_camera (RayQueue 0) and k_film (ordered per-pixel
-// accumulation).
+// accumulation).  Small waves trace a bounce's shadow rays together with the
+// next bounce's closest-hit rays (k_trace_pair, pt_wave.cuh).
 #include "pt_wave.cuh"
 
 namespace pt {

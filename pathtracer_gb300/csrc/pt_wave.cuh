@@ -1,6 +1,6 @@
 // pt_wave.cuh -- device code of the wavefront stages whose work depends on
-// the job of each path: camera, closest-hit traversal (medium free flight)
-// and shading.  Included by pt_kernels.cu (single-job waves, MJ = false: the
+// the job of each path: camera, closest-hit traversal (medium free flight),
+// the paired closest + shadow traversal of small waves, and shading.  Included by pt_kernels.cu (single-job waves, MJ = false: the
 // job is a kernel argument) and by pt_kernels_multi.cu (merged waves of many
 // jobs, MJ = true: a job table in HBM and a job index per path); the two
 // translation units compile in parallel.  The estimator restates getRayColor
