@@ -1525,6 +1525,9 @@ Context::Context(int dev) : device(dev) {
   cfg.pair_trace = 1 << 21;
   const char *pair = std::getenv("PT_PAIR_TRACE");
   if (pair) cfg.pair_trace = std::max(0, std::atoi(pair));
+  cfg.pair_from_bounce = 0;
+  const char *pfb = std::getenv("PT_PAIR_FROM_BOUNCE");
+  if (pfb) cfg.pair_from_bounce = std::max(0, std::atoi(pfb));
   cuda_check(cudaMalloc(&d_err, sizeof(int)), "cudaMalloc(err)");
   cuda_check(cudaMemsetAsync(d_err, 0, sizeof(int), stream), "memset err");
   cuda_check(cudaStreamSynchronize(stream), "context init");

@@ -61,6 +61,8 @@ struct LaunchCfg {
   unsigned family_mask;  // material types present in the scene (bit per type)
   int pair_trace;        // waves of at most this many paths trace the shadow rays of
                          // bounce b with the closest rays of b + 1 (0: never)
+  int pair_from_bounce;  // larger waves do so from this bounce on (0: from the
+                         // roulette start of a single-job wave)
 };
 
 // Per-stage CUDA-event timing of the wave kernels (pt_profile_begin/end).

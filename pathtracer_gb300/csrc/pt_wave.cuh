@@ -828,12 +828,20 @@ void launch_wave_stages(const SceneView &S, const DeviceJob &J, const JobTable &
   P.end(st);
   P.count(STAGE_CAMERA, 1);
   int qsel = 0;
-  const bool pair = n <= cfg.pair_trace;
+  // bounce b's closest rays are traced together with bounce b - 1's shadow
+  // rays (paired) in small waves, and in large ones once the queues thin
+  // out: from the job's roulette start (single-job waves), or from
+  // cfg.pair_from_bounce when set
+  int from = cfg.pair_from_bounce;
+  if (from <= 0) from = (!MJ && J.job.rr_start >= 0) ? std::max(1, (int)J.job.rr_start) : (1 << 20);
+  auto paired = [&](int b) { return b > 0 && b < bounces && (n <= cfg.pair_trace || b >= from); };
   for (int b = 0; b < bounces; ++b) {
+    const bool pair = paired(b);
     // reset next-queue and fetch counters (device side, graph friendly)
-    // ([2] shadow queue, [3] shadow fetch, [4] closest-hit fetch)
+    // ([2] shadow queue, [3] shadow fetch, [4] closest-hit fetch); a
+    // pending shadow queue of the previous bounce keeps [2]
     cudaMemsetAsync(Q.counts + (qsel ^ 1), 0, sizeof(int), st);
-    if (!pair || b == 0)
+    if (!pair)
       cudaMemsetAsync(Q.counts + 2, 0, 3 * sizeof(int), st);
     else
       cudaMemsetAsync(Q.counts + 4, 0, sizeof(int), st);
@@ -851,7 +859,7 @@ void launch_wave_stages(const SceneView &S, const DeviceJob &J, const JobTable &
     }
     P.end(st);
     P.count(STAGE_TRACE, 1);
-    if (pair && b > 0) {
+    if (pair) {
       // the previous bounce's shadow terms, before this bounce's shading
       P.begin(STAGE_SHADOW, st);
       launch_shadow_resolve(Q, LN, cfg, st);
@@ -882,7 +890,7 @@ void launch_wave_stages(const SceneView &S, const DeviceJob &J, const JobTable &
       P.end(st);
       P.count(STAGE_SHADE, 1);
     }
-    if (!pair || b + 1 == bounces) {
+    if (!paired(b + 1)) {
       P.begin(STAGE_SHADOW, st);
       launch_shadow(S, Q, LN, cfg, st);
       P.end(st);

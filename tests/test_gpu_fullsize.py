@@ -117,3 +117,21 @@ def test_full_size_window_matches_oracle(renderer, headline):
     se = np.sqrt(2 * v_o.reshape(-1, 3).sum(0) / 16) / (12 * 12)
     z = (film.reshape(-1, 3).mean(0) - m_o.reshape(-1, 3).mean(0)) / np.maximum(se, 1e-12)
     assert np.all(np.abs(z) < 3.0), z
+
+
+def test_full_size_paired_tail_equals_separate(renderer, headline, monkeypatch):
+    """A large wave with roulette traces each bounce's shadow rays with the
+    next bounce's closest rays once the queues thin out (from the roulette
+    start); the film has the bits of separate launches."""
+    sc, cam, sid = headline
+    monkeypatch.setenv("PT_PAIR_FROM_BOUNCE", "1000000")
+    sep = N.Renderer(0)
+    monkeypatch.delenv("PT_PAIR_FROM_BOUNCE")
+    try:
+        sid2 = sep.upload(sc)
+        a = renderer.render(_job(sid, cam, 0, 2))
+        b = sep.render(_job(sid2, cam, 0, 2))
+        assert np.array_equal(a.view(np.int32), b.view(np.int32))
+        sep.release(sid2)
+    finally:
+        sep.close()
