@@ -46,7 +46,9 @@ FALLBACK_HBM_GBS = 6800.0
 # default workload at 16 spp per step, from one single-pass ncu capture of
 # the 17 launches of a timed step (profiles/ncu_traffic_rough_glass_1024_16spp.md);
 # scaled by the paths per step for other step sizes.
-NCU_TRAFFIC_PER_LAUNCH_16SPP = {"shadow": 3.630e9 / 17, "trace": 3.376e9 / 17}
+# ncu DRAM bytes (read + write) of the traversal kernels of one rough-glass
+# 16-spp step and their launch count (closest, paired and shadow launches)
+NCU_TRAVERSAL_BYTES_16SPP, NCU_TRAVERSAL_LAUNCHES_16SPP = 6.9101e9, 21
 
 
 def parse():
@@ -511,8 +513,11 @@ def run_ours(args, rank, world, local_rank):
 
     if rank != 0:
         return
-    # ---- roofline of the dominant kernel (CUDA events on the library stream)
-    dom = max(("trace", "shade", "shadow"), key=lambda s: prof[s][0])
+    # ---- roofline of the dominant stage (CUDA events on the library stream):
+    # traversal = closest-hit, paired and shadow-ray launches (+ the shadow
+    # resolve), or shading
+    trav_ms = prof["trace"][0] + prof["shadow"][0]
+    dom = "traversal" if trav_ms >= prof["shade"][0] else "shade"
     peak = None
     peak_src = "fallback"
     if PEAKS.exists():
@@ -525,10 +530,10 @@ def run_ours(args, rank, world, local_rank):
         peak = FALLBACK_HBM_GBS
     # algorithmic bytes per unit (per ray for the traversal stages, per path
     # vertex for shade): queue records read and written
-    per_unit = {"trace": 48.0, "shadow": 44.0 * 2, "shade": 192.0}
-    units = {"trace": tot["rays"], "shadow": tot["shadow"], "shade": tot["segments"]}
-    dom_ms = prof[dom][0]
-    achieved = per_unit[dom] * units[dom] / (dom_ms / 1e3) / 1e9
+    alg_bytes = {"traversal": 48.0 * tot["rays"] + 88.0 * tot["shadow"], "shade": 192.0 * tot["segments"]}
+    dom_ms = trav_ms if dom == "traversal" else prof["shade"][0]
+    achieved = alg_bytes[dom] / (dom_ms / 1e3) / 1e9
+    trav_launches = prof["trace"][1] + prof["shadow"][1]
     launches = sum(v[1] for v in prof.values())
     step_bytes_gbs = tot["bytes"] / (t_dev / 1e3) / 1e9
     line = {
@@ -545,14 +550,20 @@ def run_ours(args, rank, world, local_rank):
         "rays_per_s": (tot["rays"] + tot["shadow"]) * world / t_max,
         "e2e": {"value": e2e_val, "unit": "paths/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": int(launches),
-        "roofline": {"bound": "hbm", "kernel": f"k_{'trace_closest' if dom == 'trace' else 'trace_shadow' if dom == 'shadow' else 'shade'}",
+        "roofline": {"bound": "hbm",
+                     "kernel": ("k_trace_closest / k_trace_pair / k_trace_shadow (traversal stage)"
+                                if dom == "traversal" else "k_shade"),
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_source": peak_src,
-                     "traffic": (NCU_TRAFFIC_PER_LAUNCH_16SPP[dom] * k / 16.0
-                                 if args.workload == "rough_glass" and dom in NCU_TRAFFIC_PER_LAUNCH_16SPP else None),
-                     "traffic_note": "ncu dram__bytes_read.sum + dram__bytes_write.sum per launch (average over "
-                                     "a 16-spp step's launches, scaled to this step), bytes",
-                     "note": f"stage share {prof[dom][0] / sum(v[0] for v in prof.values()):.2f}; "
+                     "traffic": (NCU_TRAVERSAL_BYTES_16SPP / NCU_TRAVERSAL_LAUNCHES_16SPP
+                                 if args.workload == "rough_glass" and dom == "traversal" and k == 16
+                                 and NCU_TRAVERSAL_BYTES_16SPP else None),
+                     "traffic_note": "ncu dram__bytes_read.sum + dram__bytes_write.sum per traversal launch "
+                                     "(all traversal launches of a 16-spp step), bytes",
+                     "algorithmic_bytes_note": "48 B per closest-hit ray (ray 32 B read, hit 16 B written) + "
+                                               "88 B per shadow ray (ShadowQueue record written and read)",
+                     "launches_per_step": trav_launches / args.steps if dom == "traversal" else None,
+                     "note": f"stage share {dom_ms / sum(v[0] for v in prof.values()):.2f}; "
                              f"whole-step queue bytes {step_bytes_gbs:.1f} GB/s"},
         "stage_ms": {kk: round(v[0], 3) for kk, v in prof.items()},
         "clocks": clk.summary(),
