@@ -66,6 +66,8 @@ def parse():
     ap.add_argument("--serve-seconds", type=float, default=10.0)
     ap.add_argument("--serve-rate", type=float, default=20.0, help="Poisson arrivals per second")
     ap.add_argument("--serve-pass-spp", type=int, default=16, help="samples per request per scheduling pass")
+    ap.add_argument("--serve-pass-paths", type=int, default=1 << 21,
+                    help="paths per request per scheduling pass (0: pass-spp only)")
     return ap.parse_args()
 
 
@@ -280,7 +282,8 @@ def run_batched(r, scenes, n_jobs: int, seed: int = 11, res=(64, 1024), spp=(4, 
     }
 
 
-def run_served(r, scenes, big, seconds: float, rate: float, seed: int = 12, pass_spp: int = 8):
+def run_served(r, scenes, big, seconds: float, rate: float, seed: int = 12, pass_spp: int = 8,
+               pass_paths: int = 0):
     """Serving: Poisson arrivals at `rate` req/s for `seconds` over the
     resident scenes; each request a seeded camera, square resolution
     log-uniform 128..512, an spp cap U{16..128} and a target RMSE of 0.02
@@ -320,7 +323,8 @@ def run_served(r, scenes, big, seconds: float, rate: float, seed: int = 12, pass
     while k < len(reqs) or outstanding:
         now = time.perf_counter() - t0
         while k < len(reqs) and reqs[k][0] <= now:
-            rid = srv.submit(reqs[k][1], target_rmse=0.02, spp_cap=reqs[k][2], spp_per_pass=pass_spp)
+            rid = srv.submit(reqs[k][1], target_rmse=0.02, spp_cap=reqs[k][2], spp_per_pass=pass_spp,
+                             paths_per_pass=pass_paths)
             arrival[rid] = (reqs[k][0], k)
             outstanding.add(rid)
             k += 1
@@ -357,7 +361,8 @@ def run_served(r, scenes, big, seconds: float, rate: float, seed: int = 12, pass
         "speedup_vs_plain": t_plain / busy if busy else None,
         "mean_spp": float(np.mean(list(spp_done.values()))) if spp_done else None,
         "mix": "4 resident scenes (cornell, rough_glass 1.3M tris, divergence, rough_glass 5.2M tris) with motion; "
-               f"res log-uniform 128..512, spp cap U{{16..128}}, target RMSE 0.02, {pass_spp} spp per pass",
+               f"res log-uniform 128..512, spp cap U{{16..128}}, target RMSE 0.02, {pass_spp} spp per pass"
+               + (f" (or ~{pass_paths} paths per request per pass)" if pass_paths else ""),
     }
 
 
@@ -596,7 +601,8 @@ def run_ours(args, rank, world, local_rank):
         # of paths each (same scenes and cameras, smaller frames and spp)
         forms["batched_small_jobs"] = run_batched(r, fs, args.batch_jobs, seed=13, res=(64, 256), spp=(4, 32),
                                                   tune_sample=32, tune_spp=32)
-        forms["served"] = run_served(r, fs, big, args.serve_seconds, args.serve_rate, pass_spp=args.serve_pass_spp)
+        forms["served"] = run_served(r, fs, big, args.serve_seconds, args.serve_rate, pass_spp=args.serve_pass_spp,
+                                     pass_paths=args.serve_pass_paths)
         line["forms"] = forms
     if not args.no_cpu_baseline:
         from oracle import pyoracle as O

@@ -498,7 +498,12 @@ typedef struct pt_request_desc {
   pt_job_desc job;
   float target_rmse;   /* stop when the estimated RMSE falls below this */
   int32_t spp_cap;     /* ... or when this many samples were taken */
-  int32_t spp_per_pass;/* samples added per scheduling pass */
+  int32_t spp_per_pass;/* samples added per scheduling pass (at least) */
+  int32_t paths_per_pass;/* > 0: per pass, enough samples for about this many
+                          * paths (width * height * spp), never fewer than
+                          * spp_per_pass -- small requests finish in fewer
+                          * passes.  Passes alternate between the two half
+                          * films whatever their size. */
 } pt_request_desc;
 
 int pt_server_create(void *ctx, int64_t hbm_budget_bytes, int32_t max_slots,

@@ -32,6 +32,7 @@ struct Request {
   float *film_a = nullptr;  // sum of even passes
   float *film_b = nullptr;  // sum of odd passes
   int spp_a = 0, spp_b = 0;
+  int passes = 0;  // scheduling passes rendered (even ones go to film_a)
   size_t bytes = 0;
   std::chrono::steady_clock::time_point t_submit, t_done;
   std::vector<float> result;
@@ -147,7 +148,8 @@ int pt_submit(void *server, const pt_request_desc *req, int64_t *request_id) {
   } catch (const std::exception &e) {
     return serr(s->ctx, PT_ERR_INVALID, e.what());
   }
-  if (req->spp_cap <= 0 || req->spp_per_pass <= 0) return serr(s->ctx, PT_ERR_INVALID, "bad spp cap / pass");
+  if (req->spp_cap <= 0 || req->spp_per_pass <= 0 || req->paths_per_pass < 0)
+    return serr(s->ctx, PT_ERR_INVALID, "bad spp cap / pass");
   Request r;
   r.id = s->next_id++;
   r.desc = *req;
@@ -202,10 +204,15 @@ int pt_server_step(void *server, int32_t *active_out) {
     pt_job_desc j = r.desc.job;
     const int spp_total = j.spp_x * j.spp_y;
     const int cap = std::min(r.desc.spp_cap, spp_total);
-    const int b = r.spp_done, e = std::min(cap, b + r.desc.spp_per_pass);
+    long long step = r.desc.spp_per_pass;
+    if (r.desc.paths_per_pass > 0) {
+      const long long px = std::max<long long>(1, (long long)j.width * j.height);
+      step = std::max(step, (r.desc.paths_per_pass + px - 1) / px);
+    }
+    const int b = r.spp_done, e = (int)std::min<long long>(cap, b + step);
     j.spp_begin = b;
     j.spp_end = e;
-    const bool to_a = ((b / std::max(1, r.desc.spp_per_pass)) % 2) == 0;
+    const bool to_a = (r.passes % 2) == 0;
     jobs.push_back(j);
     targets.push_back(to_a ? r.film_a : r.film_b);
     ends.push_back(e);
@@ -235,6 +242,7 @@ int pt_server_step(void *server, int32_t *active_out) {
     const pt_job_desc &j = jobs[q];
     (to_a_v[q] ? r.spp_a : r.spp_b) += ends[q] - j.spp_begin;
     r.spp_done = ends[q];
+    ++r.passes;
     const int cap = std::min(r.desc.spp_cap, j.spp_x * j.spp_y);
     if (r.spp_done < cap && r.desc.target_rmse > 0.f && r.spp_a > 0 && r.spp_b > 0) {
       pair_of[q] = (int)pairs.size();

@@ -144,7 +144,7 @@ class Tuning(C.Structure):
 
 class RequestDesc(C.Structure):
     _fields_ = [("job", JobDesc), ("target_rmse", C.c_float), ("spp_cap", C.c_int32),
-                ("spp_per_pass", C.c_int32)]
+                ("spp_per_pass", C.c_int32), ("paths_per_pass", C.c_int32)]
 
 
 _lib = None
@@ -629,12 +629,14 @@ class Server:
             self.lib.pt_server_destroy(self.handle)
             self.handle = C.c_void_p()
 
-    def submit(self, job: JobDesc, target_rmse: float = 0.0, spp_cap: int = 0, spp_per_pass: int = 1) -> int:
+    def submit(self, job: JobDesc, target_rmse: float = 0.0, spp_cap: int = 0, spp_per_pass: int = 1,
+               paths_per_pass: int = 0) -> int:
         req = RequestDesc()
         req.job = job
         req.target_rmse = target_rmse
         req.spp_cap = spp_cap if spp_cap > 0 else job.spp_x * job.spp_y
         req.spp_per_pass = spp_per_pass
+        req.paths_per_pass = paths_per_pass
         rid = C.c_int64()
         self.r._check(self.lib.pt_submit(self.handle, C.byref(req), C.byref(rid)))
         self.shapes[rid.value] = (job.height, job.width, 3)

@@ -147,6 +147,33 @@ def test_served_rmse_target_and_cap(renderer, scenes):
     assert res[capped][1] == 6
 
 
+def test_served_paths_per_pass(renderer, scenes):
+    """paths_per_pass sizes each pass from the request's own pixels (never
+    below spp_per_pass): the same result alone and in a mix, and the job's
+    film up to FP32 grouping."""
+    jobs = _jobs(scenes)
+    probe = jobs[1]
+    px = probe.width * probe.height
+    srv = N.Server(renderer, hbm_budget=1 << 30, max_slots=8)
+    rid = srv.submit(probe, spp_per_pass=1, paths_per_pass=3 * px)  # 3 spp per pass
+    alone, spp_alone = _serve_until_done(srv, [rid])[rid]
+    srv.close()
+    srv = N.Server(renderer, hbm_budget=1 << 30, max_slots=8)
+    other = srv.submit(jobs[2], spp_per_pass=2, paths_per_pass=1)  # floor: 2 spp per pass
+    srv.step()
+    rid = srv.submit(probe, spp_per_pass=1, paths_per_pass=3 * px)
+    res = _serve_until_done(srv, [other, rid])
+    srv.close()
+    assert res[rid][1] == spp_alone == probe.spp_x * probe.spp_y
+    assert np.array_equal(alone, res[rid][0])
+    assert np.allclose(alone, renderer.render(probe), rtol=1e-5, atol=1e-7)
+    assert np.allclose(res[other][0], renderer.render(jobs[2]), rtol=1e-5, atol=1e-7)
+    srv = N.Server(renderer, hbm_budget=1 << 30, max_slots=8)
+    with pytest.raises(N.PtError):
+        srv.submit(probe, spp_per_pass=1, paths_per_pass=-5)
+    srv.close()
+
+
 def test_server_admission_by_budget_and_cancel(renderer, scenes):
     jobs = _jobs(scenes)
     j = jobs[0]
