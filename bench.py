@@ -6,7 +6,9 @@ Workload (default): the rough-glass scene -- a seeded displaced icosphere of
 1024x512 FP32 HDRI (sky gradient + 3 Gaussian sun lobes, peak 5e3), rendered
 at 1024x1024, 256 spp (16x16 grid), depth 16, Russian roulette from depth 4,
 NEE+MIS with the luminance alias table, Owen-scrambled Halton sampler.
-One step = 16 of the 256 samples per pixel for every pixel (16.8 M paths).
+One step = 32 of the 256 samples per pixel for every pixel (33.6 M paths,
+rendered as two overlapped waves of 16.8 M paths); the 8 timed steps of the
+default run render the whole 256-spp frame once.
 
   value  paths/s with the scene resident in HBM, device film, device time
          (CUDA events on the library's stream, max over ranks);
@@ -42,12 +44,9 @@ import numpy as np  # noqa: E402
 
 PEAKS = REPO / "MEASURED_PEAKS.json"
 FALLBACK_HBM_GBS = 6800.0
-# DRAM bytes (read + write) per launch of the traversal kernels on the
-# default workload at 16 spp per step, from one single-pass ncu capture of
-# the 17 launches of a timed step (profiles/ncu_traffic_rough_glass_1024_16spp.md);
-# scaled by the paths per step for other step sizes.
 # ncu DRAM bytes (read + write) of the traversal kernels of one rough-glass
-# 16-spp step and their launch count (closest, paired and shadow launches)
+# wave of 16.8 M paths (16 spp of every pixel) and their launch count
+# (closest, paired and shadow launches; profiles/ncu_traffic_rough_glass_1024_16spp.md)
 NCU_TRAVERSAL_BYTES_16SPP, NCU_TRAVERSAL_LAUNCHES_16SPP = 6.9101e9, 21
 
 
@@ -58,7 +57,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="rough_glass", choices=["rough_glass", "cornell", "divergence"])
-    ap.add_argument("--spp-per-step", type=int, default=16)
+    ap.add_argument("--spp-per-step", type=int, default=32)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-forms", action="store_true", help="skip the batched and served forms")
     ap.add_argument("--no-rmse", action="store_true", help="skip the converged-reference RMSE")
@@ -561,10 +560,10 @@ def run_ours(args, rank, world, local_rank):
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_source": peak_src,
                      "traffic": (NCU_TRAVERSAL_BYTES_16SPP / NCU_TRAVERSAL_LAUNCHES_16SPP
-                                 if args.workload == "rough_glass" and dom == "traversal" and k == 16
+                                 if args.workload == "rough_glass" and dom == "traversal" and k % 16 == 0
                                  and NCU_TRAVERSAL_BYTES_16SPP else None),
                      "traffic_note": "ncu dram__bytes_read.sum + dram__bytes_write.sum per traversal launch "
-                                     "(all traversal launches of a 16-spp step), bytes",
+                                     "(all traversal launches of a 16.8 M-path wave), bytes",
                      "algorithmic_bytes_note": "48 B per closest-hit ray (ray 32 B read, hit 16 B written) + "
                                                "88 B per shadow ray (ShadowQueue record written and read)",
                      "launches_per_step": trav_launches / args.steps if dom == "traversal" else None,
