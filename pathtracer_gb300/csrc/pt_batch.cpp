@@ -238,6 +238,19 @@ void render_batch(Context *c, const pt_job_desc *jobs, int n, float **films, pt_
       if (!targets) cudaMemsetAsync(slot.films, 0, sizeof(float) * G.film_floats, slot.stream[0]);
       LaunchCfg lc = c->cfg;
       lc.family_mask = S->family_mask;
+      if (lc.pair_from_bounce <= 0) {
+        // paired tracing once the queues thin out: from the group's earliest
+        // roulette start when every member uses roulette
+        int from = 1 << 20;
+        bool all_rr = true;
+        for (int m : G.members) {
+          if (jobs[m].rr_start < 0)
+            all_rr = false;
+          else
+            from = std::min(from, (int)jobs[m].rr_start);
+        }
+        lc.pair_from_bounce = all_rr ? std::max(1, from) : (1 << 20);
+      }
       // consecutive waves alternate between two queue sets on two streams,
       // so one wave's sparse last bounces overlap the next wave's first
       // ones; the film stages stay in wave order (event chain), which keeps
