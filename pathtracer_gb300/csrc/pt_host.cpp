@@ -757,7 +757,31 @@ static int motion_of(const Builder &B, int bn) {
 // object's subtree root met from the world frame is never merged into a world
 // node: it becomes a child of its own (reference flagged PT_INST_BIT) whose
 // subtree is traversed in the object's frame.
-static void collapse(const Builder &B, int bn, Bvh4Out &out, int depth, int me, bool in_inst) {
+// Appends a subtree collapsed on its own (its root at index 0) behind `out`
+// and returns the root's index there: internal child references and leaf
+// item ranges are offset, so the result is the sequential collapse's.
+static int splice_collapsed(Bvh4Out &out, Bvh4Out &sub) {
+  const int base = (int)out.nodes.size(), lbase = (int)out.leaf_order.size();
+  for (Bvh4Node N : sub.nodes) {
+    for (int k = 0; k < 4; ++k) {
+      if (N.count[k] == 0)
+        N.child[k] = (N.child[k] & PT_INST_BIT) | ((N.child[k] & ~PT_INST_BIT) + base);
+      else if (N.count[k] > 0)
+        N.child[k] += lbase;
+    }
+    out.nodes.push_back(N);
+  }
+  out.node_motion.insert(out.node_motion.end(), sub.node_motion.begin(), sub.node_motion.end());
+  out.leaf_order.insert(out.leaf_order.end(), sub.leaf_order.begin(), sub.leaf_order.end());
+  out.leaf_world.insert(out.leaf_world.end(), sub.leaf_world.begin(), sub.leaf_world.end());
+  out.max_depth = std::max(out.max_depth, sub.max_depth);
+  return base;
+}
+
+// par > 0: the internal children's subtrees are collapsed on their own
+// threads (par - 1 levels further down) and spliced in child order, which
+// numbers nodes and leaf items exactly as the sequential recursion does.
+static void collapse(const Builder &B, int bn, Bvh4Out &out, int depth, int me, bool in_inst, int par = 0) {
   // gather up to 4 children by expanding the largest internal child
   int ch[4], nch = 2;
   ch[0] = B.nodes[bn].left;
@@ -790,6 +814,43 @@ static void collapse(const Builder &B, int bn, Bvh4Out &out, int depth, int me, 
     N0.hi_x[k] = N0.hi_y[k] = N0.hi_z[k] = -INFINITY;
     N0.child[k] = 0;
     N0.count[k] = -1;
+  }
+  if (par > 0) {
+    Bvh4Out subs[4];
+    bool enters[4] = {false, false, false, false};
+    std::vector<std::thread> pool;
+    for (int k = 0; k < nch; ++k) {
+      const BNode &c = B.nodes[ch[k]];
+      if (c.left < 0) continue;
+      enters[k] = !in_inst && motion_of(B, ch[k]);
+      subs[k].nodes.push_back(Bvh4Node());
+      subs[k].node_motion.push_back(enters[k] ? motion_of(B, ch[k]) : 0);
+      pool.emplace_back([&, k] { collapse(B, ch[k], subs[k], depth + 1, 0, in_inst || enters[k], par - 1); });
+    }
+    for (auto &t : pool) t.join();
+    for (int k = 0; k < nch; ++k) {
+      const BNode &c = B.nodes[ch[k]];
+      Bvh4Node &N = out.nodes[me];
+      N.lo_x[k] = c.box.lo[0];
+      N.lo_y[k] = c.box.lo[1];
+      N.lo_z[k] = c.box.lo[2];
+      N.hi_x[k] = c.box.hi[0];
+      N.hi_y[k] = c.box.hi[1];
+      N.hi_z[k] = c.box.hi[2];
+      if (c.left < 0) {
+        N.child[k] = (int)out.leaf_order.size();
+        N.count[k] = c.count;
+        for (int t = 0; t < c.count; ++t) {
+          out.leaf_order.push_back(B.leaf_prims[c.first + t]);
+          out.leaf_world.push_back(in_inst ? 0 : 1);
+        }
+      } else {
+        const int idx = splice_collapsed(out, subs[k]);
+        out.nodes[me].child[k] = enters[k] ? (idx | PT_INST_BIT) : idx;
+        out.nodes[me].count[k] = 0;
+      }
+    }
+    return;
   }
   for (int k = 0; k < nch; ++k) {
     const BNode &c = B.nodes[ch[k]];
@@ -1065,6 +1126,8 @@ std::unique_ptr<Scene> build_scene(const pt_scene_desc *d_in, cudaStream_t st, b
   }
 
   B.inst_motion.resize(B.nodes.size(), 0);
+  // large trees are collapsed on host threads (two levels of fan-out)
+  const int collapse_par = (threads != 1 && B.nodes.size() > (1u << 16)) ? 2 : 0;
   Bvh4Out out;
   out.nodes.push_back(Bvh4Node());
   out.node_motion.push_back(0);
@@ -1084,9 +1147,9 @@ std::unique_ptr<Scene> build_scene(const pt_scene_desc *d_in, cudaStream_t st, b
     R.count[0] = 0;
     out.nodes.push_back(Bvh4Node());
     out.node_motion.push_back(motion_of(B, root));
-    collapse(B, root, out, 1, 1, true);
+    collapse(B, root, out, 1, 1, true, collapse_par);
   } else {
-    collapse(B, root, out, 0, 0, false);
+    collapse(B, root, out, 0, 0, false, collapse_par);
   }
   if (out.nodes.size() >= (size_t)PT_INST_BIT) fail(PT_ERR_TOO_LARGE, "too many BVH nodes");
   if (out.leaf_order.size() >= ((size_t)1 << 28) - 8) fail(PT_ERR_TOO_LARGE, "too many leaf items");

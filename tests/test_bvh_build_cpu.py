@@ -63,3 +63,15 @@ def test_sah_tree_holds_every_item_once():
     ref, sah = N.bvh_build(sc), N.bvh_build(sc, sah=True)
     assert sah["items"] == ref["items"]
     assert sah["depth"] <= 15
+
+
+def test_parallel_collapse_equals_sequential_with_motion():
+    """Large trees are collapsed into BVH4 nodes on host threads and spliced
+    in child order: the same nodes, leaf items and motion records (content
+    hash) as the one-thread collapse, moving objects included."""
+    sc, _ = S.rough_glass(7)  # 327,680 triangles: above the parallel threshold
+    moving = S.with_motion(sc, seed=3)
+    for scene in (sc, moving):
+        one = N.bvh_build(scene, threads=1)
+        many = N.bvh_build(scene, threads=8)
+        assert one["hash"] == many["hash"] and one["nodes"] == many["nodes"] and one["depth"] == many["depth"]
