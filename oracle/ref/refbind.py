@@ -9,6 +9,7 @@ the GPU machine).
 from __future__ import annotations
 
 import ctypes as C
+import os
 from pathlib import Path
 
 import numpy as np
@@ -16,6 +17,8 @@ import numpy as np
 from pathtracer_gb300 import native as N
 
 LIB = Path(__file__).resolve().parents[1] / "_ref" / "libref_harness.so"
+# the reference sources the harness was built from (build_ref.sh's REF_ROOT)
+REF_ROOT = Path(os.environ.get("REF_ROOT", "/root/reference"))
 
 f32p = C.POINTER(C.c_float)
 i32p = C.POINTER(C.c_int32)

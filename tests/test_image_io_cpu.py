@@ -323,3 +323,35 @@ def test_scene_image_texture_and_environment_from_files(tmp_path):
     assert np.array_equal(sc.textures[t]["texels"], (img.astype(np.float32) / np.float32(255))[::-1])
     assert sc.env.shape == (16, 32, 3) and sc.env_intensity == 1.5
     assert np.array_equal(sc.env, N.load_image(hdr, hdr=True))
+
+
+def test_reference_repository_pngs_decode_like_its_image_texture():
+    """The reference repository's own PNGs (images/*.png: real-world files
+    with dynamic Huffman blocks and every scanline filter) decoded here and
+    sampled with ImageTexture's bilinear rule, against the reference's
+    ImageTexture::getTexelColor on the same files through the harness."""
+    import pytest
+    from oracle.ref import refbind
+    if not refbind.available():
+        pytest.skip("reference harness not built")
+    files = sorted((refbind.REF_ROOT / "images").glob("*.png"))
+    if not files:
+        pytest.skip("reference images absent")
+    rng = np.random.default_rng(17)
+    uv = rng.uniform(0.0, 1.0, (2000, 2)).astype(np.float32)
+    for f in files:
+        for flip in (False, True):
+            tex = N.load_image(f, flip_y=flip)  # [y][x]
+            h, w, _ = tex.shape
+            fu, fv = uv[:, 0] * np.float32(w), uv[:, 1] * np.float32(h)
+            x = fu.astype(np.int64)
+            y = fv.astype(np.int64)
+            x1, y1 = fu - x, fv - y
+            x = np.minimum(x, w - 2)
+            y = np.minimum(y, h - 2)
+            x2, y2 = np.float32(1) - x1, np.float32(1) - y1
+            c12 = tex[y, x] * x2[:, None] + tex[y, x + 1] * x1[:, None]
+            c34 = tex[y + 1, x] * x2[:, None] + tex[y + 1, x + 1] * x1[:, None]
+            ours = c12 * y2[:, None] + c34 * y1[:, None]
+            ref = refbind.image_texels(f, flip, False, uv)
+            np.testing.assert_allclose(ours, ref, rtol=0, atol=2e-6, err_msg=f"{f.name} flip={flip}")
