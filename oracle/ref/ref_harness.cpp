@@ -48,6 +48,7 @@
 #include "material/thinDielectric.hpp"
 #include "primitives/meshBVH.hpp"
 #include "primitives/triangleMesh.hpp"
+#include "mesh_io/meshLoader.hpp"
 #undef private
 #undef protected
 
@@ -384,6 +385,37 @@ int ref_image_texels(const char *path, int flip_y, int is_hdr, int n, const floa
       rgb[3 * k + 1] = c[1];
       rgb[3 * k + 2] = c[2];
     }
+    return 0;
+  } catch (...) {
+    return -1;
+  }
+}
+
+// loadOBJMesh (meshLoader.cpp:7-58): counts[0..3] = positions, normals,
+// uvs, faces; with non-null arrays also the data (faces: 3 indices each,
+// normal / uv indices -1 where absent).  Returns -1 when the load throws.
+int ref_obj_load(const char *path, int64_t *counts, float *pos, float *nrm, float *uv, int32_t *idx,
+                 int32_t *nidx, int32_t *uvidx) {
+  try {
+    auto mesh = loadOBJMesh(path, nullptr);
+    const MeshData &m = mesh->getMeshData();
+    counts[0] = (int64_t)m.positions.size();
+    counts[1] = (int64_t)m.normals.size();
+    counts[2] = (int64_t)m.uvs.size();
+    counts[3] = (int64_t)m.indices.size();
+    if (!pos) return 0;
+    for (size_t i = 0; i < m.positions.size(); ++i)
+      for (int a = 0; a < 3; ++a) pos[3 * i + a] = m.positions[i][a];
+    for (size_t i = 0; i < m.normals.size(); ++i)
+      for (int a = 0; a < 3; ++a) nrm[3 * i + a] = m.normals[i][a];
+    for (size_t i = 0; i < m.uvs.size(); ++i)
+      for (int a = 0; a < 2; ++a) uv[2 * i + a] = m.uvs[i][a];
+    for (size_t f = 0; f < m.indices.size(); ++f)
+      for (int k = 0; k < 3; ++k) {
+        idx[3 * f + k] = m.indices[f][k];
+        nidx[3 * f + k] = f < m.normalIndices.size() ? m.normalIndices[f][k] : -1;
+        uvidx[3 * f + k] = f < m.uvIndices.size() ? m.uvIndices[f][k] : -1;
+      }
     return 0;
   } catch (...) {
     return -1;

@@ -52,6 +52,7 @@ def load():
         lib.ref_render_time.argtypes = [C.c_void_p, C.POINTER(N.JobDesc), C.c_int]
         lib.ref_render_time.restype = C.c_double
         lib.ref_image_texels.argtypes = [C.c_char_p, C.c_int, C.c_int, C.c_int, f32p, f32p]
+        lib.ref_obj_load.argtypes = [C.c_char_p, C.POINTER(C.c_int64), f32p, f32p, f32p, i32p, i32p, i32p]
         _lib = lib
     return _lib
 
@@ -138,4 +139,20 @@ def image_texels(path, flip_y: bool, is_hdr: bool, uv: np.ndarray) -> np.ndarray
                                  _p(out, C.c_float))
     if rc != 0:
         raise RuntimeError(f"reference ImageTexture failed to load {path}")
+    return out
+
+
+def obj_load(path) -> dict:
+    """loadOBJMesh(path) through the harness: the MeshData arrays."""
+    lib = load()
+    counts = (C.c_int64 * 4)()
+    if lib.ref_obj_load(str(path).encode(), counts, None, None, None, None, None, None) != 0:
+        raise RuntimeError(f"reference loadOBJMesh failed on {path}")
+    nv, nn, nt, nf = list(counts)
+    out = {"positions": np.zeros((nv, 3), np.float32), "normals": np.zeros((nn, 3), np.float32),
+           "uvs": np.zeros((nt, 2), np.float32), "indices": np.zeros((nf, 3), np.int32),
+           "normal_indices": np.zeros((nf, 3), np.int32), "uv_indices": np.zeros((nf, 3), np.int32)}
+    lib.ref_obj_load(str(path).encode(), counts, _p(out["positions"], C.c_float), _p(out["normals"], C.c_float),
+                     _p(out["uvs"], C.c_float), _p(out["indices"], C.c_int32), _p(out["normal_indices"], C.c_int32),
+                     _p(out["uv_indices"], C.c_int32))
     return out
