@@ -1736,6 +1736,32 @@ void or_bsdf_sample(const pt_material_desc *md, int n, const float *wo, const fl
 // FrameBuffer::gaussianBlur (framebuffer.cpp:60-129) over a film laid out
 // [row][column][rgb] (row 0 = bottom, as pixel_color[j][i]).  Returns 0 when
 // it blurred, 1 when the reference would refuse the arguments (film copied).
+// A texture (pt_texture_desc) evaluated at n points (u, v) as the kernels'
+// ColorVariant lookups do.
+int or_tex_eval(const pt_texture_desc *d, int n, const float *uv, float *rgb) {
+  Tex T;
+  T.kind = d->kind;
+  T.c1 = V(d->color1[0], d->color1[1], d->color1[2]);
+  T.c2 = V(d->color2[0], d->color2[1], d->color2[2]);
+  T.scale = d->scale;
+  T.fractal = d->fractal;
+  if (d->kind == PT_TEX_IMAGE) {
+    if (!d->texels || d->width < 2 || d->height < 2) return -1;
+    T.w = d->width;
+    T.h = d->height;
+    T.texels.resize((size_t)T.w * T.h);
+    for (size_t i = 0; i < T.texels.size(); ++i)
+      T.texels[i] = V(d->texels[3 * i], d->texels[3 * i + 1], d->texels[3 * i + 2]);
+  }
+  for (int k = 0; k < n; ++k) {
+    const V c = tex_eval(T, uv[2 * k], uv[2 * k + 1]);
+    rgb[3 * k] = c.x;
+    rgb[3 * k + 1] = c.y;
+    rgb[3 * k + 2] = c.z;
+  }
+  return 0;
+}
+
 int or_gaussian_blur(const float *in, float *out, int W, int H, int kernel, float sigma) {
   if (kernel % 2 == 0 || kernel < 3 || !(sigma > 0.0f)) {
     std::memcpy(out, in, sizeof(float) * 3 * (size_t)W * H);

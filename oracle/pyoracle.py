@@ -38,6 +38,7 @@ def load():
                                        f32p, f32p, u32p]
         lib.or_render.argtypes = [C.c_void_p, C.POINTER(N.JobDesc), f32p, f32p, C.c_int, C.c_int]
         lib.or_gaussian_blur.argtypes = [f32p, f32p, C.c_int, C.c_int, C.c_int, C.c_float]
+        lib.or_tex_eval.argtypes = [C.POINTER(N.TextureDesc), C.c_int, f32p, f32p]
         _lib = lib
     return _lib
 
@@ -108,6 +109,25 @@ def bsdf_sample(mat, wo, nrm, front, uc, u):
                           _p(uc, C.c_float), _p(u, C.c_float), _p(ok, C.c_uint8), _p(wi, C.c_float),
                           _p(att, C.c_float), _p(pdf, C.c_float), _p(ty, C.c_uint32))
     return ok, wi, att, pdf, ty
+
+
+def tex_eval(kind: int, uv: np.ndarray, color1=(0, 0, 0), color2=(1, 1, 1), scale: float = 10.0,
+             fractal: int = 1, texels: np.ndarray | None = None) -> np.ndarray:
+    """A surface texture evaluated at each (u, v) (or_tex_eval)."""
+    d = N.TextureDesc()
+    d.kind, d.scale, d.fractal = kind, scale, fractal
+    d.color1[:] = list(color1)
+    d.color2[:] = list(color2)
+    keep = None
+    if texels is not None:
+        keep = np.ascontiguousarray(texels, np.float32)
+        d.texels = _p(keep, C.c_float)
+        d.height, d.width = keep.shape[0], keep.shape[1]
+    uv = np.ascontiguousarray(uv, np.float32).reshape(-1, 2)
+    out = np.zeros((uv.shape[0], 3), np.float32)
+    if load().or_tex_eval(C.byref(d), uv.shape[0], _p(uv, C.c_float), _p(out, C.c_float)) != 0:
+        raise ValueError("bad texture description")
+    return out
 
 
 def gaussian_blur(film, kernel, sigma):

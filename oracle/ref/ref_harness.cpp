@@ -391,6 +391,27 @@ int ref_image_texels(const char *path, int flip_y, int is_hdr, int n, const floa
   }
 }
 
+// CheckerTexture(c1, c2, scale) (kind 1) or NoiseTexture(scale, fractal)
+// (kind 2) sampled by its own getTexelColor (texture.cpp:151-193) at n
+// points (u, v).
+int ref_texture_eval(int kind, const float *c1, const float *c2, float scale, int fractal, int n, const float *uv,
+                     float *rgb) {
+  std::shared_ptr<Texture2D> tex;
+  if (kind == 1)
+    tex = std::make_shared<CheckerTexture>(gl::vec3(c1[0], c1[1], c1[2]), gl::vec3(c2[0], c2[1], c2[2]), scale);
+  else if (kind == 2)
+    tex = std::make_shared<NoiseTexture>(scale, fractal);
+  else
+    return -1;
+  for (int k = 0; k < n; ++k) {
+    gl::vec3 c = tex->getTexelColor(uv[2 * k], uv[2 * k + 1]);
+    rgb[3 * k] = c[0];
+    rgb[3 * k + 1] = c[1];
+    rgb[3 * k + 2] = c[2];
+  }
+  return 0;
+}
+
 // loadOBJMesh (meshLoader.cpp:7-58): counts[0..3] = positions, normals,
 // uvs, faces; with non-null arrays also the data (faces: 3 indices each,
 // normal / uv indices -1 where absent).  Returns -1 when the load throws.

@@ -52,6 +52,7 @@ def load():
         lib.ref_render_time.argtypes = [C.c_void_p, C.POINTER(N.JobDesc), C.c_int]
         lib.ref_render_time.restype = C.c_double
         lib.ref_image_texels.argtypes = [C.c_char_p, C.c_int, C.c_int, C.c_int, f32p, f32p]
+        lib.ref_texture_eval.argtypes = [C.c_int, f32p, f32p, C.c_float, C.c_int, C.c_int, f32p, f32p]
         lib.ref_obj_load.argtypes = [C.c_char_p, C.POINTER(C.c_int64), f32p, f32p, f32p, i32p, i32p, i32p]
         _lib = lib
     return _lib
@@ -155,4 +156,15 @@ def obj_load(path) -> dict:
     lib.ref_obj_load(str(path).encode(), counts, _p(out["positions"], C.c_float), _p(out["normals"], C.c_float),
                      _p(out["uvs"], C.c_float), _p(out["indices"], C.c_int32), _p(out["normal_indices"], C.c_int32),
                      _p(out["uv_indices"], C.c_int32))
+    return out
+
+
+def texture_eval(kind: int, c1, c2, scale: float, fractal: int, uv: np.ndarray) -> np.ndarray:
+    """CheckerTexture (kind 1) / NoiseTexture (kind 2).getTexelColor at each (u, v)."""
+    uv = np.ascontiguousarray(uv, np.float32).reshape(-1, 2)
+    a, b = np.asarray(c1, np.float32), np.asarray(c2, np.float32)
+    out = np.zeros((uv.shape[0], 3), np.float32)
+    if load().ref_texture_eval(kind, _p(a, C.c_float), _p(b, C.c_float), scale, fractal, uv.shape[0],
+                               _p(uv, C.c_float), _p(out, C.c_float)) != 0:
+        raise RuntimeError("unknown texture kind")
     return out

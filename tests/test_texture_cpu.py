@@ -80,3 +80,25 @@ def test_curves_build_and_render():
     t, prim = O.OracleScene(sc).trace_closest(np.array(rays, np.float32))
     curve_prims = set(range(3, 3 + 40))  # after the two rectangles and the sphere
     assert sum(int(p) in curve_prims for p in prim) >= 8
+
+
+def test_oracle_textures_match_reference_textures():
+    """The oracle's CheckerTexture / NoiseTexture evaluation against the
+    reference's own getTexelColor (texture.cpp:151-193, pattern.hpp:72-114)
+    through the harness, where it is built: bit for bit at random (u, v),
+    several scales and octave counts, including coordinates past the Perlin
+    lattice's period."""
+    from oracle.ref import refbind
+    if not refbind.available():
+        pytest.skip("reference harness not built")
+    rng = np.random.default_rng(4)
+    uv = rng.uniform(0.0, 1.0, (4000, 2)).astype(np.float32)
+    c1, c2 = (0.1, 0.2, 0.6), (0.9, 0.8, 0.2)
+    for scale in (1.0, 10.0, 37.5, 400.0):
+        ours = O.tex_eval(N.TEX_CHECKER, uv, c1, c2, scale)
+        ref = refbind.texture_eval(1, c1, c2, scale, 1, uv)
+        assert np.array_equal(ours, ref), scale
+        for fractal in (1, 3, 7):
+            ours = O.tex_eval(N.TEX_NOISE, uv, scale=scale, fractal=fractal)
+            ref = refbind.texture_eval(2, c1, c2, scale, fractal, uv)
+            assert np.array_equal(ours, ref), (scale, fractal)
