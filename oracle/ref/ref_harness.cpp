@@ -49,6 +49,8 @@
 #include "primitives/meshBVH.hpp"
 #include "primitives/triangleMesh.hpp"
 #include "mesh_io/meshLoader.hpp"
+#include "primitives/box.hpp"
+#include "primitives/curve.hpp"
 #undef private
 #undef protected
 
@@ -112,6 +114,8 @@ struct RefScene {
   // identification of hits: material instance -> (object index)
   std::vector<const Material *> obj_material;
   std::vector<int> obj_kind, obj_index, obj_prim_base;
+  // per object: a Box's six faces in its own order (to name the face hit)
+  std::vector<std::vector<std::shared_ptr<Hittable>>> box_faces;
   std::vector<std::shared_ptr<TriangleMesh>> meshes;  // by object, may be null
 };
 
@@ -129,7 +133,10 @@ void *ref_scene_create(const pt_scene_desc *d) {
   auto *S = new RefScene();
   S->bg = V3(d->bg_color);
   int n_tris = total_triangles_before(d, d->n_meshes);
+  const int n_boxes = d->boxes ? d->n_boxes : 0;
+  const int n_quads_all = d->n_quads + 6 * n_boxes;  // a box's faces follow the rectangles
   for (int o = 0; o < d->n_objects; ++o) {
+    S->box_faces.emplace_back();
     const pt_object_desc &od = d->objects[o];
     std::shared_ptr<Hittable> h;
     int mat_index = -1, prim_base = 0;
@@ -173,12 +180,27 @@ void *ref_scene_create(const pt_scene_desc *d) {
       if (q.flip_face) h = std::make_shared<FlipFace>(h);
       prim_base = n_tris + od.index;
       S->obj_material.push_back(mat.get());
+    } else if (od.kind == PT_OBJ_BOX) {
+      const pt_box_desc &b = d->boxes[od.index];
+      auto mat = make_material(d->materials[b.material]);
+      auto box = std::make_shared<Box>(V3(b.min_xyz), V3(b.max_xyz), mat);
+      S->box_faces.back() = box->_faces.getLists();
+      h = box;
+      prim_base = n_tris + d->n_quads + 6 * od.index;
+      S->obj_material.push_back(mat.get());
+    } else if (od.kind == PT_OBJ_CURVE) {
+      const pt_curve_desc &c = d->curves[od.index];
+      auto mat = make_material(d->materials[c.material]);
+      std::array<gl::vec3, 4> cps = {V3(c.cps[0]), V3(c.cps[1]), V3(c.cps[2]), V3(c.cps[3])};
+      h = std::make_shared<Curve>(cps, c.width0, c.width1, CurveType::Cylinder, mat);
+      prim_base = n_tris + n_quads_all + d->n_spheres + od.index;
+      S->obj_material.push_back(mat.get());
     } else {
       const pt_sphere_desc &s = d->spheres[od.index];
       auto mat = make_material(d->materials[s.material]);
       h = std::make_shared<Sphere>(V3(s.center), s.radius, mat);
       if (s.flip_face) h = std::make_shared<FlipFace>(h);
-      prim_base = n_tris + d->n_quads + od.index;
+      prim_base = n_tris + n_quads_all + od.index;
       S->obj_material.push_back(mat.get());
     }
     S->objects.addObject(h);
@@ -228,7 +250,17 @@ void ref_trace_closest(void *s, const float *rays, int n, float tmin, float tmax
     if (!hit) continue;
     for (size_t o = 0; o < S->obj_material.size(); ++o) {
       if (S->obj_material[o] != rec.material.get()) continue;
-      if (S->obj_kind[o] != PT_OBJ_MESH) {
+      if (S->obj_kind[o] == PT_OBJ_BOX) {
+        // the face the Box's ObjectList kept: the last one accepted (box.hpp:40-43)
+        float closest = tmax;
+        for (size_t f = 0; f < S->box_faces[o].size(); ++f) {
+          HitRecord tmp;
+          if (S->box_faces[o][f]->intersect(ray, tmp, tmin, closest)) {
+            closest = tmp.t;
+            prim_out[i] = S->obj_prim_base[o] + (int)f;
+          }
+        }
+      } else if (S->obj_kind[o] != PT_OBJ_MESH) {
         prim_out[i] = S->obj_prim_base[o];
       } else {
         const MeshBVHNode *root = S->meshes[o]->bvh.get();

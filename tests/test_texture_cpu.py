@@ -102,3 +102,32 @@ def test_oracle_textures_match_reference_textures():
             ours = O.tex_eval(N.TEX_NOISE, uv, scale=scale, fractal=fractal)
             ref = refbind.texture_eval(2, c1, c2, scale, fractal, uv)
             assert np.array_equal(ours, ref), (scale, fractal)
+
+
+def test_oracle_box_and_curve_hits_match_reference():
+    """Closest hits on Box objects (six rectangles, ObjectList rule) and on
+    Curve objects (cylinder segments) in the oracle against the reference's
+    own Box / Curve intersection (box.hpp, curve.hpp) under its BVHNode,
+    through the harness, where it is built: same primitive, same t."""
+    from oracle.ref import refbind
+    if not refbind.available():
+        pytest.skip("reference harness not built")
+    sc, cam = S.hair_curves(60, seed=3)
+    m = sc.add_material(N.LAMBERTIAN, [0.6, 0.5, 0.4])
+    sc.add_box((-0.7, 0.0, 0.3), (-0.3, 0.5, 0.7), m)
+    sc.add_box((0.2, 0.0, -0.6), (0.6, 0.3, -0.2), m)
+    rng = np.random.default_rng(8)
+    n = 8192
+    o = np.tile(cam["position"], (n, 1)) + rng.normal(0, 0.02, (n, 3))
+    d = np.stack([rng.uniform(-0.35, 0.35, n), rng.uniform(-0.45, 0.2, n), np.ones(n)], 1)
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    rays = np.concatenate([o, d], 1).astype(np.float32)
+    t_o, p_o = O.OracleScene(sc).trace_closest(rays)
+    t_r, p_r, _, _, _ = refbind.RefScene(sc).trace_closest(rays)
+    hit = p_r >= 0
+    assert hit.sum() > 2000
+    curve_base = len(sc.quads) + 6 * len(sc.boxes) + len(sc.spheres)
+    assert ((p_r >= curve_base) & hit).sum() > 200 and ((p_r >= len(sc.quads)) & (p_r < curve_base) & hit).sum() > 200
+    assert (p_o == p_r).mean() > 0.999
+    same = (p_o == p_r) & hit
+    assert np.array_equal(t_o[same], t_r[same])
