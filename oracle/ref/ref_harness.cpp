@@ -444,6 +444,26 @@ int ref_texture_eval(int kind, const float *c1, const float *c2, float scale, in
   return 0;
 }
 
+// FrameBuffer::gaussianBlur (framebuffer.cpp:60-129) of an H x W RGB image
+// given row by row ([row][column][channel], the framebuffer's [u][v]).
+void ref_gaussian_blur(const float *in, int W, int H, int kernel, float sigma, float *out) {
+  FrameBuffer fb((uint)W, (uint)H, 1, 1);
+  for (int i = 0; i < H; ++i)
+    for (int j = 0; j < W; ++j) {
+      const float *p = in + 3 * ((size_t)i * W + j);
+      fb.setPixelColor((uint)i, (uint)j, gl::vec3(p[0], p[1], p[2]));
+    }
+  fb.gaussianBlur(kernel, sigma);
+  for (int i = 0; i < H; ++i)
+    for (int j = 0; j < W; ++j) {
+      gl::vec3 c = fb.getPixelColor((uint)i, (uint)j);
+      float *q = out + 3 * ((size_t)i * W + j);
+      q[0] = c[0];
+      q[1] = c[1];
+      q[2] = c[2];
+    }
+}
+
 // loadOBJMesh (meshLoader.cpp:7-58): counts[0..3] = positions, normals,
 // uvs, faces; with non-null arrays also the data (faces: 3 indices each,
 // normal / uv indices -1 where absent).  Returns -1 when the load throws.

@@ -53,6 +53,7 @@ def load():
         lib.ref_render_time.restype = C.c_double
         lib.ref_image_texels.argtypes = [C.c_char_p, C.c_int, C.c_int, C.c_int, f32p, f32p]
         lib.ref_texture_eval.argtypes = [C.c_int, f32p, f32p, C.c_float, C.c_int, C.c_int, f32p, f32p]
+        lib.ref_gaussian_blur.argtypes = [f32p, C.c_int, C.c_int, C.c_int, C.c_float, f32p]
         lib.ref_obj_load.argtypes = [C.c_char_p, C.POINTER(C.c_int64), f32p, f32p, f32p, i32p, i32p, i32p]
         _lib = lib
     return _lib
@@ -167,4 +168,12 @@ def texture_eval(kind: int, c1, c2, scale: float, fractal: int, uv: np.ndarray) 
     if load().ref_texture_eval(kind, _p(a, C.c_float), _p(b, C.c_float), scale, fractal, uv.shape[0],
                                _p(uv, C.c_float), _p(out, C.c_float)) != 0:
         raise RuntimeError("unknown texture kind")
+    return out
+
+
+def gaussian_blur(img: np.ndarray, kernel: int, sigma: float) -> np.ndarray:
+    """FrameBuffer::gaussianBlur of an (H, W, 3) image through the harness."""
+    a = np.ascontiguousarray(img, np.float32)
+    out = np.zeros_like(a)
+    load().ref_gaussian_blur(_p(a, C.c_float), a.shape[1], a.shape[0], kernel, sigma, _p(out, C.c_float))
     return out

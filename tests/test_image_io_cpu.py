@@ -355,3 +355,19 @@ def test_reference_repository_pngs_decode_like_its_image_texture():
             ours = c12 * y2[:, None] + c34 * y1[:, None]
             ref = refbind.image_texels(f, flip, False, uv)
             np.testing.assert_allclose(ours, ref, rtol=0, atol=2e-6, err_msg=f"{f.name} flip={flip}")
+
+
+def test_oracle_blur_matches_reference_framebuffer():
+    """The oracle's gaussianBlur restatement (which the GPU kernel matches
+    bit for bit) against the reference's own FrameBuffer::gaussianBlur
+    through the harness, where it is built."""
+    import pytest
+    from oracle.ref import refbind
+    if not refbind.available():
+        pytest.skip("reference harness not built")
+    rng = np.random.default_rng(12)
+    for (h, w), k, sigma in (((23, 31), 3, 1.0), ((40, 17), 5, 2.5), ((9, 9), 7, 0.8), ((64, 48), 11, 3.0)):
+        img = rng.gamma(1.0, 1.0, (h, w, 3)).astype(np.float32)
+        ours = O.gaussian_blur(img, k, sigma)
+        ref = refbind.gaussian_blur(img, k, sigma)
+        assert np.array_equal(ours, ref), (h, w, k, sigma, np.abs(ours - ref).max())
