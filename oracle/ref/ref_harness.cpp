@@ -464,6 +464,20 @@ void ref_gaussian_blur(const float *in, int W, int H, int kernel, float sigma, f
     }
 }
 
+// FrameBuffer::writeToFile (framebuffer.cpp:27-58) of an H x W RGB film
+// given row by row: NaN -> 0, pow(1 / gamma), clamp, 8-bit truncation, PNG
+// flipped vertically on write.  Returns 0 on success.
+int ref_write_png(const float *in, int W, int H, float gamma, const char *path) {
+  FrameBuffer fb((uint)W, (uint)H, 1, 1);
+  for (int i = 0; i < H; ++i)
+    for (int j = 0; j < W; ++j) {
+      const float *p = in + 3 * ((size_t)i * W + j);
+      fb.setPixelColor((uint)i, (uint)j, gl::vec3(p[0], p[1], p[2]));
+    }
+  fb.writeToFile(path, gamma);
+  return 0;
+}
+
 // loadOBJMesh (meshLoader.cpp:7-58): counts[0..3] = positions, normals,
 // uvs, faces; with non-null arrays also the data (faces: 3 indices each,
 // normal / uv indices -1 where absent).  Returns -1 when the load throws.

@@ -54,6 +54,7 @@ def load():
         lib.ref_image_texels.argtypes = [C.c_char_p, C.c_int, C.c_int, C.c_int, f32p, f32p]
         lib.ref_texture_eval.argtypes = [C.c_int, f32p, f32p, C.c_float, C.c_int, C.c_int, f32p, f32p]
         lib.ref_gaussian_blur.argtypes = [f32p, C.c_int, C.c_int, C.c_int, C.c_float, f32p]
+        lib.ref_write_png.argtypes = [f32p, C.c_int, C.c_int, C.c_float, C.c_char_p]
         lib.ref_obj_load.argtypes = [C.c_char_p, C.POINTER(C.c_int64), f32p, f32p, f32p, i32p, i32p, i32p]
         _lib = lib
     return _lib
@@ -177,3 +178,9 @@ def gaussian_blur(img: np.ndarray, kernel: int, sigma: float) -> np.ndarray:
     out = np.zeros_like(a)
     load().ref_gaussian_blur(_p(a, C.c_float), a.shape[1], a.shape[0], kernel, sigma, _p(out, C.c_float))
     return out
+
+
+def write_png(film: np.ndarray, gamma: float, path) -> None:
+    """FrameBuffer::writeToFile of an (H, W, 3) film through the harness."""
+    a = np.ascontiguousarray(film, np.float32)
+    load().ref_write_png(_p(a, C.c_float), a.shape[1], a.shape[0], gamma, str(path).encode())

@@ -135,6 +135,25 @@ def make_images():
     np.savez_compressed(OUT / "image_roughglass.npz", mean=mean, var=var, width=48, height=48, spp=16, depth=6)
 
 
+def make_tonemap():
+    """A film with values past 1, NaN and +inf written by the reference's
+    FrameBuffer::writeToFile (gamma 2.2 and 1.0); the PNG's bytes (top row
+    first) are decoded back with the repository's PNG reader."""
+    import tempfile
+    rng = np.random.default_rng(31)
+    h, w = 48, 64
+    film = rng.uniform(0.0, 1.5, (h, w, 3)).astype(np.float32)
+    film[rng.integers(0, h, 20), rng.integers(0, w, 20), rng.integers(0, 3, 20)] = np.nan
+    film[rng.integers(0, h, 10), rng.integers(0, w, 10), rng.integers(0, 3, 10)] = np.inf
+    out = {"film": film}
+    with tempfile.TemporaryDirectory() as td:
+        for gamma in (2.2, 1.0):
+            p = Path(td) / "tm.png"
+            R.write_png(film, gamma, p)
+            out[f"rgb8_gamma_{gamma}"] = np.rint(N.load_image(p, flip_y=True) * 255.0).astype(np.uint8)
+    np.savez_compressed(OUT / "tonemap.npz", **out)
+
+
 if __name__ == "__main__":
     if not R.available():
         raise SystemExit("build oracle/_ref first: oracle/ref/build_ref.sh")
@@ -142,5 +161,6 @@ if __name__ == "__main__":
     make_trace()
     make_bsdf()
     make_images()
+    make_tonemap()
     for p in sorted(OUT.glob("*.npz")):
         print(p.name, p.stat().st_size)

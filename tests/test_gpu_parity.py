@@ -203,3 +203,19 @@ def test_render_deterministic(renderer):
     b = renderer.render(job)
     assert np.array_equal(a, b)
     renderer.release(sid)
+
+
+@pytest.mark.parametrize("gamma", [2.2, 1.0])
+def test_tonemap_matches_reference_write_to_file(renderer, golden, gamma):
+    """pt_tonemap against the bytes the reference's FrameBuffer::writeToFile
+    wrote for the same film (NaN -> 0, pow(1/gamma), clamp, truncation, rows
+    flipped; fixture from tests/golden/make_golden.py).  A CUDA powf result
+    one ulp from the host's can move a truncated byte by one."""
+    g = golden("tonemap.npz")
+    ours = renderer.tonemap(g["film"], gamma).astype(np.int32)
+    ref = g[f"rgb8_gamma_{gamma}"].astype(np.int32)
+    diff = np.abs(ours - ref)
+    assert diff.max() <= 1
+    assert (diff > 0).mean() < 0.005
+    nan = np.isnan(g["film"][::-1])
+    assert (ours[nan] == 0).all()

@@ -371,3 +371,15 @@ def test_oracle_blur_matches_reference_framebuffer():
         ours = O.gaussian_blur(img, k, sigma)
         ref = refbind.gaussian_blur(img, k, sigma)
         assert np.array_equal(ours, ref), (h, w, k, sigma, np.abs(ours - ref).max())
+
+
+def test_tonemap_rule_matches_reference_fixture(golden):
+    """The tone map rule pt_tonemap implements -- NaN -> 0, pow(v, 1/gamma),
+    clamp to [0, 1], x 255 truncated, rows flipped (framebuffer.cpp:27-58) --
+    restated in float32 reproduces the bytes the reference's writeToFile
+    wrote (tests/golden/tonemap.npz)."""
+    f = golden("tonemap.npz")["film"]
+    for gamma in (2.2, 1.0):
+        v = np.where(np.isnan(f), np.float32(0), np.power(f, np.float32(1.0) / np.float32(gamma)))
+        b = (np.clip(v, 0, 1) * np.float32(255)).astype(np.uint8)[::-1]
+        assert np.array_equal(b, golden("tonemap.npz")[f"rgb8_gamma_{gamma}"])
