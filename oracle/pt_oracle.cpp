@@ -283,7 +283,8 @@ static float hair_at(const Material &m, V wol, V wil) {  // hairPDF.cpp:101-152
 }
 
 bool mat_scatter(const Material &m, V ray_dir, const Hit &rec, Scatter &s, float uc, float u0, float u1) {
-  // HairMarschner's frame is the hair tangent when set (hairMarsch.cpp:12-19)
+  // HairMarschner::scatter samples in the hair tangent's frame when set
+  // (hairMarsch.cpp:12-24); its attenuation is mat_f, framed by the normal
   const V n = (m.type == PT_MAT_HAIR && rec.has_tangent) ? rec.tangent : rec.normal;
   const V wo = -ray_dir.normalize();
   switch (m.type) {
@@ -465,8 +466,9 @@ bool mat_scatter(const Material &m, V ray_dir, const Hit &rec, Scatter &s, float
 }
 
 V mat_f(const Material &m, V wo, V wi, const Hit &rec) {
-  // HairMarschner's frame is the hair tangent when set (hairMarsch.cpp:12-19)
-  const V n = (m.type == PT_MAT_HAIR && rec.has_tangent) ? rec.tangent : rec.normal;
+  // every BSDF in the normal's frame: HairMarschner::f and scatter_pdf too,
+  // on a curve as well (hairMarsch.hpp:49, hairMarsch.cpp:115)
+  const V n = rec.normal;
   switch (m.type) {
   case PT_MAT_LAMBERTIAN:
     return base_color(m) * (float)(1.0f / PI);
@@ -516,8 +518,9 @@ V mat_f(const Material &m, V wo, V wi, const Hit &rec) {
 }
 
 float mat_pdf(const Material &m, V wo, V wi, const Hit &rec) {
-  // HairMarschner's frame is the hair tangent when set (hairMarsch.cpp:12-19)
-  const V n = (m.type == PT_MAT_HAIR && rec.has_tangent) ? rec.tangent : rec.normal;
+  // every BSDF in the normal's frame: HairMarschner::f and scatter_pdf too,
+  // on a curve as well (hairMarsch.hpp:49, hairMarsch.cpp:115)
+  const V n = rec.normal;
   switch (m.type) {
   case PT_MAT_LAMBERTIAN:
     return cosine_pdf_at(n, wi);

@@ -570,10 +570,10 @@ __device__ __forceinline__ void next_event(const SceneView &S, const DeviceJob &
         f = v3(phase);
         pb = phase;
       } else {
-        // HairMarschner on a curve uses the curve tangent as its frame
-        // (hairMarsch.cpp:12-19), every other BSDF the shading normal
-        const V3 bn = ((FAM == 6 || FAM < 0) && sf.has_tan && S.materials[mat].type == PT_MAT_HAIR) ? sf.tan : sf.n;
-        bsdf_eval_t<FAM>(S.materials[mat], wo, wl, bn, sf.front, f, pb);
+        // f and scatter_pdf: every BSDF in the shading normal's frame --
+        // HairMarschner's too (hairMarsch.hpp:49, hairMarsch.cpp:115), even on
+        // a curve, whose tangent only frames its sampling
+        bsdf_eval_t<FAM>(S.materials[mat], wo, wl, sf.n, sf.front, f, pb);
         if ((FAM == 0 || FAM < 0) && tex_alb) f = alb * PT_INV_PI_F;  // textured Lambertian albedo
       }
       float w = mis ? power_heuristic((float)LN, pdf_l, 1.f, pb) : 1.f;
@@ -744,8 +744,12 @@ __global__ void __launch_bounds__(128, shade_min_blocks(FAM, MJ)) k_shade(SceneV
           float u0 = sampler_dim(Jp, dim0 + 1, P.halton_index, P.key, P.pix, P.k);
           float u1 = sampler_dim(Jp, dim0 + 2, P.halton_index, P.key, P.pix, P.k);
           wo = -normalize(d);
-          const V3 bn = ((FAM == 6 || FAM < 0) && sf.has_tan && M.type == PT_MAT_HAIR) ? sf.tan : sf.n;
-          BsdfSample bs = bsdf_sample_t<FAM>(M, wo, bn, sf.front, uc, u0, u1);
+          // HairMarschner::scatter on a curve samples the direction and its
+          // pdf in the curve tangent's frame (hairMarsch.cpp:12-24) while its
+          // attenuation is f(), framed by the normal (hairMarsch.hpp:49)
+          const bool hair_tan = (FAM == 6 || FAM < 0) && sf.has_tan && M.type == PT_MAT_HAIR;
+          BsdfSample bs = bsdf_sample_t<FAM>(M, wo, hair_tan ? sf.tan : sf.n, sf.front, uc, u0, u1);
+          if (hair_tan && bs.ok) bs.att = hair_f(M, wo, bs.wi, sf.n);
           if ((FAM == 0 || FAM < 0) && M.type == PT_MAT_LAMBERTIAN && mat_texture(M)) {
             // Lambertian with a ColorVariant texture: albedo at the hit's
             // texCoords (material.hpp:100, 133)

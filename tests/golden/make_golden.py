@@ -133,6 +133,14 @@ def make_images():
     job = N.job_desc(0, cam, 48, 48, 4, 4, 6, seed=4)
     mean, var = rs.render(job)
     np.savez_compressed(OUT / "image_roughglass.npz", mean=mean, var=var, width=48, height=48, spp=16, depth=6)
+    # hair on curves (HairMarschner framed by the curve tangent for sampling,
+    # by the normal for f / scatter_pdf), explicit sigma_a
+    sc, cam = S.hair_curves(40, seed=2)
+    sc.materials = [(t, ([0.25, 0.45, 0.9] + list(p[3:])) if t == N.HAIR else p, 0 if t == N.HAIR else f)
+                    for t, p, f in sc.materials]
+    job = N.job_desc(0, cam, 24, 24, 16, 16, 6, seed=3)
+    mean, var = R.RefScene(sc).render(job)
+    np.savez_compressed(OUT / "image_haircurves.npz", mean=mean, var=var, width=24, height=24, spp=256, depth=6)
 
 
 def make_tonemap():

@@ -101,3 +101,18 @@ def test_hair_curves_match_oracle(renderer, estimator):
     both = (prim == prim_o) & (prim >= 0)
     assert np.allclose(t[both], t_o[both], rtol=1e-5)
     assert (prim >= 3).sum() > 100  # the rays do hit curves
+
+
+def test_hair_curves_match_reference_image(renderer, golden):
+    """The GPU render of hair on curves (explicit sigma_a) against the
+    reference's own render (fixture): image means within 3 sigma."""
+    sc, cam = S.hair_curves(40, seed=2)
+    sc.materials = [(t, ([0.25, 0.45, 0.9] + list(p[3:])) if t == N.HAIR else p, 0 if t == N.HAIR else f)
+                    for t, p, f in sc.materials]
+    g = golden("image_haircurves.npz")
+    sid = renderer.upload(sc)
+    film = renderer.render(N.job_desc(sid, cam, 24, 24, 16, 16, 6, seed=3))
+    renderer.release(sid)
+    se = np.sqrt(2.0 * g["var"].reshape(-1, 3).sum(0) / 256) / (24 * 24)
+    z = (film.reshape(-1, 3).mean(0) - g["mean"].reshape(-1, 3).mean(0)) / se
+    assert np.all(np.abs(z) < 3.0), z

@@ -150,3 +150,24 @@ def test_mis_estimator_converges_to_reference(golden):
     m, v = O.render(sc, job)
     z = _img_z(m, v, g["mean"], g["var"], 64)
     assert np.all(np.abs(z) < 3.5), z
+
+
+def _hair_explicit_sigma():
+    sc, cam = S.hair_curves(40, seed=2)
+    sc.materials = [(t, ([0.25, 0.45, 0.9] + list(p[3:])) if t == N.HAIR else p, 0 if t == N.HAIR else f)
+                    for t, p, f in sc.materials]
+    return sc, cam
+
+
+def test_hair_on_curves_matches_reference(golden):
+    """HairMarschner on curves: direction and pdf sampled in the curve
+    tangent's frame, f() and scatter_pdf() in the normal's frame, as the
+    reference does (hairMarsch.cpp:12-24 and 115, hairMarsch.hpp:49).  The
+    oracle's image mean equals the reference render's (fixture written by the
+    reference through the harness) within 3 sigma per channel."""
+    g = golden("image_haircurves.npz")
+    sc, cam = _hair_explicit_sigma()
+    job = N.job_desc(0, cam, 24, 24, 16, 16, 6, seed=3)
+    m, v = O.render(sc, job)
+    z = _img_z(m, v, g["mean"], g["var"], 256)
+    assert np.all(np.abs(z) < 3.0), z
