@@ -54,3 +54,27 @@ def rel_close(a, b, rtol=1e-4, atol=1e-6):
     both_nan = np.isnan(a) & np.isnan(b)
     ok = np.abs(a - b) <= atol + rtol * np.abs(b)
     return np.all(ok | both_nan)
+
+
+def material_mix_for_reference():
+    """The 64-sphere material mix (Disney, hair, thin dielectric, Phong,
+    Lambertian; 4 sphere and 2 area lights) as the reference renders it
+    finitely through the harness: no medium (the harness builds none), hair
+    with an explicit sigma_a instead of melanin, and each Phong replaced by a
+    grey Lambertian -- the reference's Phong::scatter leaves pdf_val = 0 on
+    its diffuse branch (material.hpp:355-365) and getRayColor divides by it,
+    which writes inf/NaN into about a fifth of this image's pixels."""
+    from pathtracer_gb300 import native as N
+    from pathtracer_gb300 import scene as S
+
+    sc, cam = S.material_divergence(2, seed=3, aspect=1.0)
+    sc.medium = None
+    mats = []
+    for t, p, f in sc.materials:
+        if t == N.PHONG:
+            t, p, f = N.LAMBERTIAN, [0.5, 0.5, 0.5], 0
+        elif t == N.HAIR:
+            p, f = [0.3, 0.5, 0.9] + list(p[3:]), 0
+        mats.append((t, p, f))
+    sc.materials = mats
+    return sc, cam

@@ -141,6 +141,15 @@ def make_images():
     job = N.job_desc(0, cam, 24, 24, 16, 16, 6, seed=3)
     mean, var = R.RefScene(sc).render(job)
     np.savez_compressed(OUT / "image_haircurves.npz", mean=mean, var=var, width=24, height=24, spp=256, depth=6)
+    # every material family of the mix scene at once (tests/conftest.py's
+    # material_mix_for_reference says what was changed for the reference)
+    sys.path.insert(0, str(REPO / "tests"))
+    from conftest import material_mix_for_reference
+    sc, cam = material_mix_for_reference()
+    job = N.job_desc(0, cam, 32, 32, 8, 8, 6, seed=3)
+    mean, var = R.RefScene(sc).render(job)
+    assert np.isfinite(mean).all()
+    np.savez_compressed(OUT / "image_materials.npz", mean=mean, var=var, width=32, height=32, spp=64, depth=6)
 
 
 def make_tonemap():

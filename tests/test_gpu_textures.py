@@ -116,3 +116,19 @@ def test_hair_curves_match_reference_image(renderer, golden):
     se = np.sqrt(2.0 * g["var"].reshape(-1, 3).sum(0) / 256) / (24 * 24)
     z = (film.reshape(-1, 3).mean(0) - g["mean"].reshape(-1, 3).mean(0)) / se
     assert np.all(np.abs(z) < 3.0), z
+
+
+def test_material_mix_matches_reference_image(renderer, golden):
+    """Every surface family of the mix scene on the GPU (Disney, hair, thin
+    dielectric, Lambertian; sphere and area lights) against the reference's
+    own render (fixture): image means within 3 sigma per channel."""
+    from conftest import material_mix_for_reference
+
+    g = golden("image_materials.npz")
+    sc, cam = material_mix_for_reference()
+    sid = renderer.upload(sc)
+    film = renderer.render(N.job_desc(sid, cam, 32, 32, 8, 8, 6, seed=3))
+    renderer.release(sid)
+    se = np.sqrt(2.0 * g["var"].reshape(-1, 3).sum(0) / 64) / (32 * 32)
+    z = (film.reshape(-1, 3).mean(0) - g["mean"].reshape(-1, 3).mean(0)) / se
+    assert np.all(np.abs(z) < 3.0), z
