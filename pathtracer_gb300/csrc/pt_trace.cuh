@@ -381,7 +381,12 @@ __device__ __forceinline__ bool trav_node(const SceneView &S, TravRay &R, int32_
   return true;
 }
 
-// One traversal step of one ray: a node visit or a leaf test.  Returns true
+// One traversal step of one ray: a node visit or the test of ONE item of the
+// current leaf (the leaf reference then advances to the leaf's next item, in
+// item order, so hits and their order are those of a whole-leaf test).  The
+// short step keeps a persistent warp's lanes close: a lane in a node and a
+// lane in a 4-item leaf cost one node visit + one item test per turn, not a
+// node visit + the leaf's whole loop.  Returns true
 // when the ray is finished: closest -> R.found / R.hit hold the nearest hit;
 // any -> R.found = occluded.  *err is set when the stack would overflow or
 // the iteration cap is reached (never expected); the ray is then finished
@@ -394,11 +399,14 @@ __device__ __forceinline__ bool trav_step(const SceneView &S, TravRay &R, int32_
   }
   if (R.ref == PT_REF_EMPTY) return true;
   if (ref_is_node(R.ref)) return !trav_node<ANY>(S, R, stack, stride, err);
-  if (test_leaf<ANY, CURVES>(S, R.ref, R.o, R.d, R.dn, R.tmin, R.tmax, R.hit, R.time)) {
+  // one leaf item per step, the leaf's items in order
+  const int32_t code = ~R.ref;
+  const int32_t first = code >> 3, count = (code & 7) + 1;
+  if (test_leaf<ANY, CURVES>(S, leaf_ref(first, 1), R.o, R.d, R.dn, R.tmin, R.tmax, R.hit, R.time)) {
     R.found = true;
     if (ANY) return true;
   }
-  R.ref = trav_pop(R, stack, stride);
+  R.ref = count > 1 ? leaf_ref(first + 1, count - 1) : trav_pop(R, stack, stride);
   return false;
 }
 
