@@ -49,7 +49,7 @@ FALLBACK_HBM_GBS = 6800.0
 # ncu DRAM bytes (read + write) of the traversal kernels of one rough-glass
 # wave of 16.8 M paths (16 spp of every pixel) and their launch count
 # (closest, paired and shadow launches; profiles/ncu_traffic_rough_glass_1024_16spp.md)
-NCU_TRAVERSAL_BYTES_16SPP, NCU_TRAVERSAL_LAUNCHES_16SPP = 6.8856e9, 21
+NCU_TRAVERSAL_BYTES_16SPP, NCU_TRAVERSAL_LAUNCHES_16SPP = 6.9185e9, 21
 
 
 def parse():

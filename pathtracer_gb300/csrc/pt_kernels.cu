@@ -184,7 +184,7 @@ __global__ void __launch_bounds__(128) k_trace_shadow(SceneView S, Queues Q, int
   int rays = 0;
   for (;;) {
     unsigned idle = __ballot_sync(0xffffffffu, !active);
-    if (!exhausted && __popc(idle) >= PT_FETCH_IDLE) {
+    if (!exhausted && __popc(idle) >= PT_FETCH_IDLE_SHADOW) {
       const int k = __popc(idle);
       int base = 0;
       if (lane == 0) base = atomicAdd(fetch, k);

@@ -292,6 +292,11 @@ __global__ void k_camera(DeviceJob J0, JobTable T, Queues Q, long long g0, int n
 // rays from the queue with one atomic.  Incoherent rays of very different
 // lengths then no longer hold a warp until its longest ray ends.
 #define PT_FETCH_IDLE 16
+// Shadow rays refill sooner (8 idle lanes): an any-hit ray's length varies
+// more (an early blocker ends it), and on the rough-glass workload the
+// shadow launches ran 274 -> 253 ms over 8 steps with 8 instead of 16,
+// while closest-hit launches on the Cornell box were slower with 8.
+#define PT_FETCH_IDLE_SHADOW 8
 
 __device__ __forceinline__ unsigned lanemask_lt() {
   return (1u << (threadIdx.x & 31)) - 1u;
