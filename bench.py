@@ -5,7 +5,12 @@ Workload (default): the rough-glass scene -- a seeded displaced icosphere of
 1.5, alpha 0.05) over a GGX conductor ground (alpha 0.2), lit by a seeded
 1024x512 FP32 HDRI (sky gradient + 3 Gaussian sun lobes, peak 5e3), rendered
 at 1024x1024, 256 spp (16x16 grid), depth 16, Russian roulette from depth 4,
-NEE+MIS with the luminance alias table, Owen-scrambled Halton sampler.
+Owen-scrambled Halton sampler.  The estimator is the drop-in's: REF_NEE
+(getRayColor of maxdepth_nee.hpp restated: 4 light samples per vertex,
+uniform-sphere environment sampling), the estimator the CPU arm runs, so the
+GPU/CPU ratio compares one algorithm.  ``nee_mis`` reports the same steps
+with NEE+MIS and the luminance alias table beside it, with its own CPU
+figure from the oracle's iterative NEE+MIS.
 One step = 16 of the 256 samples per pixel for every pixel (16.8 M paths,
 one wave), so every kernel launch of the timed region runs alone and its
 CUDA-event duration is the kernel's (the roofline).  ``per_call`` reports
@@ -17,6 +22,9 @@ sets), how a full frame is rendered in practice.
   e2e    the same metric through the public C-ABI call pt_render with a
          pinned HOST film: the job descriptor and offset table go host->device
          and the 12.6 MB film device->host inside every step.
+  roofline  the dominant stage (traversal) as the contract's single kernel
+         figure, and under ``stages`` every queue stage's algorithmic bytes
+         (unit costs in STAGE_UNIT_BYTES) over its CUDA-event time.
 
 ``--impl reference`` times the reference algorithm on the host cores: the
 CPU restatement of the reference integrator (oracle/pt_oracle.cpp, REF_NEE,
@@ -46,10 +54,24 @@ import numpy as np  # noqa: E402
 
 PEAKS = REPO / "MEASURED_PEAKS.json"
 FALLBACK_HBM_GBS = 6800.0
-# ncu DRAM bytes (read + write) of the traversal kernels of one rough-glass
-# wave of 16.8 M paths (16 spp of every pixel) and their launch count
-# (closest, paired and shadow launches; profiles/ncu_traffic_rough_glass_1024_16spp.md)
-NCU_TRAVERSAL_BYTES_16SPP, NCU_TRAVERSAL_LAUNCHES_16SPP = 6.9185e9, 21
+# ncu DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of all
+# traversal launches (closest, paired, shadow) of one step of 16 spp of every
+# pixel, per (workload, estimator); from a one-pass ncu capture of the same
+# bench command
+NCU_TRAVERSAL_BYTES_PER_STEP = {("rough_glass", 1): 6.9185e9}
+# Algorithmic queue bytes per unit, by stage: the per-vertex 192 B, per
+# shadow ray 88 B and per path 24 B of the queue model, each byte charged to
+# the stage that moves it:
+#   camera    72 B per path: RayQueue record written (32) + path state written (40)
+#   traversal 48 B per closest-hit ray: ray read (32) + hit written (16);
+#             44 B per shadow ray: ShadowQueue record read
+#   sort      16 B per closest-hit ray: key + index written and read (8 x 2)
+#   shade     128 B per path vertex: hit read (16) + path state read and written (80)
+#             + continuation RayQueue record written (32);
+#             44 B per shadow ray: ShadowQueue record written
+#   film      24 B per path: FP32 RGB read-modify-write
+STAGE_UNIT_BYTES = {"camera": {"paths": 72}, "traversal": {"rays": 48, "shadow_rays": 44},
+                    "sort": {"rays": 16}, "shade": {"segments": 128, "shadow_rays": 44}, "film": {"paths": 24}}
 
 
 def parse():
@@ -59,6 +81,8 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="rough_glass", choices=["rough_glass", "cornell", "divergence"])
+    ap.add_argument("--estimator", default="ref_nee", choices=["ref_nee", "nee_mis"],
+                    help="ref_nee: the drop-in's estimator (also the CPU arm's); nee_mis: NEE+MIS + alias env")
     ap.add_argument("--spp-per-step", type=int, default=16)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-forms", action="store_true", help="skip the batched and served forms")
@@ -74,15 +98,27 @@ def parse():
 
 WORKLOADS = {
     # name: (width, height, spp_x, spp_y, depth, rr_start, estimator, sampler, env_sampling, description)
-    "rough_glass": dict(W=1024, H=1024, sx=16, sy=16, depth=16, rr=4, est=1, sampler=2, env=1,
+    "rough_glass": dict(W=1024, H=1024, sx=16, sy=16, depth=16, rr=4, est=0, sampler=2, env=0,
                         desc="rough-glass displaced icosphere (1,310,720 tris) + conductor ground + "
                              "1024x512 HDRI, 1024x1024, 256 spp, depth 16, RR from 4"),
-    "cornell": dict(W=256, H=256, sx=8, sy=8, depth=8, rr=-1, est=1, sampler=2, env=0,
+    "cornell": dict(W=256, H=256, sx=8, sy=8, depth=8, rr=-1, est=0, sampler=2, env=0,
                     desc="Cornell box + 5120-tri GGX gold icosphere, 256x256, 64 spp, depth 8"),
-    "divergence": dict(W=1920, H=1080, sx=16, sy=8, depth=12, rr=-1, est=1, sampler=3, env=0,
+    "divergence": dict(W=1920, H=1080, sx=16, sy=8, depth=12, rr=-1, est=0, sampler=3, env=0,
                        desc="64 icospheres x 20480 tris, 5 material families, homogeneous medium, "
                             "1920x1080, 128 spp, depth 12, stratified"),
 }
+
+
+ESTIMATORS = {"ref_nee": dict(est=0, env=0, name="REF_NEE (maxdepth_nee.hpp restated), uniform-sphere env sampling"),
+              "nee_mis": dict(est=1, env=1, name="NEE+MIS (power heuristic), luminance alias-table env sampling")}
+
+
+def workload(name: str, estimator: str) -> dict:
+    """The workload's settings with the estimator's (est, env) fields."""
+    wl = dict(WORKLOADS[name])
+    e = ESTIMATORS[estimator]
+    wl.update(est=e["est"], env=e["env"], est_name=e["name"])
+    return wl
 
 
 def sample_chunk(step: int, rank: int, world: int, n_chunks: int) -> int:
@@ -167,6 +203,23 @@ class ClockSampler:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
                 "samples": len(sm)}
+
+
+def stage_roofline(prof: dict, tot: dict, peak: float) -> dict:
+    """Per queue stage: algorithmic bytes (STAGE_UNIT_BYTES x the stage's unit
+    counts over the timed steps), CUDA-event milliseconds, GB/s and the
+    fraction of the HBM peak.  traversal = the trace and shadow stages
+    (closest, paired and shadow launches + resolve)."""
+    counts = {"paths": tot["paths"], "segments": tot["segments"], "rays": tot["rays"], "shadow_rays": tot["shadow"]}
+    ms = {"camera": prof["camera"][0], "traversal": prof["trace"][0] + prof["shadow"][0], "sort": prof["sort"][0],
+          "shade": prof["shade"][0], "film": prof["film"][0]}
+    out = {}
+    for st, units in STAGE_UNIT_BYTES.items():
+        b = float(sum(u * counts[c] for c, u in units.items()))
+        gbs = b / (ms[st] / 1e3) / 1e9 if ms[st] > 0 else None
+        out[st] = {"bytes": b, "ms": ms[st], "achieved_gbs": gbs, "frac": gbs / peak if gbs else None,
+                   "unit_bytes": units}
+    return out
 
 
 def cpu_paths_per_sec(osc, cam, wl, estimator, threads, target_s=12.0, max_px=1024):
@@ -399,7 +452,7 @@ def converged_rmse(r, sid, cam, wl, k_step: int, win: int = 64, ref_grid: int = 
 
 
 def run_reference(args, rank, world):
-    wl = WORKLOADS[args.workload]
+    wl = workload(args.workload, args.estimator)
     if rank != 0:
         return
     from oracle import pyoracle as O
@@ -410,7 +463,7 @@ def run_reference(args, rank, world):
     vals = []
     sample = ""
     for i in range(args.warmup + args.steps):
-        v, sample, _ = cpu_paths_per_sec(osc, cam, wl, 0, threads,
+        v, sample, _ = cpu_paths_per_sec(osc, cam, wl, wl["est"], threads,
                                          target_s=max(4.0, 90.0 / (args.steps + args.warmup)))
         if i >= args.warmup:
             vals.append(v)
@@ -419,7 +472,7 @@ def run_reference(args, rank, world):
         "impl": "reference", "metric": "paths/s", "value": value, "unit": "paths/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene generator)",
-        "config": {"workload": wl["desc"], "estimator": "REF_NEE (maxdepth_nee.hpp restated)"},
+        "config": {"workload": wl["desc"], "estimator": wl["est_name"]},
         "cpu_baseline": {"value": value, "unit": "paths/s", "cores": threads, "kind": "port",
                          "sample": sample + "; oracle/pt_oracle.cpp, the CPU restatement of the reference path"},
         "e2e": {"value": value, "unit": "paths/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -432,7 +485,7 @@ def run_ours(args, rank, world, local_rank):
 
     from pathtracer_gb300 import native as N
 
-    wl = WORKLOADS[args.workload]
+    wl = workload(args.workload, args.estimator)
     torch.cuda.set_device(local_rank)
     r = N.Renderer(local_rank)
     sc, cam = build_scene(args.workload)
@@ -519,11 +572,6 @@ def run_ours(args, rank, world, local_rank):
 
     if rank != 0:
         return
-    # ---- roofline of the dominant stage (CUDA events on the library stream):
-    # traversal = closest-hit, paired and shadow-ray launches (+ the shadow
-    # resolve), or shading
-    trav_ms = prof["trace"][0] + prof["shadow"][0]
-    dom = "traversal" if trav_ms >= prof["shade"][0] else "shade"
     peak = None
     peak_src = "fallback"
     if PEAKS.exists():
@@ -534,20 +582,22 @@ def run_ours(args, rank, world, local_rank):
             peak = None
     if peak is None:
         peak = FALLBACK_HBM_GBS
-    # algorithmic bytes per unit (per ray for the traversal stages, per path
-    # vertex for shade): queue records read and written
-    alg_bytes = {"traversal": 48.0 * tot["rays"] + 88.0 * tot["shadow"], "shade": 192.0 * tot["segments"]}
-    dom_ms = trav_ms if dom == "traversal" else prof["shade"][0]
-    achieved = alg_bytes[dom] / (dom_ms / 1e3) / 1e9
+    stages = stage_roofline(prof, tot, peak)
+    # the dominant stage (CUDA events on the library stream): traversal =
+    # closest-hit, paired and shadow-ray launches (+ the shadow resolve)
+    dom = max(("traversal", "shade"), key=lambda kk: stages[kk]["ms"])
+    dom_ms = stages[dom]["ms"]
+    achieved = stages[dom]["achieved_gbs"]
     trav_launches = prof["trace"][1] + prof["shadow"][1]
     launches = sum(v[1] for v in prof.values())
     step_bytes_gbs = tot["bytes"] / (t_dev / 1e3) / 1e9
+    ncu_bytes = NCU_TRAVERSAL_BYTES_PER_STEP.get((args.workload, wl["est"])) if k == 16 else None
     line = {
         "metric": "paths/s", "value": value, "unit": "paths/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t_dev / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene generator, no assets)",
         "config": {"workload": wl["desc"], "step": f"{k} spp x {W}x{H} px = {W * H * k} paths",
-                   "estimator": "NEE+MIS", "triangles": info["triangles"], "bvh4_nodes": info["bvh4_nodes"],
+                   "estimator": wl["est_name"], "triangles": info["triangles"], "bvh4_nodes": info["bvh4_nodes"],
                    "bvh": "BVH4 collapsed from the reference's own trees (the library default)",
                    "l2": "inputs larger than L2: BVH + leaves "
                          f"{info['device_bytes'] / 1e6:.0f} MB and ~{tot['bytes'] / args.steps / 1e9:.1f} GB of "
@@ -557,20 +607,25 @@ def run_ours(args, rank, world, local_rank):
         "e2e": {"value": e2e_val, "unit": "paths/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm",
-                     "kernel": ("k_trace_closest / k_trace_pair / k_trace_shadow (traversal stage)"
-                                if dom == "traversal" else "k_shade"),
+                     "kernel": ("k_trace_closest / k_trace_pair / k_trace_shadow + k_shadow_resolve (traversal stage)"
+                                if dom == "traversal" else "k_shade (shade stage)"),
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_source": peak_src,
-                     "traffic": (NCU_TRAVERSAL_BYTES_16SPP / NCU_TRAVERSAL_LAUNCHES_16SPP
-                                 if args.workload == "rough_glass" and dom == "traversal" and k % 16 == 0
-                                 and NCU_TRAVERSAL_BYTES_16SPP else None),
-                     "traffic_note": "ncu dram__bytes_read.sum + dram__bytes_write.sum per traversal launch "
-                                     "(all traversal launches of a 16.8 M-path wave), bytes",
-                     "algorithmic_bytes_note": "48 B per closest-hit ray (ray 32 B read, hit 16 B written) + "
-                                               "88 B per shadow ray (ShadowQueue record written and read)",
+                     "traffic": (ncu_bytes if ncu_bytes and dom == "traversal" else None),
+                     "traffic_unit": "bytes per step: ncu dram__bytes_read.sum + dram__bytes_write.sum summed over "
+                                     "all traversal launches of one step (achieved is per step too: the stage's "
+                                     "algorithmic bytes per step over its time per step)",
+                     "algorithmic_bytes_per_step": stages[dom]["bytes"] / args.steps,
+                     "algorithmic_bytes_note": "; ".join(f"{u} B per {c}" for c, u in STAGE_UNIT_BYTES[dom].items()),
                      "launches_per_step": trav_launches / args.steps if dom == "traversal" else None,
+                     "stages": stages,
+                     "counts_per_step": {kk: tot[kk2] / args.steps for kk, kk2 in
+                                         (("paths", "paths"), ("segments", "segments"), ("rays", "rays"),
+                                          ("shadow_rays", "shadow"))},
                      "note": f"stage share {dom_ms / sum(v[0] for v in prof.values()):.2f}; "
-                             f"whole-step queue bytes {step_bytes_gbs:.1f} GB/s"},
+                             f"whole-step queue bytes (192 B per vertex + 88 B per shadow ray + 24 B per path) "
+                             f"{step_bytes_gbs:.1f} GB/s; the traversal is bound by dependent node-load "
+                             "latency, not bandwidth (L2 hit rate and warp efficiency in the committed ncu summary)"},
         "stage_ms": {kk: round(v[0], 3) for kk, v in prof.items()},
         "clocks": clk.summary(),
         "wall_s": wall,
@@ -612,6 +667,26 @@ def run_ours(args, rank, world, local_rank):
         line["bvh_variants"] = {"reference_tree": value, "sah_tree": p_sah / (t_sah / 1e3),
                                 "unit": "paths/s",
                                 "note": "PT_BVH_BUILD_SAH: binned-SAH BVH4, same steps and samples, device time"}
+    if world == 1 and args.estimator == "ref_nee":
+        # the same steps with NEE+MIS and the luminance alias table (device time)
+        wm = workload(args.workload, "nee_mis")
+
+        def job_mis(step):
+            chunk = sample_chunk(step, 0, 1, max(1, spp_total // k))
+            return N.job_desc(sid, cam, W, H, wm["sx"], wm["sy"], wm["depth"], rr_start=wm["rr"],
+                              estimator=wm["est"], sampler=wm["sampler"], env_sampling=wm["env"], seed=1,
+                              spp_begin=chunk * k, spp_end=chunk * k + k)
+        for i in range(args.warmup):
+            r.render_device(job_mis(i), film.data_ptr(), sync=True)
+        t_m, p_m, r_m = 0.0, 0, 0
+        for i in range(args.steps):
+            st = r.render_device(job_mis(args.warmup + i), film.data_ptr(), sync=False, stats=True)
+            t_m += st.ms
+            p_m += st.paths
+            r_m += st.rays + st.shadow_rays
+        line["nee_mis"] = {"estimator": wm["est_name"], "paths_per_s": p_m / (t_m / 1e3),
+                           "rays_per_s": r_m / (t_m / 1e3), "unit": "paths/s",
+                           "note": "same scene, steps and sample streams, device time"}
     if world == 1 and not args.no_forms:
         fs, big, build_s, upload_s = form_scenes(r, with_big=True)
         forms = {"scene_build_s": build_s,
@@ -628,9 +703,17 @@ def run_ours(args, rank, world, local_rank):
         from oracle import pyoracle as O
 
         threads = os.cpu_count() or 1
-        v, sample, dt = cpu_paths_per_sec(O.OracleScene(sc), cam, wl, 0, threads)
+        osc = O.OracleScene(sc)
+        v, sample, dt = cpu_paths_per_sec(osc, cam, wl, wl["est"], threads)
         line["cpu_baseline"] = {"value": v, "unit": "paths/s", "cores": threads, "kind": "port",
-                                "sample": sample + f" ({dt:.1f} s); REF_NEE restatement oracle/pt_oracle.cpp"}
+                                "estimator": wl["est_name"],
+                                "sample": sample + f" ({dt:.1f} s); the reference integrator's CPU restatement "
+                                                   "oracle/pt_oracle.cpp (recursive getRayColor for REF_NEE)"}
+        if "nee_mis" in line:
+            wm = workload(args.workload, "nee_mis")
+            vm, sm, dtm = cpu_paths_per_sec(osc, cam, wm, wm["est"], threads)
+            line["nee_mis"]["cpu_paths_per_s"] = vm
+            line["nee_mis"]["cpu_sample"] = sm + f" ({dtm:.1f} s); the oracle's iterative NEE+MIS, {threads} threads"
     print(json.dumps(line), flush=True)
 
 

@@ -387,21 +387,23 @@ int pt_render_device(void *ctx, const pt_job_desc *job, float *d_film_sum,
                      int sync, pt_stats *stats);
 
 /* pt_render_device for callers that cannot allocate device memory while
- * they render (a host with its own device memory pool that forbids other
- * allocators, code running inside a CUDA graph capture, a real-time loop that
- * must not block in the allocator).  No counterpart in the reference, which
- * has no device code.  It calls no cudaMalloc/cudaFree: every work buffer of
- * the render (path state, ray/hit/shadow queues, offset and permutation
- * tables, counters) lives in one fixed 32 MiB device array inside this
- * library, which every GPU that loads the library holds until the process
- * exits; jobs are rendered in as many waves as that array's path capacity
- * needs.  Same arguments and result as pt_render_device (sum of the samples
- * added onto d_film_sum), always synchronous; stats->ms is -1 (not timed).
- * Limit: spp_x * spp_y <= 16384 (PT_ERR_TOO_LARGE beyond).  The first call
- * on a device looks up the array's device address; make that first call
- * before any stream capture.  All calls share the one array: calls that
- * overlap on the GPU (other host threads, other contexts of the same device)
- * race and must be serialised by the caller. */
+ * they render (a host whose own device memory pool forbids other allocators
+ * on its GPUs, a real-time loop that must never block in the allocator).  No
+ * counterpart in the reference, which has no device code.  It calls no
+ * cudaMalloc/cudaFree: every work buffer of the render (path state,
+ * ray/hit/shadow queues, offset and permutation tables, counters) lives in
+ * one fixed 32 MiB device array inside this library; jobs are rendered in as
+ * many waves as that array's path capacity needs.  Same arguments and result
+ * as pt_render_device (sum of the samples added onto d_film_sum), always
+ * synchronous; stats->ms is -1 (not timed).  Limit: spp_x * spp_y <= 16384
+ * (PT_ERR_TOO_LARGE beyond).  The first call on a device does the set-up:
+ * with CUDA's lazy module loading it loads the module that holds the array,
+ * which allocates the 32 MiB on that device (kept until the process exits),
+ * and it looks up the array's device address -- make one warm-up call on
+ * each device before entering a region that must not allocate, and before
+ * any stream capture.  All calls share the one array, which keeps the last
+ * call's contents: calls that overlap on the GPU (other host threads, other
+ * contexts of the same device) race and must be serialised by the caller. */
 int pt_render_device_noalloc(void *ctx, const pt_job_desc *job, float *d_film_sum, pt_stats *stats);
 
 /* Per-stage device timing of the wave kernels (no counterpart in the

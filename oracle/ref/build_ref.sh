@@ -36,4 +36,6 @@ g++ "${FLAGS[@]}" -c "$HERE/ref_harness.cpp" -o "$OUT/obj/ref_harness.o" & pids+
 g++ "${FLAGS[@]}" -c "$SHIM/ref_rng.cpp" -o "$OUT/obj/ref_rng.o" & pids+=($!)
 for p in "${pids[@]}"; do wait "$p"; done
 g++ -shared -o "$OUT/libref_harness.so" "$OUT"/obj/*.o -lpthread
+# where the harness was built from (tests read the reference's own files there)
+printf '%s\n' "$REF_ROOT" > "$OUT/REF_ROOT"
 echo "built $OUT/libref_harness.so"

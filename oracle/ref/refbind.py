@@ -17,8 +17,18 @@ import numpy as np
 from pathtracer_gb300 import native as N
 
 LIB = Path(__file__).resolve().parents[1] / "_ref" / "libref_harness.so"
-# the reference sources the harness was built from (build_ref.sh's REF_ROOT)
-REF_ROOT = Path(os.environ.get("REF_ROOT", "/root/reference"))
+
+
+def _ref_root():
+    """The reference sources the harness was built from: $REF_ROOT, else the
+    root build_ref.sh recorded beside the library; None when neither exists."""
+    if os.environ.get("REF_ROOT"):
+        return Path(os.environ["REF_ROOT"])
+    rec = LIB.parent / "REF_ROOT"
+    return Path(rec.read_text().strip()) if rec.exists() else None
+
+
+REF_ROOT = _ref_root()
 
 f32p = C.POINTER(C.c_float)
 i32p = C.POINTER(C.c_int32)

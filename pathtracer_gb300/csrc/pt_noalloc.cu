@@ -3,16 +3,18 @@
 //
 // Some callers cannot allocate device memory while they render: a host that
 // runs its own device memory pool or arena and forbids other allocators on
-// its devices, a caller inside a region being captured into a CUDA graph
-// (where cudaMalloc is not allowed), or a real-time loop that must never
-// block on the allocator.  For them this entry point keeps every buffer the
-// render needs -- the path-state and ray/hit/shadow queues, the pixel-offset
-// table, the digit-permutation tables and the counters -- in ONE file-scope
-// device array of fixed size, PT_NOALLOC_SCRATCH_BYTES, which every GPU that
-// loads this library holds until the process exits.  The caller still passes
-// its inputs (a scene already resident through pt_scene_upload, the job) and
-// its output (a device film).  Large jobs are rendered in as many waves as
-// the array's path capacity requires.
+// its devices, or a real-time loop that must never block on the allocator.
+// For them this entry point keeps every buffer the render needs -- the
+// path-state and ray/hit/shadow queues, the pixel-offset table, the
+// digit-permutation tables and the counters -- in ONE file-scope device
+// array of fixed size, PT_NOALLOC_SCRATCH_BYTES.  With CUDA's lazy module
+// loading (the default) the array is allocated on a device when this file's
+// module is first loaded there, i.e. in the first call's
+// cudaGetSymbolAddress, and it stays allocated until the process exits; a
+// caller makes one warm-up call per device before its no-allocation region.
+// The caller still passes its inputs (a scene already resident through
+// pt_scene_upload, the job) and its output (a device film).  Large jobs are
+// rendered in as many waves as the array's path capacity requires.
 #include <cuda_runtime.h>
 
 #include <cstring>

@@ -2,10 +2,12 @@
 device memory.
 
 It is meant for callers that cannot allocate device memory while they render
-(a host with its own device memory pool, a CUDA graph capture, a real-time
-loop).  Its work buffers live in one fixed device array inside the library,
-so its result must equal pt_render_device's on the same job.  The file runs
-last so that a failure here leaves every other test already run.
+(a host whose own device memory pool forbids other allocators, a real-time
+loop that must not block in the allocator).  Its work buffers live in one
+fixed device array inside the library, so its result must equal
+pt_render_device's on the same job, and after a warm-up call a render must
+leave the device's free memory unchanged.  The file runs last so that a
+failure here leaves every other test already run.
 """
 from __future__ import annotations
 
@@ -61,5 +63,25 @@ def test_noalloc_rejects_sizes_beyond_its_limit():
     buf = C.create_string_buffer(256)
     r.lib.pt_last_error(r.ctx, buf, 256)
     assert b"16384" in buf.value
+    r.release(sid)
+    r.close()
+
+
+def test_noalloc_allocates_no_device_memory():
+    # a fresh context that never ran pt_render_device, so no queue buffers of
+    # the context exist; the warm-up call loads the array (lazy module loading)
+    r = N.Renderer(0)
+    sc, cam = S.cornell_icosphere(3)
+    sid = r.upload(sc)
+    job = N.job_desc(sid, cam, 128, 128, 4, 4, 8, seed=5, estimator=N.EST_NEE_MIS)  # several waves
+    film = torch.zeros(job.height * job.width * 3, dtype=torch.float32, device="cuda:0")
+    lib = r.lib
+    assert lib.pt_render_device_noalloc(r.ctx, C.byref(job), C.c_void_p(film.data_ptr()), None) == 0
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info(0)[0]
+    for _ in range(2):
+        assert lib.pt_render_device_noalloc(r.ctx, C.byref(job), C.c_void_p(film.data_ptr()), None) == 0
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info(0)[0] == free0
     r.release(sid)
     r.close()
