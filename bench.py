@@ -59,19 +59,23 @@ FALLBACK_HBM_GBS = 6800.0
 # pixel, per (workload, estimator); from a one-pass ncu capture of the same
 # bench command
 NCU_TRAVERSAL_BYTES_PER_STEP = {("rough_glass", 1): 6.9185e9}
-# Algorithmic queue bytes per unit, by stage: the per-vertex 192 B, per
-# shadow ray 88 B and per path 24 B of the queue model, each byte charged to
-# the stage that moves it:
-#   camera    72 B per path: RayQueue record written (32) + path state written (40)
+# Algorithmic queue bytes per unit, by stage: the records each stage must
+# read or write in this layout, with the survey model's 192 B per path vertex,
+# 88 B per shadow ray (44 written by shade, 44 read by the traversal) and FP32
+# film; each byte charged to the stage that moves it:
+#   camera    64 B per path: ray origin + direction (32) and path state
+#             (throughput + pdf 16, radiance 16) written
 #   traversal 48 B per closest-hit ray: ray read (32) + hit written (16);
 #             44 B per shadow ray: ShadowQueue record read
 #   sort      16 B per closest-hit ray: key + index written and read (8 x 2)
 #   shade     128 B per path vertex: hit read (16) + path state read and written (80)
 #             + continuation RayQueue record written (32);
 #             44 B per shadow ray: ShadowQueue record written
-#   film      24 B per path: FP32 RGB read-modify-write
-STAGE_UNIT_BYTES = {"camera": {"paths": 72}, "traversal": {"rays": 48, "shadow_rays": 44},
-                    "sort": {"rays": 16}, "shade": {"segments": 128, "shadow_rays": 44}, "film": {"paths": 24}}
+#   film      16 B per path: its radiance read; 24 B per film pixel per wave:
+#             FP32 RGB read-modify-write
+STAGE_UNIT_BYTES = {"camera": {"paths": 64}, "traversal": {"rays": 48, "shadow_rays": 44},
+                    "sort": {"rays": 16}, "shade": {"segments": 128, "shadow_rays": 44},
+                    "film": {"paths": 16, "film_pixel_waves": 24}}
 
 
 def parse():
@@ -210,7 +214,8 @@ def stage_roofline(prof: dict, tot: dict, peak: float) -> dict:
     counts over the timed steps), CUDA-event milliseconds, GB/s and the
     fraction of the HBM peak.  traversal = the trace and shadow stages
     (closest, paired and shadow launches + resolve)."""
-    counts = {"paths": tot["paths"], "segments": tot["segments"], "rays": tot["rays"], "shadow_rays": tot["shadow"]}
+    counts = {"paths": tot["paths"], "segments": tot["segments"], "rays": tot["rays"], "shadow_rays": tot["shadow"],
+              "film_pixel_waves": tot["film_pixel_waves"]}
     ms = {"camera": prof["camera"][0], "traversal": prof["trace"][0] + prof["shadow"][0], "sort": prof["sort"][0],
           "shade": prof["shade"][0], "film": prof["film"][0]}
     out = {}
@@ -516,7 +521,7 @@ def run_ours(args, rank, world, local_rank):
     barrier()
     r.profile_begin()
     stats = N.Stats()
-    tot = dict(paths=0, segments=0, rays=0, shadow=0, bytes=0)
+    tot = dict(paths=0, segments=0, rays=0, shadow=0, bytes=0, film_pixel_waves=0)
     t_dev = 0.0
     with ClockSampler(local_rank) as clk:
         barrier()
@@ -529,6 +534,7 @@ def run_ours(args, rank, world, local_rank):
             tot["rays"] += st.rays
             tot["shadow"] += st.shadow_rays
             tot["bytes"] += st.algorithmic_bytes
+            tot["film_pixel_waves"] += W * H  # one wave per step
         barrier()
         wall = time.perf_counter() - w0
     prof = r.profile_end()
@@ -621,7 +627,7 @@ def run_ours(args, rank, world, local_rank):
                      "stages": stages,
                      "counts_per_step": {kk: tot[kk2] / args.steps for kk, kk2 in
                                          (("paths", "paths"), ("segments", "segments"), ("rays", "rays"),
-                                          ("shadow_rays", "shadow"))},
+                                          ("shadow_rays", "shadow"), ("film_pixel_waves", "film_pixel_waves"))},
                      "note": f"stage share {dom_ms / sum(v[0] for v in prof.values()):.2f}; "
                              f"whole-step queue bytes (192 B per vertex + 88 B per shadow ray + 24 B per path) "
                              f"{step_bytes_gbs:.1f} GB/s; the traversal is bound by dependent node-load "

@@ -176,7 +176,17 @@ typedef struct pt_object_desc {
    * shutter time; the object sits at its described position + velocity * t
    * for a ray of time t in [0, camera.shutter].  Zero: static. */
   float velocity[3];
+  /* HitRecord::is_inside of every hit on the object: PT_FACE_AS_HIT (the
+   * front-face test of set_normal, then flip_face / a reversed winding),
+   * PT_FACE_FRONT (always true) or PT_FACE_BACK (always false).  A reference
+   * object under Translate, Rotate or Scale reports is_inside = true for
+   * every hit: their intersect calls set_normal with the child's normal,
+   * which already faces the ray (objectTransform.hpp:56-57, 168,
+   * objectTransform.cpp:131, 172, 210); a FlipFace over such an object
+   * reports false.  The C++ API's decorators set this field. */
+  int32_t face;
 } pt_object_desc;
+enum { PT_FACE_AS_HIT = 0, PT_FACE_FRONT = 1, PT_FACE_BACK = 2 };
 
 /* EnvironmentLight + HDRITexture (include/light/envLight.hpp:4,
  * include/texture/texture.hpp:97).  texels are RGB float, width*height*3,
@@ -441,6 +451,24 @@ int pt_write_png(const char *path, const uint8_t *rgb8, int32_t width, int32_t h
 int pt_sampler_eval(void *ctx, int32_t strategy, uint32_t seed,
                     uint32_t first_index, int32_t n, int32_t dims, float *out);
 
+/* The sample values a job's paths draw, computed by the device code of the
+ * render, for paths [first_path, first_path + n) in render order (pixel
+ * q = g % (width * height), grid sample k = spp_begin + g / (width * height)):
+ *   pixel_offsets (2n, may be NULL): the pixel-grid offset of the path's
+ *     sample k -- FrameBuffer::setOffsets (framebuffer.cpp:131-145) with
+ *     getOffsets(spp_x, spp_y) (utils/random.hpp:47-63): one jittered grid per
+ *     frame, stratum (i, j) = (k / spp_y, k % spp_y);
+ *   dim_values (n * dims): sampler dimensions 0..dims-1 of the job's sampler
+ *     (HaltonSampler::SampleDimension, sampler.hpp:54-73, at the path's
+ *     index; PT_SAMPLER_STRATIFIED: the jittered stratum of sample k among the
+ *     pixel's spp_x * spp_y, permuted per pixel and dimension);
+ *   light_offsets (n * bounces * LN * 2, LN = light_samples_x *
+ *     light_samples_y): the light-point offsets of the vertex at each bounce,
+ *     the per-vertex getOffsets(light_samples_x, light_samples_y) grid of
+ *     maxdepth_nee.hpp:91, stratum (ls / light_samples_y, ls % light_samples_y). */
+int pt_sample_eval(void *ctx, const pt_job_desc *job, int64_t first_path, int32_t n, int32_t dims,
+                   int32_t bounces, float *pixel_offsets, float *dim_values, float *light_offsets);
+
 /* Closest hit (BVHNode::intersect, bvh.hpp:27-41 and the primitives below
  * it).  rays: n * 6 floats (origin, direction), tmin/tmax per call.
  * Outputs: t (FLT_MAX on miss), prim (-1 on miss; triangles are numbered
@@ -452,6 +480,17 @@ int pt_trace_closest(void *ctx, int32_t scene_id, const float *rays, int32_t n,
  * occluded[i] = 1 if anything is hit in [tmin, tmax_i]. */
 int pt_trace_any(void *ctx, int32_t scene_id, const float *rays,
                  const float *tmax, int32_t n, float tmin, uint8_t *occluded);
+
+/* Hittable::intersect (base/primitive.hpp:30-79) through the scene's BVH:
+ * the HitRecord of the closest hit in [tmin, tmax] of each ray (rays: n * 6
+ * floats, origin and direction).  Outputs t (FLT_MAX on miss), prim (-1 on
+ * miss), position (3n), normal (3n: HitRecord::normal, turned towards the
+ * ray by set_normal, materialBase.hpp:47-52) and is_inside (n: the
+ * front-face flag, toggled by FlipFace, objectTransform.hpp:5-38).  Objects
+ * under Translate / Rotate / Scale are resident with the transform applied
+ * to their geometry. */
+int pt_intersect(void *ctx, int32_t scene_id, const float *rays, int32_t n, float tmin, float tmax,
+                 float *t, int32_t *prim, float *position, float *normal, uint8_t *is_inside);
 
 /* BSDF evaluation (Material::f and Material::scatter_pdf(wo, wi, rec),
  * material.hpp:32-61).  Arrays of n items, 3 floats per vector. `front` is

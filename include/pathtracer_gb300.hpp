@@ -258,6 +258,9 @@ struct Flat {
   pt_sphere_desc sphere{};
   pt_box_desc box{};
   pt_curve_desc curve{};
+  // pt_object_desc.face: HitRecord::is_inside as hit, or fixed by the
+  // decorators (Translate / Rotate / Scale give true, a FlipFace over them false)
+  int32_t face = PT_FACE_AS_HIT;
   std::shared_ptr<Material> mat;
 };
 
@@ -419,6 +422,10 @@ class FlipFace : public Hittable {
   explicit FlipFace(std::shared_ptr<Hittable> o) : o(std::move(o)) {}
   Flat flatten() const override {
     Flat f = o->flatten();
+    if (f.face != PT_FACE_AS_HIT) {  // a fixed is_inside toggles
+      f.face = f.face == PT_FACE_FRONT ? PT_FACE_BACK : PT_FACE_FRONT;
+      return f;
+    }
     if (f.kind == Flat::BOX) f = detail::box_to_mesh(f);
     if (f.kind == Flat::QUAD) f.quad.flip_face ^= 1;
     if (f.kind == Flat::SPHERE) f.sphere.flip_face ^= 1;
@@ -453,6 +460,9 @@ class Translate : public Hittable {
       f.quad.d1_min += off[a1];
       f.quad.d1_max += off[a1];
     }
+    // Translate::intersect calls set_normal with the child's ray-facing
+    // normal (objectTransform.hpp:56-57): is_inside is always true
+    f.face = PT_FACE_FRONT;
     return f;
   }
   std::shared_ptr<Hittable> o;
@@ -486,6 +496,7 @@ class Scale : public Hittable {
       f.quad.d1_min *= s;
       f.quad.d1_max *= s;
     }
+    f.face = PT_FACE_FRONT;  // Scale::intersect's set_normal (objectTransform.hpp:168)
     return f;
   }
   std::shared_ptr<Hittable> o;
@@ -499,18 +510,23 @@ class Rotate : public Hittable {
     Flat f = o->flatten();
     if (f.kind == Flat::QUAD) f = detail::quad_to_mesh(f);
     if (f.kind == Flat::BOX) f = detail::box_to_mesh(f);
+    // Rotate<axis>::intersect (objectTransform.cpp:95-213) turns the ray
+    // into the child's frame with (c a - s b, s a + c b) over the axis pair
+    // (a, b) = (y, z), (x, z), (x, y) and maps the hit back with the inverse,
+    // (c a + s b, -s a + c b): the child's geometry seen in the world
     const float c = std::cos(r), s = std::sin(r);
-    const int i = A == Axis::X ? 1 : A == Axis::Y ? 2 : 0, j = A == Axis::X ? 2 : A == Axis::Y ? 0 : 1;
+    const int i = A == Axis::X ? 1 : 0, j = A == Axis::Z ? 1 : 2;
     auto rot = [&](float *p) {
       float a = p[i], b = p[j];
-      p[i] = c * a - s * b;
-      p[j] = s * a + c * b;
+      p[i] = c * a + s * b;
+      p[j] = -s * a + c * b;
     };
     for (size_t k = 0; k + 2 < f.pos.size(); k += 3) rot(&f.pos[k]);
     for (size_t k = 0; k + 2 < f.nrm.size(); k += 3) rot(&f.nrm[k]);
     if (f.kind == Flat::SPHERE) rot(f.sphere.center);
     if (f.kind == Flat::CURVE)
       for (int k = 0; k < 4; ++k) rot(f.curve.cps[k]);
+    f.face = PT_FACE_FRONT;  // Rotate<axis>::intersect's set_normal (objectTransform.cpp:131, 172, 210)
     return f;
   }
   std::shared_ptr<Hittable> o;
@@ -584,8 +600,11 @@ struct SceneInfo {
   std::vector<float> film;                   // mean radiance [j][i][c], j = 0 bottom
   std::vector<uint8_t> rgb8;                 // tone-mapped, row 0 top
 
-  void render(const std::string &out_path = "") {
-    if (!camera) throw std::runtime_error("Camera is not initialized!");
+  // Flattens the object list (decorators baked into the geometry, light
+  // discovery and BVH build in the library) and uploads it to ctx; returns
+  // the scene id (the scene set-up of SceneInfo::render,
+  // renderManager.hpp:80-95).
+  int32_t upload(void *ctx) const {
     if (objects.getLists().empty()) throw std::runtime_error("No objects in the scene!");
     std::vector<pt_material_desc> mats;
     std::vector<Flat> flats;
@@ -631,23 +650,23 @@ struct SceneInfo {
         m.n_triangles = (int32_t)(f.idx.size() / 3);
         m.material = mi;
         meshes.push_back(m);
-        objs.push_back({PT_OBJ_MESH, (int32_t)meshes.size() - 1});
+        objs.push_back({PT_OBJ_MESH, (int32_t)meshes.size() - 1, {0.f, 0.f, 0.f}, f.face});
       } else if (f.kind == Flat::CURVE) {
         f.curve.material = mi;
         curves.push_back(f.curve);
-        objs.push_back({PT_OBJ_CURVE, (int32_t)curves.size() - 1});
+        objs.push_back({PT_OBJ_CURVE, (int32_t)curves.size() - 1, {0.f, 0.f, 0.f}, f.face});
       } else if (f.kind == Flat::BOX) {
         f.box.material = mi;
         boxes.push_back(f.box);
-        objs.push_back({PT_OBJ_BOX, (int32_t)boxes.size() - 1});
+        objs.push_back({PT_OBJ_BOX, (int32_t)boxes.size() - 1, {0.f, 0.f, 0.f}, f.face});
       } else if (f.kind == Flat::QUAD) {
         f.quad.material = mi;
         quads.push_back(f.quad);
-        objs.push_back({PT_OBJ_QUAD, (int32_t)quads.size() - 1});
+        objs.push_back({PT_OBJ_QUAD, (int32_t)quads.size() - 1, {0.f, 0.f, 0.f}, f.face});
       } else {
         f.sphere.material = mi;
         spheres.push_back(f.sphere);
-        objs.push_back({PT_OBJ_SPHERE, (int32_t)spheres.size() - 1});
+        objs.push_back({PT_OBJ_SPHERE, (int32_t)spheres.size() - 1, {0.f, 0.f, 0.f}, f.face});
       }
     }
     pt_scene_desc d{};
@@ -674,11 +693,18 @@ struct SceneInfo {
       d.env = &env;
     }
     for (int c = 0; c < 3; ++c) d.bg_color[c] = bg_color[c];
+    int32_t sid = 0;
+    check(pt_scene_upload(ctx, &d, &sid), ctx);
+    return sid;
+  }
+
+  void render(const std::string &out_path = "") {
+    if (!camera) throw std::runtime_error("Camera is not initialized!");
     void *ctx = nullptr;
     check(pt_create(&ctx, device), nullptr);
     int32_t sid = 0;
     try {
-      check(pt_scene_upload(ctx, &d, &sid), ctx);
+      sid = upload(ctx);
       pt_job_desc j{};
       j.scene = sid;
       j.width = (int32_t)_width;

@@ -707,6 +707,7 @@ struct Obj {
   bool moving = false;
   Box box;
   int mat, flip, prim;
+  int face = 0;  // pt_object_desc.face: 0 as hit, 1 is_inside always true, 2 always false
   int light = -1;
   // quad
   int axis;
@@ -871,7 +872,15 @@ struct Scene {
   // A moving object (extension) is intersected in its own frame at the ray's
   // time: origin o - vel * time; the hit position is then taken on the world
   // ray.
+  // pt_object_desc.face: a decorated object's fixed is_inside (set_normal
+  // given a ray-facing normal by Translate / Rotate / Scale, toggled by an
+  // outer FlipFace: objectTransform.hpp:5-181, objectTransform.cpp:95-213).
   bool hit_obj(int oi, V o_w, V d, float tmin, float tmax, Hit &rec, float time) const {
+    if (!hit_obj_as_hit(oi, o_w, d, tmin, tmax, rec, time)) return false;
+    if (objs[oi].face) rec.is_inside = objs[oi].face == PT_FACE_FRONT;
+    return true;
+  }
+  bool hit_obj_as_hit(int oi, V o_w, V d, float tmin, float tmax, Hit &rec, float time) const {
     const Obj &ob = objs[oi];
     if (ob.kind == PT_OBJ_CURVE) return hit_curve(ob, o_w, d, tmin, tmax, rec, time);
     if (ob.kind == PT_OBJ_BOX) {  // Box::intersect: its ObjectList, closest face (objectList.hpp:84-105)
@@ -1136,6 +1145,7 @@ Scene *build_scene(const pt_scene_desc *d) {
     ob.index = od.index;
     ob.vel = V(od.velocity[0], od.velocity[1], od.velocity[2]);
     ob.moving = od.velocity[0] != 0.f || od.velocity[1] != 0.f || od.velocity[2] != 0.f;
+    ob.face = od.face;
     if (od.kind == PT_OBJ_MESH) {
       ob.box = S->meshes[od.index].aabb;
       ob.mat = d->meshes[od.index].material;
@@ -1365,15 +1375,25 @@ struct LightSample {
   bool env = false;
 };
 
+// Light-point offsets of light sample ls at a vertex of bounce `bounce`: the
+// per-vertex getOffsets(light_samples_x, light_samples_y) grid
+// (random.hpp:47-63, drawn at maxdepth_nee.hpp:91), stratum (ls / y, ls % y).
+static std::pair<float, float> light_offset(const PathCtx &P, int bounce, int ls) {
+  const pt_job_desc &j = *P.job;
+  const uint32_t rbase = 64u + 32u * (uint32_t)bounce;
+  const int si = ls / j.light_samples_y, sj = ls % j.light_samples_y;
+  return {((float)si + rand01(P.key, rbase + 2u * ls)) / (float)j.light_samples_x,
+          ((float)sj + rand01(P.key, rbase + 2u * ls + 1u)) / (float)j.light_samples_y};
+}
+
 // One NEE light sample (maxdepth_nee.hpp:94-210) at shading point x with
 // normal n.  surface: NoI weights G; in a medium (surface=false) G = NoL/d2.
 static LightSample sample_light(const PathCtx &P, V x, V n, int bounce, int ls, bool surface) {
   const Scene &S = *P.S;
   const pt_job_desc &j = *P.job;
   const uint32_t rbase = 64u + 32u * (uint32_t)bounce;
-  const int si = ls / j.light_samples_y, sj = ls % j.light_samples_y;
-  float ox = ((float)si + rand01(P.key, rbase + 2u * ls)) / (float)j.light_samples_x;
-  float oy = ((float)sj + rand01(P.key, rbase + 2u * ls + 1u)) / (float)j.light_samples_y;
+  const auto lo = light_offset(P, bounce, ls);
+  const float ox = lo.first, oy = lo.second;
   const int nl = (int)S.lights.size();
   int li = (int)(rand01(P.key, rbase + 20u + ls) * nl) % nl;
   const Light &L = S.lights[li];
@@ -1687,6 +1707,38 @@ void or_sampler_eval(int strategy, uint32_t seed, uint32_t first, int n, int dim
     for (int d = 0; d < dims; ++d) out[(size_t)i * dims + d] = halton_sample(strategy, seed, d, first + (uint32_t)i);
 }
 
+// The sample values of paths [first, first + n) of a job in render order
+// (pixel q = g % (W * H), grid sample k = spp_begin + g / (W * H)): pixel-grid
+// offsets (2n), sampler dimensions (n * dims), light-point offsets
+// (n * bounces * LN * 2) -- the values or_render's paths draw.
+void or_path_samples(const pt_job_desc *job, int64_t first, int n, int dims, int bounces, float *pix, float *dv,
+                     float *lo) {
+  const pt_job_desc &j = *job;
+  const auto off = offsets(j);
+  const bool win = j.full_width > 0 || j.full_height > 0;
+  const int X0 = win ? j.crop_x : 0, Y0 = win ? j.crop_y : 0;
+  const int FW = win ? j.full_width : j.width, FH = win ? j.full_height : j.height;
+  const int Sn = j.spp_x * j.spp_y, LN = j.light_samples_x * j.light_samples_y;
+  const int64_t npix = (int64_t)j.width * j.height;
+  for (int s = 0; s < n; ++s) {
+    const int64_t g = first + s;
+    const int q = (int)(g % npix), k = j.spp_begin + (int)(g / npix);
+    const int gi = X0 + q % j.width, gj = Y0 + q / j.width;
+    const uint64_t lin = ((uint64_t)gi * FH + gj) * (uint64_t)Sn + k;
+    PathCtx P{nullptr, &j, path_key(j.seed, lin), (uint32_t)(lin + 1u), gj * FW + gi, k};
+    pix[2 * s] = off[k].first;
+    pix[2 * s + 1] = off[k].second;
+    for (int d = 0; d < dims; ++d) dv[(size_t)s * dims + d] = dim_value(P, d);
+    for (int b = 0; b < bounces; ++b)
+      for (int ls = 0; ls < LN; ++ls) {
+        const auto o = light_offset(P, b, ls);
+        const size_t i = (((size_t)s * bounces + b) * LN + ls) * 2;
+        lo[i] = o.first;
+        lo[i + 1] = o.second;
+      }
+  }
+}
+
 void or_trace_closest(void *s, const float *rays, int n, float tmin, float tmax, float *t, int *prim) {
   const Scene &S = *static_cast<Scene *>(s);
   for (int i = 0; i < n; ++i) {
@@ -1695,6 +1747,25 @@ void or_trace_closest(void *s, const float *rays, int n, float tmin, float tmax,
     bool h = S.intersect(o, d, rec, tmin, tmax);
     t[i] = h ? rec.t : std::numeric_limits<float>::max();
     prim[i] = h ? rec.prim : -1;
+  }
+}
+
+// The HitRecord of each ray's closest hit: t, prim, position, normal (turned
+// towards the ray) and is_inside.
+void or_intersect(void *s, const float *rays, int n, float tmin, float tmax, float *t, int *prim, float *pos,
+                  float *nrm, uint8_t *inside) {
+  const Scene &S = *static_cast<Scene *>(s);
+  for (int i = 0; i < n; ++i) {
+    Hit rec;
+    V o(rays[6 * i], rays[6 * i + 1], rays[6 * i + 2]), d(rays[6 * i + 3], rays[6 * i + 4], rays[6 * i + 5]);
+    const bool h = S.intersect(o, d, rec, tmin, tmax);
+    t[i] = h ? rec.t : std::numeric_limits<float>::max();
+    prim[i] = h ? rec.prim : -1;
+    for (int c = 0; c < 3; ++c) {
+      pos[3 * i + c] = h ? rec.position[c] : 0.f;
+      nrm[3 * i + c] = h ? rec.normal[c] : 0.f;
+    }
+    inside[i] = (h && rec.is_inside) ? 1 : 0;
   }
 }
 

@@ -32,6 +32,9 @@ def load():
         lib.or_scene_destroy.argtypes = [C.c_void_p]
         lib.or_scene_num_lights.argtypes = [C.c_void_p]
         lib.or_sampler_eval.argtypes = [C.c_int, C.c_uint32, C.c_uint32, C.c_int, C.c_int, f32p]
+        lib.or_intersect.argtypes = [C.c_void_p, f32p, C.c_int, C.c_float, C.c_float, f32p, i32p, f32p, f32p, u8p]
+        lib.or_path_samples.argtypes = [C.POINTER(N.JobDesc), C.c_int64, C.c_int, C.c_int, C.c_int, f32p, f32p,
+                                        f32p]
         lib.or_trace_closest.argtypes = [C.c_void_p, f32p, C.c_int, C.c_float, C.c_float, f32p, i32p]
         lib.or_bsdf_eval.argtypes = [C.POINTER(N.MaterialDesc), C.c_int, f32p, f32p, f32p, u8p, f32p, f32p]
         lib.or_bsdf_sample.argtypes = [C.POINTER(N.MaterialDesc), C.c_int, f32p, f32p, u8p, f32p, f32p, u8p, f32p,
@@ -67,6 +70,19 @@ class OracleScene:
         self.lib.or_trace_closest(self.h, _p(rays, C.c_float), n, tmin, tmax, _p(t, C.c_float), _p(prim, C.c_int32))
         return t, prim
 
+    def intersect(self, rays, tmin=1e-4, tmax=1e5):
+        """(t, prim, position, normal, is_inside) of each ray's closest hit."""
+        rays = np.ascontiguousarray(rays, np.float32)
+        n = rays.shape[0]
+        t = np.zeros(n, np.float32)
+        prim = np.zeros(n, np.int32)
+        pos = np.zeros((n, 3), np.float32)
+        nrm = np.zeros((n, 3), np.float32)
+        ins = np.zeros(n, np.uint8)
+        self.lib.or_intersect(self.h, _p(rays, C.c_float), n, tmin, tmax, _p(t, C.c_float), _p(prim, C.c_int32),
+                              _p(pos, C.c_float), _p(nrm, C.c_float), _p(ins, C.c_uint8))
+        return t, prim, pos, nrm, ins
+
     def render(self, job, threads=0, recursive=True):
         mean = np.zeros((job.height, job.width, 3), np.float32)
         var = np.zeros_like(mean)
@@ -83,6 +99,18 @@ def sampler_eval(strategy, first_index, n, dims, seed=0):
     out = np.zeros((n, dims), np.float32)
     load().or_sampler_eval(strategy, seed, first_index, n, dims, _p(out, C.c_float))
     return out
+
+
+def path_samples(job, first_path, n, dims, bounces=0):
+    """or_path_samples: (pixel offsets (n, 2), dimension values (n, dims),
+    light offsets (n, bounces, LN, 2)) of the job's paths first_path..+n."""
+    ln = job.light_samples_x * job.light_samples_y
+    pix = np.zeros((n, 2), np.float32)
+    dv = np.zeros((n, max(dims, 1)), np.float32)
+    lo = np.zeros((n, max(bounces, 1), ln, 2), np.float32)
+    load().or_path_samples(C.byref(job), first_path, n, dims, bounces, _p(pix, C.c_float), _p(dv, C.c_float),
+                           _p(lo, C.c_float))
+    return pix, dv[:, :dims], lo[:, :bounces]
 
 
 def bsdf_eval(mat, wo, wi, nrm, front):

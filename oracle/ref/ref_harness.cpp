@@ -51,6 +51,7 @@
 #include "mesh_io/meshLoader.hpp"
 #include "primitives/box.hpp"
 #include "primitives/curve.hpp"
+#include "utils/objectTransform.hpp"
 #undef private
 #undef protected
 
@@ -260,7 +261,7 @@ void ref_trace_closest(void *s, const float *rays, int n, float tmin, float tmax
             prim_out[i] = S->obj_prim_base[o] + (int)f;
           }
         }
-      } else if (S->obj_kind[o] != PT_OBJ_MESH) {
+      } else if (S->obj_kind[o] != PT_OBJ_MESH || !S->meshes[o]) {
         prim_out[i] = S->obj_prim_base[o];
       } else {
         const MeshBVHNode *root = S->meshes[o]->bvh.get();
@@ -275,6 +276,36 @@ void ref_trace_closest(void *s, const float *rays, int n, float tmin, float tmax
       break;
     }
   }
+}
+
+// Wraps object `object` of a scene in the reference's decorators
+// (utils/objectTransform.hpp:5-181, objectTransform.cpp:95-213), innermost
+// first -- op 0 Translate(p0, p1, p2), 1 Rotate<X>(p0), 2 Rotate<Y>(p0),
+// 3 Rotate<Z>(p0), 4 Scale(p0), 5 FlipFace; three params per op -- and
+// rebuilds the scene's BVHNode.  Hits of a transformed mesh report the
+// object's first primitive id (ref_trace_closest recovers triangle ids from
+// untransformed rays only).
+int ref_scene_transform(void *s, int object, int n_ops, const int *ops, const float *params) {
+  auto *S = static_cast<RefScene *>(s);
+  if (object < 0 || object >= (int)S->objects.objects.size()) return -1;
+  std::shared_ptr<Hittable> h = S->objects.objects[object];
+  for (int k = 0; k < n_ops; ++k) {
+    const float *p = params + 3 * k;
+    switch (ops[k]) {
+    case 0: h = std::make_shared<Translate>(h, vec3(p[0], p[1], p[2])); break;
+    case 1: h = std::make_shared<Rotate<Axis::X>>(h, p[0]); break;
+    case 2: h = std::make_shared<Rotate<Axis::Y>>(h, p[0]); break;
+    case 3: h = std::make_shared<Rotate<Axis::Z>>(h, p[0]); break;
+    case 4: h = std::make_shared<Scale>(h, p[0]); break;
+    case 5: h = std::make_shared<FlipFace>(h); break;
+    default: return -1;
+    }
+  }
+  S->objects.objects[object] = h;
+  S->meshes[object] = nullptr;
+  std::srand(1);
+  S->bvh = std::make_shared<BVHNode>(S->objects);
+  return 0;
 }
 
 // HitRecord for BSDF calls: the reference materials read normal, position,

@@ -53,6 +53,7 @@ def load():
         lib.ref_scene_num_lights.argtypes = [C.c_void_p]
         lib.ref_trace_closest.argtypes = [C.c_void_p, f32p, C.c_int, C.c_float, C.c_float, f32p, i32p, f32p, f32p,
                                           u8p]
+        lib.ref_scene_transform.argtypes = [C.c_void_p, C.c_int, C.c_int, i32p, f32p]
         lib.ref_bsdf_eval.argtypes = [C.POINTER(N.MaterialDesc), C.c_int, f32p, f32p, f32p, u8p, f32p, f32p]
         lib.ref_bsdf_sample.argtypes = [C.POINTER(N.MaterialDesc), C.c_int, f32p, f32p, u8p, f32p, f32p, u8p, f32p,
                                         f32p, f32p, u32p]
@@ -98,6 +99,15 @@ class RefScene:
                                    _p(prim, C.c_int32), _p(pos, C.c_float), _p(nrm, C.c_float),
                                    _p(front, C.c_uint8))
         return t, prim, pos, nrm, front
+
+    def transform(self, obj: int, ops):
+        """Wraps object `obj` in the reference's decorators, innermost first:
+        ops = [(code, p0, p1, p2)] with code 0 Translate, 1 Rotate<X>,
+        2 Rotate<Y>, 3 Rotate<Z>, 4 Scale, 5 FlipFace; rebuilds the BVH."""
+        codes = np.array([o[0] for o in ops], np.int32)
+        params = np.array([list(o[1:]) + [0.0] * (3 - len(o[1:])) for o in ops], np.float32).reshape(-1)
+        if self.lib.ref_scene_transform(self.h, obj, len(ops), _p(codes, C.c_int32), _p(params, C.c_float)) != 0:
+            raise ValueError("bad transform")
 
     def render(self, job, threads=0):
         mean = np.zeros((job.height, job.width, 3), np.float32)

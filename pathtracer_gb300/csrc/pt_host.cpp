@@ -1092,7 +1092,23 @@ std::unique_ptr<Scene> build_scene(const pt_scene_desc *d_in, cudaStream_t st, b
   // primitives (a mesh shared by several objects takes the last one's)
   std::vector<float4> motion;
   std::vector<int> prim_motion(n_prims, 0);
+  // pt_object_desc.face per primitive: PT_PRIM_FACE_* flags (0: as hit)
+  std::vector<int> prim_face(n_prims, 0);
   B.obj_motion.assign(d->n_objects, 0);
+  for (int o = 0; o < d->n_objects; ++o) {
+    const pt_object_desc &od = d->objects[o];
+    if (od.face < PT_FACE_AS_HIT || od.face > PT_FACE_BACK) fail(PT_ERR_INVALID, "bad object face mode");
+    if (od.face == PT_FACE_AS_HIT) continue;
+    const int ff = PT_PRIM_FACE_FIXED | (od.face == PT_FACE_FRONT ? PT_PRIM_FACE_FRONT : 0);
+    if (od.kind == PT_OBJ_MESH)
+      for (int t = 0; t < d->meshes[od.index].n_triangles; ++t) prim_face[B.tri_base[od.index] + t] = ff;
+    else if (od.kind == PT_OBJ_BOX)
+      for (int k = 0; k < 6; ++k) prim_face[B.n_tris + n_user_quads + 6 * od.index + k] = ff;
+    else if (od.kind == PT_OBJ_CURVE)
+      prim_face[curve_base + od.index] = ff;
+    else
+      prim_face[od.kind == PT_OBJ_QUAD ? B.n_tris + od.index : B.n_tris + d->n_quads + od.index] = ff;
+  }
   for (int o = 0; o < d->n_objects; ++o) {
     const pt_object_desc &od = d->objects[o];
     const float *v = od.velocity;
@@ -1214,7 +1230,7 @@ std::unique_ptr<Scene> build_scene(const pt_scene_desc *d_in, cudaStream_t st, b
     std::memset(&ps, 0, sizeof ps);
     ps.item = prim_item[prim];
     ps.light = -1;
-    ps.flags = prim_motion[prim] << 8;
+    ps.flags = (prim_motion[prim] << 8) | prim_face[prim];
     if (prim < B.n_tris) {
       const pt_mesh_desc &m = d->meshes[prim_mesh[prim]];
       const int t = prim_tri[prim];
@@ -2193,6 +2209,52 @@ int pt_sampler_eval(void *ctx, int32_t strategy, uint32_t seed, uint32_t first_i
   });
 }
 
+int pt_sample_eval(void *ctx, const pt_job_desc *job, int64_t first_path, int32_t n, int32_t dims, int32_t bounces,
+                   float *pixel_offsets, float *dim_values, float *light_offsets) {
+  Context *c = static_cast<Context *>(ctx);
+  PT_GUARD(c, {
+    c = as_ctx(ctx);
+    if (!job || n < 0 || dims < 0 || bounces < 0 || (dims > 0 && !dim_values) ||
+        (bounces > 0 && !light_offsets))
+      fail(PT_ERR_INVALID, "bad sample-eval args");
+    validate_job(*job);
+    const long long npix = (long long)job->width * job->height;
+    const int e = job->spp_end ? job->spp_end : job->spp_x * job->spp_y;
+    if (first_path < 0 || first_path + n > npix * (e - job->spp_begin))
+      fail(PT_ERR_INVALID, "paths outside the job's sample range");
+    if (n == 0) return PT_OK;
+    Scene *S = c->scene(job->scene);
+    DeviceJob J = c->device_job(*job, S);
+    const std::vector<float2> off = make_offsets(*job);
+    const int LN = job->light_samples_x * job->light_samples_y;
+    const size_t nn = (size_t)n;
+    // byte sizes of the offsets table and the three outputs, 256-byte aligned
+    const size_t b_off = (off.size() * sizeof(float2) + 255) / 256 * 256;
+    const size_t b_pix = (nn * 8 + 255) / 256 * 256;
+    const size_t b_dim = (nn * dims * 4 + 255) / 256 * 256;
+    const size_t b_lo = (nn * bounces * LN * 8 + 255) / 256 * 256;
+    char *buf = (char *)c->scratch(b_off + b_pix + b_dim + b_lo);
+    float2 *d_off = (float2 *)buf;
+    float *d_pix = (float *)(buf + b_off);
+    float *d_dim = (float *)(buf + b_off + b_pix);
+    float *d_lo = (float *)(buf + b_off + b_pix + b_dim);
+    cuda_check(cudaMemcpyAsync(d_off, off.data(), off.size() * sizeof(float2), cudaMemcpyHostToDevice, c->stream),
+               "h2d offsets");
+    J.job.offsets = d_off;
+    launch_path_samples(J, first_path, n, dims, bounces, pixel_offsets ? d_pix : nullptr, dims ? d_dim : nullptr,
+                        bounces ? d_lo : nullptr, c->stream);
+    cuda_check(cudaGetLastError(), "sample-eval launch");
+    if (pixel_offsets)
+      cuda_check(cudaMemcpyAsync(pixel_offsets, d_pix, nn * 8, cudaMemcpyDeviceToHost, c->stream), "d2h");
+    if (dims)
+      cuda_check(cudaMemcpyAsync(dim_values, d_dim, nn * dims * 4, cudaMemcpyDeviceToHost, c->stream), "d2h");
+    if (bounces)
+      cuda_check(cudaMemcpyAsync(light_offsets, d_lo, nn * bounces * LN * 8, cudaMemcpyDeviceToHost, c->stream),
+                 "d2h");
+    cuda_check(cudaStreamSynchronize(c->stream), "sample eval");
+  });
+}
+
 static int trace_common(void *ctx, int32_t scene_id, bool any, const float *rays, const float *tmaxs, int32_t n,
                         float tmin, float tmax, float *t, int32_t *prim, float *uv, uint8_t *occ) {
   Context *c = static_cast<Context *>(ctx);
@@ -2240,6 +2302,40 @@ int pt_trace_any(void *ctx, int32_t scene_id, const float *rays, const float *tm
                  uint8_t *occluded) {
   if (!tmax || !occluded) return PT_ERR_INVALID;
   return trace_common(ctx, scene_id, true, rays, tmax, n, tmin, 0.f, nullptr, nullptr, nullptr, occluded);
+}
+
+int pt_intersect(void *ctx, int32_t scene_id, const float *rays, int32_t n, float tmin, float tmax, float *t,
+                 int32_t *prim, float *position, float *normal, uint8_t *is_inside) {
+  Context *c = static_cast<Context *>(ctx);
+  PT_GUARD(c, {
+    c = as_ctx(ctx);
+    if (n < 0 || !rays || !t || !prim || !position || !normal || !is_inside) fail(PT_ERR_INVALID, "bad intersect args");
+    if (n == 0) return PT_OK;
+    Scene *S = c->scene(scene_id);
+    const size_t nn = (size_t)n;
+    char *buf = (char *)c->scratch(nn * (24 + 4 + 4 + 12 + 12 + 1) + 256);
+    float *dr = (float *)buf;
+    float *dt = (float *)(buf + nn * 24);
+    int *dp = (int *)(buf + nn * 28);
+    float *dpos = (float *)(buf + nn * 32);
+    float *dn = (float *)(buf + nn * 44);
+    uint8_t *df = (uint8_t *)(buf + nn * 56);
+    cuda_check(cudaMemcpyAsync(dr, rays, nn * 24, cudaMemcpyHostToDevice, c->stream), "h2d rays");
+    launch_intersect(S->view, dr, n, tmin, tmax, dt, dp, dpos, dn, df, c->d_err, c->stream);
+    cuda_check(cudaGetLastError(), "intersect launch");
+    cuda_check(cudaMemcpyAsync(t, dt, nn * 4, cudaMemcpyDeviceToHost, c->stream), "d2h");
+    cuda_check(cudaMemcpyAsync(prim, dp, nn * 4, cudaMemcpyDeviceToHost, c->stream), "d2h");
+    cuda_check(cudaMemcpyAsync(position, dpos, nn * 12, cudaMemcpyDeviceToHost, c->stream), "d2h");
+    cuda_check(cudaMemcpyAsync(normal, dn, nn * 12, cudaMemcpyDeviceToHost, c->stream), "d2h");
+    cuda_check(cudaMemcpyAsync(is_inside, df, nn, cudaMemcpyDeviceToHost, c->stream), "d2h");
+    cuda_check(cudaStreamSynchronize(c->stream), "intersect");
+    int herr = 0;
+    cuda_check(cudaMemcpy(&herr, c->d_err, sizeof(int), cudaMemcpyDeviceToHost), "read err");
+    if (herr) {
+      cudaMemset(c->d_err, 0, sizeof(int));
+      fail(PT_ERR_DEVICE, "device traversal error flag " + std::to_string(herr));
+    }
+  });
 }
 
 int pt_bsdf_eval(void *ctx, const pt_material_desc *mat, int32_t n, const float *wo, const float *wi,

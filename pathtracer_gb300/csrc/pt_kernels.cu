@@ -34,6 +34,40 @@ __global__ void k_sampler_eval(int strategy, const uint16_t *perm, uint32_t firs
   }
 }
 
+// Sample values of the paths [first, first + n) of a single-job wave, from
+// the device functions the camera and shade stages call: the pixel-grid
+// offset of the path's sample (k_camera), the sampler dimensions
+// 0..dims-1 (sampler_dim) and, per bounce b < bounces, the LN light-point
+// offsets (light_offset at the vertex's slot base 64 + 32 b).
+__global__ void k_path_samples(DeviceJob J, long long first, int n, int dims, int bounces, int LN, float *pix,
+                               float *dv, float *lo) {
+  for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x) {
+    const PathId P = path_id(J, first + s);
+    if (pix) {
+      const float2 o = J.job.offsets[P.k];
+      pix[2 * (size_t)s] = o.x;
+      pix[2 * (size_t)s + 1] = o.y;
+    }
+    if (dv)
+      for (int d = 0; d < dims; ++d)
+        dv[(size_t)s * dims + d] = sampler_dim(J, d, P.halton_index, P.key, P.pix, P.k);
+    if (lo)
+      for (int b = 0; b < bounces; ++b)
+        for (int ls = 0; ls < LN; ++ls) {
+          const float2 o = light_offset(J, P.key, 64u + 32u * (uint32_t)b, ls);
+          const size_t i = (((size_t)s * bounces + b) * LN + ls) * 2;
+          lo[i] = o.x;
+          lo[i + 1] = o.y;
+        }
+  }
+}
+
+void launch_path_samples(const DeviceJob &J, long long first, int n, int dims, int bounces, float *pix, float *dv,
+                         float *lo, cudaStream_t st) {
+  const int LN = J.job.light_nx * J.job.light_ny;
+  k_path_samples<<<grid_for(n, 128, 152 * 8), 128, 0, st>>>(J, first, n, dims, bounces, LN, pix, dv, lo);
+}
+
 template <bool ANY>
 __global__ void __launch_bounds__(128) k_trace_test(SceneView S, const float *rays, const float *tmaxs,
                                                     int n, float tmin, float tmax, float *t_out,
@@ -55,6 +89,40 @@ __global__ void __launch_bounds__(128) k_trace_test(SceneView S, const float *ra
       uv_out[2 * i + 1] = h.v;
     }
   }
+}
+
+// Hittable::intersect's HitRecord (base/primitive.hpp:30-79) at the closest
+// hit: t, primitive, position, the normal turned towards the ray
+// (HitRecord::set_normal) and is_inside (the front-face flag, FlipFace
+// toggled) -- what surface_at gives the shade stage.
+__global__ void __launch_bounds__(128) k_intersect(SceneView S, const float *rays, int n, float tmin, float tmax,
+                                                   float *t_out, int *prim_out, float *pos, float *nrm,
+                                                   uint8_t *front, int *err) {
+  __shared__ int32_t stack[PT_STACK * 128];
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const V3 o = v3(rays[6 * i], rays[6 * i + 1], rays[6 * i + 2]);
+    const V3 d = v3(rays[6 * i + 3], rays[6 * i + 4], rays[6 * i + 5]);
+    HitRec h;
+    const bool r = traverse<false>(S, o, d, tmin, tmax, h, stack + threadIdx.x, blockDim.x, err);
+    Surf sf;
+    sf.p = sf.n = v3(0.f);
+    sf.front = false;
+    if (r) sf = surface_at(S, o, d, h, 0.f);
+    t_out[i] = r ? h.t : FLT_MAX;
+    prim_out[i] = r ? h.prim : -1;
+    pos[3 * i] = sf.p.x;
+    pos[3 * i + 1] = sf.p.y;
+    pos[3 * i + 2] = sf.p.z;
+    nrm[3 * i] = sf.n.x;
+    nrm[3 * i + 1] = sf.n.y;
+    nrm[3 * i + 2] = sf.n.z;
+    front[i] = (r && sf.front) ? 1 : 0;
+  }
+}
+
+void launch_intersect(const SceneView &S, const float *rays, int n, float tmin, float tmax, float *t, int *prim,
+                      float *pos, float *nrm, uint8_t *front, int *err, cudaStream_t st) {
+  k_intersect<<<grid_for(n, 128, 152 * 8), 128, 0, st>>>(S, rays, n, tmin, tmax, t, prim, pos, nrm, front, err);
 }
 
 __global__ void k_bsdf_eval(const MatRec *m, int n, const float *wo, const float *wi,

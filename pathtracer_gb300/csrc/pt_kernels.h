@@ -102,6 +102,10 @@ struct KernelInfo {
 };
 
 void upload_halton_tables(const HaltonTables &T, cudaStream_t st);
+void launch_intersect(const SceneView &S, const float *rays, int n, float tmin, float tmax, float *t, int *prim,
+                      float *pos, float *nrm, uint8_t *front, int *err, cudaStream_t st);
+void launch_path_samples(const DeviceJob &J, long long first, int n, int dims, int bounces, float *pix, float *dv,
+                         float *lo, cudaStream_t st);
 void launch_sampler_eval(int strategy, const uint16_t *perm, uint32_t first, int n, int dims,
                          float *out, cudaStream_t st);
 void launch_trace_test(const SceneView &S, bool any, const float *rays, const float *tmaxs, int n,

@@ -56,6 +56,9 @@ struct alignas(16) PrimShade {
 static_assert(sizeof(PrimShade) == 64, "PrimShade must be 64 bytes");
 #define PT_PRIM_SMOOTH 1
 #define PT_PRIM_FLIP 2
+// pt_object_desc.face != PT_FACE_AS_HIT: is_inside is fixed, to FACE_FRONT's value
+#define PT_PRIM_FACE_FIXED 64
+#define PT_PRIM_FACE_FRONT 128
 #define PT_PRIM_KIND(f) (((f) >> 2) & 3)
 #define PT_PRIM_AXIS(f) (((f) >> 4) & 3)
 #define PT_PRIM_MOTION(f) ((f) >> 8)  // motion index + 1 (0: static)

@@ -193,6 +193,7 @@ __device__ inline Surf surface_at(const SceneView &S, V3 o, V3 d, const HitRec &
   s.front = dot(d, n) < 0.f;  // set_normal (materialBase.hpp:48-52)
   s.n = s.front ? n : -n;
   if (ps.flags & PT_PRIM_FLIP) s.front = !s.front;
+  if (ps.flags & PT_PRIM_FACE_FIXED) s.front = (ps.flags & PT_PRIM_FACE_FRONT) != 0;
   return s;
 }
 
@@ -483,6 +484,17 @@ __device__ __forceinline__ float power_heuristic(float nf, float fpdf, float ng,
   return (f2 + g2) > 0.f ? f2 / (f2 + g2) : 0.f;
 }
 
+// Light-point offset of light sample ls at a vertex: the jittered
+// light_nx x light_ny grid of getOffsets (random.hpp:47-63) that
+// maxdepth_nee.hpp:91 draws per shading vertex, stratum (i, j) = (ls / ny,
+// ls % ny), i outer; the jitter from the path's counter stream at the
+// vertex's slot base rbase.
+__device__ __forceinline__ float2 light_offset(const DeviceJob &J, uint64_t key, uint32_t rbase, int ls) {
+  const int si = ls / J.job.light_ny, sj = ls % J.job.light_ny;
+  return make_float2(((float)si + rand01(key, rbase + 2u * ls)) / (float)J.job.light_nx,
+                     ((float)sj + rand01(key, rbase + 2u * ls + 1u)) / (float)J.job.light_ny);
+}
+
 // Next-event estimation at one vertex (maxdepth_nee.hpp:89-232): LN light
 // samples on a stratified x-by-y grid, each a ShadowQueue entry with its
 // unoccluded contribution.  MED: the vertex is a medium scattering event
@@ -498,10 +510,8 @@ __device__ __forceinline__ void next_event(const SceneView &S, const DeviceJob &
   const bool med = S.has_medium != 0;
   for (int ls = 0; ls < LN; ++ls) {
     float4 shd = make_float4(0.f, 0.f, 0.f, -1.f), shc = make_float4(0.f, 0.f, 0.f, 0.f);
-    // getOffsets(x, y): stratum (i, j), i outer (random.hpp:47-63)
-    const int si = ls / J.job.light_ny, sj = ls % J.job.light_ny;
-    float ox = ((float)si + rand01(key, rbase + 2u * ls)) / (float)J.job.light_nx;
-    float oy = ((float)sj + rand01(key, rbase + 2u * ls + 1u)) / (float)J.job.light_ny;
+    const float2 lo = light_offset(J, key, rbase, ls);
+    const float ox = lo.x, oy = lo.y;
     int li = (int)(rand01(key, rbase + 20u + ls) * S.n_lights) % S.n_lights;
     const LightRec &Lr = S.lights[li];
     V3 wl, Le;

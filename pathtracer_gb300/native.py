@@ -34,8 +34,8 @@ EXPORTS = [
     "pt_create", "pt_destroy", "pt_last_error", "pt_version", "pt_scene_upload", "pt_scene_release",
     "pt_bvh_build", "pt_set_bvh_builder", "pt_bvh_build_device", "pt_bvh_build_sah", "pt_obj_load", "pt_obj_free", "pt_load_image", "pt_free_image", "pt_scene_info", "pt_render", "pt_render_device", "pt_render_device_noalloc",
     "pt_profile_begin",
-    "pt_profile_end", "pt_tonemap", "pt_gaussian_blur", "pt_write_png", "pt_sampler_eval", "pt_trace_closest",
-    "pt_trace_any", "pt_bsdf_eval", "pt_bsdf_sample", "pt_render_batch", "pt_autotune", "pt_server_create",
+    "pt_profile_end", "pt_tonemap", "pt_gaussian_blur", "pt_write_png", "pt_sampler_eval", "pt_sample_eval", "pt_trace_closest",
+    "pt_trace_any", "pt_intersect", "pt_bsdf_eval", "pt_bsdf_sample", "pt_render_batch", "pt_autotune", "pt_server_create",
     "pt_server_destroy", "pt_submit", "pt_server_step", "pt_poll", "pt_cancel",
 ]
 
@@ -80,7 +80,7 @@ class SphereDesc(C.Structure):
 
 
 class ObjectDesc(C.Structure):
-    _fields_ = [("kind", C.c_int32), ("index", C.c_int32), ("velocity", C.c_float * 3)]
+    _fields_ = [("kind", C.c_int32), ("index", C.c_int32), ("velocity", C.c_float * 3), ("face", C.c_int32)]
 
 
 class BoxDesc(C.Structure):
@@ -185,8 +185,10 @@ def load() -> C.CDLL:
         "pt_gaussian_blur": [vp, f32p, f32p, C.c_int32, C.c_int32, C.c_int32, C.c_float],
         "pt_write_png": [C.c_char_p, u8p, C.c_int32, C.c_int32],
         "pt_sampler_eval": [vp, C.c_int32, C.c_uint32, C.c_uint32, C.c_int32, C.c_int32, f32p],
+        "pt_sample_eval": [vp, C.POINTER(JobDesc), C.c_int64, C.c_int32, C.c_int32, C.c_int32, f32p, f32p, f32p],
         "pt_trace_closest": [vp, C.c_int32, f32p, C.c_int32, C.c_float, C.c_float, f32p, i32p, f32p],
         "pt_trace_any": [vp, C.c_int32, f32p, f32p, C.c_int32, C.c_float, u8p],
+        "pt_intersect": [vp, C.c_int32, f32p, C.c_int32, C.c_float, C.c_float, f32p, i32p, f32p, f32p, u8p],
         "pt_bsdf_eval": [vp, C.POINTER(MaterialDesc), C.c_int32, f32p, f32p, f32p, u8p, f32p, f32p],
         "pt_bsdf_sample": [vp, C.POINTER(MaterialDesc), C.c_int32, f32p, f32p, u8p, f32p, f32p, u8p, f32p,
                            f32p, f32p, u32p],
@@ -284,7 +286,8 @@ def make_scene_desc(scene) -> SceneBuffers:
     d.spheres = spheres
     d.n_spheres = len(scene.spheres)
     objs = (ObjectDesc * max(1, len(scene.objects)))(
-        *[ObjectDesc(o[0], o[1], (C.c_float * 3)(*[float(x) for x in (o[2] if len(o) > 2 else (0, 0, 0))]))
+        *[ObjectDesc(o[0], o[1], (C.c_float * 3)(*[float(x) for x in (o[2] if len(o) > 2 else (0, 0, 0))]),
+                     int(o[3]) if len(o) > 3 else 0)
           for o in scene.objects])
     sb.hold(objs)
     d.objects = objs
@@ -492,6 +495,17 @@ class Renderer:
                                              _ptr(out, C.c_float)))
         return out
 
+    def sample_eval(self, job: JobDesc, first_path: int, n: int, dims: int, bounces: int = 0):
+        """pt_sample_eval: (pixel offsets (n, 2), dimension values (n, dims),
+        light offsets (n, bounces, LN, 2)) of the job's paths first_path..+n."""
+        ln = job.light_samples_x * job.light_samples_y
+        pix = np.zeros((n, 2), np.float32)
+        dv = np.zeros((n, dims), np.float32)
+        lo = np.zeros((n, bounces, ln, 2), np.float32)
+        self._check(self.lib.pt_sample_eval(self.ctx, C.byref(job), first_path, n, dims, bounces,
+                                            _ptr(pix, C.c_float), _ptr(dv, C.c_float), _ptr(lo, C.c_float)))
+        return pix, dv, lo
+
     def trace_closest(self, sid: int, rays: np.ndarray, tmin: float = 1e-4, tmax: float = 1e5):
         rays = np.ascontiguousarray(rays, dtype=np.float32)
         n = rays.shape[0]
@@ -509,6 +523,20 @@ class Renderer:
         self._check(self.lib.pt_trace_any(self.ctx, sid, _ptr(rays, C.c_float), _ptr(tmax, C.c_float),
                                           rays.shape[0], tmin, _ptr(occ, C.c_uint8)))
         return occ
+
+    def intersect(self, sid: int, rays: np.ndarray, tmin: float = 1e-4, tmax: float = 1e5):
+        """pt_intersect: (t, prim, position, normal, is_inside) of each ray's closest hit."""
+        rays = np.ascontiguousarray(rays, dtype=np.float32)
+        n = rays.shape[0]
+        t = np.zeros(n, np.float32)
+        prim = np.zeros(n, np.int32)
+        pos = np.zeros((n, 3), np.float32)
+        nrm = np.zeros((n, 3), np.float32)
+        ins = np.zeros(n, np.uint8)
+        self._check(self.lib.pt_intersect(self.ctx, sid, _ptr(rays, C.c_float), n, tmin, tmax, _ptr(t, C.c_float),
+                                          _ptr(prim, C.c_int32), _ptr(pos, C.c_float), _ptr(nrm, C.c_float),
+                                          _ptr(ins, C.c_uint8)))
+        return t, prim, pos, nrm, ins
 
     def bsdf_eval(self, mat: MaterialDesc, wo, wi, normal, front):
         wo, wi, normal = (np.ascontiguousarray(a, dtype=np.float32) for a in (wo, wi, normal))

@@ -106,6 +106,87 @@ def make_trace():
                         shadow_tmax=tmax, occluded=occ)
 
 
+# Decorator chains of the transform fixture (objectTransform.hpp), innermost
+# first: (code, p0, p1, p2) with 0 Translate, 1 Rotate<X>, 2 Rotate<Y>,
+# 3 Rotate<Z>, 4 Scale, 5 FlipFace; over a mesh (flat icosphere, radius 0.5),
+# a rectangle (XZ at y = 0.2) or a sphere (radius 0.45 at (0.1, -0.05, 0.2)).
+TRANSFORM_CASES = [
+    ("mesh_translate", 0, [(0, 0.3, -0.2, 0.5)]),
+    ("mesh_rotx", 0, [(1, 0.7, 0, 0)]),
+    ("mesh_roty_translate", 0, [(2, -1.1, 0, 0), (0, 0.2, 0.1, 0.0)]),
+    ("mesh_rotz", 0, [(3, 0.4, 0, 0)]),
+    ("mesh_scale", 0, [(4, 1.7, 0, 0)]),
+    ("mesh_flip", 0, [(5, 0, 0, 0)]),
+    ("mesh_chain", 0, [(4, 0.5, 0, 0), (1, 0.3, 0, 0), (5, 0, 0, 0), (0, -0.1, 0.2, 0.3), (3, -0.8, 0, 0)]),
+    ("quad_translate", 1, [(0, 0.1, 0.3, -0.2)]),
+    ("quad_rotz", 1, [(3, 0.3, 0, 0)]),
+    ("quad_rotx", 1, [(1, -0.5, 0, 0)]),
+    ("quad_flip", 1, [(5, 0, 0, 0)]),
+    ("quad_scale", 1, [(4, 1.4, 0, 0)]),
+    ("sphere_scale", 2, [(4, 0.6, 0, 0)]),
+    ("sphere_roty_translate", 2, [(2, 0.9, 0, 0), (0, -0.3, 0.2, 0.1)]),
+    ("sphere_flip", 2, [(5, 0, 0, 0)]),
+]
+
+
+def transform_base(kind):
+    """The untransformed object of a transform case (scene with one object)."""
+    sc = S.Scene()
+    m = sc.add_material(N.LAMBERTIAN, [0.5, 0.5, 0.5])
+    if kind == 0:
+        v, f = S.icosphere(1)
+        sc.add_mesh(S.Mesh((0.5 * v).astype(np.float32), f.astype(np.int32), None, m))
+    elif kind == 1:
+        sc.add_quad(1, 0.2, -0.5, 0.5, -0.4, 0.6, m)
+    else:
+        sc.add_sphere((0.1, -0.05, 0.2), 0.45, m)
+    return sc
+
+
+def transform_rays(n, rng):
+    # unit-length rays (as the renderer traces them) from a shell of radius 3
+    # towards points near the object
+    o = unit(rng.normal(size=(n, 3))) * 3.0
+    tgt = rng.uniform(-0.8, 0.8, size=(n, 3))
+    return np.concatenate([o, unit(tgt - o)], 1).astype(np.float32)
+
+
+def transform_point(p, ops):
+    """A point of the untransformed object seen in the world through the
+    decorators (the inverse of the ray mappings of objectTransform)."""
+    p = np.array(p, np.float64)
+    for code, a, b, c in ops:
+        if code == 0:
+            p = p + np.array([a, b, c])
+        elif code in (1, 2, 3):
+            i, j = {1: (1, 2), 2: (0, 2), 3: (0, 1)}[code]
+            cs, sn = math.cos(a), math.sin(a)
+            p[i], p[j] = cs * p[i] + sn * p[j], -sn * p[i] + cs * p[j]
+        elif code == 4:
+            p = p * a
+    return p
+
+
+def make_transforms():
+    rng = np.random.default_rng(23)
+    out = {}
+    for name, kind, ops in TRANSFORM_CASES:
+        rs = R.RefScene(transform_base(kind))
+        rs.transform(0, ops)
+        rays = transform_rays(256, rng)
+        if kind != 1:
+            # rays from inside the object: back-face hits
+            c = transform_point((0.0, 0.0, 0.0) if kind == 0 else (0.1, -0.05, 0.2), ops)
+            o = c + rng.uniform(-0.05, 0.05, size=(64, 3))
+            rays = np.concatenate([rays, np.concatenate([o, unit(rng.normal(size=(64, 3)))], 1)], 0)
+            rays = rays.astype(np.float32)
+        t, prim, pos, nrm, inside = rs.trace_closest(rays)
+        out.update({f"{name}__kind": np.int32(kind), f"{name}__ops": np.array(ops, np.float32),
+                    f"{name}__rays": rays, f"{name}__hit": (prim >= 0).astype(np.uint8), f"{name}__t": t,
+                    f"{name}__pos": pos, f"{name}__nrm": nrm, f"{name}__inside": inside})
+    np.savez_compressed(OUT / "transforms.npz", **out)
+
+
 def make_bsdf():
     rng = np.random.default_rng(5)
     out = {}
@@ -176,6 +257,7 @@ if __name__ == "__main__":
         raise SystemExit("build oracle/_ref first: oracle/ref/build_ref.sh")
     make_samplers()
     make_trace()
+    make_transforms()
     make_bsdf()
     make_images()
     make_tonemap()
