@@ -416,6 +416,20 @@ int pt_render_device(void *ctx, const pt_job_desc *job, float *d_film_sum,
  * contexts of the same device) race and must be serialised by the caller. */
 int pt_render_device_noalloc(void *ctx, const pt_job_desc *job, float *d_film_sum, pt_stats *stats);
 
+/* getRayColor (include/integrator/maxdepth_nee.hpp:9-256, the integrator
+ * SceneInfo::render calls per sample) for n given primary rays of scene
+ * job->scene: radiance (host, 3n floats) receives one path's estimate per
+ * ray, with the job's integrator settings (estimator, max_depth, rr_start,
+ * sampler, env_sampling, light samples, seed, camera shutter); its camera,
+ * size, spp and window are not used.  rays: n * 6 floats (origin,
+ * direction; the direction is normalised, as the render's camera rays are).
+ * Path i draws Halton index first_index + i (HaltonSampler::startSample,
+ * sampler.hpp:34-39; first_index >= 1) and that index's counter streams --
+ * the same draws as sample k of frame pixel (i, j) of a render when
+ * first_index + i = 1 + (i * height + j) * spp + k. */
+int pt_ray_color(void *ctx, const pt_job_desc *job, const float *rays, int32_t n, uint32_t first_index,
+                 float *radiance);
+
 /* Per-stage device timing of the wave kernels (no counterpart in the
  * reference, which times only the whole render, renderManager.hpp:164-173).
  * pt_profile_begin clears and enables CUDA-event timing on the context's
@@ -491,6 +505,26 @@ int pt_trace_any(void *ctx, int32_t scene_id, const float *rays,
  * to their geometry. */
 int pt_intersect(void *ctx, int32_t scene_id, const float *rays, int32_t n, float tmin, float tmax,
                  float *t, int32_t *prim, float *position, float *normal, uint8_t *is_inside);
+
+/* The Light interface (include/light/light.hpp:17-53) of light `light` of a
+ * resident scene -- the records the render's NEE samples.  Lights are
+ * numbered in discovery order (DiffuseEmitter rectangles and spheres in
+ * object order, lightDiscovery.hpp:5-81), the environment last; their count
+ * is pt_scene_info's [4].  For item i, with offsets (u, v) = uv[2i], uv[2i+1]
+ * and shading point x[3i..3i+2]:
+ *   point[3i]  get_sample(u, v)   QuadLight light.hpp:131-137 (v0 + u e1 + v e2),
+ *              SphereLight :254-264 (the whole sphere), EnvironmentLight
+ *              envLight.hpp:20-36 (uniform sphere direction * 1e5)
+ *   normal[3i] get_normal_at(point)          light.hpp:139-145, 266-271; envLight.hpp:48-51
+ *   dir[3i]    normalize(point - x)           (maxdepth_nee.hpp:114, 141-144)
+ *   le[3i]     L_emit at the sample towards x, texCoords (u, v)  light.hpp:157-165,
+ *              296-303; envLight.hpp:73-90 (the HDRI along dir)
+ *   pdf[i]     pdf_value(x, dir)              light.hpp:164-205, 279-294; envLight.hpp:58-70
+ *              -- or pdf_value(x, pdf_dir[3i..]) when pdf_dir (3n) is not NULL
+ * and *area (may be NULL) = get_area() (INFINITY for the environment). */
+int pt_light_sample(void *ctx, int32_t scene_id, int32_t light, int32_t n, const float *uv, const float *x,
+                    const float *pdf_dir, float *point, float *normal, float *dir, float *le, float *pdf,
+                    float *area);
 
 /* BSDF evaluation (Material::f and Material::scatter_pdf(wo, wi, rec),
  * material.hpp:32-61).  Arrays of n items, 3 floats per vector. `front` is

@@ -720,6 +720,7 @@ struct Obj {
 struct Light {
   int type;  // 0 quad, 1 sphere, 2 env
   V v0, e1, e2, normal, c, color;
+  V v2;  // quad: vertices[2]
   V vel;
   bool moving = false;
   int texture = 0;  // texture index + 1 of the colour (0: color)
@@ -1246,6 +1247,7 @@ Scene *build_scene(const pt_scene_desc *d) {
       V v0 = put(ob.d0min, ob.d1min), v1 = put(ob.d0max, ob.d1min), v3 = put(ob.d0min, ob.d1max);
       L.type = 0;
       L.v0 = v0;
+      L.v2 = put(ob.d0max, ob.d1max);
       L.e1 = v1 - v0;
       L.e2 = v3 - v0;
       L.normal = cross(L.e1, L.e2).normalize();
@@ -1386,6 +1388,79 @@ static std::pair<float, float> light_offset(const PathCtx &P, int bounce, int ls
           ((float)sj + rand01(P.key, rbase + 2u * ls + 1u)) / (float)j.light_samples_y};
 }
 
+// A point of light L seen from x: get_sample(ox, oy) (light.hpp:131-137,
+// 254-264; envLight.hpp:20-36 over the uniform sphere), get_normal_at there,
+// the direction and distance from x, L_emit towards x (texCoords (ox, oy)).
+struct LightPointO {
+  V p, n, w, Le;
+  float len;
+};
+static LightPointO light_point(const Scene &S, const Light &L, float ox, float oy, V x, float tm) {
+  LightPointO r;
+  if (L.type == 2) {  // uniformSampleSphere * 1e5 (random.hpp:7-15, envLight.hpp:26-43)
+    float z = 1.0f - 2.0f * ox;
+    float rr = std::sqrt(std::max(0.f, 1.f - z * z));
+    float phi = (float)(2.0f * PI * oy);
+    r.p = V(rr * std::cos(phi), rr * std::sin(phi), z) * 1e5f;
+    r.w = (r.p - x).normalize();
+    r.len = (r.p - x).length();
+    r.n = -r.p.normalize();
+    r.Le = S.env_le(r.w);
+    return r;
+  }
+  if (L.type == 0) {  // QuadLight::get_sample / get_normal_at
+    r.p = L.v0 + ox * L.e1 + oy * L.e2;
+    if (L.moving) r.p = V(r.p.x + L.vel.x * tm, r.p.y + L.vel.y * tm, r.p.z + L.vel.z * tm);
+    r.n = L.normal;
+  } else {  // SphereLight::get_sample
+    float theta = (float)(2 * PI * ox);
+    float phi = std::acos(2 * oy - 1);
+    const V c = L.moving ? V(L.c.x + L.vel.x * tm, L.c.y + L.vel.y * tm, L.c.z + L.vel.z * tm) : L.c;
+    r.p = c + L.radius * V(std::sin(phi) * std::cos(theta), std::sin(phi) * std::sin(theta), std::cos(phi));
+    r.n = (r.p - c).normalize();
+  }
+  V ld = r.p - x;
+  r.len = ld.length();
+  r.w = ld.normalize();
+  // L_emit (light.hpp:157-165, 296-303); a textured light at the sample's
+  // offsets (maxdepth_nee.hpp:175-176)
+  const V lcol = L.texture ? tex_eval(S.texs[L.texture - 1], ox, oy) : L.color;
+  r.Le = (dot(r.n, -r.w) > 0.0f) ? lcol * L.intensity : V(0.f);
+  return r;
+}
+
+// Light::pdf_value(origin, dir): QuadLight light.hpp:164-205 (plane hit,
+// the two triangles' edge tests as the reference writes them, dist^2 /
+// (area |cos|)), SphereLight :279-294 (1 / visible cap solid angle),
+// EnvironmentLight envLight.hpp:58-70 (HDRITexture::pdf_direction, 1 / 4 pi).
+static float light_pdf_value(const Light &L, V origin, V dir) {
+  if (L.type == 2) return (float)(1.f / (4.f * PI));
+  if (L.type == 1) {
+    V wc = L.c - origin;
+    float dc2 = dot(wc, wc), r2 = L.radius * L.radius;
+    if (dc2 <= r2) return (float)(1.f / (4.f * PI));
+    float cos_max = std::sqrt(1.f - r2 / dc2);
+    float omega = (float)(2.f * PI * (1.f - cos_max));
+    return 1.f / omega;
+  }
+  const V v0 = L.v0, v1 = L.v0 + L.e1, v3 = L.v0 + L.e2, N = L.normal;
+  float denom = dot(N, dir);
+  if (std::fabs(denom) < 1e-6f) return 0.f;
+  float t = dot(v0 - origin, N) / denom;
+  if (t <= 0) return 0.f;
+  V P = origin + dir * t;
+  auto in_tri = [&](V A, V B, V C) {
+    if (dot(cross(B - A, C - A), N) < 0) return false;
+    if (dot(cross(C - B, P - B), N) < 0) return false;
+    if (dot(cross(A - C, P - C), N) < 0) return false;
+    return true;
+  };
+  if (!in_tri(v0, v1, L.v2) && !in_tri(v0, L.v2, v3)) return 0.f;
+  float dist2 = dot(P - origin, P - origin);
+  float cos_t = std::fabs(dot(N, -dir));
+  return dist2 / (L.area * cos_t);
+}
+
 // One NEE light sample (maxdepth_nee.hpp:94-210) at shading point x with
 // normal n.  surface: NoI weights G; in a medium (surface=false) G = NoL/d2.
 static LightSample sample_light(const PathCtx &P, V x, V n, int bounce, int ls, bool surface) {
@@ -1402,12 +1477,8 @@ static LightSample sample_light(const PathCtx &P, V x, V n, int bounce, int ls, 
     float pdir;
     if (j.env_sampling == PT_ENV_ALIAS) {
       r.wl = S.env_alias_sample(ox, oy, rand01(P.key, rbase + 28u + ls), pdir);
-    } else {  // uniformSampleSphere * 1e5 (random.hpp:7-15, envLight.hpp:26-43)
-      float z = 1.0f - 2.0f * ox;
-      float rr = std::sqrt(std::max(0.f, 1.f - z * z));
-      float phi = (float)(2.0f * PI * oy);
-      V pinf = V(rr * std::cos(phi), rr * std::sin(phi), z) * 1e5f;
-      r.wl = (pinf - x).normalize();
+    } else {
+      r.wl = light_point(S, L, ox, oy, x, P.time).w;
       pdir = (float)(1.f / (4.f * PI));
     }
     r.env = true;
@@ -1419,22 +1490,10 @@ static LightSample sample_light(const PathCtx &P, V x, V n, int bounce, int ls, 
     r.valid = r.pdf > 1e-7f;
     return r;
   }
-  V lp, ln;
-  const float tm = P.time;
-  if (L.type == 0) {  // QuadLight::get_sample / get_normal_at
-    lp = L.v0 + ox * L.e1 + oy * L.e2;
-    if (L.moving) lp = V(lp.x + L.vel.x * tm, lp.y + L.vel.y * tm, lp.z + L.vel.z * tm);
-    ln = L.normal;
-  } else {  // SphereLight::get_sample
-    float theta = (float)(2 * PI * ox);
-    float phi = std::acos(2 * oy - 1);
-    const V c = L.moving ? V(L.c.x + L.vel.x * tm, L.c.y + L.vel.y * tm, L.c.z + L.vel.z * tm) : L.c;
-    lp = c + L.radius * V(std::sin(phi) * std::cos(theta), std::sin(phi) * std::sin(theta), std::cos(phi));
-    ln = (lp - c).normalize();
-  }
-  V ld = lp - x;
-  float len = ld.length();
-  r.wl = ld.normalize();
+  const LightPointO lp = light_point(S, L, ox, oy, x, P.time);
+  const V ln = lp.n;
+  const float len = lp.len;
+  r.wl = lp.w;
   r.valid = len >= 0.001f;
   r.tmax = len - 0.001f;
   r.pdf = (L.area <= 1e-7f) ? 0.f : 1.f / (L.area * (float)nl);
@@ -1442,10 +1501,7 @@ static LightSample sample_light(const PathCtx &P, V x, V n, int bounce, int ls, 
   r.NoL = std::max(0.f, dot(ln, -r.wl));
   r.d2 = len * len;
   r.G = (r.d2 < 1e-7f) ? 0.f : r.NoL * r.NoI / r.d2;
-  // L_emit (light.hpp:157-165, 296-303); a textured light at the sample's
-  // offsets (maxdepth_nee.hpp:175-176)
-  const V lcol = L.texture ? tex_eval(S.texs[L.texture - 1], ox, oy) : L.color;
-  r.Le = (dot(ln, -r.wl) > 0.0f) ? lcol * L.intensity : V(0.f);
+  r.Le = lp.Le;
   if (!(r.pdf > 1e-7f)) r.valid = false;
   return r;
 }
@@ -1750,6 +1806,28 @@ void or_trace_closest(void *s, const float *rays, int n, float tmin, float tmax,
   }
 }
 
+// The Light methods of light `light` at n items (u, v, x): get_sample,
+// get_normal_at, direction from x, L_emit towards x, pdf_value(x, dir);
+// *area = get_area(); pdf_dir (may be NULL): pdf_value(x, pdf_dir[i]).
+// Returns -1 for a bad light index.
+int or_light_eval(void *s, int light, int n, const float *uv, const float *x, const float *pdf_dir, float *point,
+                  float *normal, float *dir, float *le, float *pdf, float *area) {
+  const Scene &S = *static_cast<Scene *>(s);
+  if (light < 0 || light >= (int)S.lights.size()) return -1;
+  const Light &L = S.lights[light];
+  *area = L.type == 2 ? INFINITY : L.area;
+  for (int i = 0; i < n; ++i) {
+    const V xi(x[3 * i], x[3 * i + 1], x[3 * i + 2]);
+    const LightPointO lp = light_point(S, L, uv[2 * i], uv[2 * i + 1], xi, 0.f);
+    const V out[4] = {lp.p, lp.n, lp.w, lp.Le};
+    float *dst[4] = {point, normal, dir, le};
+    for (int k = 0; k < 4; ++k)
+      for (int c = 0; c < 3; ++c) dst[k][3 * i + c] = out[k][c];
+    pdf[i] = light_pdf_value(L, xi, pdf_dir ? V(pdf_dir[3 * i], pdf_dir[3 * i + 1], pdf_dir[3 * i + 2]) : lp.w);
+  }
+  return 0;
+}
+
 // The HitRecord of each ray's closest hit: t, prim, position, normal (turned
 // towards the ray) and is_inside.
 void or_intersect(void *s, const float *rays, int n, float tmin, float tmax, float *t, int *prim, float *pos,
@@ -1864,6 +1942,34 @@ int or_gaussian_blur(const float *in, float *out, int W, int H, int kernel, floa
       for (int ch = 0; ch < 3; ++ch) out[3 * ((size_t)i * W + j) + ch] = c[ch];
     }
   return 0;
+}
+
+// getRayColor for n given primary rays (pt_ray_color's contract): path i is
+// frame pixel (first_index - 1 + i, 0) of a one-row frame at 1 spp, Halton
+// index first_index + i; its direction is normalised.  recursive: the
+// REF_NEE recursion when the job's estimator is REF_NEE and there is no medium.
+void or_ray_color(void *s, const pt_job_desc *job, const float *rays, int n, uint32_t first_index, float *out,
+                  int recursive) {
+  const Scene &S = *static_cast<Scene *>(s);
+  pt_job_desc j = *job;
+  j.width = n;
+  j.height = 1;
+  j.spp_x = j.spp_y = 1;
+  j.spp_begin = j.spp_end = 0;
+  j.crop_x = (int32_t)(first_index - 1u);
+  j.crop_y = 0;
+  j.full_width = (int32_t)(first_index - 1u) + n;
+  j.full_height = 1;
+  const bool use_rec = recursive && !S.medium && j.estimator == PT_EST_REF_NEE;
+  for (int i = 0; i < n; ++i) {
+    const uint64_t lin = (uint64_t)(first_index - 1u) + i;
+    PathCtx P{&S, &j, path_key(j.seed, lin), (uint32_t)(lin + 1u), (int)lin, 0};
+    P.time = j.camera.shutter > 0.f ? j.camera.shutter * rand01(P.key, 3u) : 0.f;
+    const V o(rays[6 * i], rays[6 * i + 1], rays[6 * i + 2]);
+    const V d = V(rays[6 * i + 3], rays[6 * i + 4], rays[6 * i + 5]).normalize();
+    const V c = use_rec ? ray_color_ref(P, o, d, j.max_depth, 0) : ray_color_iter(P, o, d);
+    for (int ch = 0; ch < 3; ++ch) out[3 * i + ch] = c[ch];
+  }
 }
 
 int or_render(void *s, const pt_job_desc *job, float *mean, float *var, int threads, int recursive) {

@@ -32,6 +32,9 @@ def load():
         lib.or_scene_destroy.argtypes = [C.c_void_p]
         lib.or_scene_num_lights.argtypes = [C.c_void_p]
         lib.or_sampler_eval.argtypes = [C.c_int, C.c_uint32, C.c_uint32, C.c_int, C.c_int, f32p]
+        lib.or_ray_color.argtypes = [C.c_void_p, C.POINTER(N.JobDesc), f32p, C.c_int, C.c_uint32, f32p, C.c_int]
+        lib.or_light_eval.argtypes = [C.c_void_p, C.c_int, C.c_int, f32p, f32p, f32p, f32p, f32p, f32p, f32p, f32p,
+                                      f32p]
         lib.or_intersect.argtypes = [C.c_void_p, f32p, C.c_int, C.c_float, C.c_float, f32p, i32p, f32p, f32p, u8p]
         lib.or_path_samples.argtypes = [C.POINTER(N.JobDesc), C.c_int64, C.c_int, C.c_int, C.c_int, f32p, f32p,
                                         f32p]
@@ -69,6 +72,32 @@ class OracleScene:
         prim = np.zeros(n, np.int32)
         self.lib.or_trace_closest(self.h, _p(rays, C.c_float), n, tmin, tmax, _p(t, C.c_float), _p(prim, C.c_int32))
         return t, prim
+
+    def ray_color(self, job, rays, first_index=1, recursive=True):
+        """or_ray_color: one path's radiance per given primary ray (n, 3)."""
+        rays = np.ascontiguousarray(rays, np.float32).reshape(-1, 6)
+        out = np.zeros((rays.shape[0], 3), np.float32)
+        self.lib.or_ray_color(self.h, C.byref(job), _p(rays, C.c_float), rays.shape[0], first_index,
+                              _p(out, C.c_float), 1 if recursive else 0)
+        return out
+
+    def light_eval(self, light: int, uv, x, pdf_dir=None):
+        """or_light_eval: dict of point, normal, dir, le, pdf per item and area
+        (pdf at pdf_dir when given)."""
+        uv = np.ascontiguousarray(uv, np.float32).reshape(-1, 2)
+        x = np.ascontiguousarray(x, np.float32).reshape(-1, 3)
+        pd = None if pdf_dir is None else np.ascontiguousarray(pdf_dir, np.float32).reshape(-1, 3)
+        n = uv.shape[0]
+        out = {k: np.zeros((n, 3), np.float32) for k in ("point", "normal", "dir", "le")}
+        out["pdf"] = np.zeros(n, np.float32)
+        area = C.c_float()
+        if self.lib.or_light_eval(self.h, light, n, _p(uv, C.c_float), _p(x, C.c_float),
+                                  None if pd is None else _p(pd, C.c_float),
+                                  *(_p(out[k], C.c_float) for k in ("point", "normal", "dir", "le", "pdf")),
+                                  C.byref(area)) != 0:
+            raise ValueError("bad light index")
+        out["area"] = area.value
+        return out
 
     def intersect(self, rays, tmin=1e-4, tmax=1e5):
         """(t, prim, position, normal, is_inside) of each ray's closest hit."""

@@ -308,6 +308,45 @@ int ref_scene_transform(void *s, int object, int n_ops, const int *ops, const fl
   return 0;
 }
 
+// The Light methods of light `light` of a scene (LightList order: the
+// discovered emitters, then the environment) at n items (u, v, x), as
+// maxdepth_nee.hpp:104-189 calls them: point = get_sample(u, v), normal =
+// get_normal_at(point), dir = normalize(point - x), L_emit (an area light
+// with rec.normal = normal and texCoords (u, v) towards -dir; the
+// environment with rec.normal = -dir along dir), pdf = pdf_value(x, dir);
+// *area = get_area().  pdf_dir (may be NULL): pdf = pdf_value(x, pdf_dir[i]).
+int ref_light_eval(void *s, int light, int n, const float *uv, const float *x, const float *pdf_dir, float *point,
+                   float *normal, float *dir, float *le, float *pdf, float *area) {
+  auto *S = static_cast<RefScene *>(s);
+  if (light < 0 || light >= (int)S->lights.size()) return -1;
+  std::shared_ptr<Light> L = S->lights.get(light);
+  *area = L->get_area();
+  for (int i = 0; i < n; ++i) {
+    const vec3 p = L->get_sample(uv[2 * i], uv[2 * i + 1]);
+    const vec3 nl = L->get_normal_at(p);
+    const vec3 w = (p - V3(x + 3 * i)).normalize();
+    HitRecord rec;
+    rec.position = p;
+    vec3 e;
+    if (L->type == LightType::ENVIRONMENT_LIGHT) {
+      rec.normal = -w;
+      e = L->L_emit(rec, w);
+    } else {
+      rec.normal = nl;
+      rec.texCoords = vec2(uv[2 * i], uv[2 * i + 1]);
+      e = L->L_emit(rec, -w);
+    }
+    for (int c = 0; c < 3; ++c) {
+      point[3 * i + c] = p[c];
+      normal[3 * i + c] = nl[c];
+      dir[3 * i + c] = w[c];
+      le[3 * i + c] = e[c];
+    }
+    pdf[i] = L->pdf_value(V3(x + 3 * i), pdf_dir ? V3(pdf_dir + 3 * i) : w);
+  }
+  return 0;
+}
+
 // HitRecord for BSDF calls: the reference materials read normal, position,
 // is_inside and texCoords.
 static HitRecord make_rec(const float *n, uint8_t front) {

@@ -53,6 +53,8 @@ def load():
         lib.ref_scene_num_lights.argtypes = [C.c_void_p]
         lib.ref_trace_closest.argtypes = [C.c_void_p, f32p, C.c_int, C.c_float, C.c_float, f32p, i32p, f32p, f32p,
                                           u8p]
+        lib.ref_light_eval.argtypes = [C.c_void_p, C.c_int, C.c_int, f32p, f32p, f32p, f32p, f32p, f32p, f32p, f32p,
+                                       f32p]
         lib.ref_scene_transform.argtypes = [C.c_void_p, C.c_int, C.c_int, i32p, f32p]
         lib.ref_bsdf_eval.argtypes = [C.POINTER(N.MaterialDesc), C.c_int, f32p, f32p, f32p, u8p, f32p, f32p]
         lib.ref_bsdf_sample.argtypes = [C.POINTER(N.MaterialDesc), C.c_int, f32p, f32p, u8p, f32p, f32p, u8p, f32p,
@@ -99,6 +101,24 @@ class RefScene:
                                    _p(prim, C.c_int32), _p(pos, C.c_float), _p(nrm, C.c_float),
                                    _p(front, C.c_uint8))
         return t, prim, pos, nrm, front
+
+    def light_eval(self, light: int, uv, x, pdf_dir=None):
+        """Light methods of light `light` (ref_light_eval): dict of point,
+        normal, dir, le, pdf per item and area (pdf at pdf_dir when given)."""
+        uv = np.ascontiguousarray(uv, np.float32).reshape(-1, 2)
+        x = np.ascontiguousarray(x, np.float32).reshape(-1, 3)
+        pd = None if pdf_dir is None else np.ascontiguousarray(pdf_dir, np.float32).reshape(-1, 3)
+        n = uv.shape[0]
+        out = {k: np.zeros((n, 3), np.float32) for k in ("point", "normal", "dir", "le")}
+        out["pdf"] = np.zeros(n, np.float32)
+        area = C.c_float()
+        if self.lib.ref_light_eval(self.h, light, n, _p(uv, C.c_float), _p(x, C.c_float),
+                                   None if pd is None else _p(pd, C.c_float),
+                                   *(_p(out[k], C.c_float) for k in ("point", "normal", "dir", "le", "pdf")),
+                                   C.byref(area)) != 0:
+            raise ValueError("bad light index")
+        out["area"] = area.value
+        return out
 
     def transform(self, obj: int, ops):
         """Wraps object `obj` in the reference's decorators, innermost first:

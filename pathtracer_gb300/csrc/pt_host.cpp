@@ -1390,9 +1390,12 @@ std::unique_ptr<Scene> build_scene(const pt_scene_desc *d_in, cudaStream_t st, b
         else if (q.axis == 1) { v[0] = a; v[1] = q.k; v[2] = b; }
         else { v[0] = a; v[1] = b; v[2] = q.k; }
       };
+      float v2[3];
       put(v0, q.d0_min, q.d1_min);
       put(v1, q.d0_max, q.d1_min);
+      put(v2, q.d0_max, q.d1_max);
       put(v3_, q.d0_min, q.d1_max);
+      for (int a = 0; a < 3; ++a) L.v2[a] = v2[a];
       L.type = LIGHT_QUAD;
       L.prim = B.n_tris + od.index;
       V3 e1 = v3(v1[0] - v0[0], v1[1] - v0[1], v1[2] - v0[2]);
@@ -1507,6 +1510,7 @@ std::unique_ptr<Scene> build_scene(const pt_scene_desc *d_in, cudaStream_t st, b
   V.materials = S->materials;
   V.lights = S->lights;
   V.n_lights = (int)lights.size();
+  S->host_lights = lights;
   V.n_nodes = (int)out.nodes.size();
   V.n_prims = n_prims;
   V.trav_cap = trav_cap > 0 ? trav_cap : PT_TRAVERSAL_CAP;
@@ -1807,10 +1811,11 @@ DeviceJob Context::device_job(const pt_job_desc &j, Scene *S) {
   return J;
 }
 
-void Context::render_device(const pt_job_desc &j, float *d_film, pt_stats *stats, bool sync) {
+void Context::render_device(const pt_job_desc &j, float *d_film, pt_stats *stats, bool sync, const float *d_rays) {
   validate_job(j);
   Scene *S = scene(j.scene);
   DeviceJob J = device_job(j, S);
+  J.job.rays = d_rays;
   // offsets table
   std::vector<float2> off = make_offsets(j);
   if ((int)off.size() > offsets_cap) {
@@ -2144,6 +2149,46 @@ int pt_render(void *ctx, const pt_job_desc *job, float *film_rgb, pt_stats *stat
   });
 }
 
+int pt_ray_color(void *ctx, const pt_job_desc *job, const float *rays, int32_t n, uint32_t first_index,
+                 float *radiance) {
+  Context *c = static_cast<Context *>(ctx);
+  PT_GUARD(c, {
+    c = as_ctx(ctx);
+    if (!job || n < 0 || (n > 0 && (!rays || !radiance)) || first_index < 1)
+      fail(PT_ERR_INVALID, "bad ray-color args");
+    if (n == 0) return PT_OK;
+    cuda_check(cudaSetDevice(c->device), "cudaSetDevice");
+    // one film pixel per ray, one sample: path i is frame pixel
+    // (first_index - 1 + i, 0) of a one-row frame at 1 spp, i.e. Halton index
+    // first_index + i, and its film pixel receives its radiance
+    pt_job_desc j = *job;
+    j.width = n;
+    j.height = 1;
+    j.spp_x = j.spp_y = 1;
+    j.spp_begin = 0;
+    j.spp_end = 0;
+    j.crop_x = (int32_t)(first_index - 1u);
+    j.crop_y = 0;
+    j.full_width = (int32_t)std::min<int64_t>((int64_t)first_index - 1 + n, INT32_MAX);
+    j.full_height = 1;
+    if ((int64_t)first_index - 1 + n > INT32_MAX) fail(PT_ERR_INVALID, "first_index + n beyond 2^31");
+    const size_t nn = (size_t)n;
+    float *df = c->film_buffer(nn * 3);
+    float *dr = (float *)c->scratch(nn * 24);
+    cuda_check(cudaMemcpyAsync(dr, rays, nn * 24, cudaMemcpyHostToDevice, c->stream), "h2d rays");
+    cuda_check(cudaMemsetAsync(df, 0, nn * 12, c->stream), "memset film");
+    c->render_device(j, df, nullptr, false, dr);
+    cuda_check(cudaMemcpyAsync(radiance, df, nn * 12, cudaMemcpyDeviceToHost, c->stream), "d2h");
+    cuda_check(cudaStreamSynchronize(c->stream), "ray color");
+    int herr = 0;
+    cuda_check(cudaMemcpy(&herr, c->d_err, sizeof(int), cudaMemcpyDeviceToHost), "read err");
+    if (herr) {
+      cudaMemset(c->d_err, 0, sizeof(int));
+      fail(PT_ERR_DEVICE, "device traversal error flag " + std::to_string(herr));
+    }
+  });
+}
+
 int pt_tonemap(void *ctx, const float *film_rgb, int32_t width, int32_t height, float gamma, uint8_t *rgb8) {
   Context *c = static_cast<Context *>(ctx);
   PT_GUARD(c, {
@@ -2335,6 +2380,40 @@ int pt_intersect(void *ctx, int32_t scene_id, const float *rays, int32_t n, floa
       cudaMemset(c->d_err, 0, sizeof(int));
       fail(PT_ERR_DEVICE, "device traversal error flag " + std::to_string(herr));
     }
+  });
+}
+
+int pt_light_sample(void *ctx, int32_t scene_id, int32_t light, int32_t n, const float *uv, const float *x,
+                    const float *pdf_dir, float *point, float *normal, float *dir, float *le, float *pdf,
+                    float *area) {
+  Context *c = static_cast<Context *>(ctx);
+  PT_GUARD(c, {
+    c = as_ctx(ctx);
+    if (n < 0 || (n > 0 && (!uv || !x || !point || !normal || !dir || !le || !pdf)))
+      fail(PT_ERR_INVALID, "bad light-sample args");
+    Scene *S = c->scene(scene_id);
+    if (light < 0 || light >= S->view.n_lights) fail(PT_ERR_INVALID, "light index out of range");
+    const LightRec &L = S->host_lights[light];
+    if (area) *area = L.type == LIGHT_ENV ? INFINITY : L.area;
+    if (n == 0) return PT_OK;
+    const size_t nn = (size_t)n;
+    char *buf = (char *)c->scratch(nn * (8 + 12 + 12 + 12 * 4 + 4) + 256);
+    float *duv = (float *)buf;
+    float *dx = (float *)(buf + nn * 8);
+    float *dpd = (float *)(buf + nn * 20);
+    float *dout = (float *)(buf + nn * 32);  // point, normal, dir, le (3n each), pdf (n)
+    cuda_check(cudaMemcpyAsync(duv, uv, nn * 8, cudaMemcpyHostToDevice, c->stream), "h2d uv");
+    cuda_check(cudaMemcpyAsync(dx, x, nn * 12, cudaMemcpyHostToDevice, c->stream), "h2d x");
+    if (pdf_dir) cuda_check(cudaMemcpyAsync(dpd, pdf_dir, nn * 12, cudaMemcpyHostToDevice, c->stream), "h2d dir");
+    launch_light_eval(S->view, light, n, duv, dx, pdf_dir ? dpd : nullptr, dout, dout + 3 * nn, dout + 6 * nn,
+                      dout + 9 * nn, dout + 12 * nn, c->stream);
+    cuda_check(cudaGetLastError(), "light launch");
+    cuda_check(cudaMemcpyAsync(point, dout, 12 * nn, cudaMemcpyDeviceToHost, c->stream), "d2h");
+    cuda_check(cudaMemcpyAsync(normal, dout + 3 * nn, 12 * nn, cudaMemcpyDeviceToHost, c->stream), "d2h");
+    cuda_check(cudaMemcpyAsync(dir, dout + 6 * nn, 12 * nn, cudaMemcpyDeviceToHost, c->stream), "d2h");
+    cuda_check(cudaMemcpyAsync(le, dout + 9 * nn, 12 * nn, cudaMemcpyDeviceToHost, c->stream), "d2h");
+    cuda_check(cudaMemcpyAsync(pdf, dout + 12 * nn, 4 * nn, cudaMemcpyDeviceToHost, c->stream), "d2h");
+    cuda_check(cudaStreamSynchronize(c->stream), "light sample");
   });
 }
 

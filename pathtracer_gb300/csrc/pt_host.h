@@ -43,6 +43,7 @@ struct Scene {
   PrimShade *shade = nullptr;
   MatRec *materials = nullptr;
   LightRec *lights = nullptr;
+  std::vector<LightRec> host_lights;  // the lights' records (pt_light_sample's get_area)
   std::vector<void *> owned;
   int n_tris = 0, n_quads = 0, n_spheres = 0, bvh_depth = 0;
   int env_w = 0, env_h = 0;
@@ -138,7 +139,10 @@ struct Context {
   const uint16_t *perm_for(uint32_t seed);
   Scene *scene(int id);
   DeviceJob device_job(const pt_job_desc &j, Scene *S);
-  void render_device(const pt_job_desc &j, float *d_film, pt_stats *stats, bool sync);
+  // d_rays (device, 6 floats per film pixel): given primary rays instead of
+  // the camera's (pt_ray_color)
+  void render_device(const pt_job_desc &j, float *d_film, pt_stats *stats, bool sync,
+                     const float *d_rays = nullptr);
   float *film_buffer(size_t floats);
   void *scratch(size_t bytes);
 };

@@ -125,6 +125,33 @@ void launch_intersect(const SceneView &S, const float *rays, int n, float tmin, 
   k_intersect<<<grid_for(n, 128, 152 * 8), 128, 0, st>>>(S, rays, n, tmin, tmax, t, prim, pos, nrm, front, err);
 }
 
+// The Light methods of one light of a resident scene at n (u, v, x) items:
+// get_sample, get_normal_at, the direction from x, L_emit towards x and
+// pdf_value(x, dir) -- light_point / light_pdf_value, the code NEE runs.
+__global__ void k_light_eval(SceneView S, int light, int n, const float *uv, const float *x, const float *pdf_dir,
+                             float *point, float *normal, float *dir, float *le, float *pdf) {
+  const LightRec &Lr = S.lights[light];
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const V3 xi = v3(x[3 * i], x[3 * i + 1], x[3 * i + 2]);
+    const LightPoint P = light_point(S, Lr, uv[2 * i], uv[2 * i + 1], xi, 0.f);
+    const V3 pd = pdf_dir ? v3(pdf_dir[3 * i], pdf_dir[3 * i + 1], pdf_dir[3 * i + 2]) : P.w;
+    const float pv = light_pdf_value(Lr, xi, pd);
+    const V3 out[4] = {P.p, P.n, P.w, P.Le};
+    float *dst[4] = {point, normal, dir, le};
+    for (int k = 0; k < 4; ++k) {
+      dst[k][3 * i] = out[k].x;
+      dst[k][3 * i + 1] = out[k].y;
+      dst[k][3 * i + 2] = out[k].z;
+    }
+    pdf[i] = pv;
+  }
+}
+
+void launch_light_eval(const SceneView &S, int light, int n, const float *uv, const float *x, const float *pdf_dir,
+                       float *point, float *normal, float *dir, float *le, float *pdf, cudaStream_t st) {
+  k_light_eval<<<grid_for(n, 128, 152 * 8), 128, 0, st>>>(S, light, n, uv, x, pdf_dir, point, normal, dir, le, pdf);
+}
+
 __global__ void k_bsdf_eval(const MatRec *m, int n, const float *wo, const float *wi,
                             const float *nrm, const uint8_t *front, float *f, float *pdf) {
   MatRec mat = *m;

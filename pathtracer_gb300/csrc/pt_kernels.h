@@ -102,6 +102,8 @@ struct KernelInfo {
 };
 
 void upload_halton_tables(const HaltonTables &T, cudaStream_t st);
+void launch_light_eval(const SceneView &S, int light, int n, const float *uv, const float *x, const float *pdf_dir,
+                       float *point, float *normal, float *dir, float *le, float *pdf, cudaStream_t st);
 void launch_intersect(const SceneView &S, const float *rays, int n, float tmin, float tmax, float *t, int *prim,
                       float *pos, float *nrm, uint8_t *front, int *err, cudaStream_t st);
 void launch_path_samples(const DeviceJob &J, long long first, int n, int dims, int bounces, float *pix, float *dv,

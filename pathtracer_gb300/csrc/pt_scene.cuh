@@ -88,6 +88,8 @@ struct alignas(16) LightRec {
   float pad2;
   float color[3];   // ConstantTexture colour
   int32_t texture;  // texture index + 1 of the emitter's colour (0: color)
+  float v2[3];      // quad: vertices[2] (QuadLight::pdf_value's second triangle)
+  float pad3;
 };
 
 struct EnvMap {
@@ -175,6 +177,7 @@ struct JobView {
   float shutter;          // motion blur: a path's time is shutter * u
   CameraView cam;
   const float2 *offsets;  // per grid sample k: jittered pixel offset
+  const float *rays;      // given primary rays (origin, direction per film pixel), or null: the camera's
 };
 
 }  // namespace pt

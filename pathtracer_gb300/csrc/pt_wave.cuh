@@ -260,19 +260,27 @@ __global__ void k_camera(DeviceJob J0, JobTable T, Queues Q, long long g0, int n
     }
     const DeviceJob &J = MJ ? T.jobs[jk] : J0;
     PathId P = path_id(J, g);
-    const CameraView &C = J.job.cam;
-    float2 off = __ldg(J.job.offsets + P.k);
-    float u = ((float)P.i + off.x) / (float)J.job.full_w;
-    float v = ((float)P.j + off.y) / (float)J.job.full_h;
-    const float r = C.lens_radius;
-    float lx = -r + (r - -r) * rand01(P.key, 1u);
-    float ly = -r + (r - -r) * rand01(P.key, 2u);
-    V3 hv = v3(C.h_vec[0], C.h_vec[1], C.h_vec[2]), vv = v3(C.v_vec[0], C.v_vec[1], C.v_vec[2]);
-    V3 ps = v3(C.position[0], C.position[1], C.position[2]) + (hv * lx + vv * ly);
-    V3 dir = v3(C.bottom_left[0], C.bottom_left[1], C.bottom_left[2]) +
-             u * v3(C.horizontal[0], C.horizontal[1], C.horizontal[2]) +
-             v * v3(C.vertical[0], C.vertical[1], C.vertical[2]) - ps;
-    dir = normalize(dir);
+    V3 ps, dir;
+    if (!MJ && J.job.rays) {
+      // pt_ray_color: the given primary ray of the path's film pixel
+      const float *rr = J.job.rays + 6 * (size_t)P.q;
+      ps = v3(rr[0], rr[1], rr[2]);
+      dir = normalize(v3(rr[3], rr[4], rr[5]));
+    } else {
+      const CameraView &C = J.job.cam;
+      float2 off = __ldg(J.job.offsets + P.k);
+      float u = ((float)P.i + off.x) / (float)J.job.full_w;
+      float v = ((float)P.j + off.y) / (float)J.job.full_h;
+      const float r = C.lens_radius;
+      float lx = -r + (r - -r) * rand01(P.key, 1u);
+      float ly = -r + (r - -r) * rand01(P.key, 2u);
+      V3 hv = v3(C.h_vec[0], C.h_vec[1], C.h_vec[2]), vv = v3(C.v_vec[0], C.v_vec[1], C.v_vec[2]);
+      ps = v3(C.position[0], C.position[1], C.position[2]) + (hv * lx + vv * ly);
+      dir = v3(C.bottom_left[0], C.bottom_left[1], C.bottom_left[2]) +
+            u * v3(C.horizontal[0], C.horizontal[1], C.horizontal[2]) +
+            v * v3(C.vertical[0], C.vertical[1], C.vertical[2]) - ps;
+      dir = normalize(dir);
+    }
     // motion blur: the path's time, used by every ray of the path
     const float time = J.job.shutter > 0.f ? J.job.shutter * rand01(P.key, 3u) : 0.f;
     Q.ray_o[0][s] = make_float4(ps.x, ps.y, ps.z, __int_as_float(s));
@@ -495,6 +503,101 @@ __device__ __forceinline__ float2 light_offset(const DeviceJob &J, uint64_t key,
                      ((float)sj + rand01(key, rbase + 2u * ls + 1u)) / (float)J.job.light_ny);
 }
 
+// A light sample seen from x (maxdepth_nee.hpp:104-189): the point of
+// Light::get_sample(u, v) (QuadLight light.hpp:131-137: v0 + u e1 + v e2;
+// SphereLight :254-264: the whole sphere; EnvironmentLight envLight.hpp:20-36:
+// HDRITexture's uniform sphere direction, texture.hpp:120-124, times 1e5),
+// the normal get_normal_at gives there (light.hpp:139-145, 266-271,
+// envLight.hpp:48-51), the normalised direction w from x and the distance,
+// and L_emit towards x (light.hpp:157-165, 296-303: one-sided, the colour
+// texture at texCoords (u, v), maxdepth_nee.hpp:175-176; envLight.hpp:73-90:
+// the HDRI along w).  A moving light is taken at `time`.
+struct LightPoint {
+  V3 p, n, w, Le;
+  float len;
+};
+__device__ __forceinline__ LightPoint light_point(const SceneView &S, const LightRec &Lr, float ox, float oy, V3 x,
+                                                  float time) {
+  LightPoint L;
+  if (Lr.type == LIGHT_ENV) {
+    // uniformSampleSphere * 1e5 (texture.hpp:120-124, envLight.hpp:26-43)
+    float z = 1.f - 2.f * ox;
+    float rr = sqrtf(fmaxf(0.f, 1.f - z * z));
+    float sp, cp;
+    sincospi_(2.f * oy, &sp, &cp);
+    L.p = v3(rr * cp, rr * sp, z) * 1e5f;
+    L.w = normalize(L.p - x);
+    L.len = length(L.p - x);
+    L.n = -normalize(L.p);
+    L.Le = env_lookup(S.env, L.w);
+    return L;
+  }
+  if (Lr.type == LIGHT_QUAD) {
+    // QuadLight::get_sample / get_normal_at (light.hpp:131-147)
+    L.p = v3(Lr.v0[0], Lr.v0[1], Lr.v0[2]) + ox * v3(Lr.e1[0], Lr.e1[1], Lr.e1[2]) +
+          oy * v3(Lr.e2[0], Lr.e2[1], Lr.e2[2]);
+    if (Lr.motion) L.p = moved_point(S, Lr.motion, L.p, time);
+    L.n = v3(Lr.normal[0], Lr.normal[1], Lr.normal[2]);
+  } else {
+    // SphereLight::get_sample (light.hpp:254-264): the whole sphere
+    float sth, cth, sph, cph;
+    sincospi_(2.f * ox, &sth, &cth);
+    float phi = acosf(2.f * oy - 1.f);
+    sincos_(phi, &sph, &cph);
+    V3 c = v3(Lr.v0[0], Lr.v0[1], Lr.v0[2]);
+    if (Lr.motion) c = moved_point(S, Lr.motion, c, time);
+    L.p = c + Lr.radius * v3(sph * cth, sph * sth, cph);
+    L.n = normalize(L.p - c);
+  }
+  V3 ld = L.p - x;
+  L.len = length(ld);
+  L.w = normalize(ld);
+  // L_emit of the light (light.hpp:157-165, 296-303); a textured light
+  // is looked up at the sample's offsets (maxdepth_nee.hpp:175-176)
+  const V3 lcol = Lr.texture ? tex_eval(S.textures[Lr.texture - 1], ox, oy)
+                             : v3(Lr.color[0], Lr.color[1], Lr.color[2]);
+  L.Le = (dot(L.n, -L.w) > 0.f) ? lcol * Lr.intensity : v3(0.f);
+  return L;
+}
+
+// Light::pdf_value(origin, dir): the solid-angle density of sampling dir
+// from origin.  QuadLight (light.hpp:164-205): the quad's plane hit, inside
+// one of its two triangles by the reference's edge tests (the first test is
+// the triangle's own orientation, so a triangle checks two of its edges),
+// dist^2 / (area |cos|); SphereLight (:279-294): 1 / the solid angle of the
+// visible cap, 1 / (4 pi) from inside; EnvironmentLight (envLight.hpp:58-70):
+// HDRITexture::pdf_direction, uniform 1 / (4 pi) (texture.hpp:126-131).
+__device__ inline float light_pdf_value(const LightRec &Lr, V3 origin, V3 dir) {
+  if (Lr.type == LIGHT_ENV) return (float)(1.0 / (4.0 * PT_PI));
+  if (Lr.type == LIGHT_SPHERE) {
+    const V3 wc = v3(Lr.v0[0], Lr.v0[1], Lr.v0[2]) - origin;
+    const float dc2 = dot(wc, wc), r2 = Lr.radius * Lr.radius;
+    if (dc2 <= r2) return (float)(1.0 / (4.0 * PT_PI));
+    const float cos_max = sqrtf(1.f - r2 / dc2);
+    const float omega = (float)(2.0 * PT_PI * (double)(1.f - cos_max));
+    return 1.f / omega;
+  }
+  const V3 v0 = v3(Lr.v0[0], Lr.v0[1], Lr.v0[2]);
+  const V3 v1 = v0 + v3(Lr.e1[0], Lr.e1[1], Lr.e1[2]), v3_ = v0 + v3(Lr.e2[0], Lr.e2[1], Lr.e2[2]);
+  const V3 v2 = v3(Lr.v2[0], Lr.v2[1], Lr.v2[2]);
+  const V3 N = v3(Lr.normal[0], Lr.normal[1], Lr.normal[2]);
+  const float denom = dot(N, dir);
+  if (fabsf(denom) < 1e-6f) return 0.f;
+  const float t = dot(v0 - origin, N) / denom;
+  if (t <= 0.f) return 0.f;
+  const V3 P = origin + dir * t;
+  auto in_tri = [&](V3 A, V3 B, V3 C) {
+    if (dot(cross(B - A, C - A), N) < 0.f) return false;
+    if (dot(cross(C - B, P - B), N) < 0.f) return false;
+    if (dot(cross(A - C, P - C), N) < 0.f) return false;
+    return true;
+  };
+  if (!in_tri(v0, v1, v2) && !in_tri(v0, v2, v3_)) return 0.f;
+  const float dist2 = dot(P - origin, P - origin);
+  const float cos_t = fabsf(dot(N, -dir));
+  return dist2 / (Lr.area * cos_t);
+}
+
 // Next-event estimation at one vertex (maxdepth_nee.hpp:89-232): LN light
 // samples on a stratified x-by-y grid, each a ShadowQueue entry with its
 // unoccluded contribution.  MED: the vertex is a medium scattering event
@@ -521,44 +624,24 @@ __device__ __forceinline__ void next_event(const SceneView &S, const DeviceJob &
       float pdir;
       if (J.job.env_sampling == PT_ENV_ALIAS) {
         wl = env_alias_sample(S.env, ox, oy, rand01(key, rbase + 28u + ls), pdir);
+        Le = env_lookup(S.env, wl);
       } else {
-        // uniformSampleSphere * 1e5 (texture.hpp:120-124, envLight.hpp:26-43)
-        float z = 1.f - 2.f * ox;
-        float rr = sqrtf(fmaxf(0.f, 1.f - z * z));
-        float sp, cp;
-        sincospi_(2.f * oy, &sp, &cp);
-        V3 pinf = v3(rr * cp, rr * sp, z) * 1e5f;
-        wl = normalize(pinf - sf.p);
+        const LightPoint P = light_point(S, Lr, ox, oy, sf.p, time);
+        wl = P.w;
+        Le = P.Le;
         pdir = (float)(1.0 / (4.0 * PT_PI));
       }
       tmax = FLT_MAX;
       pdf_l = pdir / (float)S.n_lights;
       NoI = MED ? 1.f : fmaxf(0.f, dot(sf.n, wl));
       G = NoI;
-      Le = env_lookup(S.env, wl);
       valid = pdf_l > 1e-7f && !med;  // no light reaches through an infinite medium
     } else {
-      V3 lp, ln;
-      if (Lr.type == LIGHT_QUAD) {
-        // QuadLight::get_sample / get_normal_at (light.hpp:131-147)
-        lp = v3(Lr.v0[0], Lr.v0[1], Lr.v0[2]) + ox * v3(Lr.e1[0], Lr.e1[1], Lr.e1[2]) +
-             oy * v3(Lr.e2[0], Lr.e2[1], Lr.e2[2]);
-        if (Lr.motion) lp = moved_point(S, Lr.motion, lp, time);
-        ln = v3(Lr.normal[0], Lr.normal[1], Lr.normal[2]);
-      } else {
-        // SphereLight::get_sample (light.hpp:254-264): the whole sphere
-        float sth, cth, sph, cph;
-        sincospi_(2.f * ox, &sth, &cth);
-        float phi = acosf(2.f * oy - 1.f);
-        sincos_(phi, &sph, &cph);
-        V3 c = v3(Lr.v0[0], Lr.v0[1], Lr.v0[2]);
-        if (Lr.motion) c = moved_point(S, Lr.motion, c, time);
-        lp = c + Lr.radius * v3(sph * cth, sph * sth, cph);
-        ln = normalize(lp - c);
-      }
-      V3 ld = lp - sf.p;
-      float len = length(ld);
-      wl = normalize(ld);
+      const LightPoint P = light_point(S, Lr, ox, oy, sf.p, time);
+      const V3 ln = P.n;
+      const float len = P.len;
+      wl = P.w;
+      Le = P.Le;
       if (len < 0.001f) valid = false;
       tmax = len - 0.001f;
       pdf_l = (Lr.area <= 1e-7f) ? 0.f : 1.f / (Lr.area * (float)S.n_lights);
@@ -566,11 +649,6 @@ __device__ __forceinline__ void next_event(const SceneView &S, const DeviceJob &
       float NoL = fmaxf(0.f, dot(ln, -wl));
       float d2 = len * len;
       G = (d2 < 1e-7f) ? 0.f : NoL * NoI / d2;
-      // L_emit of the light (light.hpp:157-165, 296-303); a textured light
-      // is looked up at the sample's offsets (maxdepth_nee.hpp:175-176)
-      const V3 lcol = Lr.texture ? tex_eval(S.textures[Lr.texture - 1], ox, oy)
-                                 : v3(Lr.color[0], Lr.color[1], Lr.color[2]);
-      Le = (dot(ln, -wl) > 0.f) ? lcol * Lr.intensity : v3(0.f);
       if (!(pdf_l > 1e-7f)) valid = false;
       if (mis && valid && NoL > 0.f) {
         pdf_l = pdf_l * d2 / NoL;  // solid-angle pdf

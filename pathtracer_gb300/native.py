@@ -32,10 +32,10 @@ BVH_BUILD_HOST, BVH_BUILD_DEVICE, BVH_BUILD_SAH = 0, 1, 2
 # exported symbols of the C-ABI, in header order
 EXPORTS = [
     "pt_create", "pt_destroy", "pt_last_error", "pt_version", "pt_scene_upload", "pt_scene_release",
-    "pt_bvh_build", "pt_set_bvh_builder", "pt_bvh_build_device", "pt_bvh_build_sah", "pt_obj_load", "pt_obj_free", "pt_load_image", "pt_free_image", "pt_scene_info", "pt_render", "pt_render_device", "pt_render_device_noalloc",
+    "pt_bvh_build", "pt_set_bvh_builder", "pt_bvh_build_device", "pt_bvh_build_sah", "pt_obj_load", "pt_obj_free", "pt_load_image", "pt_free_image", "pt_scene_info", "pt_render", "pt_render_device", "pt_render_device_noalloc", "pt_ray_color",
     "pt_profile_begin",
     "pt_profile_end", "pt_tonemap", "pt_gaussian_blur", "pt_write_png", "pt_sampler_eval", "pt_sample_eval", "pt_trace_closest",
-    "pt_trace_any", "pt_intersect", "pt_bsdf_eval", "pt_bsdf_sample", "pt_render_batch", "pt_autotune", "pt_server_create",
+    "pt_trace_any", "pt_intersect", "pt_light_sample", "pt_bsdf_eval", "pt_bsdf_sample", "pt_render_batch", "pt_autotune", "pt_server_create",
     "pt_server_destroy", "pt_submit", "pt_server_step", "pt_poll", "pt_cancel",
 ]
 
@@ -179,6 +179,7 @@ def load() -> C.CDLL:
         "pt_render": [vp, C.POINTER(JobDesc), f32p, C.POINTER(Stats)],
         "pt_render_device": [vp, C.POINTER(JobDesc), vp, C.c_int, C.POINTER(Stats)],
         "pt_render_device_noalloc": [vp, C.POINTER(JobDesc), vp, C.POINTER(Stats)],
+        "pt_ray_color": [vp, C.POINTER(JobDesc), f32p, C.c_int32, C.c_uint32, f32p],
         "pt_profile_begin": [vp],
         "pt_profile_end": [vp, C.POINTER(C.c_double), C.POINTER(C.c_int64)],
         "pt_tonemap": [vp, f32p, C.c_int32, C.c_int32, C.c_float, u8p],
@@ -189,6 +190,8 @@ def load() -> C.CDLL:
         "pt_trace_closest": [vp, C.c_int32, f32p, C.c_int32, C.c_float, C.c_float, f32p, i32p, f32p],
         "pt_trace_any": [vp, C.c_int32, f32p, f32p, C.c_int32, C.c_float, u8p],
         "pt_intersect": [vp, C.c_int32, f32p, C.c_int32, C.c_float, C.c_float, f32p, i32p, f32p, f32p, u8p],
+        "pt_light_sample": [vp, C.c_int32, C.c_int32, C.c_int32, f32p, f32p, f32p, f32p, f32p, f32p, f32p, f32p,
+                            f32p],
         "pt_bsdf_eval": [vp, C.POINTER(MaterialDesc), C.c_int32, f32p, f32p, f32p, u8p, f32p, f32p],
         "pt_bsdf_sample": [vp, C.POINTER(MaterialDesc), C.c_int32, f32p, f32p, u8p, f32p, f32p, u8p, f32p,
                            f32p, f32p, u32p],
@@ -445,6 +448,14 @@ class Renderer:
                                               C.byref(st) if stats else None))
         return st
 
+    def ray_color(self, job: JobDesc, rays: np.ndarray, first_index: int = 1) -> np.ndarray:
+        """pt_ray_color: one path's radiance per given primary ray (n, 3)."""
+        rays = np.ascontiguousarray(rays, dtype=np.float32).reshape(-1, 6)
+        out = np.zeros((rays.shape[0], 3), np.float32)
+        self._check(self.lib.pt_ray_color(self.ctx, C.byref(job), _ptr(rays, C.c_float), rays.shape[0], first_index,
+                                          _ptr(out, C.c_float)))
+        return out
+
     STAGES = ["camera", "trace", "sort", "shade", "shadow", "film"]
 
     def profile_begin(self):
@@ -537,6 +548,23 @@ class Renderer:
                                           _ptr(prim, C.c_int32), _ptr(pos, C.c_float), _ptr(nrm, C.c_float),
                                           _ptr(ins, C.c_uint8)))
         return t, prim, pos, nrm, ins
+
+    def light_sample(self, sid: int, light: int, uv: np.ndarray, x: np.ndarray, pdf_dir=None):
+        """pt_light_sample: dict of point, normal, dir, le, pdf (per item) and
+        area; pdf at pdf_dir (n, 3) when given, else at the sample's direction."""
+        uv = np.ascontiguousarray(uv, dtype=np.float32).reshape(-1, 2)
+        x = np.ascontiguousarray(x, dtype=np.float32).reshape(-1, 3)
+        pd = None if pdf_dir is None else np.ascontiguousarray(pdf_dir, dtype=np.float32).reshape(-1, 3)
+        n = uv.shape[0]
+        out = {k: np.zeros((n, 3), np.float32) for k in ("point", "normal", "dir", "le")}
+        out["pdf"] = np.zeros(n, np.float32)
+        area = C.c_float()
+        self._check(self.lib.pt_light_sample(self.ctx, sid, light, n, _ptr(uv, C.c_float), _ptr(x, C.c_float),
+                                             None if pd is None else _ptr(pd, C.c_float),
+                                             *(_ptr(out[k], C.c_float) for k in ("point", "normal", "dir", "le",
+                                                                                 "pdf")), C.byref(area)))
+        out["area"] = area.value
+        return out
 
     def bsdf_eval(self, mat: MaterialDesc, wo, wi, normal, front):
         wo, wi, normal = (np.ascontiguousarray(a, dtype=np.float32) for a in (wo, wi, normal))

@@ -187,6 +187,54 @@ def make_transforms():
     np.savez_compressed(OUT / "transforms.npz", **out)
 
 
+def light_scene():
+    """Emitters discovered as lights (DiffuseEmitter rectangles of the three
+    axes and spheres, a non-emitting rectangle and sphere between them) and a
+    seeded environment map: the LightList the light fixture evaluates."""
+    sc = S.Scene()
+    grey = sc.add_material(N.LAMBERTIAN, [0.5, 0.5, 0.5])
+    l1 = sc.add_material(N.DIFFUSE_EMITTER, [17.0, 12.0, 4.0, 1.0])
+    l2 = sc.add_material(N.DIFFUSE_EMITTER, [2.0, 3.0, 4.0, 2.5])
+    l3 = sc.add_material(N.DIFFUSE_EMITTER, [1.0, 0.5, 0.25, 3.0])
+    l4 = sc.add_material(N.DIFFUSE_EMITTER, [5.0, 4.0, 3.0, 1.5])
+    sc.add_quad(1, 0.999, 0.375, 0.625, 0.375, 0.625, l1)
+    sc.add_quad(1, 0.0, 0.0, 1.0, 0.0, 1.0, grey)
+    sc.add_quad(0, 0.05, 0.2, 0.5, 0.1, 0.7, l2)
+    sc.add_sphere((0.5, 0.5, 0.5), 0.2, grey)
+    sc.add_quad(2, 0.9, 0.1, 0.4, 0.6, 0.95, l3)
+    sc.add_sphere((0.3, 0.6, 0.4), 0.1, l4)
+    sc.add_sphere((0.7, 0.2, 0.6), 0.05, l2)
+    rng = np.random.default_rng(41)
+    h, w = 32, 64
+    y = (np.arange(h) + 0.5) / h
+    env = np.stack([0.2 + 0.8 * y, 0.3 + 0.6 * y, 0.9 - 0.3 * y], 1)[:, None, :] * np.ones((1, w, 1))
+    env = env + rng.uniform(0.0, 0.5, (h, w, 3))
+    sc.env = env.astype(np.float32)
+    sc.env_intensity = 1.7
+    return sc
+
+
+def make_lights():
+    rng = np.random.default_rng(43)
+    rs = R.RefScene(light_scene())
+    n_lights = rs.lib.ref_scene_num_lights(rs.h)
+    out = {"n_lights": np.int32(n_lights)}
+    for li in range(n_lights):
+        uv = rng.uniform(0.0, 1.0, (512, 2)).astype(np.float32)
+        x = rng.uniform(0.0, 1.0, (512, 3)).astype(np.float32)
+        r = rs.light_eval(li, uv, x)
+        out.update({f"light{li}__uv": uv, f"light{li}__x": x, f"light{li}__area": np.float32(r["area"])})
+        out.update({f"light{li}__{k}": r[k] for k in ("point", "normal", "dir", "le", "pdf")})
+        # pdf_value at directions that are not the sample's: towards points
+        # near the light (often missing a quad) and random directions
+        pd = unit(r["point"] + rng.normal(scale=0.1, size=(512, 3)) - x) if li < n_lights - 1 else \
+            unit(rng.normal(size=(512, 3)))
+        pd = pd.astype(np.float32)
+        out[f"light{li}__pdf_dir"] = pd
+        out[f"light{li}__pdf_at_dir"] = rs.light_eval(li, uv, x, pdf_dir=pd)["pdf"]
+    np.savez_compressed(OUT / "lights.npz", **out)
+
+
 def make_bsdf():
     rng = np.random.default_rng(5)
     out = {}
@@ -258,6 +306,7 @@ if __name__ == "__main__":
     make_samplers()
     make_trace()
     make_transforms()
+    make_lights()
     make_bsdf()
     make_images()
     make_tonemap()

@@ -27,8 +27,9 @@ def test_oracle_pixel_grid_light_grid_and_strata():
     ls = np.arange(6)
     assert np.all((lo[..., 0] >= (ls // 3) / 2) & (lo[..., 0] < (ls // 3 + 1) / 2))
     assert np.all((lo[..., 1] >= (ls % 3) / 3) & (lo[..., 1] < (ls % 3 + 1) / 3))
-    strata = np.sort(np.floor(dv.reshape(spp, npix, 6) * spp).astype(int), axis=0)
-    assert np.array_equal(strata, np.broadcast_to(np.arange(spp)[:, None, None], strata.shape))
+    srt = np.sort(dv.reshape(spp, npix, 6).astype(np.float64), axis=0)
+    kk = np.arange(spp)[:, None, None]
+    assert np.all((srt >= kk / spp) & (srt <= (kk + 1) / spp))
 
 
 def test_oracle_halton_dims_equal_sampler_eval():
