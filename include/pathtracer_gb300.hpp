@@ -50,6 +50,72 @@ inline float to_radian(float deg) { return deg * 3.14159265358979323846f / 180.f
 enum class TransportMode { Radiance, Importance };
 enum class Axis { X = 0, Y = 1, Z = 2 };
 
+namespace detail {
+inline void check(int rc, void *ctx) {
+  if (rc != PT_OK) {
+    char buf[512] = {0};
+    pt_last_error(ctx, buf, sizeof buf);
+    throw std::runtime_error(std::string("pathtracer_gb300: ") + buf);
+  }
+}
+// The device context of the API's calls made outside SceneInfo::render
+// (Material::f / scatter / scatter_pdf, HaltonSampler): one per host thread,
+// on device 0, created at first use and destroyed with the thread.
+inline void *thread_context() {
+  struct Holder {
+    void *ctx = nullptr;
+    ~Holder() {
+      if (ctx) pt_destroy(ctx);
+    }
+  };
+  thread_local Holder h;
+  if (!h.ctx) check(pt_create(&h.ctx, 0), nullptr);
+  return h.ctx;
+}
+}  // namespace detail
+
+// ------------------------------------------------------------- records
+// Ray (base/ray.hpp), HitRecord / ScatterRecord (material/materialBase.hpp:
+// 11-53) with the fields the materials and lights read, BxDFFlags
+// (material/materialFlags.hpp:3-17).
+struct Ray {
+  Ray() = default;
+  Ray(vec3 origin, vec3 direction) : o(origin), d(direction) {}
+  vec3 getOrigin() const { return o; }
+  vec3 getDirection() const { return d; }
+  vec3 o, d;
+};
+enum BxDFFlags : uint32_t {
+  Reflection = 1u << 0,
+  Transmission = 1u << 1,
+  Diffuse = 1u << 2,
+  Glossy = 1u << 3,
+  Specular = 1u << 4,
+  DiffuseReflection = Diffuse | Reflection,
+  DiffuseTransmission = Diffuse | Transmission,
+  GlossyReflection = Glossy | Reflection,
+  GlossyTransmission = Glossy | Transmission,
+  SpecularReflection = Specular | Reflection,
+  SpecularTransmission = Specular | Transmission,
+  All = ~0u
+};
+struct HitRecord {
+  float t = 3.402823466e+38f;
+  vec3 normal;       // turned towards the incoming ray (set_normal)
+  vec3 position;
+  vec2 texCoords;
+  bool is_inside = false;  // the front-face flag (materialBase.hpp:47-52)
+};
+struct ScatterRecord {
+  Ray sampled_ray;
+  uint32_t sampled_type = All;
+  float pdf_val = 0.f;
+  vec3 attenuation;
+  bool is_specular() const { return (sampled_type & Specular) != 0; }
+  bool is_specular_reflection() const { return (sampled_type & SpecularReflection) == SpecularReflection; }
+  bool is_specular_transmission() const { return (sampled_type & SpecularTransmission) == SpecularTransmission; }
+};
+
 // ------------------------------------------------------------- materials
 // ------------------------------------------------------------ textures
 // Texture2D and its kinds (texture/texture.hpp:20-95); an ImageTexture takes
@@ -145,6 +211,76 @@ class Material {
   virtual bool is_emitter() const { return false; }
   // ColorVariant: the texture of the albedo / emission colour, if any
   virtual std::shared_ptr<Texture2D> texture() const { return nullptr; }
+
+  // Material::f (material.hpp:32-38): the BSDF for outgoing wo and incident
+  // wi at rec (its normal and is_inside), evaluated by the device code the
+  // render runs (pt_bsdf_eval).  The device implements the reference's
+  // configured transport mode, TransportMode::Importance (config.hpp:23);
+  // Radiance and textured colours are rejected (std::invalid_argument).
+  vec3 f(const vec3 &wo, const vec3 &wi, const HitRecord &rec,
+         TransportMode mode = TransportMode::Importance) const {
+    float fv[3], pdf;
+    eval(wo, wi, rec, mode, fv, pdf);
+    return vec3(fv[0], fv[1], fv[2]);
+  }
+  // Material::scatter_pdf(wo, wi, rec) (material.hpp:50-61).
+  float scatter_pdf(const vec3 &wo, const vec3 &wi, const HitRecord &rec,
+                    TransportMode mode = TransportMode::Importance) const {
+    float fv[3], pdf;
+    eval(wo, wi, rec, mode, fv, pdf);
+    return pdf;
+  }
+  // Material::scatter (material.hpp:18-27): samples the incident direction
+  // for ray_in at rec with the sampler values uc, u (pt_bsdf_sample); srec
+  // gets the sampled ray (from rec.position), attenuation, pdf_val and
+  // sampled_type.  False: no scattering (an emitter, or an invalid sample).
+  bool scatter(const Ray &ray_in, HitRecord &rec, ScatterRecord &srec, float uc, const vec2 &u,
+               TransportMode mode = TransportMode::Importance) const {
+    const pt_material_desc d = checked_desc(mode);
+    const vec3 dd = ray_in.getDirection();
+    const float wo[3] = {-dd[0], -dd[1], -dd[2]};
+    const float nrm[3] = {rec.normal[0], rec.normal[1], rec.normal[2]};
+    const uint8_t front = rec.is_inside ? 1 : 0;
+    const float uu[2] = {u.v[0], u.v[1]};
+    uint8_t ok = 0;
+    float wi[3], att[3], pdf = 0.f;
+    uint32_t type = 0;
+    void *ctx = detail::thread_context();
+    detail::check(pt_bsdf_sample(ctx, &d, 1, wo, nrm, &front, &uc, uu, &ok, wi, att, &pdf, &type), ctx);
+    if (!ok) return false;
+    srec.sampled_ray = Ray(rec.position, vec3(wi[0], wi[1], wi[2]));
+    srec.attenuation = vec3(att[0], att[1], att[2]);
+    srec.pdf_val = pdf;
+    srec.sampled_type = type;
+    return true;
+  }
+  // Material::emit (material.hpp:483-488 for DiffuseEmitter): its colour times
+  // intensity where the ray meets the normal's side, else black; zero for
+  // every other material.
+  vec3 emit(const Ray &ray_in, const HitRecord &rec) const {
+    if (!is_emitter()) return vec3(0.f);
+    if (texture()) throw std::invalid_argument("emit(): textured emitters are evaluated by the render only");
+    const pt_material_desc d = desc();
+    const vec3 dd = ray_in.getDirection();
+    const float c = -(rec.normal[0] * dd[0] + rec.normal[1] * dd[1] + rec.normal[2] * dd[2]);
+    return c > 0.f ? vec3(d.p[0] * d.p[3], d.p[1] * d.p[3], d.p[2] * d.p[3]) : vec3(0.f);
+  }
+
+ private:
+  pt_material_desc checked_desc(TransportMode mode) const {
+    if (mode != TransportMode::Importance)
+      throw std::invalid_argument("the device BSDFs implement TransportMode::Importance (config.hpp:23)");
+    if (texture()) throw std::invalid_argument("textured colours are evaluated by the render only");
+    return desc();
+  }
+  void eval(const vec3 &wo, const vec3 &wi, const HitRecord &rec, TransportMode mode, float *fv, float &pdf) const {
+    const pt_material_desc d = checked_desc(mode);
+    const float o[3] = {wo[0], wo[1], wo[2]}, w[3] = {wi[0], wi[1], wi[2]};
+    const float nrm[3] = {rec.normal[0], rec.normal[1], rec.normal[2]};
+    const uint8_t front = rec.is_inside ? 1 : 0;
+    void *ctx = detail::thread_context();
+    detail::check(pt_bsdf_eval(ctx, &d, 1, o, w, nrm, &front, fv, &pdf), ctx);
+  }
 };
 namespace detail {
 inline pt_material_desc make(int32_t type, std::initializer_list<float> p, int32_t flags = 0) {
@@ -584,6 +720,158 @@ class PerspectiveCamera {  // base/camera.hpp
   float fov, aspect, focalDist, aperture;
   vec3 up, front, position;
 };
+
+// ------------------------------------------------------------ samplers
+// Sampler / HaltonSampler (sampler/sampler.hpp:7-83): the sample index
+// advances with startSample() and the dimension counter restarts; get1D /
+// get2D take the next dimensions of the index's point, computed by the device
+// code the render runs (pt_sampler_eval, fetched 32 dimensions at a time).
+enum class RandomStrategy { None, PermuteDigits, Owen };
+class Sampler {
+ public:
+  virtual ~Sampler() = default;
+  virtual float get1D() = 0;
+  virtual vec2 get2D() = 0;
+};
+class HaltonSampler : public Sampler {
+ public:
+  explicit HaltonSampler(uint32_t seed = 0, RandomStrategy strat = RandomStrategy::Owen)
+      : strategy(strat), seed_(seed) {}
+  void startSample() {
+    ++sampleIndex_;
+    dimension_ = 0;
+    block_.clear();
+  }
+  float get1D() override { return dim(dimension_++); }
+  vec2 get2D() override {
+    const float x = dim(dimension_++);
+    const float y = dim(dimension_++);
+    return vec2(x, y);
+  }
+  // The current sample index (the reference's sampleIndex_; the render's
+  // path (i, j, k) of a W x H x spp frame uses 1 + ((i H + j) spp + k)).
+  uint32_t sampleIndex() const { return sampleIndex_; }
+  void setSampleIndex(uint32_t index) {
+    sampleIndex_ = index;
+    dimension_ = 0;
+    block_.clear();
+  }
+
+ private:
+  float dim(int d) {
+    if (d >= (int)block_.size()) {
+      const int dims = (d / 32 + 1) * 32;
+      block_.assign((size_t)dims, 0.f);
+      void *ctx = detail::thread_context();
+      detail::check(pt_sampler_eval(ctx, (int32_t)strategy, seed_, sampleIndex_, 1, dims, block_.data()), ctx);
+    }
+    return block_[(size_t)d];
+  }
+  RandomStrategy strategy;
+  uint32_t seed_;
+  uint32_t sampleIndex_ = 0;
+  int dimension_ = 0;
+  std::vector<float> block_;  // dimensions of the current index fetched so far
+};
+
+// ------------------------------------------------------------- lights
+// Light (light/light.hpp:17-53): light `index` of a scene uploaded to ctx,
+// in the LightList order the render samples (lightDiscovery.hpp:5-81: the
+// DiffuseEmitter rectangles and spheres in object order, then the
+// environment), evaluated by the device code of next-event estimation
+// (pt_light_sample).  get_normal_at and L_emit are taken at the point
+// get_sample(u, v) gives, the only points the reference's NEE asks about
+// (maxdepth_nee.hpp:171-176).
+enum class LightType { QUAD_LIGHT, SPHERE_LIGHT, ENVIRONMENT_LIGHT };
+struct LightSample {
+  vec3 point, normal, dir, Le;
+  float pdf = 0.f;
+};
+class Light {
+ public:
+  Light(void *ctx, int32_t scene, int32_t index) : ctx(ctx), scene(scene), index(index) {}
+  // get_sample(u, v) with get_normal_at there, the direction from x to it,
+  // L_emit towards x (texCoords (u, v)) and pdf_value(x, that direction)
+  LightSample sample(float u, float v, const vec3 &x) const { return eval(u, v, x, nullptr); }
+  vec3 get_sample(float u, float v) const { return eval(u, v, vec3(0.f), nullptr).point; }
+  vec3 get_normal_at_sample(float u, float v) const { return eval(u, v, vec3(0.f), nullptr).normal; }
+  vec3 L_emit_towards(float u, float v, const vec3 &x) const { return eval(u, v, x, nullptr).Le; }
+  float pdf_value(const vec3 &origin, const vec3 &dir) const { return eval(0.5f, 0.5f, origin, &dir).pdf; }
+  float get_area() const {
+    float a = 0.f;
+    detail::check(pt_light_sample(ctx, scene, index, 0, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
+                                  nullptr, nullptr, &a),
+                  ctx);
+    return a;
+  }
+
+ private:
+  LightSample eval(float u, float v, const vec3 &x, const vec3 *pdf_dir) const {
+    const float uv[2] = {u, v}, xx[3] = {x[0], x[1], x[2]};
+    float pd[3] = {0.f, 0.f, 0.f};
+    if (pdf_dir)
+      for (int c = 0; c < 3; ++c) pd[c] = (*pdf_dir)[c];
+    float p[3], n[3], w[3], le[3], pdf;
+    detail::check(pt_light_sample(ctx, scene, index, 1, uv, xx, pdf_dir ? pd : nullptr, p, n, w, le, &pdf, nullptr),
+                  ctx);
+    LightSample r;
+    r.point = vec3(p[0], p[1], p[2]);
+    r.normal = vec3(n[0], n[1], n[2]);
+    r.dir = vec3(w[0], w[1], w[2]);
+    r.Le = vec3(le[0], le[1], le[2]);
+    r.pdf = pdf;
+    return r;
+  }
+  void *ctx;
+  int32_t scene, index;
+};
+// LightList (base/lightList.hpp:5-40) of a scene uploaded to ctx.
+class LightList {
+ public:
+  LightList(void *ctx, int32_t scene) : ctx(ctx), scene(scene) {
+    int64_t info[6] = {0};
+    detail::check(pt_scene_info(ctx, scene, info), ctx);
+    n = (int)info[4];
+  }
+  size_t size() const { return (size_t)n; }
+  Light get(int i) const {
+    if (i < 0 || i >= n) throw std::out_of_range("light index");
+    return Light(ctx, scene, i);
+  }
+
+ private:
+  void *ctx;
+  int32_t scene;
+  int n = 0;
+};
+
+// getRayColor (integrator/maxdepth_nee.hpp:9-256) for rays through a scene
+// uploaded to ctx, on the device (pt_ray_color): one path per ray, ray i with
+// Halton index first_index + i.  estimator PT_EST_REF_NEE is the reference's
+// NEE integrator; light samples 2 x 2 (LIGHT_SAMPLE_X/Y, config.hpp:5-6).
+inline std::vector<vec3> getRayColor(void *ctx, int32_t scene, const std::vector<Ray> &rays, uint32_t max_depth,
+                                     uint32_t first_index = 1, int32_t estimator = PT_EST_REF_NEE,
+                                     uint32_t seed = 0) {
+  std::vector<float> r;
+  for (const Ray &ray : rays)
+    for (int c = 0; c < 6; ++c) r.push_back(c < 3 ? ray.getOrigin()[c] : ray.getDirection()[c - 3]);
+  pt_job_desc j{};
+  j.scene = scene;
+  j.width = j.height = j.spp_x = j.spp_y = 1;
+  j.max_depth = (int32_t)max_depth;
+  j.rr_start = -1;
+  j.estimator = estimator;
+  j.sampler = PT_SAMPLER_HALTON_OWEN;
+  j.env_sampling = PT_ENV_UNIFORM;
+  j.light_samples_x = j.light_samples_y = 2;
+  j.seed = seed;
+  j.gamma = 1.f;
+  std::vector<float> out(rays.size() * 3);
+  detail::check(pt_ray_color(ctx, &j, r.data(), (int32_t)rays.size(), first_index, out.data()), ctx);
+  std::vector<vec3> c;
+  for (size_t i = 0; i < rays.size(); ++i) c.push_back(vec3(out[3 * i], out[3 * i + 1], out[3 * i + 2]));
+  return c;
+}
 
 // SceneInfo (render/renderManager.hpp:35-176): render() uploads the scene and
 // renders it through the C-ABI; the film and the tone-mapped bytes are kept.
