@@ -4,8 +4,13 @@ reference's golden fixtures.
 Bars (from the path's contract): sampler sequences bit-exact; closest-hit
 primitive ids identical with t within 1e-5 relative (the primitive tests
 restate the reference's arithmetic, so t is compared bit for bit where the
-reference's traversal order cannot differ); BSDF eval/pdf/sample within 1e-4
-relative; images statistically equal (per-channel image mean within 3 sigma).
+reference's traversal order cannot differ); BSDF eval/pdf within 1e-4
+relative; BSDF samples: the same decision and lobe, direction within 2e-5,
+attenuation and pdf within 1e-4 relative (or within 8 FP32 steps of the
+reference's own conditioning where a lobe is so peaky that one rounding step
+of the direction moves it by more than 1e-5); images statistically equal
+(per-channel image mean within 3 sigma) and per pixel equal to the oracle's,
+which draws the same sample streams.
 """
 from __future__ import annotations
 
@@ -117,20 +122,56 @@ def test_emitter_does_not_scatter(renderer):
     assert not ok.any() and not G["ok"].any()
 
 
+def _conditioning(mat, G, delta=1e-6, k=6):
+    """Relative sensitivity of the reference's f and pdf (through the oracle,
+    pinned to the reference's eval at ~1e-6) to a change of the sampled
+    direction: max over k random tangent perturbations of size delta of
+    |d f| / |f| / delta and |d pdf| / pdf / delta."""
+    rng = np.random.default_rng(0)
+    wi = G["s_wi"].astype(np.float64)
+    f0, p0 = O.bsdf_eval(mat, G["wo"], G["s_wi"], G["nrm"], G["front"])
+    kap = np.zeros(len(wi))
+    for _ in range(k):
+        d = rng.normal(size=wi.shape)
+        d -= (d * wi).sum(1, keepdims=True) * wi
+        d /= np.linalg.norm(d, axis=1, keepdims=True) + 1e-30
+        w2 = wi + delta * d
+        w2 /= np.linalg.norm(w2, axis=1, keepdims=True) + 1e-30
+        f1, p1 = O.bsdf_eval(mat, G["wo"], w2.astype(np.float32), G["nrm"], G["front"])
+        kap = np.maximum(kap, np.abs(p1 - p0) / (np.abs(p0) + 1e-30) / delta)
+        kap = np.maximum(kap, (np.abs(f1 - f0) / (np.abs(f0) + 1e-30)).max(1) / delta)
+    return kap
+
+
 @pytest.mark.parametrize("name", sorted(n for n in CASES if n not in ("phong", "emitter")))
 def test_bsdf_sample_matches_reference(renderer, name):
+    """Material::scatter against the reference's on the same (wo, uc, u):
+    the same decision (ok) and lobe (sampled_type) for every sample; the
+    sampled direction within 2e-5 (absolute, unit vectors); attenuation and
+    pdf_val within 1e-4 relative -- or, where one FP32 rounding step of the
+    direction (eps = 2^-23) already moves the reference's own f or pdf by more
+    than 1e-5 (a peaky lobe: the anisotropic glass of Disney at alpha_y 0.012),
+    within 8 such steps of that conditioning, kappa * eps * 8, kappa measured
+    on the reference's eval at its own sampled direction."""
     G = CASES[name]
     mat = N.material(int(G["type"]), G["params"], int(G["flags"]))
     ok, wi, att, pdf, ty = renderer.bsdf_sample(mat, G["wo"], G["nrm"], G["front"], G["uc"], G["u"])
     okr = G["ok"].astype(bool)
-    # a sample on the boundary of a branch may flip; allow a handful
-    assert (ok == okr).mean() > 0.99
-    m = ok & okr & (ty == G["s_type"])
-    assert m.sum() >= 0.97 * okr.sum()
-    assert np.abs(wi[m] - G["s_wi"][m]).max(initial=0) < 2e-3
-    close = np.isclose(att[m], G["s_att"][m], rtol=1e-3, atol=1e-4).all(1) & \
-        np.isclose(pdf[m], G["s_pdf"][m], rtol=1e-3, atol=1e-4)
-    assert close.mean() > 0.98
+    assert np.array_equal(ok.astype(bool), okr)
+    assert np.array_equal(ty[okr], G["s_type"][okr])
+    m = okr
+    assert np.abs(wi[m] - G["s_wi"][m]).max(initial=0) < 2e-5
+    kap = _conditioning(mat, G)
+    tol = np.maximum(1e-4, 8.0 * kap * 2.0 ** -23)
+    ea = (np.abs(att - G["s_att"]) / (np.abs(G["s_att"]) + 1e-12)).max(1)
+    ea = np.where(np.abs(att - G["s_att"]).max(1) <= 1e-6, 0.0, ea)  # both ~0
+    ep = np.abs(pdf - G["s_pdf"]) / (np.abs(G["s_pdf"]) + 1e-12)
+    ep = np.where(np.abs(pdf - G["s_pdf"]) <= 1e-6, 0.0, ep)
+    assert np.all(ea[m] <= tol[m]), (name, ea[m].max(), int((ea[m] > tol[m]).sum()))
+    assert np.all(ep[m] <= tol[m]), (name, ep[m].max(), int((ep[m] > tol[m]).sum()))
+    # the strict 1e-4 bar holds on every sample the conditioning does not excuse
+    strict = m & (kap * 2.0 ** -23 < 1e-5)
+    assert np.all(ea[strict] <= 1e-4) and np.all(ep[strict] <= 1e-4)
 
 
 def test_phong_sample_consistent(renderer):
@@ -192,6 +233,29 @@ def test_render_material_divergence_matches_oracle(renderer):
     assert np.isfinite(film).all()
     z = _img_z(film, v_o, m_o, v_o, 16)
     assert np.all(np.abs(z) < 3.0), z
+    # same sample streams as the oracle (stratified dimensions, medium free
+    # flights, all five material families): per-pixel agreement
+    close = np.isclose(film, m_o, rtol=1e-3, atol=1e-4).all(-1)
+    assert close.mean() > 0.95, close.mean()
+    renderer.release(sid)
+
+
+def test_render_cornell_full_size_matches_oracle(renderer):
+    """The Cornell workload at its full size -- 256 x 256, 64 spp (8 x 8),
+    depth 8, the 5120-triangle gold icosphere, REF_NEE -- against the oracle
+    on all host cores: per-channel image means within 3 sigma and per-pixel
+    agreement (same sample streams)."""
+    sc, cam = S.cornell_icosphere(4)
+    sid = renderer.upload(sc)
+    job = N.job_desc(sid, cam, 256, 256, 8, 8, 8, seed=1)
+    film = renderer.render(job)
+    job.scene = 0
+    m_o, v_o = O.render(sc, job)
+    assert np.isfinite(film).all()
+    z = _img_z(film, v_o, m_o, v_o, 64)
+    assert np.all(np.abs(z) < 3.0), z
+    close = np.isclose(film, m_o, rtol=1e-3, atol=1e-4).all(-1)
+    assert close.mean() > 0.97, close.mean()
     renderer.release(sid)
 
 

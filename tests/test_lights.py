@@ -9,7 +9,8 @@ give, in that order).
 CPU: the oracle's restatement.  GPU: pt_light_sample through the C-ABI (the
 device code next-event estimation runs).  Bars: points, normals, directions
 and radiance within 1e-5 relative (the GPU evaluates sin/cos(2 pi u) as
-sincospi, without the reference's rounding of 2 pi u), pdf_value within
+sincospi, without the reference's rounding of 2 pi u; vector components
+relative to the vector's length), pdf_value within
 1e-4 relative, areas equal to 1e-6."""
 from __future__ import annotations
 
@@ -32,8 +33,12 @@ def _light_scene():
 
 def _check(g, li, got):
     pre = f"light{li}__"
-    for k in ("point", "normal", "dir", "le"):
-        assert rel_close(got[k], g[pre + k], rtol=1e-5, atol=1e-6), (li, k, np.abs(got[k] - g[pre + k]).max())
+    for k in ("point", "normal", "dir"):
+        # vectors: component errors relative to the vector's length (an
+        # environment point is a direction times 1e5)
+        err = np.abs(got[k] - g[pre + k]).max(1) / np.linalg.norm(g[pre + k], axis=1)
+        assert (err <= 1e-5).all(), (li, k, err.max())
+    assert rel_close(got["le"], g[pre + "le"], rtol=1e-5, atol=1e-6), (li, np.abs(got["le"] - g[pre + "le"]).max())
     assert rel_close(got["pdf"], g[pre + "pdf"], rtol=1e-4, atol=1e-7), (li, np.abs(got["pdf"] - g[pre + "pdf"]).max())
     # pdf_value at other directions: equal where both agree that the ray
     # meets the light (a direction grazing a quad's edge may fall either side)
