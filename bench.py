@@ -97,6 +97,10 @@ def parse():
     ap.add_argument("--serve-pass-spp", type=int, default=16, help="samples per request per scheduling pass")
     ap.add_argument("--serve-pass-paths", type=int, default=1 << 21,
                     help="paths per request per scheduling pass (0: pass-spp only)")
+    ap.add_argument("--config4-seconds", type=float, default=120.0,
+                    help="arrival window of the served config-4 mix (20 req/s; 0: skip)")
+    ap.add_argument("--config4-drain", type=float, default=20.0,
+                    help="seconds the config-4 server keeps running after the arrivals end")
     return ap.parse_args()
 
 
@@ -425,6 +429,112 @@ def run_served(r, scenes, big, seconds: float, rate: float, seed: int = 12, pass
     }
 
 
+def run_served_config4(r, scenes, big, seconds: float, rate: float, drain: float, seed: int = 14,
+                       pass_paths: int = 1 << 26, max_queue: int = 512, max_slots: int = 256):
+    """The served workload as specified for serving: Poisson arrivals at
+    `rate` req/s for `seconds` over the 4 resident scenes (Cornell, rough glass
+    1.3 M tris, material divergence, rough glass 5.2 M tris), each request a
+    seeded camera, square resolution log-uniform 128..2048, an spp cap
+    U{16..1024} and a target RMSE of 0.02 (whichever first).  Admission by
+    free HBM and slots, SRPT scheduling (pt_server_set_policy: the least
+    remaining work first, `pass_paths` per pass), a bounded queue (PT_ERR_BUSY
+    beyond `max_queue` waiting requests: refused).  The loop runs until the
+    arrivals end plus `drain` seconds; requests still unfinished then are
+    cancelled and counted.  This mix asks for far more paths than one GPU
+    renders in that time (a 2048^2 request at its cap is 4.3 G paths), so the
+    numbers describe an overloaded server: which requests finish, and how
+    fast."""
+    from pathtracer_gb300 import native as N
+    from pathtracer_gb300 import scene as S
+
+    rng = np.random.default_rng(seed)
+    pool = dict(scenes)
+    if big is not None:
+        pool["rough_glass_5m"] = big
+    names = sorted(pool)
+    reqs = []
+    t = 0.0
+    while True:
+        t += float(rng.exponential(1.0 / rate))
+        if t > seconds:
+            break
+        name = names[int(rng.integers(len(names)))]
+        key = "rough_glass" if name == "rough_glass_5m" else name
+        sid, cam, focus = pool[name]
+        side = int(round(np.exp(rng.uniform(np.log(128), np.log(2048)))))
+        cap = int(rng.integers(16, 1025))
+        job = S.job_mix({key: (sid, cam, focus)}, 1, seed=int(rng.integers(1 << 30)), res=(side, side),
+                        spp=(cap, cap))[0]
+        reqs.append((t, job, cap, side))
+    srv = N.Server(r, hbm_budget=64 << 30, max_slots=max_slots)
+    srv.set_policy(N.SERVE_SRPT, pass_paths=pass_paths, max_queue=max_queue)
+    refused, outstanding, ids = 0, set(), {}
+    done = {}
+    busy, k, passes = 0.0, 0, 0
+    t0 = time.perf_counter()
+    while True:
+        now = time.perf_counter() - t0
+        while k < len(reqs) and reqs[k][0] <= now:
+            try:
+                rid = srv.submit(reqs[k][1], target_rmse=0.02, spp_cap=reqs[k][2], spp_per_pass=16)
+                ids[rid] = k
+                outstanding.add(rid)
+            except N.PtError as e:
+                if e.code != -6:
+                    raise
+                refused += 1
+            k += 1
+        if now > seconds + drain:
+            break
+        if not outstanding:
+            if k >= len(reqs):
+                break
+            time.sleep(max(0.0, min(reqs[k][0], seconds + drain) - (time.perf_counter() - t0)))
+            continue
+        s0 = time.perf_counter()
+        srv.step()
+        busy += time.perf_counter() - s0
+        passes += 1
+        for rid in list(outstanding):
+            st, n = srv.state(rid)
+            if st >= N.REQ_DONE:
+                outstanding.discard(rid)
+                if st == N.REQ_DONE:
+                    done[rid] = n
+    wall = time.perf_counter() - t0
+    queued_at_end = sum(1 for rid in outstanding if srv.state(rid)[0] == N.REQ_QUEUED)
+    lat, qd = [], []
+    for rid in ids:
+        q, l_ms = srv.times(rid)
+        if q >= 0:
+            qd.append(q)
+        if rid in done:
+            lat.append(l_ms)
+    for rid in outstanding:
+        srv.cancel(rid)
+    srv.close()
+    paths = sum(reqs[ids[rid]][1].width * reqs[ids[rid]][1].height * n for rid, n in done.items())
+    lat.sort()
+    qd.sort()
+    pct = lambda v, q: v[min(len(v) - 1, int(q * len(v)))] if v else None
+    sides = [reqs[ids[rid]][3] for rid in done]
+    return {
+        "rate_req_s": rate, "arrival_seconds": seconds, "drain_seconds": drain, "arrivals": len(reqs),
+        "submitted": len(ids), "refused_queue_full": refused, "completed": len(done),
+        "unfinished_cancelled": len(outstanding), "still_queued_at_end": queued_at_end,
+        "p50_ms": pct(lat, 0.5), "p99_ms": pct(lat, 0.99), "max_ms": lat[-1] if lat else None,
+        "queue_delay_p50_ms": pct(qd, 0.5), "queue_delay_p99_ms": pct(qd, 0.99),
+        "completed_median_side": int(np.median(sides)) if sides else None,
+        "completed_max_side": max(sides) if sides else None,
+        "mean_spp_completed": float(np.mean(list(done.values()))) if done else None,
+        "paths_completed": paths, "paths_per_s_busy": paths / busy if busy else None,
+        "passes": passes, "wall_s": wall,
+        "mix": "4 resident scenes (cornell, rough_glass 1.3M tris, divergence, rough_glass 5.2M tris) with "
+               "motion; res log-uniform 128..2048, spp cap U{16..1024}, target RMSE 0.02, NEE+MIS; SRPT "
+               f"with {pass_paths} paths per pass, queue bound {max_queue}, {max_slots} slots",
+    }
+
+
 def converged_rmse(r, sid, cam, wl, k_step: int, win: int = 64, ref_grid: int = 256):
     """RMSE of the workload's render against a converged reference on the
     frame's centre window: the reference is the GPU render of that window at
@@ -704,6 +814,11 @@ def run_ours(args, rank, world, local_rank):
                                                   tune_sample=32, tune_spp=32)
         forms["served"] = run_served(r, fs, big, args.serve_seconds, args.serve_rate, pass_spp=args.serve_pass_spp,
                                      pass_paths=args.serve_pass_paths)
+        if args.config4_seconds > 0:
+            forms["served_config4"] = run_served_config4(r, fs, big, args.config4_seconds, 20.0,
+                                                         args.config4_drain)
+            forms["served_config4_saturating"] = run_served_config4(r, fs, big, 5.0, 200.0, args.config4_drain,
+                                                                    seed=15)
         line["forms"] = forms
     if not args.no_cpu_baseline:
         from oracle import pyoracle as O

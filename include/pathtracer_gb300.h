@@ -30,7 +30,7 @@ enum {
   PT_ERR_NOMEM = -3,       /* device or host allocation failed             */
   PT_ERR_NOT_FOUND = -4,   /* unknown scene / request id                   */
   PT_ERR_DEVICE = -5,      /* device-side error flag (iteration cap hit)   */
-  PT_ERR_BUSY = -6,        /* admission refused: not enough free HBM       */
+  PT_ERR_BUSY = -6,        /* admission refused: the server's queue is full */
   PT_ERR_CANCELLED = -7,   /* request was cancelled                        */
   PT_ERR_TOO_LARGE = -8    /* size beyond a fixed, documented maximum      */
 };
@@ -594,6 +594,20 @@ int pt_server_step(void *server, int32_t *active);
 int pt_poll(void *server, int64_t request_id, int32_t *state, float *film,
             int32_t *spp_done, double *latency_ms);
 int pt_cancel(void *server, int64_t request_id);
+
+/* Scheduling policy of a server.  PT_SERVE_FAIR (default): admission in
+ * arrival order, and every pass renders the next chunk of every active
+ * request.  PT_SERVE_SRPT (shortest remaining work first): the queued request
+ * of least total work (width * height * spp cap) is admitted first, and a pass
+ * takes the active requests in order of remaining paths until it holds
+ * pass_paths (0: all; at least one request per pass) -- small requests finish
+ * in few passes while large ones wait.  max_queue > 0: pt_submit refuses with
+ * PT_ERR_BUSY while that many requests wait for admission (0: unbounded). */
+enum { PT_SERVE_FAIR = 0, PT_SERVE_SRPT = 1 };
+int pt_server_set_policy(void *server, int32_t policy, int64_t pass_paths, int32_t max_queue);
+/* Queueing delay of a request (submit to admission; -1 while queued) and its
+ * latency (submit to completion; -1 until done), milliseconds. */
+int pt_request_times(void *server, int64_t request_id, double *queue_ms, double *latency_ms);
 
 #ifdef __cplusplus
 }

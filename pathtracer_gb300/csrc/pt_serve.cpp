@@ -34,7 +34,8 @@ struct Request {
   int spp_a = 0, spp_b = 0;
   int passes = 0;  // scheduling passes rendered (even ones go to film_a)
   size_t bytes = 0;
-  std::chrono::steady_clock::time_point t_submit, t_done;
+  std::chrono::steady_clock::time_point t_submit, t_admit, t_done;
+  bool admitted = false;
   std::vector<float> result;
   std::string error;
   double last_rmse = INFINITY;  // latest estimate of the mean image's RMSE
@@ -49,6 +50,10 @@ struct Server {
   std::deque<int64_t> queue;
   std::vector<int64_t> active;
   int64_t used = 0;
+  // scheduling (pt_server_set_policy)
+  int policy = PT_SERVE_FAIR;
+  int64_t pass_paths = 0;  // SRPT: paths per pass (0: no limit)
+  int max_queue = 0;       // > 0: pt_submit refuses beyond this many queued requests
   // device scratch of the RMSE estimates: pairs, partial sums, results
   FilmPair *d_pairs = nullptr;
   double *d_partials = nullptr, *d_out = nullptr;
@@ -70,6 +75,14 @@ struct Server {
     pairs_cap = 0;
   }
 };
+
+// The request's samples cap and the paths still to render (SRPT's key).
+static int request_cap(const Request &r) {
+  return std::min(r.desc.spp_cap, r.desc.job.spp_x * r.desc.job.spp_y);
+}
+static long long remaining_paths(const Request &r) {
+  return (long long)r.desc.job.width * r.desc.job.height * (request_cap(r) - r.spp_done);
+}
 
 static void release_films(Request &r, Server &s) {
   if (r.film_a) cudaFree(r.film_a);
@@ -150,6 +163,8 @@ int pt_submit(void *server, const pt_request_desc *req, int64_t *request_id) {
   }
   if (req->spp_cap <= 0 || req->spp_per_pass <= 0 || req->paths_per_pass < 0)
     return serr(s->ctx, PT_ERR_INVALID, "bad spp cap / pass");
+  if (s->max_queue > 0 && (int)s->queue.size() >= s->max_queue)
+    return serr(s->ctx, PT_ERR_BUSY, "admission refused: " + std::to_string(s->queue.size()) + " requests queued");
   Request r;
   r.id = s->next_id++;
   r.desc = *req;
@@ -164,8 +179,15 @@ int pt_server_step(void *server, int32_t *active_out) {
   if (!server) return PT_ERR_INVALID;
   Server *s = static_cast<Server *>(server);
   Context *c = s->ctx;
-  // admission: FIFO while slots and HBM allow
+  // admission while slots and HBM allow: FIFO, or (SRPT) the queued request
+  // of least total work first
   while (!s->queue.empty() && (int)s->active.size() < s->max_slots) {
+    if (s->policy == PT_SERVE_SRPT) {
+      auto best = s->queue.begin();
+      for (auto it = s->queue.begin(); it != s->queue.end(); ++it)
+        if (remaining_paths(s->reqs[*it]) < remaining_paths(s->reqs[*best])) best = it;
+      std::iter_swap(s->queue.begin(), best);
+    }
     Request &r = s->reqs[s->queue.front()];
     if (r.state == 3) {
       s->queue.pop_front();
@@ -185,12 +207,16 @@ int pt_server_step(void *server, int32_t *active_out) {
     r.bytes = need;
     s->used += (int64_t)need;
     r.state = 1;
+    r.admitted = true;
+    r.t_admit = std::chrono::steady_clock::now();
     s->active.push_back(r.id);
     s->queue.pop_front();
   }
-  // one pass over every active request: a batch with one job per request
-  // (its next spp_per_pass samples), rendered as one graph launch
-  std::vector<int64_t> still, live;
+  // one pass over the active requests: a batch with one job per request (its
+  // next spp_per_pass samples), rendered as one graph launch.  FAIR: every
+  // active request; SRPT: in order of remaining paths until the pass holds
+  // pass_paths (at least one request), the others wait for a later pass
+  std::vector<int64_t> still, live, order;
   std::vector<pt_job_desc> jobs;
   std::vector<float *> targets;
   std::vector<int> ends;
@@ -199,6 +225,19 @@ int pt_server_step(void *server, int32_t *active_out) {
     Request &r = s->reqs[id];
     if (r.state != 1) {
       release_films(r, *s);
+      continue;
+    }
+    order.push_back(id);
+  }
+  if (s->policy == PT_SERVE_SRPT)
+    std::stable_sort(order.begin(), order.end(), [&](int64_t a, int64_t b) {
+      return remaining_paths(s->reqs[a]) < remaining_paths(s->reqs[b]);
+    });
+  long long pass_sum = 0;
+  for (int64_t id : order) {
+    Request &r = s->reqs[id];
+    if (s->policy == PT_SERVE_SRPT && s->pass_paths > 0 && !jobs.empty() && pass_sum >= s->pass_paths) {
+      still.push_back(id);  // not in this pass
       continue;
     }
     pt_job_desc j = r.desc.job;
@@ -218,6 +257,7 @@ int pt_server_step(void *server, int32_t *active_out) {
     ends.push_back(e);
     to_a_v.push_back(to_a);
     live.push_back(id);
+    pass_sum += (long long)j.width * j.height * (e - b);
   }
   if (!jobs.empty()) {
     try {
@@ -299,6 +339,29 @@ int pt_server_step(void *server, int32_t *active_out) {
   s->active = still;
   cudaStreamSynchronize(c->stream);
   if (active_out) *active_out = (int32_t)(s->active.size() + s->queue.size());
+  return PT_OK;
+}
+
+int pt_server_set_policy(void *server, int32_t policy, int64_t pass_paths, int32_t max_queue) {
+  if (!server) return PT_ERR_INVALID;
+  Server *s = static_cast<Server *>(server);
+  if ((policy != PT_SERVE_FAIR && policy != PT_SERVE_SRPT) || pass_paths < 0 || max_queue < 0)
+    return serr(s->ctx, PT_ERR_INVALID, "bad server policy");
+  s->policy = policy;
+  s->pass_paths = pass_paths;
+  s->max_queue = max_queue;
+  return PT_OK;
+}
+
+int pt_request_times(void *server, int64_t request_id, double *queue_ms, double *latency_ms) {
+  if (!server) return PT_ERR_INVALID;
+  Server *s = static_cast<Server *>(server);
+  auto it = s->reqs.find(request_id);
+  if (it == s->reqs.end()) return serr(s->ctx, PT_ERR_NOT_FOUND, "unknown request");
+  const Request &r = it->second;
+  using ms = std::chrono::duration<double, std::milli>;
+  if (queue_ms) *queue_ms = r.admitted ? ms(r.t_admit - r.t_submit).count() : -1.0;
+  if (latency_ms) *latency_ms = r.state == 2 ? ms(r.t_done - r.t_submit).count() : -1.0;
   return PT_OK;
 }
 

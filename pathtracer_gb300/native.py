@@ -28,6 +28,7 @@ EST_REF_NEE, EST_NEE_MIS = 0, 1
 SAMPLER_HALTON_NONE, SAMPLER_HALTON_PERMUTE, SAMPLER_HALTON_OWEN, SAMPLER_STRATIFIED = range(4)
 ENV_UNIFORM, ENV_ALIAS = 0, 1
 BVH_BUILD_HOST, BVH_BUILD_DEVICE, BVH_BUILD_SAH = 0, 1, 2
+SERVE_FAIR, SERVE_SRPT = 0, 1
 
 # exported symbols of the C-ABI, in header order
 EXPORTS = [
@@ -36,7 +37,8 @@ EXPORTS = [
     "pt_profile_begin",
     "pt_profile_end", "pt_tonemap", "pt_gaussian_blur", "pt_write_png", "pt_sampler_eval", "pt_sample_eval", "pt_trace_closest",
     "pt_trace_any", "pt_intersect", "pt_light_sample", "pt_bsdf_eval", "pt_bsdf_sample", "pt_render_batch", "pt_autotune", "pt_server_create",
-    "pt_server_destroy", "pt_submit", "pt_server_step", "pt_poll", "pt_cancel",
+    "pt_server_destroy", "pt_submit", "pt_server_step", "pt_poll", "pt_cancel", "pt_server_set_policy",
+    "pt_request_times",
 ]
 
 f32p = C.POINTER(C.c_float)
@@ -203,6 +205,8 @@ def load() -> C.CDLL:
         "pt_server_step": [vp, i32p],
         "pt_poll": [vp, C.c_int64, i32p, f32p, i32p, C.POINTER(C.c_double)],
         "pt_cancel": [vp, C.c_int64],
+        "pt_server_set_policy": [vp, C.c_int32, C.c_int64, C.c_int32],
+        "pt_request_times": [vp, C.c_int64, C.POINTER(C.c_double), C.POINTER(C.c_double)],
     }
     for name, args in sig.items():
         fn = getattr(lib, name)
@@ -697,6 +701,18 @@ class Server:
         self.r._check(self.lib.pt_submit(self.handle, C.byref(req), C.byref(rid)))
         self.shapes[rid.value] = (job.height, job.width, 3)
         return rid.value
+
+    def set_policy(self, policy: int, pass_paths: int = 0, max_queue: int = 0):
+        """pt_server_set_policy: SERVE_FAIR or SERVE_SRPT (shortest remaining
+        work first, pass_paths per pass); max_queue > 0 refuses submissions
+        (PtError PT_ERR_BUSY) while that many requests are queued."""
+        self.r._check(self.lib.pt_server_set_policy(self.handle, policy, pass_paths, max_queue))
+
+    def times(self, rid: int):
+        """(queue_ms, latency_ms) of a request, -1 where not reached."""
+        q, lat = C.c_double(), C.c_double()
+        self.r._check(self.lib.pt_request_times(self.handle, rid, C.byref(q), C.byref(lat)))
+        return q.value, lat.value
 
     def step(self) -> int:
         active = C.c_int32()

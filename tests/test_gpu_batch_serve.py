@@ -174,6 +174,42 @@ def test_served_paths_per_pass(renderer, scenes):
     srv.close()
 
 
+def test_served_srpt_small_first_same_results(renderer, scenes):
+    """Shortest remaining work first: with a pass budget below the large
+    request's work, the small requests finish before it; every result equals
+    the same request served alone (a request's samples depend on its own job
+    only); a full queue refuses with PT_ERR_BUSY; queueing delay and latency
+    are reported."""
+    jobs = _jobs(scenes)
+    big, small = jobs[3], [jobs[0], jobs[1], jobs[2]]
+    alone = {}
+    for k, j in enumerate([big] + small):
+        srv = N.Server(renderer, hbm_budget=1 << 30, max_slots=8)
+        rid = srv.submit(j, spp_per_pass=2)
+        alone[k] = _serve_until_done(srv, [rid])[rid]
+        srv.close()
+    srv = N.Server(renderer, hbm_budget=1 << 30, max_slots=8)
+    budget = min(j.width * j.height * 2 for j in small)
+    srv.set_policy(N.SERVE_SRPT, pass_paths=budget, max_queue=4)
+    ids = [srv.submit(big, spp_per_pass=2)] + [srv.submit(j, spp_per_pass=2) for j in small]
+    with pytest.raises(N.PtError) as ei:
+        srv.submit(small[0], spp_per_pass=2)  # four requests wait: the queue is full
+    assert ei.value.code == -6
+    done_order = []
+    while len(done_order) < len(ids):
+        srv.step()
+        for rid in ids:
+            if rid not in done_order and srv.poll(rid)[0] == N.REQ_DONE:
+                done_order.append(rid)
+    assert done_order[-1] == ids[0]  # the large request finishes last
+    for k, rid in enumerate(ids):
+        st, film, spp, lat = srv.poll(rid)
+        assert np.array_equal(film, alone[k][0]) and spp == alone[k][1]
+        q, lat2 = srv.times(rid)
+        assert 0.0 <= q <= lat2
+    srv.close()
+
+
 def test_server_admission_by_budget_and_cancel(renderer, scenes):
     jobs = _jobs(scenes)
     j = jobs[0]
