@@ -2149,6 +2149,26 @@ int pt_render(void *ctx, const pt_job_desc *job, float *film_rgb, pt_stats *stat
   });
 }
 
+// pt_ray_color's job: one film pixel per ray, one sample -- path i is frame
+// pixel (first_index - 1 + i, 0) of a one-row frame at 1 spp, i.e. Halton
+// index first_index + i, and its film pixel receives its radiance.  The
+// camera is not used (the rays are given) beyond its shutter.
+static pt_job_desc ray_color_job(const pt_job_desc &job, int32_t n, uint32_t first_index) {
+  pt_job_desc j = job;
+  const float shutter = job.camera.shutter;
+  j.camera = pt_camera_desc{1.f, 1.f, 1.f, 1e3f, {0.f, 1.f, 0.f}, {0.f, 0.f, 1.f}, {0.f, 0.f, 0.f}, shutter};
+  j.width = n;
+  j.height = 1;
+  j.spp_x = j.spp_y = 1;
+  j.spp_begin = 0;
+  j.spp_end = 0;
+  j.crop_x = (int32_t)(first_index - 1u);
+  j.crop_y = 0;
+  j.full_width = (int32_t)((int64_t)first_index - 1 + n);
+  j.full_height = 1;
+  return j;
+}
+
 int pt_ray_color(void *ctx, const pt_job_desc *job, const float *rays, int32_t n, uint32_t first_index,
                  float *radiance) {
   Context *c = static_cast<Context *>(ctx);
@@ -2158,20 +2178,8 @@ int pt_ray_color(void *ctx, const pt_job_desc *job, const float *rays, int32_t n
       fail(PT_ERR_INVALID, "bad ray-color args");
     if (n == 0) return PT_OK;
     cuda_check(cudaSetDevice(c->device), "cudaSetDevice");
-    // one film pixel per ray, one sample: path i is frame pixel
-    // (first_index - 1 + i, 0) of a one-row frame at 1 spp, i.e. Halton index
-    // first_index + i, and its film pixel receives its radiance
-    pt_job_desc j = *job;
-    j.width = n;
-    j.height = 1;
-    j.spp_x = j.spp_y = 1;
-    j.spp_begin = 0;
-    j.spp_end = 0;
-    j.crop_x = (int32_t)(first_index - 1u);
-    j.crop_y = 0;
-    j.full_width = (int32_t)std::min<int64_t>((int64_t)first_index - 1 + n, INT32_MAX);
-    j.full_height = 1;
     if ((int64_t)first_index - 1 + n > INT32_MAX) fail(PT_ERR_INVALID, "first_index + n beyond 2^31");
+    const pt_job_desc j = ray_color_job(*job, n, first_index);
     const size_t nn = (size_t)n;
     float *df = c->film_buffer(nn * 3);
     float *dr = (float *)c->scratch(nn * 24);

@@ -38,7 +38,9 @@ def test_cpp_surface_matches_c_abi(tmp_path, renderer):
     from pathtracer_gb300 import native as N
     from pathtracer_gb300 import scene as S
 
-    out = subprocess.run([str(_build(tmp_path))], capture_output=True, text=True, check=True).stdout.split("\n")
+    proc = subprocess.run([str(_build(tmp_path))], capture_output=True, text=True)
+    assert proc.returncode == 0, proc.stderr
+    out = proc.stdout.split("\n")
     rows = [np.array([float(x) for x in ln.split()]) for ln in out if ln.strip()]
     gold = N.material(N.CONDUCTOR, [0.143, 0.374, 1.442, 3.983, 2.385, 1.603, 0.3, 0.3])
     wo = np.array([[0.3, -0.2, 0.932738]], np.float32)
