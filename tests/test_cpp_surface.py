@@ -61,7 +61,7 @@ def test_cpp_surface_matches_c_abi(tmp_path, renderer):
     k = 11
     n_lights = int(rows[k][0])
     k += 1
-    sc = S.Scene()
+    sc = S.Scene(bg=(0.7, 0.8, 1.0))  # SceneInfo's default bg_color (renderManager.hpp:41)
     white = sc.add_material(N.LAMBERTIAN, [0.75, 0.75, 0.75])
     lm = sc.add_material(N.DIFFUSE_EMITTER, [17.0, 12.0, 4.0, 1.0])
     gm = sc.add_material(N.CONDUCTOR, [0.143, 0.374, 1.442, 3.983, 2.385, 1.603, 0.3, 0.3])
