@@ -549,6 +549,15 @@ int pt_bsdf_sample(void *ctx, const pt_material_desc *mat, int32_t n,
 int pt_render_batch(void *ctx, const pt_job_desc *jobs, int32_t n_jobs,
                     float **films, pt_stats *stats);
 
+/* How pt_render_batch (and the server's passes) run the groups of jobs of one
+ * scene: PT_BATCH_GRAPH (default) -- per-stage kernels of merged waves, each
+ * group a branch of one CUDA graph; PT_BATCH_PERSISTENT -- ONE cooperative
+ * launch per group that runs all its waves and bounces (camera, closest hit,
+ * generic shading, shadow rays, films) with grid barriers between stages;
+ * groups one after another.  Both give each job the same samples. */
+enum { PT_BATCH_GRAPH = 0, PT_BATCH_PERSISTENT = 1 };
+int pt_set_batch_mode(void *ctx, int32_t mode);
+
 /* Launch autotuner (extension): renders the batch under candidate launch
  * configurations -- paths per wave of each job, material sorting on/off,
  * blocks per SM of the traversal and shade kernels -- keeps the fastest for

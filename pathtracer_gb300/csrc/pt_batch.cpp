@@ -47,6 +47,9 @@ void BatchSlot::release() {
   fr(d_start);
   fr(offsets);
   fr(films);
+  fr(d_films);
+  fr(d_barrier);
+  d_films_cap = 0;
   jobs_cap = 0;
   offsets_cap = films_cap = 0;
   for (int h = 0; h < 2; ++h) {
@@ -144,76 +147,12 @@ static std::string signature(const pt_job_desc *jobs, int n, const LaunchCfg &cf
   return s;
 }
 
-// Renders the batch; films[k] (host, may be null) receive job k's mean image;
-// with targets, job k's samples are added onto the device film targets[k].
-void render_batch(Context *c, const pt_job_desc *jobs, int n, float **films, pt_stats *stats,
-                  float **targets) {
+// The groups as branches of ONE CUDA graph (captured per batch composition,
+// updated in place when only parameters change): per-stage kernels of merged
+// waves; returns the graph's device milliseconds.
+static float render_groups_graph(Context *c, const pt_job_desc *jobs, int n, std::vector<Group> &groups,
+                                 float **targets) {
   Batch &B = c->batch;
-  if (!B.fork) cuda_check(cudaEventCreateWithFlags(&B.fork, cudaEventDisableTiming), "cudaEventCreate");
-  // ---- groups
-  std::vector<Group> groups;
-  std::map<std::pair<int, int>, int> gidx;
-  for (int k = 0; k < n; ++k) {
-    const pt_job_desc &j = jobs[k];
-    validate_job(j);
-    c->scene(j.scene);
-    const int ln = j.light_samples_x * j.light_samples_y;
-    auto key = std::make_pair(j.scene, ln);
-    auto it = gidx.find(key);
-    if (it == gidx.end()) {
-      it = gidx.emplace(key, (int)groups.size()).first;
-      groups.push_back(Group{j.scene, ln, {}, {}, 0, 0, {}, 0});
-    }
-    groups[it->second].members.push_back(k);
-  }
-  if ((int)B.slots.size() < (int)groups.size()) B.slots.resize(groups.size());
-  // ---- tables
-  for (size_t gi = 0; gi < groups.size(); ++gi) {
-    Group &G = groups[gi];
-    Scene *S = c->scene(G.scene);
-    MergedJobs &M = G.M;
-    M.LN = G.ln;
-    M.start.push_back(0);
-    size_t n_off = 0, film_floats = 0;
-    for (int k : G.members) {
-      const pt_job_desc &j = jobs[k];
-      const long long npix = (long long)j.width * j.height;
-      const int e = j.spp_end ? j.spp_end : j.spp_x * j.spp_y;
-      M.start.push_back(M.start.back() + npix * (e - j.spp_begin));
-      M.bounces = std::max(M.bounces, j.max_depth + (j.estimator == PT_EST_NEE_MIS ? 1 : 0));
-      n_off += (size_t)j.spp_x * j.spp_y;
-      G.film_off.push_back(film_floats);
-      film_floats += (size_t)npix * 3;
-    }
-    G.total = M.start.back();
-    G.film_floats = film_floats;
-    G.wave = (int)std::min<long long>(c->batch_wave_cap, G.total);
-    BatchSlot &slot = B.slots[gi];
-    slot.ensure(G.wave, G.ln, (int)G.members.size(), n_off, targets ? 1 : film_floats);
-    std::vector<float2> offs;
-    offs.reserve(n_off);
-    for (size_t m = 0; m < G.members.size(); ++m) {
-      const pt_job_desc &j = jobs[G.members[m]];
-      DeviceJob dj = c->device_job(j, S);
-      dj.job.offsets = slot.offsets + offs.size();
-      std::vector<float2> o = make_offsets(j);
-      offs.insert(offs.end(), o.begin(), o.end());
-      M.jobs.push_back(dj);
-      M.films.push_back(targets ? targets[G.members[m]] : slot.films + G.film_off[m]);
-    }
-    cuda_check(cudaMemcpyAsync(slot.offsets, offs.data(), offs.size() * sizeof(float2), cudaMemcpyHostToDevice,
-                               c->stream),
-               "upload offsets");
-    cuda_check(cudaMemcpyAsync(slot.d_jobs, M.jobs.data(), sizeof(DeviceJob) * M.jobs.size(),
-                               cudaMemcpyHostToDevice, c->stream),
-               "upload job table");
-    cuda_check(cudaMemcpyAsync(slot.d_start, M.start.data(), sizeof(long long) * M.start.size(),
-                               cudaMemcpyHostToDevice, c->stream),
-               "upload job starts");
-    M.T = JobTable{slot.d_jobs, slot.d_start, (int)G.members.size()};
-  }
-  cuda_check(cudaStreamSynchronize(c->stream), "batch set-up");
-  // ---- graph
   const std::string sig = signature(jobs, n, c->cfg, c->batch_wave_cap, targets);
   if (!B.exec || sig != B.sig) {
     cudaGraph_t graph = nullptr;
@@ -315,6 +254,130 @@ void render_batch(Context *c, const pt_job_desc *jobs, int n, float **films, pt_
   cudaEventElapsedTime(&ms, e0, e1);
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
+  return ms;
+}
+
+// The groups in the persistent form: one cooperative launch per group that
+// runs all its waves and bounces (pt_kernels_persist.cu), the groups one
+// after another on the context's stream; returns device milliseconds.
+static float render_groups_persistent(Context *c, std::vector<Group> &groups, bool targets) {
+  Batch &B = c->batch;
+  cudaEvent_t e0, e1;
+  cuda_check(cudaEventCreate(&e0), "cudaEventCreate");
+  cuda_check(cudaEventCreate(&e1), "cudaEventCreate");
+  cudaEventRecord(e0, c->stream);
+  for (size_t gi = 0; gi < groups.size(); ++gi) {
+    Group &G = groups[gi];
+    BatchSlot &slot = B.slots[gi];
+    Scene *S = c->scene(G.scene);
+    const int nm = (int)G.members.size();
+    if (nm > slot.d_films_cap) {
+      if (slot.d_films) cudaFree(slot.d_films);
+      slot.d_films = nullptr;
+      cuda_check(cudaMalloc(&slot.d_films, sizeof(float *) * nm), "cudaMalloc(film table)");
+      slot.d_films_cap = nm;
+    }
+    if (!slot.d_barrier) cuda_check(cudaMalloc(&slot.d_barrier, 16), "cudaMalloc(grid barrier)");
+    cuda_check(cudaMemcpyAsync(slot.d_films, G.M.films.data(), sizeof(float *) * nm, cudaMemcpyHostToDevice,
+                               c->stream),
+               "upload film table");
+    cuda_check(cudaMemsetAsync(slot.d_barrier, 0, 16, c->stream), "memset barrier");
+    cuda_check(cudaMemsetAsync(slot.Q[0].stats, 0, 64, c->stream), "memset stats");
+    cuda_check(cudaMemsetAsync(slot.Q[1].stats, 0, 64, c->stream), "memset stats");
+    if (!targets) cuda_check(cudaMemsetAsync(slot.films, 0, sizeof(float) * G.film_floats, c->stream), "memset films");
+    const int grid = persistent_grid(S->view.curves != nullptr, c->num_sms);
+    cuda_check(launch_group_persistent(S->view, G.M.T, slot.Q[0], slot.d_films, G.total, G.wave, G.M.LN,
+                                       G.M.bounces, slot.d_barrier, grid, c->stream),
+               "persistent group launch");
+  }
+  cudaEventRecord(e1, c->stream);
+  cuda_check(cudaStreamSynchronize(c->stream), "batch render");
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  for (size_t gi = 0; gi < groups.size(); ++gi) {
+    int bar[4] = {0, 0, 0, 0};
+    cuda_check(cudaMemcpy(bar, B.slots[gi].d_barrier, 16, cudaMemcpyDeviceToHost), "read barrier");
+    if (bar[2]) fail(PT_ERR_DEVICE, "persistent batch: a grid barrier wait ran out in group " + std::to_string(gi));
+  }
+  return ms;
+}
+
+// Renders the batch; films[k] (host, may be null) receive job k's mean image;
+// with targets, job k's samples are added onto the device film targets[k].
+void render_batch(Context *c, const pt_job_desc *jobs, int n, float **films, pt_stats *stats,
+                  float **targets) {
+  Batch &B = c->batch;
+  if (!B.fork) cuda_check(cudaEventCreateWithFlags(&B.fork, cudaEventDisableTiming), "cudaEventCreate");
+  // ---- groups
+  std::vector<Group> groups;
+  std::map<std::pair<int, int>, int> gidx;
+  for (int k = 0; k < n; ++k) {
+    const pt_job_desc &j = jobs[k];
+    validate_job(j);
+    c->scene(j.scene);
+    const int ln = j.light_samples_x * j.light_samples_y;
+    auto key = std::make_pair(j.scene, ln);
+    auto it = gidx.find(key);
+    if (it == gidx.end()) {
+      it = gidx.emplace(key, (int)groups.size()).first;
+      groups.push_back(Group{j.scene, ln, {}, {}, 0, 0, {}, 0});
+    }
+    groups[it->second].members.push_back(k);
+  }
+  if ((int)B.slots.size() < (int)groups.size()) B.slots.resize(groups.size());
+  // ---- tables
+  for (size_t gi = 0; gi < groups.size(); ++gi) {
+    Group &G = groups[gi];
+    Scene *S = c->scene(G.scene);
+    MergedJobs &M = G.M;
+    M.LN = G.ln;
+    M.start.push_back(0);
+    size_t n_off = 0, film_floats = 0;
+    for (int k : G.members) {
+      const pt_job_desc &j = jobs[k];
+      const long long npix = (long long)j.width * j.height;
+      const int e = j.spp_end ? j.spp_end : j.spp_x * j.spp_y;
+      M.start.push_back(M.start.back() + npix * (e - j.spp_begin));
+      M.bounces = std::max(M.bounces, j.max_depth + (j.estimator == PT_EST_NEE_MIS ? 1 : 0));
+      n_off += (size_t)j.spp_x * j.spp_y;
+      G.film_off.push_back(film_floats);
+      film_floats += (size_t)npix * 3;
+    }
+    G.total = M.start.back();
+    G.film_floats = film_floats;
+    G.wave = (int)std::min<long long>(c->batch_wave_cap, G.total);
+    BatchSlot &slot = B.slots[gi];
+    slot.ensure(G.wave, G.ln, (int)G.members.size(), n_off, targets ? 1 : film_floats);
+    std::vector<float2> offs;
+    offs.reserve(n_off);
+    for (size_t m = 0; m < G.members.size(); ++m) {
+      const pt_job_desc &j = jobs[G.members[m]];
+      DeviceJob dj = c->device_job(j, S);
+      dj.job.offsets = slot.offsets + offs.size();
+      std::vector<float2> o = make_offsets(j);
+      offs.insert(offs.end(), o.begin(), o.end());
+      M.jobs.push_back(dj);
+      M.films.push_back(targets ? targets[G.members[m]] : slot.films + G.film_off[m]);
+    }
+    cuda_check(cudaMemcpyAsync(slot.offsets, offs.data(), offs.size() * sizeof(float2), cudaMemcpyHostToDevice,
+                               c->stream),
+               "upload offsets");
+    cuda_check(cudaMemcpyAsync(slot.d_jobs, M.jobs.data(), sizeof(DeviceJob) * M.jobs.size(),
+                               cudaMemcpyHostToDevice, c->stream),
+               "upload job table");
+    cuda_check(cudaMemcpyAsync(slot.d_start, M.start.data(), sizeof(long long) * M.start.size(),
+                               cudaMemcpyHostToDevice, c->stream),
+               "upload job starts");
+    M.T = JobTable{slot.d_jobs, slot.d_start, (int)G.members.size()};
+  }
+  cuda_check(cudaStreamSynchronize(c->stream), "batch set-up");
+  float ms = 0.f;
+  if (c->batch_mode == PT_BATCH_PERSISTENT)
+    ms = render_groups_persistent(c, groups, targets != nullptr);
+  else
+    ms = render_groups_graph(c, jobs, n, groups, targets);
   // ---- results
   pt_stats tot;
   std::memset(&tot, 0, sizeof tot);

@@ -1587,6 +1587,7 @@ Context::Context(int dev) : device(dev) {
   halton = make_halton_tables();
   upload_halton_tables(halton, stream);
   upload_halton_tables_multi(halton, stream);
+  upload_halton_tables_persist(halton, stream);
   kernel_attributes(&kinfo);
   cfg.trace_blocks = num_sms * std::max(1, kinfo.trace_blocks_per_sm);
   cfg.shade_blocks = num_sms * std::max(1, kinfo.shade_blocks_per_sm);
@@ -1597,6 +1598,7 @@ Context::Context(int dev) : device(dev) {
   cfg.family_mask = 0x7f;
   const char *cap = std::getenv("PT_WAVE_PATHS");
   wave_cap = cap ? std::max(1024, std::atoi(cap)) : (1 << 24);
+  if (cap) batch_wave_cap = wave_cap;  // batched waves of the same size (tests of many-wave renders)
   // bound on one ray's traversal steps (scenes uploaded by this context);
   // exceeding it sets the device error flag, reported as PT_ERR_DEVICE
   const char *tc = std::getenv("PT_TRAVERSAL_CAP");

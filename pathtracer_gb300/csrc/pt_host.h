@@ -75,6 +75,11 @@ struct BatchSlot {
   size_t offsets_cap = 0;
   float *films = nullptr;       // the jobs' films (when no targets are given), concatenated
   size_t films_cap = 0;
+  // persistent form (PT_BATCH_PERSISTENT): the members' film pointers on the
+  // device and the group's grid barrier
+  float **d_films = nullptr;
+  int d_films_cap = 0;
+  void *d_barrier = nullptr;
   cudaStream_t stream[2] = {nullptr, nullptr};
   cudaEvent_t done[2] = {nullptr, nullptr};
   void ensure(int want_cap, int want_ln, int n_jobs, size_t n_offsets, size_t film_floats);
@@ -131,6 +136,7 @@ struct Context {
   Profiler prof;
   Batch batch;
   int batch_wave_cap = 1 << 22;  // paths per wave of each batched job
+  int batch_mode = PT_BATCH_GRAPH;  // pt_set_batch_mode
 
   explicit Context(int dev);
   ~Context();

@@ -261,113 +261,16 @@ __global__ void k_sort_scatter(Queues Q, int qsel) {
   }
 }
 
-// k_trace_shadow: the ShadowQueue's rays (vertex v, light sample ls; ray
-// r = v * LN + ls) through the BVH, any-hit, with the persistent warps of
-// k_trace_closest.  Each ray's visibility goes to Q.sh_vis; k_shadow_resolve
-// then adds the visible terms of every vertex to its path in a fixed order,
-// so the result does not depend on which warp traced which ray.
+// k_trace_shadow, k_shadow_resolve, k_film: their bodies are in pt_wave.cuh
+// (trace_shadow_body, shadow_resolve_body, film_body).
 template <bool CURVES>
 __global__ void __launch_bounds__(128) k_trace_shadow(SceneView S, Queues Q, int LN) {
   __shared__ int32_t stack[PT_STACK * 128];
-  const int n = Q.counts[2] * LN;
-  int *fetch = Q.counts + 3;
-  const int lane = threadIdx.x & 31;
-  int32_t *my_stack = stack + threadIdx.x;
-  TravRay R;
-  bool active = false, exhausted = false;
-  size_t slot = 0;
-  int rays = 0;
-  for (;;) {
-    unsigned idle = __ballot_sync(0xffffffffu, !active);
-    if (!exhausted && __popc(idle) >= PT_FETCH_IDLE_SHADOW) {
-      const int k = __popc(idle);
-      int base = 0;
-      if (lane == 0) base = atomicAdd(fetch, k);
-      base = __shfl_sync(0xffffffffu, base, 0);
-      if (base + k >= n) exhausted = true;
-      if (!active) {
-        const int r = base + __popc(idle & lanemask_lt());
-        if (r < n) {
-          const int v = r / LN, ls = r - v * LN;
-          slot = (size_t)ls * Q.cap + v;
-          float4 dd = ld4(Q.sh_d + slot);
-          if (dd.w >= 0.f) {
-            float4 so = ld4(Q.sh_o + v);
-            const float time = S.has_motion ? ld4(Q.sh_c + slot).w : 0.f;
-            trav_init(R, v3(so.x, so.y, so.z), v3(dd.x, dd.y, dd.z), 0.001f, dd.w, time);
-            active = true;
-            ++rays;
-          }
-        }
-      }
-      idle = __ballot_sync(0xffffffffu, !active);
-    }
-    if (idle == 0xffffffffu) {
-      if (exhausted) break;
-      continue;
-    }
-    if (active && trav_step<true, CURVES>(S, R, my_stack, blockDim.x, Q.err)) {
-      Q.sh_vis[slot] = R.found ? 0 : 1;
-      active = false;
-    }
-  }
-  warp_count(&Q.stats[3], rays);
+  trace_shadow_body<CURVES>(S, Q, LN, stack);
 }
-
-// k_shadow_resolve: per vertex, the visible NEE terms in light-sample order
-// added to the path's L.  Rays that were never traced (no contribution) have
-// a zero term, whatever their stale visibility byte says.
-__global__ void k_shadow_resolve(Queues Q, int LN) {
-  const int n = Q.counts[2];
-  for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
-    V3 acc = v3(0.f);
-    for (int ls = 0; ls < LN; ++ls) {
-      const size_t slot = (size_t)ls * Q.cap + v;
-      if (Q.sh_vis[slot]) {
-        float4 cc = ld4(Q.sh_c + slot);
-        acc += v3(cc.x, cc.y, cc.z);
-      }
-    }
-    if (acc.x != 0.f || acc.y != 0.f || acc.z != 0.f) {
-      const int path = __float_as_int(ld4(Q.sh_o + v).w);
-      float4 L = Q.L[path];
-      Q.L[path] = make_float4(L.x + acc.x, L.y + acc.y, L.z + acc.z, 0.f);
-    }
-  }
-}
-
-// k_film: per pixel, adds the wave's paths to the film one by one in sample
-// order.  Adding sample by sample (not a per-wave partial sum) makes the film
-// independent of how the samples are split into waves, so a job gives the
-// same bits alone, in a batch, or in a served mix.
+__global__ void k_shadow_resolve(Queues Q, int LN) { shadow_resolve_body(Q, LN); }
 __global__ void k_film(DeviceJob J, Queues Q, long long g0, int n, long long slot0, float *film) {
-  const long long npix = (long long)J.job.width * J.job.height;
-  const long long g1 = g0 + n;
-  const long long plane0 = g0 / npix, plane1 = (g1 - 1) / npix;
-  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < npix;
-       t += (long long)gridDim.x * blockDim.x) {
-    bool any = false;
-    float ax = 0.f, ay = 0.f, az = 0.f;
-    for (long long pl = plane0; pl <= plane1; ++pl) {
-      long long g = pl * npix + t;
-      if (g < g0 || g >= g1) continue;
-      if (!any) {
-        ax = film[3 * t];
-        ay = film[3 * t + 1];
-        az = film[3 * t + 2];
-        any = true;
-      }
-      float4 L = Q.L[g - g0 + slot0];
-      ax += L.x;
-      ay += L.y;
-      az += L.z;
-    }
-    if (any) {
-      film[3 * t] = ax;
-      film[3 * t + 1] = ay;
-      film[3 * t + 2] = az;
-    }
-  }
+  film_body(J, Q, g0, n, slot0, film);
 }
 
 // Serving: RMSE of a request's mean image estimated from its two

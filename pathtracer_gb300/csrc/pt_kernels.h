@@ -149,6 +149,15 @@ void launch_wave_multi(const SceneView &S, const MergedJobs &M, const Queues &Q,
                        const LaunchCfg &cfg, cudaStream_t st, Profiler *prof, cudaEvent_t film_after = nullptr,
                        cudaEvent_t film_done = nullptr);
 void upload_halton_tables_multi(const HaltonTables &T, cudaStream_t st);
+// Persistent form of a merged group (pt_kernels_persist.cu): every wave and
+// bounce of the group in one cooperative launch of `grid` blocks;
+// d_barrier: 16 zeroed bytes (the grid barrier; its third int is set when a
+// barrier wait ran out).  persistent_grid: the resident-block grid.
+void upload_halton_tables_persist(const HaltonTables &T, cudaStream_t st);
+int persistent_grid(bool curves, int num_sms);
+cudaError_t launch_group_persistent(const SceneView &S, const JobTable &T, const Queues &Q, float *const *d_films,
+                                    long long total, int wave, int LN, int bounces, void *d_barrier, int grid,
+                                    cudaStream_t st);
 void launch_tonemap(const float *film, int W, int H, float gamma, uint8_t *out, cudaStream_t st);
 void launch_gaussian_blur(const float *in, float *out, int W, int H, int K, const float *w, cudaStream_t st);
 

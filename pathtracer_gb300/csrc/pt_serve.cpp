@@ -118,6 +118,13 @@ int pt_render_batch(void *ctx, const pt_job_desc *jobs, int32_t n_jobs, float **
   }
 }
 
+int pt_set_batch_mode(void *ctx, int32_t mode) {
+  if (!ctx) return PT_ERR_INVALID;
+  if (mode != PT_BATCH_GRAPH && mode != PT_BATCH_PERSISTENT) return serr(ctx, PT_ERR_INVALID, "bad batch mode");
+  static_cast<Context *>(ctx)->batch_mode = mode;
+  return PT_OK;
+}
+
 int pt_autotune(void *ctx, const pt_job_desc *jobs, int32_t n_jobs, pt_tuning *out) {
   if (!ctx || !jobs || n_jobs <= 0) return serr(ctx, PT_ERR_INVALID, "bad autotune args");
   Context *c = static_cast<Context *>(ctx);

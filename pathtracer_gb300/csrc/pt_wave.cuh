@@ -243,7 +243,8 @@ __device__ __forceinline__ const DeviceJob &path_job(const DeviceJob &J, const J
 // Merged waves: the path's job by binary search of the jobs' first merged
 // indices (start[0] = 0 <= g < start[n]), stored for the later stages.
 template <bool MJ>
-__global__ void k_camera(DeviceJob J0, JobTable T, Queues Q, long long g0, int n) {
+__device__ __forceinline__ void camera_body(const DeviceJob &J0, const JobTable &T, const Queues &Q, long long g0,
+                                            int n) {
   for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x) {
     long long g = g0 + s;
     int jk = 0;
@@ -293,6 +294,10 @@ __global__ void k_camera(DeviceJob J0, JobTable T, Queues Q, long long g0, int n
     atomicAdd(&Q.stats[0], (unsigned long long)n);
   }
 }
+template <bool MJ>
+__global__ void k_camera(DeviceJob J0, JobTable T, Queues Q, long long g0, int n) {
+  camera_body<MJ>(J0, T, Q, g0, n);
+}
 
 // Persistent traversal warps with dynamic ray fetch (Aila and Laine,
 // "Understanding the efficiency of ray traversal on GPUs", HPG 2009, and the
@@ -318,9 +323,9 @@ __device__ __forceinline__ unsigned lanemask_lt() {
 // distance).  That is the same decision as comparing the distance with the
 // closest hit.
 template <bool MJ, bool CURVES>
-__global__ void __launch_bounds__(128) k_trace_closest(SceneView S, DeviceJob J, JobTable T, Queues Q, int qsel,
-                                                       int bounce, long long g0) {
-  __shared__ int32_t stack[PT_STACK * 128];
+__device__ __forceinline__ void trace_closest_body(const SceneView &S, const DeviceJob &J, const JobTable &T,
+                                                   const Queues &Q, int qsel, int bounce, long long g0,
+                                                   int32_t *stack) {
   const int n = Q.counts[qsel];
   int *fetch = Q.counts + 4;
   const int lane = threadIdx.x & 31;
@@ -375,6 +380,12 @@ __global__ void __launch_bounds__(128) k_trace_closest(SceneView S, DeviceJob J,
   }
   warp_count(&Q.stats[2], rays);
 }
+template <bool MJ, bool CURVES>
+__global__ void __launch_bounds__(128) k_trace_closest(SceneView S, DeviceJob J, JobTable T, Queues Q, int qsel,
+                                                       int bounce, long long g0) {
+  __shared__ int32_t stack[PT_STACK * 128];
+  trace_closest_body<MJ, CURVES>(S, J, T, Q, qsel, bounce, g0, stack);
+}
 
 // k_trace_pair: the closest-hit rays of bounce `bounce` (RayQueue qsel)
 // and the shadow rays of the bounce before it (ShadowQueue, LN light
@@ -387,9 +398,9 @@ __global__ void __launch_bounds__(128) k_trace_closest(SceneView S, DeviceJob J,
 // the shadow terms are still added (k_shadow_resolve) before the next shade
 // pass, in the same order.
 template <bool MJ, bool CURVES>
-__global__ void __launch_bounds__(128, 7) k_trace_pair(SceneView S, DeviceJob J, JobTable T, Queues Q, int qsel,
-                                                    int bounce, long long g0, int LN) {
-  __shared__ int32_t stack[PT_STACK * 128];
+__device__ __forceinline__ void trace_pair_body(const SceneView &S, const DeviceJob &J, const JobTable &T,
+                                                const Queues &Q, int qsel, int bounce, long long g0, int LN,
+                                                int32_t *stack) {
   const int nc = Q.counts[qsel];
   const int n = nc + Q.counts[2] * LN;
   int *fetch = Q.counts + 4;
@@ -463,6 +474,12 @@ __global__ void __launch_bounds__(128, 7) k_trace_pair(SceneView S, DeviceJob J,
   }
   warp_count(&Q.stats[2], crays);
   warp_count(&Q.stats[3], srays);
+}
+template <bool MJ, bool CURVES>
+__global__ void __launch_bounds__(128, 7) k_trace_pair(SceneView S, DeviceJob J, JobTable T, Queues Q, int qsel,
+                                                    int bounce, long long g0, int LN) {
+  __shared__ int32_t stack[PT_STACK * 128];
+  trace_pair_body<MJ, CURVES>(S, J, T, Q, qsel, bounce, g0, LN, stack);
 }
 
 // The hit point in its object's rest frame (texture coordinates of moving
@@ -707,8 +724,8 @@ __device__ __forceinline__ void next_event(const SceneView &S, const DeviceJob &
 constexpr int shade_min_blocks(int fam, bool) { return (fam == 5 || fam == 6 || fam < 0) ? 4 : 5; }
 
 template <int FAM, bool MJ>
-__global__ void __launch_bounds__(128, shade_min_blocks(FAM, MJ)) k_shade(SceneView S, DeviceJob J, JobTable T, Queues Q, int qsel, int bounce,
-                                               long long g0) {
+__device__ __forceinline__ void shade_body(const SceneView &S, const DeviceJob &J, const JobTable &T, const Queues &Q,
+                                           int qsel, int bounce, long long g0) {
   int lo = 0, hi = Q.counts[qsel];
   if (FAM >= 0) {
     lo = Q.seg[FAM];
@@ -906,6 +923,120 @@ __global__ void __launch_bounds__(128, shade_min_blocks(FAM, MJ)) k_shade(SceneV
     }
   }
   warp_count(&Q.stats[1], segs);
+}
+template <int FAM, bool MJ>
+__global__ void __launch_bounds__(128, shade_min_blocks(FAM, MJ)) k_shade(SceneView S, DeviceJob J, JobTable T, Queues Q, int qsel, int bounce,
+                                               long long g0) {
+  shade_body<FAM, MJ>(S, J, T, Q, qsel, bounce, g0);
+}
+
+// k_trace_shadow: the ShadowQueue's rays (vertex v, light sample ls; ray
+// r = v * LN + ls) through the BVH, any-hit, with the persistent warps of
+// k_trace_closest.  Each ray's visibility goes to Q.sh_vis; k_shadow_resolve
+// then adds the visible terms of every vertex to its path in a fixed order,
+// so the result does not depend on which warp traced which ray.
+template <bool CURVES>
+__device__ __forceinline__ void trace_shadow_body(const SceneView &S, const Queues &Q, int LN, int32_t *stack) {
+  const int n = Q.counts[2] * LN;
+  int *fetch = Q.counts + 3;
+  const int lane = threadIdx.x & 31;
+  int32_t *my_stack = stack + threadIdx.x;
+  TravRay R;
+  bool active = false, exhausted = false;
+  size_t slot = 0;
+  int rays = 0;
+  for (;;) {
+    unsigned idle = __ballot_sync(0xffffffffu, !active);
+    if (!exhausted && __popc(idle) >= PT_FETCH_IDLE_SHADOW) {
+      const int k = __popc(idle);
+      int base = 0;
+      if (lane == 0) base = atomicAdd(fetch, k);
+      base = __shfl_sync(0xffffffffu, base, 0);
+      if (base + k >= n) exhausted = true;
+      if (!active) {
+        const int r = base + __popc(idle & lanemask_lt());
+        if (r < n) {
+          const int v = r / LN, ls = r - v * LN;
+          slot = (size_t)ls * Q.cap + v;
+          float4 dd = ld4(Q.sh_d + slot);
+          if (dd.w >= 0.f) {
+            float4 so = ld4(Q.sh_o + v);
+            const float time = S.has_motion ? ld4(Q.sh_c + slot).w : 0.f;
+            trav_init(R, v3(so.x, so.y, so.z), v3(dd.x, dd.y, dd.z), 0.001f, dd.w, time);
+            active = true;
+            ++rays;
+          }
+        }
+      }
+      idle = __ballot_sync(0xffffffffu, !active);
+    }
+    if (idle == 0xffffffffu) {
+      if (exhausted) break;
+      continue;
+    }
+    if (active && trav_step<true, CURVES>(S, R, my_stack, blockDim.x, Q.err)) {
+      Q.sh_vis[slot] = R.found ? 0 : 1;
+      active = false;
+    }
+  }
+  warp_count(&Q.stats[3], rays);
+}
+
+// k_shadow_resolve: per vertex, the visible NEE terms in light-sample order
+// added to the path's L.  Rays that were never traced (no contribution) have
+// a zero term, whatever their stale visibility byte says.
+__device__ __forceinline__ void shadow_resolve_body(const Queues &Q, int LN) {
+  const int n = Q.counts[2];
+  for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
+    V3 acc = v3(0.f);
+    for (int ls = 0; ls < LN; ++ls) {
+      const size_t slot = (size_t)ls * Q.cap + v;
+      if (Q.sh_vis[slot]) {
+        float4 cc = ld4(Q.sh_c + slot);
+        acc += v3(cc.x, cc.y, cc.z);
+      }
+    }
+    if (acc.x != 0.f || acc.y != 0.f || acc.z != 0.f) {
+      const int path = __float_as_int(ld4(Q.sh_o + v).w);
+      float4 L = Q.L[path];
+      Q.L[path] = make_float4(L.x + acc.x, L.y + acc.y, L.z + acc.z, 0.f);
+    }
+  }
+}
+
+// k_film: per pixel, adds the wave's paths to the film one by one in sample
+// order.  Adding sample by sample (not a per-wave partial sum) makes the film
+// independent of how the samples are split into waves, so a job gives the
+// same bits alone, in a batch, or in a served mix.
+__device__ __forceinline__ void film_body(const DeviceJob &J, const Queues &Q, long long g0, int n, long long slot0,
+                                          float *film) {
+  const long long npix = (long long)J.job.width * J.job.height;
+  const long long g1 = g0 + n;
+  const long long plane0 = g0 / npix, plane1 = (g1 - 1) / npix;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < npix;
+       t += (long long)gridDim.x * blockDim.x) {
+    bool any = false;
+    float ax = 0.f, ay = 0.f, az = 0.f;
+    for (long long pl = plane0; pl <= plane1; ++pl) {
+      long long g = pl * npix + t;
+      if (g < g0 || g >= g1) continue;
+      if (!any) {
+        ax = film[3 * t];
+        ay = film[3 * t + 1];
+        az = film[3 * t + 2];
+        any = true;
+      }
+      float4 L = Q.L[g - g0 + slot0];
+      ax += L.x;
+      ay += L.y;
+      az += L.z;
+    }
+    if (any) {
+      film[3 * t] = ax;
+      film[3 * t + 1] = ay;
+      film[3 * t + 2] = az;
+    }
+  }
 }
 
 static inline int grid_for(long long n, int block, int max_blocks) {

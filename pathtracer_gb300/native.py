@@ -29,6 +29,7 @@ SAMPLER_HALTON_NONE, SAMPLER_HALTON_PERMUTE, SAMPLER_HALTON_OWEN, SAMPLER_STRATI
 ENV_UNIFORM, ENV_ALIAS = 0, 1
 BVH_BUILD_HOST, BVH_BUILD_DEVICE, BVH_BUILD_SAH = 0, 1, 2
 SERVE_FAIR, SERVE_SRPT = 0, 1
+BATCH_GRAPH, BATCH_PERSISTENT = 0, 1
 
 # exported symbols of the C-ABI, in header order
 EXPORTS = [
@@ -36,7 +37,7 @@ EXPORTS = [
     "pt_bvh_build", "pt_set_bvh_builder", "pt_bvh_build_device", "pt_bvh_build_sah", "pt_obj_load", "pt_obj_free", "pt_load_image", "pt_free_image", "pt_scene_info", "pt_render", "pt_render_device", "pt_render_device_noalloc", "pt_ray_color",
     "pt_profile_begin",
     "pt_profile_end", "pt_tonemap", "pt_gaussian_blur", "pt_write_png", "pt_sampler_eval", "pt_sample_eval", "pt_trace_closest",
-    "pt_trace_any", "pt_intersect", "pt_light_sample", "pt_bsdf_eval", "pt_bsdf_sample", "pt_render_batch", "pt_autotune", "pt_server_create",
+    "pt_trace_any", "pt_intersect", "pt_light_sample", "pt_bsdf_eval", "pt_bsdf_sample", "pt_render_batch", "pt_set_batch_mode", "pt_autotune", "pt_server_create",
     "pt_server_destroy", "pt_submit", "pt_server_step", "pt_poll", "pt_cancel", "pt_server_set_policy",
     "pt_request_times",
 ]
@@ -198,6 +199,7 @@ def load() -> C.CDLL:
         "pt_bsdf_sample": [vp, C.POINTER(MaterialDesc), C.c_int32, f32p, f32p, u8p, f32p, f32p, u8p, f32p,
                            f32p, f32p, u32p],
         "pt_render_batch": [vp, C.POINTER(JobDesc), C.c_int32, C.POINTER(f32p), C.POINTER(Stats)],
+        "pt_set_batch_mode": [vp, C.c_int32],
         "pt_autotune": [vp, C.POINTER(JobDesc), C.c_int32, C.POINTER(Tuning)],
         "pt_server_create": [vp, C.c_int64, C.c_int32, C.POINTER(vp)],
         "pt_server_destroy": [vp],
@@ -496,6 +498,11 @@ class Renderer:
         st = Stats()
         self._check(self.lib.pt_render_batch(self.ctx, arr, n, ptrs, C.byref(st)))
         return (films, st) if stats else films
+
+    def set_batch_mode(self, mode: int):
+        """pt_set_batch_mode: BATCH_GRAPH (per-stage kernels in one graph) or
+        BATCH_PERSISTENT (one cooperative launch per scene group)."""
+        self._check(self.lib.pt_set_batch_mode(self.ctx, mode))
 
     def autotune(self, jobs) -> dict:
         n = len(jobs)

@@ -69,6 +69,7 @@ int main() {
   std::vector<Ray> rays;
   for (int i = 0; i < 64; ++i)
     rays.push_back(Ray(vec3(0.5f, 0.5f, -1.4f), vec3(-0.2f + 0.4f * (i % 8) / 7.f, -0.2f + 0.4f * (i / 8) / 7.f, 1.f)));
+  for (const Ray &r : rays) put(r.getDirection());  // the rays as this program rounded them
   for (const vec3 &c : getRayColor(ctx, sid, rays, 8, 101)) put(c);
   pt_scene_release(ctx, sid);
   pt_destroy(ctx);

@@ -83,10 +83,9 @@ def test_cpp_surface_matches_c_abi(tmp_path, renderer):
         assert np.float32(rows[k + 4][0]) == r["pdf"][0] and np.float32(rows[k + 4][1]) == np.float32(r["area"])
         k += 5
     cam = S.camera((0.5, 0.5, -1.4), (0.0, 0.0, 1.0), 40.0, 1.0)
-    i = np.arange(64)
-    d = np.stack([-0.2 + 0.4 * (i % 8) / 7.0, -0.2 + 0.4 * (i // 8) / 7.0, np.ones(64)], 1)
-    rays = np.concatenate([np.tile([0.5, 0.5, -1.4], (64, 1)), d], 1).astype(np.float32)
+    d = np.array(rows[k:k + 64], np.float32)  # the directions the program built
+    rays = np.concatenate([np.tile(np.float32([0.5, 0.5, -1.4]), (64, 1)), d], 1).astype(np.float32)
     want = renderer.ray_color(N.job_desc(sid, cam, 1, 1, 1, 1, 8), rays, first_index=101)
-    got = np.array(rows[k:k + 64], np.float32)
+    got = np.array(rows[k + 64:k + 128], np.float32)
     assert np.array_equal(got, want)
     renderer.release(sid)

@@ -95,6 +95,47 @@ def test_autotune_picks_a_candidate(scenes):
     r.close()
 
 
+def test_batch_persistent_equals_graph(renderer, scenes):
+    """PT_BATCH_PERSISTENT (one cooperative launch per scene group, all waves
+    and bounces, grid barriers between the stages) renders the same samples
+    as the per-stage graph form: the same path / vertex / ray counts and the
+    same films up to FP32 rounding of the generically compiled shading (the
+    graph form shades per material family), across several waves."""
+    jobs = _jobs(scenes)
+    films_g, st_g = renderer.render_batch(jobs, stats=True)
+    renderer.set_batch_mode(N.BATCH_PERSISTENT)
+    try:
+        films_p, st_p = renderer.render_batch(jobs, stats=True)
+        again = renderer.render_batch(jobs)
+    finally:
+        renderer.set_batch_mode(N.BATCH_GRAPH)
+    assert st_p.paths == st_g.paths
+    for a, b, c in zip(films_p, films_g, again):
+        assert np.isfinite(a).all()
+        assert np.array_equal(a, c)  # deterministic
+        close = np.isclose(a, b, rtol=1e-4, atol=1e-6).all(-1)
+        assert close.mean() > 0.99, close.mean()
+    with pytest.raises(N.PtError):
+        renderer.set_batch_mode(7)
+
+
+def test_batch_persistent_many_waves(monkeypatch):
+    # tiny waves: the persistent kernel loops over many waves of each group
+    monkeypatch.setenv("PT_WAVE_PATHS", "4096")
+    small = N.Renderer(0)
+    try:
+        sc, cam = S.cornell_icosphere(2)
+        sid = small.upload(sc)
+        job = N.job_desc(sid, cam, 32, 24, 4, 4, 6, seed=9, estimator=N.EST_NEE_MIS)
+        ref = small.render(job)
+        small.set_batch_mode(N.BATCH_PERSISTENT)
+        films = small.render_batch([job, job])
+        for f in films:
+            assert np.isclose(f, ref, rtol=1e-4, atol=1e-6).all(-1).mean() > 0.99
+    finally:
+        small.close()
+
+
 def _serve_until_done(srv, ids, max_steps=10000):
     for _ in range(max_steps):
         if srv.step() == 0:
