@@ -322,6 +322,19 @@ def run_batched(r, scenes, n_jobs: int, seed: int = 11, res=(64, 1024), spp=(4, 
     t0 = time.perf_counter()
     films_b, st = r.render_batch(jobs, stats=True)
     t_batch = time.perf_counter() - t0
+    # the same batch as ONE persistent cooperative launch per scene group
+    from pathtracer_gb300 import native as N
+    r.set_batch_mode(N.BATCH_PERSISTENT)
+    try:
+        r.render_batch(jobs)
+        t0 = time.perf_counter()
+        films_q, st_q = r.render_batch(jobs, stats=True)
+        t_pers = time.perf_counter() - t0
+    finally:
+        r.set_batch_mode(N.BATCH_GRAPH)
+    rel_q = 0.0
+    for a, b in zip(films_q, films_b):
+        rel_q = max(rel_q, float(np.abs(a - b).max() / max(1e-12, float(np.abs(b).max()))))
     # plain wavefront, one job after the other (warm the context's queues first)
     r.render(jobs[0])
     t0 = time.perf_counter()
@@ -336,6 +349,11 @@ def run_batched(r, scenes, n_jobs: int, seed: int = 11, res=(64, 1024), spp=(4, 
         "jobs": n_jobs, "paths": paths, "paths_per_s": paths / t_batch, "plain_paths_per_s": paths / t_plain,
         "speedup_vs_plain": t_plain / t_batch, "batch_s": t_batch, "plain_s": t_plain,
         "graph_device_ms": st.ms, "max_rel_film_diff_vs_plain": rel,
+        "persistent": {"paths_per_s": paths / t_pers, "speedup_vs_plain": t_plain / t_pers,
+                       "vs_graph": t_batch / t_pers, "device_ms": st_q.ms,
+                       "max_rel_film_diff_vs_graph": rel_q,
+                       "form": "one cooperative launch per scene group: every wave and bounce, grid barriers "
+                               "between stages, generic (unsorted) shading"},
         "equal_rmse": "same samples in both arms: identical images up to FP32 summation order",
         "mix": f"{n_jobs} jobs over cornell/rough_glass/divergence with per-object motion; square resolution "
                f"log-uniform {res[0]}..{res[1]} (median {sides[len(sides) // 2]}), spp U{{{spp[0]}..{spp[1]}}}, "

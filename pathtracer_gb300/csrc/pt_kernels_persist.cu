@@ -19,7 +19,10 @@
 // and every block returns at its next barrier, so a fault ends the kernel
 // with an error the host reports, never a hang.  The cooperative launch
 // guarantees that every block of the grid is resident, which the barrier
-// needs.
+// needs.  Stages read queue records that earlier stages of the same kernel
+// wrote, so they are read from L2 (PT_QUEUE_LOADS_COHERENT), not through the
+// read-only cache the per-stage kernels use.
+#define PT_QUEUE_LOADS_COHERENT
 #include "pt_wave.cuh"
 
 namespace pt {
@@ -72,6 +75,8 @@ __device__ __forceinline__ bool grid_sync(GridBarrier *b, Last last) {
     }
   }
   __syncthreads();
+  // every thread orders its later loads after the other blocks' stores
+  __threadfence();
   return ok != 0;
 }
 

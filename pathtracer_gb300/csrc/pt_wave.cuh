@@ -22,7 +22,16 @@ namespace pt {
 static __constant__ HaltonTables c_halton;
 
 // ---------------------------------------------------------------- helpers
+// Queue records are read through the read-only data cache (ld.global.nc):
+// a per-stage kernel never reads records it wrote itself.  The persistent
+// form runs all stages in one kernel, so its later stages read what earlier
+// ones wrote; it defines PT_QUEUE_LOADS_COHERENT and reads them from L2
+// (ld.global.cg).
+#ifdef PT_QUEUE_LOADS_COHERENT
+__device__ __forceinline__ float4 ld4(const float4 *p) { return __ldcg(p); }
+#else
 __device__ __forceinline__ float4 ld4(const float4 *p) { return __ldg(p); }
+#endif
 
 // Warp-aggregated slot allocation in a queue counter.
 __device__ __forceinline__ int warp_alloc(int *counter, bool want) {
