@@ -1497,7 +1497,18 @@ std::unique_ptr<Scene> build_scene(const pt_scene_desc *d_in, cudaStream_t st, b
 
   // upload
   auto up = [&](const auto &v) { return device ? dupload(v, S->owned, st) : nullptr; };
-  S->nodes = up(out.nodes);
+  {
+    // the device copy carries each child's traversal reference in place of
+    // its count (the node visit then needs neither the child row nor any
+    // decoding); the host tree and its hash keep (child, count)
+    std::vector<Bvh4Node> dev = out.nodes;
+    for (Bvh4Node &N : dev)
+      for (int k = 0; k < 4; ++k) {
+        if (N.count[k] > 8) fail(PT_ERR_INVALID, "leaf of more than 8 items");
+        N.count[k] = trav_ref(N.child[k], N.count[k]);
+      }
+    S->nodes = up(dev);
+  }
   S->items = up(items);
   S->shade = up(shade);
   S->materials = up(mats);

@@ -28,9 +28,22 @@ struct alignas(128) Bvh4Node {
   float lo_y[4], hi_y[4];
   float lo_z[4], hi_z[4];
   int32_t child[4];  // internal: node index; leaf: first item index
-  int32_t count[4];  // internal: 0; leaf: number of items; empty slot: -1
+  int32_t count[4];  // internal: 0; leaf: number of items; empty slot: -1 --
+                     // in the uploaded copy: each child's traversal reference
+                     // (trav_ref), which the node visit reads as is
 };
 static_assert(sizeof(Bvh4Node) == 128, "BVH4 node must be one 128-byte line");
+
+// Traversal references (a node's children on the device, the stack): a node
+// index (>= 0; PT_INST_BIT: entering a moving object), a leaf
+// ~(first_item << 3 | count - 1) (count <= 8), PT_FRAME_END (stack only) or
+// PT_REF_EMPTY (an empty child slot; as the next reference: nothing pending).
+#define PT_REF_EMPTY ((int32_t)0x80000001)
+PT_HD int32_t leaf_ref(int32_t first, int32_t count) { return ~((first << 3) | (count - 1)); }
+// A child's reference from its (child, count) pair.
+PT_HD int32_t trav_ref(int32_t child, int32_t count) {
+  return count < 0 ? PT_REF_EMPTY : count == 0 ? child : leaf_ref(child, count);
+}
 
 // Leaf item (48 B).  a.w / b.w carry the primitive id and the item type as
 // integer bits.

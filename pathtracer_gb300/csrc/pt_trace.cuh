@@ -24,9 +24,6 @@ struct HitRec {
   float u, v;
 };
 
-// Leaf references on the stack: ~(first_item << 3 | count - 1), count <= 8.
-PT_HD int32_t leaf_ref(int32_t first, int32_t count) { return ~((first << 3) | (count - 1)); }
-
 // Moller-Trumbore exactly as hitTriangle orders it.
 __device__ __forceinline__ bool hit_triangle(const Item &it, V3 o, V3 d, float tmin, float tmax,
                                              float &t_out, float &u_out, float &v_out) {
@@ -249,9 +246,6 @@ struct TravRay {
   HitRec hit;
 };
 
-// The stack is empty: the ray is finished once no leaf is pending.
-#define PT_REF_EMPTY ((int32_t)0x80000001)
-
 __device__ __forceinline__ bool ref_is_node(int32_t r) { return r >= 0 || r == PT_FRAME_END; }
 __device__ __forceinline__ bool ref_is_leaf(int32_t r) { return r < 0 && r != PT_FRAME_END && r != PT_REF_EMPTY; }
 
@@ -314,12 +308,13 @@ __device__ __forceinline__ bool trav_node(const SceneView &S, TravRay &R, int32_
   const int sx = signbit(R.inv.x) ? 1 : 0, sy = signbit(R.inv.y) ? 1 : 0, sz = signbit(R.inv.z) ? 1 : 0;
   float4 nx = __ldg(np + sx), fx = __ldg(np + (sx ^ 1)), ny = __ldg(np + 2 + sy), fy = __ldg(np + 2 + (sy ^ 1));
   float4 nz = __ldg(np + 4 + sz), fz = __ldg(np + 4 + (sz ^ 1));
-  int4 ch = __ldg(reinterpret_cast<const int4 *>(np + 6));
-  int4 cn = __ldg(reinterpret_cast<const int4 *>(np + 7));
+  // the children's traversal references, ready made by the upload (node
+  // index, leaf reference, or PT_REF_EMPTY for an empty slot)
+  const int4 rf = __ldg(reinterpret_cast<const int4 *>(np + 7));
   const float nxa[4] = {nx.x, nx.y, nx.z, nx.w}, fxa[4] = {fx.x, fx.y, fx.z, fx.w};
   const float nya[4] = {ny.x, ny.y, ny.z, ny.w}, fya[4] = {fy.x, fy.y, fy.z, fy.w};
   const float nza[4] = {nz.x, nz.y, nz.z, nz.w}, fza[4] = {fz.x, fz.y, fz.z, fz.w};
-  const int cha[4] = {ch.x, ch.y, ch.z, ch.w}, cna[4] = {cn.x, cn.y, cn.z, cn.w};
+  const int rfa[4] = {rf.x, rf.y, rf.z, rf.w};
   const V3 inv = R.inv, oi = R.oi;
   const float tmin = R.tmin, tmax = R.tmax;
   // entry distance per child (+inf when missed or empty), kept in registers;
@@ -332,8 +327,8 @@ __device__ __forceinline__ bool trav_node(const SceneView &S, TravRay &R, int32_
                      fmaxf(fmaf(nza[c], inv.z, oi.z), tmin));                                        \
     float tf = fminf(fminf(fmaf(fxa[c], inv.x, oi.x), fmaf(fya[c], inv.y, oi.y)),                  \
                      fminf(fmaf(fza[c], inv.z, oi.z), tmax));                                        \
-    dd = (cna[c] >= 0 && tn <= tf) ? tn : INFINITY;                                                 \
-    rr = cna[c] == 0 ? cha[c] : leaf_ref(cha[c], max(cna[c], 1));                                   \
+    dd = (rfa[c] != PT_REF_EMPTY && tn <= tf) ? tn : INFINITY;                                      \
+    rr = rfa[c];                                                                                     \
   }
   PT_CHILD(0, d0, r0)
   PT_CHILD(1, d1, r1)
