@@ -192,42 +192,38 @@ __device__ __forceinline__ V3 moved_origin(const SceneView &S, uint32_t motion, 
   return v3(xsub(o.x, xmul(v.x, time)), xsub(o.y, xmul(v.y, time)), xsub(o.z, xmul(v.z, time)));
 }
 
+// Tests leaf item `idx` (a whole leaf is its items in order); for ANY
+// returns true on a hit in [tmin, tmax], for closest hit records the hit and
+// shrinks tmax (acceptance is inclusive: of equal-t items the later wins).
 // CURVES = false compiles the curve test out (curve items then never hit):
 // the closest-hit kernel of a scene without curves keeps 8 fewer registers.
 template <bool ANY, bool CURVES = true>
-__device__ __forceinline__ bool test_leaf(const SceneView &S, int32_t ref, V3 o_w, V3 d, V3 dn,
-                                          float tmin, float &tmax, HitRec &hit, float time) {
-  const int32_t code = ~ref;
-  const int first = code >> 3, count = (code & 7) + 1;
-  bool any = false;
-  for (int k = 0; k < count; ++k) {
-    Item it = load_item(S.items, first + k);
-    const int type = (int)f2u(it.b[3]);
-    const uint32_t motion = f2u(it.c[3]);
-    const V3 o = motion ? moved_origin(S, motion, o_w, time) : o_w;
-    float t, u = 0.f, v = 0.f;
-    bool h;
-    if (type == ITEM_TRI)
-      h = hit_triangle(it, o, d, tmin, tmax, t, u, v);
-    else if (type == ITEM_QUAD)
-      h = hit_quad(it, o, dn, tmin, tmax, t);
-    else if (type == ITEM_SPHERE)
-      h = hit_sphere(it, o, dn, tmin, tmax, t);
-    else if (CURVES)
-      h = hit_curve(S.curves + 4 * (size_t)f2u(it.a[0]), o, d, tmin, tmax, t, u, v);
-    else
-      h = false;
-    if (h) {
-      if (ANY) return true;
-      tmax = t;
-      hit.t = t;
-      hit.prim = (int32_t)f2u(it.a[3]);
-      hit.u = u;
-      hit.v = v;
-      any = true;
-    }
+__device__ __forceinline__ bool test_item(const SceneView &S, int idx, V3 o_w, V3 d, V3 dn, float tmin,
+                                          float &tmax, HitRec &hit, float time) {
+  Item it = load_item(S.items, idx);
+  const int type = (int)f2u(it.b[3]);
+  const uint32_t motion = f2u(it.c[3]);
+  const V3 o = motion ? moved_origin(S, motion, o_w, time) : o_w;
+  float t, u = 0.f, v = 0.f;
+  bool h;
+  if (type == ITEM_TRI)
+    h = hit_triangle(it, o, d, tmin, tmax, t, u, v);
+  else if (type == ITEM_QUAD)
+    h = hit_quad(it, o, dn, tmin, tmax, t);
+  else if (type == ITEM_SPHERE)
+    h = hit_sphere(it, o, dn, tmin, tmax, t);
+  else if (CURVES)
+    h = hit_curve(S.curves + 4 * (size_t)f2u(it.a[0]), o, d, tmin, tmax, t, u, v);
+  else
+    h = false;
+  if (h && !ANY) {
+    tmax = t;
+    hit.t = t;
+    hit.prim = (int32_t)f2u(it.a[3]);
+    hit.u = u;
+    hit.v = v;
   }
-  return any;
+  return h;
 }
 
 // Traversal state of one ray.  The walk is a sequence of node visits and
@@ -401,13 +397,13 @@ __device__ __forceinline__ bool trav_step(const SceneView &S, TravRay &R, int32_
   if (R.ref == PT_REF_EMPTY) return true;
   if (ref_is_node(R.ref)) return !trav_node<ANY>(S, R, stack, stride, err);
   // one leaf item per step, the leaf's items in order
-  const int32_t code = ~R.ref;
-  const int32_t first = code >> 3, count = (code & 7) + 1;
-  if (test_leaf<ANY, CURVES>(S, leaf_ref(first, 1), R.o, R.d, R.dn, R.tmin, R.tmax, R.hit, R.time)) {
+  const int32_t code = ~R.ref;  // first_item << 3 | count - 1
+  if (test_item<ANY, CURVES>(S, code >> 3, R.o, R.d, R.dn, R.tmin, R.tmax, R.hit, R.time)) {
     R.found = true;
     if (ANY) return true;
   }
-  R.ref = count > 1 ? leaf_ref(first + 1, count - 1) : trav_pop(R, stack, stride);
+  // the rest of the leaf, (first + 1, count - 1), is ~(code + 7) = ref - 7
+  R.ref = (code & 7) ? R.ref - 7 : trav_pop(R, stack, stride);
   return false;
 }
 
