@@ -84,16 +84,38 @@ struct NoReset {
   __device__ void operator()() const {}
 };
 
+// The stages as separately compiled functions: each gets its own register
+// allocation (the traversal does not inherit the shading's register pressure
+// and spills), and reads the kernel's parameters in place (__grid_constant__).
+template <bool CURVES>
+__device__ __noinline__ void st_trace(const SceneView &S, const DeviceJob &none, const JobTable &T, const Queues &Q,
+                                      int qsel, int b, long long g0, int LN, int32_t *stack) {
+  if (b > 0)
+    trace_pair_body<true, CURVES>(S, none, T, Q, qsel, b, g0, LN, stack);
+  else
+    trace_closest_body<true, CURVES>(S, none, T, Q, qsel, b, g0, stack);
+}
+__device__ __noinline__ void st_shade(const SceneView &S, const DeviceJob &none, const JobTable &T, const Queues &Q,
+                                      int qsel, int b, long long g0) {
+  shade_body<-1, true>(S, none, T, Q, qsel, b, g0);
+}
+template <bool CURVES>
+__device__ __noinline__ void st_shadow(const SceneView &S, const Queues &Q, int LN, int32_t *stack) {
+  trace_shadow_body<CURVES>(S, Q, LN, stack);
+}
+
 // The whole group: for each wave of `wave` paths over [0, total), camera ->
 // per bounce (trace [+ previous shadow rays] -> resolve -> shade) -> last
 // shadow rays -> resolve -> films.
 template <bool CURVES>
 __global__ void __launch_bounds__(PT_PERSIST_THREADS, PT_PERSIST_MIN_BLOCKS)
-    k_group_persistent(SceneView S, JobTable T, Queues Q, float *const *films, long long total, int wave, int LN,
+    k_group_persistent(const __grid_constant__ SceneView S, const __grid_constant__ JobTable T,
+                       const __grid_constant__ Queues Q, float *const *films, long long total, int wave, int LN,
                        int bounces, GridBarrier *bar) {
   __shared__ int32_t stack[PT_STACK * PT_PERSIST_THREADS];
-  DeviceJob none;
-  memset(&none, 0, sizeof none);
+  __shared__ DeviceJob none;  // unused by merged waves (each path's job comes from T)
+  if (threadIdx.x == 0) memset(&none, 0, sizeof none);
+  __syncthreads();
   int *cnt = Q.counts;
   for (long long g0 = 0; g0 < total; g0 += wave) {
     const int n = (int)min((long long)wave, total - g0);
@@ -101,21 +123,18 @@ __global__ void __launch_bounds__(PT_PERSIST_THREADS, PT_PERSIST_MIN_BLOCKS)
     if (!grid_sync(bar, [=] { cnt[1] = 0; cnt[2] = 0; cnt[3] = 0; cnt[4] = 0; })) return;
     int qsel = 0;
     for (int b = 0; b < bounces; ++b) {
-      if (b > 0)
-        trace_pair_body<true, CURVES>(S, none, T, Q, qsel, b, g0, LN, stack);
-      else
-        trace_closest_body<true, CURVES>(S, none, T, Q, qsel, b, g0, stack);
+      st_trace<CURVES>(S, none, T, Q, qsel, b, g0, LN, stack);
       const int nq = qsel ^ 1;
       if (!grid_sync(bar, [=] { cnt[nq] = 0; cnt[4] = 0; })) return;
       if (b > 0) {
         shadow_resolve_body(Q, LN);
         if (!grid_sync(bar, [=] { cnt[2] = 0; cnt[3] = 0; })) return;
       }
-      shade_body<-1, true>(S, none, T, Q, qsel, b, g0);
+      st_shade(S, none, T, Q, qsel, b, g0);
       if (!grid_sync(bar, NoReset())) return;
       qsel = nq;
     }
-    trace_shadow_body<CURVES>(S, Q, LN, stack);
+    st_shadow<CURVES>(S, Q, LN, stack);
     if (!grid_sync(bar, NoReset())) return;
     shadow_resolve_body(Q, LN);
     if (!grid_sync(bar, NoReset())) return;
