@@ -448,14 +448,17 @@ def run_served(r, scenes, big, seconds: float, rate: float, seed: int = 12, pass
 
 
 def run_served_config4(r, scenes, big, seconds: float, rate: float, drain: float, seed: int = 14,
-                       pass_paths: int = 1 << 26, max_queue: int = 512, max_slots: int = 256):
+                       pass_paths: int = 1 << 27, max_queue: int = 512, max_slots: int = 256,
+                       request_pass_paths: int = 1 << 22):
     """The served workload as specified for serving: Poisson arrivals at
     `rate` req/s for `seconds` over the 4 resident scenes (Cornell, rough glass
     1.3 M tris, material divergence, rough glass 5.2 M tris), each request a
     seeded camera, square resolution log-uniform 128..2048, an spp cap
     U{16..1024} and a target RMSE of 0.02 (whichever first).  Admission by
     free HBM and slots, SRPT scheduling (pt_server_set_policy: the least
-    remaining work first, `pass_paths` per pass), a bounded queue (PT_ERR_BUSY
+    remaining work first, `pass_paths` per pass; each request's chunk per pass
+    is enough samples for about `request_pass_paths` paths, at least 16 spp),
+    a bounded queue (PT_ERR_BUSY
     beyond `max_queue` waiting requests: refused).  The loop runs until the
     arrivals end plus `drain` seconds; requests still unfinished then are
     cancelled and counted.  This mix asks for far more paths than one GPU
@@ -494,7 +497,8 @@ def run_served_config4(r, scenes, big, seconds: float, rate: float, drain: float
         now = time.perf_counter() - t0
         while k < len(reqs) and reqs[k][0] <= now:
             try:
-                rid = srv.submit(reqs[k][1], target_rmse=0.02, spp_cap=reqs[k][2], spp_per_pass=16)
+                rid = srv.submit(reqs[k][1], target_rmse=0.02, spp_cap=reqs[k][2], spp_per_pass=16,
+                                 paths_per_pass=request_pass_paths)
                 ids[rid] = k
                 outstanding.add(rid)
             except N.PtError as e:
@@ -549,7 +553,8 @@ def run_served_config4(r, scenes, big, seconds: float, rate: float, drain: float
         "passes": passes, "wall_s": wall,
         "mix": "4 resident scenes (cornell, rough_glass 1.3M tris, divergence, rough_glass 5.2M tris) with "
                "motion; res log-uniform 128..2048, spp cap U{16..1024}, target RMSE 0.02, NEE+MIS; SRPT "
-               f"with {pass_paths} paths per pass, queue bound {max_queue}, {max_slots} slots",
+               f"with {pass_paths} paths per pass, ~{request_pass_paths} paths (>= 16 spp) per request per pass, "
+               f"queue bound {max_queue}, {max_slots} slots",
     }
 
 
