@@ -55,10 +55,10 @@ import numpy as np  # noqa: E402
 PEAKS = REPO / "MEASURED_PEAKS.json"
 FALLBACK_HBM_GBS = 6800.0
 # ncu DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of all
-# traversal launches (closest, paired, shadow) of one step of 16 spp of every
-# pixel, per (workload, estimator); from a one-pass ncu capture of the same
-# bench command
-NCU_TRAVERSAL_BYTES_PER_STEP = {("rough_glass", 1): 6.9185e9}
+# traversal-stage launches (closest, paired, shadow and the shadow resolve) of
+# one step of 16 spp of every pixel, per (workload, estimator); from a
+# one-pass ncu capture of the same bench command
+NCU_TRAVERSAL_BYTES_PER_STEP = {("rough_glass", 0): 8.850e9}
 # Algorithmic queue bytes per unit, by stage: the records each stage must
 # read or write in this layout, with the survey model's 192 B per path vertex,
 # 88 B per shadow ray (44 written by shade, 44 read by the traversal) and FP32
@@ -752,8 +752,9 @@ def run_ours(args, rank, world, local_rank):
                      "peak_source": peak_src,
                      "traffic": (ncu_bytes if ncu_bytes and dom == "traversal" else None),
                      "traffic_unit": "bytes per step: ncu dram__bytes_read.sum + dram__bytes_write.sum summed over "
-                                     "all traversal launches of one step (achieved is per step too: the stage's "
-                                     "algorithmic bytes per step over its time per step)",
+                                     "the traversal stage's launches of one step (closest, paired, shadow, resolve; "
+                                     "achieved is per step too: the stage's algorithmic bytes per step over its "
+                                     "time per step)",
                      "algorithmic_bytes_per_step": stages[dom]["bytes"] / args.steps,
                      "algorithmic_bytes_note": "; ".join(f"{u} B per {c}" for c, u in STAGE_UNIT_BYTES[dom].items()),
                      "launches_per_step": trav_launches / args.steps if dom == "traversal" else None,
