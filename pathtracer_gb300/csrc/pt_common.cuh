@@ -161,15 +161,21 @@ PT_HD uint64_t mix_bits(uint64_t v) {
   return v;
 }
 
-// gl::permutationElement (utils/utility.hpp:434-464): Kensler's hashed
-// permutation of [0, l) ("Correlated Multi-Jittered Sampling", 2013).
-PT_HD uint32_t permutation_element(uint32_t i, uint32_t l, uint32_t p) {
+// l - 1 with every bit below its highest set bit set.
+PT_HD uint32_t fill_mask(uint32_t l) {
   uint32_t w = l - 1;
   w |= w >> 1;
   w |= w >> 2;
   w |= w >> 4;
   w |= w >> 8;
   w |= w >> 16;
+  return w;
+}
+
+// The rejection loop of gl::permutationElement (utils/utility.hpp:434-464):
+// Kensler's hashed permutation of [0, l) ("Correlated Multi-Jittered
+// Sampling", 2013) before its final offset; w = fill_mask(l).
+PT_HD uint32_t permutation_index(uint32_t i, uint32_t l, uint32_t w, uint32_t p) {
   do {
     i ^= p;
     i *= 0xe170893du;
@@ -190,7 +196,12 @@ PT_HD uint32_t permutation_element(uint32_t i, uint32_t l, uint32_t p) {
     i &= w;
     i ^= i >> 5;
   } while (i >= l);
-  return (i + p) % l;
+  return i;
+}
+
+// gl::permutationElement: the permuted index, offset by p modulo l.
+PT_HD uint32_t permutation_element(uint32_t i, uint32_t l, uint32_t p) {
+  return (permutation_index(i, l, fill_mask(l), p) + p) % l;
 }
 
 // Counter-based uniform draws for everything the reference takes from
@@ -222,7 +233,50 @@ struct HaltonTables {
   int32_t ndigits[PT_PRIME_COUNT];    // digits visited by the double loop test
   double inv_base_m[PT_PRIME_COUNT];  // invBase^ndigits, accumulated as the loop does
   int32_t perm_offset[PT_PRIME_COUNT];// into perm[] (PermuteDigits tables)
+  // a / prime as a multiply-high and shifts (division by an invariant
+  // integer, Granlund and Montgomery, PLDI 1994): magic 0 = power of two
+  uint32_t div_magic[PT_PRIME_COUNT];
+  int32_t div_shift[PT_PRIME_COUNT];  // shift; bit 6 set: the 33-bit (add) form
 };
+
+// The magic multiplier and shift of a / d for every 32-bit a (d >= 2):
+// m = 2^(32 + floor(log2 d)) / d + 1 when that leaves an error below
+// 2^floor(log2 d), else the 33-bit multiplier whose top bit the add form of
+// div_prime supplies.
+inline void div_invariant(uint32_t d, uint32_t &magic, int32_t &shift) {
+  int l = 0;
+  while ((d >> (l + 1)) != 0) ++l;  // floor(log2 d)
+  if ((d & (d - 1)) == 0) {
+    magic = 0;
+    shift = l;
+    return;
+  }
+  const uint64_t num = (uint64_t)1 << (32 + l);
+  uint32_t m = (uint32_t)(num / d), rem = (uint32_t)(num % d);
+  if (d - rem < (1u << l)) {
+    shift = l;
+  } else {
+    m += m;
+    const uint32_t twice = rem + rem;
+    if (twice >= d || twice < rem) m += 1;
+    shift = l | 64;
+  }
+  magic = m + 1;
+}
+
+// a / T.prime[bi] for every 32-bit a.
+PT_HD uint32_t div_prime(const HaltonTables &T, int bi, uint32_t a) {
+  const uint32_t m = T.div_magic[bi];
+  const int s = T.div_shift[bi];
+  if (!m) return a >> s;
+#ifdef __CUDA_ARCH__
+  const uint32_t q = __umulhi(m, a);
+#else
+  const uint32_t q = (uint32_t)(((uint64_t)m * a) >> 32);
+#endif
+  if (s & 64) return (((a - q) >> 1) + q) >> (s & 63);
+  return q >> s;
+}
 
 // gl::radicalInverse (utility.hpp:406-420), float arithmetic.
 PT_HD float radical_inverse(const HaltonTables &T, int dim, uint64_t a) {
@@ -255,14 +309,17 @@ PT_HD float owen_radical_inverse(const HaltonTables &T, int dim, uint32_t index)
   const int bi = dim % PT_PRIME_COUNT;
   const uint32_t base = (uint32_t)T.prime[bi];
   const uint32_t hash = (uint32_t)mix_bits(1u + ((uint32_t)dim << 4));
+  const uint32_t w = fill_mask(base);
   uint32_t a = index;
   uint64_t rev = 0;
   const int nd = T.ndigits[bi];
   for (int di = 0; di < nd; ++di) {
-    uint32_t next = a / base;
+    uint32_t next = div_prime(T, bi, a);
     uint32_t digit = a - next * base;
     uint32_t dh = (uint32_t)mix_bits(hash ^ (uint32_t)rev ^ ((uint32_t)di << 16));
-    digit = permutation_element(digit, base, dh);
+    // permutation_element(digit, base, dh), its modulo by the base's divisor
+    const uint32_t s = permutation_index(digit, base, w, dh) + dh;
+    digit = s - div_prime(T, bi, s) * base;
     rev = rev * base + digit;
     a = next;
   }
@@ -280,7 +337,7 @@ PT_HD float permuted_radical_inverse(const HaltonTables &T, const uint16_t *perm
   uint64_t rev = 0;
   const int nd = T.ndigits[dim];
   for (int di = 0; di < nd; ++di) {
-    uint32_t next = a / base;
+    uint32_t next = div_prime(T, dim, a);
     uint32_t digit = a - next * base;
     rev = rev * base + p[di * base + digit];
     a = next;

@@ -57,6 +57,7 @@ HaltonTables make_halton_tables() {
     T.inv_base_m[b] = inv_base_m;
     T.perm_offset[b] = off;
     off += nd * base;
+    div_invariant((uint32_t)base, T.div_magic[b], T.div_shift[b]);
   }
   return T;
 }
