@@ -237,6 +237,10 @@ struct HaltonTables {
   // integer, Granlund and Montgomery, PLDI 1994): magic 0 = power of two
   uint32_t div_magic[PT_PRIME_COUNT];
   int32_t div_shift[PT_PRIME_COUNT];  // shift; bit 6 set: the 33-bit (add) form
+  // Owen-scrambled digits after which the value is tested for being settled
+  // (the least k with prime^k >= 2^38), and prime^(ndigits - owen_check)
+  int32_t owen_check[PT_PRIME_COUNT];
+  uint64_t owen_tail[PT_PRIME_COUNT];
 };
 
 // The magic multiplier and shift of a / d for every 32-bit a (d >= 2):
@@ -305,25 +309,43 @@ PT_HD float clamp_to_float(double r) {
 // gl::owenScrambledRadicalInverse (sampler/digitPerm.hpp:99-133) with the
 // hash HaltonSampler passes (sampler.hpp:69-71).  The sample index is a
 // uint32 in the reference, so the digit extraction runs on 32 bits.
+//
+// The value is rev * invBase^ndigits rounded to double and then to float,
+// a non-decreasing function f of rev, and the digits still to come after
+// the first k can only place rev in [rev_k * b^r, rev_k * b^r + b^r - 1]
+// (r = ndigits - k).  Where f takes the same value at both ends, that is
+// the result whatever the remaining digits are, so the loop stops there;
+// after T.owen_check digits this settles all but a few in 10^4 samples
+// (the rest run every digit as the reference does).
+struct OwenDigits {
+  uint32_t a;    // the index's digits not yet taken
+  uint64_t rev;  // the scrambled digits so far, most significant first
+};
+PT_HD void owen_digit(const HaltonTables &T, int bi, uint32_t base, uint32_t w, uint32_t hash, int di,
+                      OwenDigits &s) {
+  const uint32_t next = div_prime(T, bi, s.a);
+  const uint32_t digit = s.a - next * base;
+  const uint32_t dh = (uint32_t)mix_bits(hash ^ (uint32_t)s.rev ^ ((uint32_t)di << 16));
+  // permutation_element(digit, base, dh), its modulo by the base's divisor
+  const uint32_t v = permutation_index(digit, base, w, dh) + dh;
+  s.rev = s.rev * base + (v - div_prime(T, bi, v) * base);
+  s.a = next;
+}
 PT_HD float owen_radical_inverse(const HaltonTables &T, int dim, uint32_t index) {
   const int bi = dim % PT_PRIME_COUNT;
   const uint32_t base = (uint32_t)T.prime[bi];
   const uint32_t hash = (uint32_t)mix_bits(1u + ((uint32_t)dim << 4));
   const uint32_t w = fill_mask(base);
-  uint32_t a = index;
-  uint64_t rev = 0;
-  const int nd = T.ndigits[bi];
-  for (int di = 0; di < nd; ++di) {
-    uint32_t next = div_prime(T, bi, a);
-    uint32_t digit = a - next * base;
-    uint32_t dh = (uint32_t)mix_bits(hash ^ (uint32_t)rev ^ ((uint32_t)di << 16));
-    // permutation_element(digit, base, dh), its modulo by the base's divisor
-    const uint32_t s = permutation_index(digit, base, w, dh) + dh;
-    digit = s - div_prime(T, bi, s) * base;
-    rev = rev * base + digit;
-    a = next;
-  }
-  return clamp_to_float(xdmul(T.inv_base_m[bi], (double)rev));
+  const double scale = T.inv_base_m[bi];
+  OwenDigits s{index, 0};
+  const int nd = T.ndigits[bi], nc = T.owen_check[bi];
+  int di = 0;
+  for (; di < nc; ++di) owen_digit(T, bi, base, w, hash, di, s);
+  const uint64_t lo = s.rev * T.owen_tail[bi];
+  const float flo = clamp_to_float(xdmul(scale, (double)lo));
+  if (flo == clamp_to_float(xdmul(scale, (double)(lo + (T.owen_tail[bi] - 1))))) return flo;
+  for (; di < nd; ++di) owen_digit(T, bi, base, w, hash, di, s);
+  return clamp_to_float(xdmul(scale, (double)s.rev));
 }
 
 // gl::scrambledRadicalInverse with DigitPermutation tables

@@ -58,6 +58,12 @@ HaltonTables make_halton_tables() {
     T.perm_offset[b] = off;
     off += nd * base;
     div_invariant((uint32_t)base, T.div_magic[b], T.div_shift[b]);
+    int check = 0;
+    for (uint64_t p = 1; p < (1ull << 38) && check < nd; p *= (uint64_t)base) ++check;
+    uint64_t tail = 1;
+    for (int r = check; r < nd; ++r) tail *= (uint64_t)base;
+    T.owen_check[b] = check;
+    T.owen_tail[b] = tail;
   }
   return T;
 }
