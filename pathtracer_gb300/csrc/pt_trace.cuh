@@ -407,6 +407,22 @@ __device__ __forceinline__ bool trav_step(const SceneView &S, TravRay &R, int32_
   return false;
 }
 
+// The kind of step a warp's lanes take this turn: leaf-item tests when at
+// least half of the active lanes stand at a leaf, else node visits (lanes
+// whose traversal has ended take theirs in node turns).  Every lane steps in
+// one code path per turn instead of the warp issuing both paths each turn for
+// its mix of lanes; lanes of the other kind wait a turn.  Each ray takes the
+// same steps in the same order either way, so hits are unchanged.  Called by
+// every lane of the warp.
+__device__ __forceinline__ bool warp_leaf_turn(bool active, int32_t ref) {
+  const unsigned am = __ballot_sync(0xffffffffu, active);
+  const unsigned lm = __ballot_sync(0xffffffffu, active && ref_is_leaf(ref));
+  return 2 * __popc(lm) >= __popc(am);
+}
+__device__ __forceinline__ bool lane_turn(bool active, int32_t ref, bool leaf_turn) {
+  return active && ref_is_leaf(ref) == leaf_turn;
+}
+
 // Whole traversal of one ray by one thread (batch test kernels).
 template <bool ANY>
 __device__ bool traverse(const SceneView &S, V3 o, V3 d, float tmin, float tmax, HitRec &hit,

@@ -379,7 +379,8 @@ __device__ __forceinline__ void trace_closest_body(const SceneView &S, const Dev
       if (exhausted) break;
       continue;
     }
-    if (active && trav_step<false, CURVES>(S, R, my_stack, blockDim.x, Q.err)) {
+    const bool lt = warp_leaf_turn(active, R.ref);
+    if (lane_turn(active, R.ref, lt) && trav_step<false, CURVES>(S, R, my_stack, blockDim.x, Q.err)) {
       const bool hit = R.found;
       int prim = hit ? R.hit.prim : (t_s < 1e5f ? PT_HIT_MEDIUM : -1);
       float t = hit ? R.hit.t : (prim == PT_HIT_MEDIUM ? t_s : FLT_MAX);
@@ -469,14 +470,16 @@ __device__ __forceinline__ void trace_pair_body(const SceneView &S, const Device
       if (exhausted) break;
       continue;
     }
-    if (active && !shadow && trav_step<false, CURVES>(S, R, my_stack, blockDim.x, Q.err)) {
+    const bool lt = warp_leaf_turn(active, R.ref);
+    const bool turn = lane_turn(active, R.ref, lt);
+    if (turn && !shadow && trav_step<false, CURVES>(S, R, my_stack, blockDim.x, Q.err)) {
       const bool hit = R.found;
       int prim = hit ? R.hit.prim : (t_s < 1e5f ? PT_HIT_MEDIUM : -1);
       float t = hit ? R.hit.t : (prim == PT_HIT_MEDIUM ? t_s : FLT_MAX);
       Q.hit[slot] = make_float4(t, __int_as_float(prim), R.hit.u, R.hit.v);
       active = false;
     }
-    if (active && shadow && trav_step<true, CURVES>(S, R, my_stack, blockDim.x, Q.err)) {
+    if (turn && shadow && trav_step<true, CURVES>(S, R, my_stack, blockDim.x, Q.err)) {
       Q.sh_vis[slot] = R.found ? 0 : 1;
       active = false;
     }
@@ -983,7 +986,8 @@ __device__ __forceinline__ void trace_shadow_body(const SceneView &S, const Queu
       if (exhausted) break;
       continue;
     }
-    if (active && trav_step<true, CURVES>(S, R, my_stack, blockDim.x, Q.err)) {
+    const bool lt = warp_leaf_turn(active, R.ref);
+    if (lane_turn(active, R.ref, lt) && trav_step<true, CURVES>(S, R, my_stack, blockDim.x, Q.err)) {
       Q.sh_vis[slot] = R.found ? 0 : 1;
       active = false;
     }
