@@ -321,31 +321,46 @@ struct OwenDigits {
   uint32_t a;    // the index's digits not yet taken
   uint64_t rev;  // the scrambled digits so far, most significant first
 };
+template <bool BASE2>
 PT_HD void owen_digit(const HaltonTables &T, int bi, uint32_t base, uint32_t w, uint32_t hash, int di,
                       OwenDigits &s) {
-  const uint32_t next = div_prime(T, bi, s.a);
-  const uint32_t digit = s.a - next * base;
   const uint32_t dh = (uint32_t)mix_bits(hash ^ (uint32_t)s.rev ^ ((uint32_t)di << 16));
-  // permutation_element(digit, base, dh), its modulo by the base's divisor
-  const uint32_t v = permutation_index(digit, base, w, dh) + dh;
-  s.rev = s.rev * base + (v - div_prime(T, bi, v) * base);
-  s.a = next;
+  if (BASE2) {
+    // permutation_element(d, 2, p) = d ^ bit 0 of (p >> 8 ^ p >> 16 ^ p >> 23):
+    // with w = 1 every odd multiplier keeps bit 0, every (i & w) >> k
+    // shift is 0, the loop runs once and the final + p cancels p's bit 0
+    // (checked for every p and d)
+    const uint32_t digit = (s.a & 1u) ^ (((dh >> 8) ^ (dh >> 16) ^ (dh >> 23)) & 1u);
+    s.rev = (s.rev << 1) | digit;
+    s.a >>= 1;
+  } else {
+    const uint32_t next = div_prime(T, bi, s.a);
+    const uint32_t digit = s.a - next * base;
+    // permutation_element(digit, base, dh), its modulo by the base's divisor
+    const uint32_t v = permutation_index(digit, base, w, dh) + dh;
+    s.rev = s.rev * base + (v - div_prime(T, bi, v) * base);
+    s.a = next;
+  }
 }
-PT_HD float owen_radical_inverse(const HaltonTables &T, int dim, uint32_t index) {
-  const int bi = dim % PT_PRIME_COUNT;
+template <bool BASE2>
+PT_HD float owen_digits(const HaltonTables &T, int bi, uint32_t hash, uint32_t index) {
   const uint32_t base = (uint32_t)T.prime[bi];
-  const uint32_t hash = (uint32_t)mix_bits(1u + ((uint32_t)dim << 4));
   const uint32_t w = fill_mask(base);
   const double scale = T.inv_base_m[bi];
   OwenDigits s{index, 0};
   const int nd = T.ndigits[bi], nc = T.owen_check[bi];
   int di = 0;
-  for (; di < nc; ++di) owen_digit(T, bi, base, w, hash, di, s);
+  for (; di < nc; ++di) owen_digit<BASE2>(T, bi, base, w, hash, di, s);
   const uint64_t lo = s.rev * T.owen_tail[bi];
   const float flo = clamp_to_float(xdmul(scale, (double)lo));
   if (flo == clamp_to_float(xdmul(scale, (double)(lo + (T.owen_tail[bi] - 1))))) return flo;
-  for (; di < nd; ++di) owen_digit(T, bi, base, w, hash, di, s);
+  for (; di < nd; ++di) owen_digit<BASE2>(T, bi, base, w, hash, di, s);
   return clamp_to_float(xdmul(scale, (double)s.rev));
+}
+PT_HD float owen_radical_inverse(const HaltonTables &T, int dim, uint32_t index) {
+  const int bi = dim % PT_PRIME_COUNT;
+  const uint32_t hash = (uint32_t)mix_bits(1u + ((uint32_t)dim << 4));
+  return T.prime[bi] == 2 ? owen_digits<true>(T, bi, hash, index) : owen_digits<false>(T, bi, hash, index);
 }
 
 // gl::scrambledRadicalInverse with DigitPermutation tables
