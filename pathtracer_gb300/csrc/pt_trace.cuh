@@ -245,13 +245,23 @@ struct TravRay {
 __device__ __forceinline__ bool ref_is_node(int32_t r) { return r >= 0 || r == PT_FRAME_END; }
 __device__ __forceinline__ bool ref_is_leaf(int32_t r) { return r < 0 && r != PT_FRAME_END && r != PT_REF_EMPTY; }
 
+// 1/d of one axis for the slab test.  An axis the ray does not move along
+// (d = +-0, or |d| so small that 1/d overflows) gets +-1e20 with d's sign in
+// place of +-inf: the slab test computes fmaf(plane, inv, -o * inv), and with
+// an infinite inv a ray inside the slab gives inf - inf = NaN, which the
+// min / max then drop -- that slab is not tested at all, and an axis-aligned
+// ray walks every box its other slabs cross (the whole tree, ~10^5 steps for
+// one ray).  With a finite inv the slab gives (-huge, +huge) inside it and an
+// entry beyond any tmax outside.
+__device__ __forceinline__ float slab_inv(float d) { return fabsf(d) > 1e-20f ? 1.f / d : copysignf(1e20f, d); }
+
 __device__ __forceinline__ void trav_init(TravRay &R, V3 o, V3 d, float tmin, float tmax, float time = 0.f) {
   R.time = time;
   R.o = o;
   R.ow = o;
   R.d = d;
   R.dn = xnormalize(d);
-  R.inv = v3(1.f / d.x, 1.f / d.y, 1.f / d.z);
+  R.inv = v3(slab_inv(d.x), slab_inv(d.y), slab_inv(d.z));
   R.oi = v3(-o.x * R.inv.x, -o.y * R.inv.y, -o.z * R.inv.z);
   R.tmin = tmin;
   R.tmax = tmax;

@@ -102,6 +102,32 @@ def test_trace_matches_oracle_random_rays(renderer, subdiv):
     renderer.release(sid)
 
 
+def test_trace_axis_aligned_rays_match_oracle(renderer):
+    """Rays that do not move along one or two axes (direction components
+    exactly +-0, as a uniform-sphere sample at u = 0 gives): the slab test
+    must still bound them on those axes -- same hits as the oracle, and
+    both traversals end (no walk of the whole tree per ray)."""
+    rng = np.random.default_rng(7)
+    sc, _ = S.material_divergence(subdiv=3, seed=1)
+    sid = renderer.upload(sc)
+    n = 6000
+    o = rng.uniform(-6, 6, size=(n, 3))
+    dirs = [(0, 0, 1), (0, 0, -1), (0, 1, 0), (0, -1, 0), (1, 0, 0), (-1, 0, 0),
+            (0.6, 0.8, 0), (-0.6, 0, 0.8), (0, -0.8, 0.6), (-0.0, -0.0, 1)]
+    d = np.array([dirs[i % len(dirs)] for i in range(n)], np.float64)
+    rays = np.concatenate([o, d], 1).astype(np.float32)
+    t, prim, _ = renderer.trace_closest(sid, rays)
+    t2, prim2 = O.OracleScene(sc).trace_closest(rays)
+    same = prim == prim2
+    assert same.mean() > 0.999, same.mean()
+    hit = (prim2 >= 0) & same
+    assert hit.sum() > n // 20
+    assert np.all(np.abs(t[hit] - t2[hit]) <= 1e-5 * np.abs(t2[hit]))
+    occ = renderer.trace_any(sid, rays, np.full(n, 1e5, np.float32), tmin=1e-4)
+    assert np.array_equal(occ.astype(bool), prim2 >= 0)
+    renderer.release(sid)
+
+
 CASES = bsdf_cases()
 
 
