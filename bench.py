@@ -101,6 +101,8 @@ def parse():
                     help="arrival window of the served config-4 mix (20 req/s; 0: skip)")
     ap.add_argument("--config4-drain", type=float, default=20.0,
                     help="seconds the config-4 server keeps running after the arrivals end")
+    ap.add_argument("--persistent-config3", action="store_true",
+                    help="also time the config-3 batch in the persistent form (about two more minutes)")
     return ap.parse_args()
 
 
@@ -255,6 +257,46 @@ def cpu_paths_per_sec(osc, cam, wl, estimator, threads, target_s=12.0, max_px=10
     return res * res / dt, f"{res}x{res} pixels x 1 spp of the workload's scene and camera", dt
 
 
+def run_full_frames(r, names, cpu: bool, threads: int) -> dict:
+    """The other single-job workloads (configs 0 and 2) at their full size:
+    one whole frame (every sample) per estimator through pt_render with a
+    host film -- device time from the library's events, e2e from the wall
+    clock around the call -- and, with `cpu`, the oracle's REF_NEE on a
+    bounded sample of the same scene on the host cores."""
+    from pathtracer_gb300 import native as N
+
+    out = {}
+    for name in names:
+        sc, cam = build_scene(name)
+        sid = r.upload(sc)
+        res = {"workload": WORKLOADS[name]["desc"]}
+        for est in ("ref_nee", "nee_mis"):
+            wl = workload(name, est)
+            job = N.job_desc(sid, cam, wl["W"], wl["H"], wl["sx"], wl["sy"], wl["depth"], rr_start=wl["rr"],
+                             estimator=wl["est"], sampler=wl["sampler"], env_sampling=wl["env"], seed=1)
+            warm = N.job_desc(sid, cam, wl["W"], wl["H"], wl["sx"], wl["sy"], wl["depth"], rr_start=wl["rr"],
+                              estimator=wl["est"], sampler=wl["sampler"], env_sampling=wl["env"], seed=1,
+                              spp_begin=0, spp_end=1)
+            r.render(warm)
+            t0 = time.perf_counter()
+            film, st = r.render(job, stats=True)
+            wall = time.perf_counter() - t0
+            res[est] = {"paths": int(st.paths), "paths_per_s": st.paths / (st.ms / 1e3),
+                        "e2e_paths_per_s": st.paths / wall, "rays_per_s": (st.rays + st.shadow_rays) / (st.ms / 1e3),
+                        "frame_s": wall, "finite": bool(np.isfinite(film).all()), "estimator": wl["est_name"]}
+        if cpu:
+            from oracle import pyoracle as O
+
+            wl = workload(name, "ref_nee")
+            v, sample, dt = cpu_paths_per_sec(O.OracleScene(sc), cam, wl, wl["est"], threads, target_s=6.0)
+            res["cpu_baseline"] = {"value": v, "unit": "paths/s", "cores": threads, "kind": "port",
+                                   "sample": sample + f" ({dt:.1f} s), REF_NEE"}
+            res["e2e_vs_cpu"] = res["ref_nee"]["e2e_paths_per_s"] / v
+        r.release(sid)
+        out[name] = res
+    return out
+
+
 def form_scenes(r, with_big: bool):
     """The resident scenes of the batched and served forms: the three
     workloads with seeded per-object motion (meshes and spheres move, walls,
@@ -294,7 +336,7 @@ def form_scenes(r, with_big: bool):
 
 
 def run_batched(r, scenes, n_jobs: int, seed: int = 11, res=(64, 1024), spp=(4, 256), tune: bool = True,
-                tune_sample: int = 8, tune_spp: int = 4):
+                tune_sample: int = 8, tune_spp: int = 4, persistent: bool = True):
     """Config-3 job mix: one pt_render_batch call (one CUDA-graph launch)
     against the plain wavefront drop-in (pt_render per job, one after the
     other); both with host films, so both are end to end.  The two arms
@@ -322,19 +364,21 @@ def run_batched(r, scenes, n_jobs: int, seed: int = 11, res=(64, 1024), spp=(4, 
     t0 = time.perf_counter()
     films_b, st = r.render_batch(jobs, stats=True)
     t_batch = time.perf_counter() - t0
-    # the same batch as ONE persistent cooperative launch per scene group
-    from pathtracer_gb300 import native as N
-    r.set_batch_mode(N.BATCH_PERSISTENT)
-    try:
-        r.render_batch(jobs)
-        t0 = time.perf_counter()
-        films_q, st_q = r.render_batch(jobs, stats=True)
-        t_pers = time.perf_counter() - t0
-    finally:
-        r.set_batch_mode(N.BATCH_GRAPH)
-    rel_q = 0.0
-    for a, b in zip(films_q, films_b):
-        rel_q = max(rel_q, float(np.abs(a - b).max() / max(1e-12, float(np.abs(b).max()))))
+    pers = None
+    if persistent:
+        # the same batch as ONE persistent cooperative launch per scene group
+        from pathtracer_gb300 import native as N
+        r.set_batch_mode(N.BATCH_PERSISTENT)
+        try:
+            r.render_batch(jobs)
+            t0 = time.perf_counter()
+            films_q, st_q = r.render_batch(jobs, stats=True)
+            t_pers = time.perf_counter() - t0
+        finally:
+            r.set_batch_mode(N.BATCH_GRAPH)
+        rel_q = 0.0
+        for a, b in zip(films_q, films_b):
+            rel_q = max(rel_q, float(np.abs(a - b).max() / max(1e-12, float(np.abs(b).max()))))
     # plain wavefront, one job after the other (warm the context's queues first)
     r.render(jobs[0])
     t0 = time.perf_counter()
@@ -344,16 +388,16 @@ def run_batched(r, scenes, n_jobs: int, seed: int = 11, res=(64, 1024), spp=(4, 
     for a, b in zip(films_b, films_p):
         d = np.abs(a - b).max() / max(1e-12, float(np.abs(b).max()))
         rel = max(rel, float(d))
+    if persistent:
+        pers = {"paths_per_s": paths / t_pers, "speedup_vs_plain": t_plain / t_pers, "vs_graph": t_batch / t_pers,
+                "device_ms": st_q.ms, "max_rel_film_diff_vs_graph": rel_q,
+                "form": "one cooperative launch per scene group: every wave and bounce, grid barriers between "
+                        "stages, generic (unsorted) shading"}
     sides = sorted(j.width for j in jobs)
-    return {
+    out = {
         "jobs": n_jobs, "paths": paths, "paths_per_s": paths / t_batch, "plain_paths_per_s": paths / t_plain,
         "speedup_vs_plain": t_plain / t_batch, "batch_s": t_batch, "plain_s": t_plain,
         "graph_device_ms": st.ms, "max_rel_film_diff_vs_plain": rel,
-        "persistent": {"paths_per_s": paths / t_pers, "speedup_vs_plain": t_plain / t_pers,
-                       "vs_graph": t_batch / t_pers, "device_ms": st_q.ms,
-                       "max_rel_film_diff_vs_graph": rel_q,
-                       "form": "one cooperative launch per scene group: every wave and bounce, grid barriers "
-                               "between stages, generic (unsorted) shading"},
         "equal_rmse": "same samples in both arms: identical images up to FP32 summation order",
         "mix": f"{n_jobs} jobs over cornell/rough_glass/divergence with per-object motion; square resolution "
                f"log-uniform {res[0]}..{res[1]} (median {sides[len(sides) // 2]}), spp U{{{spp[0]}..{spp[1]}}}, "
@@ -361,6 +405,9 @@ def run_batched(r, scenes, n_jobs: int, seed: int = 11, res=(64, 1024), spp=(4, 
         "autotune": ({k: tuning[k] for k in ("wave_paths", "sort_by_material", "trace_blocks", "shade_blocks")} |
                      {"candidates": tuning["candidates"], "seconds": tune_s}) if tuning else "as tuned above",
     }
+    if pers is not None:
+        out["persistent"] = pers
+    return out
 
 
 def run_served(r, scenes, big, seconds: float, rate: float, seed: int = 12, pass_spp: int = 8,
@@ -831,7 +878,9 @@ def run_ours(args, rank, world, local_rank):
         fs, big, build_s, upload_s = form_scenes(r, with_big=True)
         forms = {"scene_build_s": build_s,
                  "big_scene_upload_s": dict(upload_s, triangles=5242880)}
-        forms["batched"] = run_batched(r, fs, args.batch_jobs)
+        # the persistent form of the config-3 mix runs ~5x longer than the
+        # graph form (about two minutes), so it is opt-in here
+        forms["batched"] = run_batched(r, fs, args.batch_jobs, persistent=args.persistent_config3)
         # the regime batching exists for: many jobs far below one GPU's worth
         # of paths each (same scenes and cameras, smaller frames and spp)
         forms["batched_small_jobs"] = run_batched(r, fs, args.batch_jobs, seed=13, res=(64, 256), spp=(4, 32),
@@ -844,6 +893,10 @@ def run_ours(args, rank, world, local_rank):
             forms["served_config4_saturating"] = run_served_config4(r, fs, big, 5.0, 200.0, args.config4_drain,
                                                                     seed=15)
         line["forms"] = forms
+    if world == 1 and not args.no_forms:
+        # configs 0 and 2 (Cornell, material divergence) at full size
+        others = [n for n in ("cornell", "divergence") if n != args.workload]
+        line["full_frames"] = run_full_frames(r, others, not args.no_cpu_baseline, os.cpu_count() or 1)
     if not args.no_cpu_baseline:
         from oracle import pyoracle as O
 
