@@ -410,8 +410,9 @@ int pt_render_device(void *ctx, const pt_job_desc *job, float *d_film_sum,
  * with CUDA's lazy module loading it loads the module that holds the array,
  * which allocates the 32 MiB on that device (kept until the process exits),
  * and it looks up the array's device address -- make one warm-up call on
- * each device before entering a region that must not allocate, and before
- * any stream capture.  All calls share the one array, which keeps the last
+ * each device before entering a region that must not allocate.  Every call
+ * synchronises the context's stream and reads its error word and counts back
+ * before it returns.  All calls share the one array, which keeps the last
  * call's contents: calls that overlap on the GPU (other host threads, other
  * contexts of the same device) race and must be serialised by the caller. */
 int pt_render_device_noalloc(void *ctx, const pt_job_desc *job, float *d_film_sum, pt_stats *stats);
