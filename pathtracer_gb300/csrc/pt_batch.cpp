@@ -57,6 +57,7 @@ void BatchSlot::release() {
     stream[h] = nullptr;
     if (done[h]) cudaEventDestroy(done[h]);
     done[h] = nullptr;
+    side[h].destroy();
   }
 }
 
@@ -64,6 +65,7 @@ void BatchSlot::ensure(int want_cap, int want_ln, int n_jobs, size_t n_offsets, 
   for (int h = 0; h < 2; ++h) {
     if (!stream[h]) cuda_check(cudaStreamCreateWithFlags(&stream[h], cudaStreamNonBlocking), "cudaStreamCreate");
     if (!done[h]) cuda_check(cudaEventCreateWithFlags(&done[h], cudaEventDisableTiming), "cudaEventCreate");
+    side[h].create();
   }
   if (want_cap > cap || want_ln > ln) {
     for (void *p : mem) cudaFree(p);
@@ -205,7 +207,7 @@ static float render_groups_graph(Context *c, const pt_job_desc *jobs, int n, std
           cudaStreamWaitEvent(slot.stream[1], slot.done[0], 0);
         }
         cudaEvent_t mine = B.film_events[ev++];
-        launch_wave_multi(S->view, G.M, slot.Q[h], g0, cnt, lc, slot.stream[h], nullptr, prev, mine);
+        launch_wave_multi(S->view, G.M, slot.Q[h], g0, cnt, lc, slot.stream[h], nullptr, prev, mine, &slot.side[h]);
         prev = mine;
       }
       for (int h = 0; h < 2; ++h) {

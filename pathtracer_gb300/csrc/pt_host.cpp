@@ -1599,6 +1599,7 @@ Scene::~Scene() {
 Context::Context(int dev) : device(dev) {
   cuda_check(cudaSetDevice(dev), "cudaSetDevice");
   cuda_check(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "cudaStreamCreate");
+  side1.create();
   cudaDeviceProp prop;
   cuda_check(cudaGetDeviceProperties(&prop, dev), "cudaGetDeviceProperties");
   num_sms = prop.multiProcessorCount;
@@ -1641,6 +1642,8 @@ Context::~Context() {
   free_queues();
   for (void *p : qmem2) cudaFree(p);
   if (stream2) cudaStreamDestroy(stream2);
+  side1.destroy();
+  side2.destroy();
   if (ev_fork) cudaEventDestroy(ev_fork);
   if (ev_join) cudaEventDestroy(ev_join);
   for (cudaEvent_t e : film_ev) cudaEventDestroy(e);
@@ -1703,6 +1706,7 @@ void Context::ensure_queues(int cap, int ln) {
 
 void Context::ensure_queues2(int cap, int ln) {
   if (!stream2) cuda_check(cudaStreamCreateWithFlags(&stream2, cudaStreamNonBlocking), "cudaStreamCreate");
+  side2.create();
   if (!ev_fork) cuda_check(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming), "cudaEventCreate");
   if (!ev_join) cuda_check(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming), "cudaEventCreate");
   if (cap <= q2_cap && ln <= q2_ln) return;
@@ -1864,7 +1868,7 @@ void Context::render_device(const pt_job_desc &j, float *d_film, pt_stats *stats
   lc.family_mask = S->family_mask;
   const long long waves = (total + n - 1) / n;
   if (waves == 1) {
-    launch_wave(S->view, J, Q, 0, (int)total, d_film, lc, stream, &prof);
+    launch_wave(S->view, J, Q, 0, (int)total, d_film, lc, stream, &prof, nullptr, nullptr, &side1);
   } else {
     // consecutive waves alternate between two queue sets on two streams so
     // that one wave's sparse last bounces overlap the next wave's first ones;
@@ -1883,7 +1887,7 @@ void Context::render_device(const pt_job_desc &j, float *d_film, pt_stats *stats
       const int cnt = (int)std::min<long long>(n, total - g0);
       const bool odd = (w & 1) != 0;
       launch_wave(S->view, J, odd ? Q2 : Q, g0, cnt, d_film, lc, odd ? stream2 : stream, &prof,
-                  w > 0 ? film_ev[w - 1] : nullptr, film_ev[w]);
+                  w > 0 ? film_ev[w - 1] : nullptr, film_ev[w], odd ? &side2 : &side1);
     }
     cudaEventRecord(ev_join, stream2);
     cudaStreamWaitEvent(stream, ev_join, 0);

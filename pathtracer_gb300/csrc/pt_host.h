@@ -82,6 +82,7 @@ struct BatchSlot {
   void *d_barrier = nullptr;
   cudaStream_t stream[2] = {nullptr, nullptr};
   cudaEvent_t done[2] = {nullptr, nullptr};
+  ShadeStreams side[2];  // side streams of stream[0], stream[1]
   void ensure(int want_cap, int want_ln, int n_jobs, size_t n_offsets, size_t film_floats);
   void release();
 };
@@ -124,6 +125,7 @@ struct Context {
   int q2_cap = 0, q2_ln = 0;
   cudaStream_t stream2 = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  ShadeStreams side1, side2;  // side streams of stream, stream2
   std::vector<cudaEvent_t> film_ev;
   void ensure_queues2(int cap, int ln);
   float *d_film = nullptr;

@@ -384,13 +384,13 @@ void launch_bsdf_sample(const MatRec *m, int n, const float *wo, const float *nr
 // One wave of a single job: camera, max_depth (+1 for MIS) bounces, film.
 void launch_wave(const SceneView &S, const DeviceJob &J, const Queues &Q, long long g0, int n,
                  float *film, const LaunchCfg &cfg, cudaStream_t st, Profiler *prof, cudaEvent_t film_after,
-                 cudaEvent_t film_done) {
+                 cudaEvent_t film_done, const ShadeStreams *ss) {
   const int LN = J.job.light_nx * J.job.light_ny;
   const int bounces = J.job.max_depth + (J.job.estimator == PT_EST_NEE_MIS ? 1 : 0);
   Profiler dummy;
   Profiler &P = prof ? *prof : dummy;
   const JobTable none{nullptr, nullptr, 0};
-  launch_wave_stages<false>(S, J, none, Q, g0, n, LN, bounces, cfg, st, P);
+  launch_wave_stages<false>(S, J, none, Q, g0, n, LN, bounces, cfg, st, P, ss);
   if (film_after) cudaStreamWaitEvent(st, film_after, 0);
   P.begin(STAGE_FILM, st);
   launch_film(J, Q, g0, n, 0, film, cfg, st);

@@ -65,6 +65,37 @@ struct LaunchCfg {
                          // roulette start of a single-job wave)
 };
 
+// Side streams of one wave's stream: a bounce's per-family shade kernels
+// are independent (each owns its segment of the sorted queue and its paths;
+// queue slots come from atomics), so they run concurrently on the wave's
+// stream and these, forked and joined by events -- in a captured graph,
+// parallel branches.  One set per stream that runs waves.
+struct ShadeStreams {
+  static constexpr int N = 3;
+  cudaStream_t aux[N] = {};
+  cudaEvent_t fork = nullptr, join[N] = {};
+  bool ready() const { return fork != nullptr; }
+  void create() {
+    if (fork) return;
+    for (int i = 0; i < N; ++i) {
+      cudaStreamCreateWithFlags(&aux[i], cudaStreamNonBlocking);
+      cudaEventCreateWithFlags(&join[i], cudaEventDisableTiming);
+    }
+    cudaEventCreateWithFlags(&fork, cudaEventDisableTiming);
+  }
+  void destroy() {
+    if (!fork) return;
+    for (int i = 0; i < N; ++i) {
+      cudaStreamDestroy(aux[i]);
+      cudaEventDestroy(join[i]);
+      aux[i] = nullptr;
+      join[i] = nullptr;
+    }
+    cudaEventDestroy(fork);
+    fork = nullptr;
+  }
+};
+
 // Per-stage CUDA-event timing of the wave kernels (pt_profile_begin/end).
 enum StageKind { STAGE_CAMERA = 0, STAGE_TRACE, STAGE_SORT, STAGE_SHADE, STAGE_SHADOW, STAGE_FILM, STAGE_COUNT };
 struct Profiler {
@@ -120,9 +151,11 @@ void launch_bsdf_sample(const MatRec *m, int n, const float *wo, const float *nr
                         float *wi, float *att, float *pdf, uint32_t *type, cudaStream_t st);
 // film_after (may be null): the film stage waits for it; film_done (may be
 // null) is recorded after this wave's film stage (wave order across streams).
+// ss (may be null): the stream's side streams for concurrent shade kernels.
 void launch_wave(const SceneView &S, const DeviceJob &J, const Queues &Q, long long g0, int n,
                  float *film, const LaunchCfg &cfg, cudaStream_t st, Profiler *prof,
-                 cudaEvent_t film_after = nullptr, cudaEvent_t film_done = nullptr);
+                 cudaEvent_t film_after = nullptr, cudaEvent_t film_done = nullptr,
+                 const ShadeStreams *ss = nullptr);
 // Job-independent stages (pt_kernels.cu), also used by merged waves.
 void launch_sort(const SceneView &S, const Queues &Q, int qsel, const LaunchCfg &cfg, cudaStream_t st);
 void launch_shadow(const SceneView &S, const Queues &Q, int LN, const LaunchCfg &cfg, cudaStream_t st);
@@ -147,7 +180,7 @@ struct MergedJobs {
 // this wave's films.
 void launch_wave_multi(const SceneView &S, const MergedJobs &M, const Queues &Q, long long g0, int n,
                        const LaunchCfg &cfg, cudaStream_t st, Profiler *prof, cudaEvent_t film_after = nullptr,
-                       cudaEvent_t film_done = nullptr);
+                       cudaEvent_t film_done = nullptr, const ShadeStreams *ss = nullptr);
 void upload_halton_tables_multi(const HaltonTables &T, cudaStream_t st);
 // Persistent form of a merged group (pt_kernels_persist.cu): every wave and
 // bounce of the group in one cooperative launch of `grid` blocks;

@@ -14,12 +14,12 @@ void upload_halton_tables_multi(const HaltonTables &T, cudaStream_t st) {
 
 void launch_wave_multi(const SceneView &S, const MergedJobs &M, const Queues &Q, long long g0, int n,
                        const LaunchCfg &cfg, cudaStream_t st, Profiler *prof, cudaEvent_t film_after,
-                       cudaEvent_t film_done) {
+                       cudaEvent_t film_done, const ShadeStreams *ss) {
   Profiler dummy;
   Profiler &P = prof ? *prof : dummy;
   DeviceJob none;
   std::memset(&none, 0, sizeof none);
-  launch_wave_stages<true>(S, none, M.T, Q, g0, n, M.LN, M.bounces, cfg, st, P);
+  launch_wave_stages<true>(S, none, M.T, Q, g0, n, M.LN, M.bounces, cfg, st, P, ss);
   if (film_after) cudaStreamWaitEvent(st, film_after, 0);
   P.begin(STAGE_FILM, st);
   const long long g1 = g0 + n;

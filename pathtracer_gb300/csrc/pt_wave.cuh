@@ -1063,7 +1063,8 @@ static inline int grid_for(long long n, int block, int max_blocks) {
 // trace -> [sort] -> shade -> shadow per bounce.
 template <bool MJ>
 void launch_wave_stages(const SceneView &S, const DeviceJob &J, const JobTable &T, const Queues &Q, long long g0,
-                        int n, int LN, int bounces, const LaunchCfg &cfg, cudaStream_t st, Profiler &P) {
+                        int n, int LN, int bounces, const LaunchCfg &cfg, cudaStream_t st, Profiler &P,
+                        const ShadeStreams *ss) {
   P.begin(STAGE_CAMERA, st);
   k_camera<MJ><<<grid_for(n, 256, cfg.max_blocks_simple), 256, 0, st>>>(J, T, Q, g0, n);
   P.end(st);
@@ -1115,14 +1116,33 @@ void launch_wave_stages(const SceneView &S, const DeviceJob &J, const JobTable &
       P.end(st);
       P.count(STAGE_SORT, 2);
       P.begin(STAGE_SHADE, st);
-      if (cfg.family_mask & (1u << 0)) k_shade<0, MJ><<<cfg.shade_fam_blocks[0], 128, 0, st>>>(S, J, T, Q, qsel, b, g0);
-      if (cfg.family_mask & (1u << 1)) k_shade<1, MJ><<<cfg.shade_fam_blocks[1], 128, 0, st>>>(S, J, T, Q, qsel, b, g0);
-      if (cfg.family_mask & (1u << 2)) k_shade<2, MJ><<<cfg.shade_fam_blocks[2], 128, 0, st>>>(S, J, T, Q, qsel, b, g0);
-      if (cfg.family_mask & (1u << 3)) k_shade<3, MJ><<<cfg.shade_fam_blocks[3], 128, 0, st>>>(S, J, T, Q, qsel, b, g0);
-      if (cfg.family_mask & (1u << 4)) k_shade<4, MJ><<<cfg.shade_fam_blocks[4], 128, 0, st>>>(S, J, T, Q, qsel, b, g0);
-      if (cfg.family_mask & (1u << 5)) k_shade<5, MJ><<<cfg.shade_fam_blocks[5], 128, 0, st>>>(S, J, T, Q, qsel, b, g0);
-      if (cfg.family_mask & (1u << 6)) k_shade<6, MJ><<<cfg.shade_fam_blocks[6], 128, 0, st>>>(S, J, T, Q, qsel, b, g0);
-      k_shade<PT_FAM_MISC, MJ><<<cfg.shade_fam_blocks[PT_FAM_MISC], 128, 0, st>>>(S, J, T, Q, qsel, b, g0);
+      // the families present, then misses / emitters / medium events, each
+      // on the next of the stream and its side streams (round robin)
+      int used = 0;  // side streams forked
+      int k = 0;     // kernels launched
+      auto next_stream = [&]() -> cudaStream_t {
+        const int slot = ss ? k % (ShadeStreams::N + 1) : 0;
+        ++k;
+        if (slot == 0) return st;
+        if (slot > used) {
+          if (used == 0) cudaEventRecord(ss->fork, st);
+          cudaStreamWaitEvent(ss->aux[slot - 1], ss->fork, 0);
+          used = slot;
+        }
+        return ss->aux[slot - 1];
+      };
+      if (cfg.family_mask & (1u << 0)) k_shade<0, MJ><<<cfg.shade_fam_blocks[0], 128, 0, next_stream()>>>(S, J, T, Q, qsel, b, g0);
+      if (cfg.family_mask & (1u << 1)) k_shade<1, MJ><<<cfg.shade_fam_blocks[1], 128, 0, next_stream()>>>(S, J, T, Q, qsel, b, g0);
+      if (cfg.family_mask & (1u << 2)) k_shade<2, MJ><<<cfg.shade_fam_blocks[2], 128, 0, next_stream()>>>(S, J, T, Q, qsel, b, g0);
+      if (cfg.family_mask & (1u << 3)) k_shade<3, MJ><<<cfg.shade_fam_blocks[3], 128, 0, next_stream()>>>(S, J, T, Q, qsel, b, g0);
+      if (cfg.family_mask & (1u << 4)) k_shade<4, MJ><<<cfg.shade_fam_blocks[4], 128, 0, next_stream()>>>(S, J, T, Q, qsel, b, g0);
+      if (cfg.family_mask & (1u << 5)) k_shade<5, MJ><<<cfg.shade_fam_blocks[5], 128, 0, next_stream()>>>(S, J, T, Q, qsel, b, g0);
+      if (cfg.family_mask & (1u << 6)) k_shade<6, MJ><<<cfg.shade_fam_blocks[6], 128, 0, next_stream()>>>(S, J, T, Q, qsel, b, g0);
+      k_shade<PT_FAM_MISC, MJ><<<cfg.shade_fam_blocks[PT_FAM_MISC], 128, 0, next_stream()>>>(S, J, T, Q, qsel, b, g0);
+      for (int u = 0; u < used; ++u) {
+        cudaEventRecord(ss->join[u], ss->aux[u]);
+        cudaStreamWaitEvent(st, ss->join[u], 0);
+      }
       P.end(st);
       P.count(STAGE_SHADE, 1 + __builtin_popcount(cfg.family_mask & 0x7fu));
     } else {
