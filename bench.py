@@ -60,7 +60,7 @@ FALLBACK_HBM_GBS = 6800.0
 # one-pass ncu capture of the same bench command
 NCU_TRAVERSAL_BYTES_PER_STEP = {("rough_glass", 0): 8.850e9}
 # Algorithmic queue bytes per unit, by stage: the records each stage must
-# read or write in this layout, with the survey model's 192 B per path vertex,
+# read or write in this layout -- 192 B per path vertex,
 # 88 B per shadow ray (44 written by shade, 44 read by the traversal) and FP32
 # film; each byte charged to the stage that moves it:
 #   camera    64 B per path: ray origin + direction (32) and path state
