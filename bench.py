@@ -645,17 +645,19 @@ def run_reference(args, rank, world):
     sc, cam = build_scene(args.workload)
     osc = O.OracleScene(sc)
     threads = os.cpu_count() or 1
-    vals = []
+    vals, secs = [], []
     sample = ""
     for i in range(args.warmup + args.steps):
-        v, sample, _ = cpu_paths_per_sec(osc, cam, wl, wl["est"], threads,
-                                         target_s=max(4.0, 90.0 / (args.steps + args.warmup)))
+        v, sample, dt = cpu_paths_per_sec(osc, cam, wl, wl["est"], threads,
+                                          target_s=max(4.0, 90.0 / (args.steps + args.warmup)))
         if i >= args.warmup:
             vals.append(v)
+            secs.append(dt)
     value = statistics.median(vals)
     line = {
         "impl": "reference", "metric": "paths/s", "value": value, "unit": "paths/s", "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * statistics.median(secs),
+        "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene generator)",
         "config": {"workload": wl["desc"], "estimator": wl["est_name"]},
         "cpu_baseline": {"value": value, "unit": "paths/s", "cores": threads, "kind": "port",
