@@ -287,7 +287,7 @@ static float render_groups_persistent(Context *c, std::vector<Group> &groups, bo
     cuda_check(cudaMemsetAsync(slot.Q[0].stats, 0, 64, c->stream), "memset stats");
     cuda_check(cudaMemsetAsync(slot.Q[1].stats, 0, 64, c->stream), "memset stats");
     if (!targets) cuda_check(cudaMemsetAsync(slot.films, 0, sizeof(float) * G.film_floats, c->stream), "memset films");
-    const int grid = persistent_grid(S->view.curves != nullptr, c->num_sms);
+    const int grid = persistent_grid(S->view, c->num_sms);
     cuda_check(launch_group_persistent(S->view, G.M.T, slot.Q[0], slot.d_films, G.total, G.wave, G.M.LN,
                                        G.M.bounces, slot.d_barrier, grid, c->stream),
                "persistent group launch");

@@ -1532,6 +1532,9 @@ std::unique_ptr<Scene> build_scene(const pt_scene_desc *d_in, cudaStream_t st, b
   V.n_nodes = (int)out.nodes.size();
   V.n_prims = n_prims;
   V.trav_cap = trav_cap > 0 ? trav_cap : PT_TRAVERSAL_CAP;
+  // a node visit pushes at most 3 entries per level, plus a moving object's
+  // frame marker; 2 entries to spare
+  V.stack_entries = std::min(PT_STACK, 3 * out.max_depth + 4);
   for (int c = 0; c < 3; ++c) V.bg[c] = d->bg_color[c];
   if (d->env) {
     V.env.texels = up(tex);

@@ -73,7 +73,7 @@ __global__ void __launch_bounds__(128) k_trace_test(SceneView S, const float *ra
                                                     int n, float tmin, float tmax, float *t_out,
                                                     int *prim_out, float *uv_out, uint8_t *occ,
                                                     int *err) {
-  __shared__ int32_t stack[PT_STACK * 128];
+  extern __shared__ int32_t stack[];  // S.stack_entries x 128
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     V3 o = v3(rays[6 * i], rays[6 * i + 1], rays[6 * i + 2]);
     V3 d = v3(rays[6 * i + 3], rays[6 * i + 4], rays[6 * i + 5]);
@@ -98,7 +98,7 @@ __global__ void __launch_bounds__(128) k_trace_test(SceneView S, const float *ra
 __global__ void __launch_bounds__(128) k_intersect(SceneView S, const float *rays, int n, float tmin, float tmax,
                                                    float *t_out, int *prim_out, float *pos, float *nrm,
                                                    uint8_t *front, int *err) {
-  __shared__ int32_t stack[PT_STACK * 128];
+  extern __shared__ int32_t stack[];  // S.stack_entries x 128
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const V3 o = v3(rays[6 * i], rays[6 * i + 1], rays[6 * i + 2]);
     const V3 d = v3(rays[6 * i + 3], rays[6 * i + 4], rays[6 * i + 5]);
@@ -122,7 +122,8 @@ __global__ void __launch_bounds__(128) k_intersect(SceneView S, const float *ray
 
 void launch_intersect(const SceneView &S, const float *rays, int n, float tmin, float tmax, float *t, int *prim,
                       float *pos, float *nrm, uint8_t *front, int *err, cudaStream_t st) {
-  k_intersect<<<grid_for(n, 128, 152 * 8), 128, 0, st>>>(S, rays, n, tmin, tmax, t, prim, pos, nrm, front, err);
+  k_intersect<<<grid_for(n, 128, 152 * 8), 128, stack_bytes(S, 128), st>>>(S, rays, n, tmin, tmax, t, prim, pos, nrm,
+                                                                         front, err);
 }
 
 // The Light methods of one light of a resident scene at n (u, v, x) items:
@@ -265,7 +266,7 @@ __global__ void k_sort_scatter(Queues Q, int qsel) {
 // (trace_shadow_body, shadow_resolve_body, film_body).
 template <bool CURVES>
 __global__ void __launch_bounds__(128) k_trace_shadow(SceneView S, Queues Q, int LN) {
-  __shared__ int32_t stack[PT_STACK * 128];
+  extern __shared__ int32_t stack[];  // S.stack_entries x 128
   trace_shadow_body<CURVES>(S, Q, LN, stack);
 }
 __global__ void k_shadow_resolve(Queues Q, int LN) { shadow_resolve_body(Q, LN); }
@@ -365,9 +366,9 @@ void launch_trace_test(const SceneView &S, bool any, const float *rays, const fl
                        cudaStream_t st) {
   int g = grid_for(n, 128, 152 * 8);
   if (any)
-    k_trace_test<true><<<g, 128, 0, st>>>(S, rays, tmaxs, n, tmin, tmax, t, prim, uv, occ, err);
+    k_trace_test<true><<<g, 128, stack_bytes(S, 128), st>>>(S, rays, tmaxs, n, tmin, tmax, t, prim, uv, occ, err);
   else
-    k_trace_test<false><<<g, 128, 0, st>>>(S, rays, tmaxs, n, tmin, tmax, t, prim, uv, occ, err);
+    k_trace_test<false><<<g, 128, stack_bytes(S, 128), st>>>(S, rays, tmaxs, n, tmin, tmax, t, prim, uv, occ, err);
 }
 
 void launch_bsdf_eval(const MatRec *m, int n, const float *wo, const float *wi, const float *nrm,
@@ -407,9 +408,9 @@ void launch_sort(const SceneView &S, const Queues &Q, int qsel, const LaunchCfg 
 
 void launch_shadow(const SceneView &S, const Queues &Q, int LN, const LaunchCfg &cfg, cudaStream_t st) {
   if (S.curves)
-    k_trace_shadow<true><<<cfg.trace_blocks, 128, 0, st>>>(S, Q, LN);
+    k_trace_shadow<true><<<cfg.trace_blocks, 128, stack_bytes(S, 128), st>>>(S, Q, LN);
   else
-    k_trace_shadow<false><<<cfg.trace_blocks, 128, 0, st>>>(S, Q, LN);
+    k_trace_shadow<false><<<cfg.trace_blocks, 128, stack_bytes(S, 128), st>>>(S, Q, LN);
   k_shadow_resolve<<<cfg.max_blocks_simple, 256, 0, st>>>(Q, LN);
 }
 void launch_shadow_resolve(const Queues &Q, int LN, const LaunchCfg &cfg, cudaStream_t st) {
@@ -447,11 +448,13 @@ void kernel_attributes(KernelInfo *info) {
   cudaFuncGetAttributes(&a, k_shade<-1, false>);
   info->shade_regs = a.numRegs;
   int nb = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_trace_closest<false, false>, 128, 0);
+  // occupancy at the largest stack (the grids must fit every scene)
+  const size_t smax = (size_t)PT_STACK * 128 * sizeof(int32_t);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_trace_closest<false, false>, 128, smax);
   info->trace_blocks_per_sm = nb;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_shade<-1, false>, 128, 0);
   info->shade_blocks_per_sm = nb;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_trace_shadow<false>, 128, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_trace_shadow<false>, 128, smax);
   info->shadow_blocks_per_sm = nb;
   int *fb = info->shade_fam_blocks_per_sm;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fb[0], k_shade<0, false>, 128, 0);

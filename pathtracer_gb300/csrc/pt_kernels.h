@@ -187,7 +187,7 @@ void upload_halton_tables_multi(const HaltonTables &T, cudaStream_t st);
 // d_barrier: 16 zeroed bytes (the grid barrier; its third int is set when a
 // barrier wait ran out).  persistent_grid: the resident-block grid.
 void upload_halton_tables_persist(const HaltonTables &T, cudaStream_t st);
-int persistent_grid(bool curves, int num_sms);
+int persistent_grid(const SceneView &S, int num_sms);
 cudaError_t launch_group_persistent(const SceneView &S, const JobTable &T, const Queues &Q, float *const *d_films,
                                     long long total, int wave, int LN, int bounces, void *d_barrier, int grid,
                                     cudaStream_t st);

@@ -112,7 +112,7 @@ __global__ void __launch_bounds__(PT_PERSIST_THREADS, PT_PERSIST_MIN_BLOCKS)
     k_group_persistent(const __grid_constant__ SceneView S, const __grid_constant__ JobTable T,
                        const __grid_constant__ Queues Q, float *const *films, long long total, int wave, int LN,
                        int bounces, GridBarrier *bar) {
-  __shared__ int32_t stack[PT_STACK * PT_PERSIST_THREADS];
+  extern __shared__ int32_t stack[];  // S.stack_entries x PT_PERSIST_THREADS
   __shared__ DeviceJob none;  // unused by merged waves (each path's job comes from T)
   if (threadIdx.x == 0) memset(&none, 0, sizeof none);
   __syncthreads();
@@ -149,12 +149,13 @@ __global__ void __launch_bounds__(PT_PERSIST_THREADS, PT_PERSIST_MIN_BLOCKS)
   }
 }
 
-int persistent_grid(bool curves, int num_sms) {
+int persistent_grid(const SceneView &S, int num_sms) {
   int per = 0;
-  if (curves)
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_group_persistent<true>, PT_PERSIST_THREADS, 0);
+  const size_t smem = stack_bytes(S, PT_PERSIST_THREADS);
+  if (S.curves)
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_group_persistent<true>, PT_PERSIST_THREADS, smem);
   else
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_group_persistent<false>, PT_PERSIST_THREADS, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_group_persistent<false>, PT_PERSIST_THREADS, smem);
   return std::max(1, per) * num_sms;
 }
 
@@ -168,7 +169,8 @@ cudaError_t launch_group_persistent(const SceneView &S, const JobTable &T, const
   GridBarrier *b = static_cast<GridBarrier *>(d_barrier);
   void *args[] = {&s, &t, &q, &f, &total, &wave, &LN, &bounces, &b};
   const void *fn = S.curves ? (const void *)k_group_persistent<true> : (const void *)k_group_persistent<false>;
-  return cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(PT_PERSIST_THREADS), args, 0, st);
+  return cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(PT_PERSIST_THREADS), args,
+                                     stack_bytes(S, PT_PERSIST_THREADS), st);
 }
 
 }  // namespace pt

@@ -15,6 +15,10 @@
 
 // Entries of the per-thread traversal stack (shared memory).  A BVH4 of
 // depth D needs at most 3 * D + 1 entries; scene upload rejects deeper trees.
+// Largest traversal stack, in entries per thread.  A scene's kernels get
+// SceneView::stack_entries (3 * its BVH4 depth + 4) entries each, in dynamic
+// shared memory: a shallow tree leaves more of the SM's on-chip memory to the
+// L1 cache that serves the node loads.
 #ifndef PT_STACK
 #define PT_STACK 48
 #endif
@@ -147,11 +151,18 @@ struct SceneView {
   const int32_t *node_motion;  // per BVH4 node: motion index + 1 of the moving object it roots
   int32_t has_motion;
   int32_t trav_cap;  // steps one ray's traversal may take before the device error flag is set
+  int32_t stack_entries;  // traversal stack entries per thread: 3 * BVH4 depth + 4 (<= PT_STACK)
   const TexRec *textures;  // surface textures (materials' flags >> PT_MAT_TEXTURE_SHIFT)
   const float4 *prim_uv;   // per primitive texture-coordinate records (null: no textures)
   int32_t n_textures;
   const float4 *curves;    // per curve: (cp0, width0), (cp1, width1), (cp2, 0), (cp3, 0)
 };
+
+// Dynamic shared memory of a traversal kernel's stack: the scene's entries
+// per thread, for `threads` threads (one column per thread).
+inline size_t stack_bytes(const SceneView &S, int threads) {
+  return (size_t)S.stack_entries * (size_t)threads * sizeof(int32_t);
+}
 
 // Child references of a BVH4 node entering a moving object's subtree carry
 // PT_INST_BIT; the traversal then pushes PT_FRAME_END (never a leaf

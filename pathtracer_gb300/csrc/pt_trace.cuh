@@ -296,7 +296,7 @@ __device__ __forceinline__ bool trav_node(const SceneView &S, TravRay &R, int32_
     // entering a moving object's subtree: the ray in the object's frame at
     // its time, until PT_FRAME_END comes off the stack
     R.ref &= ~PT_INST_BIT;
-    if (R.sp + 1 > PT_STACK) {
+    if (R.sp + 1 > S.stack_entries) {
       *err = 1;
       return false;
     }
@@ -363,7 +363,7 @@ __device__ __forceinline__ bool trav_node(const SceneView &S, TravRay &R, int32_
     R.ref = trav_pop(R, stack, stride);
     return true;
   }
-  if (R.sp + nh - 1 > PT_STACK) {
+  if (R.sp + nh - 1 > S.stack_entries) {
     *err = 1;
     return false;
   }

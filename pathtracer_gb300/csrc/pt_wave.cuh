@@ -393,7 +393,7 @@ __device__ __forceinline__ void trace_closest_body(const SceneView &S, const Dev
 template <bool MJ, bool CURVES>
 __global__ void __launch_bounds__(128) k_trace_closest(SceneView S, DeviceJob J, JobTable T, Queues Q, int qsel,
                                                        int bounce, long long g0) {
-  __shared__ int32_t stack[PT_STACK * 128];
+  extern __shared__ int32_t stack[];  // S.stack_entries x 128
   trace_closest_body<MJ, CURVES>(S, J, T, Q, qsel, bounce, g0, stack);
 }
 
@@ -490,7 +490,7 @@ __device__ __forceinline__ void trace_pair_body(const SceneView &S, const Device
 template <bool MJ, bool CURVES>
 __global__ void __launch_bounds__(128, 7) k_trace_pair(SceneView S, DeviceJob J, JobTable T, Queues Q, int qsel,
                                                     int bounce, long long g0, int LN) {
-  __shared__ int32_t stack[PT_STACK * 128];
+  extern __shared__ int32_t stack[];  // S.stack_entries x 128
   trace_pair_body<MJ, CURVES>(S, J, T, Q, qsel, bounce, g0, LN, stack);
 }
 
@@ -1091,13 +1091,13 @@ void launch_wave_stages(const SceneView &S, const DeviceJob &J, const JobTable &
     if (pair) {
       // this bounce's closest rays with the previous bounce's shadow rays
       if (S.curves)
-        k_trace_pair<MJ, true><<<cfg.trace_blocks, 128, 0, st>>>(S, J, T, Q, qsel, b, g0, LN);
+        k_trace_pair<MJ, true><<<cfg.trace_blocks, 128, stack_bytes(S, 128), st>>>(S, J, T, Q, qsel, b, g0, LN);
       else
-        k_trace_pair<MJ, false><<<cfg.trace_blocks, 128, 0, st>>>(S, J, T, Q, qsel, b, g0, LN);
+        k_trace_pair<MJ, false><<<cfg.trace_blocks, 128, stack_bytes(S, 128), st>>>(S, J, T, Q, qsel, b, g0, LN);
     } else if (S.curves) {
-      k_trace_closest<MJ, true><<<cfg.trace_blocks, 128, 0, st>>>(S, J, T, Q, qsel, b, g0);
+      k_trace_closest<MJ, true><<<cfg.trace_blocks, 128, stack_bytes(S, 128), st>>>(S, J, T, Q, qsel, b, g0);
     } else {
-      k_trace_closest<MJ, false><<<cfg.trace_blocks, 128, 0, st>>>(S, J, T, Q, qsel, b, g0);
+      k_trace_closest<MJ, false><<<cfg.trace_blocks, 128, stack_bytes(S, 128), st>>>(S, J, T, Q, qsel, b, g0);
     }
     P.end(st);
     P.count(STAGE_TRACE, 1);
