@@ -318,7 +318,10 @@ int pt_version(void);
 
 /* Flattens and uploads a scene (replaces the scene set-up part of
  * SceneInfo::render, include/render/renderManager.hpp:80-95: BVH build,
- * light discovery).  Host arrays are copied; the caller keeps ownership. */
+ * light discovery).  Host arrays are copied; the caller keeps ownership.
+ * The traversal stack of the scene's kernels is sized by its BVH4 depth (3
+ * entries per level + 4, in shared memory); a tree deeper than 15 levels is
+ * refused with PT_ERR_TOO_LARGE. */
 int pt_scene_upload(void *ctx, const pt_scene_desc *desc, int32_t *scene_id);
 int pt_scene_release(void *ctx, int32_t scene_id);
 
